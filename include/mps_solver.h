@@ -1,0 +1,112 @@
+/*
+ * mps_solver.h - the GB300-native semi-implicit MPS step (one GPU, library-owned memory).
+ *
+ * No single reference function corresponds to this API: it runs the reference's
+ * per-step schedule (CMultiGPUHandler::Calculate, MultiGPUHandler.cpp:1389-1559:
+ * topology, walls, drag, predictor, topology, walls, pressure, pressure-gradient
+ * correction, wall motion) with the pressure obtained from a pressure Poisson
+ * equation solved by Jacobi-preconditioned CG.  The reference parses the switches for
+ * that solver (bCGSolver / bNJPCGSolver, IO.cpp:273-283, 364-373) and declares, but
+ * never defines, CalculatePressureCG / CalculatePressureNJPCG
+ * (solver/MPS_SOLVER_WITH_ROTATION/PMMultiGPU/Source/CGPUCellSet.h:218-240).
+ *
+ * Inputs use the reference's parameter and wall types (mps_types.h).  Particle state
+ * is kept in FP64 on the device, permanently in cell-sorted order; particle identity
+ * travels in an id array.  Precision modes:
+ *   MPS_PREC_FP64     every operator, the PPE and CG in FP64 (the "plain FP64
+ *                     Jacobi-CG" path);
+ *   MPS_PREC_FP32_IR  particle operators and CG in FP32, inside an FP64 iterative
+ *                     refinement of the PPE (FP64 dot products, residual norms,
+ *                     refinement residual, n0 and position/velocity accumulation).
+ * A learned initial guess and diagonal scaling (mps_solver_set_learned) drive a
+ * flexible CG; plain Jacobi-CG is the fallback whenever it does not converge.
+ * Every call returns a CCTStatusType.
+ */
+#ifndef MPS_SOLVER_H
+#define MPS_SOLVER_H
+
+#include <stddef.h>
+
+#include "mps_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct MpsSolver MpsSolver;
+
+enum { MPS_PREC_FP64 = 0, MPS_PREC_FP32_IR = 1 };
+enum { MPS_PRESSURE_PPE = 0, MPS_PRESSURE_EXPLICIT = 1 };
+
+typedef struct MpsSolverOptions {
+    int precision;          /* MPS_PREC_* */
+    int pressure_mode;      /* MPS_PRESSURE_PPE, or the reference's equation of state */
+    int learned;            /* 1: use the learned initial guess and scaling if set */
+    double n0_pnd;          /* reference PND at the gradient radius (<= 0: CParameter n0) */
+    double n0_lap;          /* reference PND at the Laplacian radius (<= 0: CParameter n0) */
+    double lambda;          /* Laplacian lambda (<= 0: CParameter LambdaValue) */
+    double compressibility; /* artificial compressibility alpha [1/Pa] (Ikeda et al.) */
+    double cg_rtol;         /* PPE relative residual target (||b - A p|| / ||b||) */
+    int cg_max_iter;        /* CG iteration cap (per solve) */
+    double ir_inner_rtol;   /* FP32 inner CG tolerance relative to the refinement residual */
+    int ir_max_outer;       /* refinement pass cap */
+    int max_neighbours;     /* capacity of a Laplacian neighbour row */
+    int check_every;        /* CG convergence is read back every this many iterations */
+} MpsSolverOptions;
+
+typedef struct MpsStepStats {
+    int particles;
+    int interior;           /* particles in the PPE (not free surface) */
+    int cg_iterations;      /* total CG iterations of the step (inner ones in FP32_IR) */
+    int ir_passes;          /* refinement passes (FP32_IR) */
+    int fallback;           /* 1 if the learned solve fell back to plain Jacobi-CG */
+    int max_row;            /* longest neighbour row */
+    double cg_relres;       /* final FP64 relative residual */
+    double b_norm;
+    unsigned error_flags;   /* MPS_ERR_* bits seen during the step */
+} MpsStepStats;
+
+void mps_solver_default_options(MpsSolverOptions* opt);
+CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
+                                const MpsSolverOptions* opt, MpsSolver** out);
+void mps_solver_destroy(MpsSolver* s);
+/* host arrays: pos/vel n*3, press/visc n (press may be NULL), type n (may be NULL) */
+CCTStatusType mps_solver_set_particles(MpsSolver* s, int n, const double* pos, const double* vel,
+                                       const double* press, const double* visc, const int* type);
+/* vertices t*9 (three vertices per triangle), model t, params per model */
+CCTStatusType mps_solver_set_triangles(MpsSolver* s, int t, const double* vertices, const int* model, int models,
+                                       const CTriangleParameters* params);
+CCTStatusType mps_solver_set_drag(MpsSolver* s, int count, const DragParameter* params);
+CCTStatusType mps_solver_step(MpsSolver* s, int step, MpsStepStats* stats);
+/* current particle state in the solver's (cell-sorted) order, with particle ids;
+ * any pointer may be NULL */
+CCTStatusType mps_solver_get_particles(MpsSolver* s, int* n, double* pos, double* vel, double* press, double* pnd,
+                                       int* id);
+CCTStatusType mps_solver_get_triangles(MpsSolver* s, double* vertices);
+/* PPE data of the last step in sorted order: PND, diagonal, right-hand side,
+ * solution, particle id, Laplacian neighbour count, sum of neighbour ids */
+CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, double* rhs, double* sol, int* id,
+                                   int* nbr_count, double* nbr_idsum);
+/* Device pointer of the pressure array (FP64, sorted order) and particle count. */
+CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);
+/* Pressure read back to a host buffer, in the solver's order (e2e output). */
+CCTStatusType mps_solver_copy_pressure(MpsSolver* s, double* host_press);
+/* Stream the solver launches on (cudaStream_t), for event timing by the caller. */
+CCTStatusType mps_solver_stream(MpsSolver* s, void** stream);
+
+/* ---- learned initial guess / preconditioner (BF16 tensor-core MLP) ---- */
+/* MLP 12 -> 128 -> 128 -> 128 -> 2 (SiLU); FP32 master parameters, layout:
+ * W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[128][2] b4[2]
+ * (row-major, input-major) = 35,330 floats. */
+#define MPS_MLP_PARAMS 35330
+#define MPS_MLP_FEATURES 12
+CCTStatusType mps_solver_set_learned(MpsSolver* s, const float* params, int count);
+/* Features (n*12, FP32) and training targets (n*2: normalised pressure increment,
+ * log of the ideal diagonal scale) of the last PPE solve, sorted order. */
+CCTStatusType mps_solver_learned_samples(MpsSolver* s, float* features, float* targets, int* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

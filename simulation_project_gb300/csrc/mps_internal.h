@@ -1,0 +1,31 @@
+// mps_internal.h - declarations shared between the translation units of the library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "../../include/mps_types.h"
+
+namespace mps {
+
+// radix sort (sort.cu)
+size_t radix_scratch_bytes(int n);
+int radix_passes(unsigned range);
+cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, void* scratch, cudaStream_t st);
+cudaError_t key_minmax(int n, const int* keys, int* mm_dev, cudaStream_t st);
+cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st);
+
+// library-owned scratch for the reference-named entry points, which take no scratch
+// argument (runtime.cu).  Grows on demand; one buffer per slot.
+void* scratch_get(int slot, size_t bytes);
+void scratch_release_all();
+
+inline CCTStatusType cuda_status(cudaError_t e) { return e == cudaSuccess ? CCT_NOERR : CCT_CUDAERR; }
+
+}  // namespace mps
+
+#define MPS_CUDA_TRY(expr)                                  \
+    do {                                                    \
+        cudaError_t _e = (expr);                            \
+        if (_e != cudaSuccess) return CCT_CUDAERR;          \
+    } while (0)

@@ -1,0 +1,91 @@
+// native.cuh - data layout and kernel declarations of the GB300-native solver.
+//
+// Layout in HBM (all arrays indexed by the current cell-sorted particle order):
+//   pos, vel        double4  (x, y, z, unused)   FP64 master state, 32 B each
+//   opos, ovel      float4                        FP32 operator copies (FP32 mode)
+//   press           double                        pressure (PPE solution)
+//   visc            float, type int, id int       carried per particle
+//   key, idx        int                           hash keys / sort permutation
+//   cstart, cend    int[cells]                    cell ranges (-1 = empty)
+//   nbr, nbrw       int / T [n * K]               Laplacian neighbour rows, row-major,
+//                                                 row i at i*K, nbr_cnt[i] entries
+//   gnbr, gnbrr     int / T [n * KG]              gradient-radius rows (index, r)
+//   tri             double[9*T], tnrm double[3*T] walls; tcs[cells+1]/tids CSR bins
+// Kernels take the whole record as one __grid_constant__ parameter.
+#pragma once
+
+#include "mps_common.cuh"
+#include "mps_internal.h"
+#include "../../include/mps_solver.h"
+
+namespace mps {
+
+struct Consts {
+    double l0, re_lap, re_grad, mind_lap, mind_grad;
+    double coef_lap;      // 2d / (lambda n0_lap)
+    double n0_pnd, n0_lap, beta, rho, dt, kappa;
+    double c1;            // 2d / n0_pnd
+    double c2;            // rho / dt^2
+    double vmax;          // l0 * Courant / dt
+    double wall_fric, offset_l0, tol, sonic2;
+    double g[3];
+    int dim;
+    int explicit_pressure;
+};
+
+struct Dev {
+    int n, cells, K, KG, tri_n, drag_n;
+    CGridBox box;
+    Consts c;
+    double4 *pos, *vel;
+    double* press;
+    float* visc;
+    int *type, *id;
+    double4 *pos2, *vel2;
+    double* press2;
+    float* visc2;
+    int *type2, *id2;
+    float4 *opos, *ovel;
+    int *key, *idx;
+    int *cstart, *cend;
+    int* cell_list;
+    int* cell_count;
+    // walls
+    double* tri;
+    double* tnrm;
+    int* tmodel;
+    CTriangleParameters* tparams;
+    DragParameter* drag;
+    int *tcs, *tids;
+    double* wdist;
+    double* wdir;
+    int* wid;
+    double* dragv;
+    // neighbour rows
+    int* nbr;
+    void* nbrw;
+    int* nbr_cnt;
+    int* gnbr;
+    void* gnbrr;
+    int* gcnt;
+    // PPE
+    double *pnd, *diag, *rhs, *sumw;
+    unsigned char* inner;
+    double *r, *z, *p, *q;     // FP64 CG vectors
+    float *r32, *z32, *p32, *q32, *d32, *m32;  // FP32 inner CG vectors, m32 = preconditioner
+    double* minv;              // FP64 preconditioner (1/diag or learned)
+    double* feat_aux;          // per-particle auxiliaries for features (div, mean P, ...)
+    double* red;               // block partial sums
+    double* scal;              // device scalars
+    unsigned* red_count;       // last-block counters
+    unsigned* err;
+    int* nbr_idsum_cnt;        // debug
+};
+
+// device scalar slots
+enum {
+    S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_BNORM, S_TOL, S_CONV, S_ITER, S_RZNEW, S_RNORM, S_R0NORM,
+    S_IRTOL, S_TMP0, S_TMP1, S_COUNT
+};
+
+}  // namespace mps

@@ -1,0 +1,822 @@
+// native_kernels.cuh - kernels of the GB300-native semi-implicit step.
+//
+// Every particle kernel works in the cell-sorted order.  Neighbour passes run one CTA
+// per non-empty cell: the CTA stages the nine z-runs of the 27 surrounding cells (each
+// run is contiguous in sorted order) into shared memory as float4, then each warp takes
+// one target particle at a time and its 32 lanes test 32 staged candidates per step;
+// accepted neighbours are compacted with __ballot_sync/__popc so a warp writes each
+// neighbour row as contiguous, coalesced segments.
+#pragma once
+
+#include <type_traits>
+
+#include "native.cuh"
+
+namespace mps {
+
+constexpr int kNbThreads = 256;
+constexpr int kStageCap = 2048;
+constexpr int kRedBlocks = 1216;   // 152 SMs x 8 resident CTAs of 256 threads
+constexpr int kVecThreads = 256;
+
+enum { NB_PREDICT = 0, NB_LIST = 1 };
+
+template <class T> struct V3 { T x, y, z; };
+template <class T> __device__ __forceinline__ V3<T> v3(T x, T y, T z) { V3<T> r; r.x = x; r.y = y; r.z = z; return r; }
+
+// ---------------------------------------------------------------------------
+// deterministic block + grid reductions (last CTA finishes the sum)
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* red, unsigned* counter, double (&out)[NV]) {
+    __shared__ double sm[NV][32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sm[k][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int i = 0; i < nw; ++i) s += sm[k][i];
+            red[(size_t)k * gridDim.x + blockIdx.x] = s;
+        }
+        __threadfence();
+        const unsigned t = atomicAdd(counter, 1u);
+        last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += ((volatile double*)red)[(size_t)k * gridDim.x + i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) sm[k][w] = s;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        double s = 0.0;
+        for (int i = 0; i < nw; ++i) s += sm[k][i];
+        out[k] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// grid build
+// ---------------------------------------------------------------------------
+__global__ void k_zone_flags(const __grid_constant__ Dev d, unsigned* keep) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double4 p = d.pos[i];
+    keep[i] = in_zone<double>(d.box, p.x, p.y, p.z, d.c.tol) ? 1u : 0u;
+}
+
+// stable compaction: survivors keep their relative order
+__global__ void k_compact(const __grid_constant__ Dev d, const unsigned* keep, const unsigned* rank) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n || !keep[i]) return;
+    const int o = (int)rank[i];
+    d.pos2[o] = d.pos[i];
+    d.vel2[o] = d.vel[i];
+    d.press2[o] = d.press[i];
+    d.visc2[o] = d.visc[i];
+    d.type2[o] = d.type[i];
+    d.id2[o] = d.id[i];
+}
+
+__global__ void k_hash(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double4 p = d.pos[i];
+    const double cs = d.box.m_CellSize;
+    const int a = f2i((p.x - (double)d.box.m_BufferedZone.m_MinBound.x) / cs);
+    const int b = f2i((p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
+    const int c = f2i((p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs);
+    int k = cell_key(d.box.m_GridSize, a, b, c);
+    if (k < 0 || k >= d.cells) {
+        atomicOr(d.err, MPS_ERR_KEY_RANGE);
+        k = k < 0 ? 0 : d.cells - 1;
+    }
+    d.key[i] = k;
+    d.idx[i] = i;
+}
+
+// gather into sorted order + cell ranges + list of non-empty cells
+__global__ void k_gather(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int s = d.idx[i];
+    const double4 p = d.pos[s], v = d.vel[s];
+    d.pos2[i] = p;
+    d.vel2[i] = v;
+    d.press2[i] = d.press[s];
+    d.visc2[i] = d.visc[s];
+    d.type2[i] = d.type[s];
+    d.id2[i] = d.id[s];
+    d.opos[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+    d.ovel[i] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+    const int h = d.key[i];
+    if (i == 0 || h != d.key[i - 1]) {
+        d.cstart[h] = i;
+        if (i > 0) d.cend[d.key[i - 1]] = i;
+        const int slot = atomicAdd(d.cell_count, 1);
+        d.cell_list[slot] = h;
+    }
+    if (i == d.n - 1) d.cend[h] = i + 1;
+}
+
+// ---------------------------------------------------------------------------
+// walls: bounding-box binning, exact distances, drag, motion
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void tri_cell_box(const Dev& d, int t, int& i0, int& j0, int& k0, int& i1, int& j1, int& k1) {
+    const double* v = d.tri + 9 * (size_t)t;
+    double lo[3] = {v[0], v[1], v[2]}, hi[3] = {v[0], v[1], v[2]};
+    for (int q = 1; q < 3; ++q)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fmin(lo[a], v[3 * q + a]);
+            hi[a] = fmax(hi[a], v[3 * q + a]);
+        }
+    const double cs = d.box.m_CellSize;
+    const CBox& B = d.box.m_BufferedZone;
+    i0 = max(f2i((lo[0] - (double)B.m_MinBound.x) / cs), 0);
+    j0 = max(f2i((lo[1] - (double)B.m_MinBound.y) / cs), 0);
+    k0 = max(f2i((lo[2] - (double)B.m_MinBound.z) / cs), 0);
+    i1 = min(f2i((hi[0] - (double)B.m_MinBound.x) / cs), d.box.m_GridSize.x - 1);
+    j1 = min(f2i((hi[1] - (double)B.m_MinBound.y) / cs), d.box.m_GridSize.y - 1);
+    k1 = min(f2i((hi[2] - (double)B.m_MinBound.z) / cs), d.box.m_GridSize.z - 1);
+}
+__global__ void k_bin_count(const __grid_constant__ Dev d, unsigned* cnt) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.tri_n) return;
+    int i0, j0, k0, i1, j1, k1;
+    tri_cell_box(d, t, i0, j0, k0, i1, j1, k1);
+    const long long c = (long long)max(i1 - i0 + 1, 0) * max(j1 - j0 + 1, 0) * max(k1 - k0 + 1, 0);
+    cnt[t] = (unsigned)min(c, (long long)1 << 20);
+}
+__global__ void k_bin_fill(const __grid_constant__ Dev d, const unsigned* off, int* vcell, int* vtri) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.tri_n) return;
+    int i0, j0, k0, i1, j1, k1;
+    tri_cell_box(d, t, i0, j0, k0, i1, j1, k1);
+    unsigned o = off[t];
+    const unsigned e = off[t + 1];
+    for (int i = i0; i <= i1; ++i)
+        for (int j = j0; j <= j1; ++j)
+            for (int k = k0; k <= k1; ++k) {
+                if (o >= e) return;
+                vcell[o] = cell_key(d.box.m_GridSize, i, j, k);
+                vtri[o] = t;
+                ++o;
+            }
+}
+__global__ void k_bin_bounds(int nv, const int* vcell, int* ts, int* te) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    const int c = vcell[i];
+    if (i == 0 || c != vcell[i - 1]) {
+        ts[c] = i;
+        if (i > 0) te[vcell[i - 1]] = i;
+    }
+    if (i == nv - 1) te[c] = i + 1;
+}
+
+// Closest point on triangle (a, b, c) to p by Voronoi-region classification
+// (Ericson, Real-Time Collision Detection, 5.1.5).
+template <class T>
+__device__ V3<T> closest_on_tri(const V3<T>& p, const V3<T>& a, const V3<T>& b, const V3<T>& c) {
+    const V3<T> ab = v3(b.x - a.x, b.y - a.y, b.z - a.z), ac = v3(c.x - a.x, c.y - a.y, c.z - a.z);
+    const V3<T> ap = v3(p.x - a.x, p.y - a.y, p.z - a.z);
+    const T d1 = ab.x * ap.x + ab.y * ap.y + ab.z * ap.z, d2 = ac.x * ap.x + ac.y * ap.y + ac.z * ap.z;
+    if (d1 <= T(0) && d2 <= T(0)) return a;
+    const V3<T> bp = v3(p.x - b.x, p.y - b.y, p.z - b.z);
+    const T d3 = ab.x * bp.x + ab.y * bp.y + ab.z * bp.z, d4 = ac.x * bp.x + ac.y * bp.y + ac.z * bp.z;
+    if (d3 >= T(0) && d4 <= d3) return b;
+    const T vc = d1 * d4 - d3 * d2;
+    if (vc <= T(0) && d1 >= T(0) && d3 <= T(0)) {
+        const T s = d1 / (d1 - d3);
+        return v3(a.x + s * ab.x, a.y + s * ab.y, a.z + s * ab.z);
+    }
+    const V3<T> cp = v3(p.x - c.x, p.y - c.y, p.z - c.z);
+    const T d5 = ab.x * cp.x + ab.y * cp.y + ab.z * cp.z, d6 = ac.x * cp.x + ac.y * cp.y + ac.z * cp.z;
+    if (d6 >= T(0) && d5 <= d6) return c;
+    const T vb = d5 * d2 - d1 * d6;
+    if (vb <= T(0) && d2 >= T(0) && d6 <= T(0)) {
+        const T s = d2 / (d2 - d6);
+        return v3(a.x + s * ac.x, a.y + s * ac.y, a.z + s * ac.z);
+    }
+    const T va = d3 * d6 - d5 * d4;
+    if (va <= T(0) && (d4 - d3) >= T(0) && (d5 - d6) >= T(0)) {
+        const T s = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        return v3(b.x + s * (c.x - b.x), b.y + s * (c.y - b.y), b.z + s * (c.z - b.z));
+    }
+    const T den = T(1) / (va + vb + vc);
+    const T v = vb * den, w = vc * den;
+    return v3(a.x + ab.x * v + ac.x * w, a.y + ab.y * v + ac.y * w, a.z + ab.z * v + ac.z * w);
+}
+
+template <class T>
+__device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md, V3<T>& mdir, int& mid) {
+    md = T(1e8);
+    mdir = v3(T(0), T(0), T(0));
+    mid = -1;
+    const double cs = d.box.m_CellSize;
+    const int cx = f2i(((double)p.x - (double)d.box.m_BufferedZone.m_MinBound.x) / cs);
+    const int cy = f2i(((double)p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
+    const int cz = f2i(((double)p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs);
+    for (int k = -1; k <= 1; ++k)
+        for (int j = -1; j <= 1; ++j)
+            for (int i = -1; i <= 1; ++i) {
+                const int m = cell_key(d.box.m_GridSize, cx + i, cy + j, cz + k);
+                if (m < 0 || m >= d.cells) continue;
+                const int s = d.tcs[m];
+                if (s < 0) continue;
+                const int e = d.tcs[d.cells + m];
+                for (int l = s; l < e; ++l) {
+                    const int t = d.tids[l];
+                    if (drag_only && !d.tparams[d.tmodel[t]].isDrag) continue;
+                    if (t == mid) continue;
+                    const double* v = d.tri + 9 * (size_t)t;
+                    const V3<T> q = closest_on_tri<T>(p, v3<T>((T)v[0], (T)v[1], (T)v[2]), v3<T>((T)v[3], (T)v[4], (T)v[5]),
+                                                      v3<T>((T)v[6], (T)v[7], (T)v[8]));
+                    const V3<T> dv = v3(p.x - q.x, p.y - q.y, p.z - q.z);
+                    const T dd = sqrt(dv.x * dv.x + dv.y * dv.y + dv.z * dv.z);
+                    if (dd < md) {
+                        md = dd;
+                        mdir = dv;
+                        mid = t;
+                    }
+                }
+            }
+}
+
+template <class T>
+__device__ __forceinline__ V3<T> load_p(const Dev& d, int i) {
+    if constexpr (sizeof(T) == 8) {
+        const double4 p = d.pos[i];
+        return v3<T>(p.x, p.y, p.z);
+    } else {
+        const float4 p = d.opos[i];
+        return v3<T>(p.x, p.y, p.z);
+    }
+}
+template <class T>
+__device__ __forceinline__ V3<T> load_v(const Dev& d, int i) {
+    if constexpr (sizeof(T) == 8) {
+        const double4 p = d.vel[i];
+        return v3<T>(p.x, p.y, p.z);
+    } else {
+        const float4 p = d.ovel[i];
+        return v3<T>(p.x, p.y, p.z);
+    }
+}
+
+template <class T>
+__global__ void k_wall_distance(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    T md;
+    V3<T> dir;
+    int mid;
+    nearest_tri<T>(d, load_p<T>(d, i), false, md, dir, mid);
+    d.wdist[i] = md;
+    d.wdir[3 * (size_t)i] = dir.x;
+    d.wdir[3 * (size_t)i + 1] = dir.y;
+    d.wdir[3 * (size_t)i + 2] = dir.z;
+    d.wid[i] = mid;
+}
+
+// Per-body drag (CalcDragEffect_Kernel, DeviceProcess_Kernel.h:309-389, without the
+// reference's sorted/original index mix-up): nearest drag-model triangle within the
+// influence radius; 'E'+'V'/'B': velocity decrement k |u|^e n / permeability;
+// 'C': constant velocity; 'F': velocity factor.
+template <class T>
+__global__ void k_drag(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    double dv[3] = {0, 0, 0};
+    T md;
+    V3<T> dir;
+    int mid;
+    nearest_tri<T>(d, load_p<T>(d, i), true, md, dir, mid);
+    if (mid >= 0) {
+        const DragParameter dp = d.drag[d.tparams[d.tmodel[mid]].DragTriangleID];
+        if ((double)md <= (double)dp.CoefficientofInflueneRegion * d.c.l0) {
+            double4 v = d.vel[i];
+            if (dp.DragToken == 'E' && (dp.InputVelocityToken1 == 'V' || dp.InputVelocityToken1 == 'B')) {
+                const double sv = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+                const double pr = (double)dp.VelocityIndex * pow(sv, (double)dp.VelocityExponential);
+                if (dp.VelocityDragPermiabilityConstant != 0) {
+                    const double f = pr / (double)dp.VelocityDragPermiabilityConstant;
+                    dv[0] = f * d.tnrm[3 * mid];
+                    dv[1] = f * d.tnrm[3 * mid + 1];
+                    dv[2] = f * d.tnrm[3 * mid + 2];
+                }
+            } else if (dp.DragToken == 'C' && (dp.InputVelocityToken1 == 'V' || dp.InputVelocityToken1 == 'v')) {
+                v.x = dp.ConstantVx; v.y = dp.ConstantVy; v.z = dp.ConstantVz;
+                d.vel[i] = v;
+                d.ovel[i] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+            } else if (dp.DragToken == 'F' && (dp.InputVelocityToken1 == 'V' || dp.InputVelocityToken1 == 'v')) {
+                const double f = dp.VelocityMagnitueFactor;
+                v.x *= f; v.y *= f; v.z *= f;
+                d.vel[i] = v;
+                d.ovel[i] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
+            }
+        }
+    }
+    d.dragv[3 * (size_t)i] = dv[0];
+    d.dragv[3 * (size_t)i + 1] = dv[1];
+    d.dragv[3 * (size_t)i + 2] = dv[2];
+}
+
+// ---------------------------------------------------------------------------
+// neighbour passes (shared-memory staged, warp per target)
+// ---------------------------------------------------------------------------
+// exact r (no contracted multiply-add) so FP64 neighbour sets equal the oracle's
+__device__ __forceinline__ double exact_r(double dx, double dy, double dz) {
+    return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+template <class T, int MODE>
+__global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant__ Dev d) {
+    __shared__ float4 spos[kStageCap];
+    __shared__ float4 svel[kStageCap];
+    __shared__ int rs[9], rl[9], rp[10];
+    const int ci = blockIdx.x;
+    if (ci >= *d.cell_count) return;
+    const int cell = d.cell_list[ci];
+    const int s0 = d.cstart[cell], e0 = d.cend[cell];
+    const Integer3 G = d.box.m_GridSize;
+    const int cx = cell / (G.y * G.z), cy = (cell / G.z) % G.y, cz = cell % G.z;
+    if (threadIdx.x < 9) {
+        const int x = cx + (int)threadIdx.x / 3 - 1, y = cy + (int)threadIdx.x % 3 - 1;
+        int first = -1, last = -1;
+        if (x >= 0 && x < G.x && y >= 0 && y < G.y) {
+            for (int dk = -1; dk <= 1; ++dk) {
+                const int z = cz + dk;
+                if (z < 0 || z >= G.z) continue;
+                const int c = cell_key(G, x, y, z);
+                const int st = d.cstart[c];
+                if (st >= 0) {
+                    if (first < 0) first = st;
+                    last = d.cend[c];
+                }
+            }
+        }
+        rs[threadIdx.x] = first < 0 ? 0 : first;
+        rl[threadIdx.x] = first < 0 ? 0 : last - first;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        rp[0] = 0;
+        for (int r = 0; r < 9; ++r) rp[r + 1] = rp[r] + rl[r];
+    }
+    __syncthreads();
+    const int S = rp[9];
+    const bool staged = S <= kStageCap;
+    if (staged) {
+        for (int c = threadIdx.x; c < S; c += blockDim.x) {
+            int r = 0;
+            while (c >= rp[r + 1]) ++r;
+            const int j = rs[r] + (c - rp[r]);
+            spos[c] = d.opos[j];
+            svel[c] = d.ovel[j];
+        }
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const T re = (T)d.c.re_lap, reg = (T)d.c.re_grad, mind = (T)d.c.mind_lap, mindg = (T)d.c.mind_grad;
+    const float re2f = (float)(d.c.re_lap * d.c.re_lap) * 1.0001f;
+    for (int i = s0 + warp; i < e0; i += nwarp) {
+        const float4 pf = d.opos[i];
+        const V3<T> pi = load_p<T>(d, i);
+        const V3<T> vi = load_v<T>(d, i);
+        T a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;   // mode-specific accumulators
+        int cnt = 0, gcnt = 0;
+        for (int r = 0; r < 9; ++r) {
+            const int len = rl[r];
+            for (int b = 0; b < len; b += 32) {
+                const int o = b + lane;
+                const bool valid = o < len;
+                const int j = rs[r] + o;
+                bool acc = false, gacc = false;
+                T rr = T(0);
+                V3<T> dv = v3(T(0), T(0), T(0));
+                float4 vj4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (valid && j != i) {
+                    const float4 q = staged ? spos[rp[r] + o] : d.opos[j];
+                    if constexpr (sizeof(T) == 8) {
+                        const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
+                        if (dxf * dxf + dyf * dyf + dzf * dzf < re2f) {
+                            const double4 pj = d.pos[j];
+                            const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                            const double rd = exact_r(dx, dy, dz);
+                            if (rd < re) {
+                                acc = true;
+                                rr = rd;
+                                dv = v3<T>(dx, dy, dz);
+                            }
+                        }
+                    } else {
+                        const float dx = q.x - pf.x, dy = q.y - pf.y, dz = q.z - pf.z;
+                        const float rf = sqrtf(dx * dx + dy * dy + dz * dz);
+                        if (rf < (float)re) {
+                            acc = true;
+                            rr = rf;
+                            dv = v3<T>(dx, dy, dz);
+                        }
+                    }
+                    if (acc) vj4 = staged ? svel[rp[r] + o] : d.ovel[j];
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, acc);
+                if (acc) {
+                    const T w = re / (rr > mind ? rr : mind) - T(1);
+                    if constexpr (MODE == NB_PREDICT) {
+                        V3<T> vj;
+                        if constexpr (sizeof(T) == 8) {
+                            const double4 v = d.vel[j];
+                            vj = v3<T>(v.x, v.y, v.z);
+                        } else {
+                            vj = v3<T>(vj4.x, vj4.y, vj4.z);
+                        }
+                        a0 += (vj.x - vi.x) * w;
+                        a1 += (vj.y - vi.y) * w;
+                        a2 += (vj.z - vi.z) * w;
+                    } else {
+                        const int slot = cnt + __popc(bal & lt);
+                        if (slot < d.K) {
+                            d.nbr[(size_t)i * d.K + slot] = j;
+                            ((T*)d.nbrw)[(size_t)i * d.K + slot] = w;
+                        }
+                        a0 += w;                                   // sum of Laplacian weights
+                        a1 += (T)d.press[j];                       // neighbour pressure (feature)
+                        a4 += (T)d.id[j];                          // id checksum (debug)
+                        if (rr < reg) {
+                            gacc = true;
+                            const T rg = rr > mindg ? rr : mindg;
+                            const T wg = reg / rg - T(1);
+                            a2 += wg;                              // PND
+                            // velocity divergence (feature): sum (v_j - v_i).d w / r^2
+                            a3 += ((T(vj4.x) - vi.x) * dv.x + (T(vj4.y) - vi.y) * dv.y + (T(vj4.z) - vi.z) * dv.z) *
+                                  wg / (rg * rg);
+                        }
+                    }
+                }
+                cnt += __popc(bal);
+                if constexpr (MODE == NB_LIST) {
+                    const unsigned gb = __ballot_sync(0xffffffffu, gacc);
+                    if (gacc) {
+                        const int slot = gcnt + __popc(gb & lt);
+                        if (slot < d.KG) {
+                            d.gnbr[(size_t)i * d.KG + slot] = j;
+                            ((T*)d.gnbrr)[(size_t)i * d.KG + slot] = rr;
+                        }
+                    }
+                    gcnt += __popc(gb);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a0 += __shfl_down_sync(0xffffffffu, a0, o);
+            a1 += __shfl_down_sync(0xffffffffu, a1, o);
+            a2 += __shfl_down_sync(0xffffffffu, a2, o);
+            a3 += __shfl_down_sync(0xffffffffu, a3, o);
+            a4 += __shfl_down_sync(0xffffffffu, a4, o);
+        }
+        if (lane != 0) continue;
+        if constexpr (MODE == NB_PREDICT) {
+            // wall friction term, viscosity, gravity, drag (CalcExplicitly_Kernel)
+            double lx = a0, ly = a1, lz = a2;
+            const int t = d.wid[i];
+            const double wd = d.wdist[i];
+            if (t >= 0 && wd > 0 && wd < d.c.re_lap) {
+                const double ww = exact_z<double>(d.c.dim == 2 ? c_zlap2 : c_zlap3, d.c.dim == 2 ? 23 : 25, wd, d.c.l0);
+                const Scalar3 vw = d.tparams[d.tmodel[t]].Velocity;
+                lx += ((double)vw.x - (double)vi.x) * d.c.wall_fric * ww;
+                ly += ((double)vw.y - (double)vi.y) * d.c.wall_fric * ww;
+                lz += ((double)vw.z - (double)vi.z) * d.c.wall_fric * ww;
+            }
+            const double cf = d.c.coef_lap * (double)d.visc[i];
+            const double4 v = d.vel[i];
+            const double4 p = d.pos[i];
+            const double dt = d.c.dt;
+            double4 vn, pn;
+            vn.x = v.x + (d.c.g[0] + lx * cf) * dt - d.dragv[3 * (size_t)i];
+            vn.y = v.y + (d.c.g[1] + ly * cf) * dt - d.dragv[3 * (size_t)i + 1];
+            vn.z = v.z + (d.c.g[2] + lz * cf) * dt - d.dragv[3 * (size_t)i + 2];
+            vn.w = 0.0;
+            pn.x = p.x + vn.x * dt;
+            pn.y = p.y + vn.y * dt;
+            pn.z = p.z + vn.z * dt;
+            pn.w = 0.0;
+            if (!(isfinite(vn.x) && isfinite(vn.y) && isfinite(vn.z))) {
+                atomicOr(d.err, MPS_ERR_NONFINITE);
+                vn = v;
+                pn = p;
+            }
+            d.vel2[i] = vn;
+            d.pos2[i] = pn;
+        } else {
+            if (cnt > d.K || gcnt > d.KG) atomicOr(d.err, MPS_ERR_NEIGHBOUR_CAP);
+            d.nbr_cnt[i] = cnt < d.K ? cnt : d.K;
+            d.gcnt[i] = gcnt < d.KG ? gcnt : d.KG;
+            double pnd = (double)a2;
+            const double riw = d.wdist[i];
+            if (d.wid[i] >= 0 && riw >= 0 && riw <= d.c.re_grad)
+                pnd += exact_z<double>(d.c.dim == 2 ? c_zgrad2 : c_zgrad3, d.c.dim == 2 ? 23 : 21, riw, d.c.l0);
+            d.pnd[i] = pnd;
+            d.sumw[i] = (double)a0;
+            d.feat_aux[4 * (size_t)i] = cnt > 0 ? (double)a1 / cnt : 0.0;
+            d.feat_aux[4 * (size_t)i + 1] = (double)a3 * (double)d.c.dim / d.c.n0_pnd;
+            d.feat_aux[4 * (size_t)i + 2] = (double)cnt;
+            d.feat_aux[4 * (size_t)i + 3] = (double)a4;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PPE assembly, explicit pressure
+// ---------------------------------------------------------------------------
+__global__ void k_ppe_setup(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double pnd = d.pnd[i];
+    const bool in = pnd > d.c.beta * d.c.n0_pnd;
+    d.inner[i] = in ? 1 : 0;
+    if (in) {
+        const double dg = d.c.coef_lap * d.sumw[i] + d.c.kappa;
+        d.diag[i] = dg;
+        d.rhs[i] = d.c.rho / (d.c.dt * d.c.dt) * (pnd - d.c.n0_pnd) / d.c.n0_pnd;
+        d.minv[i] = 1.0 / dg;
+    } else {
+        d.diag[i] = 1.0;
+        d.rhs[i] = 0.0;
+        d.minv[i] = 0.0;
+        d.press[i] = 0.0;
+    }
+}
+
+// The reference's equation of state (CalcExplicitPressure_Kernel :1043-1047)
+__global__ void k_eos(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double pnd = d.pnd[i];
+    d.press[i] = pnd > d.c.beta * d.c.n0_pnd ? d.c.sonic2 * d.c.rho / d.c.n0_pnd * (pnd - d.c.n0_pnd) : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// CG machinery: warp-per-row SpMV over the neighbour rows, vector updates with
+// fused FP64 dot products, convergence decided on the device.
+// ---------------------------------------------------------------------------
+// y = A x for interior rows (y = 0 elsewhere); A = diag - coef * W.  MODE 0: plain
+// (+ dot x.y -> S_PQ, alpha = rz / pq); MODE 1: residual r = b - A x (FP64 out),
+// norms -> S_RR, S_BNORM.
+template <class TW, class TX, class TY, int MODE>
+__global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w,
+                                              const TX* __restrict__ x, TY* __restrict__ y, const double* __restrict__ b,
+                                              int slot) {
+    if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    double part0 = 0.0, part1 = 0.0;
+    const double coef = d.c.coef_lap;
+    for (int i = gw; i < d.n; i += nw) {
+        if (!d.inner[i]) {
+            if (lane == 0) y[i] = TY(0);
+            continue;
+        }
+        const int cnt = d.nbr_cnt[i];
+        const size_t base = (size_t)i * d.K;
+        using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE == 1), double, float>::type;
+        TA acc = TA(0);
+        for (int k = lane; k < cnt; k += 32) acc += (TA)w[base + k] * (TA)x[d.nbr[base + k]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
+            if (MODE == 0) {
+                y[i] = (TY)yi;
+                part0 += (double)x[i] * (double)(TY)yi;
+            } else {
+                const double ri = b[i] - yi;
+                y[i] = (TY)ri;
+                part0 += ri * ri;
+                part1 += b[i] * b[i];
+            }
+        }
+    }
+    double v[2] = {part0, part1}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        if (MODE == 0) {
+            d.scal[S_PQ] = out[0];
+            d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
+        } else {
+            d.scal[S_RR] = out[0];
+            d.scal[S_RNORM] = sqrt(out[0]);
+            d.scal[S_BNORM] = sqrt(out[1]);
+        }
+    }
+}
+
+// CG start: z = M r, p = z, rz = r.z, plus the convergence test on ||r||.
+// r / z / p of type TV; TR the type r is read from (FP64 residual for FP32 inner).
+template <class TV>
+__global__ void __launch_bounds__(256) k_cg_start(const __grid_constant__ Dev d, TV* r, TV* z, TV* p, const double* r64,
+                                                  double scale, const double* m64, const float* m32, TV* xd, int slot,
+                                                  double tol_abs, int maxit) {
+    double prz = 0.0, prr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        double ri = r64 ? r64[i] * scale : (double)r[i];
+        if (!d.inner[i]) ri = 0.0;
+        const double mi = m32 ? (double)m32[i] : m64[i];
+        const TV rv = (TV)ri, zv = (TV)(ri * mi);
+        r[i] = rv;
+        z[i] = zv;
+        p[i] = zv;
+        if (xd) xd[i] = TV(0);
+        prz += (double)rv * (double)zv;
+        prr += (double)rv * (double)rv;
+    }
+    double v[2] = {prz, prr}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        d.scal[S_RZ] = out[0];
+        d.scal[S_RNORM] = sqrt(out[1]);
+        d.scal[S_R0NORM] = sqrt(out[1]);
+        d.scal[S_TOL] = tol_abs;
+        d.scal[S_ITER] = 0.0;
+        d.scal[S_TMP0] = (double)maxit;
+        d.scal[S_CONV] = (sqrt(out[1]) <= tol_abs || maxit <= 0) ? 1.0 : 0.0;
+    }
+}
+
+// x += alpha p; r -= alpha q; z = M r; rz, rr; then beta, convergence.
+template <class TV, class TXA>
+__global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d, TXA* x, TV* r, TV* z, const TV* p,
+                                                   const TV* q, const double* m64, const float* m32, int slot) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const double alpha = d.scal[S_ALPHA];
+    double prz = 0.0, prr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        if (!d.inner[i]) continue;
+        x[i] = (TXA)((double)x[i] + alpha * (double)p[i]);
+        const TV ri = (TV)((double)r[i] - alpha * (double)q[i]);
+        r[i] = ri;
+        const double mi = m32 ? (double)m32[i] : m64[i];
+        const TV zi = (TV)((double)ri * mi);
+        z[i] = zi;
+        prz += (double)ri * (double)zi;
+        prr += (double)ri * (double)ri;
+    }
+    double v[2] = {prz, prr}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        const double rz = d.scal[S_RZ];
+        d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
+        d.scal[S_RZ] = out[0];
+        const double rn = sqrt(out[1]);
+        d.scal[S_RNORM] = rn;
+        const double it = d.scal[S_ITER] + 1.0;
+        d.scal[S_ITER] = it;
+        if (rn <= d.scal[S_TOL] || it >= d.scal[S_TMP0] || !(rn == rn)) d.scal[S_CONV] = 1.0;
+    }
+}
+
+template <class TV>
+__global__ void k_cg_p(const __grid_constant__ Dev d, TV* p, const TV* z) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const double beta = d.scal[S_BETA];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)
+        p[i] = (TV)((double)z[i] + beta * (double)p[i]);
+}
+
+__global__ void k_to_float(int n, const double* a, float* b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
+// x (FP64) += s * dx (FP32), interior only
+__global__ void k_axpy_ir(const __grid_constant__ Dev d, double* x, const float* dx, double s) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)
+        if (d.inner[i]) x[i] += s * (double)dx[i];
+}
+
+// ---------------------------------------------------------------------------
+// pressure-gradient correction (CalcExplicitPressureGradient_Kernel semantics)
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_correct(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const V3<T> pi = load_p<T>(d, i);
+    const double Pi = d.press[i];
+    const T reg = (T)d.c.re_grad, mindg = (T)d.c.mind_grad;
+    T gx = 0, gy = 0, gz = 0;
+    const int cnt = d.gcnt[i];
+    const size_t base = (size_t)i * d.KG;
+    for (int k = 0; k < cnt; ++k) {
+        const int j = d.gnbr[base + k];
+        const T r = ((const T*)d.gnbrr)[base + k];
+        const V3<T> pj = load_p<T>(d, j);
+        const T rr = r > mindg ? r : mindg;
+        const T pc = (T)(0.5 * (d.press[j] + Pi)) * (reg / rr - T(1)) / (rr * rr);
+        gx += (pj.x - pi.x) * pc;
+        gy += (pj.y - pi.y) * pc;
+        gz += (pj.z - pi.z) * pc;
+    }
+    double g[3] = {(double)gx * d.c.c1, (double)gy * d.c.c1, (double)gz * d.c.c1};
+    if (d.wid[i] >= 0) {
+        const double m = d.wdist[i];
+        const double* dir = d.wdir + 3 * (size_t)i;
+        if (m > 0 && m <= d.c.re_grad) {
+            const double ww = exact_z<double>(c_zgrad3, 21, m, d.c.l0);
+            const double wc = 0.5 * d.c.c1 * ww * Pi / (m * m);
+            for (int a = 0; a < 3; ++a) g[a] -= wc * dir[a];
+        }
+        if (m > 0 && m <= d.c.offset_l0) {
+            const double mc = d.c.c2 * (d.c.offset_l0 - m) / m;
+            for (int a = 0; a < 3; ++a) g[a] -= mc * dir[a];
+        }
+    }
+    const double4 v = d.vel[i];
+    const double4 p = d.pos[i];
+    const double c3 = -d.c.dt / d.c.rho;
+    double4 vn = make_double4(v.x + c3 * g[0], v.y + c3 * g[1], v.z + c3 * g[2], 0.0);
+    const double a = sqrt(vn.x * vn.x + vn.y * vn.y + vn.z * vn.z);
+    if (a > d.c.vmax) {
+        const double s = d.c.vmax / a;
+        vn.x *= s; vn.y *= s; vn.z *= s;
+    }
+    if (!(isfinite(vn.x) && isfinite(vn.y) && isfinite(vn.z))) {
+        atomicOr(d.err, MPS_ERR_NONFINITE);
+        vn = v;
+    }
+    d.vel2[i] = vn;
+    d.pos2[i] = make_double4(p.x + (vn.x - v.x) * d.c.dt, p.y + (vn.y - v.y) * d.c.dt, p.z + (vn.z - v.z) * d.c.dt, 0.0);
+}
+
+// Wall motion: translation + incremental rotation with linear ramp, FP64, exactly
+// normalised axis (RotateTrianglePosition_Kernel semantics).
+__global__ void k_walls_move(const __grid_constant__ Dev d, int step) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= d.tri_n) return;
+    const CTriangleParameters tp = d.tparams[d.tmodel[t]];
+    double* v = d.tri + 9 * (size_t)t;
+    const double dt = d.c.dt;
+    for (int q = 0; q < 3; ++q) {
+        v[3 * q] += (double)tp.Velocity.x * dt;
+        v[3 * q + 1] += (double)tp.Velocity.y * dt;
+        v[3 * q + 2] += (double)tp.Velocity.z * dt;
+    }
+    if (!tp.RotatingOrNot) return;
+    const double tpass = dt * step;
+    if (tpass < tp.RotationStartTime || tp.AngleOfRotationInDegree == 0) return;
+    double ang;
+    if (tpass < tp.TimeToReachRPM) {
+        const int req = (int)((tp.TimeToReachRPM - tp.RotationStartTime) / dt);
+        ang = ((double)tp.AngleOfRotationInDegree / (double)(req + 1)) * (step - tp.RotationStartTime / dt);
+    } else {
+        ang = tp.AngleOfRotationInDegree;
+    }
+    if (ang == 0) return;
+    const double cx = tp.CenterOfRotation.x, cy = tp.CenterOfRotation.y, cz = tp.CenterOfRotation.z;
+    double ax = tp.SecondPointOfRotation.x - cx, ay = tp.SecondPointOfRotation.y - cy, az = tp.SecondPointOfRotation.z - cz;
+    const double al = sqrt(ax * ax + ay * ay + az * az);
+    if (!(al > 0)) return;
+    ax /= al; ay /= al; az /= al;
+    const double th = ang * 3.14159265358979323846 / 180.0;
+    double st, ct;
+    sincos(th, &st, &ct);
+    for (int q = 0; q < 3; ++q) {
+        const double px = v[3 * q] - cx, py = v[3 * q + 1] - cy, pz = v[3 * q + 2] - cz;
+        const double kx = ay * pz - az * py, ky = az * px - ax * pz, kz = ax * py - ay * px;
+        const double kv = ax * px + ay * py + az * pz;
+        v[3 * q] = cx + px * ct + kx * st + ax * kv * (1.0 - ct);
+        v[3 * q + 1] = cy + py * ct + ky * st + ay * kv * (1.0 - ct);
+        v[3 * q + 2] = cz + pz * ct + kz * st + az * kv * (1.0 - ct);
+    }
+    const double e1x = v[3] - v[0], e1y = v[4] - v[1], e1z = v[5] - v[2];
+    const double e2x = v[6] - v[0], e2y = v[7] - v[1], e2z = v[8] - v[2];
+    double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+    const double nl = sqrt(nx * nx + ny * ny + nz * nz);
+    if (nl > 0) {
+        d.tnrm[3 * t] = nx / nl;
+        d.tnrm[3 * t + 1] = ny / nl;
+        d.tnrm[3 * t + 2] = nz / nl;
+    }
+}
+
+}  // namespace mps

@@ -1,0 +1,587 @@
+// solver.cu - host orchestration of the GB300-native semi-implicit MPS step and its
+// C-ABI (include/mps_solver.h).
+//
+// One step follows the reference's schedule (CMultiGPUHandler::Calculate,
+// MultiGPUHandler.cpp:1389-1559) with the explicit pressure replaced by a pressure
+// Poisson equation:
+//   compact -> hash / radix sort / gather -> wall bins + wall distance -> drag ->
+//   viscosity/gravity predictor -> compact -> hash / sort / gather -> wall distance ->
+//   neighbour rows + PND -> PPE (Jacobi-PCG, FP64 or FP32 inside FP64 refinement) ->
+//   pressure-gradient correction -> wall motion.
+// All state stays on the device in cell-sorted order; the host reads back only the
+// particle count after each compaction and the CG convergence word every
+// `check_every` iterations.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+#include <vector>
+
+#include "native_kernels.cuh"
+
+namespace mps {
+
+namespace {
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        return cudaMalloc((void**)&p, sizeof(T) * std::max<size_t>(count, 1));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+};
+
+inline int blocks_for(int n, int threads = kBlock) { return std::max(1, div_up(n, threads)); }
+
+}  // namespace
+
+struct Solver {
+    MpsSolverOptions opt;
+    CParameter param;
+    Dev d{};
+    int nmax = 0;
+    int bins_dirty = 1;
+    int models = 0;
+    int walls_move = 0;
+    cudaStream_t st = nullptr;
+    std::vector<void*> allocs;
+    void* sort_scratch = nullptr;
+    size_t sort_scratch_bytes = 0;
+    unsigned *keep = nullptr, *rank = nullptr;
+    double* h_scal = nullptr;   // pinned mirror of the device scalars
+    int* h_int = nullptr;       // pinned small ints
+    // wall-bin scratch
+    unsigned* bin_off = nullptr;
+    int* bin_visit = nullptr;
+    size_t bin_visit_cap = 0;
+    void* bin_sort = nullptr;
+    size_t bin_sort_bytes = 0;
+    MpsStepStats last{};
+    // learned parameters (optional)
+    bool learned_ready = false;
+
+    template <class T>
+    cudaError_t mk(T** ptr, size_t count) {
+        cudaError_t e = cudaMalloc((void**)ptr, sizeof(T) * std::max<size_t>(count, 1));
+        if (e == cudaSuccess) allocs.push_back((void*)*ptr);
+        return e;
+    }
+
+    bool fp64() const { return opt.precision == MPS_PREC_FP64; }
+
+    CCTStatusType init(const CParameter* prm, const CGridBox* box, int max_particles, const MpsSolverOptions* o) {
+        opt = *o;
+        param = *prm;
+        nmax = max_particles;
+        d.box = *box;
+        d.cells = box->m_GridSize.x * box->m_GridSize.y * box->m_GridSize.z;
+        if (d.cells <= 0 || nmax <= 0) return CCT_PARAMERR;
+        d.K = opt.max_neighbours > 0 ? opt.max_neighbours : 384;
+        d.KG = 64;
+        Consts& c = d.c;
+        const CParameter& P = param;
+        c.l0 = P.InitialParticleDistance;
+        c.re_lap = (double)P.LaplacianInfluenceRadiusCoefficient * c.l0;
+        c.re_grad = (double)P.GradientInfluenceRadiusCoefficient * c.l0;
+        c.mind_lap = c.re_lap * 1e-3;
+        c.mind_grad = c.re_grad * 1e-3;
+        c.n0_pnd = opt.n0_pnd > 0 ? opt.n0_pnd : (double)P.ConstantParticleDensity;
+        c.n0_lap = opt.n0_lap > 0 ? opt.n0_lap : (double)P.ConstantParticleDensity;
+        const double lam = opt.lambda > 0 ? opt.lambda : (double)P.LambdaValue;
+        c.dim = P.Dimension;
+        c.coef_lap = 2.0 * c.dim / (lam * c.n0_lap);
+        c.beta = P.FreeSurfaceThreshold;
+        c.rho = P.Density;
+        c.dt = P.Dt;
+        c.kappa = opt.compressibility * c.rho / (c.dt * c.dt);
+        c.c1 = 2.0 * c.dim / c.n0_pnd;
+        c.c2 = c.rho / (c.dt * c.dt);
+        c.vmax = c.l0 * (double)P.CourantNumber / c.dt;
+        c.wall_fric = P.WallFrictionCoeffieicnt;
+        c.offset_l0 = c.l0 * (double)P.OffSet;
+        c.tol = P.Tolerance;
+        c.sonic2 = (double)P.SonicVelocity * (double)P.SonicVelocity;
+        c.g[0] = P.GravityConstant.x;
+        c.g[1] = P.GravityConstant.y;
+        c.g[2] = P.GravityConstant.z;
+        c.explicit_pressure = opt.pressure_mode == MPS_PRESSURE_EXPLICIT;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CCT_CUDAERR;
+        const size_t N = nmax;
+        const size_t wsz = fp64() ? sizeof(double) : sizeof(float);
+        cudaError_t e = cudaSuccess;
+        e = e ? e : mk(&d.pos, N); e = e ? e : mk(&d.vel, N); e = e ? e : mk(&d.pos2, N); e = e ? e : mk(&d.vel2, N);
+        e = e ? e : mk(&d.press, N); e = e ? e : mk(&d.press2, N); e = e ? e : mk(&d.visc, N); e = e ? e : mk(&d.visc2, N);
+        e = e ? e : mk(&d.type, N); e = e ? e : mk(&d.type2, N); e = e ? e : mk(&d.id, N); e = e ? e : mk(&d.id2, N);
+        e = e ? e : mk(&d.opos, N); e = e ? e : mk(&d.ovel, N);
+        e = e ? e : mk(&d.key, N); e = e ? e : mk(&d.idx, N);
+        e = e ? e : mk(&d.cstart, (size_t)d.cells); e = e ? e : mk(&d.cend, (size_t)d.cells);
+        e = e ? e : mk(&d.cell_list, (size_t)d.cells); e = e ? e : mk(&d.cell_count, 1);
+        e = e ? e : mk(&d.wdist, N); e = e ? e : mk(&d.wdir, 3 * N); e = e ? e : mk(&d.wid, N);
+        e = e ? e : mk(&d.dragv, 3 * N);
+        e = e ? e : mk(&d.tcs, 2 * (size_t)d.cells);
+        e = e ? e : mk(&d.nbr, N * d.K); e = e ? e : mk((char**)&d.nbrw, N * d.K * wsz);
+        e = e ? e : mk(&d.nbr_cnt, N);
+        e = e ? e : mk(&d.gnbr, N * d.KG); e = e ? e : mk((char**)&d.gnbrr, N * d.KG * wsz);
+        e = e ? e : mk(&d.gcnt, N);
+        e = e ? e : mk(&d.pnd, N); e = e ? e : mk(&d.diag, N); e = e ? e : mk(&d.rhs, N); e = e ? e : mk(&d.sumw, N);
+        e = e ? e : mk(&d.inner, N);
+        e = e ? e : mk(&d.r, N); e = e ? e : mk(&d.z, N); e = e ? e : mk(&d.p, N); e = e ? e : mk(&d.q, N);
+        e = e ? e : mk(&d.minv, N);
+        e = e ? e : mk(&d.r32, N); e = e ? e : mk(&d.z32, N); e = e ? e : mk(&d.p32, N); e = e ? e : mk(&d.q32, N);
+        e = e ? e : mk(&d.d32, N); e = e ? e : mk(&d.m32, N);
+        e = e ? e : mk(&d.feat_aux, 4 * N);
+        e = e ? e : mk(&d.red, 4 * (size_t)kRedBlocks);
+        e = e ? e : mk(&d.scal, (size_t)S_COUNT);
+        e = e ? e : mk(&d.red_count, 16);
+        e = e ? e : mk(&d.err, 1);
+        e = e ? e : mk(&keep, N + 1);
+        e = e ? e : mk(&rank, N + 1);
+        if (e != cudaSuccess) return CCT_MEMERR;
+        sort_scratch_bytes = radix_scratch_bytes(nmax);
+        if (cudaMalloc(&sort_scratch, sort_scratch_bytes) != cudaSuccess) return CCT_MEMERR;
+        allocs.push_back(sort_scratch);
+        if (cudaMallocHost((void**)&h_scal, sizeof(double) * S_COUNT) != cudaSuccess) return CCT_MEMERR;
+        if (cudaMallocHost((void**)&h_int, sizeof(int) * 8) != cudaSuccess) return CCT_MEMERR;
+        cudaMemset(d.red_count, 0, sizeof(unsigned) * 16);
+        cudaMemset(d.scal, 0, sizeof(double) * S_COUNT);
+        cudaMemset(d.err, 0, sizeof(unsigned));
+        return cudaDeviceSynchronize() == cudaSuccess ? CCT_NOERR : CCT_CUDAERR;
+    }
+
+    void destroy() {
+        cudaDeviceSynchronize();
+        for (void* p : allocs) cudaFree(p);
+        allocs.clear();
+        if (bin_off) cudaFree(bin_off);
+        if (bin_visit) cudaFree(bin_visit);
+        if (bin_sort) cudaFree(bin_sort);
+        if (d.tri) cudaFree(d.tri);
+        if (d.tnrm) cudaFree(d.tnrm);
+        if (d.tmodel) cudaFree(d.tmodel);
+        if (d.tparams) cudaFree(d.tparams);
+        if (d.drag) cudaFree(d.drag);
+        if (h_scal) cudaFreeHost(h_scal);
+        if (h_int) cudaFreeHost(h_int);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    void swap_state() {
+        std::swap(d.pos, d.pos2);
+        std::swap(d.vel, d.vel2);
+        std::swap(d.press, d.press2);
+        std::swap(d.visc, d.visc2);
+        std::swap(d.type, d.type2);
+        std::swap(d.id, d.id2);
+    }
+
+    CCTStatusType set_particles(int n, const double* pos, const double* vel, const double* press, const double* visc,
+                                const int* type) {
+        if (n < 0 || n > nmax) return CCT_PARAMERR;
+        std::vector<double4> P(n), V(n);
+        std::vector<double> pr(n, 0.0);
+        std::vector<float> vi(n);
+        std::vector<int> ty(n, 0), id(n);
+        for (int i = 0; i < n; ++i) {
+            P[i] = make_double4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+            V[i] = make_double4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
+            if (press) pr[i] = press[i];
+            vi[i] = (float)visc[i];
+            if (type) ty[i] = type[i];
+            id[i] = i;
+        }
+        d.n = n;
+        cudaError_t e = cudaMemcpyAsync(d.pos, P.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(d.vel, V.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(d.press, pr.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(d.visc, vi.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(d.type, ty.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(d.id, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaStreamSynchronize(st);
+        return cuda_status(e);
+    }
+
+    CCTStatusType set_triangles(int t, const double* v, const int* model, int nmodels, const CTriangleParameters* tp) {
+        if (d.tri) { cudaFree(d.tri); cudaFree(d.tnrm); cudaFree(d.tmodel); cudaFree(d.tparams); }
+        d.tri = nullptr; d.tnrm = nullptr; d.tmodel = nullptr; d.tparams = nullptr;
+        d.tri_n = t;
+        models = nmodels;
+        walls_move = 0;
+        for (int m = 0; m < nmodels; ++m) {
+            const Scalar3 vv = tp[m].Velocity;
+            if (tp[m].RotatingOrNot || vv.x != 0 || vv.y != 0 || vv.z != 0) walls_move = 1;
+        }
+        if (t <= 0) return CCT_NOERR;
+        std::vector<double> nrm(3 * (size_t)t);
+        for (int i = 0; i < t; ++i) {
+            const double* q = v + 9 * (size_t)i;
+            const double e1[3] = {q[3] - q[0], q[4] - q[1], q[5] - q[2]}, e2[3] = {q[6] - q[0], q[7] - q[1], q[8] - q[2]};
+            double n3[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            const double l = std::sqrt(n3[0] * n3[0] + n3[1] * n3[1] + n3[2] * n3[2]);
+            for (int a = 0; a < 3; ++a) nrm[3 * (size_t)i + a] = l > 0 ? n3[a] / l : 0.0;
+        }
+        cudaError_t e = cudaMalloc(&d.tri, sizeof(double) * 9 * (size_t)t);
+        if (!e) e = cudaMalloc(&d.tnrm, sizeof(double) * 3 * (size_t)t);
+        if (!e) e = cudaMalloc(&d.tmodel, sizeof(int) * (size_t)t);
+        if (!e) e = cudaMalloc(&d.tparams, sizeof(CTriangleParameters) * std::max(nmodels, 1));
+        if (e) return CCT_MEMERR;
+        e = cudaMemcpy(d.tri, v, sizeof(double) * 9 * (size_t)t, cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(d.tnrm, nrm.data(), sizeof(double) * 3 * (size_t)t, cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(d.tmodel, model, sizeof(int) * (size_t)t, cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(d.tparams, tp, sizeof(CTriangleParameters) * nmodels, cudaMemcpyHostToDevice);
+        bins_dirty = 1;
+        return cuda_status(e);
+    }
+
+    CCTStatusType set_drag(int count, const DragParameter* dp) {
+        if (d.drag) cudaFree(d.drag);
+        d.drag = nullptr;
+        d.drag_n = count;
+        if (count <= 0) return CCT_NOERR;
+        if (cudaMalloc(&d.drag, sizeof(DragParameter) * count)) return CCT_MEMERR;
+        return cuda_status(cudaMemcpy(d.drag, dp, sizeof(DragParameter) * count, cudaMemcpyHostToDevice));
+    }
+
+    // ---- phases ----
+    CCTStatusType compact() {
+        const int n = d.n;
+        if (n <= 0) return CCT_NOERR;
+        k_zone_flags<<<blocks_for(n), kBlock, 0, st>>>(d, keep);
+        cudaMemcpyAsync(rank, keep, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
+        scan_exclusive(rank, n, rank + n, st);
+        k_compact<<<blocks_for(n), kBlock, 0, st>>>(d, keep, rank);
+        cudaMemcpyAsync(h_int, rank + n, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
+        swap_state();
+        d.n = h_int[0];
+        return CCT_NOERR;
+    }
+
+    CCTStatusType grid() {
+        const int n = d.n;
+        if (n <= 0) return CCT_NOERR;
+        k_hash<<<blocks_for(n), kBlock, 0, st>>>(d);
+        if (radix_sort_pairs(n, d.key, d.idx, 0, radix_passes((unsigned)(d.cells - 1)), sort_scratch, st)) return CCT_CUDAERR;
+        cudaMemsetAsync(d.cstart, 0xff, sizeof(int) * d.cells, st);
+        cudaMemsetAsync(d.cend, 0xff, sizeof(int) * d.cells, st);
+        cudaMemsetAsync(d.cell_count, 0, sizeof(int), st);
+        k_gather<<<blocks_for(n), kBlock, 0, st>>>(d);
+        swap_state();
+        return cuda_status(cudaGetLastError());
+    }
+
+    CCTStatusType bin_walls() {
+        const int t = d.tri_n;
+        if (t <= 0) return CCT_NOERR;
+        if (!bin_off && cudaMalloc(&bin_off, sizeof(unsigned) * ((size_t)t + 2))) return CCT_MEMERR;
+        k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off);
+        scan_exclusive(bin_off, t + 1, nullptr, st);
+        cudaMemcpyAsync(h_int, bin_off + t, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
+        const unsigned nv = (unsigned)h_int[0];
+        if (nv == 0) {
+            cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 2 * d.cells, st);
+            bins_dirty = 0;
+            return CCT_NOERR;
+        }
+        if (nv > bin_visit_cap) {
+            if (bin_visit) cudaFree(bin_visit);
+            if (bin_sort) cudaFree(bin_sort);
+            bin_visit_cap = nv + nv / 2;
+            if (cudaMalloc(&bin_visit, sizeof(int) * 2 * bin_visit_cap)) return CCT_MEMERR;
+            bin_sort_bytes = radix_scratch_bytes((int)bin_visit_cap);
+            if (cudaMalloc(&bin_sort, bin_sort_bytes)) return CCT_MEMERR;
+            d.tids = bin_visit + bin_visit_cap;
+        }
+        int* vcell = bin_visit;
+        d.tids = bin_visit + bin_visit_cap;
+        k_bin_fill<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, vcell, d.tids);
+        if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(d.cells - 1)), bin_sort, st))
+            return CCT_CUDAERR;
+        cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 2 * d.cells, st);
+        k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, st>>>((int)nv, vcell, d.tcs, d.tcs + d.cells);
+        bins_dirty = 0;
+        return cuda_status(cudaGetLastError());
+    }
+
+    template <class T>
+    void walls_distance() {
+        if (d.tri_n > 0) {
+            k_wall_distance<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+        } else {
+            cudaMemsetAsync(d.wid, 0xff, sizeof(int) * d.n, st);
+        }
+    }
+
+    template <class T>
+    CCTStatusType run_step(int step, MpsStepStats* out) {
+        MpsStepStats S{};
+        cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
+        CCTStatusType rc;
+        if ((rc = compact())) return rc;
+        if ((rc = grid())) return rc;
+        if (d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
+        walls_distance<T>();
+        if (d.drag_n > 0 && d.tri_n > 0) k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+        else cudaMemsetAsync(d.dragv, 0, sizeof(double) * 3 * d.n, st);
+        const int nb_grid = std::max(1, std::min(d.cells, d.n));
+        k_neighbours<T, NB_PREDICT><<<nb_grid, kNbThreads, 0, st>>>(d);
+        std::swap(d.pos, d.pos2);
+        std::swap(d.vel, d.vel2);
+        if ((rc = compact())) return rc;
+        if ((rc = grid())) return rc;
+        walls_distance<T>();
+        k_neighbours<T, NB_LIST><<<std::max(1, std::min(d.cells, d.n)), kNbThreads, 0, st>>>(d);
+        if (opt.pressure_mode == MPS_PRESSURE_EXPLICIT) {
+            k_eos<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+        } else {
+            k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
+        }
+        k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+        std::swap(d.pos, d.pos2);
+        std::swap(d.vel, d.vel2);
+        if (d.tri_n > 0 && walls_move) {
+            k_walls_move<<<blocks_for(d.tri_n), kBlock, 0, st>>>(d, step);
+            bins_dirty = 1;
+        }
+        cudaMemcpyAsync(h_int, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
+        S.error_flags = (unsigned)h_int[0];
+        S.particles = d.n;
+        last = S;
+        if (out) *out = S;
+        return CCT_NOERR;
+    }
+
+    // read the device scalars
+    CCTStatusType pull_scal() {
+        cudaMemcpyAsync(h_scal, d.scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st);
+        return cudaStreamSynchronize(st) == cudaSuccess ? CCT_NOERR : CCT_CUDAERR;
+    }
+
+    template <class TW, class TV, class TXA>
+    int cg_loop(TXA* x, TV* r, TV* z, TV* p, TV* q, const TW* w, const double* m64, const float* m32, int maxit) {
+        const int every = opt.check_every > 0 ? opt.check_every : 8;
+        int done = 0;
+        while (done < maxit + every) {
+            for (int k = 0; k < every; ++k) {
+                k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+                k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1);
+                k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
+            }
+            done += every;
+            if (pull_scal()) return -1;
+            if (h_scal[S_CONV] != 0.0) break;
+        }
+        return (int)h_scal[S_ITER];
+    }
+
+    // plain FP64 Jacobi-PCG from the warm start in press
+    CCTStatusType solve_fp64(MpsStepStats& S) {
+        const double* w = (const double*)d.nbrw;
+        k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        if (pull_scal()) return CCT_CUDAERR;
+        const double bnorm = h_scal[S_BNORM];
+        const double tol = opt.cg_rtol * bnorm;
+        k_cg_start<double><<<kRedBlocks, 256, 0, st>>>(d, d.r, d.z, d.p, nullptr, 1.0, d.minv, nullptr, nullptr, 3, tol,
+                                                       opt.cg_max_iter);
+        const int it = cg_loop<double, double, double>(d.press, d.r, d.z, d.p, d.q, w, d.minv, nullptr, opt.cg_max_iter);
+        if (it < 0) return CCT_CUDAERR;
+        // true residual
+        k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        if (pull_scal()) return CCT_CUDAERR;
+        S.cg_iterations += it;
+        S.b_norm = bnorm;
+        S.cg_relres = bnorm > 0 ? h_scal[S_RNORM] / bnorm : 0.0;
+        if (bnorm > 0 && S.cg_relres > opt.cg_rtol) S.error_flags |= MPS_ERR_CG;
+        return CCT_NOERR;
+    }
+
+    // FP32 Jacobi-PCG inside FP64 iterative refinement
+    CCTStatusType solve_ir(MpsStepStats& S) {
+        const float* w = (const float*)d.nbrw;
+        k_to_float<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.minv, d.m32);
+        double bnorm = 0.0;
+        int outer = 0;
+        for (;;) {
+            k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+            if (pull_scal()) return CCT_CUDAERR;
+            bnorm = h_scal[S_BNORM];
+            const double rn = h_scal[S_RNORM];
+            S.cg_relres = bnorm > 0 ? rn / bnorm : 0.0;
+            if (bnorm == 0.0 || rn <= opt.cg_rtol * bnorm || outer >= opt.ir_max_outer) break;
+            // inner FP32 solve of A d = r / ||r|| to ir_inner_rtol
+            k_cg_start<float><<<kRedBlocks, 256, 0, st>>>(d, d.r32, d.z32, d.p32, d.r, 1.0 / rn, nullptr, d.m32, d.d32, 3,
+                                                          opt.ir_inner_rtol, opt.cg_max_iter);
+            const int it = cg_loop<float, float, float>(d.d32, d.r32, d.z32, d.p32, d.q32, w, nullptr, d.m32,
+                                                        opt.cg_max_iter);
+            if (it < 0) return CCT_CUDAERR;
+            S.cg_iterations += it;
+            k_axpy_ir<<<kRedBlocks, 256, 0, st>>>(d, d.press, d.d32, rn);
+            ++outer;
+        }
+        S.ir_passes = outer;
+        S.b_norm = bnorm;
+        if (bnorm > 0 && S.cg_relres > opt.cg_rtol) S.error_flags |= MPS_ERR_CG;
+        return CCT_NOERR;
+    }
+
+    CCTStatusType step(int stepi, MpsStepStats* out) {
+        return fp64() ? run_step<double>(stepi, out) : run_step<float>(stepi, out);
+    }
+};
+
+}  // namespace mps
+
+using mps::Solver;
+
+struct MpsSolver {
+    Solver s;
+};
+
+extern "C" {
+
+void mps_solver_default_options(MpsSolverOptions* o) {
+    std::memset(o, 0, sizeof(*o));
+    o->precision = MPS_PREC_FP32_IR;
+    o->pressure_mode = MPS_PRESSURE_PPE;
+    o->learned = 0;
+    o->compressibility = 1e-9;
+    o->cg_rtol = 1e-8;
+    o->cg_max_iter = 5000;
+    o->ir_inner_rtol = 1e-4;
+    o->ir_max_outer = 12;
+    o->max_neighbours = 384;
+    o->check_every = 8;
+}
+
+CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
+                                const MpsSolverOptions* opt, MpsSolver** out) {
+    if (!param || !box || !out) return CCT_PARAMERR;
+    MpsSolverOptions o;
+    if (opt) o = *opt; else mps_solver_default_options(&o);
+    MpsSolver* s = new MpsSolver();
+    CCTStatusType rc = s->s.init(param, box, max_particles, &o);
+    if (rc != CCT_NOERR) {
+        s->s.destroy();
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return CCT_NOERR;
+}
+
+void mps_solver_destroy(MpsSolver* s) {
+    if (!s) return;
+    s->s.destroy();
+    delete s;
+}
+
+CCTStatusType mps_solver_set_particles(MpsSolver* s, int n, const double* pos, const double* vel, const double* press,
+                                       const double* visc, const int* type) {
+    if (!s || !pos || !vel || !visc) return CCT_PARAMERR;
+    return s->s.set_particles(n, pos, vel, press, visc, type);
+}
+
+CCTStatusType mps_solver_set_triangles(MpsSolver* s, int t, const double* v, const int* model, int models,
+                                       const CTriangleParameters* params) {
+    if (!s || (t > 0 && (!v || !model || !params))) return CCT_PARAMERR;
+    return s->s.set_triangles(t, v, model, models, params);
+}
+
+CCTStatusType mps_solver_set_drag(MpsSolver* s, int count, const DragParameter* params) {
+    if (!s) return CCT_PARAMERR;
+    return s->s.set_drag(count, params);
+}
+
+CCTStatusType mps_solver_step(MpsSolver* s, int step, MpsStepStats* stats) {
+    if (!s) return CCT_PARAMERR;
+    return s->s.step(step, stats);
+}
+
+CCTStatusType mps_solver_get_particles(MpsSolver* s, int* n, double* pos, double* vel, double* press, double* pnd,
+                                       int* id) {
+    if (!s) return CCT_PARAMERR;
+    mps::Dev& d = s->s.d;
+    *n = d.n;
+    std::vector<double4> tmp(d.n);
+    cudaError_t e = cudaStreamSynchronize(s->s.st);
+    if (!e && pos) {
+        e = cudaMemcpy(tmp.data(), d.pos, sizeof(double4) * d.n, cudaMemcpyDeviceToHost);
+        for (int i = 0; i < d.n; ++i) { pos[3 * i] = tmp[i].x; pos[3 * i + 1] = tmp[i].y; pos[3 * i + 2] = tmp[i].z; }
+    }
+    if (!e && vel) {
+        e = cudaMemcpy(tmp.data(), d.vel, sizeof(double4) * d.n, cudaMemcpyDeviceToHost);
+        for (int i = 0; i < d.n; ++i) { vel[3 * i] = tmp[i].x; vel[3 * i + 1] = tmp[i].y; vel[3 * i + 2] = tmp[i].z; }
+    }
+    if (!e && press) e = cudaMemcpy(press, d.press, sizeof(double) * d.n, cudaMemcpyDeviceToHost);
+    if (!e && pnd) e = cudaMemcpy(pnd, d.pnd, sizeof(double) * d.n, cudaMemcpyDeviceToHost);
+    if (!e && id) e = cudaMemcpy(id, d.id, sizeof(int) * d.n, cudaMemcpyDeviceToHost);
+    return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_get_triangles(MpsSolver* s, double* v) {
+    if (!s) return CCT_PARAMERR;
+    if (s->s.d.tri_n <= 0) return CCT_NOERR;
+    cudaStreamSynchronize(s->s.st);
+    return mps::cuda_status(cudaMemcpy(v, s->s.d.tri, sizeof(double) * 9 * s->s.d.tri_n, cudaMemcpyDeviceToHost));
+}
+
+CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, double* rhs, double* sol, int* id,
+                                   int* nbr_count, double* nbr_idsum) {
+    if (!s) return CCT_PARAMERR;
+    mps::Dev& d = s->s.d;
+    const int n = d.n;
+    cudaError_t e = cudaStreamSynchronize(s->s.st);
+    if (!e && pnd) e = cudaMemcpy(pnd, d.pnd, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (!e && diag) e = cudaMemcpy(diag, d.diag, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (!e && rhs) e = cudaMemcpy(rhs, d.rhs, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (!e && sol) e = cudaMemcpy(sol, d.press, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    if (!e && id) e = cudaMemcpy(id, d.id, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    if (!e && nbr_count) e = cudaMemcpy(nbr_count, d.nbr_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    if (!e && nbr_idsum) {
+        std::vector<double> aux(4 * (size_t)n);
+        e = cudaMemcpy(aux.data(), d.feat_aux, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost);
+        for (int i = 0; i < n; ++i) nbr_idsum[i] = aux[4 * (size_t)i + 3];
+    }
+    return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n) {
+    if (!s) return CCT_PARAMERR;
+    *press = s->s.d.press;
+    *n = s->s.d.n;
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_solver_copy_pressure(MpsSolver* s, double* host_press) {
+    if (!s) return CCT_PARAMERR;
+    cudaError_t e = cudaMemcpyAsync(host_press, s->s.d.press, sizeof(double) * s->s.d.n, cudaMemcpyDeviceToHost, s->s.st);
+    if (!e) e = cudaStreamSynchronize(s->s.st);
+    return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_stream(MpsSolver* s, void** stream) {
+    if (!s) return CCT_PARAMERR;
+    *stream = (void*)s->s.st;
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_solver_set_learned(MpsSolver* s, const float* params, int count) {
+    (void)s; (void)params; (void)count;
+    return CCT_PARAMERR;
+}
+
+CCTStatusType mps_solver_learned_samples(MpsSolver* s, float* features, float* targets, int* n) {
+    (void)s; (void)features; (void)targets; (void)n;
+    return CCT_PARAMERR;
+}
+
+}  // extern "C"

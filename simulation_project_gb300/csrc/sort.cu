@@ -1,0 +1,212 @@
+// sort.cu - stable LSD radix sort of (int key, int value) pairs on the GPU.
+//
+// Replaces the reference's thrust::sort_by_key call (SortUsingThrust,
+// radix/SPVSOLVER/MultiGPUSolver/DeviceProcess.cu:207-220).  For int keys Thrust's
+// sort is a stable radix sort, so the result is uniquely the stable order; this sort
+// produces exactly that order.
+//
+// Per 8-bit digit pass:
+//   k_digit_hist : each 2048-key tile counts its digits (warp-aggregated with
+//                  __match_any_sync, then shared-memory adds); counts stored
+//                  digit-major: counts[d * tiles + tile]
+//   k_scan_excl  : one CTA turns the counts into exclusive offsets
+//   k_scatter    : each tile re-reads its keys in index order (warp w owns keys
+//                  [w*256, w*256+256) of the tile, 32 per round), ranks them stably
+//                  with __match_any_sync + per-warp running digit counters, and
+//                  writes key and value to offset[d][tile] + warp prefix + rank.
+// Keys are sorted as unsigned offsets (key - kmin), so negative keys sort correctly
+// and a pass runs only for the digits the key range actually spans.
+#include "mps_common.cuh"
+#include "mps_internal.h"
+
+namespace mps {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kRadix = 256;
+
+__device__ __forceinline__ unsigned digit_of(int key, int kmin, int shift) {
+    return (((unsigned)key - (unsigned)kmin) >> shift) & 255u;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_digit_hist(const int* __restrict__ keys, int n, int kmin, int shift,
+                                                            int tiles, unsigned* __restrict__ counts) {
+    __shared__ unsigned h[kRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int base = blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * kSortThreads + threadIdx.x;
+        const bool ok = idx < n;
+        const unsigned d = ok ? digit_of(keys[idx], kmin, shift) : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (ok && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[d], (unsigned)__popc(peers));
+    }
+    __syncthreads();
+    counts[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of len unsigned values, in place, by one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_excl(unsigned* __restrict__ a, int len, unsigned* __restrict__ total) {
+    __shared__ unsigned wsum[32];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int per = (len + 1023) / 1024;
+    const int b = min(len, tid * per), e = min(len, b + per);
+    unsigned s = 0;
+    for (int i = b; i < e; ++i) s += a[i];
+    unsigned inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        const unsigned x = wsum[lane];
+        unsigned xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(0xffffffffu, xi, o);
+            if (lane >= o) xi += v;
+        }
+        wsum[lane] = xi - x;
+        if (lane == 31 && total) *total = xi;
+    }
+    __syncthreads();
+    unsigned run = inc - s + wsum[w];
+    for (int i = b; i < e; ++i) {
+        const unsigned c = a[i];
+        a[i] = run;
+        run += c;
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_scatter(const int* __restrict__ kin, const int* __restrict__ vin,
+                                                         int* __restrict__ kout, int* __restrict__ vout, int n,
+                                                         int kmin, int shift, int tiles,
+                                                         const unsigned* __restrict__ offsets) {
+    __shared__ unsigned wcount[kSortThreads / 32][kRadix];
+    __shared__ unsigned toff[kRadix];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < (kSortThreads / 32) * kRadix; i += kSortThreads) (&wcount[0][0])[i] = 0;
+    toff[threadIdx.x] = offsets[threadIdx.x * tiles + blockIdx.x];
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile + w * (32 * kSortItems);
+    int key[kSortItems], val[kSortItems];
+    unsigned dig[kSortItems], rank[kSortItems];
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * 32 + lane;
+        const bool ok = idx < n;
+        key[r] = ok ? kin[idx] : 0;
+        val[r] = ok ? vin[idx] : 0;
+        const unsigned d = ok ? digit_of(key[r], kmin, shift) : 256u;
+        dig[r] = d;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const unsigned lt = peers & ((1u << lane) - 1u);
+        const unsigned before = ok ? wcount[w][d] : 0u;
+        __syncwarp();
+        if (ok && lt == 0) wcount[w][d] = before + (unsigned)__popc(peers);
+        __syncwarp();
+        rank[r] = before + (unsigned)__popc(lt);
+    }
+    __syncthreads();
+    {
+        unsigned run = 0;
+        for (int ww = 0; ww < kSortThreads / 32; ++ww) {
+            const unsigned c = wcount[ww][threadIdx.x];
+            wcount[ww][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const unsigned d = dig[r];
+        if (d < 256u) {
+            const unsigned dst = toff[d] + wcount[w][d] + rank[r];
+            kout[dst] = key[r];
+            vout[dst] = val[r];
+        }
+    }
+}
+
+__global__ void k_minmax(const int* __restrict__ keys, int n, int* __restrict__ mm) {
+    int lo = INT_MAX, hi = INT_MIN;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int k = keys[i];
+        lo = min(lo, k);
+        hi = max(hi, k);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&mm[0], lo);
+        atomicMax(&mm[1], hi);
+    }
+}
+
+__global__ void k_minmax_init(int* mm) {
+    mm[0] = INT_MAX;
+    mm[1] = INT_MIN;
+}
+
+size_t radix_scratch_bytes(int n) {
+    const int tiles = div_up(n > 0 ? n : 1, kSortTile);
+    return sizeof(int) * 2 * (size_t)n + sizeof(unsigned) * ((size_t)kRadix * tiles + 8) + 256;
+}
+
+int radix_passes(unsigned range) {
+    int bits = 0;
+    while (bits < 32 && (range >> bits) != 0u) ++bits;
+    return (bits + 7) / 8;
+}
+
+cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, void* scratch, cudaStream_t st) {
+    if (n <= 1 || passes <= 0) return cudaSuccess;
+    const int tiles = div_up(n, kSortTile);
+    char* p = (char*)scratch;
+    int* kalt = (int*)p;
+    p += sizeof(int) * (size_t)n;
+    int* valt = (int*)p;
+    p += sizeof(int) * (size_t)n;
+    unsigned* counts = (unsigned*)p;
+    int* ka = keys;
+    int* va = vals;
+    int* kb = kalt;
+    int* vb = valt;
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = pass * 8;
+        k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts);
+        k_scan_excl<<<1, 1024, 0, st>>>(counts, kRadix * tiles, nullptr);
+        k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, kmin, shift, tiles, counts);
+        int* t = ka; ka = kb; kb = t;
+        t = va; va = vb; vb = t;
+    }
+    if (ka != keys) {
+        cudaMemcpyAsync(keys, ka, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(vals, va, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t key_minmax(int n, const int* keys, int* mm_dev, cudaStream_t st) {
+    k_minmax_init<<<1, 1, 0, st>>>(mm_dev);
+    const int blocks = min(div_up(n, 1024), 152 * 4);
+    if (n > 0) k_minmax<<<blocks, 1024, 0, st>>>(keys, n, mm_dev);
+    return cudaGetLastError();
+}
+
+cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st) {
+    if (len <= 0) return cudaSuccess;
+    k_scan_excl<<<1, 1024, 0, st>>>(a, len, total_dev);
+    return cudaGetLastError();
+}
+
+}  // namespace mps
