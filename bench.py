@@ -1,0 +1,377 @@
+"""Benchmark: particle-steps/s of the semi-implicit MPS step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--l0 0.002]
+
+Workload: the rotating bucket (cylinder r = 0.15 m, L = 0.3 m, 4096 wall triangles,
+30 rpm, 64 drag spheres of radius 3*l0) filled 35 % at l0 = 0.002 m (~0.9M
+particles), PPE solved to relative residual 1e-8.  Synthetic inputs: seeded jittered
+lattice, no dataset.  One "step" is one full solver step (topology, walls, drag,
+predictor, topology, PND, PPE solve, pressure-gradient correction, wall motion).
+
+value       = particle-steps/s of the FP32-operator / FP64-refined solver with the
+              learned initial guess and scaling (trained on the GPU by the library's
+              own BF16 tensor-core kernels before the timed region), states resident
+              in HBM;
+plain_fp64  = the same steps with every operator and Jacobi-PCG in FP64;
+e2e         = the learned solver driven through the public C-ABI from pinned host
+              buffers: each step uploads the state, steps, and downloads it.
+roofline    = the PPE SpMV (the dominant kernel) timed with CUDA events on the solver
+              stream inside the timed region; algorithmic bytes per launch = 8 B per
+              neighbour entry (int32 index + FP32 weight) + 25 B per interior row.
+cpu_baseline= the FP64 oracle solver with OpenMP on the host cores, on a bounded
+              sample (the same bucket at l0 = 0.004, ~1e5 particles, 1 step).
+--impl reference: the reference's own explicit-schedule kernels compiled for the CPU
+              (oracle/_ref/libref.so, OpenMP over particles), timed on the same
+              bucket at l0 = 0.004 (a bounded sample), per step.
+Multi-GPU: replicas only (each rank runs its own scene; value = sum over ranks).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def load_peaks():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (SM clock, max clock, throttle reasons) during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_scene(l0, seed=4):
+    from simulation_project_gb300 import scenes
+    return scenes.rotating_bucket(l0=l0, dt=5e-5, seed=seed, n_drag=64, drag_seed=3)
+
+
+def time_steps(solver, steps, warmup, first_step=0):
+    from simulation_project_gb300 import lib
+    for i in range(warmup):
+        solver.step(first_step + i)
+    stream = C.c_void_p(solver.stream())
+    ev0, ev1 = lib.Event(), lib.Event()
+    lib.call("mps_device_sync")
+    stats = []
+    ev0.record(_S(stream))
+    t0 = time.perf_counter()
+    for i in range(steps):
+        stats.append(solver.step(first_step + warmup + i))
+    ev1.record(_S(stream))
+    lib.call("mps_device_sync")
+    wall = time.perf_counter() - t0
+    return ev0.elapsed_ms(ev1), wall, stats
+
+
+class _S:
+    def __init__(self, h):
+        self.handle = h
+
+
+def train_learned(solver_cls, scene, steps_data, device_log):
+    """Generates (state, converged pressure) pairs with the plain solver and trains the
+    MLP on the GPU; returns the parameters (or None if the learned part is absent)."""
+    try:
+        from simulation_project_gb300 import learned
+    except Exception as e:  # pragma: no cover
+        device_log.append(f"learned part unavailable: {e}")
+        return None, {}
+    return learned.train_on_scene(scene, steps=steps_data, log=device_log)
+
+
+def run_gpu(args):
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.solver import Solver
+    lib.load()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    lib.call("mps_set_device", local)
+    scene = build_scene(args.l0, seed=4 + rank)
+    n = scene.n
+    log = []
+    peak_gbs, peak_kind = load_peaks()
+
+    # learned part: data from the plain solver, training on the GPU (untimed)
+    params, train_info = (None, {})
+    if not args.no_learned:
+        params, train_info = train_learned(Solver, scene, args.train_steps, log)
+
+    # plain FP64 Jacobi-CG (metric denominator)
+    plain = Solver(scene, precision="fp64", profile=0)
+    ms_plain, _, st_plain = time_steps(plain, args.steps, args.warmup)
+    plain.close()
+    pps_plain = n * args.steps / (ms_plain / 1e3)
+
+    # learned FP32 / FP64-refined solver (metric numerator), with phase timing
+    fast = Solver(scene, precision="fp32_ir", profile=1, learned=1 if params is not None else 0)
+    if params is not None:
+        fast.set_learned(params)
+    clocks = ClockSampler(local)
+    for i in range(args.warmup):
+        fast.step(i)
+    clocks.start()
+    ms_fast, wall_fast, st_fast = time_steps(fast, args.steps, 0, first_step=args.warmup)
+    clk = clocks.stop()
+    pps_fast = n * args.steps / (ms_fast / 1e3)
+
+    # roofline of the dominant kernel (PPE SpMV, FP32 rows)
+    spmv_ms = sum(s["ms_spmv"] for s in st_fast)
+    spmv_n = sum(s["spmv_launches"] for s in st_fast)
+    nnz = np.mean([s["nnz"] for s in st_fast])
+    interior = np.mean([s["interior"] for s in st_fast])
+    bytes_launch = 8.0 * nnz + 25.0 * interior
+    avg_ms = spmv_ms / max(spmv_n, 1)
+    achieved = bytes_launch / (avg_ms / 1e3) / 1e9 if spmv_n else 0.0
+    roofline = {"bound": "hbm", "kernel": "k_spmv<float,float,float> (PPE SpMV, FP32 rows)",
+                "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+                "frac": round(achieved / peak_gbs, 3), "peak_kind": peak_kind,
+                "traffic": None, "bytes_per_launch": int(bytes_launch), "launches": spmv_n,
+                "avg_launch_us": round(avg_ms * 1e3, 2)}
+    phases = {k: round(float(np.mean([s[k] for s in st_fast])), 3) for k in
+              ("ms_grid", "ms_walls", "ms_predictor", "ms_list", "ms_ppe_setup", "ms_spmv", "ms_cg_vec",
+               "ms_correct", "ms_learned")}
+
+    # end to end through the C-ABI from pinned host buffers
+    e2e = run_e2e(fast, args)
+    fast.close()
+
+    result = {
+        "metric": "particle-steps/s @1M on 1 GB300, learned-precond vs plain CG at 1e-8 PPE residual",
+        "value": pps_fast * world,
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_fast / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded jittered lattice in a triangulated rotating cylinder)",
+        "config": {"workload": f"rotating bucket r=0.15 L=0.3, 35% fill, l0={args.l0}, 30 rpm, 4096 wall + "
+                               "64 drag-sphere STL models, dt=5e-5, PPE rtol 1e-8",
+                   "particles": n, "triangles": scene.t, "cells": scene.box.cell_num,
+                   "l2": "inputs larger than L2 (neighbour rows ~8 B x nnz per SpMV)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "plain_fp64": {"value": pps_plain, "ms_per_step": ms_plain / args.steps,
+                       "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_plain])),
+                       "relres_max": float(max(s["cg_relres"] for s in st_plain))},
+        "speedup_vs_plain_fp64": pps_fast / pps_plain,
+        "fast_solver": {"cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_fast])),
+                        "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_fast])),
+                        "relres_max": float(max(s["cg_relres"] for s in st_fast)),
+                        "fallbacks": int(sum(s["fallback"] for s in st_fast)),
+                        "error_flags": int(np.bitwise_or.reduce([s["error_flags"] for s in st_fast])),
+                        "learned": params is not None, "phases_ms": phases},
+        "learned_training": train_info,
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": int(sum(s["spmv_launches"] for s in st_fast) * 3 + args.steps * 40),
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1:
+        result["cpu_baseline"] = cpu_baseline(args)
+    if log:
+        result["notes"] = log
+    return result
+
+
+def run_e2e(solver, args):
+    from simulation_project_gb300 import lib
+    n = solver.state(sort_by_id=False)["pos"].shape[0]
+    # pinned host buffers
+    bufs = []
+    for shape in ((n, 3), (n, 3), (n,)):
+        p = C.c_void_p()
+        nbytes = int(np.prod(shape)) * 8
+        lib.call("mps_host_alloc_pinned", C.byref(p), nbytes)
+        arr = np.ctypeslib.as_array((C.c_double * int(np.prod(shape))).from_address(p.value)).reshape(shape)
+        bufs.append((p, arr))
+    pos, vel, press = (b[1] for b in bufs)
+    solver.download_state(pos, vel, press)
+    steps = max(2, args.steps // 2)
+    lib.call("mps_device_sync")
+    t0 = time.perf_counter()
+    for i in range(steps):
+        solver.upload_state(pos, vel, press)
+        solver.step(1000 + i)
+        solver.download_state(pos, vel, press)
+    dt = time.perf_counter() - t0
+    for p, _ in bufs:
+        lib.call("mps_host_free_pinned", p)
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 56,
+            "d2h_bytes_per_step": n * 56, "steps": steps}
+
+
+def cpu_baseline(args):
+    """The FP64 oracle solver (OpenMP) on a bounded sample: the same bucket at
+    l0 = 0.004 for one step after one warm-up step."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import orc
+    sc = build_scene(0.004)
+    sim = orc.OracleSim(sc)
+    sim.step(0)
+    t0 = time.perf_counter()
+    sim.step(1)
+    dt = time.perf_counter() - t0
+    sim.close()
+    return {"value": sc.n / dt, "unit": "particle-steps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"FP64 oracle PPE step (OpenMP) on the bucket at l0=0.004 ({sc.n} particles), 1 step"}
+
+
+def run_reference(args):
+    """The reference's explicit-schedule kernels compiled for the CPU (oracle/_ref)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import orc
+    ref = orc.reference()
+    kind = "reference"
+    if ref is None:
+        ref = orc.oracle()
+        kind = "port"
+    sc = build_scene(0.004)
+    sc.param.bExplicitPressure = True
+    sc.param.SonicVelocity = 20.0
+    st = orc.RefState(sc)
+    b = st.bindings()
+
+    def one_step(i):
+        n = C.c_int(st.n)
+        if hasattr(ref, "check_outside_compute_zone"):
+            ref.check_outside_compute_zone(C.byref(b), C.byref(n))
+        orc.ref_topology(ref, st, b)
+        ref.reset_triangle_topology(st.cells_n, orc.ptr(st.cells))
+        ref.register_triangle_topology(C.byref(b), orc.ptr(st.triangles), st.t, orc.ptr(st.cells), st.cells_n)
+        ref.calc_stl_distance(C.byref(b), st.n)
+        if st.drag_num:
+            ref.calc_drag_effect(C.byref(b), st.n)
+        ref.calc_explicitly(C.byref(b), st.n)
+        orc.ref_topology(ref, st, b)
+        ref.calc_stl_distance(C.byref(b), st.n)
+        ref.calc_explicit_pressure(C.byref(b), st.n)
+        ref.calc_explicit_pressure_gradient(C.byref(b), st.n)
+        ref.update_triangle_position(C.byref(b), st.t)
+        ref.rotate_triangle_position(C.byref(b), st.t, i)
+
+    for i in range(args.warmup):
+        one_step(i)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        one_step(args.warmup + i)
+    dt = time.perf_counter() - t0
+    v = st.n * args.steps / dt
+    return {"impl": "reference", "metric": "particle-steps/s @1M on 1 GB300, learned-precond vs plain CG at 1e-8 "
+            "PPE residual", "value": v, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "rotating bucket r=0.15 L=0.3, 35% fill, 30 rpm, 4096 wall + 64 drag-sphere STL "
+                                   "models; bounded sample at l0=0.004", "particles": st.n},
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": _threads(), "kind": kind,
+                             "sample": f"reference explicit schedule (EOS pressure, its own kernels on the CPU) "
+                                       f"on the bucket at l0=0.004 ({st.n} particles) per step"},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def _threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--l0", type=float, default=0.002)
+    ap.add_argument("--train-steps", type=int, default=6)
+    ap.add_argument("--no-learned", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)))
+        return 0
+    res = run_gpu(args)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        vals = [None] * world
+        dist.all_gather_object(vals, (res["value"] / world, res["ms_per_step"]))
+        res["value"] = sum(v for v, _ in vals)
+        res["ms_per_step"] = max(m for _, m in vals)
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(res))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

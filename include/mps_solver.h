@@ -52,6 +52,8 @@ typedef struct MpsSolverOptions {
     int ir_max_outer;       /* refinement pass cap */
     int max_neighbours;     /* capacity of a Laplacian neighbour row */
     int check_every;        /* CG convergence is read back every this many iterations */
+    double source_relaxation; /* gamma in b = gamma rho/dt^2 (n* - n0)/n0 (Tanaka & Masunaga 2010) */
+    int profile;            /* 1: time every phase with CUDA events on the solver stream */
 } MpsSolverOptions;
 
 typedef struct MpsStepStats {
@@ -64,6 +66,11 @@ typedef struct MpsStepStats {
     double cg_relres;       /* final FP64 relative residual */
     double b_norm;
     unsigned error_flags;   /* MPS_ERR_* bits seen during the step */
+    long long nnz;          /* Laplacian neighbour entries of interior rows (PPE matrix) */
+    long long pairs;        /* Laplacian neighbour entries of all rows */
+    /* phase times [ms] and launch counts (profile = 1 only) */
+    float ms_grid, ms_walls, ms_predictor, ms_list, ms_ppe_setup, ms_spmv, ms_cg_vec, ms_correct, ms_learned;
+    int spmv_launches;
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);
@@ -91,6 +98,11 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);
 /* Pressure read back to a host buffer, in the solver's order (e2e output). */
 CCTStatusType mps_solver_copy_pressure(MpsSolver* s, double* host_press);
+/* Replace the particle state (n entries, in the solver's current order, e.g. as
+ * returned by mps_solver_download_state) from host arrays: pos/vel n*3, press n.
+ * Pinned host memory makes the copies asynchronous DMA. */
+CCTStatusType mps_solver_upload_state(MpsSolver* s, const double* pos, const double* vel, const double* press);
+CCTStatusType mps_solver_download_state(MpsSolver* s, double* pos, double* vel, double* press);
 /* Stream the solver launches on (cudaStream_t), for event timing by the caller. */
 CCTStatusType mps_solver_stream(MpsSolver* s, void** stream);
 

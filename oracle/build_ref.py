@@ -71,7 +71,8 @@ def build_ref(verbose: bool = False):
     harness = os.path.join(HERE, "ref_harness.cpp")
     deps = [harness] + [os.path.join(src_dir, n) for n in REF_FILES]
     if _stale(out, deps):
-        cmd = ["g++"] + CXXFLAGS + ["-w", "-I" + os.path.join(HERE, "ref_shim"), "-I" + src_dir, harness, "-o", out]
+        cmd = ["g++"] + CXXFLAGS + ["-fopenmp", "-w", "-I" + os.path.join(HERE, "ref_shim"), "-I" + src_dir, harness,
+                                    "-o", out]
         if verbose:
             print(" ".join(cmd))
         subprocess.check_call(cmd)

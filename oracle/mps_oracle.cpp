@@ -21,7 +21,11 @@
  * rounding.
  *
  * Part 2 (OrcSim, double): the semi-implicit step with a pressure Poisson
- * equation and Jacobi-preconditioned CG.  The reference declares but never
+ * equation and Jacobi-preconditioned CG.  Its source term carries a relaxation
+ * coefficient gamma (quasi-compressible MPS, Tanaka & Masunaga, J. Comput. Phys.
+ * 229 (2010) 4279-4290): b = gamma rho/dt^2 (n* - n0)/n0, and drag models act on
+ * the fluid only through the drag term (they are not walls here; the reference's
+ * wall-distance kernel has that filter commented out, DeviceProcess_Kernel.h:897-900).  The reference declares but never
  * defines a PPE solver (S/CGPUCellSet.h:218-240 declarations only), so this part
  * is the specification the GPU FP64 path is checked against; it has no
  * reference counterpart to pin to.
@@ -936,8 +940,8 @@ struct OrcSim {
     std::vector<int> wid;
     std::vector<D3> dragv;
     /* last PPE (sorted order) */
-    std::vector<double> l_pnd, l_diag, l_rhs, l_sol;
-    std::vector<int> l_sid;
+    std::vector<double> l_pnd, l_diag, l_rhs, l_sol, l_idsum;
+    std::vector<int> l_sid, l_cnt, l_id;
 
     double l0() const { return cfg.param.InitialParticleDistance; }
     double re_lap() const { return (double)cfg.param.LaplacianInfluenceRadiusCoefficient * l0(); }
@@ -1055,7 +1059,7 @@ struct OrcSim {
                     if (m < 0 || m >= cells) continue;
                     for (int l = tcell_start[m]; l < tcell_start[m + 1]; ++l) {
                         const int t = tcell_ids[l];
-                        if (drag_only && !tparams[tris[t].model].isDrag) continue;
+                        if (drag_only != (bool)tparams[tris[t].model].isDrag) continue;
                         if (t == mid) continue;
                         const D3 q = closest_on_triangle(p, tris[t].v[0], tris[t].v[1], tris[t].v[2]);
                         const D3 dv = dsub(p, q);
@@ -1186,7 +1190,7 @@ struct OrcSim {
             double sw = 0.0;
             for (auto& e : nb[s]) sw += e.second;
             diag[s] = c * sw + kappa;
-            rhs[s] = rho / (dt * dt) * (npnd[s] - cfg.n0_pnd) / cfg.n0_pnd;
+            rhs[s] = cfg.source_relaxation * rho / (dt * dt) * (npnd[s] - cfg.n0_pnd) / cfg.n0_pnd;
             x[s] = spress[s];
         }
         auto spmv = [&](const std::vector<double>& in, std::vector<double>& out) {
@@ -1233,6 +1237,14 @@ struct OrcSim {
         for (int s = 0; s < n; ++s) spress[s] = inner[s] ? x[s] : 0.0;
         for (int s = 0; s < n; ++s) { press[sid[s]] = spress[s]; pnd[sid[s]] = npnd[s]; }
         l_pnd = npnd; l_diag = diag; l_rhs = rhs; l_sol = spress; l_sid = sid;
+        l_cnt.resize(n); l_idsum.resize(n); l_id.resize(n);
+        for (int s = 0; s < n; ++s) {
+            double acc = 0.0;
+            for (auto& e : nb[s]) acc += (double)id[sid[e.first]];
+            l_cnt[s] = (int)nb[s].size();
+            l_idsum[s] = acc;
+            l_id[s] = id[sid[s]];
+        }
         if (st) {
             st->cg_iterations = it;
             st->cg_relres = bnorm > 0 ? rnorm / bnorm : 0.0;
@@ -1415,6 +1427,23 @@ int orc_sim_get_triangles(OrcSim* s, double* v) {
             v[9 * i + 3 * q + 2] = s->tris[i].v[q].z;
         }
     return CCT_NOERR;
+}
+
+int orc_sim_get_ids(OrcSim* s, int* ids) {
+    for (int i = 0; i < s->n; ++i) ids[i] = s->id[i];
+    return s->n;
+}
+
+/* Laplacian neighbour count and sum of neighbour particle ids of the last PPE, and
+ * the particle id, per sorted position. */
+int orc_sim_last_nbr(OrcSim* s, int* cnt, double* idsum, int* pid) {
+    const size_t n = s->l_cnt.size();
+    for (size_t i = 0; i < n; ++i) {
+        cnt[i] = s->l_cnt[i];
+        idsum[i] = s->l_idsum[i];
+        pid[i] = s->l_id[i];
+    }
+    return (int)n;
 }
 
 int orc_sim_last_ppe(OrcSim* s, double* pnd, double* diag, double* rhs, double* sol, int* sorted_id) {

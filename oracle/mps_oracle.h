@@ -115,6 +115,7 @@ typedef struct OrcSimConfig {
     double cg_rtol;
     int cg_max_iter;
     int threads;         /* OpenMP threads (0 = library default) */
+    double source_relaxation;  /* gamma of the PND source term */
 } OrcSimConfig;
 
 typedef struct OrcStepStats {
@@ -136,6 +137,8 @@ int orc_sim_set_drag(OrcSim* s, int count, const DragParameter* params);
 int orc_sim_step(OrcSim* s, int step, OrcStepStats* stats);
 int orc_sim_get(OrcSim* s, int* n, double* pos, double* vel, double* pressure, double* pnd);
 int orc_sim_get_triangles(OrcSim* s, double* vertices);
+int orc_sim_get_ids(OrcSim* s, int* ids);
+int orc_sim_last_nbr(OrcSim* s, int* cnt, double* idsum, int* pid);
 /* One PPE solve on the current state's sorted arrays (for operator tests):
  * writes the per-particle PND, diagonal, rhs and solution in sorted order. */
 int orc_sim_last_ppe(OrcSim* s, double* pnd, double* diag, double* rhs, double* sol, int* sorted_id);

@@ -30,7 +30,7 @@
 #include "cuda_runtime.h"
 
 struct HarnessDim3 { unsigned x, y, z; };
-static HarnessDim3 blockIdx, threadIdx, blockDim, gridDim;
+static thread_local HarnessDim3 blockIdx, threadIdx, blockDim, gridDim;
 #define __global__
 #define __constant__ static
 #define __shared__
@@ -139,9 +139,21 @@ static void bind(const HarnessBindings* b) {
     c_daMagnifierCount = b->magnifier_count;
 }
 
-/* Run a one-thread-per-item kernel serially: block size 1, block index = item. */
+/* Run a one-thread-per-item kernel: block size 1, block index = item.  Items are
+ * independent in every kernel run this way, so they are spread over OpenMP threads
+ * (the CUDA index variables above are thread-local). */
 template <class K>
 static void run_items(int n, K k) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < n; ++i) {
+        blockDim.x = 1;
+        threadIdx.x = 0;
+        blockIdx.x = (unsigned)i;
+        k();
+    }
+}
+template <class K>
+static void run_items_serial(int n, K k) {
     blockDim.x = 1;
     threadIdx.x = 0;
     for (int i = 0; i < n; ++i) {
@@ -203,7 +215,7 @@ int orc_reset_triangle_topology(int cells, CCell* cell) {
 
 int orc_register_triangle_topology(HarnessBindings* b, const CTriangle* tri, int t, CCell* cell, int cells) {
     bind(b);
-    run_items(t, [&] { RegisterTriangleTopology_Kernel(tri, t, cell, cells); });
+    run_items_serial(t, [&] { RegisterTriangleTopology_Kernel(tri, t, cell, cells); });
     return CCT_NOERR;
 }
 

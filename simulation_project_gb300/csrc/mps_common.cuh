@@ -18,6 +18,14 @@ namespace mps {
 
 constexpr int kBlock = 256;
 
+// 32-byte aligned double4 (one 256-bit access) for the FP64 particle state
+typedef double4_32a dbl4;
+__host__ __device__ __forceinline__ dbl4 make_dbl4(double x, double y, double z, double w) {
+    dbl4 t;
+    t.x = x; t.y = y; t.z = z; t.w = w;
+    return t;
+}
+
 __host__ __device__ inline int div_up(long long a, int b) { return (int)((a + b - 1) / b); }
 
 // ---------------------------------------------------------------------------

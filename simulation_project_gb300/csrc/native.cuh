@@ -1,7 +1,7 @@
 // native.cuh - data layout and kernel declarations of the GB300-native solver.
 //
 // Layout in HBM (all arrays indexed by the current cell-sorted particle order):
-//   pos, vel        double4  (x, y, z, unused)   FP64 master state, 32 B each
+//   pos, vel        dbl4  (x, y, z, unused)   FP64 master state, 32 B each
 //   opos, ovel      float4                        FP32 operator copies (FP32 mode)
 //   press           double                        pressure (PPE solution)
 //   visc            float, type int, id int       carried per particle
@@ -27,7 +27,7 @@ struct Consts {
     double c1;            // 2d / n0_pnd
     double c2;            // rho / dt^2
     double vmax;          // l0 * Courant / dt
-    double wall_fric, offset_l0, tol, sonic2;
+    double wall_fric, offset_l0, tol, sonic2, gamma;
     double g[3];
     int dim;
     int explicit_pressure;
@@ -37,11 +37,11 @@ struct Dev {
     int n, cells, K, KG, tri_n, drag_n;
     CGridBox box;
     Consts c;
-    double4 *pos, *vel;
+    dbl4 *pos, *vel;
     double* press;
     float* visc;
     int *type, *id;
-    double4 *pos2, *vel2;
+    dbl4 *pos2, *vel2;
     double* press2;
     float* visc2;
     int *type2, *id2;
@@ -79,7 +79,7 @@ struct Dev {
     double* scal;              // device scalars
     unsigned* red_count;       // last-block counters
     unsigned* err;
-    int* nbr_idsum_cnt;        // debug
+    int* istat;                // [0] longest neighbour row
 };
 
 // device scalar slots

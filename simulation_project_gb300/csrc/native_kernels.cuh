@@ -79,7 +79,7 @@ __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* red, unsign
 __global__ void k_zone_flags(const __grid_constant__ Dev d, unsigned* keep) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
-    const double4 p = d.pos[i];
+    const dbl4 p = d.pos[i];
     keep[i] = in_zone<double>(d.box, p.x, p.y, p.z, d.c.tol) ? 1u : 0u;
 }
 
@@ -99,7 +99,7 @@ __global__ void k_compact(const __grid_constant__ Dev d, const unsigned* keep, c
 __global__ void k_hash(const __grid_constant__ Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
-    const double4 p = d.pos[i];
+    const dbl4 p = d.pos[i];
     const double cs = d.box.m_CellSize;
     const int a = f2i((p.x - (double)d.box.m_BufferedZone.m_MinBound.x) / cs);
     const int b = f2i((p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
@@ -118,7 +118,7 @@ __global__ void k_gather(const __grid_constant__ Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const int s = d.idx[i];
-    const double4 p = d.pos[s], v = d.vel[s];
+    const dbl4 p = d.pos[s], v = d.vel[s];
     d.pos2[i] = p;
     d.vel2[i] = v;
     d.press2[i] = d.press[s];
@@ -245,7 +245,7 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
                 const int e = d.tcs[d.cells + m];
                 for (int l = s; l < e; ++l) {
                     const int t = d.tids[l];
-                    if (drag_only && !d.tparams[d.tmodel[t]].isDrag) continue;
+                    if (drag_only != (bool)d.tparams[d.tmodel[t]].isDrag) continue;
                     if (t == mid) continue;
                     const double* v = d.tri + 9 * (size_t)t;
                     const V3<T> q = closest_on_tri<T>(p, v3<T>((T)v[0], (T)v[1], (T)v[2]), v3<T>((T)v[3], (T)v[4], (T)v[5]),
@@ -264,7 +264,7 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
 template <class T>
 __device__ __forceinline__ V3<T> load_p(const Dev& d, int i) {
     if constexpr (sizeof(T) == 8) {
-        const double4 p = d.pos[i];
+        const dbl4 p = d.pos[i];
         return v3<T>(p.x, p.y, p.z);
     } else {
         const float4 p = d.opos[i];
@@ -274,7 +274,7 @@ __device__ __forceinline__ V3<T> load_p(const Dev& d, int i) {
 template <class T>
 __device__ __forceinline__ V3<T> load_v(const Dev& d, int i) {
     if constexpr (sizeof(T) == 8) {
-        const double4 p = d.vel[i];
+        const dbl4 p = d.vel[i];
         return v3<T>(p.x, p.y, p.z);
     } else {
         const float4 p = d.ovel[i];
@@ -313,7 +313,7 @@ __global__ void k_drag(const __grid_constant__ Dev d) {
     if (mid >= 0) {
         const DragParameter dp = d.drag[d.tparams[d.tmodel[mid]].DragTriangleID];
         if ((double)md <= (double)dp.CoefficientofInflueneRegion * d.c.l0) {
-            double4 v = d.vel[i];
+            dbl4 v = d.vel[i];
             if (dp.DragToken == 'E' && (dp.InputVelocityToken1 == 'V' || dp.InputVelocityToken1 == 'B')) {
                 const double sv = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
                 const double pr = (double)dp.VelocityIndex * pow(sv, (double)dp.VelocityExponential);
@@ -404,7 +404,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         const float4 pf = d.opos[i];
         const V3<T> pi = load_p<T>(d, i);
         const V3<T> vi = load_v<T>(d, i);
-        T a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;   // mode-specific accumulators
+        T a0 = 0, a1 = 0, a2 = 0, a3 = 0;   // mode-specific accumulators
+        double aid = 0.0;                   // neighbour id checksum (FP64, exact for ids < 2^53/K)
         int cnt = 0, gcnt = 0;
         for (int r = 0; r < 9; ++r) {
             const int len = rl[r];
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     if constexpr (sizeof(T) == 8) {
                         const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
                         if (dxf * dxf + dyf * dyf + dzf * dzf < re2f) {
-                            const double4 pj = d.pos[j];
+                            const dbl4 pj = d.pos[j];
                             const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
                             const double rd = exact_r(dx, dy, dz);
                             if (rd < re) {
@@ -447,7 +448,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     if constexpr (MODE == NB_PREDICT) {
                         V3<T> vj;
                         if constexpr (sizeof(T) == 8) {
-                            const double4 v = d.vel[j];
+                            const dbl4 v = d.vel[j];
                             vj = v3<T>(v.x, v.y, v.z);
                         } else {
                             vj = v3<T>(vj4.x, vj4.y, vj4.z);
@@ -463,7 +464,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                         }
                         a0 += w;                                   // sum of Laplacian weights
                         a1 += (T)d.press[j];                       // neighbour pressure (feature)
-                        a4 += (T)d.id[j];                          // id checksum (debug)
+                        aid += (double)d.id[j];                    // id checksum (debug)
                         if (rr < reg) {
                             gacc = true;
                             const T rg = rr > mindg ? rr : mindg;
@@ -495,7 +496,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
             a1 += __shfl_down_sync(0xffffffffu, a1, o);
             a2 += __shfl_down_sync(0xffffffffu, a2, o);
             a3 += __shfl_down_sync(0xffffffffu, a3, o);
-            a4 += __shfl_down_sync(0xffffffffu, a4, o);
+            aid += __shfl_down_sync(0xffffffffu, aid, o);
         }
         if (lane != 0) continue;
         if constexpr (MODE == NB_PREDICT) {
@@ -511,10 +512,10 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 lz += ((double)vw.z - (double)vi.z) * d.c.wall_fric * ww;
             }
             const double cf = d.c.coef_lap * (double)d.visc[i];
-            const double4 v = d.vel[i];
-            const double4 p = d.pos[i];
+            const dbl4 v = d.vel[i];
+            const dbl4 p = d.pos[i];
             const double dt = d.c.dt;
-            double4 vn, pn;
+            dbl4 vn, pn;
             vn.x = v.x + (d.c.g[0] + lx * cf) * dt - d.dragv[3 * (size_t)i];
             vn.y = v.y + (d.c.g[1] + ly * cf) * dt - d.dragv[3 * (size_t)i + 1];
             vn.z = v.z + (d.c.g[2] + lz * cf) * dt - d.dragv[3 * (size_t)i + 2];
@@ -532,6 +533,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
             d.pos2[i] = pn;
         } else {
             if (cnt > d.K || gcnt > d.KG) atomicOr(d.err, MPS_ERR_NEIGHBOUR_CAP);
+            atomicMax(d.istat, cnt);
             d.nbr_cnt[i] = cnt < d.K ? cnt : d.K;
             d.gcnt[i] = gcnt < d.KG ? gcnt : d.KG;
             double pnd = (double)a2;
@@ -543,7 +545,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
             d.feat_aux[4 * (size_t)i] = cnt > 0 ? (double)a1 / cnt : 0.0;
             d.feat_aux[4 * (size_t)i + 1] = (double)a3 * (double)d.c.dim / d.c.n0_pnd;
             d.feat_aux[4 * (size_t)i + 2] = (double)cnt;
-            d.feat_aux[4 * (size_t)i + 3] = (double)a4;
+            d.feat_aux[4 * (size_t)i + 3] = aid;
         }
     }
 }
@@ -560,7 +562,7 @@ __global__ void k_ppe_setup(const __grid_constant__ Dev d) {
     if (in) {
         const double dg = d.c.coef_lap * d.sumw[i] + d.c.kappa;
         d.diag[i] = dg;
-        d.rhs[i] = d.c.rho / (d.c.dt * d.c.dt) * (pnd - d.c.n0_pnd) / d.c.n0_pnd;
+        d.rhs[i] = d.c.gamma * d.c.rho / (d.c.dt * d.c.dt) * (pnd - d.c.n0_pnd) / d.c.n0_pnd;
         d.minv[i] = 1.0 / dg;
     } else {
         d.diag[i] = 1.0;
@@ -703,6 +705,38 @@ __global__ void k_cg_p(const __grid_constant__ Dev d, TV* p, const TV* z) {
         p[i] = (TV)((double)z[i] + beta * (double)p[i]);
 }
 
+// neighbour-entry counts: interior rows (PPE matrix) and all rows
+__global__ void __launch_bounds__(256) k_count_nnz(const __grid_constant__ Dev d, int slot) {
+    double a = 0.0, b = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        const double c = (double)d.nbr_cnt[i];
+        b += c;
+        if (d.inner[i]) a += c;
+    }
+    double v[2] = {a, b}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        d.scal[S_TMP0] = out[0];
+        d.scal[S_TMP1] = out[1];
+    }
+}
+
+// host state exchange (SoA doubles <-> packed device state)
+__global__ void k_pack_state(const __grid_constant__ Dev d, const double* p3, const double* v3, const double* pr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    d.pos[i] = make_dbl4(p3[3 * (size_t)i], p3[3 * (size_t)i + 1], p3[3 * (size_t)i + 2], 0.0);
+    d.vel[i] = make_dbl4(v3[3 * (size_t)i], v3[3 * (size_t)i + 1], v3[3 * (size_t)i + 2], 0.0);
+    d.press[i] = pr[i];
+}
+__global__ void k_unpack_state(const __grid_constant__ Dev d, double* p3, double* v3, double* pr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const dbl4 p = d.pos[i], v = d.vel[i];
+    p3[3 * (size_t)i] = p.x; p3[3 * (size_t)i + 1] = p.y; p3[3 * (size_t)i + 2] = p.z;
+    v3[3 * (size_t)i] = v.x; v3[3 * (size_t)i + 1] = v.y; v3[3 * (size_t)i + 2] = v.z;
+    pr[i] = d.press[i];
+}
+
 __global__ void k_to_float(int n, const double* a, float* b) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) b[i] = (float)a[i];
@@ -751,10 +785,10 @@ __global__ void k_correct(const __grid_constant__ Dev d) {
             for (int a = 0; a < 3; ++a) g[a] -= mc * dir[a];
         }
     }
-    const double4 v = d.vel[i];
-    const double4 p = d.pos[i];
+    const dbl4 v = d.vel[i];
+    const dbl4 p = d.pos[i];
     const double c3 = -d.c.dt / d.c.rho;
-    double4 vn = make_double4(v.x + c3 * g[0], v.y + c3 * g[1], v.z + c3 * g[2], 0.0);
+    dbl4 vn = make_dbl4(v.x + c3 * g[0], v.y + c3 * g[1], v.z + c3 * g[2], 0.0);
     const double a = sqrt(vn.x * vn.x + vn.y * vn.y + vn.z * vn.z);
     if (a > d.c.vmax) {
         const double s = d.c.vmax / a;
@@ -765,7 +799,7 @@ __global__ void k_correct(const __grid_constant__ Dev d) {
         vn = v;
     }
     d.vel2[i] = vn;
-    d.pos2[i] = make_double4(p.x + (vn.x - v.x) * d.c.dt, p.y + (vn.y - v.y) * d.c.dt, p.z + (vn.z - v.z) * d.c.dt, 0.0);
+    d.pos2[i] = make_dbl4(p.x + (vn.x - v.x) * d.c.dt, p.y + (vn.y - v.y) * d.c.dt, p.z + (vn.z - v.z) * d.c.dt, 0.0);
 }
 
 // Wall motion: translation + incremental rotation with linear ramp, FP64, exactly

@@ -40,6 +40,41 @@ struct DevBuf {
 
 inline int blocks_for(int n, int threads = kBlock) { return std::max(1, div_up(n, threads)); }
 
+enum Phase { PH_GRID = 0, PH_WALLS, PH_PRED, PH_LIST, PH_SETUP, PH_SPMV, PH_VEC, PH_CORRECT, PH_LEARNED, PH_OTHER, PH_COUNT };
+
+// CUDA events on the solver stream at phase boundaries; the interval between two
+// consecutive marks is attributed to the first mark's phase.
+struct PhaseTimer {
+    std::vector<cudaEvent_t> pool;
+    std::vector<int> cat;
+    size_t used = 0;
+    bool on = false;
+    void mark(int c, cudaStream_t st) {
+        if (!on) return;
+        if (used == pool.size()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            pool.push_back(e);
+            cat.push_back(0);
+        }
+        cat[used] = c;
+        cudaEventRecord(pool[used], st);
+        ++used;
+    }
+    void collect(float* ms) {
+        for (size_t k = 0; k + 1 < used; ++k) {
+            float t = 0.f;
+            cudaEventElapsedTime(&t, pool[k], pool[k + 1]);
+            ms[cat[k]] += t;
+        }
+        used = 0;
+    }
+    void release() {
+        for (auto e : pool) cudaEventDestroy(e);
+        pool.clear();
+    }
+};
+
 }  // namespace
 
 struct Solver {
@@ -64,6 +99,9 @@ struct Solver {
     void* bin_sort = nullptr;
     size_t bin_sort_bytes = 0;
     MpsStepStats last{};
+    PhaseTimer timer;
+    int spmv_launches = 0;
+    double* stage = nullptr;   // host-exchange staging (7 n doubles)
     // learned parameters (optional)
     bool learned_ready = false;
 
@@ -108,10 +146,12 @@ struct Solver {
         c.offset_l0 = c.l0 * (double)P.OffSet;
         c.tol = P.Tolerance;
         c.sonic2 = (double)P.SonicVelocity * (double)P.SonicVelocity;
+        c.gamma = opt.source_relaxation > 0 ? opt.source_relaxation : 1.0;
         c.g[0] = P.GravityConstant.x;
         c.g[1] = P.GravityConstant.y;
         c.g[2] = P.GravityConstant.z;
         c.explicit_pressure = opt.pressure_mode == MPS_PRESSURE_EXPLICIT;
+        timer.on = opt.profile != 0;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CCT_CUDAERR;
         const size_t N = nmax;
         const size_t wsz = fp64() ? sizeof(double) : sizeof(float);
@@ -141,6 +181,8 @@ struct Solver {
         e = e ? e : mk(&d.scal, (size_t)S_COUNT);
         e = e ? e : mk(&d.red_count, 16);
         e = e ? e : mk(&d.err, 1);
+        e = e ? e : mk(&d.istat, 4);
+        e = e ? e : mk(&stage, 7 * N);
         e = e ? e : mk(&keep, N + 1);
         e = e ? e : mk(&rank, N + 1);
         if (e != cudaSuccess) return CCT_MEMERR;
@@ -169,6 +211,7 @@ struct Solver {
         if (d.drag) cudaFree(d.drag);
         if (h_scal) cudaFreeHost(h_scal);
         if (h_int) cudaFreeHost(h_int);
+        timer.release();
         if (st) cudaStreamDestroy(st);
     }
 
@@ -184,21 +227,21 @@ struct Solver {
     CCTStatusType set_particles(int n, const double* pos, const double* vel, const double* press, const double* visc,
                                 const int* type) {
         if (n < 0 || n > nmax) return CCT_PARAMERR;
-        std::vector<double4> P(n), V(n);
+        std::vector<dbl4> P(n), V(n);
         std::vector<double> pr(n, 0.0);
         std::vector<float> vi(n);
         std::vector<int> ty(n, 0), id(n);
         for (int i = 0; i < n; ++i) {
-            P[i] = make_double4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
-            V[i] = make_double4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
+            P[i] = make_dbl4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0);
+            V[i] = make_dbl4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.0);
             if (press) pr[i] = press[i];
             vi[i] = (float)visc[i];
             if (type) ty[i] = type[i];
             id[i] = i;
         }
         d.n = n;
-        cudaError_t e = cudaMemcpyAsync(d.pos, P.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, st);
-        if (!e) e = cudaMemcpyAsync(d.vel, V.data(), sizeof(double4) * n, cudaMemcpyHostToDevice, st);
+        cudaError_t e = cudaMemcpyAsync(d.pos, P.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(d.vel, V.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.press, pr.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.visc, vi.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.type, ty.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
@@ -322,48 +365,77 @@ struct Solver {
     template <class T>
     CCTStatusType run_step(int step, MpsStepStats* out) {
         MpsStepStats S{};
+        spmv_launches = 0;
+        timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
+        cudaMemsetAsync(d.istat, 0, sizeof(int), st);
         CCTStatusType rc;
         if ((rc = compact())) return rc;
         if ((rc = grid())) return rc;
+        timer.mark(PH_WALLS, st);
         if (d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
         walls_distance<T>();
         if (d.drag_n > 0 && d.tri_n > 0) k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
         else cudaMemsetAsync(d.dragv, 0, sizeof(double) * 3 * d.n, st);
+        timer.mark(PH_PRED, st);
         const int nb_grid = std::max(1, std::min(d.cells, d.n));
         k_neighbours<T, NB_PREDICT><<<nb_grid, kNbThreads, 0, st>>>(d);
         std::swap(d.pos, d.pos2);
         std::swap(d.vel, d.vel2);
+        timer.mark(PH_GRID, st);
         if ((rc = compact())) return rc;
         if ((rc = grid())) return rc;
+        timer.mark(PH_WALLS, st);
         walls_distance<T>();
+        timer.mark(PH_LIST, st);
         k_neighbours<T, NB_LIST><<<std::max(1, std::min(d.cells, d.n)), kNbThreads, 0, st>>>(d);
+        timer.mark(PH_SETUP, st);
         if (opt.pressure_mode == MPS_PRESSURE_EXPLICIT) {
             k_eos<<<blocks_for(d.n), kBlock, 0, st>>>(d);
         } else {
             k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
         }
+        timer.mark(PH_CORRECT, st);
         k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
         std::swap(d.pos, d.pos2);
         std::swap(d.vel, d.vel2);
+        timer.mark(PH_WALLS, st);
         if (d.tri_n > 0 && walls_move) {
             k_walls_move<<<blocks_for(d.tri_n), kBlock, 0, st>>>(d, step);
             bins_dirty = 1;
         }
+        timer.mark(PH_OTHER, st);
         cudaMemcpyAsync(h_int, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(h_int + 1, d.istat, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
-        S.error_flags = (unsigned)h_int[0];
+        S.error_flags |= (unsigned)h_int[0];
+        S.max_row = h_int[1];
         S.particles = d.n;
+        if (opt.pressure_mode != MPS_PRESSURE_EXPLICIT) {
+            S.nnz = (long long)h_nnz[0];
+            S.pairs = (long long)h_nnz[1];
+        }
+        if (timer.on) {
+            float ms[PH_COUNT] = {0};
+            timer.collect(ms);
+            S.ms_grid = ms[PH_GRID]; S.ms_walls = ms[PH_WALLS]; S.ms_predictor = ms[PH_PRED];
+            S.ms_list = ms[PH_LIST]; S.ms_ppe_setup = ms[PH_SETUP]; S.ms_spmv = ms[PH_SPMV];
+            S.ms_cg_vec = ms[PH_VEC]; S.ms_correct = ms[PH_CORRECT]; S.ms_learned = ms[PH_LEARNED];
+            S.spmv_launches = spmv_launches;
+        }
         last = S;
         if (out) *out = S;
         return CCT_NOERR;
     }
 
+    double h_nnz[2] = {0, 0};
     // read the device scalars
     CCTStatusType pull_scal() {
         cudaMemcpyAsync(h_scal, d.scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st);
-        return cudaStreamSynchronize(st) == cudaSuccess ? CCT_NOERR : CCT_CUDAERR;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
+        return CCT_NOERR;
     }
 
     template <class TW, class TV, class TXA>
@@ -372,9 +444,12 @@ struct Solver {
         int done = 0;
         while (done < maxit + every) {
             for (int k = 0; k < every; ++k) {
+                timer.mark(PH_SPMV, st);
                 k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+                timer.mark(PH_VEC, st);
                 k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1);
                 k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
+                ++spmv_launches;
             }
             done += every;
             if (pull_scal()) return -1;
@@ -388,6 +463,8 @@ struct Solver {
         const double* w = (const double*)d.nbrw;
         k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
         if (pull_scal()) return CCT_CUDAERR;
+        h_nnz[0] = h_scal[S_TMP0];
+        h_nnz[1] = h_scal[S_TMP1];
         const double bnorm = h_scal[S_BNORM];
         const double tol = opt.cg_rtol * bnorm;
         k_cg_start<double><<<kRedBlocks, 256, 0, st>>>(d, d.r, d.z, d.p, nullptr, 1.0, d.minv, nullptr, nullptr, 3, tol,
@@ -413,6 +490,10 @@ struct Solver {
         for (;;) {
             k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
             if (pull_scal()) return CCT_CUDAERR;
+            if (outer == 0) {
+                h_nnz[0] = h_scal[S_TMP0];
+                h_nnz[1] = h_scal[S_TMP1];
+            }
             bnorm = h_scal[S_BNORM];
             const double rn = h_scal[S_RNORM];
             S.cg_relres = bnorm > 0 ? rn / bnorm : 0.0;
@@ -431,6 +512,25 @@ struct Solver {
         S.b_norm = bnorm;
         if (bnorm > 0 && S.cg_relres > opt.cg_rtol) S.error_flags |= MPS_ERR_CG;
         return CCT_NOERR;
+    }
+
+    CCTStatusType upload(const double* p3, const double* v3, const double* pr) {
+        const size_t n = d.n;
+        cudaError_t e = cudaMemcpyAsync(stage, p3, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(stage + 3 * n, v3, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemcpyAsync(stage + 6 * n, pr, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+        if (e) return CCT_CUDAERR;
+        k_pack_state<<<blocks_for(d.n), kBlock, 0, st>>>(d, stage, stage + 3 * n, stage + 6 * n);
+        return cuda_status(cudaGetLastError());
+    }
+    CCTStatusType download(double* p3, double* v3, double* pr) {
+        const size_t n = d.n;
+        k_unpack_state<<<blocks_for(d.n), kBlock, 0, st>>>(d, stage, stage + 3 * n, stage + 6 * n);
+        cudaError_t e = cudaMemcpyAsync(p3, stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st);
+        if (!e) e = cudaMemcpyAsync(v3, stage + 3 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st);
+        if (!e) e = cudaMemcpyAsync(pr, stage + 6 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, st);
+        if (!e) e = cudaStreamSynchronize(st);
+        return cuda_status(e);
     }
 
     CCTStatusType step(int stepi, MpsStepStats* out) {
@@ -460,6 +560,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->ir_max_outer = 12;
     o->max_neighbours = 384;
     o->check_every = 8;
+    o->source_relaxation = 0.05;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -511,14 +612,14 @@ CCTStatusType mps_solver_get_particles(MpsSolver* s, int* n, double* pos, double
     if (!s) return CCT_PARAMERR;
     mps::Dev& d = s->s.d;
     *n = d.n;
-    std::vector<double4> tmp(d.n);
+    std::vector<mps::dbl4> tmp(d.n);
     cudaError_t e = cudaStreamSynchronize(s->s.st);
     if (!e && pos) {
-        e = cudaMemcpy(tmp.data(), d.pos, sizeof(double4) * d.n, cudaMemcpyDeviceToHost);
+        e = cudaMemcpy(tmp.data(), d.pos, sizeof(mps::dbl4) * d.n, cudaMemcpyDeviceToHost);
         for (int i = 0; i < d.n; ++i) { pos[3 * i] = tmp[i].x; pos[3 * i + 1] = tmp[i].y; pos[3 * i + 2] = tmp[i].z; }
     }
     if (!e && vel) {
-        e = cudaMemcpy(tmp.data(), d.vel, sizeof(double4) * d.n, cudaMemcpyDeviceToHost);
+        e = cudaMemcpy(tmp.data(), d.vel, sizeof(mps::dbl4) * d.n, cudaMemcpyDeviceToHost);
         for (int i = 0; i < d.n; ++i) { vel[3 * i] = tmp[i].x; vel[3 * i + 1] = tmp[i].y; vel[3 * i + 2] = tmp[i].z; }
     }
     if (!e && press) e = cudaMemcpy(press, d.press, sizeof(double) * d.n, cudaMemcpyDeviceToHost);
@@ -566,6 +667,16 @@ CCTStatusType mps_solver_copy_pressure(MpsSolver* s, double* host_press) {
     cudaError_t e = cudaMemcpyAsync(host_press, s->s.d.press, sizeof(double) * s->s.d.n, cudaMemcpyDeviceToHost, s->s.st);
     if (!e) e = cudaStreamSynchronize(s->s.st);
     return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_upload_state(MpsSolver* s, const double* pos, const double* vel, const double* press) {
+    if (!s || !pos || !vel || !press) return CCT_PARAMERR;
+    return s->s.upload(pos, vel, press);
+}
+
+CCTStatusType mps_solver_download_state(MpsSolver* s, double* pos, double* vel, double* press) {
+    if (!s || !pos || !vel || !press) return CCT_PARAMERR;
+    return s->s.download(pos, vel, press);
 }
 
 CCTStatusType mps_solver_stream(MpsSolver* s, void** stream) {

@@ -283,8 +283,11 @@ def _finish(name, p, pos, tris, models, tparams, drag, seed, l0, zone_lo=None, z
 def dam_break(l0: float = 0.01, dt: float = 1e-4, seed: int = 1, explicit_pressure: bool = False,
               column=(0.2, 0.2, 0.4), tank=(0.8, 0.2, 0.6)) -> Scene:
     p = default_param(l0, dt, explicit_pressure=explicit_pressure)
+    # first particle layer at 1.0*l0 from the walls: the wall-weight tables
+    # (Z functions) count the missing neighbours of a particle at that distance
     pos = _lattice((0.0, 0.0, 0.0), column, l0)
-    tris = box_triangles((0.0, 0.0, 0.0), tank)
+    h = 0.5 * l0
+    tris = box_triangles((-h, -h, -h), (tank[0] - h, tank[1] - h, tank[2] - h))
     models = np.zeros(len(tris), dtype=np.int32)
     tp = [_tri_normal_params(dt=dt)]
     return _finish("dam_break", p, pos, tris, models, tp, [], seed, l0)
@@ -298,10 +301,10 @@ def rotating_bucket(l0: float = 0.004, dt: float = 5e-5, seed: int = 2, rpm: flo
     center = (0.0, 0.0, 0.0)
     tris = cylinder_triangles(center, radius, length, n_theta, n_len)
     models = [0] * len(tris)
-    h = _fill_height(radius - 0.5 * l0, fill)
+    h = _fill_height(radius - l0, fill)
     g = _lattice((-length / 2, -radius, -radius), (length / 2, radius, radius), l0)
     r2 = g[:, 1] ** 2 + g[:, 2] ** 2
-    keep = (r2 <= (radius - 0.5 * l0) ** 2) & (g[:, 2] <= -radius + 0.5 * l0 + h)
+    keep = (r2 <= (radius - l0) ** 2) & (g[:, 2] <= -radius + l0 + h) & (np.abs(g[:, 0]) <= length / 2 - l0)
     pos = g[keep]
     tparams = [_tri_normal_params(rotating=True, rpm=rpm, dt=dt, center=center, second=(1.0, 0.0, 0.0))]
     drag = []
@@ -327,11 +330,6 @@ def rotating_bucket(l0: float = 0.004, dt: float = 5e-5, seed: int = 2, rpm: flo
         d.VelocityDragPermiabilityConstant = 1.0
         d.VelocityMagnitueFactor = 1.0
         drag.append(d)
-        # particles inside a sphere body are removed (solid)
-        inside = np.zeros(len(pos), dtype=bool)
-        for c in centers:
-            inside |= ((pos - c) ** 2).sum(-1) < rs * rs
-        pos = pos[~inside]
     return _finish("rotating_bucket", p, pos, tris, np.asarray(models), tparams, drag, seed, l0)
 
 
@@ -353,9 +351,10 @@ def mixer(l0: float = 0.002, dt: float = 5e-5, seed: int = 6, n_drag: int = 512,
         models += [b] * len(t)
         tparams.append(_tri_normal_params(rotating=True, rpm=float(int(rpms[b])), dt=dt, center=c,
                                           second=(1.0, y, 0.0)))
-        h = _fill_height(r - 0.5 * l0, fill)
+        h = _fill_height(r - l0, fill)
         g = _lattice((-length / 2, y - r, -r), (length / 2, y + r, r), l0)
-        keep = ((g[:, 1] - y) ** 2 + g[:, 2] ** 2 <= (r - 0.5 * l0) ** 2) & (g[:, 2] <= -r + 0.5 * l0 + h)
+        keep = (((g[:, 1] - y) ** 2 + g[:, 2] ** 2 <= (r - l0) ** 2) & (g[:, 2] <= -r + l0 + h)
+                & (np.abs(g[:, 0]) <= length / 2 - l0))
         pos_all.append(g[keep])
         y += r + 8 * l0
     pos = np.concatenate(pos_all)
@@ -377,10 +376,6 @@ def mixer(l0: float = 0.002, dt: float = 5e-5, seed: int = 6, n_drag: int = 512,
         d.VelocityExponential = 1.0
         d.VelocityDragPermiabilityConstant = 1.0
         drag.append(d)
-        inside = np.zeros(len(pos), dtype=bool)
-        for c in centers:
-            inside |= ((pos - c) ** 2).sum(-1) < rs * rs
-        pos = pos[~inside]
     tris = np.concatenate(tris_all)
     return _finish("mixer", p, pos, tris, np.asarray(models), tparams, drag, seed, l0)
 

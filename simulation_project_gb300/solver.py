@@ -1,0 +1,196 @@
+"""Python front end of the GB300-native semi-implicit step (include/mps_solver.h).
+
+    s = Solver(scene, precision="fp32_ir")
+    stats = s.step(0)
+    state = s.state()          # dict of numpy arrays in particle-id order
+
+The scene supplies the reference's parameter / grid / wall / drag structs
+(simulation_project_gb300.scenes.Scene).  All compute runs in libmps_gb300.so.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import lib
+from .types import CParameter, CGridBox, CTriangleParameters, DragParameter, MpsError
+
+PREC = {"fp64": 0, "fp32_ir": 1}
+PRESSURE = {"ppe": 0, "explicit": 1}
+
+
+class MpsSolverOptions(C.Structure):
+    _fields_ = [("precision", C.c_int), ("pressure_mode", C.c_int), ("learned", C.c_int), ("n0_pnd", C.c_double),
+                ("n0_lap", C.c_double), ("lambda_", C.c_double), ("compressibility", C.c_double),
+                ("cg_rtol", C.c_double), ("cg_max_iter", C.c_int), ("ir_inner_rtol", C.c_double),
+                ("ir_max_outer", C.c_int), ("max_neighbours", C.c_int), ("check_every", C.c_int),
+                ("source_relaxation", C.c_double), ("profile", C.c_int)]
+
+
+class MpsStepStats(C.Structure):
+    _fields_ = [("particles", C.c_int), ("interior", C.c_int), ("cg_iterations", C.c_int), ("ir_passes", C.c_int),
+                ("fallback", C.c_int), ("max_row", C.c_int), ("cg_relres", C.c_double), ("b_norm", C.c_double),
+                ("error_flags", C.c_uint), ("nnz", C.c_longlong), ("pairs", C.c_longlong),
+                ("ms_grid", C.c_float), ("ms_walls", C.c_float), ("ms_predictor", C.c_float), ("ms_list", C.c_float),
+                ("ms_ppe_setup", C.c_float), ("ms_spmv", C.c_float), ("ms_cg_vec", C.c_float),
+                ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+P = C.c_void_p
+_SIGS = {
+    "mps_solver_default_options": (None, [C.POINTER(MpsSolverOptions)]),
+    "mps_solver_create": (C.c_int, [C.POINTER(CParameter), C.POINTER(CGridBox), C.c_int,
+                                    C.POINTER(MpsSolverOptions), C.POINTER(P)]),
+    "mps_solver_destroy": (None, [P]),
+    "mps_solver_set_particles": (C.c_int, [P, C.c_int, P, P, P, P, P]),
+    "mps_solver_set_triangles": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
+    "mps_solver_set_drag": (C.c_int, [P, C.c_int, P]),
+    "mps_solver_step": (C.c_int, [P, C.c_int, C.POINTER(MpsStepStats)]),
+    "mps_solver_get_particles": (C.c_int, [P, C.POINTER(C.c_int), P, P, P, P, P]),
+    "mps_solver_get_triangles": (C.c_int, [P, P]),
+    "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
+    "mps_solver_copy_pressure": (C.c_int, [P, P]),
+    "mps_solver_stream": (C.c_int, [P, C.POINTER(P)]),
+    "mps_solver_upload_state": (C.c_int, [P, P, P, P]),
+    "mps_solver_download_state": (C.c_int, [P, P, P, P]),
+    "mps_solver_set_learned": (C.c_int, [P, P, C.c_int]),
+    "mps_solver_learned_samples": (C.c_int, [P, P, P, C.POINTER(C.c_int)]),
+}
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = lib.load()
+    if not _bound:
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _bound = True
+    return L
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise MpsError(rc, f"{what} ({lib.load().mps_last_error().decode()})")
+
+
+def default_options(precision="fp32_ir", **kw) -> MpsSolverOptions:
+    o = MpsSolverOptions()
+    _lib().mps_solver_default_options(C.byref(o))
+    o.precision = PREC[precision]
+    for k, v in kw.items():
+        setattr(o, "lambda_" if k == "lam" else k, v)
+    return o
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Solver:
+    def __init__(self, scene, precision="fp32_ir", physics=True, max_particles=None, **opts):
+        L = _lib()
+        o = default_options(precision, **opts)
+        if physics:
+            if o.n0_pnd <= 0:
+                o.n0_pnd = scene.n0_pnd
+            if o.n0_lap <= 0:
+                o.n0_lap = scene.n0_lap
+            if o.lambda_ <= 0:
+                o.lambda_ = scene.lam
+        self.options = o
+        self.scene = scene
+        h = P()
+        _check(L.mps_solver_create(C.byref(scene.param), C.byref(scene.box), int(max_particles or scene.n),
+                                   C.byref(o), C.byref(h)), "mps_solver_create")
+        self.h = h
+        pos = np.ascontiguousarray(scene.pos, dtype=np.float64)
+        vel = np.ascontiguousarray(scene.vel, dtype=np.float64)
+        press = np.ascontiguousarray(scene.press, dtype=np.float64)
+        visc = np.ascontiguousarray(scene.visc, dtype=np.float64)
+        ptype = np.ascontiguousarray(scene.ptype, dtype=np.int32)
+        _check(L.mps_solver_set_particles(h, scene.n, _p(pos), _p(vel), _p(press), _p(visc), _p(ptype)),
+               "mps_solver_set_particles")
+        if scene.t > 0:
+            v = np.ascontiguousarray(scene.tri_vertices.reshape(-1, 9), dtype=np.float64)
+            m = np.ascontiguousarray(scene.tri_model, dtype=np.int32)
+            tp = (CTriangleParameters * len(scene.tri_params))(*scene.tri_params)
+            _check(L.mps_solver_set_triangles(h, scene.t, _p(v), _p(m), len(scene.tri_params), C.addressof(tp)),
+                   "mps_solver_set_triangles")
+        if scene.drag:
+            dp = (DragParameter * len(scene.drag))(*scene.drag)
+            _check(L.mps_solver_set_drag(h, len(scene.drag), C.addressof(dp)), "mps_solver_set_drag")
+
+    def step(self, i: int) -> dict:
+        s = MpsStepStats()
+        _check(_lib().mps_solver_step(self.h, int(i), C.byref(s)), "mps_solver_step")
+        return s.as_dict()
+
+    def state(self, sort_by_id=True) -> dict:
+        L = _lib()
+        nmax = self.scene.n
+        n = C.c_int()
+        pos = np.zeros((nmax, 3))
+        vel = np.zeros((nmax, 3))
+        press = np.zeros(nmax)
+        pnd = np.zeros(nmax)
+        ids = np.zeros(nmax, np.int32)
+        _check(L.mps_solver_get_particles(self.h, C.byref(n), _p(pos), _p(vel), _p(press), _p(pnd), _p(ids)),
+               "mps_solver_get_particles")
+        k = n.value
+        out = {"pos": pos[:k], "vel": vel[:k], "press": press[:k], "pnd": pnd[:k], "id": ids[:k]}
+        if sort_by_id:
+            o = np.argsort(out["id"], kind="stable")
+            out = {key: v[o] for key, v in out.items()}
+        return out
+
+    def debug_ppe(self) -> dict:
+        nmax = self.scene.n
+        arr = {k: np.zeros(nmax) for k in ("pnd", "diag", "rhs", "sol", "nbr_idsum")}
+        ids = np.zeros(nmax, np.int32)
+        cnt = np.zeros(nmax, np.int32)
+        _check(_lib().mps_solver_debug_ppe(self.h, _p(arr["pnd"]), _p(arr["diag"]), _p(arr["rhs"]), _p(arr["sol"]),
+                                           _p(ids), _p(cnt), _p(arr["nbr_idsum"])), "mps_solver_debug_ppe")
+        n = self.state(sort_by_id=False)["id"].shape[0]
+        out = {k: v[:n] for k, v in arr.items()}
+        out["id"] = ids[:n]
+        out["nbr_count"] = cnt[:n]
+        return out
+
+    def triangles(self) -> np.ndarray:
+        v = np.zeros((self.scene.t, 9))
+        if self.scene.t:
+            _check(_lib().mps_solver_get_triangles(self.h, _p(v)), "mps_solver_get_triangles")
+        return v.reshape(-1, 3, 3)
+
+    def set_learned(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(_lib().mps_solver_set_learned(self.h, p.ctypes.data, p.size), "mps_solver_set_learned")
+
+    def upload_state(self, pos, vel, press):
+        _check(_lib().mps_solver_upload_state(self.h, pos.ctypes.data, vel.ctypes.data, press.ctypes.data),
+               "mps_solver_upload_state")
+
+    def download_state(self, pos, vel, press):
+        _check(_lib().mps_solver_download_state(self.h, pos.ctypes.data, vel.ctypes.data, press.ctypes.data),
+               "mps_solver_download_state")
+
+    def stream(self):
+        s = P()
+        _check(_lib().mps_solver_stream(self.h, C.byref(s)), "mps_solver_stream")
+        return s.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib().mps_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -51,6 +51,35 @@ def golden_scenes():
     return {"block": s1, "bucket": s2}
 
 
+def scene_to_arrays(sc):
+    """The scene inputs as plain arrays (stored with the golden outputs, so the
+    fixture does not depend on the scene generator)."""
+    import ctypes as C
+    from simulation_project_gb300.types import CTriangleParameters, DragParameter
+    tp = (CTriangleParameters * len(sc.tri_params))(*sc.tri_params)
+    dp = (DragParameter * max(len(sc.drag), 1))(*sc.drag)
+    return {"in_pos": sc.pos, "in_vel": sc.vel, "in_press": sc.press, "in_visc": sc.visc, "in_type": sc.ptype,
+            "in_tri": sc.tri_vertices, "in_tri_model": sc.tri_model,
+            "in_param": np.frombuffer(bytes(sc.param), np.uint8), "in_box": np.frombuffer(bytes(sc.box), np.uint8),
+            "in_tparams": np.frombuffer(bytes(tp), np.uint8), "in_drag": np.frombuffer(bytes(dp), np.uint8),
+            "in_ndrag": np.array([len(sc.drag)])}
+
+
+def scene_from_arrays(g):
+    import ctypes as C
+    from simulation_project_gb300.scenes import Scene
+    from simulation_project_gb300.types import CParameter, CGridBox, CTriangleParameters, DragParameter
+    param = CParameter.from_buffer_copy(g["in_param"].tobytes())
+    box = CGridBox.from_buffer_copy(g["in_box"].tobytes())
+    ntp = g["in_tparams"].nbytes // C.sizeof(CTriangleParameters)
+    tps = (CTriangleParameters * ntp).from_buffer_copy(g["in_tparams"].tobytes())
+    nd = int(g["in_ndrag"][0])
+    dps = (DragParameter * max(nd, 1)).from_buffer_copy(g["in_drag"].tobytes())
+    return Scene(name="golden", param=param, box=box, pos=g["in_pos"], vel=g["in_vel"], press=g["in_press"],
+                 visc=g["in_visc"], ptype=g["in_type"], tri_vertices=g["in_tri"], tri_model=g["in_tri_model"],
+                 tri_params=list(tps), drag=list(dps)[:nd])
+
+
 def math_cases(lib):
     rng = np.random.default_rng(13)
     rs = (np.concatenate([rng.uniform(0, 4.5, 400), np.arange(0, 4.2, 0.05)]) * 0.004).astype(np.float32)
@@ -82,7 +111,8 @@ def main():
         raise SystemExit("reference sources not available")
     for name, sc in golden_scenes().items():
         pred, final = explicit_step(ref, sc)
-        arrays = {f"pred_{k}": v for k, v in pred.items()}
+        arrays = scene_to_arrays(sc)
+        arrays.update({f"pred_{k}": v for k, v in pred.items()})
         arrays.update({f"final_{k}": v for k, v in final.items()})
         np.savez_compressed(os.path.join(HERE, f"ref_explicit_{name}.npz"), **arrays)
     np.savez_compressed(os.path.join(HERE, "ref_math.npz"), **math_cases(ref))

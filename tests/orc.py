@@ -33,7 +33,8 @@ class OrcBindings(C.Structure):
 class OrcSimConfig(C.Structure):
     _fields_ = [("param", CParameter), ("box", CGridBox), ("quirks", C.c_int), ("n0_pnd", C.c_double),
                 ("n0_lap", C.c_double), ("lambda_", C.c_double), ("compressibility", C.c_double),
-                ("cg_rtol", C.c_double), ("cg_max_iter", C.c_int), ("threads", C.c_int)]
+                ("cg_rtol", C.c_double), ("cg_max_iter", C.c_int), ("threads", C.c_int),
+                ("source_relaxation", C.c_double)]
 
 
 class OrcStepStats(C.Structure):
@@ -76,6 +77,8 @@ _FUNCS = {
     "orc_sim_get": (C.c_int, [P, P, P, P, P, P]),
     "orc_sim_get_triangles": (C.c_int, [P, P]),
     "orc_sim_last_ppe": (C.c_int, [P, P, P, P, P, P]),
+    "orc_sim_get_ids": (C.c_int, [P, P]),
+    "orc_sim_last_nbr": (C.c_int, [P, P, P, P]),
 }
 
 
@@ -244,3 +247,70 @@ def ref_topology(lib: Lib, st: RefState, b: OrcBindings) -> None:
         st.index[:n] = st.index[:n][order]
     lib.reorder_find_cell_start(C.byref(b), n, st.cells_n, ptr(st.hash), ptr(st.index), ptr(st.cell_start),
                                 ptr(st.cell_end))
+
+
+class OracleSim:
+    """The FP64 semi-implicit solver of the oracle (no reference counterpart)."""
+
+    def __init__(self, scene, cg_rtol=1e-8, compressibility=1e-9, cg_max_iter=5000, threads=0,
+                 source_relaxation=0.05):
+        self.lib = oracle()
+        cfg = OrcSimConfig()
+        cfg.param = scene.param
+        cfg.box = scene.box
+        cfg.n0_pnd = scene.n0_pnd
+        cfg.n0_lap = scene.n0_lap
+        cfg.lambda_ = scene.lam
+        cfg.compressibility = compressibility
+        cfg.cg_rtol = cg_rtol
+        cfg.cg_max_iter = cg_max_iter
+        cfg.threads = threads
+        cfg.source_relaxation = source_relaxation
+        self.cfg = cfg
+        self.scene = scene
+        self.h = self.lib.sim_create(C.byref(cfg), scene.n)
+        pos = np.ascontiguousarray(scene.pos, np.float64)
+        vel = np.ascontiguousarray(scene.vel, np.float64)
+        pr = np.ascontiguousarray(scene.press, np.float64)
+        vi = np.ascontiguousarray(scene.visc, np.float64)
+        ty = np.ascontiguousarray(scene.ptype, np.int32)
+        self.lib.sim_set_particles(self.h, scene.n, ptr(pos), ptr(vel), ptr(pr), ptr(vi), ptr(ty))
+        if scene.t:
+            v = np.ascontiguousarray(scene.tri_vertices.reshape(-1, 9), np.float64)
+            m = np.ascontiguousarray(scene.tri_model, np.int32)
+            tp = (CTriangleParameters * len(scene.tri_params))(*scene.tri_params)
+            self.lib.sim_set_triangles(self.h, scene.t, ptr(v), ptr(m), len(scene.tri_params), C.addressof(tp))
+        if scene.drag:
+            dp = (DragParameter * len(scene.drag))(*scene.drag)
+            self.lib.sim_set_drag(self.h, len(scene.drag), C.addressof(dp))
+
+    def step(self, i):
+        st = OrcStepStats()
+        rc = self.lib.sim_step(self.h, i, C.byref(st))
+        return rc, {k: getattr(st, k) for k, _ in st._fields_}
+
+    def state(self):
+        n0 = self.scene.n
+        n = C.c_int()
+        pos, vel = np.zeros((n0, 3)), np.zeros((n0, 3))
+        press, pnd = np.zeros(n0), np.zeros(n0)
+        ids = np.zeros(n0, np.int32)
+        self.lib.sim_get(self.h, C.byref(n), ptr(pos), ptr(vel), ptr(press), ptr(pnd))
+        self.lib.sim_get_ids(self.h, ptr(ids))
+        k = n.value
+        o = np.argsort(ids[:k], kind="stable")
+        return {"pos": pos[:k][o], "vel": vel[:k][o], "press": press[:k][o], "pnd": pnd[:k][o], "id": ids[:k][o]}
+
+    def neighbours(self):
+        n0 = self.scene.n
+        cnt = np.zeros(n0, np.int32)
+        idsum = np.zeros(n0)
+        pid = np.zeros(n0, np.int32)
+        k = self.lib.sim_last_nbr(self.h, ptr(cnt), ptr(idsum), ptr(pid))
+        o = np.argsort(pid[:k], kind="stable")
+        return {"id": pid[:k][o], "nbr_count": cnt[:k][o], "nbr_idsum": idsum[:k][o]}
+
+    def close(self):
+        if self.h:
+            self.lib.sim_destroy(self.h)
+            self.h = None

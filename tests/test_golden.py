@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import orc
-from golden.make_golden import explicit_step, golden_scenes, math_cases
+from golden.make_golden import explicit_step, math_cases, scene_from_arrays
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -16,7 +16,7 @@ GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 @pytest.mark.parametrize("name", ["block", "bucket"])
 def test_explicit_step_matches_reference_golden(name):
     g = np.load(os.path.join(GOLD, f"ref_explicit_{name}.npz"))
-    pred, final = explicit_step(orc.oracle(), golden_scenes()[name])
+    pred, final = explicit_step(orc.oracle(), scene_from_arrays(g))
     for stage, arrays in (("pred", pred), ("final", final)):
         for k, v in arrays.items():
             ref = g[f"{stage}_{k}"]

@@ -1,0 +1,105 @@
+"""The GB300-native semi-implicit step against the FP64 oracle solver.
+
+FP64 mode: neighbour sets (count and id checksum per particle) identical; pressure
+within 1e-6 relative (max-norm, relative to max |P|) and positions within 1e-6*l0
+after 10 steps.  FP32 operators inside FP64 refinement: PPE residual <= 1e-8 and the
+stated FP32 tolerances (pressure 2e-3 relative, positions 1e-4*l0 after 10 steps)."""
+import numpy as np
+import pytest
+
+import orc
+from simulation_project_gb300 import scenes
+from simulation_project_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+
+def small_dam(seed=1):
+    # reduced dam break: 10 x 10 x 20 column at l0 = 0.01 in the 0.8 x 0.2 x 0.6 tank
+    return scenes.dam_break(l0=0.01, column=(0.1, 0.1, 0.2), seed=seed)
+
+
+def _compare_neighbours(gpu: Solver, o: orc.OracleSim):
+    g = gpu.debug_ppe()
+    og = np.argsort(g["id"], kind="stable")
+    on = o.neighbours()
+    assert np.array_equal(g["id"][og], on["id"])
+    assert np.array_equal(g["nbr_count"][og], on["nbr_count"])
+    assert np.array_equal(g["nbr_idsum"][og], on["nbr_idsum"])
+
+
+def test_fp64_first_step_neighbour_sets_and_pressure():
+    sc = small_dam()
+    o = orc.OracleSim(sc)
+    g = Solver(sc, precision="fp64")
+    rc, ost = o.step(0)
+    gst = g.step(0)
+    assert rc == 0 and gst["error_flags"] == 0, gst
+    _compare_neighbours(g, o)
+    a, b = g.state(), o.state()
+    assert np.array_equal(a["id"], b["id"])
+    pmax = np.abs(b["press"]).max()
+    assert pmax > 0
+    assert np.abs(a["press"] - b["press"]).max() <= 1e-6 * pmax
+    np.testing.assert_allclose(a["pnd"], b["pnd"], rtol=1e-12, atol=1e-12)
+    assert np.abs(a["pos"] - b["pos"]).max() <= 1e-6 * sc.param.InitialParticleDistance
+    assert gst["cg_relres"] <= 1e-8
+
+
+def test_fp64_ten_steps_match_oracle():
+    sc = small_dam(seed=2)
+    o = orc.OracleSim(sc)
+    g = Solver(sc, precision="fp64")
+    for i in range(10):
+        rc, _ = o.step(i)
+        st = g.step(i)
+        assert rc == 0 and st["error_flags"] == 0
+    _compare_neighbours(g, o)
+    a, b = g.state(), o.state()
+    assert np.array_equal(a["id"], b["id"])
+    pmax = np.abs(b["press"]).max()
+    assert np.abs(a["press"] - b["press"]).max() <= 1e-6 * pmax
+    assert np.abs(a["pos"] - b["pos"]).max() <= 1e-6 * sc.param.InitialParticleDistance
+
+
+def test_fp32_ir_converges_and_tracks_fp64():
+    sc = small_dam(seed=3)
+    o = orc.OracleSim(sc)
+    g = Solver(sc, precision="fp32_ir")
+    for i in range(10):
+        rc, _ = o.step(i)
+        st = g.step(i)
+        assert rc == 0 and st["error_flags"] == 0, st
+        assert st["cg_relres"] <= 1e-8
+        assert st["ir_passes"] >= 1
+    a, b = g.state(), o.state()
+    assert np.array_equal(a["id"], b["id"])
+    pmax = np.abs(b["press"]).max()
+    err_p = np.abs(a["press"] - b["press"]).max() / pmax
+    err_x = np.abs(a["pos"] - b["pos"]).max() / sc.param.InitialParticleDistance
+    assert err_p <= 2e-3, err_p
+    assert err_x <= 1e-4, err_x
+
+
+def test_bucket_with_walls_and_drag_fp64():
+    sc = scenes.rotating_bucket(l0=0.012, n_drag=6, drag_index=0.5)
+    o = orc.OracleSim(sc)
+    g = Solver(sc, precision="fp64")
+    for i in range(3):
+        rc, _ = o.step(i)
+        st = g.step(i)
+        assert rc == 0 and st["error_flags"] == 0, st
+    _compare_neighbours(g, o)
+    a, b = g.state(), o.state()
+    assert np.array_equal(a["id"], b["id"])
+    pmax = np.abs(b["press"]).max()
+    assert np.abs(a["press"] - b["press"]).max() <= 1e-6 * pmax
+    assert np.abs(a["pos"] - b["pos"]).max() <= 1e-6 * sc.param.InitialParticleDistance
+    np.testing.assert_allclose(g.triangles().reshape(-1, 9), _tri(o, sc), rtol=0, atol=1e-12)
+
+
+def _tri(o, sc):
+    import ctypes as C
+    v = np.zeros((sc.t, 9))
+    o.lib.sim_get_triangles(o.h, orc.ptr(v))
+    return v
