@@ -1,0 +1,57 @@
+/*
+ * mps_learned.h - the learned PPE initial guess / preconditioner scaling (BF16 MLP).
+ *
+ * No counterpart in the reference (its NJPCG solver is declared only:
+ * solver/MPS_SOLVER_WITH_ROTATION/PMMultiGPU/Source/CGPUCellSet.h:224-225, 239).
+ *
+ * Network: 12 features -> 128 -> 128 -> 128 (SiLU) -> 2 outputs (pressure increment
+ * in units of the step's pressure scale, log of the diagonal preconditioner scale).
+ * Weights are BF16 on the tensor cores, accumulation and the master copy are FP32.
+ * Parameter vector layout (FP32, MPS_MLP_PARAMS = 35,330 floats):
+ *   W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[128][2] b4[2]
+ * (W[k][n]: input k, output n).
+ *
+ * All array arguments are DEVICE pointers unless stated; `stream` is a cudaStream_t
+ * (NULL = legacy default stream).  Every call returns a CCTStatusType.
+ */
+#ifndef MPS_LEARNED_H
+#define MPS_LEARNED_H
+
+#include "mps_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* C[m][n] = act(sum_k A(m,k) B(k,n) + bias[n]) (+ beta * C) with BF16 A, B and FP32
+ * accumulation on the tensor cores.  A(m,k) = A[m*lda + k] (transA = 0) or
+ * A[k*lda + m] (transA = 1); B(k,n) = B[k*ldb + n] (transB = 0) or B[n*ldb + k]
+ * (transB = 1).  Any K (tiles are zero-filled).  C (FP32, ldc) and/or Cb (BF16, ldcb)
+ * may be NULL.  act: 0 none, 1 SiLU (Cz, if given, receives the pre-activation FP32).
+ * split_k > 1 splits the K loop over CTAs and accumulates into C with atomics
+ * (beta must be 1 and act 0 then). */
+CCTStatusType mps_gemm_bf16(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb,
+                            int transB, float* C, int ldc, void* Cb, int ldcb, float* Cz, const float* bias, int act,
+                            float beta, int split_k, void* stream);
+
+typedef struct MpsMlp MpsMlp;
+CCTStatusType mps_mlp_create(int max_batch, unsigned long long seed, MpsMlp** out);
+void mps_mlp_destroy(MpsMlp* m);
+/* host FP32 parameter vector in / out (MPS_MLP_PARAMS floats) */
+CCTStatusType mps_mlp_set_params(MpsMlp* m, const float* host_params);
+CCTStatusType mps_mlp_get_params(MpsMlp* m, float* host_params);
+/* Y[M][2] = MLP(X[M][12]) (device FP32) */
+CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* stream);
+/* loss = mean over rows of (y0-t0)^2 + w1 (y1-t1)^2 and the gradient of every
+ * parameter (device FP32, MPS_MLP_PARAMS floats) by the tensor-core backward pass */
+CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T, float w1, float* grad,
+                                float* host_loss, void* stream);
+/* one Adam step (lr, beta1 0.9, beta2 0.999, eps 1e-8) on a mini-batch */
+CCTStatusType mps_mlp_train_step(MpsMlp* m, int M, const float* X, const float* T, float w1, float lr,
+                                 float* host_loss, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -116,6 +116,8 @@ CCTStatusType mps_solver_set_learned(MpsSolver* s, const float* params, int coun
 /* Features (n*12, FP32) and training targets (n*2: normalised pressure increment,
  * log of the ideal diagonal scale) of the last PPE solve, sorted order. */
 CCTStatusType mps_solver_learned_samples(MpsSolver* s, float* features, float* targets, int* n);
+/* 1: compute features and targets at every PPE solve (for mps_solver_learned_samples) */
+CCTStatusType mps_solver_collect(MpsSolver* s, int on);
 
 #ifdef __cplusplus
 }

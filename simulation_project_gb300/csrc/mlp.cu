@@ -1,0 +1,467 @@
+// mlp.cu - BF16 tensor-core GEMM and the learned-preconditioner MLP (forward,
+// backward, Adam) of the GB300 MPS library (include/mps_learned.h).
+//
+// GEMM: one CTA of 4 warps computes a 64x64 FP32 tile of C with warp-level
+// mma.sync.m16n8k16 (BF16 in, FP32 accumulate); each warp owns a 32x32 sub-tile
+// (2 x 4 MMA tiles).  K advances 32 at a time through padded shared-memory tiles
+// As[m][k] and Bs[n][k], so every A and B fragment register is one 32-bit shared
+// load of two consecutive k.  Transposed operands are handled by the tile loader.
+// The epilogue adds a bias, optionally keeps the FP32 pre-activation, applies SiLU
+// and writes FP32 and/or BF16; split-K CTAs accumulate with FP32 atomics.
+// The network is tiny (69 kFLOP per particle per forward), so these kernels are a
+// small part of a solver step; they exist so the network is trained on the GPU by
+// this library's own kernels.
+#include <cuda_bf16.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "mps_common.cuh"
+#include "mps_internal.h"
+#include "../../include/mps_learned.h"
+#include "../../include/mps_solver.h"
+
+namespace mps {
+
+typedef __nv_bfloat16 bf16;
+constexpr int GT_M = 64, GT_N = 64, GT_K = 32, GT_PAD = 8;
+constexpr int H = 128;      // hidden width
+constexpr int FIN = 12;     // input features
+constexpr int FINP = 16;    // padded input width
+constexpr int FOUT = 2;     // outputs
+constexpr int FOUTP = 16;   // padded output width
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu_grad(float z) {
+    const float s = 1.0f / (1.0f + __expf(-z));
+    return s * (1.0f + z * (1.0f - s));
+}
+
+__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16* __restrict__ A, int lda, int ta,
+                                                  const bf16* __restrict__ B, int ldb, int tb, float* C, int ldc,
+                                                  bf16* Cb, int ldcb, float* Cz, const float* __restrict__ bias, int act,
+                                                  float beta, int kchunk) {
+    __shared__ __align__(16) bf16 As[GT_M][GT_K + GT_PAD];
+    __shared__ __align__(16) bf16 Bs[GT_N][GT_K + GT_PAD];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 2, c = lane & 3;
+    const int m0 = blockIdx.y * GT_M, n0 = blockIdx.x * GT_N;
+    const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[a][b][q] = 0.f;
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int k0 = kbeg; k0 < kend; k0 += GT_K) {
+        for (int e = tid; e < GT_M * GT_K; e += 128) {
+            int mm, kk;
+            if (ta == 0) { mm = e / GT_K; kk = e % GT_K; } else { kk = e / GT_M; mm = e % GT_M; }
+            const int m = m0 + mm, k = k0 + kk;
+            bf16 v = zero;
+            if (m < M && k < kend) v = ta == 0 ? A[(size_t)m * lda + k] : A[(size_t)k * lda + m];
+            As[mm][kk] = v;
+        }
+        for (int e = tid; e < GT_N * GT_K; e += 128) {
+            int nn, kk;
+            if (tb == 0) { kk = e / GT_N; nn = e % GT_N; } else { nn = e / GT_K; kk = e % GT_K; }
+            const int n = n0 + nn, k = k0 + kk;
+            bf16 v = zero;
+            if (n < N && k < kend) v = tb == 0 ? B[(size_t)k * ldb + n] : B[(size_t)n * ldb + k];
+            Bs[nn][kk] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GT_K; kk += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                const int r = wm + mt * 16 + g;
+                af[mt][0] = *(const uint32_t*)&As[r][kk + 2 * c];
+                af[mt][1] = *(const uint32_t*)&As[r + 8][kk + 2 * c];
+                af[mt][2] = *(const uint32_t*)&As[r][kk + 2 * c + 8];
+                af[mt][3] = *(const uint32_t*)&As[r + 8][kk + 2 * c + 8];
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const int r = wn + nt * 8 + g;
+                bfr[nt][0] = *(const uint32_t*)&Bs[r][kk + 2 * c];
+                bfr[nt][1] = *(const uint32_t*)&Bs[r][kk + 2 * c + 8];
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+                for (int nt = 0; nt < 4; ++nt) mma_bf16(acc[mt][nt], af[mt], bfr[nt]);
+        }
+        __syncthreads();
+    }
+    const bool split = gridDim.z > 1;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int row = m0 + wm + mt * 16 + g + (q >= 2 ? 8 : 0);
+                const int col = n0 + wn + nt * 8 + 2 * c + (q & 1);
+                if (row >= M || col >= N) continue;
+                float v = acc[mt][nt][q];
+                if (split) {
+                    atomicAdd(C + (size_t)row * ldc + col, v);
+                    continue;
+                }
+                if (bias) v += bias[col];
+                if (Cz) Cz[(size_t)row * ldc + col] = v;
+                if (act == 1) v = silu(v);
+                if (C) C[(size_t)row * ldc + col] = beta != 0.f ? beta * C[(size_t)row * ldc + col] + v : v;
+                if (Cb) Cb[(size_t)row * ldcb + col] = __float2bfloat16(v);
+            }
+}
+
+cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, int ta, const bf16* B, int ldb, int tb, float* C, int ldc,
+                 bf16* Cb, int ldcb, float* Cz, const float* bias, int act, float beta, int split, cudaStream_t st) {
+    if (M <= 0 || N <= 0 || K <= 0) return cudaErrorInvalidValue;
+    split = max(1, split);
+    int kchunk = (K + split - 1) / split;
+    kchunk = (kchunk + GT_K - 1) / GT_K * GT_K;
+    split = (K + kchunk - 1) / kchunk;
+    dim3 grid(div_up(N, GT_N), div_up(M, GT_M), split);
+    k_gemm_bf16<<<grid, 128, 0, st>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, Cz, bias, act, beta, kchunk);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// elementwise helpers of the MLP
+// ---------------------------------------------------------------------------
+__global__ void k_pack_input(int M, const float* __restrict__ X, bf16* __restrict__ Xb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * FINP) return;
+    const int r = i / FINP, c = i % FINP;
+    Xb[i] = __float2bfloat16(c < FIN ? X[(size_t)r * FIN + c] : 0.f);
+}
+// FP32 master parameters -> padded BF16 weights and FP32 biases
+struct Layers {
+    bf16 *W1, *W2, *W3, *W4;      // [16][128], [128][128], [128][128], [128][16]
+    float *b1, *b2, *b3, *b4;     // [128] x3, [16]
+};
+__global__ void k_params_to_layers(const float* __restrict__ p, Layers L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int o1 = FIN * H, o2 = o1 + H, o3 = o2 + H * H, o4 = o3 + H, o5 = o4 + H * H, o6 = o5 + H, o7 = o6 + H * FOUT;
+    if (i < FINP * H) {
+        const int k = i / H, n = i % H;
+        L.W1[i] = __float2bfloat16(k < FIN ? p[k * H + n] : 0.f);
+    }
+    if (i < H) {
+        L.b1[i] = p[o1 + i];
+        L.b2[i] = p[o3 + i];
+        L.b3[i] = p[o5 + i];
+    }
+    if (i < H * H) {
+        L.W2[i] = __float2bfloat16(p[o2 + i]);
+        L.W3[i] = __float2bfloat16(p[o4 + i]);
+    }
+    if (i < H * FOUTP) {
+        const int k = i / FOUTP, n = i % FOUTP;
+        L.W4[i] = __float2bfloat16(n < FOUT ? p[o6 + k * FOUT + n] : 0.f);
+    }
+    if (i < FOUTP) L.b4[i] = i < FOUT ? p[o7 + i] : 0.f;
+}
+__global__ void k_unpad_output(int M, const float* __restrict__ Yp, float* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * FOUT) return;
+    Y[i] = Yp[(size_t)(i / FOUT) * FOUTP + (i % FOUT)];
+}
+// dY = d loss / d y for loss = mean((y0 - t0)^2 + w1 (y1 - t1)^2); loss partial sums
+__global__ void k_loss_grad(int M, const float* __restrict__ Yp, const float* __restrict__ T, float w1,
+                            bf16* __restrict__ dYb, float* __restrict__ dY, double* __restrict__ loss) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (i < M) {
+        const float e0 = Yp[(size_t)i * FOUTP] - T[2 * (size_t)i];
+        const float e1 = Yp[(size_t)i * FOUTP + 1] - T[2 * (size_t)i + 1];
+        l = (double)e0 * e0 + (double)w1 * e1 * e1;
+        const float s = 2.0f / (float)M;
+        for (int c = 0; c < FOUTP; ++c) {
+            const float gv = c == 0 ? s * e0 : (c == 1 ? s * w1 * e1 : 0.f);
+            dY[(size_t)i * FOUTP + c] = gv;
+            dYb[(size_t)i * FOUTP + c] = __float2bfloat16(gv);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+__global__ void k_silu_back(int n, const float* __restrict__ dH, const float* __restrict__ Z, float* __restrict__ dZ,
+                            bf16* __restrict__ dZb) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = dH[i] * silu_grad(Z[i]);
+    dZ[i] = v;
+    dZb[i] = __float2bfloat16(v);
+}
+// column sums (bias gradients), FP32 -> out[c]
+__global__ void k_colsum(int M, int N, const float* __restrict__ A, float* __restrict__ out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    float s = 0.f;
+    for (int r = 0; r < M; ++r) s += A[(size_t)r * N + c];
+    out[c] = s;
+}
+// gradient buffers (padded layer shapes) -> parameter-vector layout
+__global__ void k_grad_to_vec(const float* __restrict__ dW1, const float* __restrict__ db1, const float* __restrict__ dW2,
+                              const float* __restrict__ db2, const float* __restrict__ dW3, const float* __restrict__ db3,
+                              const float* __restrict__ dW4, const float* __restrict__ db4, float* __restrict__ g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int o1 = FIN * H, o2 = o1 + H, o3 = o2 + H * H, o4 = o3 + H, o5 = o4 + H * H, o6 = o5 + H, o7 = o6 + H * FOUT;
+    if (i < FIN * H) g[i] = dW1[i];
+    if (i < H) {
+        g[o1 + i] = db1[i];
+        g[o3 + i] = db2[i];
+        g[o5 + i] = db3[i];
+    }
+    if (i < H * H) {
+        g[o2 + i] = dW2[i];
+        g[o4 + i] = dW3[i];
+    }
+    if (i < H * FOUT) g[o6 + i] = dW4[(i / FOUT) * FOUTP + (i % FOUT)];
+    if (i < FOUT) g[o7 + i] = db4[i];
+}
+__global__ void k_adam(int n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1t, float b2t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = 0.9f * m[i] + 0.1f * gi;
+    const float vi = 0.999f * v[i] + 0.001f * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float mh = mi / (1.f - b1t), vh = vi / (1.f - b2t);
+    p[i] -= lr * mh / (sqrtf(vh) + 1e-8f);
+}
+
+}  // namespace mps
+
+using namespace mps;
+
+struct MpsMlp {
+    int maxb = 0;
+    int nparams = MPS_MLP_PARAMS;
+    float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+    Layers L{};
+    bf16 *Xb = nullptr, *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dYb = nullptr, *dZb = nullptr;
+    float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *Yp = nullptr, *dY = nullptr, *dH = nullptr, *dZ = nullptr;
+    float *dW1 = nullptr, *dW2 = nullptr, *dW3 = nullptr, *dW4 = nullptr, *db = nullptr;
+    double* loss = nullptr;
+    double* h_loss = nullptr;
+    int t = 0;
+    std::vector<void*> allocs;
+
+    template <class T>
+    cudaError_t mk(T** ptr, size_t count) {
+        cudaError_t e = cudaMalloc((void**)ptr, sizeof(T) * (count ? count : 1));
+        if (e == cudaSuccess) allocs.push_back(*ptr);
+        return e;
+    }
+    cudaError_t init(int b) {
+        maxb = (b + 63) / 64 * 64;
+        const size_t B = maxb;
+        cudaError_t e = cudaSuccess;
+        e = e ? e : mk(&p, nparams); e = e ? e : mk(&g, nparams); e = e ? e : mk(&m, nparams); e = e ? e : mk(&v, nparams);
+        e = e ? e : mk(&L.W1, FINP * H); e = e ? e : mk(&L.W2, H * H); e = e ? e : mk(&L.W3, H * H);
+        e = e ? e : mk(&L.W4, H * FOUTP);
+        e = e ? e : mk(&L.b1, H); e = e ? e : mk(&L.b2, H); e = e ? e : mk(&L.b3, H); e = e ? e : mk(&L.b4, FOUTP);
+        e = e ? e : mk(&Xb, B * FINP); e = e ? e : mk(&H1, B * H); e = e ? e : mk(&H2, B * H); e = e ? e : mk(&H3, B * H);
+        e = e ? e : mk(&Z1, B * H); e = e ? e : mk(&Z2, B * H); e = e ? e : mk(&Z3, B * H);
+        e = e ? e : mk(&Yp, B * FOUTP); e = e ? e : mk(&dY, B * FOUTP); e = e ? e : mk(&dYb, B * FOUTP);
+        e = e ? e : mk(&dH, B * H); e = e ? e : mk(&dZ, B * H); e = e ? e : mk(&dZb, B * H);
+        e = e ? e : mk(&dW1, FINP * H); e = e ? e : mk(&dW2, H * H); e = e ? e : mk(&dW3, H * H);
+        e = e ? e : mk(&dW4, H * FOUTP); e = e ? e : mk(&db, 4 * H);
+        e = e ? e : mk(&loss, 1);
+        if (e) return e;
+        if ((e = cudaMallocHost((void**)&h_loss, sizeof(double)))) return e;
+        cudaMemset(m, 0, sizeof(float) * nparams);
+        cudaMemset(v, 0, sizeof(float) * nparams);
+        return cudaDeviceSynchronize();
+    }
+    void release() {
+        cudaDeviceSynchronize();
+        for (void* a : allocs) cudaFree(a);
+        allocs.clear();
+        if (h_loss) cudaFreeHost(h_loss);
+        h_loss = nullptr;
+    }
+    cudaError_t sync_layers(cudaStream_t st) {
+        k_params_to_layers<<<div_up(H * H, 256), 256, 0, st>>>(p, L);
+        return cudaGetLastError();
+    }
+    // forward over M rows (M <= maxb); keep pre-activations when train
+    cudaError_t forward(int M, const float* X, cudaStream_t st, bool train) {
+        k_pack_input<<<div_up(M * FINP, 256), 256, 0, st>>>(M, X, Xb);
+        cudaError_t e = gemm(M, H, FINP, Xb, FINP, 0, L.W1, H, 0, nullptr, H, H1, H, train ? Z1 : nullptr, L.b1, 1,
+                             0.f, 1, st);
+        if (!e) e = gemm(M, H, H, H1, H, 0, L.W2, H, 0, nullptr, H, H2, H, train ? Z2 : nullptr, L.b2, 1, 0.f, 1, st);
+        if (!e) e = gemm(M, H, H, H2, H, 0, L.W3, H, 0, nullptr, H, H3, H, train ? Z3 : nullptr, L.b3, 1, 0.f, 1, st);
+        if (!e) e = gemm(M, FOUTP, H, H3, H, 0, L.W4, FOUTP, 0, Yp, FOUTP, nullptr, 0, nullptr, L.b4, 0, 0.f, 1, st);
+        return e;
+    }
+    cudaError_t backward(int M, const float* T, float w1, cudaStream_t st) {
+        cudaMemsetAsync(loss, 0, sizeof(double), st);
+        k_loss_grad<<<div_up(M, 256), 256, 0, st>>>(M, Yp, T, w1, dYb, dY, loss);
+        const int split = max(1, min(64, M / 512));
+        cudaMemsetAsync(dW4, 0, sizeof(float) * H * FOUTP, st);
+        cudaMemsetAsync(dW3, 0, sizeof(float) * H * H, st);
+        cudaMemsetAsync(dW2, 0, sizeof(float) * H * H, st);
+        cudaMemsetAsync(dW1, 0, sizeof(float) * FINP * H, st);
+        const int Kb = M;   // batch as K; the tile loader zero-fills k >= K
+        cudaError_t e = gemm(H, FOUTP, Kb, H3, H, 1, dYb, FOUTP, 0, dW4, FOUTP, nullptr, 0, nullptr, nullptr, 0, 1.f,
+                             split, st);
+        k_colsum<<<1, 128, 0, st>>>(M, FOUTP, dY, db + 3 * H);
+        // layer 3
+        if (!e) e = gemm(M, H, FOUTP, dYb, FOUTP, 0, L.W4, FOUTP, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
+        k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z3, dZ, dZb);
+        if (!e) e = gemm(H, H, Kb, H2, H, 1, dZb, H, 0, dW3, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db + 2 * H);
+        // layer 2
+        if (!e) e = gemm(M, H, H, dZb, H, 0, L.W3, H, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
+        k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z2, dZ, dZb);
+        if (!e) e = gemm(H, H, Kb, H1, H, 1, dZb, H, 0, dW2, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db + 1 * H);
+        // layer 1
+        if (!e) e = gemm(M, H, H, dZb, H, 0, L.W2, H, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
+        k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z1, dZ, dZb);
+        if (!e) e = gemm(FINP, H, Kb, Xb, FINP, 1, dZb, H, 0, dW1, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db);
+        k_grad_to_vec<<<div_up(H * H, 256), 256, 0, st>>>(dW1, db, dW2, db + H, dW3, db + 2 * H, dW4, db + 3 * H, g);
+        return e ? e : cudaGetLastError();
+    }
+};
+
+namespace mps {
+// used by the solver: forward of a created MLP on M rows of features
+cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st) {
+    for (int r = 0; r < M; r += m->maxb) {
+        const int cnt = min(m->maxb, M - r);
+        cudaError_t e = m->forward(cnt, X + (size_t)r * FIN, st, false);
+        if (e) return e;
+        k_unpad_output<<<div_up(cnt * FOUT, 256), 256, 0, st>>>(cnt, m->Yp, Y + (size_t)r * FOUT);
+    }
+    return cudaGetLastError();
+}
+}  // namespace mps
+
+extern "C" {
+
+CCTStatusType mps_gemm_bf16(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb,
+                            int transB, float* C, int ldc, void* Cb, int ldcb, float* Cz, const float* bias, int act,
+                            float beta, int split_k, void* stream) {
+    if (split_k > 1 && (act != 0 || beta != 1.f || !C)) return CCT_PARAMERR;
+    cudaError_t e = gemm(M, N, K, (const bf16*)A, lda, transA, (const bf16*)B, ldb, transB, C, ldc, (bf16*)Cb, ldcb, Cz,
+                         bias, act, beta, split_k, (cudaStream_t)stream);
+    return e == cudaErrorInvalidValue ? CCT_PARAMERR : cuda_status(e);
+}
+
+CCTStatusType mps_mlp_create(int max_batch, unsigned long long seed, MpsMlp** out) {
+    if (max_batch <= 0 || !out) return CCT_PARAMERR;
+    MpsMlp* m = new MpsMlp();
+    if (m->init(max_batch) != cudaSuccess) {
+        m->release();
+        delete m;
+        return CCT_MEMERR;
+    }
+    // PyTorch-Linear-style uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)), last layer x0.1
+    std::vector<float> p(MPS_MLP_PARAMS);
+    unsigned long long s = seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto rnd = [&]() {
+        s = s * 6364136223846793005ULL + 1442695040888963407ULL;
+        return (float)((s >> 11) * (1.0 / 9007199254740992.0)) * 2.f - 1.f;
+    };
+    size_t o = 0;
+    const int fan[4] = {FIN, H, H, H}, outs[4] = {H, H, H, FOUT};
+    for (int l = 0; l < 4; ++l) {
+        const float b = 1.f / sqrtf((float)fan[l]) * (l == 3 ? 0.1f : 1.f);
+        for (int i = 0; i < fan[l] * outs[l]; ++i) p[o++] = b * rnd();
+        for (int i = 0; i < outs[l]; ++i) p[o++] = b * rnd();
+    }
+    if (mps_mlp_set_params(m, p.data()) != CCT_NOERR) {
+        m->release();
+        delete m;
+        return CCT_CUDAERR;
+    }
+    *out = m;
+    return CCT_NOERR;
+}
+
+void mps_mlp_destroy(MpsMlp* m) {
+    if (!m) return;
+    m->release();
+    delete m;
+}
+
+CCTStatusType mps_mlp_set_params(MpsMlp* m, const float* host_params) {
+    if (!m || !host_params) return CCT_PARAMERR;
+    cudaError_t e = cudaMemcpy(m->p, host_params, sizeof(float) * MPS_MLP_PARAMS, cudaMemcpyHostToDevice);
+    if (!e) e = m->sync_layers(0);
+    if (!e) e = cudaDeviceSynchronize();
+    m->t = 0;
+    cudaMemset(m->m, 0, sizeof(float) * MPS_MLP_PARAMS);
+    cudaMemset(m->v, 0, sizeof(float) * MPS_MLP_PARAMS);
+    return cuda_status(e);
+}
+
+CCTStatusType mps_mlp_get_params(MpsMlp* m, float* host_params) {
+    if (!m || !host_params) return CCT_PARAMERR;
+    return cuda_status(cudaMemcpy(host_params, m->p, sizeof(float) * MPS_MLP_PARAMS, cudaMemcpyDeviceToHost));
+}
+
+CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* stream) {
+    if (!m || M < 0) return CCT_PARAMERR;
+    if (M == 0) return CCT_NOERR;
+    return cuda_status(mlp_forward(m, M, X, Y, (cudaStream_t)stream));
+}
+
+CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T, float w1, float* grad,
+                                float* host_loss, void* stream) {
+    if (!m || M <= 0 || M > m->maxb) return CCT_PARAMERR;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = m->forward(M, X, st, true);
+    if (!e) e = m->backward(M, T, w1, st);
+    if (!e && grad) e = cudaMemcpyAsync(grad, m->g, sizeof(float) * MPS_MLP_PARAMS, cudaMemcpyDeviceToDevice, st);
+    if (!e) e = cudaMemcpyAsync(m->h_loss, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    if (!e && host_loss) *host_loss = (float)(*m->h_loss / M);
+    return cuda_status(e);
+}
+
+CCTStatusType mps_mlp_train_step(MpsMlp* m, int M, const float* X, const float* T, float w1, float lr,
+                                 float* host_loss, void* stream) {
+    if (!m || M <= 0 || M > m->maxb) return CCT_PARAMERR;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = m->forward(M, X, st, true);
+    if (!e) e = m->backward(M, T, w1, st);
+    if (e) return cuda_status(e);
+    m->t += 1;
+    const float b1t = powf(0.9f, (float)m->t), b2t = powf(0.999f, (float)m->t);
+    k_adam<<<div_up(MPS_MLP_PARAMS, 256), 256, 0, st>>>(MPS_MLP_PARAMS, m->p, m->g, m->m, m->v, lr, b1t, b2t);
+    e = m->sync_layers(st);
+    if (!e && host_loss) {
+        e = cudaMemcpyAsync(m->h_loss, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (!e) e = cudaStreamSynchronize(st);
+        if (!e) *host_loss = (float)(*m->h_loss / M);
+    }
+    return cuda_status(e ? e : cudaGetLastError());
+}
+
+}  // extern "C"

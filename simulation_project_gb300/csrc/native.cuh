@@ -80,12 +80,16 @@ struct Dev {
     unsigned* red_count;       // last-block counters
     unsigned* err;
     int* istat;                // [0] longest neighbour row
+    double* pprev;             // warm-start pressure of the step (learned path)
+    float* feat;               // [n][12] learned features
+    float* mlp_out;            // [n][2] network outputs
+    float* targets;            // [n][2] training targets
 };
 
 // device scalar slots
 enum {
     S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_BNORM, S_TOL, S_CONV, S_ITER, S_RZNEW, S_RNORM, S_R0NORM,
-    S_IRTOL, S_TMP0, S_TMP1, S_COUNT
+    S_IRTOL, S_TMP0, S_TMP1, S_PSCALE, S_COUNT
 };
 
 }  // namespace mps

@@ -587,6 +587,28 @@ __global__ void k_eos(const __grid_constant__ Dev d) {
 // y = A x for interior rows (y = 0 elsewhere); A = diag - coef * W.  MODE 0: plain
 // (+ dot x.y -> S_PQ, alpha = rz / pq); MODE 1: residual r = b - A x (FP64 out),
 // norms -> S_RR, S_BNORM.
+// One warp per row.  A row (capacity K, a multiple of 128) is read as 16-byte vectors:
+// lane l loads entries [128c + 4l, 128c + 4l + 4) of chunk c, so each warp load moves
+// 512 contiguous bytes of indices (and of FP32 weights; FP64 weights take two).  All
+// chunks of the row are issued before the first gather, with streaming (evict-first)
+// loads so the matrix does not displace the x vector from L2.
+template <class TW> struct WVec;
+template <> struct WVec<float> {
+    float v[4];
+    __device__ __forceinline__ void load(const float* p) {
+        const float4 t = __ldcs((const float4*)p);
+        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+    }
+};
+template <> struct WVec<double> {
+    double v[4];
+    __device__ __forceinline__ void load(const double* p) {
+        const double2 a = __ldcs((const double2*)p), b = __ldcs((const double2*)(p + 2));
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+};
+constexpr int kMaxRowChunks = 4;   // rows up to 512 entries
+
 template <class TW, class TX, class TY, int MODE>
 __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w,
                                               const TX* __restrict__ x, TY* __restrict__ y, const double* __restrict__ b,
@@ -597,6 +619,7 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
     const int nw = (gridDim.x * blockDim.x) >> 5;
     double part0 = 0.0, part1 = 0.0;
     const double coef = d.c.coef_lap;
+    using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE == 1), double, float>::type;
     for (int i = gw; i < d.n; i += nw) {
         if (!d.inner[i]) {
             if (lane == 0) y[i] = TY(0);
@@ -604,9 +627,27 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
         }
         const int cnt = d.nbr_cnt[i];
         const size_t base = (size_t)i * d.K;
-        using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE == 1), double, float>::type;
+        int4 id[kMaxRowChunks];
+        WVec<TW> wv[kMaxRowChunks];
+#pragma unroll
+        for (int c = 0; c < kMaxRowChunks; ++c) {
+            const int k = c * 128 + 4 * lane;
+            if (k < cnt) {
+                id[c] = __ldcs((const int4*)(d.nbr + base + k));
+                wv[c].load(w + base + k);
+            }
+        }
         TA acc = TA(0);
-        for (int k = lane; k < cnt; k += 32) acc += (TA)w[base + k] * (TA)x[d.nbr[base + k]];
+#pragma unroll
+        for (int c = 0; c < kMaxRowChunks; ++c) {
+            const int k = c * 128 + 4 * lane;
+            if (k < cnt) {
+                acc += (TA)wv[c].v[0] * (TA)x[id[c].x];
+                if (k + 1 < cnt) acc += (TA)wv[c].v[1] * (TA)x[id[c].y];
+                if (k + 2 < cnt) acc += (TA)wv[c].v[2] * (TA)x[id[c].z];
+                if (k + 3 < cnt) acc += (TA)wv[c].v[3] * (TA)x[id[c].w];
+            }
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) {
@@ -735,6 +776,103 @@ __global__ void k_unpack_state(const __grid_constant__ Dev d, double* p3, double
     p3[3 * (size_t)i] = p.x; p3[3 * (size_t)i + 1] = p.y; p3[3 * (size_t)i + 2] = p.z;
     v3[3 * (size_t)i] = v.x; v3[3 * (size_t)i + 1] = v.y; v3[3 * (size_t)i + 2] = v.z;
     pr[i] = d.press[i];
+}
+
+// ---------------------------------------------------------------------------
+// learned initial guess / scaling
+// ---------------------------------------------------------------------------
+// pressure scale of the step: max(rms of the warm start over interior rows, rho |g| l0)
+__global__ void __launch_bounds__(256) k_pressure_scale(const __grid_constant__ Dev d, int slot) {
+    double a = 0.0, b = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)
+        if (d.inner[i]) {
+            a += d.press[i] * d.press[i];
+            b += 1.0;
+        }
+    double v[2] = {a, b}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        const double g = sqrt(d.c.g[0] * d.c.g[0] + d.c.g[1] * d.c.g[1] + d.c.g[2] * d.c.g[2]);
+        const double floor_p = d.c.rho * (g > 0 ? g : 1.0) * d.c.l0;
+        const double rms = out[1] > 0 ? sqrt(out[0] / out[1]) : 0.0;
+        d.scal[S_PSCALE] = rms > floor_p ? rms : floor_p;
+    }
+}
+
+// 12 features per particle (FP32); r holds the FP64 initial residual b - A p_prev
+__global__ void k_features(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double ps = d.scal[S_PSCALE];
+    float* f = d.feat + 12 * (size_t)i;
+    const double dg = d.diag[i];
+    f[0] = (float)((d.pnd[i] - d.c.n0_pnd) / d.c.n0_pnd * 10.0);
+    f[1] = (float)(d.feat_aux[4 * (size_t)i + 1] * d.c.dt * 10.0);
+    const int t = d.wid[i];
+    if (t >= 0 && d.wdist[i] < d.c.re_lap) {
+        const double* w = d.wdir + 3 * (size_t)i;
+        const double l = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        f[2] = (float)(d.wdist[i] / d.c.re_lap);
+        f[3] = l > 0 ? (float)(w[0] / l) : 0.f;
+        f[4] = l > 0 ? (float)(w[1] / l) : 0.f;
+        f[5] = l > 0 ? (float)(w[2] / l) : 0.f;
+    } else {
+        f[2] = 1.f; f[3] = 0.f; f[4] = 0.f; f[5] = 0.f;
+    }
+    f[6] = (float)(d.press[i] / ps);
+    f[7] = (float)(d.feat_aux[4 * (size_t)i] / ps);
+    f[8] = (float)(d.rhs[i] / dg / ps);
+    f[9] = (float)(d.feat_aux[4 * (size_t)i + 2] / 250.0);
+    f[10] = (float)(d.inner[i] ? d.r[i] / dg / ps : 0.0);
+    const dbl4 v = d.vel[i];
+    f[11] = (float)(sqrt(v.x * v.x + v.y * v.y + v.z * v.z) * d.c.dt / d.c.l0 * 100.0);
+}
+
+// initial guess p = p_prev + scale * y0, preconditioner M^-1 = exp(y1) / diag
+__global__ void k_learned_apply(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    if (!d.inner[i]) {
+        d.press[i] = 0.0;
+        d.minv[i] = 0.0;
+        return;
+    }
+    const float y0 = d.mlp_out[2 * (size_t)i], y1 = d.mlp_out[2 * (size_t)i + 1];
+    const double inc = (double)fminf(fmaxf(y0, -50.f), 50.f) * d.scal[S_PSCALE];
+    d.press[i] = d.pprev[i] + (isfinite(inc) ? inc : 0.0);
+    const double s = exp((double)fminf(fmaxf(isfinite(y1) ? y1 : 0.f, -2.3f), 2.3f));
+    d.minv[i] = s / d.diag[i];
+}
+
+// training targets after a plain solve: (p - p_prev) / scale and the log of the
+// diagonal scale that maps the initial residual onto the error, clamped to [0.1, 10]
+__global__ void k_targets(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    float* t = d.targets + 2 * (size_t)i;
+    if (!d.inner[i]) {
+        t[0] = nanf("");
+        t[1] = nanf("");
+        return;
+    }
+    const double ps = d.scal[S_PSCALE];
+    const double e = d.press[i] - d.pprev[i];
+    t[0] = (float)(e / ps);
+    const double r0n = (double)d.feat[12 * (size_t)i + 10];   // r0 / (diag ps)
+    const double en = e / ps;
+    double ls = 0.0;
+    if (fabs(r0n) > 1e-6) {
+        double s = en / r0n;
+        s = s < 0.1 ? 0.1 : (s > 10.0 ? 10.0 : s);
+        ls = log(s);
+    }
+    t[1] = (float)ls;
+}
+
+__global__ void k_restore_plain(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    d.press[i] = d.inner[i] ? d.pprev[i] : 0.0;
+    d.minv[i] = d.inner[i] ? 1.0 / d.diag[i] : 0.0;
 }
 
 __global__ void k_to_float(int n, const double* a, float* b) {

@@ -19,8 +19,10 @@
 #include <vector>
 
 #include "native_kernels.cuh"
+#include "../../include/mps_learned.h"
 
 namespace mps {
+cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st);
 
 namespace {
 
@@ -104,6 +106,8 @@ struct Solver {
     double* stage = nullptr;   // host-exchange staging (7 n doubles)
     // learned parameters (optional)
     bool learned_ready = false;
+    bool collect = false;
+    MpsMlp* mlp = nullptr;
 
     template <class T>
     cudaError_t mk(T** ptr, size_t count) {
@@ -121,7 +125,9 @@ struct Solver {
         d.box = *box;
         d.cells = box->m_GridSize.x * box->m_GridSize.y * box->m_GridSize.z;
         if (d.cells <= 0 || nmax <= 0) return CCT_PARAMERR;
+        // row capacity: a multiple of 128 (16-byte vector rows), at most 512
         d.K = opt.max_neighbours > 0 ? opt.max_neighbours : 384;
+        d.K = std::min(512, std::max(128, (d.K + 127) / 128 * 128));
         d.KG = 64;
         Consts& c = d.c;
         const CParameter& P = param;
@@ -183,6 +189,10 @@ struct Solver {
         e = e ? e : mk(&d.err, 1);
         e = e ? e : mk(&d.istat, 4);
         e = e ? e : mk(&stage, 7 * N);
+        e = e ? e : mk(&d.pprev, N);
+        e = e ? e : mk(&d.feat, 12 * N);
+        e = e ? e : mk(&d.mlp_out, 2 * N);
+        e = e ? e : mk(&d.targets, 2 * N);
         e = e ? e : mk(&keep, N + 1);
         e = e ? e : mk(&rank, N + 1);
         if (e != cudaSuccess) return CCT_MEMERR;
@@ -212,6 +222,8 @@ struct Solver {
         if (h_scal) cudaFreeHost(h_scal);
         if (h_int) cudaFreeHost(h_int);
         timer.release();
+        if (mlp) mps_mlp_destroy(mlp);
+        mlp = nullptr;
         if (st) cudaStreamDestroy(st);
     }
 
@@ -395,7 +407,37 @@ struct Solver {
         } else {
             k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
             k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
+            const bool use_learned = learned_ready && opt.learned;
+            if (use_learned || collect) {
+                timer.mark(PH_LEARNED, st);
+                cudaMemcpyAsync(d.pprev, d.press, sizeof(double) * d.n, cudaMemcpyDeviceToDevice, st);
+                if (fp64())
+                    k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
+                                                                                  d.r, d.rhs, 2);
+                else
+                    k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.press,
+                                                                                 d.r, d.rhs, 2);
+                k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
+                k_features<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                if (use_learned) {
+                    if (mlp_forward(mlp, d.n, d.feat, d.mlp_out, st)) return CCT_CUDAERR;
+                    k_learned_apply<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                }
+                timer.mark(PH_SETUP, st);
+            }
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
+            if (use_learned && S.cg_relres > opt.cg_rtol) {
+                // the learned solve did not reach the tolerance: plain Jacobi-CG from the warm start
+                k_restore_plain<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                MpsStepStats S2{};
+                if ((rc = fp64() ? solve_fp64(S2) : solve_ir(S2))) return rc;
+                S.cg_iterations += S2.cg_iterations;
+                S.ir_passes += S2.ir_passes;
+                S.cg_relres = S2.cg_relres;
+                S.error_flags = (S.error_flags & ~MPS_ERR_CG) | S2.error_flags;
+                S.fallback = 1;
+            }
+            if (collect) k_targets<<<blocks_for(d.n), kBlock, 0, st>>>(d);
         }
         timer.mark(PH_CORRECT, st);
         k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -498,9 +540,12 @@ struct Solver {
             const double rn = h_scal[S_RNORM];
             S.cg_relres = bnorm > 0 ? rn / bnorm : 0.0;
             if (bnorm == 0.0 || rn <= opt.cg_rtol * bnorm || outer >= opt.ir_max_outer) break;
-            // inner FP32 solve of A d = r / ||r|| to ir_inner_rtol
+            // inner FP32 solve of A d = r / ||r||: to the reduction still needed (with a
+            // 0.3 margin), but not below what FP32 CG reliably reaches (ir_inner_rtol)
+            const double need = 0.3 * opt.cg_rtol * bnorm / rn;
+            const double inner_tol = std::max(need, opt.ir_inner_rtol);
             k_cg_start<float><<<kRedBlocks, 256, 0, st>>>(d, d.r32, d.z32, d.p32, d.r, 1.0 / rn, nullptr, d.m32, d.d32, 3,
-                                                          opt.ir_inner_rtol, opt.cg_max_iter);
+                                                          inner_tol, opt.cg_max_iter);
             const int it = cg_loop<float, float, float>(d.d32, d.r32, d.z32, d.p32, d.q32, w, nullptr, d.m32,
                                                         opt.cg_max_iter);
             if (it < 0) return CCT_CUDAERR;
@@ -556,7 +601,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->compressibility = 1e-9;
     o->cg_rtol = 1e-8;
     o->cg_max_iter = 5000;
-    o->ir_inner_rtol = 1e-4;
+    o->ir_inner_rtol = 2e-6;
     o->ir_max_outer = 12;
     o->max_neighbours = 384;
     o->check_every = 8;
@@ -686,13 +731,32 @@ CCTStatusType mps_solver_stream(MpsSolver* s, void** stream) {
 }
 
 CCTStatusType mps_solver_set_learned(MpsSolver* s, const float* params, int count) {
-    (void)s; (void)params; (void)count;
-    return CCT_PARAMERR;
+    if (!s || !params || count != MPS_MLP_PARAMS) return CCT_PARAMERR;
+    Solver& v = s->s;
+    if (!v.mlp) {
+        CCTStatusType rc = mps_mlp_create(std::min(v.nmax, 1 << 18), 1, &v.mlp);
+        if (rc) return rc;
+    }
+    CCTStatusType rc = mps_mlp_set_params(v.mlp, params);
+    if (rc) return rc;
+    v.learned_ready = true;
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_solver_collect(MpsSolver* s, int on) {
+    if (!s) return CCT_PARAMERR;
+    s->s.collect = on != 0;
+    return CCT_NOERR;
 }
 
 CCTStatusType mps_solver_learned_samples(MpsSolver* s, float* features, float* targets, int* n) {
-    (void)s; (void)features; (void)targets; (void)n;
-    return CCT_PARAMERR;
+    if (!s || !n) return CCT_PARAMERR;
+    mps::Dev& d = s->s.d;
+    *n = d.n;
+    cudaError_t e = cudaStreamSynchronize(s->s.st);
+    if (!e && features) e = cudaMemcpy(features, d.feat, sizeof(float) * 12 * d.n, cudaMemcpyDeviceToHost);
+    if (!e && targets) e = cudaMemcpy(targets, d.targets, sizeof(float) * 2 * d.n, cudaMemcpyDeviceToHost);
+    return mps::cuda_status(e);
 }
 
 }  // extern "C"

@@ -57,6 +57,7 @@ _SIGS = {
     "mps_solver_download_state": (C.c_int, [P, P, P, P]),
     "mps_solver_set_learned": (C.c_int, [P, P, C.c_int]),
     "mps_solver_learned_samples": (C.c_int, [P, P, P, C.POINTER(C.c_int)]),
+    "mps_solver_collect": (C.c_int, [P, C.c_int]),
 }
 _bound = False
 
@@ -170,6 +171,21 @@ class Solver:
     def set_learned(self, params):
         p = np.ascontiguousarray(params, dtype=np.float32)
         _check(_lib().mps_solver_set_learned(self.h, p.ctypes.data, p.size), "mps_solver_set_learned")
+
+    def collect(self, on=True):
+        _check(_lib().mps_solver_collect(self.h, 1 if on else 0), "mps_solver_collect")
+
+    def learned_samples(self):
+        """(features [n,12], targets [n,2]) of the last PPE solve, interior rows only."""
+        nmax = self.scene.n
+        f = np.zeros((nmax, 12), np.float32)
+        t = np.zeros((nmax, 2), np.float32)
+        n = C.c_int()
+        _check(_lib().mps_solver_learned_samples(self.h, f.ctypes.data, t.ctypes.data, C.byref(n)),
+               "mps_solver_learned_samples")
+        f, t = f[:n.value], t[:n.value]
+        ok = np.isfinite(t).all(1) & np.isfinite(f).all(1)
+        return f[ok], t[ok]
 
     def upload_state(self, pos, vel, press):
         _check(_lib().mps_solver_upload_state(self.h, pos.ctypes.data, vel.ctypes.data, press.ctypes.data),

@@ -1,0 +1,116 @@
+"""The learned PPE initial guess / scaling: BF16 tensor-core GEMM, MLP forward and
+backward against the numpy oracle (oracle/mlp_oracle.py, same BF16 rounding points),
+training on the GPU, and what the trained network gains inside the solver."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from simulation_project_gb300 import lib, scenes
+from simulation_project_gb300.lib import DeviceArray
+from simulation_project_gb300.learned import Mlp, gemm_bf16, collect_samples, train
+from simulation_project_gb300.solver import Solver
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import mlp_oracle as mo  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def to_bf16_bits(a):
+    a = np.ascontiguousarray(np.asarray(a, np.float32))
+    b = a.view(np.uint32).astype(np.uint64)
+    return (((b + 0x7FFF + ((b >> 16) & 1)) >> 16) & 0xFFFF).astype(np.uint16)
+
+
+@pytest.mark.parametrize("M,N,K,ta,tb,split", [(64, 64, 32, 0, 0, 1), (100, 128, 48, 0, 0, 1), (128, 16, 1000, 1, 0, 8),
+                                               (333, 128, 16, 0, 1, 1), (16, 128, 517, 1, 0, 4)])
+def test_gemm_bf16_matches_numpy(M, N, K, ta, tb, split):
+    rng = np.random.default_rng(M + N + K)
+    A = rng.normal(0, 1, (K, M) if ta else (M, K)).astype(np.float32)
+    B = rng.normal(0, 1, (N, K) if tb else (K, N)).astype(np.float32)
+    dA, dB = DeviceArray.from_host(to_bf16_bits(A)), DeviceArray.from_host(to_bf16_bits(B))
+    C = DeviceArray((M, N), np.float32)
+    C.fill_bytes(0)
+    gemm_bf16(M, N, K, dA.ptr, M if ta else K, ta, dB.ptr, K if tb else N, tb, C.ptr, N, beta=1.0 if split > 1 else 0.0,
+              split=split)
+    Am = mo.bf16(A.T if ta else A)
+    Bm = mo.bf16(B.T if tb else B)
+    ref = Am @ Bm
+    got = C.download()
+    assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max() + 1e-3 * np.sqrt(K) * 1e-2
+
+
+def _net(seed=3):
+    m = Mlp(max_batch=4096, seed=seed)
+    p = m.params().astype(np.float64)
+    return m, p
+
+
+def test_mlp_forward_matches_oracle():
+    m, p = _net()
+    X = np.random.default_rng(1).normal(0, 1, (1000, 12)).astype(np.float32)
+    dX, dY = DeviceArray.from_host(X), DeviceArray((1000, 2), np.float32)
+    m.forward(dX.ptr, dY.ptr, 1000)
+    ref = mo.forward(p, X)
+    got = dY.download()
+    assert np.abs(got - ref).max() <= 2e-2 * np.abs(ref).max() + 1e-4
+
+
+def test_mlp_gradient_matches_oracle():
+    m, p = _net(seed=5)
+    rng = np.random.default_rng(2)
+    X = rng.normal(0, 1, (2048, 12)).astype(np.float32)
+    T = rng.normal(0, 1, (2048, 2)).astype(np.float32)
+    dX, dT = DeviceArray.from_host(X), DeviceArray.from_host(T)
+    g = DeviceArray((mo.NPARAMS,), np.float32)
+    loss = m.loss_grad(dX.ptr, dT.ptr, 2048, g.ptr)
+    ref_loss, ref_g = mo.loss_grad(p, X, T)
+    got = g.download().astype(np.float64)
+    assert abs(loss - ref_loss) <= 1e-3 * abs(ref_loss)
+    # per-layer relative error of the gradient blocks
+    o = 0
+    for fi, fo in ((12, 128), (128, 128), (128, 128), (128, 2)):
+        for size in (fi * fo, fo):
+            a, b = got[o:o + size], ref_g[o:o + size]
+            assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b) + 1e-7, (o, size)
+            o += size
+    assert o == mo.NPARAMS
+
+
+def test_training_reduces_loss_on_a_smooth_target():
+    rng = np.random.default_rng(4)
+    X = rng.normal(0, 1, (40000, 12)).astype(np.float32)
+    T = np.stack([np.tanh(X[:, 0] + 0.5 * X[:, 1] * X[:, 2]), 0.3 * X[:, 3] - 0.2 * X[:, 4] ** 2], 1).astype(np.float32)
+    p, info = train(X, T, epochs=6, batch=4096, lr=3e-3)
+    assert info["val_loss_after"] < 0.2 * info["val_loss_before"], info
+
+
+def test_learned_solver_converges_and_reports_gain():
+    """Trains on the plain solver's own solves of a small bucket, then runs the same
+    steps with and without the network: both must reach 1e-8; the iteration counts
+    and whether the learned path needed its fallback are printed."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=8)
+    f, t = collect_samples(sc, steps=6, precision="fp64")
+    p, info = train(f, t, epochs=6, batch=4096, lr=2e-3)
+    assert info["val_loss_after"] < info["val_loss_before"]
+    plain = Solver(sc, precision="fp32_ir")
+    learned = Solver(sc, precision="fp32_ir", learned=1)
+    learned.set_learned(p)
+    it_p, it_l = 0, 0
+    for i in range(8):
+        sp = plain.step(i)
+        sl = learned.step(i)
+        assert sp["cg_relres"] <= 1e-8 and sl["cg_relres"] <= 1e-8
+        assert sl["error_flags"] == 0
+        if i >= 2:
+            it_p += sp["cg_iterations"]
+            it_l += sl["cg_iterations"]
+    print(f"\nCG iterations steps 2-7: plain {it_p}, learned {it_l}, saved {it_p - it_l} "
+          f"({100.0 * (it_p - it_l) / max(it_p, 1):.1f}%); training {info}")
+    a, b = plain.state(), learned.state()
+    assert np.array_equal(a["id"], b["id"])
+    pm = np.abs(a["press"]).max()
+    # both converged to 1e-8 residual: pressures agree to the solve tolerance
+    assert np.abs(a["press"] - b["press"]).max() <= 1e-3 * pm
