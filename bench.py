@@ -109,6 +109,34 @@ def build_scene(l0, seed=4):
     return scenes.rotating_bucket(l0=l0, dt=5e-5, seed=seed, n_drag=64, drag_seed=3)
 
 
+def barrier():
+    """Host barrier over the replica ranks (no-op for one process)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
+def combine_replicas(units, ms, steps):
+    """Whole-job throughput of independent replicas: the particle-steps every rank
+    completed over the slowest rank's timed region.  `units` and `ms` are the ranks'
+    own (particle-steps, milliseconds) in a list over ranks."""
+    slowest = max(ms)
+    return {"value": sum(units) / (slowest / 1e3), "ms_per_step": slowest / steps}
+
+
+def gather_replicas(res):
+    """Replace a rank's own value / ms_per_step with the whole-job numbers (all ranks
+    call this; a gloo group carries two numbers per rank, nothing on the data path)."""
+    import torch.distributed as dist
+    world = dist.get_world_size()
+    mine = (res["units"], res["ms_per_step"] * res["steps"])
+    rows = [None] * world
+    dist.all_gather_object(rows, mine)
+    res.update(combine_replicas([u for u, _ in rows], [m for _, m in rows], res["steps"]))
+    res["n_gpus"] = world
+    return res
+
+
 def time_steps(solver, steps, warmup, first_step=0):
     from simulation_project_gb300 import lib
     for i in range(warmup):
@@ -116,7 +144,9 @@ def time_steps(solver, steps, warmup, first_step=0):
     stream = C.c_void_p(solver.stream())
     ev0, ev1 = lib.Event(), lib.Event()
     lib.call("mps_device_sync")
+    barrier()
     stats = []
+    launches0 = lib.kernel_launches()
     ev0.record(_S(stream))
     t0 = time.perf_counter()
     for i in range(steps):
@@ -124,6 +154,9 @@ def time_steps(solver, steps, warmup, first_step=0):
     ev1.record(_S(stream))
     lib.call("mps_device_sync")
     wall = time.perf_counter() - t0
+    barrier()
+    if stats:
+        stats[0]["launches_in_region"] = lib.kernel_launches() - launches0
     return ev0.elapsed_ms(ev1), wall, stats
 
 
@@ -167,8 +200,14 @@ def run_gpu(args):
     plain.close()
     pps_plain = n * args.steps / (ms_plain / 1e3)
 
+    # FP32 / FP64-refined solver without the network
+    ir = Solver(scene, precision="fp32_ir", profile=0)
+    ms_ir, _, st_ir = time_steps(ir, args.steps, args.warmup)
+    ir.close()
+    pps_ir = n * args.steps / (ms_ir / 1e3)
+
     # learned FP32 / FP64-refined solver (metric numerator), with phase timing
-    fast = Solver(scene, precision="fp32_ir", profile=1, learned=1 if params is not None else 0)
+    fast = Solver(scene, precision="fp32_ir", profile=1, learned=args.learned_mode if params is not None else 0)
     if params is not None:
         fast.set_learned(params)
     clocks = ClockSampler(local)
@@ -202,7 +241,8 @@ def run_gpu(args):
 
     result = {
         "metric": "particle-steps/s @1M on 1 GB300, learned-precond vs plain CG at 1e-8 PPE residual",
-        "value": pps_fast * world,
+        "value": pps_fast,
+        "units": n * args.steps,
         "unit": "particle-steps/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -222,6 +262,11 @@ def run_gpu(args):
                        "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_plain])),
                        "relres_max": float(max(s["cg_relres"] for s in st_plain))},
         "speedup_vs_plain_fp64": pps_fast / pps_plain,
+        "fp32_ir_without_network": {"value": pps_ir, "ms_per_step": ms_ir / args.steps,
+                                    "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_ir])),
+                                    "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_ir]))},
+        "network_iterations_saved_per_step": float(np.mean([s["cg_iterations"] for s in st_ir]) -
+                                                   np.mean([s["cg_iterations"] for s in st_fast])),
         "fast_solver": {"cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_fast])),
                         "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_fast])),
                         "relres_max": float(max(s["cg_relres"] for s in st_fast)),
@@ -231,7 +276,7 @@ def run_gpu(args):
         "learned_training": train_info,
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": int(sum(s["spmv_launches"] for s in st_fast) * 3 + args.steps * 40),
+        "gpu_launches": int(st_fast[0]["launches_in_region"]),
         "clocks": clk,
     }
     if rank == 0 and world == 1:
@@ -239,6 +284,22 @@ def run_gpu(args):
     if log:
         result["notes"] = log
     return result
+
+
+def run_profile_case(args):
+    """Only the FP32-IR solver steps (no training, no other arms): the command the ncu
+    captures under profiles/ run."""
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.solver import Solver
+    lib.load()
+    scene = build_scene(args.l0)
+    s = Solver(scene, precision="fp64" if args.fp64 else "fp32_ir", profile=1)
+    ms, _, st = time_steps(s, args.steps, args.warmup)
+    s.close()
+    print(json.dumps({"profile_case": True, "particles": scene.n, "ms_per_step": ms / args.steps,
+                      "phases": {k: st[-1][k] for k in st[-1] if k.startswith("ms_")},
+                      "spmv_launches": st[-1]["spmv_launches"], "nnz": st[-1]["nnz"]}))
+    return 0
 
 
 def run_e2e(solver, args):
@@ -350,24 +411,30 @@ def main():
     ap.add_argument("--l0", type=float, default=0.002)
     ap.add_argument("--train-steps", type=int, default=6)
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-mode", type=int, default=1, help="bit 0 initial guess, bit 1 diagonal scaling")
+    ap.add_argument("--profile-case", action="store_true", help="only the solver steps (for ncu captures)")
+    ap.add_argument("--fp64", action="store_true", help="with --profile-case: the plain FP64 solver")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))
+    if args.profile_case:
+        return run_profile_case(args)
     if args.impl == "reference":
         if rank != 0:
             return 0
         print(json.dumps(run_reference(args)))
         return 0
-    res = run_gpu(args)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if world > 1:
+        # replicas: one independent bucket per GPU; gloo carries only barriers and the
+        # final two numbers per rank
         import torch.distributed as dist
         dist.init_process_group("gloo")
-        vals = [None] * world
-        dist.all_gather_object(vals, (res["value"] / world, res["ms_per_step"]))
-        res["value"] = sum(v for v, _ in vals)
-        res["ms_per_step"] = max(m for _, m in vals)
+    res = run_gpu(args)
+    if world > 1:
+        gather_replicas(res)
         dist.destroy_process_group()
+    res.pop("units", None)
     if rank == 0:
         print(json.dumps(res))
     return 0

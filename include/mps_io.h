@@ -1,0 +1,47 @@
+/*
+ * mps_io.h - the reference solver's input formats and setup helpers (host code).
+ *
+ *   mps_read_parameter_file  IO::Load(parameter file), radix/SPVSOLVER/MultiGPUSolver/IO.cpp:65-446
+ *                            positional whitespace-separated fields; every optional
+ *                            trailing group is read only while input remains, and
+ *                            missing groups take the reference's defaults.
+ *   mps_read_particle_file   IO::Load(particle file), IO.cpp:6-63: rows of
+ *                            "x y z vx vy vz P n T nu solidRate type(0|1|2)", no
+ *                            header, IDs 0..N-1 in file order; call with out = NULL to
+ *                            count, then with a buffer of that capacity.
+ *   mps_read_stl             IO::Load(model list) + CSTLSerializer::Load, IO.cpp:470-523,
+ *                            STLSerializer.cpp:225-357: ASCII when the first token is
+ *                            "solid", else binary (80-byte header, uint32 count, 50-byte
+ *                            records); normals recomputed from the vertices with the
+ *                            reference's float arithmetic (CalcTriangleNormal,
+ *                            IO.cpp:449-467); the model offset is added to every vertex
+ *                            (MultiGPUHandler.cpp:713-735).  out = NULL counts.
+ *   mps_lambda_table         CalculateLambdaValueLocal, MultiGPUHandler.cpp:757-921,
+ *                            including its chained-comparison branch selection.
+ *   mps_grid_box             CCellSet::SetComputeZone, CGPUCellSet.cpp:109-152.
+ *   mps_lattice_constants    n0 and lambda of the cubic lattice for a radius (FP64);
+ *                            no reference counterpart (it reads n0 from the file).
+ * All return CCT_NOERR, CCT_FILEERR (cannot open / malformed) or CCT_PARAMERR.
+ */
+#ifndef MPS_IO_H
+#define MPS_IO_H
+
+#include "mps_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+CCTStatusType mps_read_parameter_file(const char* path, CParameter* out);
+CCTStatusType mps_read_particle_file(const char* path, int* count, CParticle* out, int capacity);
+CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset, int* count, CTriangle* out,
+                           int capacity);
+float mps_lambda_table(float l0);
+CCTStatusType mps_grid_box(const CBox* compute_zone, const CParameter* param, CGridBox* out);
+CCTStatusType mps_lattice_constants(double re_coefficient, double l0, int dimension, double* n0, double* lambda);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

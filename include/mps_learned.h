@@ -7,7 +7,7 @@
  * Network: 12 features -> 128 -> 128 -> 128 (SiLU) -> 2 outputs (pressure increment
  * in units of the step's pressure scale, log of the diagonal preconditioner scale).
  * Weights are BF16 on the tensor cores, accumulation and the master copy are FP32.
- * Parameter vector layout (FP32, MPS_MLP_PARAMS = 35,330 floats):
+ * Parameter vector layout (FP32, MPS_MLP_PARAMS = 34,946 floats):
  *   W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[128][2] b4[2]
  * (W[k][n]: input k, output n).
  *

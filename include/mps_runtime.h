@@ -38,10 +38,14 @@ CCTStatusType mps_event_record(void* event, void* stream);
 CCTStatusType mps_event_elapsed_ms(void* start, void* stop, float* ms);
 /* last CUDA error string of the calling thread (never NULL) */
 const char* mps_last_error(void);
+/* resets the recorded error and the CUDA runtime's last (non-sticky) error */
+void mps_clear_error(void);
 /* bytes of library-owned scratch currently held by the reference-named entry points */
 size_t mps_scratch_bytes(void);
 /* build identification: "sm_103a" and the library version */
 const char* mps_build_info(void);
+/* kernels this library has launched since it was loaded (all threads, all devices) */
+unsigned long long mps_kernel_launches(void);
 
 #ifdef __cplusplus
 }

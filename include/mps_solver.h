@@ -41,7 +41,8 @@ enum { MPS_PRESSURE_PPE = 0, MPS_PRESSURE_EXPLICIT = 1 };
 typedef struct MpsSolverOptions {
     int precision;          /* MPS_PREC_* */
     int pressure_mode;      /* MPS_PRESSURE_PPE, or the reference's equation of state */
-    int learned;            /* 1: use the learned initial guess and scaling if set */
+    int learned;            /* bit 0: learned initial guess (A-norm line search along the
+                               predicted increment); bit 1: learned diagonal scaling */
     double n0_pnd;          /* reference PND at the gradient radius (<= 0: CParameter n0) */
     double n0_lap;          /* reference PND at the Laplacian radius (<= 0: CParameter n0) */
     double lambda;          /* Laplacian lambda (<= 0: CParameter LambdaValue) */
@@ -109,8 +110,8 @@ CCTStatusType mps_solver_stream(MpsSolver* s, void** stream);
 /* ---- learned initial guess / preconditioner (BF16 tensor-core MLP) ---- */
 /* MLP 12 -> 128 -> 128 -> 128 -> 2 (SiLU); FP32 master parameters, layout:
  * W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[128][2] b4[2]
- * (row-major, input-major) = 35,330 floats. */
-#define MPS_MLP_PARAMS 35330
+ * (row-major, input-major) = 34,946 floats. */
+#define MPS_MLP_PARAMS 34946
 #define MPS_MLP_FEATURES 12
 CCTStatusType mps_solver_set_learned(MpsSolver* s, const float* params, int count);
 /* Features (n*12, FP32) and training targets (n*2: normalised pressure increment,

@@ -9,7 +9,7 @@ the tensor cores.  Used by tests/test_gpu_learned.py to check the GPU forward pa
 the gradients of the backward pass and the training loop.
 
 Parameter vector layout: W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128]
-W4[128][2] b4[2] (35,330 floats).
+W4[128][2] b4[2] (34,946 floats).
 """
 import numpy as np
 

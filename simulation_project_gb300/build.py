@@ -24,7 +24,7 @@ LIB = os.path.join(PKG, "libmps_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
           "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-PER_FILE = {"ref_kernels.cu": ["-fmad=false"]}
+PER_FILE = {"ref_kernels.cu": ["-fmad=false"], "io.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:

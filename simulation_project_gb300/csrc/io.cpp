@@ -1,0 +1,338 @@
+// io.cpp - the reference's input formats (include/mps_io.h), host C++ without Boost.
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/mps_io.h"
+
+namespace {
+
+struct Tokens {
+    std::vector<std::string> t;
+    size_t i = 0;
+    bool more() const { return i < t.size(); }
+    template <class T>
+    bool get(T& v) {
+        if (i >= t.size()) return false;
+        std::istringstream ss(t[i++]);
+        ss >> v;
+        return !ss.fail();
+    }
+    bool on() { return i < t.size() && t[i++] == "ON"; }
+};
+
+// float helper: fast inverse square root of the reference (sqrt_stl, STLSerializer.h:23-29)
+float sqrt_stl(float x) {
+    float xhalf = 0.5f * x;
+    int32_t i;
+    std::memcpy(&i, &x, 4);
+    i = 0x5f3759df - (i >> 1);
+    std::memcpy(&x, &i, 4);
+    x = x * (1.5f - xhalf * x * x);
+    return 1.0f / x;
+}
+
+// CalcTriangleNormal (IO.cpp:449-467): the normal keeps its file value when the
+// cross product vanishes
+void triangle_normal(CTriangle& T) {
+    const Scalar3 a = {T.Vertex[1].x - T.Vertex[0].x, T.Vertex[1].y - T.Vertex[0].y, T.Vertex[1].z - T.Vertex[0].z};
+    const Scalar3 b = {T.Vertex[2].x - T.Vertex[0].x, T.Vertex[2].y - T.Vertex[0].y, T.Vertex[2].z - T.Vertex[0].z};
+    Scalar3 n;
+    n.x = a.y * b.z - b.y * a.z;
+    n.y = a.z * b.x - b.z * a.x;
+    n.z = a.x * b.y - b.x * a.y;
+    const float ab = sqrt_stl(n.x * n.x + n.y * n.y + n.z * n.z);
+    if (ab != 0.0f) {
+        T.Normal.x = n.x / ab;
+        T.Normal.y = n.y / ab;
+        T.Normal.z = n.z / ab;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+CCTStatusType mps_read_parameter_file(const char* path, CParameter* P) {
+    if (!path || !P) return CCT_PARAMERR;
+    std::ifstream f(path);
+    if (!f.is_open()) return CCT_FILEERR;
+    Tokens tk;
+    std::string w;
+    while (f >> w) tk.t.push_back(w);
+    std::memset(P, 0, sizeof(*P));
+    bool ok = true;
+    ok &= tk.get(P->Dimension);
+    ok &= tk.get(P->GravityConstant.x) && tk.get(P->GravityConstant.y) && tk.get(P->GravityConstant.z);
+    ok &= tk.get(P->Density) && tk.get(P->ConstantParticleDensity) && tk.get(P->SurfaceTensionCoefficient);
+    ok &= tk.get(P->InitialParticleDistance) && tk.get(P->FreeSurfaceThreshold);
+    ok &= tk.get(P->GradientInfluenceRadiusCoefficient) && tk.get(P->LaplacianInfluenceRadiusCoefficient);
+    ok &= tk.get(P->TemperatureInfluenceRadiusCoefficient);
+    ok &= tk.get(P->FruidInitializeialTemperature) && tk.get(P->WallInitializeialTemperature);
+    ok &= tk.get(P->FruidThermalResistance) && tk.get(P->WallThermalResistance);
+    ok &= tk.get(P->FruidThermalConductivity) && tk.get(P->WallThermalConductivity);
+    ok &= tk.get(P->FruidSpecificHeat) && tk.get(P->FruidDensity);
+    ok &= tk.get(P->Dt) && tk.get(P->AnalysisStep) && tk.get(P->ThermalStep);
+    ok &= tk.get(P->NegativeCalculationStep) && tk.get(P->OutputStep) && tk.get(P->LambdaID);
+    ok &= tk.get(P->SORJacobianRelaxationCoefficient) && tk.get(P->SORLoopMax) && tk.get(P->SORConvergenceConstant);
+    if (!ok) return CCT_FILEERR;
+    P->bUpdateTemperature = tk.on();
+    if (tk.more()) {
+        tk.get(P->ViscosityUpdateParameterA);
+        tk.get(P->ViscosityUpdateParameterB);
+        tk.get(P->MaxWallTemperature);
+        tk.get(P->MinWallTemperature);
+    }
+    if (tk.more()) tk.get(P->CourantNumber);
+    if (tk.more()) {
+        tk.get(P->InitialTimeForZeroAngle);
+        tk.get(P->FinalTimeToReachAngle);
+        tk.get(P->CellSize.z);
+    }
+    if (tk.more()) {
+        tk.get(P->MvVelocity.x);
+        tk.get(P->MvVelocity.y);
+        tk.get(P->MvVelocity.z);
+    }
+    if (tk.more()) tk.get(P->OffSet);
+    if (tk.more()) {
+        tk.get(P->ParticleGenerationStep);
+        tk.get(P->TotalGenerationStep);
+    }
+    if (tk.more()) tk.get(P->Alpha);
+    if (tk.more()) tk.get(P->AlphaLightWeight);
+    if (tk.more()) {
+        P->bExplicitCollisonCheck = tk.on();
+        P->bExplicitCollisionOut = tk.on();
+        P->bImplicitCollisonCheck = tk.on();
+    }
+    if (tk.more()) {
+        tk.get(P->CollisionCheckCoefficient);
+        tk.get(P->MinDistanceCoefficient);
+    }
+    P->Time1 = P->Dt;
+    if (tk.more()) {
+        P->bFreeSurfacePressureUpdate = tk.on();
+        tk.get(P->BasePressure);
+        tk.get(P->MaxPressure);
+        tk.get(P->Time1);
+        tk.get(P->TriggerStep);
+        tk.get(P->EndStep);
+        tk.get(P->AnalysisArea);
+    }
+    if (tk.more()) P->bExplicitOut = tk.on();
+    if (tk.more()) tk.get(P->WallFrictionCoeffieicnt);
+    if (tk.more()) tk.get(P->DragCoefficient);
+    if (tk.more()) P->bTwoPhase = tk.on();
+    P->StopWallStep = INT_MAX;
+    if (tk.more()) tk.get(P->StopWallStep);
+    if (tk.more()) tk.get(P->Tolerance);
+    if (tk.more()) tk.get(P->ImplicitSurfaceThreshold);
+    if (tk.more()) P->bCGSolver = tk.on();
+    if (tk.more()) P->bUpdateInnerPressure = tk.on();
+    if (tk.more()) tk.get(P->SurfaceInfluenceRadiusCoefficient);
+    if (tk.more()) tk.get(P->SurfaceThreshold);
+    if (tk.more()) tk.get(P->GradientForce);
+    if (tk.more()) tk.get(P->StartStep);
+    if (tk.more()) tk.get(P->InitialForce);
+    if (tk.more()) tk.get(P->VelocityThreshold);
+    if (tk.more()) P->bExplicitPressure = tk.on();
+    if (tk.more()) tk.get(P->SonicVelocity);
+    if (tk.more()) tk.get(P->ArtificialPressure);
+    if (tk.more()) tk.get(P->r_coeff);
+    if (tk.more()) P->bImplicitVelocity = tk.on();
+    if (tk.more()) P->bNJPCGSolver = tk.on();
+    P->PressureMax = FLT_MAX;
+    if (tk.more()) tk.get(P->PressureMax);
+    P->RLimitCoefficient = FLT_MAX;
+    if (tk.more()) tk.get(P->RLimitCoefficient);
+    P->SmagorinskyConstant = 0.1f;
+    P->FilterWidth = P->InitialParticleDistance;
+    if (tk.more()) {
+        P->bTurbulance = tk.on();
+        tk.get(P->SmagorinskyConstant);
+        tk.get(P->FilterWidth);
+        tk.get(P->TurbulanViscosityRatio);
+        tk.get(P->Cnue);
+        tk.get(P->Cepsilon);
+        tk.get(P->TurbulanceIntensity);
+    }
+    P->ConstantCheckStep = -1;
+    if (tk.more()) P->bNegativePressure = tk.on();
+    if (tk.more()) tk.get(P->ConstantCheckStep);
+    P->MaxNeighborhoodNum = P->Dimension == 2 ? 81 : 729;
+    P->LambdaValue = mps_lambda_table(P->InitialParticleDistance);
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_read_particle_file(const char* path, int* count, CParticle* out, int capacity) {
+    if (!path || !count) return CCT_PARAMERR;
+    std::ifstream f(path);
+    if (!f.is_open()) return CCT_FILEERR;
+    int n = 0;
+    for (;;) {
+        CParticle p;
+        std::memset(&p, 0, sizeof(p));
+        int type = 0;
+        f >> p.Position.x >> p.Position.y >> p.Position.z >> p.Velocity.x >> p.Velocity.y >> p.Velocity.z >>
+            p.Pressure >> p.Density >> p.Temperature >> p.KineticViscosity >> p.SolidPhaseRate >> type;
+        if (f.fail()) break;
+        p.Type = type == 1 ? TYPE_HEAVY_WEIGHT_FREE_SURFACE : (type == 2 ? TYPE_LIGHT_WEIGHT : TYPE_HEAVY_WEIGHT);
+        p.ID = n;
+        if (out) {
+            if (n >= capacity) return CCT_PARAMERR;
+            out[n] = p;
+        }
+        ++n;
+    }
+    *count = n;
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset, int* count, CTriangle* out,
+                           int capacity) {
+    if (!path || !count) return CCT_PARAMERR;
+    std::ifstream probe(path);
+    if (!probe.is_open()) return CCT_FILEERR;
+    std::string first;
+    probe >> first;
+    probe.close();
+    std::vector<CTriangle> tris;
+    if (first == "solid") {
+        std::ifstream f(path);
+        std::string w;
+        CTriangle T;
+        std::memset(&T, 0, sizeof(T));
+        int v = 0;
+        bool in_facet = false;
+        while (f >> w) {
+            if (w == "facet") {
+                std::memset(&T, 0, sizeof(T));
+                std::string nrm;
+                f >> nrm >> T.Normal.x >> T.Normal.y >> T.Normal.z;
+                v = 0;
+                in_facet = true;
+            } else if (w == "vertex" && in_facet) {
+                if (v < 3) f >> T.Vertex[v].x >> T.Vertex[v].y >> T.Vertex[v].z;
+                ++v;
+            } else if (w == "endfacet" && in_facet) {
+                if (v != 3) return CCT_FILEERR;
+                tris.push_back(T);
+                in_facet = false;
+            }
+            if (f.fail()) return CCT_FILEERR;
+        }
+    } else {
+        std::ifstream f(path, std::ios::binary);
+        char header[80];
+        f.read(header, 80);
+        uint32_t nt = 0;
+        f.read((char*)&nt, 4);
+        if (!f) return CCT_FILEERR;
+        for (uint32_t i = 0; i < nt; ++i) {
+            float rec[12];
+            char attr[2];
+            f.read((char*)rec, sizeof(rec));
+            f.read(attr, 2);
+            if (!f) return CCT_FILEERR;
+            CTriangle T;
+            T.Normal = {rec[0], rec[1], rec[2]};
+            for (int q = 0; q < 3; ++q) T.Vertex[q] = {rec[3 + 3 * q], rec[4 + 3 * q], rec[5 + 3 * q]};
+            tris.push_back(T);
+        }
+    }
+    for (auto& T : tris) {
+        T.ModelIDNumber = model_id;
+        if (offset)
+            for (int q = 0; q < 3; ++q) {
+                T.Vertex[q].x += offset->x;
+                T.Vertex[q].y += offset->y;
+                T.Vertex[q].z += offset->z;
+            }
+        triangle_normal(T);
+    }
+    *count = (int)tris.size();
+    if (out) {
+        if ((int)tris.size() > capacity) return CCT_PARAMERR;
+        std::memcpy(out, tris.data(), sizeof(CTriangle) * tris.size());
+    }
+    return CCT_NOERR;
+}
+
+// CalculateLambdaValueLocal (MultiGPUHandler.cpp:757-921): "lo < l0 <= hi" evaluates
+// as (lo < l0) <= hi, so the first row whose lower bound is not below l0 (l0 promoted
+// to double), or whose upper bound is >= 1, is taken; lambda = a*l0 + b in float.
+float mps_lambda_table(float l0) {
+    struct Row { double lo, hi, a, b; };
+    static const Row rows[] = {
+        {0, 0.0001, 5.02608E-06, 3.82946E-10},   {0.0001, 0.0005, 0.000124918, 1.81984E-08},
+        {0.0005, 0.001, 0.0017886, -4.84707E-07}, {0.001, 0.002, 0.00373277, -2.15486E-06},
+        {0.002, 0.003, 0.0066746, -6.72384E-06},  {0.003, 0.004, 0.0107452, -1.76386E-05},
+        {0.004, 0.005, 0.0141993, -3.08052E-05},  {0.005, 0.006, 0.0164975, -4.14937E-05},
+        {0.006, 0.007, 0.0181782, -4.95251E-05},  {0.007, 0.008, 0.0205885, -6.28759E-05},
+        {0.008, 0.009, 0.0222761, -7.17244E-05},  {0.009, 0.01, 0.0231972, -7.34117E-05},
+        {0.01, 0.02, 0.0369119, -0.000210081},    {0.02, 0.03, 0.0667457, -0.000672376},
+        {0.03, 0.04, 0.106105, -0.00171939},      {0.04, 0.05, 0.141998, -0.00308074},
+        {0.05, 0.06, 0.164981, -0.00414971},      {0.05, 0.06, 0.164981, -0.00414971},
+        {0.06, 0.07, 0.178483, -0.00474469},      {0.07, 0.08, 0.197539, -0.00567825},
+        {0.08, 0.09, 0.208407, -0.00598107},      {0.09, 0.1, 0.211437, -0.00543137},
+        {0.01, 0.5, 0.369118, -0.021008},         {0.5, 1, 1.78861, -0.48471},
+        {1, 10, 0.423015, 4.1213},                {10, 1000, 0.0138964, 745.762}};
+    float a = 0.0f, b = 0.0f;
+    for (const Row& r : rows) {
+        const double lt = (r.lo < (double)l0) ? 1.0 : 0.0;
+        if (lt <= r.hi) {
+            a = (float)r.a;
+            b = (float)r.b;
+            break;
+        }
+    }
+    return a * l0 + b;
+}
+
+CCTStatusType mps_grid_box(const CBox* zone, const CParameter* P, CGridBox* B) {
+    if (!zone || !P || !B) return CCT_PARAMERR;
+    std::memset(B, 0, sizeof(*B));
+    const float mx = std::max(P->LaplacianInfluenceRadiusCoefficient, P->GradientInfluenceRadiusCoefficient);
+    const float r = P->InitialParticleDistance * mx;
+    if (!(r > 0.0f)) return CCT_PARAMERR;
+    const Scalar3 lo = zone->m_MinBound, hi = zone->m_MaxBound;
+    B->m_ComputeZone = *zone;
+    B->m_ParentZone = *zone;
+    B->m_PressureZone.m_MinBound = {lo.x - r, lo.y - r, lo.z - r};
+    B->m_PressureZone.m_MaxBound = {hi.x + r, hi.y + r, hi.z + r};
+    B->m_BufferedZone.m_MinBound = {lo.x - 2 * r, lo.y - 2 * r, lo.z - 2 * r};
+    B->m_BufferedZone.m_MaxBound = {hi.x + 2 * r, hi.y + 2 * r, hi.z + 2 * r};
+    B->m_CellSize = r;
+    B->m_GridSize.x = (int)std::ceil((hi.x - lo.x) / r + 4);
+    B->m_GridSize.y = (int)std::ceil((hi.y - lo.y) / r + 4);
+    B->m_GridSize.z = (int)std::ceil((hi.z - lo.z) / r + 4);
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_lattice_constants(double re, double l0, int dim, double* n0, double* lambda) {
+    if (!(re > 0) || !(l0 > 0) || (dim != 2 && dim != 3) || !n0 || !lambda) return CCT_PARAMERR;
+    const int m = (int)std::ceil(re) + 1;
+    double sw = 0.0, sr2w = 0.0;
+    for (int i = -m; i <= m; ++i)
+        for (int j = -m; j <= m; ++j)
+            for (int k = (dim == 3 ? -m : 0); k <= (dim == 3 ? m : 0); ++k) {
+                const double r = std::sqrt((double)(i * i + j * j + k * k));
+                if (r > 0 && r < re) {
+                    const double w = re / r - 1.0;
+                    sw += w;
+                    sr2w += r * r * w;
+                }
+            }
+    *n0 = sw;
+    *lambda = sr2w / sw * l0 * l0;
+    return CCT_NOERR;
+}
+
+}  // extern "C"

@@ -13,6 +13,7 @@
 // this library's own kernels.
 #include <cuda_bf16.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -32,6 +33,8 @@ constexpr int FIN = 12;     // input features
 constexpr int FINP = 16;    // padded input width
 constexpr int FOUT = 2;     // outputs
 constexpr int FOUTP = 16;   // padded output width
+static_assert(MPS_MLP_PARAMS == FIN * H + H + 2 * (H * H + H) + H * FOUT + FOUT,
+              "parameter vector length must match the layer layout");
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
     asm volatile(
@@ -139,7 +142,7 @@ cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, int ta, const bf16
     kchunk = (kchunk + GT_K - 1) / GT_K * GT_K;
     split = (K + kchunk - 1) / kchunk;
     dim3 grid(div_up(N, GT_N), div_up(M, GT_M), split);
-    k_gemm_bf16<<<grid, 128, 0, st>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, Cz, bias, act, beta, kchunk);
+    MPS_COUNT_LAUNCH k_gemm_bf16<<<grid, 128, 0, st>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, Cz, bias, act, beta, kchunk);
     return cudaGetLastError();
 }
 
@@ -304,12 +307,12 @@ struct MpsMlp {
         h_loss = nullptr;
     }
     cudaError_t sync_layers(cudaStream_t st) {
-        k_params_to_layers<<<div_up(H * H, 256), 256, 0, st>>>(p, L);
+        MPS_COUNT_LAUNCH k_params_to_layers<<<div_up(H * H, 256), 256, 0, st>>>(p, L);
         return cudaGetLastError();
     }
     // forward over M rows (M <= maxb); keep pre-activations when train
     cudaError_t forward(int M, const float* X, cudaStream_t st, bool train) {
-        k_pack_input<<<div_up(M * FINP, 256), 256, 0, st>>>(M, X, Xb);
+        MPS_COUNT_LAUNCH k_pack_input<<<div_up(M * FINP, 256), 256, 0, st>>>(M, X, Xb);
         cudaError_t e = gemm(M, H, FINP, Xb, FINP, 0, L.W1, H, 0, nullptr, H, H1, H, train ? Z1 : nullptr, L.b1, 1,
                              0.f, 1, st);
         if (!e) e = gemm(M, H, H, H1, H, 0, L.W2, H, 0, nullptr, H, H2, H, train ? Z2 : nullptr, L.b2, 1, 0.f, 1, st);
@@ -318,34 +321,49 @@ struct MpsMlp {
         return e;
     }
     cudaError_t backward(int M, const float* T, float w1, cudaStream_t st) {
-        cudaMemsetAsync(loss, 0, sizeof(double), st);
-        k_loss_grad<<<div_up(M, 256), 256, 0, st>>>(M, Yp, T, w1, dYb, dY, loss);
+        cudaError_t e = cudaSuccess;
+#define MLP_STEP(label, call)                       \
+    do {                                             \
+        call;                                        \
+        if ((e = cudaGetLastError())) {              \
+            note_error(label, e);                    \
+            return e;                                \
+        }                                            \
+    } while (0)
+#define MLP_GEMM(label, ...)                         \
+    do {                                             \
+        if ((e = gemm(__VA_ARGS__))) {               \
+            note_error(label, e);                    \
+            return e;                                \
+        }                                            \
+    } while (0)
+        MLP_STEP("loss reset", cudaMemsetAsync(loss, 0, sizeof(double), st));
+        MLP_STEP("k_loss_grad", (MPS_COUNT_LAUNCH k_loss_grad<<<div_up(M, 256), 256, 0, st>>>(M, Yp, T, w1, dYb, dY, loss)));
         const int split = max(1, min(64, M / 512));
-        cudaMemsetAsync(dW4, 0, sizeof(float) * H * FOUTP, st);
-        cudaMemsetAsync(dW3, 0, sizeof(float) * H * H, st);
-        cudaMemsetAsync(dW2, 0, sizeof(float) * H * H, st);
-        cudaMemsetAsync(dW1, 0, sizeof(float) * FINP * H, st);
+        MLP_STEP("grad reset", cudaMemsetAsync(dW4, 0, sizeof(float) * H * FOUTP, st));
+        MLP_STEP("grad reset", cudaMemsetAsync(dW3, 0, sizeof(float) * H * H, st));
+        MLP_STEP("grad reset", cudaMemsetAsync(dW2, 0, sizeof(float) * H * H, st));
+        MLP_STEP("grad reset", cudaMemsetAsync(dW1, 0, sizeof(float) * FINP * H, st));
         const int Kb = M;   // batch as K; the tile loader zero-fills k >= K
-        cudaError_t e = gemm(H, FOUTP, Kb, H3, H, 1, dYb, FOUTP, 0, dW4, FOUTP, nullptr, 0, nullptr, nullptr, 0, 1.f,
-                             split, st);
-        k_colsum<<<1, 128, 0, st>>>(M, FOUTP, dY, db + 3 * H);
-        // layer 3
-        if (!e) e = gemm(M, H, FOUTP, dYb, FOUTP, 0, L.W4, FOUTP, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
-        k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z3, dZ, dZb);
-        if (!e) e = gemm(H, H, Kb, H2, H, 1, dZb, H, 0, dW3, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
-        k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db + 2 * H);
-        // layer 2
-        if (!e) e = gemm(M, H, H, dZb, H, 0, L.W3, H, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
-        k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z2, dZ, dZb);
-        if (!e) e = gemm(H, H, Kb, H1, H, 1, dZb, H, 0, dW2, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
-        k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db + 1 * H);
-        // layer 1
-        if (!e) e = gemm(M, H, H, dZb, H, 0, L.W2, H, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
-        k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z1, dZ, dZb);
-        if (!e) e = gemm(FINP, H, Kb, Xb, FINP, 1, dZb, H, 0, dW1, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
-        k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db);
-        k_grad_to_vec<<<div_up(H * H, 256), 256, 0, st>>>(dW1, db, dW2, db + H, dW3, db + 2 * H, dW4, db + 3 * H, g);
-        return e ? e : cudaGetLastError();
+        MLP_GEMM("dW4", H, FOUTP, Kb, H3, H, 1, dYb, FOUTP, 0, dW4, FOUTP, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        MLP_STEP("db4", (MPS_COUNT_LAUNCH k_colsum<<<1, 128, 0, st>>>(M, FOUTP, dY, db + 3 * H)));
+        MLP_GEMM("dH3", M, H, FOUTP, dYb, FOUTP, 0, L.W4, FOUTP, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
+        MLP_STEP("silu3", (MPS_COUNT_LAUNCH k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z3, dZ, dZb)));
+        MLP_GEMM("dW3", H, H, Kb, H2, H, 1, dZb, H, 0, dW3, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        MLP_STEP("db3", (MPS_COUNT_LAUNCH k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db + 2 * H)));
+        MLP_GEMM("dH2", M, H, H, dZb, H, 0, L.W3, H, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
+        MLP_STEP("silu2", (MPS_COUNT_LAUNCH k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z2, dZ, dZb)));
+        MLP_GEMM("dW2", H, H, Kb, H1, H, 1, dZb, H, 0, dW2, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        MLP_STEP("db2", (MPS_COUNT_LAUNCH k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db + 1 * H)));
+        MLP_GEMM("dH1", M, H, H, dZb, H, 0, L.W2, H, 1, dH, H, nullptr, 0, nullptr, nullptr, 0, 0.f, 1, st);
+        MLP_STEP("silu1", (MPS_COUNT_LAUNCH k_silu_back<<<div_up(M * H, 256), 256, 0, st>>>(M * H, dH, Z1, dZ, dZb)));
+        MLP_GEMM("dW1", FINP, H, Kb, Xb, FINP, 1, dZb, H, 0, dW1, H, nullptr, 0, nullptr, nullptr, 0, 1.f, split, st);
+        MLP_STEP("db1", (MPS_COUNT_LAUNCH k_colsum<<<1, 128, 0, st>>>(M, H, dZ, db)));
+        MLP_STEP("grad vec", (MPS_COUNT_LAUNCH k_grad_to_vec<<<div_up(H * H, 256), 256, 0, st>>>(dW1, db, dW2, db + H, dW3, db + 2 * H,
+                                                                                 dW4, db + 3 * H, g)));
+#undef MLP_STEP
+#undef MLP_GEMM
+        return cudaSuccess;
     }
 };
 
@@ -356,7 +374,7 @@ cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t
         const int cnt = min(m->maxb, M - r);
         cudaError_t e = m->forward(cnt, X + (size_t)r * FIN, st, false);
         if (e) return e;
-        k_unpad_output<<<div_up(cnt * FOUT, 256), 256, 0, st>>>(cnt, m->Yp, Y + (size_t)r * FOUT);
+        MPS_COUNT_LAUNCH k_unpad_output<<<div_up(cnt * FOUT, 256), 256, 0, st>>>(cnt, m->Yp, Y + (size_t)r * FOUT);
     }
     return cudaGetLastError();
 }
@@ -436,13 +454,23 @@ CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T
                                 float* host_loss, void* stream) {
     if (!m || M <= 0 || M > m->maxb) return CCT_PARAMERR;
     cudaStream_t st = (cudaStream_t)stream;
-    cudaError_t e = m->forward(M, X, st, true);
-    if (!e) e = m->backward(M, T, w1, st);
-    if (!e && grad) e = cudaMemcpyAsync(grad, m->g, sizeof(float) * MPS_MLP_PARAMS, cudaMemcpyDeviceToDevice, st);
-    if (!e) e = cudaMemcpyAsync(m->h_loss, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st);
-    if (!e) e = cudaStreamSynchronize(st);
-    if (!e && host_loss) *host_loss = (float)(*m->h_loss / M);
-    return cuda_status(e);
+    cudaError_t e = cudaGetLastError();
+    if (e) { note_error("mps_mlp_loss_grad: pending error on entry", e); return CCT_CUDAERR; }
+    if ((e = m->forward(M, X, st, true))) { note_error("mlp forward", e); return CCT_CUDAERR; }
+    if ((e = m->backward(M, T, w1, st))) return CCT_CUDAERR;   // backward names the failing launch
+    if (grad && (e = cudaMemcpyAsync(grad, m->g, sizeof(float) * MPS_MLP_PARAMS, cudaMemcpyDeviceToDevice, st))) {
+        char what[96];
+        snprintf(what, sizeof(what), "gradient copy %p <- %p", (void*)grad, (void*)m->g);
+        note_error(what, e);
+        return CCT_CUDAERR;
+    }
+    if ((e = cudaMemcpyAsync(m->h_loss, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st))) {
+        note_error("loss copy", e);
+        return CCT_CUDAERR;
+    }
+    if ((e = cudaStreamSynchronize(st))) { note_error("mps_mlp_loss_grad sync", e); return CCT_CUDAERR; }
+    if (host_loss) *host_loss = (float)(*m->h_loss / M);
+    return CCT_NOERR;
 }
 
 CCTStatusType mps_mlp_train_step(MpsMlp* m, int M, const float* X, const float* T, float w1, float lr,
@@ -454,7 +482,7 @@ CCTStatusType mps_mlp_train_step(MpsMlp* m, int M, const float* X, const float* 
     if (e) return cuda_status(e);
     m->t += 1;
     const float b1t = powf(0.9f, (float)m->t), b2t = powf(0.999f, (float)m->t);
-    k_adam<<<div_up(MPS_MLP_PARAMS, 256), 256, 0, st>>>(MPS_MLP_PARAMS, m->p, m->g, m->m, m->v, lr, b1t, b2t);
+    MPS_COUNT_LAUNCH k_adam<<<div_up(MPS_MLP_PARAMS, 256), 256, 0, st>>>(MPS_MLP_PARAMS, m->p, m->g, m->m, m->v, lr, b1t, b2t);
     e = m->sync_layers(st);
     if (!e && host_loss) {
         e = cudaMemcpyAsync(m->h_loss, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st);

@@ -18,6 +18,13 @@ cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream
 // library-owned scratch for the reference-named entry points, which take no scratch
 // argument (runtime.cu).  Grows on demand; one buffer per slot.
 void* scratch_get(int slot, size_t bytes);
+// records "where: CUDA error string" for mps_last_error()
+void note_error(const char* where, cudaError_t e);
+
+// Kernel launches issued by this library since load (every launch site is written as
+// MPS_COUNT_LAUNCH k<<<...>>>(...); read by mps_kernel_launches()).
+extern unsigned long long g_kernel_launches;
+#define MPS_COUNT_LAUNCH __atomic_fetch_add(&::mps::g_kernel_launches, 1ull, __ATOMIC_RELAXED),
 void scratch_release_all();
 
 inline CCTStatusType cuda_status(cudaError_t e) { return e == cudaSuccess ? CCT_NOERR : CCT_CUDAERR; }

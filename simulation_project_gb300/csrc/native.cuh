@@ -7,8 +7,9 @@
 //   visc            float, type int, id int       carried per particle
 //   key, idx        int                           hash keys / sort permutation
 //   cstart, cend    int[cells]                    cell ranges (-1 = empty)
-//   nbr, nbrw       int / T [n * K]               Laplacian neighbour rows, row-major,
-//                                                 row i at i*K, nbr_cnt[i] entries
+//   nbr, nbrw       int / T [ceil(n/32)*32 * K]  Laplacian neighbour rows in SELL-32
+//                                                 layout: entry k of row i at
+//                                                 ((i/32)*K + k)*32 + i%32; nbr_cnt[i] entries
 //   gnbr, gnbrr     int / T [n * KG]              gradient-radius rows (index, r)
 //   tri             double[9*T], tnrm double[3*T] walls; tcs[cells+1]/tids CSR bins
 // Kernels take the whole record as one __grid_constant__ parameter.
@@ -89,7 +90,7 @@ struct Dev {
 // device scalar slots
 enum {
     S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_BNORM, S_TOL, S_CONV, S_ITER, S_RZNEW, S_RNORM, S_R0NORM,
-    S_IRTOL, S_TMP0, S_TMP1, S_PSCALE, S_COUNT
+    S_IRTOL, S_TMP0, S_TMP1, S_PSCALE, S_MAXIT, S_NNZ0, S_NNZ1, S_LS0, S_LS1, S_COUNT
 };
 
 }  // namespace mps

@@ -22,6 +22,11 @@ constexpr int kVecThreads = 256;
 enum { NB_PREDICT = 0, NB_LIST = 1 };
 
 template <class T> struct V3 { T x, y, z; };
+
+// SELL-32 position of entry k of row i (row capacity K)
+__device__ __forceinline__ size_t sell_index(int i, int k, int K) {
+    return ((size_t)(i >> 5) * K + k) * 32 + (i & 31);
+}
 template <class T> __device__ __forceinline__ V3<T> v3(T x, T y, T z) { V3<T> r; r.x = x; r.y = y; r.z = z; return r; }
 
 // ---------------------------------------------------------------------------
@@ -459,8 +464,9 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     } else {
                         const int slot = cnt + __popc(bal & lt);
                         if (slot < d.K) {
-                            d.nbr[(size_t)i * d.K + slot] = j;
-                            ((T*)d.nbrw)[(size_t)i * d.K + slot] = w;
+                            const size_t e = sell_index(i, slot, d.K);
+                            d.nbr[e] = j;
+                            ((T*)d.nbrw)[e] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
                         a1 += (T)d.press[j];                       // neighbour pressure (feature)
@@ -586,29 +592,12 @@ __global__ void k_eos(const __grid_constant__ Dev d) {
 // ---------------------------------------------------------------------------
 // y = A x for interior rows (y = 0 elsewhere); A = diag - coef * W.  MODE 0: plain
 // (+ dot x.y -> S_PQ, alpha = rz / pq); MODE 1: residual r = b - A x (FP64 out),
-// norms -> S_RR, S_BNORM.
-// One warp per row.  A row (capacity K, a multiple of 128) is read as 16-byte vectors:
-// lane l loads entries [128c + 4l, 128c + 4l + 4) of chunk c, so each warp load moves
-// 512 contiguous bytes of indices (and of FP32 weights; FP64 weights take two).  All
-// chunks of the row are issued before the first gather, with streaming (evict-first)
-// loads so the matrix does not displace the x vector from L2.
-template <class TW> struct WVec;
-template <> struct WVec<float> {
-    float v[4];
-    __device__ __forceinline__ void load(const float* p) {
-        const float4 t = __ldcs((const float4*)p);
-        v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-    }
-};
-template <> struct WVec<double> {
-    double v[4];
-    __device__ __forceinline__ void load(const double* p) {
-        const double2 a = __ldcs((const double2*)p), b = __ldcs((const double2*)(p + 2));
-        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-    }
-};
-constexpr int kMaxRowChunks = 4;   // rows up to 512 entries
-
+// norms -> S_RR, S_BNORM; MODE 2: y = A x with dots x.y -> S_LS0 and x.b -> S_LS1.
+// SELL-32: one warp per slice of 32 consecutive rows, one lane per row; entry k of
+// the slice is 32 consecutive words, so every index / weight load of a warp is one
+// full 128-byte line (256 for FP64 weights) and no cross-lane reduction is needed.
+// The k loop runs to the slice's longest row, unrolled 4x so that eight line loads
+// are in flight per warp before the gathers; matrix loads are evict-first.
 template <class TW, class TX, class TY, int MODE>
 __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w,
                                               const TX* __restrict__ x, TY* __restrict__ y, const double* __restrict__ b,
@@ -617,50 +606,54 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int nslices = (d.n + 31) >> 5;
     double part0 = 0.0, part1 = 0.0;
     const double coef = d.c.coef_lap;
-    using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE == 1), double, float>::type;
-    for (int i = gw; i < d.n; i += nw) {
-        if (!d.inner[i]) {
-            if (lane == 0) y[i] = TY(0);
+    using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE != 0), double, float>::type;
+    for (int sl = gw; sl < nslices; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+        const size_t base = (size_t)sl * d.K * 32 + lane;
+        TA acc = TA(0);
+        int k = 0;
+        for (; k + 4 <= kmax; k += 4) {
+            int id[4];
+            TW wv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                id[u] = __ldcs(d.nbr + base + (size_t)(k + u) * 32);
+                wv[u] = __ldcs(w + base + (size_t)(k + u) * 32);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (k + u < cnt) acc += (TA)wv[u] * (TA)x[id[u]];
+        }
+        for (; k < kmax; ++k) {
+            const int idk = __ldcs(d.nbr + base + (size_t)k * 32);
+            const TW wk = __ldcs(w + base + (size_t)k * 32);
+            if (k < cnt) acc += (TA)wk * (TA)x[idk];
+        }
+        if (!row) continue;
+        if (!in) {
+            y[i] = TY(0);
             continue;
         }
-        const int cnt = d.nbr_cnt[i];
-        const size_t base = (size_t)i * d.K;
-        int4 id[kMaxRowChunks];
-        WVec<TW> wv[kMaxRowChunks];
-#pragma unroll
-        for (int c = 0; c < kMaxRowChunks; ++c) {
-            const int k = c * 128 + 4 * lane;
-            if (k < cnt) {
-                id[c] = __ldcs((const int4*)(d.nbr + base + k));
-                wv[c].load(w + base + k);
-            }
-        }
-        TA acc = TA(0);
-#pragma unroll
-        for (int c = 0; c < kMaxRowChunks; ++c) {
-            const int k = c * 128 + 4 * lane;
-            if (k < cnt) {
-                acc += (TA)wv[c].v[0] * (TA)x[id[c].x];
-                if (k + 1 < cnt) acc += (TA)wv[c].v[1] * (TA)x[id[c].y];
-                if (k + 2 < cnt) acc += (TA)wv[c].v[2] * (TA)x[id[c].z];
-                if (k + 3 < cnt) acc += (TA)wv[c].v[3] * (TA)x[id[c].w];
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-            const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
-            if (MODE == 0) {
-                y[i] = (TY)yi;
-                part0 += (double)x[i] * (double)(TY)yi;
-            } else {
-                const double ri = b[i] - yi;
-                y[i] = (TY)ri;
-                part0 += ri * ri;
-                part1 += b[i] * b[i];
-            }
+        const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
+        if (MODE == 0) {
+            y[i] = (TY)yi;
+            part0 += (double)x[i] * (double)(TY)yi;
+        } else if (MODE == 2) {
+            y[i] = (TY)yi;
+            part0 += (double)x[i] * yi;
+            part1 += (double)x[i] * b[i];
+        } else {
+            const double ri = b[i] - yi;
+            y[i] = (TY)ri;
+            part0 += ri * ri;
+            part1 += b[i] * b[i];
         }
     }
     double v[2] = {part0, part1}, out[2];
@@ -668,6 +661,9 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
         if (MODE == 0) {
             d.scal[S_PQ] = out[0];
             d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
+        } else if (MODE == 2) {
+            d.scal[S_LS0] = out[0];
+            d.scal[S_LS1] = out[1];
         } else {
             d.scal[S_RR] = out[0];
             d.scal[S_RNORM] = sqrt(out[0]);
@@ -702,7 +698,7 @@ __global__ void __launch_bounds__(256) k_cg_start(const __grid_constant__ Dev d,
         d.scal[S_R0NORM] = sqrt(out[1]);
         d.scal[S_TOL] = tol_abs;
         d.scal[S_ITER] = 0.0;
-        d.scal[S_TMP0] = (double)maxit;
+        d.scal[S_MAXIT] = (double)maxit;
         d.scal[S_CONV] = (sqrt(out[1]) <= tol_abs || maxit <= 0) ? 1.0 : 0.0;
     }
 }
@@ -734,7 +730,7 @@ __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d
         d.scal[S_RNORM] = rn;
         const double it = d.scal[S_ITER] + 1.0;
         d.scal[S_ITER] = it;
-        if (rn <= d.scal[S_TOL] || it >= d.scal[S_TMP0] || !(rn == rn)) d.scal[S_CONV] = 1.0;
+        if (rn <= d.scal[S_TOL] || it >= d.scal[S_MAXIT] || !(rn == rn)) d.scal[S_CONV] = 1.0;
     }
 }
 
@@ -756,8 +752,8 @@ __global__ void __launch_bounds__(256) k_count_nnz(const __grid_constant__ Dev d
     }
     double v[2] = {a, b}, out[2];
     if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
-        d.scal[S_TMP0] = out[0];
-        d.scal[S_TMP1] = out[1];
+        d.scal[S_NNZ0] = out[0];
+        d.scal[S_NNZ1] = out[1];
     }
 }
 
@@ -827,20 +823,32 @@ __global__ void k_features(const __grid_constant__ Dev d) {
     f[11] = (float)(sqrt(v.x * v.x + v.y * v.y + v.z * v.z) * d.c.dt / d.c.l0 * 100.0);
 }
 
-// initial guess p = p_prev + scale * y0, preconditioner M^-1 = exp(y1) / diag
-__global__ void k_learned_apply(const __grid_constant__ Dev d) {
+// predicted increment dp = scale * y0 (into z), preconditioner M^-1 = exp(y1) / diag
+// when the scaling output is used (else Jacobi)
+__global__ void k_learned_apply(const __grid_constant__ Dev d, int use_scaling) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     if (!d.inner[i]) {
-        d.press[i] = 0.0;
+        d.z[i] = 0.0;
         d.minv[i] = 0.0;
         return;
     }
     const float y0 = d.mlp_out[2 * (size_t)i], y1 = d.mlp_out[2 * (size_t)i + 1];
     const double inc = (double)fminf(fmaxf(y0, -50.f), 50.f) * d.scal[S_PSCALE];
-    d.press[i] = d.pprev[i] + (isfinite(inc) ? inc : 0.0);
-    const double s = exp((double)fminf(fmaxf(isfinite(y1) ? y1 : 0.f, -2.3f), 2.3f));
+    d.z[i] = isfinite(inc) ? inc : 0.0;
+    const double s = use_scaling ? exp((double)fminf(fmaxf(isfinite(y1) ? y1 : 0.f, -2.3f), 2.3f)) : 1.0;
     d.minv[i] = s / d.diag[i];
+}
+
+// p = p_prev + alpha dp with alpha = (dp . r0) / (dp . A dp), the A-norm-optimal step
+// along the predicted increment (so the start is never worse than p_prev in A-norm)
+__global__ void k_learned_finish(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double dad = d.scal[S_LS0], dr = d.scal[S_LS1];
+    double a = (dad > 0.0 && isfinite(dr / dad)) ? dr / dad : 0.0;
+    if (i == 0) d.scal[S_IRTOL] = a;
+    d.press[i] = d.inner[i] ? d.pprev[i] + a * d.z[i] : 0.0;
 }
 
 // training targets after a plain solve: (p - p_prev) / scale and the log of the

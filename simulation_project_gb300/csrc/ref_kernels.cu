@@ -743,7 +743,7 @@ CCTStatusType CaculateCellIDandInitializeHash(cudaStream_t& Stream, Integer Part
                                               Scalar3* particlePosition) {
     (void)CellNum;
     if (ParticleNum <= 0) return CCT_NOERR;
-    k_ref_hash<<<grid_of(ParticleNum), kBlock, 0, Stream>>>(ParticleNum, g_bind.box, particlePosition,
+    MPS_COUNT_LAUNCH k_ref_hash<<<grid_of(ParticleNum), kBlock, 0, Stream>>>(ParticleNum, g_bind.box, particlePosition,
                                                              dGridParticleHash, dGridParticleIndex);
     return launch_status();
 }
@@ -754,7 +754,7 @@ CCTStatusType reorderDataAndFindCellStart(cudaStream_t& Stream, Integer numParti
     if (numParticles <= 0) return CCT_NOERR;
     MPS_CUDA_TRY(cudaMemsetAsync(cellStart, 0xff, sizeof(int) * (size_t)numCells, Stream));
     MPS_CUDA_TRY(cudaMemsetAsync(cellEnd, 0xff, sizeof(int) * (size_t)numCells, Stream));
-    k_ref_reorder<<<grid_of(numParticles), kBlock, 0, Stream>>>(numParticles, numCells, gridParticleHash,
+    MPS_COUNT_LAUNCH k_ref_reorder<<<grid_of(numParticles), kBlock, 0, Stream>>>(numParticles, numCells, gridParticleHash,
                                                                  gridParticleIndex, cellStart, cellEnd, g_bind);
     return launch_status();
 }
@@ -793,10 +793,10 @@ CCTStatusType CheckParticleOutsideComputeZone(cudaStream_t& Stream, Integer* Par
     if (!flag || !rank) return CCT_MEMERR;
     int* removed = (int*)(rank + n);
     MPS_CUDA_TRY(cudaMemsetAsync(removed, 0, sizeof(int), Stream));
-    k_ref_outside_flags<<<grid_of(n), kBlock, 0, Stream>>>(n, g_bind, flag);
+    MPS_COUNT_LAUNCH k_ref_outside_flags<<<grid_of(n), kBlock, 0, Stream>>>(n, g_bind, flag);
     MPS_CUDA_TRY(cudaMemcpyAsync(rank, flag, sizeof(unsigned) * (size_t)n, cudaMemcpyDeviceToDevice, Stream));
     MPS_CUDA_TRY(scan_exclusive(rank, n, nullptr, Stream));
-    k_ref_compact<<<grid_of(n), kBlock, 0, Stream>>>(n, g_bind, flag, rank, removed);
+    MPS_COUNT_LAUNCH k_ref_compact<<<grid_of(n), kBlock, 0, Stream>>>(n, g_bind, flag, rank, removed);
     int r = 0;
     MPS_CUDA_TRY(cudaMemcpyAsync(&r, removed, sizeof(int), cudaMemcpyDeviceToHost, Stream));
     MPS_CUDA_TRY(cudaStreamSynchronize(Stream));
@@ -807,7 +807,7 @@ CCTStatusType CheckParticleOutsideComputeZone(cudaStream_t& Stream, Integer* Par
 
 CCTStatusType ResetTriangleTopology(cudaStream_t& Stream, Integer CellNum, CCell* aCell) {
     if (CellNum <= 0) return CCT_NOERR;
-    k_tri_reset<<<grid_of(CellNum), kBlock, 0, Stream>>>(CellNum, aCell);
+    MPS_COUNT_LAUNCH k_tri_reset<<<grid_of(CellNum), kBlock, 0, Stream>>>(CellNum, aCell);
     return launch_status();
 }
 
@@ -818,7 +818,7 @@ CCTStatusType RegisterTriangleTopology(cudaStream_t& Stream, CTriangle* daTriang
     unsigned* off = (unsigned*)scratch_get(4, sizeof(unsigned) * ((size_t)t + 4));
     if (!off) return CCT_MEMERR;
     unsigned* total_dev = off + t;
-    k_tri_count<<<grid_of(t), kBlock, 0, Stream>>>(t, daTriangle, g_bind.box, CellNum, off);
+    MPS_COUNT_LAUNCH k_tri_count<<<grid_of(t), kBlock, 0, Stream>>>(t, daTriangle, g_bind.box, CellNum, off);
     MPS_CUDA_TRY(scan_exclusive(off, t, total_dev, Stream));
     unsigned nv = 0;
     MPS_CUDA_TRY(cudaMemcpyAsync(&nv, total_dev, sizeof(unsigned), cudaMemcpyDeviceToHost, Stream));
@@ -829,64 +829,64 @@ CCTStatusType RegisterTriangleTopology(cudaStream_t& Stream, CTriangle* daTriang
     void* sscr = scratch_get(7, radix_scratch_bytes((int)nv));
     if (!vcell || !vrange || !sscr) return CCT_MEMERR;
     int* vtri = vcell + nv;
-    k_tri_fill<<<grid_of(t), kBlock, 0, Stream>>>(t, daTriangle, g_bind.box, CellNum, off, vcell, vtri);
+    MPS_COUNT_LAUNCH k_tri_fill<<<grid_of(t), kBlock, 0, Stream>>>(t, daTriangle, g_bind.box, CellNum, off, vcell, vtri);
     MPS_CUDA_TRY(radix_sort_pairs((int)nv, vcell, vtri, 0, radix_passes((unsigned)CellNum), sscr, Stream));
     MPS_CUDA_TRY(cudaMemsetAsync(vrange, 0xff, sizeof(int) * (size_t)CellNum * 2, Stream));
-    k_tri_bounds<<<grid_of((int)nv), kBlock, 0, Stream>>>((int)nv, vcell, vrange, vrange + CellNum);
-    k_tri_cells<<<grid_of(CellNum), kBlock, 0, Stream>>>(CellNum, vrange, vrange + CellNum, vtri, daCell);
+    MPS_COUNT_LAUNCH k_tri_bounds<<<grid_of((int)nv), kBlock, 0, Stream>>>((int)nv, vcell, vrange, vrange + CellNum);
+    MPS_COUNT_LAUNCH k_tri_cells<<<grid_of(CellNum), kBlock, 0, Stream>>>(CellNum, vrange, vrange + CellNum, vtri, daCell);
     return launch_status();
 }
 
 CCTStatusType UpdateTrianglePosition(cudaStream_t& Stream, const Integer TriangleNum, CTriangle* daTriangles) {
     if (TriangleNum <= 0) return CCT_NOERR;
-    k_tri_translate<<<grid_of(TriangleNum), kBlock, 0, Stream>>>(TriangleNum, daTriangles, g_bind);
+    MPS_COUNT_LAUNCH k_tri_translate<<<grid_of(TriangleNum), kBlock, 0, Stream>>>(TriangleNum, daTriangles, g_bind);
     return launch_status();
 }
 
 CCTStatusType RotateTrianglePosition(cudaStream_t& Stream, const Integer TriangleNum, CTriangle* daTriangles,
                                      const Integer analysisStep) {
     if (TriangleNum <= 0) return CCT_NOERR;
-    k_tri_rotate<<<grid_of(TriangleNum), kBlock, 0, Stream>>>(TriangleNum, daTriangles, analysisStep, g_bind);
+    MPS_COUNT_LAUNCH k_tri_rotate<<<grid_of(TriangleNum), kBlock, 0, Stream>>>(TriangleNum, daTriangles, analysisStep, g_bind);
     return launch_status();
 }
 
 CCTStatusType ResetWallPosition(cudaStream_t& Stream, const Integer TriangleNum, const Integer AnalysisStep,
                                 const CTriangle* daTriangles) {
     if (TriangleNum <= 0) return CCT_NOERR;
-    k_tri_reset_wall<<<grid_of(TriangleNum), kBlock, 0, Stream>>>(TriangleNum, AnalysisStep, daTriangles, g_bind);
+    MPS_COUNT_LAUNCH k_tri_reset_wall<<<grid_of(TriangleNum), kBlock, 0, Stream>>>(TriangleNum, AnalysisStep, daTriangles, g_bind);
     return launch_status();
 }
 
 CCTStatusType CalcSTLDistance(cudaStream_t& Stream, Integer ComputeParticleNum) {
     if (ComputeParticleNum <= 0) return CCT_NOERR;
     MPS_CUDA_TRY(cudaMemsetAsync(g_bind.stl_id, 0xff, sizeof(int) * (size_t)ComputeParticleNum, Stream));
-    k_ref_stl_distance<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    MPS_COUNT_LAUNCH k_ref_stl_distance<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
     return launch_status();
 }
 
 CCTStatusType CalcDragEffect(cudaStream_t& Stream, Integer ComputeParticleNum) {
     if (ComputeParticleNum <= 0) return CCT_NOERR;
-    k_ref_drag<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    MPS_COUNT_LAUNCH k_ref_drag<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
     return launch_status();
 }
 
 CCTStatusType CalcExplicitly(cudaStream_t& Stream, Integer ParticleNum) {
     if (ParticleNum <= 0) return CCT_NOERR;
     if (g_bind.param.bTurbulance) return CCT_PARAMERR;
-    k_ref_explicitly<<<grid_of(ParticleNum), kBlock, 0, Stream>>>(ParticleNum, g_bind);
+    MPS_COUNT_LAUNCH k_ref_explicitly<<<grid_of(ParticleNum), kBlock, 0, Stream>>>(ParticleNum, g_bind);
     return launch_status();
 }
 
 CCTStatusType CalcExplicitPressure(cudaStream_t& Stream, Integer ComputeParticleNum) {
     if (ComputeParticleNum <= 0) return CCT_NOERR;
-    k_ref_pressure<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    MPS_COUNT_LAUNCH k_ref_pressure<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
     return launch_status();
 }
 
 CCTStatusType CalcExplicitPressureGradient(cudaStream_t& Stream, Integer ComputeParticleNum) {
     if (ComputeParticleNum <= 0) return CCT_NOERR;
     if (g_bind.param.bNegativePressure) return CCT_PARAMERR;
-    k_ref_gradient<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    MPS_COUNT_LAUNCH k_ref_gradient<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
     return launch_status();
 }
 

@@ -26,6 +26,12 @@ CCTStatusType rec(cudaError_t e) {
 }
 }  // namespace
 
+unsigned long long g_kernel_launches = 0;
+
+void note_error(const char* where, cudaError_t e) {
+    snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(e));
+}
+
 void* scratch_get(int slot, size_t bytes) {
     if (slot < 0 || slot >= kSlots) return nullptr;
     Slot& s = g_slots[slot];
@@ -90,9 +96,23 @@ CCTStatusType mps_event_elapsed_ms(void* start, void* stop, float* ms) {
     return rec(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)stop));
 }
 const char* mps_last_error(void) {
+    // a failing runtime call also leaves its error pending: keep the message that names
+    // the failing step and append what is pending, if it is not already part of it
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) snprintf(mps::g_err, sizeof(mps::g_err), "%s", cudaGetErrorString(e));
+    if (e != cudaSuccess) {
+        const char* what = cudaGetErrorString(e);
+        if (strcmp(mps::g_err, "no error") == 0) {
+            snprintf(mps::g_err, sizeof(mps::g_err), "%s", what);
+        } else if (!strstr(mps::g_err, what)) {
+            const size_t len = strlen(mps::g_err);
+            snprintf(mps::g_err + len, sizeof(mps::g_err) - len, " (pending: %s)", what);
+        }
+    }
     return mps::g_err;
+}
+void mps_clear_error(void) {
+    cudaGetLastError();
+    snprintf(mps::g_err, sizeof(mps::g_err), "no error");
 }
 size_t mps_scratch_bytes(void) {
     size_t s = 0;
@@ -100,5 +120,7 @@ size_t mps_scratch_bytes(void) {
     return s;
 }
 const char* mps_build_info(void) { return "gb300-mps 0.1 sm_103a"; }
+
+unsigned long long mps_kernel_launches(void) { return __atomic_load_n(&mps::g_kernel_launches, __ATOMIC_RELAXED); }
 
 }  // extern "C"

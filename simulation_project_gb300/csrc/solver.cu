@@ -172,7 +172,8 @@ struct Solver {
         e = e ? e : mk(&d.wdist, N); e = e ? e : mk(&d.wdir, 3 * N); e = e ? e : mk(&d.wid, N);
         e = e ? e : mk(&d.dragv, 3 * N);
         e = e ? e : mk(&d.tcs, 2 * (size_t)d.cells);
-        e = e ? e : mk(&d.nbr, N * d.K); e = e ? e : mk((char**)&d.nbrw, N * d.K * wsz);
+        const size_t N32 = (N + 31) / 32 * 32;
+        e = e ? e : mk(&d.nbr, N32 * d.K); e = e ? e : mk((char**)&d.nbrw, N32 * d.K * wsz);
         e = e ? e : mk(&d.nbr_cnt, N);
         e = e ? e : mk(&d.gnbr, N * d.KG); e = e ? e : mk((char**)&d.gnbrr, N * d.KG * wsz);
         e = e ? e : mk(&d.gcnt, N);
@@ -307,10 +308,10 @@ struct Solver {
     CCTStatusType compact() {
         const int n = d.n;
         if (n <= 0) return CCT_NOERR;
-        k_zone_flags<<<blocks_for(n), kBlock, 0, st>>>(d, keep);
+        MPS_COUNT_LAUNCH k_zone_flags<<<blocks_for(n), kBlock, 0, st>>>(d, keep);
         cudaMemcpyAsync(rank, keep, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
         scan_exclusive(rank, n, rank + n, st);
-        k_compact<<<blocks_for(n), kBlock, 0, st>>>(d, keep, rank);
+        MPS_COUNT_LAUNCH k_compact<<<blocks_for(n), kBlock, 0, st>>>(d, keep, rank);
         cudaMemcpyAsync(h_int, rank + n, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
         swap_state();
@@ -321,12 +322,12 @@ struct Solver {
     CCTStatusType grid() {
         const int n = d.n;
         if (n <= 0) return CCT_NOERR;
-        k_hash<<<blocks_for(n), kBlock, 0, st>>>(d);
+        MPS_COUNT_LAUNCH k_hash<<<blocks_for(n), kBlock, 0, st>>>(d);
         if (radix_sort_pairs(n, d.key, d.idx, 0, radix_passes((unsigned)(d.cells - 1)), sort_scratch, st)) return CCT_CUDAERR;
         cudaMemsetAsync(d.cstart, 0xff, sizeof(int) * d.cells, st);
         cudaMemsetAsync(d.cend, 0xff, sizeof(int) * d.cells, st);
         cudaMemsetAsync(d.cell_count, 0, sizeof(int), st);
-        k_gather<<<blocks_for(n), kBlock, 0, st>>>(d);
+        MPS_COUNT_LAUNCH k_gather<<<blocks_for(n), kBlock, 0, st>>>(d);
         swap_state();
         return cuda_status(cudaGetLastError());
     }
@@ -335,7 +336,7 @@ struct Solver {
         const int t = d.tri_n;
         if (t <= 0) return CCT_NOERR;
         if (!bin_off && cudaMalloc(&bin_off, sizeof(unsigned) * ((size_t)t + 2))) return CCT_MEMERR;
-        k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off);
+        MPS_COUNT_LAUNCH k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off);
         scan_exclusive(bin_off, t + 1, nullptr, st);
         cudaMemcpyAsync(h_int, bin_off + t, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
@@ -356,11 +357,11 @@ struct Solver {
         }
         int* vcell = bin_visit;
         d.tids = bin_visit + bin_visit_cap;
-        k_bin_fill<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, vcell, d.tids);
+        MPS_COUNT_LAUNCH k_bin_fill<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, vcell, d.tids);
         if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(d.cells - 1)), bin_sort, st))
             return CCT_CUDAERR;
         cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 2 * d.cells, st);
-        k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, st>>>((int)nv, vcell, d.tcs, d.tcs + d.cells);
+        MPS_COUNT_LAUNCH k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, st>>>((int)nv, vcell, d.tcs, d.tcs + d.cells);
         bins_dirty = 0;
         return cuda_status(cudaGetLastError());
     }
@@ -368,7 +369,7 @@ struct Solver {
     template <class T>
     void walls_distance() {
         if (d.tri_n > 0) {
-            k_wall_distance<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            MPS_COUNT_LAUNCH k_wall_distance<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
         } else {
             cudaMemsetAsync(d.wid, 0xff, sizeof(int) * d.n, st);
         }
@@ -387,11 +388,11 @@ struct Solver {
         timer.mark(PH_WALLS, st);
         if (d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
         walls_distance<T>();
-        if (d.drag_n > 0 && d.tri_n > 0) k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+        if (d.drag_n > 0 && d.tri_n > 0) MPS_COUNT_LAUNCH k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
         else cudaMemsetAsync(d.dragv, 0, sizeof(double) * 3 * d.n, st);
         timer.mark(PH_PRED, st);
         const int nb_grid = std::max(1, std::min(d.cells, d.n));
-        k_neighbours<T, NB_PREDICT><<<nb_grid, kNbThreads, 0, st>>>(d);
+        MPS_COUNT_LAUNCH k_neighbours<T, NB_PREDICT><<<nb_grid, kNbThreads, 0, st>>>(d);
         std::swap(d.pos, d.pos2);
         std::swap(d.vel, d.vel2);
         timer.mark(PH_GRID, st);
@@ -400,35 +401,42 @@ struct Solver {
         timer.mark(PH_WALLS, st);
         walls_distance<T>();
         timer.mark(PH_LIST, st);
-        k_neighbours<T, NB_LIST><<<std::max(1, std::min(d.cells, d.n)), kNbThreads, 0, st>>>(d);
+        MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST><<<std::max(1, std::min(d.cells, d.n)), kNbThreads, 0, st>>>(d);
         timer.mark(PH_SETUP, st);
         if (opt.pressure_mode == MPS_PRESSURE_EXPLICIT) {
-            k_eos<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            MPS_COUNT_LAUNCH k_eos<<<blocks_for(d.n), kBlock, 0, st>>>(d);
         } else {
-            k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
-            k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
+            MPS_COUNT_LAUNCH k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            MPS_COUNT_LAUNCH k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
             const bool use_learned = learned_ready && opt.learned;
             if (use_learned || collect) {
                 timer.mark(PH_LEARNED, st);
                 cudaMemcpyAsync(d.pprev, d.press, sizeof(double) * d.n, cudaMemcpyDeviceToDevice, st);
                 if (fp64())
-                    k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
+                    MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
                                                                                   d.r, d.rhs, 2);
                 else
-                    k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.press,
+                    MPS_COUNT_LAUNCH k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.press,
                                                                                  d.r, d.rhs, 2);
-                k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
-                k_features<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
+                MPS_COUNT_LAUNCH k_features<<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 if (use_learned) {
                     if (mlp_forward(mlp, d.n, d.feat, d.mlp_out, st)) return CCT_CUDAERR;
-                    k_learned_apply<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                    MPS_COUNT_LAUNCH k_learned_apply<<<blocks_for(d.n), kBlock, 0, st>>>(d, (opt.learned & 2) ? 1 : 0);
+                    if (fp64())
+                        MPS_COUNT_LAUNCH k_spmv<double, double, double, 2><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.z,
+                                                                                      d.q, d.r, 6);
+                    else
+                        MPS_COUNT_LAUNCH k_spmv<float, double, double, 2><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.z, d.q,
+                                                                                     d.r, 6);
+                    MPS_COUNT_LAUNCH k_learned_finish<<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 }
                 timer.mark(PH_SETUP, st);
             }
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
             if (use_learned && S.cg_relres > opt.cg_rtol) {
                 // the learned solve did not reach the tolerance: plain Jacobi-CG from the warm start
-                k_restore_plain<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                MPS_COUNT_LAUNCH k_restore_plain<<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 MpsStepStats S2{};
                 if ((rc = fp64() ? solve_fp64(S2) : solve_ir(S2))) return rc;
                 S.cg_iterations += S2.cg_iterations;
@@ -437,15 +445,15 @@ struct Solver {
                 S.error_flags = (S.error_flags & ~MPS_ERR_CG) | S2.error_flags;
                 S.fallback = 1;
             }
-            if (collect) k_targets<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            if (collect) MPS_COUNT_LAUNCH k_targets<<<blocks_for(d.n), kBlock, 0, st>>>(d);
         }
         timer.mark(PH_CORRECT, st);
-        k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+        MPS_COUNT_LAUNCH k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
         std::swap(d.pos, d.pos2);
         std::swap(d.vel, d.vel2);
         timer.mark(PH_WALLS, st);
         if (d.tri_n > 0 && walls_move) {
-            k_walls_move<<<blocks_for(d.tri_n), kBlock, 0, st>>>(d, step);
+            MPS_COUNT_LAUNCH k_walls_move<<<blocks_for(d.tri_n), kBlock, 0, st>>>(d, step);
             bins_dirty = 1;
         }
         timer.mark(PH_OTHER, st);
@@ -487,10 +495,10 @@ struct Solver {
         while (done < maxit + every) {
             for (int k = 0; k < every; ++k) {
                 timer.mark(PH_SPMV, st);
-                k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+                MPS_COUNT_LAUNCH k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
                 timer.mark(PH_VEC, st);
-                k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1);
-                k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
+                MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1);
+                MPS_COUNT_LAUNCH k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
                 ++spmv_launches;
             }
             done += every;
@@ -503,18 +511,18 @@ struct Solver {
     // plain FP64 Jacobi-PCG from the warm start in press
     CCTStatusType solve_fp64(MpsStepStats& S) {
         const double* w = (const double*)d.nbrw;
-        k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
         if (pull_scal()) return CCT_CUDAERR;
-        h_nnz[0] = h_scal[S_TMP0];
-        h_nnz[1] = h_scal[S_TMP1];
+        h_nnz[0] = h_scal[S_NNZ0];
+        h_nnz[1] = h_scal[S_NNZ1];
         const double bnorm = h_scal[S_BNORM];
         const double tol = opt.cg_rtol * bnorm;
-        k_cg_start<double><<<kRedBlocks, 256, 0, st>>>(d, d.r, d.z, d.p, nullptr, 1.0, d.minv, nullptr, nullptr, 3, tol,
+        MPS_COUNT_LAUNCH k_cg_start<double><<<kRedBlocks, 256, 0, st>>>(d, d.r, d.z, d.p, nullptr, 1.0, d.minv, nullptr, nullptr, 3, tol,
                                                        opt.cg_max_iter);
         const int it = cg_loop<double, double, double>(d.press, d.r, d.z, d.p, d.q, w, d.minv, nullptr, opt.cg_max_iter);
         if (it < 0) return CCT_CUDAERR;
         // true residual
-        k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
         if (pull_scal()) return CCT_CUDAERR;
         S.cg_iterations += it;
         S.b_norm = bnorm;
@@ -526,15 +534,15 @@ struct Solver {
     // FP32 Jacobi-PCG inside FP64 iterative refinement
     CCTStatusType solve_ir(MpsStepStats& S) {
         const float* w = (const float*)d.nbrw;
-        k_to_float<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.minv, d.m32);
+        MPS_COUNT_LAUNCH k_to_float<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.minv, d.m32);
         double bnorm = 0.0;
         int outer = 0;
         for (;;) {
-            k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+            MPS_COUNT_LAUNCH k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
             if (pull_scal()) return CCT_CUDAERR;
             if (outer == 0) {
-                h_nnz[0] = h_scal[S_TMP0];
-                h_nnz[1] = h_scal[S_TMP1];
+                h_nnz[0] = h_scal[S_NNZ0];
+                h_nnz[1] = h_scal[S_NNZ1];
             }
             bnorm = h_scal[S_BNORM];
             const double rn = h_scal[S_RNORM];
@@ -544,13 +552,13 @@ struct Solver {
             // 0.3 margin), but not below what FP32 CG reliably reaches (ir_inner_rtol)
             const double need = 0.3 * opt.cg_rtol * bnorm / rn;
             const double inner_tol = std::max(need, opt.ir_inner_rtol);
-            k_cg_start<float><<<kRedBlocks, 256, 0, st>>>(d, d.r32, d.z32, d.p32, d.r, 1.0 / rn, nullptr, d.m32, d.d32, 3,
+            MPS_COUNT_LAUNCH k_cg_start<float><<<kRedBlocks, 256, 0, st>>>(d, d.r32, d.z32, d.p32, d.r, 1.0 / rn, nullptr, d.m32, d.d32, 3,
                                                           inner_tol, opt.cg_max_iter);
             const int it = cg_loop<float, float, float>(d.d32, d.r32, d.z32, d.p32, d.q32, w, nullptr, d.m32,
                                                         opt.cg_max_iter);
             if (it < 0) return CCT_CUDAERR;
             S.cg_iterations += it;
-            k_axpy_ir<<<kRedBlocks, 256, 0, st>>>(d, d.press, d.d32, rn);
+            MPS_COUNT_LAUNCH k_axpy_ir<<<kRedBlocks, 256, 0, st>>>(d, d.press, d.d32, rn);
             ++outer;
         }
         S.ir_passes = outer;
@@ -565,12 +573,12 @@ struct Solver {
         if (!e) e = cudaMemcpyAsync(stage + 3 * n, v3, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(stage + 6 * n, pr, sizeof(double) * n, cudaMemcpyHostToDevice, st);
         if (e) return CCT_CUDAERR;
-        k_pack_state<<<blocks_for(d.n), kBlock, 0, st>>>(d, stage, stage + 3 * n, stage + 6 * n);
+        MPS_COUNT_LAUNCH k_pack_state<<<blocks_for(d.n), kBlock, 0, st>>>(d, stage, stage + 3 * n, stage + 6 * n);
         return cuda_status(cudaGetLastError());
     }
     CCTStatusType download(double* p3, double* v3, double* pr) {
         const size_t n = d.n;
-        k_unpack_state<<<blocks_for(d.n), kBlock, 0, st>>>(d, stage, stage + 3 * n, stage + 6 * n);
+        MPS_COUNT_LAUNCH k_unpack_state<<<blocks_for(d.n), kBlock, 0, st>>>(d, stage, stage + 3 * n, stage + 6 * n);
         cudaError_t e = cudaMemcpyAsync(p3, stage, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st);
         if (!e) e = cudaMemcpyAsync(v3, stage + 3 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, st);
         if (!e) e = cudaMemcpyAsync(pr, stage + 6 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, st);

@@ -13,7 +13,7 @@ import numpy as np
 from . import lib
 from .types import MpsError
 
-NPARAMS = 35330
+NPARAMS = 34946   # 12*128+128 + 2*(128*128+128) + 128*2+2
 P = C.c_void_p
 _SIGS = {
     "mps_gemm_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, P, C.c_int, C.c_int, P, C.c_int, P,

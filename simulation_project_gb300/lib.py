@@ -37,8 +37,10 @@ _SIGS = {
     "mps_event_record": (I, [P, P]),
     "mps_event_elapsed_ms": (I, [P, P, C.POINTER(C.c_float)]),
     "mps_last_error": (C.c_char_p, []),
+    "mps_clear_error": (None, []),
     "mps_scratch_bytes": (C.c_size_t, []),
     "mps_build_info": (C.c_char_p, []),
+    "mps_kernel_launches": (C.c_ulonglong, []),
     # reference-named launcher API (include/mps_device_process.h)
     "CalcTurbulenceViscosity": (I, [C.POINTER(P), I]),
     "CheckParticleOutsideComputeZone": (I, [C.POINTER(P), C.POINTER(I)]),
@@ -94,6 +96,11 @@ def call(name: str, *args):
     if st != 0:
         raise MpsError(st, f"{name} ({load().mps_last_error().decode()})")
     return st
+
+
+def kernel_launches() -> int:
+    """Kernels the library has launched since it was loaded."""
+    return int(load().mps_kernel_launches())
 
 
 class DeviceArray:

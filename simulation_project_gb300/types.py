@@ -253,3 +253,5 @@ CELL_DTYPE = np.dtype([("m_TriangleNum", "<u4"), ("m_TriangleID", "<i4", CELLMAX
 assert TRIANGLE_DTYPE.itemsize == C.sizeof(CTriangle)
 assert DISTANCE_DTYPE.itemsize == C.sizeof(CDistance)
 assert CELL_DTYPE.itemsize == C.sizeof(CCell)
+
+CParticle_size = 52   # sizeof(CParticle) (DataType.h:220-240)

@@ -98,17 +98,23 @@ def test_learned_solver_converges_and_reports_gain():
     plain = Solver(sc, precision="fp32_ir")
     learned = Solver(sc, precision="fp32_ir", learned=1)
     learned.set_learned(p)
-    it_p, it_l = 0, 0
+    scaled = Solver(sc, precision="fp32_ir", learned=3)
+    scaled.set_learned(p)
+    it_p, it_l, it_s = 0, 0, 0
     for i in range(8):
         sp = plain.step(i)
         sl = learned.step(i)
-        assert sp["cg_relres"] <= 1e-8 and sl["cg_relres"] <= 1e-8
-        assert sl["error_flags"] == 0
+        ss = scaled.step(i)
+        for s in (sp, sl, ss):
+            assert s["cg_relres"] <= 1e-8 and s["error_flags"] == 0, s
         if i >= 2:
             it_p += sp["cg_iterations"]
             it_l += sl["cg_iterations"]
-    print(f"\nCG iterations steps 2-7: plain {it_p}, learned {it_l}, saved {it_p - it_l} "
-          f"({100.0 * (it_p - it_l) / max(it_p, 1):.1f}%); training {info}")
+            it_s += ss["cg_iterations"]
+    print(f"\nCG iterations steps 2-7: plain {it_p}, learned guess {it_l} (saved {it_p - it_l}, "
+          f"{100.0 * (it_p - it_l) / max(it_p, 1):.1f}%), guess+scaling {it_s}; training {info}")
+    # the line-searched guess is never worse than the warm start in A-norm
+    assert it_l <= it_p * 1.05 + 2
     a, b = plain.state(), learned.state()
     assert np.array_equal(a["id"], b["id"])
     pm = np.abs(a["press"]).max()

@@ -34,3 +34,12 @@ def test_bf16_rounding_is_nearest_even():
     assert r[1] == 1.0            # tie -> even
     assert r[2] == 1.0078125      # above tie -> up
     assert np.all(np.abs(r - x) <= np.abs(x) * 2 ** -8)
+
+
+def test_parameter_count_matches_headers_and_binding():
+    import re
+    from simulation_project_gb300 import learned
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = open(os.path.join(root, "include", "mps_solver.h")).read()
+    n = int(re.search(r"#define MPS_MLP_PARAMS (\d+)", hdr).group(1))
+    assert n == mo.NPARAMS == learned.NPARAMS
