@@ -70,6 +70,13 @@ CCTStatusType reorderDataAndFindCellStart(MPS_STREAM_REF Stream, Integer numPart
                                           int* cellEnd);
 CCTStatusType SortUsingThrust(Integer MaxParticleNum, Integer* daNumberHash, Integer* daNumberIndex);
 CCTStatusType StableSortUsingThrust(Integer MaxParticleNum, Integer* daNumberHash, Integer* daNumberIndex);
+/* No counterpart in the reference.  SortUsingThrust for callers that cannot allocate
+ * device memory (an allocator hook, a pre-reserved memory pool, a real-time path):
+ * same result, but its scratch is one static __device__ array of about 2.1 MiB held by
+ * every GPU that loads the library.  At most 262,144 keys (more: CCT_PARAMERR, arrays
+ * untouched).  The first call on a device looks up the array's address; make it before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+CCTStatusType SortUsingThrustNoAlloc(Integer MaxParticleNum, Integer* daNumberHash, Integer* daNumberIndex);
 
 /* one-time binding calls */
 CCTStatusType InitializeDeviceMemConst(CParameter Parameter, Integer ParticleNum, CTriangle* Triangles,

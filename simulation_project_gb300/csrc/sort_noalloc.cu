@@ -1,0 +1,97 @@
+// sort_noalloc.cu - SortUsingThrustNoAlloc: the stable (key, index) radix sort of
+// SortUsingThrust for callers that cannot allocate device memory.
+//
+// Who needs it: code that runs where cudaMalloc is not allowed or not wanted -- inside
+// an allocator hook or a memory-pool callback (allocating would recurse), in a process
+// whose device memory is pre-reserved and fenced by a host framework, or on a
+// real-time path where a driver allocation (and its implicit synchronisation) is not
+// acceptable.  SortUsingThrust takes no scratch argument and grows library-owned
+// buffers with cudaMalloc; this variant uses one file-scope __device__ array instead.
+//
+// Limits and rules:
+//   * at most kNoAllocMaxKeys = 262,144 keys per call; larger n returns CCT_PARAMERR
+//     (mps_last_error() says why) without touching the arrays;
+//   * the array (2,228,768 bytes, about 2.1 MiB) lives in every GPU that loads the
+//     library, until the process exits;
+//   * the first call on a device looks up the array's device address with
+//     cudaGetSymbolAddress (once per device, with that device current); make that first
+//     call before any stream capture;
+//   * every call shares the array, and it keeps the last call's contents: the sort
+//     writes each scratch word before it reads it (min/max re-initialised, histograms
+//     fully rewritten per pass), so nothing is stale -- but calls that overlap on the
+//     GPU (from several host threads or streams) race on it and must be serialised;
+//   * like SortUsingThrust it runs on the legacy default stream and returns after the
+//     sort has finished.
+#include <stdio.h>
+
+#include "mps_common.cuh"
+#include "mps_internal.h"
+#include "../../include/mps_device_process.h"
+
+namespace mps {
+namespace {
+
+constexpr int kNoAllocMaxKeys = 1 << 18;
+constexpr int kNoAllocTile = 2048;      // keys per radix tile (sort.cu)
+constexpr int kNoAllocRadix = 256;      // digits per pass
+constexpr size_t kNoAllocHeader = 256;  // min/max words, padded to the array alignment
+constexpr size_t kNoAllocSortBytes =
+    sizeof(int) * 2 * (size_t)kNoAllocMaxKeys +
+    sizeof(unsigned) * ((size_t)kNoAllocRadix * ((kNoAllocMaxKeys + kNoAllocTile - 1) / kNoAllocTile) + 8) + 256;
+constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocSortBytes;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices];
+
+// device address of the array for the current device (looked up once per device)
+CCTStatusType noalloc_scratch(void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        note_error("SortUsingThrustNoAlloc: cudaGetDevice", e);
+        return CCT_CUDAERR;
+    }
+    if (dev < 0 || dev >= kMaxDevices) return CCT_PARAMERR;
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            note_error("SortUsingThrustNoAlloc: cudaGetSymbolAddress", e);
+            return CCT_CUDAERR;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return CCT_NOERR;
+}
+
+}  // namespace
+}  // namespace mps
+
+using namespace mps;
+
+extern "C" CCTStatusType SortUsingThrustNoAlloc(Integer MaxParticleNum, Integer* daNumberHash, Integer* daNumberIndex) {
+    const int n = MaxParticleNum;
+    if (n > kNoAllocMaxKeys) {
+        note_error("SortUsingThrustNoAlloc: more keys than the 262144 its static scratch holds", cudaErrorInvalidValue);
+        return CCT_PARAMERR;
+    }
+    if (n <= 1) return CCT_NOERR;
+    if (radix_scratch_bytes(n) > kNoAllocSortBytes) return CCT_PARAMERR;
+    void* base = nullptr;
+    CCTStatusType rc = noalloc_scratch(&base);
+    if (rc != CCT_NOERR) return rc;
+    int* mm = (int*)base;
+    void* scr = (char*)base + kNoAllocHeader;
+    cudaStream_t st = 0;
+    MPS_CUDA_TRY(key_minmax(n, daNumberHash, mm, st));
+    int h[2];
+    MPS_CUDA_TRY(cudaMemcpyAsync(h, mm, sizeof(h), cudaMemcpyDeviceToHost, st));
+    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    const int passes = radix_passes((unsigned)h[1] - (unsigned)h[0]);
+    MPS_CUDA_TRY(radix_sort_pairs(n, daNumberHash, daNumberIndex, h[0], passes, scr, st));
+    MPS_CUDA_TRY(cudaStreamSynchronize(st));
+    return cuda_status(cudaGetLastError());
+}
