@@ -32,17 +32,20 @@ template <class T> __device__ __forceinline__ V3<T> v3(T x, T y, T z) { V3<T> r;
 // ---------------------------------------------------------------------------
 // deterministic block + grid reductions (last CTA finishes the sum)
 // ---------------------------------------------------------------------------
-template <int NV>
+// TS: type of the in-warp shuffle stage (float for the FP32 inner solve, whose
+// per-thread partials are float anyway; the FP64 pipe is narrow on GB300); the
+// cross-warp and cross-block stages are always FP64.
+template <int NV, class TS = double>
 __device__ __forceinline__ bool grid_reduce(double (&v)[NV], double* red, unsigned* counter, double (&out)[NV]) {
     __shared__ double sm[NV][32];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        double x = v[k];
+        TS x = (TS)v[k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sm[k][w] = x;
+        if (lane == 0) sm[k][w] = (double)x;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -610,6 +613,7 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
     double part0 = 0.0, part1 = 0.0;
     const double coef = d.c.coef_lap;
     using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE != 0), double, float>::type;
+    TA partw = TA(0);   // MODE 0 partial dot, in the arithmetic type
     for (int sl = gw; sl < nslices; sl += nw) {
         const int i = sl * 32 + lane;
         const bool row = i < d.n;
@@ -644,7 +648,7 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
         const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
         if (MODE == 0) {
             y[i] = (TY)yi;
-            part0 += (double)x[i] * (double)(TY)yi;
+            partw += (TA)x[i] * (TA)(TY)yi;
         } else if (MODE == 2) {
             y[i] = (TY)yi;
             part0 += (double)x[i] * yi;
@@ -656,8 +660,10 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
             part1 += b[i] * b[i];
         }
     }
+    if (MODE == 0) part0 = (double)partw;
     double v[2] = {part0, part1}, out[2];
-    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+    if (grid_reduce<2, typename std::conditional<MODE == 0, TA, double>::type>(v, d.red, d.red_count + slot, out) &&
+        threadIdx.x == 0) {
         if (MODE == 0) {
             d.scal[S_PQ] = out[0];
             d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
@@ -678,21 +684,23 @@ template <class TV>
 __global__ void __launch_bounds__(256) k_cg_start(const __grid_constant__ Dev d, TV* r, TV* z, TV* p, const double* r64,
                                                   double scale, const double* m64, const float* m32, TV* xd, int slot,
                                                   double tol_abs, int maxit) {
-    double prz = 0.0, prr = 0.0;
+    // element arithmetic in TV (FP32 for the inner solve: GB300's FP64 pipe is narrow);
+    // per-thread partial dots in TV over <= a few rows, cross-thread sums in FP64
+    TV prz = TV(0), prr = TV(0);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
-        double ri = r64 ? r64[i] * scale : (double)r[i];
-        if (!d.inner[i]) ri = 0.0;
-        const double mi = m32 ? (double)m32[i] : m64[i];
-        const TV rv = (TV)ri, zv = (TV)(ri * mi);
+        TV rv = r64 ? (TV)(r64[i] * scale) : r[i];
+        if (!d.inner[i]) rv = TV(0);
+        const TV mi = m32 ? (TV)m32[i] : (TV)m64[i];
+        const TV zv = rv * mi;
         r[i] = rv;
         z[i] = zv;
         p[i] = zv;
         if (xd) xd[i] = TV(0);
-        prz += (double)rv * (double)zv;
-        prr += (double)rv * (double)rv;
+        prz += rv * zv;
+        prr += rv * rv;
     }
-    double v[2] = {prz, prr}, out[2];
-    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+    double v[2] = {(double)prz, (double)prr}, out[2];
+    if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
         d.scal[S_RZ] = out[0];
         d.scal[S_RNORM] = sqrt(out[1]);
         d.scal[S_R0NORM] = sqrt(out[1]);
@@ -708,21 +716,21 @@ template <class TV, class TXA>
 __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d, TXA* x, TV* r, TV* z, const TV* p,
                                                    const TV* q, const double* m64, const float* m32, int slot) {
     if (d.scal[S_CONV] != 0.0) return;
-    const double alpha = d.scal[S_ALPHA];
-    double prz = 0.0, prr = 0.0;
+    const TV alpha = (TV)d.scal[S_ALPHA];
+    TV prz = TV(0), prr = TV(0);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
         if (!d.inner[i]) continue;
-        x[i] = (TXA)((double)x[i] + alpha * (double)p[i]);
-        const TV ri = (TV)((double)r[i] - alpha * (double)q[i]);
+        x[i] = x[i] + (TXA)alpha * (TXA)p[i];
+        const TV ri = r[i] - alpha * q[i];
         r[i] = ri;
-        const double mi = m32 ? (double)m32[i] : m64[i];
-        const TV zi = (TV)((double)ri * mi);
+        const TV mi = m32 ? (TV)m32[i] : (TV)m64[i];
+        const TV zi = ri * mi;
         z[i] = zi;
-        prz += (double)ri * (double)zi;
-        prr += (double)ri * (double)ri;
+        prz += ri * zi;
+        prr += ri * ri;
     }
-    double v[2] = {prz, prr}, out[2];
-    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+    double v[2] = {(double)prz, (double)prr}, out[2];
+    if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
         const double rz = d.scal[S_RZ];
         d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
         d.scal[S_RZ] = out[0];
@@ -737,9 +745,9 @@ __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d
 template <class TV>
 __global__ void k_cg_p(const __grid_constant__ Dev d, TV* p, const TV* z) {
     if (d.scal[S_CONV] != 0.0) return;
-    const double beta = d.scal[S_BETA];
+    const TV beta = (TV)d.scal[S_BETA];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)
-        p[i] = (TV)((double)z[i] + beta * (double)p[i]);
+        p[i] = z[i] + beta * p[i];
 }
 
 // neighbour-entry counts: interior rows (PPE matrix) and all rows

@@ -183,9 +183,9 @@ cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, 
     int* vb = valt;
     for (int pass = 0; pass < passes; ++pass) {
         const int shift = pass * 8;
-        k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts);
-        k_scan_excl<<<1, 1024, 0, st>>>(counts, kRadix * tiles, nullptr);
-        k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, kmin, shift, tiles, counts);
+        MPS_COUNT_LAUNCH k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts);
+        MPS_COUNT_LAUNCH k_scan_excl<<<1, 1024, 0, st>>>(counts, kRadix * tiles, nullptr);
+        MPS_COUNT_LAUNCH k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, kmin, shift, tiles, counts);
         int* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
     }
@@ -197,15 +197,15 @@ cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, 
 }
 
 cudaError_t key_minmax(int n, const int* keys, int* mm_dev, cudaStream_t st) {
-    k_minmax_init<<<1, 1, 0, st>>>(mm_dev);
+    MPS_COUNT_LAUNCH k_minmax_init<<<1, 1, 0, st>>>(mm_dev);
     const int blocks = min(div_up(n, 1024), 152 * 4);
-    if (n > 0) k_minmax<<<blocks, 1024, 0, st>>>(keys, n, mm_dev);
+    if (n > 0) MPS_COUNT_LAUNCH k_minmax<<<blocks, 1024, 0, st>>>(keys, n, mm_dev);
     return cudaGetLastError();
 }
 
 cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st) {
     if (len <= 0) return cudaSuccess;
-    k_scan_excl<<<1, 1024, 0, st>>>(a, len, total_dev);
+    MPS_COUNT_LAUNCH k_scan_excl<<<1, 1024, 0, st>>>(a, len, total_dev);
     return cudaGetLastError();
 }
 
