@@ -200,14 +200,19 @@ def run_gpu(args):
     plain.close()
     pps_plain = n * args.steps / (ms_plain / 1e3)
 
-    # FP32 / FP64-refined solver without the network
-    ir = Solver(scene, precision="fp32_ir", profile=0)
+    # FP32 / FP64-refined solver without the network: Jacobi, then multilevel
+    ir = Solver(scene, precision="fp32_ir", profile=0, preconditioner=0)
     ms_ir, _, st_ir = time_steps(ir, args.steps, args.warmup)
     ir.close()
     pps_ir = n * args.steps / (ms_ir / 1e3)
+    irm = Solver(scene, precision="fp32_ir", profile=0, preconditioner=1)
+    ms_irm, _, st_irm = time_steps(irm, args.steps, args.warmup)
+    irm.close()
+    pps_irm = n * args.steps / (ms_irm / 1e3)
 
     # learned FP32 / FP64-refined solver (metric numerator), with phase timing
-    fast = Solver(scene, precision="fp32_ir", profile=1, learned=args.learned_mode if params is not None else 0)
+    fast = Solver(scene, precision="fp32_ir", profile=1, preconditioner=args.precond,
+                  learned=args.learned_mode if params is not None else 0)
     if params is not None:
         fast.set_learned(params)
     clocks = ClockSampler(local)
@@ -233,7 +238,7 @@ def run_gpu(args):
                 "avg_launch_us": round(avg_ms * 1e3, 2)}
     phases = {k: round(float(np.mean([s[k] for s in st_fast])), 3) for k in
               ("ms_grid", "ms_walls", "ms_predictor", "ms_list", "ms_ppe_setup", "ms_spmv", "ms_cg_vec",
-               "ms_correct", "ms_learned")}
+               "ms_correct", "ms_learned", "ms_precond")}
 
     # end to end through the C-ABI from pinned host buffers
     e2e = run_e2e(fast, args)
@@ -262,17 +267,24 @@ def run_gpu(args):
                        "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_plain])),
                        "relres_max": float(max(s["cg_relres"] for s in st_plain))},
         "speedup_vs_plain_fp64": pps_fast / pps_plain,
-        "fp32_ir_without_network": {"value": pps_ir, "ms_per_step": ms_ir / args.steps,
-                                    "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_ir])),
-                                    "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_ir]))},
-        "network_iterations_saved_per_step": float(np.mean([s["cg_iterations"] for s in st_ir]) -
-                                                   np.mean([s["cg_iterations"] for s in st_fast])),
+        "fp32_ir_jacobi_without_network": {"value": pps_ir, "ms_per_step": ms_ir / args.steps,
+                                           "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_ir])),
+                                           "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_ir]))},
+        "fp32_ir_multilevel_without_network": {
+            "value": pps_irm, "ms_per_step": ms_irm / args.steps,
+            "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_irm])),
+            "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_irm]))},
+        "network_iterations_saved_per_step": float(
+            np.mean([s["cg_iterations"] for s in (st_irm if args.precond else st_ir)]) -
+            np.mean([s["cg_iterations"] for s in st_fast])),
         "fast_solver": {"cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_fast])),
                         "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_fast])),
                         "relres_max": float(max(s["cg_relres"] for s in st_fast)),
                         "fallbacks": int(sum(s["fallback"] for s in st_fast)),
                         "error_flags": int(np.bitwise_or.reduce([s["error_flags"] for s in st_fast])),
-                        "learned": params is not None, "phases_ms": phases},
+                        "learned": params is not None, "preconditioner": ["jacobi", "multilevel"][args.precond],
+                        "mg_levels": int(st_fast[-1]["mg_levels"]), "mg_level1": int(st_fast[-1]["mg_level1"]),
+                        "phases_ms": phases},
         "learned_training": train_info,
         "roofline": roofline,
         "e2e": e2e,
@@ -293,12 +305,13 @@ def run_profile_case(args):
     from simulation_project_gb300.solver import Solver
     lib.load()
     scene = build_scene(args.l0)
-    s = Solver(scene, precision="fp64" if args.fp64 else "fp32_ir", profile=1)
+    s = Solver(scene, precision="fp64" if args.fp64 else "fp32_ir", profile=1, preconditioner=args.precond)
     ms, _, st = time_steps(s, args.steps, args.warmup)
     s.close()
     print(json.dumps({"profile_case": True, "particles": scene.n, "ms_per_step": ms / args.steps,
                       "phases": {k: st[-1][k] for k in st[-1] if k.startswith("ms_")},
-                      "spmv_launches": st[-1]["spmv_launches"], "nnz": st[-1]["nnz"]}))
+                      "spmv_launches": st[-1]["spmv_launches"], "nnz": st[-1]["nnz"],
+                      "cg_iterations": st[-1]["cg_iterations"], "mg_levels": st[-1]["mg_levels"]}))
     return 0
 
 
@@ -412,6 +425,7 @@ def main():
     ap.add_argument("--train-steps", type=int, default=6)
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-mode", type=int, default=1, help="bit 0 initial guess, bit 1 diagonal scaling")
+    ap.add_argument("--precond", type=int, default=1, help="0 Jacobi, 1 multilevel (FP32 inner solve)")
     ap.add_argument("--profile-case", action="store_true", help="only the solver steps (for ncu captures)")
     ap.add_argument("--fp64", action="store_true", help="with --profile-case: the plain FP64 solver")
     args = ap.parse_args()

@@ -37,6 +37,13 @@ typedef struct MpsSolver MpsSolver;
 
 enum { MPS_PREC_FP64 = 0, MPS_PREC_FP32_IR = 1 };
 enum { MPS_PRESSURE_PPE = 0, MPS_PRESSURE_EXPLICIT = 1 };
+/* preconditioner of the FP32 inner CG (the FP64 solver is always Jacobi):
+ *   MPS_PRECOND_JACOBI      diagonal
+ *   MPS_PRECOND_MULTILEVEL  diagonal + cell-aggregate coarse correction: level-1 unknowns
+ *                           are the non-empty neighbour-search cells, coarser levels
+ *                           aggregate 2x2x2 cells down to <= 128 unknowns (explicit
+ *                           inverse there), one weighted-Jacobi V-cycle per application */
+enum { MPS_PRECOND_JACOBI = 0, MPS_PRECOND_MULTILEVEL = 1 };
 
 typedef struct MpsSolverOptions {
     int precision;          /* MPS_PREC_* */
@@ -55,6 +62,8 @@ typedef struct MpsSolverOptions {
     int check_every;        /* CG convergence is read back every this many iterations */
     double source_relaxation; /* gamma in b = gamma rho/dt^2 (n* - n0)/n0 (Tanaka & Masunaga 2010) */
     int profile;            /* 1: time every phase with CUDA events on the solver stream */
+    int preconditioner;     /* MPS_PRECOND_* (FP32_IR) */
+    double mg_omega;        /* Jacobi weight of the multilevel smoothing sweeps */
 } MpsSolverOptions;
 
 typedef struct MpsStepStats {
@@ -72,6 +81,9 @@ typedef struct MpsStepStats {
     /* phase times [ms] and launch counts (profile = 1 only) */
     float ms_grid, ms_walls, ms_predictor, ms_list, ms_ppe_setup, ms_spmv, ms_cg_vec, ms_correct, ms_learned;
     int spmv_launches;
+    float ms_precond;       /* multilevel setup and V-cycles */
+    int mg_levels;          /* coarse levels of the multilevel preconditioner (0: Jacobi) */
+    int mg_level1;          /* level-1 aggregates */
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);

@@ -1,0 +1,395 @@
+// coarse.cuh - cell-aggregate multilevel preconditioner of the FP32 inner PPE solve.
+//
+// M^-1 r = D^-1 r + P1 V(P1^T r): the Jacobi part plus a coarse correction whose
+// level-1 unknowns are the non-empty cells of the neighbour-search grid (one
+// aggregate per cell, piecewise-constant prolongation P1 over its interior
+// particles).  Level l+1 aggregates the 2x2x2 cells of level l, until at most
+// kMgMaxDense aggregates remain; that level is solved with an explicit inverse.
+// V is one V-cycle with weighted-Jacobi smoothing (one sweep down, one up), a
+// symmetric operator, so plain PCG applies.  Coarse operators are Galerkin
+// products A_{l+1} = P^T A_l P stored as 27-point stencils (cells interact only
+// with their 26 neighbours because the Laplacian radius equals the cell size).
+//
+// Every sum has a fixed order (per-thread shared-memory columns, per-lane slot
+// ownership, child cells in a fixed order), so the preconditioner is deterministic.
+#pragma once
+
+namespace mps {
+
+constexpr int kMgMaxLevels = 10;
+constexpr int kMgMaxDense = 128;
+constexpr int kMgAsmThreads = 128;
+
+struct MgLevel {
+    int n;             // aggregates
+    int gx, gy, gz;    // grid of this level
+    int* cmap;         // [cells] cell -> aggregate or -1
+    int* ccell;        // [n] aggregate -> cell
+    int* nb;           // [27 n] neighbour aggregates (-1: none), slot (dx+1)*9+(dy+1)*3+(dz+1)
+    int* par;          // [n] aggregate of the next level containing it (-1 on the last level)
+    float* a;          // [27 n] Galerkin stencil
+    float* dinv;       // [n] 1 / diagonal (0 for an aggregate without interior particles)
+    float* r;          // [n] restricted residual
+    float* e;          // [n] correction after the down sweep
+    float* e2;         // [n] correction after the up sweep (the level's result)
+};
+
+struct Mg {
+    int levels;        // levels in use: 1 .. levels, the last one solved densely
+    float omega;       // Jacobi weight of the smoothing sweeps
+    MgLevel L[kMgMaxLevels + 1];   // L[0] unused
+    float* ainv;       // [n_last^2] inverse of the last level's matrix
+    int* agg1;         // [n] particle -> level-1 aggregate
+    unsigned* pcc;     // [n] cell coordinates of the particle, 10 bits each (x<<20 | y<<10 | z)
+};
+
+__device__ __forceinline__ void mg_decode(int c, int gy, int gz, int& x, int& y, int& z) {
+    x = c / (gy * gz);
+    y = (c / gz) % gy;
+    z = c % gz;
+}
+__device__ __forceinline__ int mg_slot_dx(int s) { return s / 9 - 1; }
+__device__ __forceinline__ int mg_slot_dy(int s) { return (s / 3) % 3 - 1; }
+__device__ __forceinline__ int mg_slot_dz(int s) { return s % 3 - 1; }
+
+// ---------------------------------------------------------------------------
+// setup: aggregates, links, operators (once per step)
+// ---------------------------------------------------------------------------
+// level-1 occupancy: a grid cell is an aggregate when it holds particles
+__global__ void k_mg_flags1(const __grid_constant__ Dev d, unsigned* flag) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < d.cells) flag[c] = d.cstart[c] >= 0 ? 1u : 0u;
+}
+
+// level l occupancy from the 2x2x2 children at level l-1
+__global__ void k_mg_flags_up(MgLevel lo, MgLevel hi, unsigned* flag) {
+    const int C = blockIdx.x * blockDim.x + threadIdx.x;
+    if (C >= hi.gx * hi.gy * hi.gz) return;
+    int X, Y, Z;
+    mg_decode(C, hi.gy, hi.gz, X, Y, Z);
+    unsigned any = 0;
+    for (int q = 0; q < 8; ++q) {
+        const int x = 2 * X + (q >> 2), y = 2 * Y + ((q >> 1) & 1), z = 2 * Z + (q & 1);
+        if (x < lo.gx && y < lo.gy && z < lo.gz && lo.cmap[(x * lo.gy + y) * lo.gz + z] >= 0) any = 1;
+    }
+    flag[C] = any;
+}
+
+// aggregate numbering from the exclusive scan of the occupancy (pre[cells] = total)
+__global__ void k_mg_fill(MgLevel lv, const unsigned* pre) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= lv.gx * lv.gy * lv.gz) return;
+    const unsigned f = pre[c + 1] - pre[c];
+    lv.cmap[c] = f ? (int)pre[c] : -1;
+    if (f) lv.ccell[pre[c]] = c;
+}
+
+// neighbour aggregates and parent of every aggregate of a level
+__global__ void k_mg_links(MgLevel lv, MgLevel up, int has_up) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= lv.n) return;
+    int x, y, z;
+    mg_decode(lv.ccell[I], lv.gy, lv.gz, x, y, z);
+    for (int s = 0; s < 27; ++s) {
+        const int xx = x + mg_slot_dx(s), yy = y + mg_slot_dy(s), zz = z + mg_slot_dz(s);
+        const bool in = xx >= 0 && yy >= 0 && zz >= 0 && xx < lv.gx && yy < lv.gy && zz < lv.gz;
+        lv.nb[(size_t)I * 27 + s] = in ? lv.cmap[(xx * lv.gy + yy) * lv.gz + zz] : -1;
+    }
+    lv.par[I] = has_up ? up.cmap[((x >> 1) * up.gy + (y >> 1)) * up.gz + (z >> 1)] : -1;
+}
+
+// per particle: level-1 aggregate and packed cell coordinates
+__global__ void k_mg_particles(const __grid_constant__ Dev d, const __grid_constant__ Mg mg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int c = d.key[i];
+    if (c < 0 || c >= d.cells) {
+        mg.agg1[i] = -1;
+        mg.pcc[i] = 0xffffffffu;
+        return;
+    }
+    int x, y, z;
+    mg_decode(c, d.box.m_GridSize.y, d.box.m_GridSize.z, x, y, z);
+    mg.pcc[i] = ((unsigned)x << 20) | ((unsigned)y << 10) | (unsigned)z;
+    mg.agg1[i] = mg.L[1].cmap[c];
+}
+
+// Level-1 Galerkin stencil: CTA per aggregate (cell).  A1[I, J] = sum over interior
+// i in I and interior neighbours j in J of A_ij; A1[I, I] adds the diagonals.  Each
+// thread owns one shared-memory column of 27 partial sums (no atomics, fixed order).
+template <class TW>
+__global__ void __launch_bounds__(kMgAsmThreads) k_mg_assemble1(const __grid_constant__ Dev d,
+                                                               const __grid_constant__ Mg mg,
+                                                               const TW* __restrict__ w) {
+    __shared__ float acc[27][kMgAsmThreads];
+    __shared__ double dsum[kMgAsmThreads];
+    __shared__ float slot_sum[28];
+    const MgLevel& L1 = mg.L[1];
+    const int I = blockIdx.x;
+    if (I >= L1.n) return;
+    const int tid = threadIdx.x;
+    const int c = L1.ccell[I];
+    int cx, cy, cz;
+    mg_decode(c, d.box.m_GridSize.y, d.box.m_GridSize.z, cx, cy, cz);
+    for (int s = 0; s < 27; ++s) acc[s][tid] = 0.f;
+    double ds = 0.0;
+    const int b = d.cstart[c], e = d.cend[c];
+    for (int i = b + tid; i < e; i += kMgAsmThreads) {
+        if (!d.inner[i]) continue;
+        ds += d.diag[i];
+        const int cnt = d.nbr_cnt[i];
+        for (int k = 0; k < cnt; ++k) {
+            const size_t ek = sell_index(i, k, d.K);
+            const int j = d.nbr[ek];
+            if (!d.inner[j]) continue;
+            const unsigned pj = mg.pcc[j];
+            const int dx = (int)(pj >> 20) - cx, dy = (int)((pj >> 10) & 1023u) - cy, dz = (int)(pj & 1023u) - cz;
+            if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
+            acc[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)][tid] += (float)w[ek];
+        }
+    }
+    dsum[tid] = ds;
+    __syncthreads();
+    const int warp = tid >> 5, lane = tid & 31;
+    for (int s = warp; s < 28; s += kMgAsmThreads / 32) {
+        if (s < 27) {
+            float v = 0.f;
+            for (int q = lane; q < kMgAsmThreads; q += 32) v += acc[s][q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) slot_sum[s] = v;
+        } else {
+            double v = 0.0;
+            for (int q = lane; q < kMgAsmThreads; q += 32) v += dsum[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) slot_sum[27] = (float)v;
+        }
+    }
+    __syncthreads();
+    if (tid < 27) {
+        const float coef = (float)d.c.coef_lap;
+        const float v = tid == 13 ? slot_sum[27] - coef * slot_sum[13] : -coef * slot_sum[tid];
+        L1.a[(size_t)I * 27 + tid] = v;
+        if (tid == 13) L1.dinv[I] = v > 0.f ? 1.f / v : 0.f;
+    }
+}
+
+// Galerkin stencil of level hi from level lo: warp per hi aggregate.  The 8 x 28
+// (child, slot) terms are spread over the lanes (7 each); each term's target slot
+// and value go to shared memory, then lane s sums the values of slot s in term
+// order (fixed order: deterministic).
+constexpr int kMgCoarsenWarps = 8;
+__global__ void __launch_bounds__(kMgCoarsenWarps * 32) k_mg_coarsen(MgLevel lo, MgLevel hi) {
+    __shared__ float val[kMgCoarsenWarps][224];
+    __shared__ signed char slot2[kMgCoarsenWarps][224];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int I2 = blockIdx.x * kMgCoarsenWarps + wib;
+    if (I2 >= hi.n) return;   // warp-uniform
+    int X, Y, Z;
+    mg_decode(hi.ccell[I2], hi.gy, hi.gz, X, Y, Z);
+    int child = -1;
+    if (lane < 8) {
+        const int x = 2 * X + (lane >> 2), y = 2 * Y + ((lane >> 1) & 1), z = 2 * Z + (lane & 1);
+        if (x < lo.gx && y < lo.gy && z < lo.gz) child = lo.cmap[(x * lo.gy + y) * lo.gz + z];
+    }
+    for (int t = lane; t < 224; t += 32) {
+        const int q = t / 28, s = t % 28;
+        const int I = __shfl_sync(0xffffffffu, child, q);
+        signed char tgt = -1;
+        float v = 0.f;
+        if (I >= 0 && s < 27 && lo.nb[(size_t)I * 27 + s] >= 0) {
+            const int x = 2 * X + (q >> 2), y = 2 * Y + ((q >> 1) & 1), z = 2 * Z + (q & 1);
+            const int px = ((x + mg_slot_dx(s)) >> 1) - X, py = ((y + mg_slot_dy(s)) >> 1) - Y,
+                      pz = ((z + mg_slot_dz(s)) >> 1) - Z;
+            tgt = (signed char)((px + 1) * 9 + (py + 1) * 3 + (pz + 1));
+            v = lo.a[(size_t)I * 27 + s];
+        }
+        val[wib][t] = v;
+        slot2[wib][t] = tgt;
+    }
+    __syncwarp();
+    if (lane < 27) {
+        float sum = 0.f;
+        for (int t = 0; t < 224; ++t)
+            if (slot2[wib][t] == lane) sum += val[wib][t];
+        hi.a[(size_t)I2 * 27 + lane] = sum;
+        if (lane == 13) hi.dinv[I2] = sum > 0.f ? 1.f / sum : 0.f;
+    }
+}
+
+// explicit inverse of the last level (n <= kMgMaxDense) by Gauss-Jordan elimination
+// in shared memory; the matrix is symmetric positive definite, so no pivoting.
+// An aggregate without interior particles has an empty row: its diagonal is set
+// to 1 (its residual is always 0).
+__global__ void __launch_bounds__(1024) k_mg_dense_inverse(MgLevel lv, float* __restrict__ ainv) {
+    extern __shared__ float sm[];
+    const int n = lv.n, w2 = 2 * n;
+    float* M = sm;              // [n][2n]: [A | I]
+    float* f = sm + n * w2;     // [n] elimination factors
+    for (int t = threadIdx.x; t < n * w2; t += blockDim.x) M[t] = 0.f;
+    __syncthreads();
+    for (int t = threadIdx.x; t < n * 27; t += blockDim.x) {
+        const int I = t / 27, s = t % 27;
+        const int J = lv.nb[(size_t)I * 27 + s];
+        if (J >= 0) M[I * w2 + J] = lv.a[(size_t)I * 27 + s];
+    }
+    for (int I = threadIdx.x; I < n; I += blockDim.x) M[I * w2 + n + I] = 1.f;
+    __syncthreads();
+    for (int I = threadIdx.x; I < n; I += blockDim.x)
+        if (!(M[I * w2 + I] > 0.f)) M[I * w2 + I] = 1.f;
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        const float piv = M[k * w2 + k];
+        __syncthreads();
+        for (int t = threadIdx.x; t < w2; t += blockDim.x) M[k * w2 + t] /= piv;
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = i == k ? 0.f : M[i * w2 + k];
+        __syncthreads();
+        for (int t = threadIdx.x; t < n * w2; t += blockDim.x) {
+            const int i = t / w2, col = t % w2;
+            if (i != k) M[t] -= f[i] * M[k * w2 + col];
+        }
+        __syncthreads();
+    }
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) ainv[t] = M[(t / n) * w2 + n + (t % n)];
+}
+
+// ---------------------------------------------------------------------------
+// application (every CG iteration); all return once the solve has converged
+// ---------------------------------------------------------------------------
+// level-1 residual: warp per aggregate sums its rows (non-interior rows hold r = 0);
+// first down sweep from a zero start: e1 = omega D1^-1 r1
+template <class TV>
+__global__ void k_mg_restrict_fine(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
+                                   const TV* __restrict__ r) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const MgLevel& L1 = mg.L[1];
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I >= L1.n) return;
+    const int c = L1.ccell[I];
+    float s = 0.f;
+    for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) s += (float)r[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+        L1.r[I] = s;
+        L1.e[I] = mg.omega * L1.dinv[I] * s;
+    }
+}
+
+// Residual of the level-lo iterate summed over the children of level-hi aggregate I2,
+// by one warp: the 8 x 28 (child, slot) terms, 7 per lane, then a fixed shuffle tree
+// (every lane returns the sum).  Slot 27 is the child's own restricted residual.
+__device__ __forceinline__ float mg_child_residual_warp(const MgLevel& lo, const MgLevel& hi, int I2, int lane) {
+    int X, Y, Z;
+    mg_decode(hi.ccell[I2], hi.gy, hi.gz, X, Y, Z);
+    int child = -1;
+    if (lane < 8) {
+        const int x = 2 * X + (lane >> 2), y = 2 * Y + ((lane >> 1) & 1), z = 2 * Z + (lane & 1);
+        if (x < lo.gx && y < lo.gy && z < lo.gz) child = lo.cmap[(x * lo.gy + y) * lo.gz + z];
+    }
+    float v = 0.f;
+    for (int t = lane; t < 224; t += 32) {
+        const int q = t / 28, s = t % 28;
+        const int I = __shfl_sync(0xffffffffu, child, q);
+        if (I < 0) continue;
+        if (s == 27) {
+            v += lo.r[I];
+        } else {
+            const int J = lo.nb[(size_t)I * 27 + s];
+            if (J >= 0) v -= lo.a[(size_t)I * 27 + s] * lo.e[J];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// restriction lo -> hi and the first down sweep on hi: warp per hi aggregate
+__global__ void k_mg_down(const double* __restrict__ scal, MgLevel lo, MgLevel hi, float omega) {
+    if (scal[S_CONV] != 0.0) return;
+    const int I2 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I2 >= hi.n) return;   // warp-uniform
+    const float s = mg_child_residual_warp(lo, hi, I2, lane);
+    if (lane == 0) {
+        hi.r[I2] = s;
+        hi.e[I2] = omega * hi.dinv[I2] * s;
+    }
+}
+
+// last level (one CTA of 32 warps): restriction from lo (if from_lo), then
+// e2 = A^-1 r with the explicit inverse, a warp per row, lanes over columns
+__global__ void __launch_bounds__(1024) k_mg_bottom(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
+                                                    int from_lo, const float* __restrict__ ainv) {
+    if (scal[S_CONV] != 0.0) return;
+    __shared__ float rs[kMgMaxDense];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int I = w; I < hi.n; I += nw) {
+        float s;
+        if (from_lo) {
+            s = mg_child_residual_warp(lo, hi, I, lane);
+            if (lane == 0) hi.r[I] = s;
+        } else {
+            s = hi.r[I];
+        }
+        if (lane == 0) rs[I] = s;
+    }
+    __syncthreads();
+    for (int I = w; I < hi.n; I += nw) {
+        float v = 0.f;
+        for (int J = lane; J < hi.n; J += 32) v += ainv[I * hi.n + J] * rs[J];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) hi.e2[I] = v;
+    }
+}
+
+// prolongation hi -> lo and the up sweep on lo: e' = e + P e_hi,
+// e2 = e' + omega D^-1 (r - A e'); warp per lo aggregate, lane per stencil slot
+__global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi, float omega) {
+    if (scal[S_CONV] != 0.0) return;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I >= lo.n) return;   // warp-uniform
+    float t = 0.f;
+    if (lane < 27) {
+        const int J = lo.nb[(size_t)I * 27 + lane];
+        if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.par[J]]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) lo.e2[I] = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
+}
+
+// fine level: z = m r + e1[aggregate] on interior rows (0 elsewhere), rz = r.z;
+// mode 1 (start): S_RZ = rz and p = z; mode 0: S_BETA = rz / S_RZ, S_RZ = rz
+template <class TV>
+__global__ void __launch_bounds__(256) k_mg_fine_z(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
+                                                   const TV* __restrict__ r, TV* __restrict__ z, TV* __restrict__ p,
+                                                   const float* __restrict__ m32, int mode, int slot) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const float* e1 = mg.L[1].e2;
+    TV prz = TV(0);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        TV zi = TV(0);
+        if (d.inner[i]) {
+            const int a = mg.agg1[i];
+            zi = (TV)m32[i] * r[i] + (a >= 0 ? (TV)e1[a] : TV(0));
+            prz += r[i] * zi;
+        }
+        z[i] = zi;
+        if (mode == 1) p[i] = zi;
+    }
+    double v[1] = {(double)prz}, out[1];
+    if (grid_reduce<1, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        if (mode == 1) {
+            d.scal[S_RZ] = out[0];
+        } else {
+            const double rz = d.scal[S_RZ];
+            d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
+            d.scal[S_RZ] = out[0];
+        }
+    }
+}
+
+}  // namespace mps

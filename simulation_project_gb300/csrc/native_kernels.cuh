@@ -712,9 +712,12 @@ __global__ void __launch_bounds__(256) k_cg_start(const __grid_constant__ Dev d,
 }
 
 // x += alpha p; r -= alpha q; z = M r; rz, rr; then beta, convergence.
+// with_z = 0: the preconditioner is applied by separate kernels (z, rz and beta
+// are theirs); only x, r and the convergence test here.
 template <class TV, class TXA>
 __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d, TXA* x, TV* r, TV* z, const TV* p,
-                                                   const TV* q, const double* m64, const float* m32, int slot) {
+                                                   const TV* q, const double* m64, const float* m32, int slot,
+                                                   int with_z) {
     if (d.scal[S_CONV] != 0.0) return;
     const TV alpha = (TV)d.scal[S_ALPHA];
     TV prz = TV(0), prr = TV(0);
@@ -723,17 +726,21 @@ __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d
         x[i] = x[i] + (TXA)alpha * (TXA)p[i];
         const TV ri = r[i] - alpha * q[i];
         r[i] = ri;
-        const TV mi = m32 ? (TV)m32[i] : (TV)m64[i];
-        const TV zi = ri * mi;
-        z[i] = zi;
-        prz += ri * zi;
+        if (with_z) {
+            const TV mi = m32 ? (TV)m32[i] : (TV)m64[i];
+            const TV zi = ri * mi;
+            z[i] = zi;
+            prz += ri * zi;
+        }
         prr += ri * ri;
     }
     double v[2] = {(double)prz, (double)prr}, out[2];
     if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
-        const double rz = d.scal[S_RZ];
-        d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
-        d.scal[S_RZ] = out[0];
+        if (with_z) {
+            const double rz = d.scal[S_RZ];
+            d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
+            d.scal[S_RZ] = out[0];
+        }
         const double rn = sqrt(out[1]);
         d.scal[S_RNORM] = rn;
         const double it = d.scal[S_ITER] + 1.0;

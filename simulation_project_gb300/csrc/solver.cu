@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "native_kernels.cuh"
+#include "coarse.cuh"
 #include "../../include/mps_learned.h"
 
 namespace mps {
@@ -42,7 +43,8 @@ struct DevBuf {
 
 inline int blocks_for(int n, int threads = kBlock) { return std::max(1, div_up(n, threads)); }
 
-enum Phase { PH_GRID = 0, PH_WALLS, PH_PRED, PH_LIST, PH_SETUP, PH_SPMV, PH_VEC, PH_CORRECT, PH_LEARNED, PH_OTHER, PH_COUNT };
+enum Phase { PH_GRID = 0, PH_WALLS, PH_PRED, PH_LIST, PH_SETUP, PH_SPMV, PH_VEC, PH_CORRECT, PH_LEARNED, PH_PRECOND,
+             PH_OTHER, PH_COUNT };
 
 // CUDA events on the solver stream at phase boundaries; the interval between two
 // consecutive marks is attributed to the first mark's phase.
@@ -108,6 +110,14 @@ struct Solver {
     bool learned_ready = false;
     bool collect = false;
     MpsMlp* mlp = nullptr;
+    // multilevel preconditioner
+    Mg mg{};
+    int mg_grid_levels = 0;    // levels with a grid (1 .. mg_grid_levels)
+    bool mg_on = false;        // enabled and supported by the grid
+    bool mg_ready = false;     // set up for the current step
+    unsigned* mg_flag = nullptr;
+    unsigned* mg_counts = nullptr;
+    unsigned* h_counts = nullptr;
 
     template <class T>
     cudaError_t mk(T** ptr, size_t count) {
@@ -202,6 +212,10 @@ struct Solver {
         allocs.push_back(sort_scratch);
         if (cudaMallocHost((void**)&h_scal, sizeof(double) * S_COUNT) != cudaSuccess) return CCT_MEMERR;
         if (cudaMallocHost((void**)&h_int, sizeof(int) * 8) != cudaSuccess) return CCT_MEMERR;
+        if (opt.preconditioner == MPS_PRECOND_MULTILEVEL && !fp64()) {
+            const CCTStatusType rc = mg_init();
+            if (rc != CCT_NOERR) return rc;
+        }
         cudaMemset(d.red_count, 0, sizeof(unsigned) * 16);
         cudaMemset(d.scal, 0, sizeof(double) * S_COUNT);
         cudaMemset(d.err, 0, sizeof(unsigned));
@@ -222,6 +236,7 @@ struct Solver {
         if (d.drag) cudaFree(d.drag);
         if (h_scal) cudaFreeHost(h_scal);
         if (h_int) cudaFreeHost(h_int);
+        if (h_counts) cudaFreeHost(h_counts);
         timer.release();
         if (mlp) mps_mlp_destroy(mlp);
         mlp = nullptr;
@@ -302,6 +317,92 @@ struct Solver {
         if (count <= 0) return CCT_NOERR;
         if (cudaMalloc(&d.drag, sizeof(DragParameter) * count)) return CCT_MEMERR;
         return cuda_status(cudaMemcpy(d.drag, dp, sizeof(DragParameter) * count, cudaMemcpyHostToDevice));
+    }
+
+    // ---- multilevel preconditioner ----
+    // level grids halve (rounding up) until one cell; cell coordinates are packed
+    // in 10 bits, so every grid dimension must be below 1024
+    CCTStatusType mg_init() {
+        const CGridBox& b = d.box;
+        if (b.m_GridSize.x >= 1024 || b.m_GridSize.y >= 1024 || b.m_GridSize.z >= 1024) return CCT_NOERR;
+        int gx = b.m_GridSize.x, gy = b.m_GridSize.y, gz = b.m_GridSize.z;
+        cudaError_t e = cudaSuccess;
+        int l = 1;
+        for (; l <= kMgMaxLevels; ++l) {
+            MgLevel& L = mg.L[l];
+            L.gx = gx; L.gy = gy; L.gz = gz; L.n = 0;
+            const size_t nc = (size_t)gx * gy * gz;
+            e = e ? e : mk(&L.cmap, nc); e = e ? e : mk(&L.ccell, nc); e = e ? e : mk(&L.nb, 27 * nc);
+            e = e ? e : mk(&L.par, nc); e = e ? e : mk(&L.a, 27 * nc); e = e ? e : mk(&L.dinv, nc);
+            e = e ? e : mk(&L.r, nc); e = e ? e : mk(&L.e, nc); e = e ? e : mk(&L.e2, nc);
+            if (nc == 1) break;
+            gx = (gx + 1) / 2; gy = (gy + 1) / 2; gz = (gz + 1) / 2;
+        }
+        mg_grid_levels = std::min(l, kMgMaxLevels);
+        e = e ? e : mk(&mg.ainv, (size_t)kMgMaxDense * kMgMaxDense);
+        e = e ? e : mk(&mg.agg1, (size_t)nmax); e = e ? e : mk(&mg.pcc, (size_t)nmax);
+        e = e ? e : mk(&mg_flag, (size_t)d.cells + 1); e = e ? e : mk(&mg_counts, (size_t)kMgMaxLevels + 1);
+        if (e) return CCT_MEMERR;
+        if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
+        const int smem = (2 * kMgMaxDense * kMgMaxDense + kMgMaxDense) * (int)sizeof(float);
+        if (cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) return CCT_CUDAERR;
+        mg.omega = opt.mg_omega > 0 ? (float)opt.mg_omega : 0.85f;
+        mg_on = mg_grid_levels >= 1;
+        return CCT_NOERR;
+    }
+
+    // aggregates, links and operators of the current particle order (after the PPE
+    // setup: needs interior flags, diagonals and the FP32 neighbour rows)
+    CCTStatusType mg_setup() {
+        mg_ready = false;
+        if (!mg_on || d.n <= 0) return CCT_NOERR;
+        MgLevel* L = mg.L;
+        MPS_COUNT_LAUNCH k_mg_flags1<<<blocks_for(d.cells), kBlock, 0, st>>>(d, mg_flag);
+        for (int l = 1; l <= mg_grid_levels; ++l) {
+            const int nc = L[l].gx * L[l].gy * L[l].gz;
+            if (l > 1) MPS_COUNT_LAUNCH k_mg_flags_up<<<blocks_for(nc), kBlock, 0, st>>>(L[l - 1], L[l], mg_flag);
+            if (scan_exclusive(mg_flag, nc, mg_flag + nc, st)) return CCT_CUDAERR;
+            MPS_COUNT_LAUNCH k_mg_fill<<<blocks_for(nc), kBlock, 0, st>>>(L[l], mg_flag);
+            cudaMemcpyAsync(mg_counts + l, mg_flag + nc, sizeof(unsigned), cudaMemcpyDeviceToDevice, st);
+        }
+        cudaMemcpyAsync(h_counts, mg_counts, sizeof(unsigned) * (kMgMaxLevels + 1), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
+        int levels = 0;
+        for (int l = 1; l <= mg_grid_levels; ++l) {
+            L[l].n = (int)h_counts[l];
+            if (!levels && L[l].n <= kMgMaxDense) levels = l;
+        }
+        if (!levels || L[1].n <= 0) return CCT_NOERR;   // no small enough level: Jacobi this step
+        mg.levels = levels;
+        for (int l = 1; l <= levels; ++l)
+            MPS_COUNT_LAUNCH k_mg_links<<<blocks_for(L[l].n), kBlock, 0, st>>>(L[l], L[l < levels ? l + 1 : l], l < levels);
+        MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, st>>>(d, mg);
+        MPS_COUNT_LAUNCH k_mg_assemble1<float><<<L[1].n, kMgAsmThreads, 0, st>>>(d, mg, (const float*)d.nbrw);
+        for (int l = 1; l < levels; ++l)
+            MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, st>>>(L[l], L[l + 1]);
+        const int nd = L[levels].n;
+        MPS_COUNT_LAUNCH k_mg_dense_inverse<<<1, 1024, (2 * nd * nd + nd) * sizeof(float), st>>>(L[levels], mg.ainv);
+        if (cudaGetLastError()) return CCT_CUDAERR;
+        mg_ready = true;
+        return CCT_NOERR;
+    }
+
+    // z = M^-1 r (interior rows), rz; mode 1 also sets p = z and S_RZ, mode 0 S_BETA
+    void mg_apply(const float* r, float* z, float* p, int mode) {
+        MgLevel* L = mg.L;
+        const int lv = mg.levels;
+        const float om = mg.omega;
+        MPS_COUNT_LAUNCH k_mg_restrict_fine<float><<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d, mg, r);
+        if (lv == 1) {
+            MPS_COUNT_LAUNCH k_mg_bottom<<<1, 1024, 0, st>>>(d.scal, L[1], L[1], 0, mg.ainv);
+        } else {
+            for (int l = 1; l + 1 < lv; ++l)
+                MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+            MPS_COUNT_LAUNCH k_mg_bottom<<<1, 1024, 0, st>>>(d.scal, L[lv - 1], L[lv], 1, mg.ainv);
+            for (int l = lv - 1; l >= 1; --l)
+                MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+        }
+        MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7);
     }
 
     // ---- phases ----
@@ -473,6 +574,7 @@ struct Solver {
             S.ms_grid = ms[PH_GRID]; S.ms_walls = ms[PH_WALLS]; S.ms_predictor = ms[PH_PRED];
             S.ms_list = ms[PH_LIST]; S.ms_ppe_setup = ms[PH_SETUP]; S.ms_spmv = ms[PH_SPMV];
             S.ms_cg_vec = ms[PH_VEC]; S.ms_correct = ms[PH_CORRECT]; S.ms_learned = ms[PH_LEARNED];
+            S.ms_precond = ms[PH_PRECOND];
             S.spmv_launches = spmv_launches;
         }
         last = S;
@@ -497,7 +599,16 @@ struct Solver {
                 timer.mark(PH_SPMV, st);
                 MPS_COUNT_LAUNCH k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
                 timer.mark(PH_VEC, st);
-                MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1);
+                const bool use_mg = std::is_same<TV, float>::value && mg_ready;
+                MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1,
+                                                                                  use_mg ? 0 : 1);
+                if constexpr (std::is_same<TV, float>::value) {
+                    if (use_mg) {
+                        timer.mark(PH_PRECOND, st);
+                        mg_apply(r, z, p, 0);
+                        timer.mark(PH_VEC, st);
+                    }
+                }
                 MPS_COUNT_LAUNCH k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
                 ++spmv_launches;
             }
@@ -535,6 +646,11 @@ struct Solver {
     CCTStatusType solve_ir(MpsStepStats& S) {
         const float* w = (const float*)d.nbrw;
         MPS_COUNT_LAUNCH k_to_float<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.minv, d.m32);
+        timer.mark(PH_PRECOND, st);
+        if (mg_setup()) return CCT_CUDAERR;
+        S.mg_levels = mg_ready ? mg.levels : 0;
+        S.mg_level1 = mg_ready ? mg.L[1].n : 0;
+        timer.mark(PH_VEC, st);
         double bnorm = 0.0;
         int outer = 0;
         for (;;) {
@@ -554,6 +670,11 @@ struct Solver {
             const double inner_tol = std::max(need, opt.ir_inner_rtol);
             MPS_COUNT_LAUNCH k_cg_start<float><<<kRedBlocks, 256, 0, st>>>(d, d.r32, d.z32, d.p32, d.r, 1.0 / rn, nullptr, d.m32, d.d32, 3,
                                                           inner_tol, opt.cg_max_iter);
+            if (mg_ready) {
+                timer.mark(PH_PRECOND, st);
+                mg_apply(d.r32, d.z32, d.p32, 1);
+                timer.mark(PH_VEC, st);
+            }
             const int it = cg_loop<float, float, float>(d.d32, d.r32, d.z32, d.p32, d.q32, w, nullptr, d.m32,
                                                         opt.cg_max_iter);
             if (it < 0) return CCT_CUDAERR;
@@ -614,6 +735,8 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->max_neighbours = 384;
     o->check_every = 8;
     o->source_relaxation = 0.05;
+    o->preconditioner = MPS_PRECOND_MULTILEVEL;
+    o->mg_omega = 0.85;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,

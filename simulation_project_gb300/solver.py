@@ -23,7 +23,8 @@ class MpsSolverOptions(C.Structure):
                 ("n0_lap", C.c_double), ("lambda_", C.c_double), ("compressibility", C.c_double),
                 ("cg_rtol", C.c_double), ("cg_max_iter", C.c_int), ("ir_inner_rtol", C.c_double),
                 ("ir_max_outer", C.c_int), ("max_neighbours", C.c_int), ("check_every", C.c_int),
-                ("source_relaxation", C.c_double), ("profile", C.c_int)]
+                ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
+                ("mg_omega", C.c_double)]
 
 
 class MpsStepStats(C.Structure):
@@ -32,7 +33,8 @@ class MpsStepStats(C.Structure):
                 ("error_flags", C.c_uint), ("nnz", C.c_longlong), ("pairs", C.c_longlong),
                 ("ms_grid", C.c_float), ("ms_walls", C.c_float), ("ms_predictor", C.c_float), ("ms_list", C.c_float),
                 ("ms_ppe_setup", C.c_float), ("ms_spmv", C.c_float), ("ms_cg_vec", C.c_float),
-                ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int)]
+                ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int),
+                ("ms_precond", C.c_float), ("mg_levels", C.c_int), ("mg_level1", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
