@@ -13,7 +13,11 @@ size_t radix_scratch_bytes(int n);
 int radix_passes(unsigned range);
 cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, void* scratch, cudaStream_t st);
 cudaError_t key_minmax(int n, const int* keys, int* mm_dev, cudaStream_t st);
-cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st);
+// in-place exclusive scan of len unsigned values, total to *total_dev (if not NULL);
+// tile_sums (scan_tile_sums_capacity() values, or NULL: single-CTA scan) lets it
+// run on many CTAs
+cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st, unsigned* tile_sums = nullptr);
+size_t scan_tile_sums_capacity();
 
 // library-owned scratch for the reference-named entry points, which take no scratch
 // argument (runtime.cu).  Grows on demand; one buffer per slot.

@@ -19,7 +19,7 @@ constexpr int kStageCap = 2048;
 constexpr int kRedBlocks = 1216;   // 152 SMs x 8 resident CTAs of 256 threads
 constexpr int kVecThreads = 256;
 
-enum { NB_PREDICT = 0, NB_LIST = 1 };
+enum { NB_PREDICT = 0, NB_LIST = 1, NB_LIST_FEAT = 2 };
 
 template <class T> struct V3 { T x, y, z; };
 
@@ -356,10 +356,74 @@ __device__ __forceinline__ double exact_r(double dx, double dy, double dz) {
     return sqrt(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
 }
 
+// Epilogue of one target of k_neighbours (run lane-parallel: each lane finishes the
+// target it parked, so the FP64 state update uses every lane of the FP64 pipe).
+template <class T, int MODE>
+__device__ __forceinline__ void nb_epilogue(const Dev& d, int i, T a0, T a1, T a2, T a3, int cnt, int gcnt) {
+    if constexpr (MODE == NB_PREDICT) {
+        // wall friction term, viscosity, gravity, drag (CalcExplicitly_Kernel)
+        const V3<T> vi = load_v<T>(d, i);
+        double lx = a0, ly = a1, lz = a2;
+        const int t = d.wid[i];
+        const double wd = d.wdist[i];
+        if (t >= 0 && wd > 0 && wd < d.c.re_lap) {
+            const double ww = exact_z<double>(d.c.dim == 2 ? c_zlap2 : c_zlap3, d.c.dim == 2 ? 23 : 25, wd, d.c.l0);
+            const Scalar3 vw = d.tparams[d.tmodel[t]].Velocity;
+            lx += ((double)vw.x - (double)vi.x) * d.c.wall_fric * ww;
+            ly += ((double)vw.y - (double)vi.y) * d.c.wall_fric * ww;
+            lz += ((double)vw.z - (double)vi.z) * d.c.wall_fric * ww;
+        }
+        const double cf = d.c.coef_lap * (double)d.visc[i];
+        const dbl4 v = d.vel[i];
+        const dbl4 p = d.pos[i];
+        const double dt = d.c.dt;
+        dbl4 vn, pn;
+        vn.x = v.x + (d.c.g[0] + lx * cf) * dt - d.dragv[3 * (size_t)i];
+        vn.y = v.y + (d.c.g[1] + ly * cf) * dt - d.dragv[3 * (size_t)i + 1];
+        vn.z = v.z + (d.c.g[2] + lz * cf) * dt - d.dragv[3 * (size_t)i + 2];
+        vn.w = 0.0;
+        pn.x = p.x + vn.x * dt;
+        pn.y = p.y + vn.y * dt;
+        pn.z = p.z + vn.z * dt;
+        pn.w = 0.0;
+        if (!(isfinite(vn.x) && isfinite(vn.y) && isfinite(vn.z))) {
+            atomicOr(d.err, MPS_ERR_NONFINITE);
+            vn = v;
+            pn = p;
+        }
+        d.vel2[i] = vn;
+        d.pos2[i] = pn;
+    } else {
+        if (cnt > d.K || gcnt > d.KG) atomicOr(d.err, MPS_ERR_NEIGHBOUR_CAP);
+        atomicMax(d.istat, cnt);
+        d.nbr_cnt[i] = cnt < d.K ? cnt : d.K;
+        d.gcnt[i] = gcnt < d.KG ? gcnt : d.KG;
+        double pnd = (double)a2;
+        const double riw = d.wdist[i];
+        if (d.wid[i] >= 0 && riw >= 0 && riw <= d.c.re_grad)
+            pnd += exact_z<double>(d.c.dim == 2 ? c_zgrad2 : c_zgrad3, d.c.dim == 2 ? 23 : 21, riw, d.c.l0);
+        d.pnd[i] = pnd;
+        d.sumw[i] = (double)a0;
+        if constexpr (MODE == NB_LIST_FEAT) {
+            d.feat_aux[4 * (size_t)i] = cnt > 0 ? (double)a1 / cnt : 0.0;
+            d.feat_aux[4 * (size_t)i + 1] = (double)a3 * (double)d.c.dim / d.c.n0_pnd;
+            d.feat_aux[4 * (size_t)i + 2] = (double)cnt;
+        }
+    }
+}
+
+// Neighbour passes, CTA per non-empty cell.  The 9 (x, y) columns of the 27-cell
+// neighbourhood are contiguous z-runs in the sorted order; their positions are
+// staged in shared memory (float4), a warp takes one target particle at a time and
+// its lanes test 32 candidates per round.  MODE:
+//   NB_PREDICT    Laplacian of the velocity -> viscosity/gravity/drag predictor
+//   NB_LIST       Laplacian rows (SELL-32), gradient rows, PND, sum of weights
+//   NB_LIST_FEAT  NB_LIST plus the learned features' neighbour aggregates
+// The warp's butterfly sums are parked in lane k%32 for its k-th target and the
+// epilogues run lane-parallel.
 template <class T, int MODE>
 __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant__ Dev d) {
     __shared__ float4 spos[kStageCap];
-    __shared__ float4 svel[kStageCap];
     __shared__ int rs[9], rl[9], rp[10];
     const int ci = blockIdx.x;
     if (ci >= *d.cell_count) return;
@@ -397,9 +461,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         for (int c = threadIdx.x; c < S; c += blockDim.x) {
             int r = 0;
             while (c >= rp[r + 1]) ++r;
-            const int j = rs[r] + (c - rp[r]);
-            spos[c] = d.opos[j];
-            svel[c] = d.ovel[j];
+            spos[c] = d.opos[rs[r] + (c - rp[r])];
         }
     }
     __syncthreads();
@@ -408,12 +470,15 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
     const unsigned lt = (1u << lane) - 1u;
     const T re = (T)d.c.re_lap, reg = (T)d.c.re_grad, mind = (T)d.c.mind_lap, mindg = (T)d.c.mind_grad;
     const float re2f = (float)(d.c.re_lap * d.c.re_lap) * 1.0001f;
-    for (int i = s0 + warp; i < e0; i += nwarp) {
+    // target parked in this lane for the lane-parallel epilogue
+    int my_i = -1, my_cnt = 0, my_gcnt = 0;
+    T m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+    int k = 0;
+    for (int i = s0 + warp; i < e0; i += nwarp, ++k) {
         const float4 pf = d.opos[i];
         const V3<T> pi = load_p<T>(d, i);
         const V3<T> vi = load_v<T>(d, i);
         T a0 = 0, a1 = 0, a2 = 0, a3 = 0;   // mode-specific accumulators
-        double aid = 0.0;                   // neighbour id checksum (FP64, exact for ids < 2^53/K)
         int cnt = 0, gcnt = 0;
         for (int r = 0; r < 9; ++r) {
             const int len = rl[r];
@@ -424,12 +489,12 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 bool acc = false, gacc = false;
                 T rr = T(0);
                 V3<T> dv = v3(T(0), T(0), T(0));
-                float4 vj4 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (valid && j != i) {
                     const float4 q = staged ? spos[rp[r] + o] : d.opos[j];
-                    if constexpr (sizeof(T) == 8) {
-                        const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
-                        if (dxf * dxf + dyf * dyf + dzf * dzf < re2f) {
+                    const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
+                    const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+                    if (d2f < re2f) {
+                        if constexpr (sizeof(T) == 8) {
                             const dbl4 pj = d.pos[j];
                             const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
                             const double rd = exact_r(dx, dy, dz);
@@ -438,17 +503,15 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                                 rr = rd;
                                 dv = v3<T>(dx, dy, dz);
                             }
-                        }
-                    } else {
-                        const float dx = q.x - pf.x, dy = q.y - pf.y, dz = q.z - pf.z;
-                        const float rf = sqrtf(dx * dx + dy * dy + dz * dz);
-                        if (rf < (float)re) {
-                            acc = true;
-                            rr = rf;
-                            dv = v3<T>(dx, dy, dz);
+                        } else {
+                            const float rf = sqrtf(d2f);
+                            if (rf < (float)re) {
+                                acc = true;
+                                rr = rf;
+                                dv = v3<T>(dxf, dyf, dzf);
+                            }
                         }
                     }
-                    if (acc) vj4 = staged ? svel[rp[r] + o] : d.ovel[j];
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
                 if (acc) {
@@ -459,7 +522,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                             const dbl4 v = d.vel[j];
                             vj = v3<T>(v.x, v.y, v.z);
                         } else {
-                            vj = v3<T>(vj4.x, vj4.y, vj4.z);
+                            const float4 v = d.ovel[j];
+                            vj = v3<T>(v.x, v.y, v.z);
                         }
                         a0 += (vj.x - vi.x) * w;
                         a1 += (vj.y - vi.y) * w;
@@ -472,21 +536,23 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                             ((T*)d.nbrw)[e] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
-                        a1 += (T)d.press[j];                       // neighbour pressure (feature)
-                        aid += (double)d.id[j];                    // id checksum (debug)
+                        if constexpr (MODE == NB_LIST_FEAT) a1 += (T)d.press[j];   // neighbour pressure
                         if (rr < reg) {
                             gacc = true;
                             const T rg = rr > mindg ? rr : mindg;
                             const T wg = reg / rg - T(1);
                             a2 += wg;                              // PND
-                            // velocity divergence (feature): sum (v_j - v_i).d w / r^2
-                            a3 += ((T(vj4.x) - vi.x) * dv.x + (T(vj4.y) - vi.y) * dv.y + (T(vj4.z) - vi.z) * dv.z) *
-                                  wg / (rg * rg);
+                            if constexpr (MODE == NB_LIST_FEAT) {
+                                // velocity divergence (feature): sum (v_j - v_i).d w / r^2
+                                const float4 vj4 = d.ovel[j];
+                                a3 += ((T(vj4.x) - vi.x) * dv.x + (T(vj4.y) - vi.y) * dv.y +
+                                       (T(vj4.z) - vi.z) * dv.z) * wg / (rg * rg);
+                            }
                         }
                     }
                 }
                 cnt += __popc(bal);
-                if constexpr (MODE == NB_LIST) {
+                if constexpr (MODE != NB_PREDICT) {
                     const unsigned gb = __ballot_sync(0xffffffffu, gacc);
                     if (gacc) {
                         const int slot = gcnt + __popc(gb & lt);
@@ -501,62 +567,30 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            a0 += __shfl_down_sync(0xffffffffu, a0, o);
-            a1 += __shfl_down_sync(0xffffffffu, a1, o);
-            a2 += __shfl_down_sync(0xffffffffu, a2, o);
-            a3 += __shfl_down_sync(0xffffffffu, a3, o);
-            aid += __shfl_down_sync(0xffffffffu, aid, o);
+            a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+            a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+            a3 += __shfl_xor_sync(0xffffffffu, a3, o);
         }
-        if (lane != 0) continue;
-        if constexpr (MODE == NB_PREDICT) {
-            // wall friction term, viscosity, gravity, drag (CalcExplicitly_Kernel)
-            double lx = a0, ly = a1, lz = a2;
-            const int t = d.wid[i];
-            const double wd = d.wdist[i];
-            if (t >= 0 && wd > 0 && wd < d.c.re_lap) {
-                const double ww = exact_z<double>(d.c.dim == 2 ? c_zlap2 : c_zlap3, d.c.dim == 2 ? 23 : 25, wd, d.c.l0);
-                const Scalar3 vw = d.tparams[d.tmodel[t]].Velocity;
-                lx += ((double)vw.x - (double)vi.x) * d.c.wall_fric * ww;
-                ly += ((double)vw.y - (double)vi.y) * d.c.wall_fric * ww;
-                lz += ((double)vw.z - (double)vi.z) * d.c.wall_fric * ww;
-            }
-            const double cf = d.c.coef_lap * (double)d.visc[i];
-            const dbl4 v = d.vel[i];
-            const dbl4 p = d.pos[i];
-            const double dt = d.c.dt;
-            dbl4 vn, pn;
-            vn.x = v.x + (d.c.g[0] + lx * cf) * dt - d.dragv[3 * (size_t)i];
-            vn.y = v.y + (d.c.g[1] + ly * cf) * dt - d.dragv[3 * (size_t)i + 1];
-            vn.z = v.z + (d.c.g[2] + lz * cf) * dt - d.dragv[3 * (size_t)i + 2];
-            vn.w = 0.0;
-            pn.x = p.x + vn.x * dt;
-            pn.y = p.y + vn.y * dt;
-            pn.z = p.z + vn.z * dt;
-            pn.w = 0.0;
-            if (!(isfinite(vn.x) && isfinite(vn.y) && isfinite(vn.z))) {
-                atomicOr(d.err, MPS_ERR_NONFINITE);
-                vn = v;
-                pn = p;
-            }
-            d.vel2[i] = vn;
-            d.pos2[i] = pn;
-        } else {
-            if (cnt > d.K || gcnt > d.KG) atomicOr(d.err, MPS_ERR_NEIGHBOUR_CAP);
-            atomicMax(d.istat, cnt);
-            d.nbr_cnt[i] = cnt < d.K ? cnt : d.K;
-            d.gcnt[i] = gcnt < d.KG ? gcnt : d.KG;
-            double pnd = (double)a2;
-            const double riw = d.wdist[i];
-            if (d.wid[i] >= 0 && riw >= 0 && riw <= d.c.re_grad)
-                pnd += exact_z<double>(d.c.dim == 2 ? c_zgrad2 : c_zgrad3, d.c.dim == 2 ? 23 : 21, riw, d.c.l0);
-            d.pnd[i] = pnd;
-            d.sumw[i] = (double)a0;
-            d.feat_aux[4 * (size_t)i] = cnt > 0 ? (double)a1 / cnt : 0.0;
-            d.feat_aux[4 * (size_t)i + 1] = (double)a3 * (double)d.c.dim / d.c.n0_pnd;
-            d.feat_aux[4 * (size_t)i + 2] = (double)cnt;
-            d.feat_aux[4 * (size_t)i + 3] = aid;
+        if (lane == (k & 31)) {
+            my_i = i; m0 = a0; m1 = a1; m2 = a2; m3 = a3; my_cnt = cnt; my_gcnt = gcnt;
+        }
+        if ((k & 31) == 31) {
+            if (my_i >= 0) nb_epilogue<T, MODE>(d, my_i, m0, m1, m2, m3, my_cnt, my_gcnt);
+            my_i = -1;
         }
     }
+    if (my_i >= 0) nb_epilogue<T, MODE>(d, my_i, m0, m1, m2, m3, my_cnt, my_gcnt);
+}
+
+// FP64 checksum of the neighbour ids of every row (neighbour-set comparison in tests)
+__global__ void k_row_idsum(const __grid_constant__ Dev d, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    double s = 0.0;
+    const int cnt = d.nbr_cnt[i];
+    for (int k = 0; k < cnt; ++k) s += (double)d.id[d.nbr[sell_index(i, k, d.K)]];
+    out[i] = s;
 }
 
 // ---------------------------------------------------------------------------

@@ -94,6 +94,7 @@ struct Solver {
     void* sort_scratch = nullptr;
     size_t sort_scratch_bytes = 0;
     unsigned *keep = nullptr, *rank = nullptr;
+    unsigned* scan_sums = nullptr;   // tile sums of the multi-CTA scans
     double* h_scal = nullptr;   // pinned mirror of the device scalars
     int* h_int = nullptr;       // pinned small ints
     // wall-bin scratch
@@ -204,6 +205,7 @@ struct Solver {
         e = e ? e : mk(&d.feat, 12 * N);
         e = e ? e : mk(&d.mlp_out, 2 * N);
         e = e ? e : mk(&d.targets, 2 * N);
+        e = e ? e : mk(&scan_sums, scan_tile_sums_capacity());
         e = e ? e : mk(&keep, N + 1);
         e = e ? e : mk(&rank, N + 1);
         if (e != cudaSuccess) return CCT_MEMERR;
@@ -361,7 +363,7 @@ struct Solver {
         for (int l = 1; l <= mg_grid_levels; ++l) {
             const int nc = L[l].gx * L[l].gy * L[l].gz;
             if (l > 1) MPS_COUNT_LAUNCH k_mg_flags_up<<<blocks_for(nc), kBlock, 0, st>>>(L[l - 1], L[l], mg_flag);
-            if (scan_exclusive(mg_flag, nc, mg_flag + nc, st)) return CCT_CUDAERR;
+            if (scan_exclusive(mg_flag, nc, mg_flag + nc, st, scan_sums)) return CCT_CUDAERR;
             MPS_COUNT_LAUNCH k_mg_fill<<<blocks_for(nc), kBlock, 0, st>>>(L[l], mg_flag);
             cudaMemcpyAsync(mg_counts + l, mg_flag + nc, sizeof(unsigned), cudaMemcpyDeviceToDevice, st);
         }
@@ -411,7 +413,7 @@ struct Solver {
         if (n <= 0) return CCT_NOERR;
         MPS_COUNT_LAUNCH k_zone_flags<<<blocks_for(n), kBlock, 0, st>>>(d, keep);
         cudaMemcpyAsync(rank, keep, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
-        scan_exclusive(rank, n, rank + n, st);
+        scan_exclusive(rank, n, rank + n, st, scan_sums);
         MPS_COUNT_LAUNCH k_compact<<<blocks_for(n), kBlock, 0, st>>>(d, keep, rank);
         cudaMemcpyAsync(h_int, rank + n, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
@@ -438,7 +440,7 @@ struct Solver {
         if (t <= 0) return CCT_NOERR;
         if (!bin_off && cudaMalloc(&bin_off, sizeof(unsigned) * ((size_t)t + 2))) return CCT_MEMERR;
         MPS_COUNT_LAUNCH k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off);
-        scan_exclusive(bin_off, t + 1, nullptr, st);
+        scan_exclusive(bin_off, t + 1, nullptr, st, scan_sums);
         cudaMemcpyAsync(h_int, bin_off + t, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
         const unsigned nv = (unsigned)h_int[0];
@@ -502,7 +504,11 @@ struct Solver {
         timer.mark(PH_WALLS, st);
         walls_distance<T>();
         timer.mark(PH_LIST, st);
-        MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST><<<std::max(1, std::min(d.cells, d.n)), kNbThreads, 0, st>>>(d);
+        const int nb_cells = std::max(1, std::min(d.cells, d.n));
+        if ((learned_ready && opt.learned) || collect)
+            MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST_FEAT><<<nb_cells, kNbThreads, 0, st>>>(d);
+        else
+            MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST><<<nb_cells, kNbThreads, 0, st>>>(d);
         timer.mark(PH_SETUP, st);
         if (opt.pressure_mode == MPS_PRESSURE_EXPLICIT) {
             MPS_COUNT_LAUNCH k_eos<<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -823,10 +829,15 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
     if (!e && sol) e = cudaMemcpy(sol, d.press, sizeof(double) * n, cudaMemcpyDeviceToHost);
     if (!e && id) e = cudaMemcpy(id, d.id, sizeof(int) * n, cudaMemcpyDeviceToHost);
     if (!e && nbr_count) e = cudaMemcpy(nbr_count, d.nbr_cnt, sizeof(int) * n, cudaMemcpyDeviceToHost);
-    if (!e && nbr_idsum) {
-        std::vector<double> aux(4 * (size_t)n);
-        e = cudaMemcpy(aux.data(), d.feat_aux, sizeof(double) * 4 * n, cudaMemcpyDeviceToHost);
-        for (int i = 0; i < n; ++i) nbr_idsum[i] = aux[4 * (size_t)i + 3];
+    if (!e && nbr_idsum && n > 0) {
+        double* tmp = nullptr;
+        e = cudaMalloc(&tmp, sizeof(double) * n);
+        if (!e) {
+            MPS_COUNT_LAUNCH mps::k_row_idsum<<<mps::blocks_for(n), mps::kBlock, 0, s->s.st>>>(d, tmp);
+            e = cudaStreamSynchronize(s->s.st);
+            if (!e) e = cudaMemcpy(nbr_idsum, tmp, sizeof(double) * n, cudaMemcpyDeviceToHost);
+            cudaFree(tmp);
+        }
     }
     return mps::cuda_status(e);
 }

@@ -84,6 +84,91 @@ __global__ void __launch_bounds__(1024) k_scan_excl(unsigned* __restrict__ a, in
     }
 }
 
+// Multi-CTA exclusive scan (scan_exclusive with a tile-sum buffer): tiles of
+// kScanTile elements loaded coalesced into shared memory; k_scan_tile_sums writes
+// each tile's sum, k_scan_tiles scans one tile (4 contiguous items per thread plus
+// a block scan of the thread sums) starting from the tile's offset.  The tile sums
+// are scanned in place by k_scan_tiles as a single tile.
+constexpr int kScanThreads = 1024;
+constexpr int kScanTile = 4 * kScanThreads;
+
+__device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* ws, unsigned& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        unsigned s = ws[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        ws[lane] = s;
+    }
+    __syncthreads();
+    const unsigned ex = x - v + (w > 0 ? ws[w - 1] : 0u);
+    total = ws[31];
+    return ex;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const unsigned* __restrict__ a, int len,
+                                                                 unsigned* __restrict__ sums) {
+    __shared__ unsigned ws[32];
+    const int base = blockIdx.x * kScanTile;
+    unsigned s = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = base + q * kScanThreads + threadIdx.x;
+        if (i < len) s += a[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned t = ws[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(unsigned* __restrict__ a, int len,
+                                                             const unsigned* __restrict__ offsets,
+                                                             unsigned* __restrict__ total_dev) {
+    __shared__ unsigned t[kScanTile];
+    __shared__ unsigned ws[32];
+    const int base = blockIdx.x * kScanTile;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = base + q * kScanThreads + threadIdx.x;
+        t[q * kScanThreads + threadIdx.x] = i < len ? a[i] : 0u;
+    }
+    __syncthreads();
+    const int o4 = 4 * threadIdx.x;
+    const unsigned v0 = t[o4], v1 = t[o4 + 1], v2 = t[o4 + 2], v3 = t[o4 + 3];
+    unsigned total;
+    const unsigned off = (offsets ? offsets[blockIdx.x] : 0u);
+    const unsigned ex = block_exclusive(v0 + v1 + v2 + v3, ws, total) + off;
+    t[o4] = ex;
+    t[o4 + 1] = ex + v0;
+    t[o4 + 2] = ex + v0 + v1;
+    t[o4 + 3] = ex + v0 + v1 + v2;
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int i = base + q * kScanThreads + threadIdx.x;
+        if (i < len) a[i] = t[q * kScanThreads + threadIdx.x];
+    }
+    if (total_dev && threadIdx.x == 0 && blockIdx.x == gridDim.x - 1) *total_dev = off + total;
+}
+
 __global__ void __launch_bounds__(kSortThreads) k_scatter(const int* __restrict__ kin, const int* __restrict__ vin,
                                                          int* __restrict__ kout, int* __restrict__ vout, int n,
                                                          int kmin, int shift, int tiles,
@@ -203,10 +288,21 @@ cudaError_t key_minmax(int n, const int* keys, int* mm_dev, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st) {
+cudaError_t scan_exclusive(unsigned* a, int len, unsigned* total_dev, cudaStream_t st, unsigned* tile_sums) {
     if (len <= 0) return cudaSuccess;
-    MPS_COUNT_LAUNCH k_scan_excl<<<1, 1024, 0, st>>>(a, len, total_dev);
+    const int tiles = (len + kScanTile - 1) / kScanTile;
+    if (tiles == 1) {
+        MPS_COUNT_LAUNCH k_scan_tiles<<<1, kScanThreads, 0, st>>>(a, len, nullptr, total_dev);
+    } else if (tile_sums && tiles <= kScanTile) {
+        MPS_COUNT_LAUNCH k_scan_tile_sums<<<tiles, kScanThreads, 0, st>>>(a, len, tile_sums);
+        MPS_COUNT_LAUNCH k_scan_tiles<<<1, kScanThreads, 0, st>>>(tile_sums, tiles, nullptr, nullptr);
+        MPS_COUNT_LAUNCH k_scan_tiles<<<tiles, kScanThreads, 0, st>>>(a, len, tile_sums, total_dev);
+    } else {
+        MPS_COUNT_LAUNCH k_scan_excl<<<1, 1024, 0, st>>>(a, len, total_dev);
+    }
     return cudaGetLastError();
 }
+
+size_t scan_tile_sums_capacity() { return (size_t)kScanTile; }
 
 }  // namespace mps
