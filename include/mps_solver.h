@@ -107,6 +107,10 @@ CCTStatusType mps_solver_get_triangles(MpsSolver* s, double* vertices);
  * solution, particle id, Laplacian neighbour count, sum of neighbour ids */
 CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, double* rhs, double* sol, int* id,
                                    int* nbr_count, double* nbr_idsum);
+/* refinement residual r = b - A p of the current state (FP32_IR solvers; host
+ * array of n doubles, may be NULL) and ||r|| / ||b||: variant 0 with FP64
+ * products and sums, variant 1 with the double-float kernel the solver uses */
+CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, double* relres);
 /* Device pointer of the pressure array (FP64, sorted order) and particle count. */
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);
 /* Pressure read back to a host buffer, in the solver's order (e2e output). */

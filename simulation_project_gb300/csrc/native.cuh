@@ -75,6 +75,7 @@ struct Dev {
     double *r, *z, *p, *q;     // FP64 CG vectors
     float *r32, *z32, *p32, *q32, *d32, *m32;  // FP32 inner CG vectors, m32 = preconditioner
     double* minv;              // FP64 preconditioner (1/diag or learned)
+    float *xh, *xl;            // x = xh + xl (to ~2^-48): split pressure for the double-float residual
     double* feat_aux;          // per-particle auxiliaries for features (div, mean P, ...)
     double* red;               // block partial sums
     double* scal;              // device scalars

@@ -646,7 +646,8 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
     const int nslices = (d.n + 31) >> 5;
     double part0 = 0.0, part1 = 0.0;
     const double coef = d.c.coef_lap;
-    using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE != 0), double, float>::type;
+    // entry arithmetic: FP32 unless a weight or x is FP64, or the FP64 residual (MODE 1)
+    using TA = typename std::conditional<(sizeof(TX) == 8 || sizeof(TW) == 8 || MODE == 1), double, float>::type;
     TA partw = TA(0);   // MODE 0 partial dot, in the arithmetic type
     for (int sl = gw; sl < nslices; sl += nw) {
         const int i = sl * 32 + lane;
@@ -709,6 +710,85 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
             d.scal[S_RNORM] = sqrt(out[0]);
             d.scal[S_BNORM] = sqrt(out[1]);
         }
+    }
+}
+
+// x = xh + xl: the FP64 pressure split into two floats (representation error
+// about 2^-48 |x|) for the double-float residual
+__global__ void k_split_x(int n, const double* __restrict__ x, float* __restrict__ xh, float* __restrict__ xl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    const float h = (float)v;
+    xh[i] = h;
+    xl[i] = (float)(v - (double)h);
+}
+
+// Refinement residual r = b - A x with FP32 weights, in double-float arithmetic:
+// every product w*xh is kept exactly as the pair (p, fma(w, xh, -p)), w*xl joins
+// the low word, and the row sum is a (hi, lo) float pair updated by TwoSum
+// (Knuth; rounding-explicit intrinsics so nothing is contracted).  Only the row
+// term diag*x and the final difference are FP64, so the FP64 pipe does per-row
+// work instead of per-entry work.  Error: about 2^-44 of sum |w x| per row.
+// Norms ||r||^2 -> S_RR / S_RNORM and ||b|| -> S_BNORM as in k_spmv MODE 1.
+__global__ void __launch_bounds__(256) k_residual_df(const __grid_constant__ Dev d, const float* __restrict__ w,
+                                                     const double* __restrict__ x, double* __restrict__ r,
+                                                     const double* __restrict__ b, int slot) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const int nslices = (d.n + 31) >> 5;
+    const float* __restrict__ xh = d.xh;
+    const float* __restrict__ xl = d.xl;
+    double part0 = 0.0, part1 = 0.0;
+    for (int sl = gw; sl < nslices; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+        const size_t base = (size_t)sl * d.K * 32 + lane;
+        float S = 0.f, C = 0.f;
+        for (int k = 0; k < kmax; k += 4) {
+            int id[4];
+            float wv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool a = k + u < kmax;
+                id[u] = a ? __ldcs(d.nbr + base + (size_t)(k + u) * 32) : 0;
+                wv[u] = a ? __ldcs(w + base + (size_t)(k + u) * 32) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                if (k + u < cnt) {
+                    const float h = xh[id[u]], l = xl[id[u]];
+                    const float p = __fmul_rn(wv[u], h);
+                    const float pe = __fmaf_rn(wv[u], h, -p);
+                    const float lo = __fmaf_rn(wv[u], l, pe);
+                    const float s = __fadd_rn(S, p);
+                    const float bb = __fsub_rn(s, S);
+                    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+                    S = s;
+                    C = __fadd_rn(C, __fadd_rn(err, lo));
+                }
+            }
+        }
+        if (!row) continue;
+        if (!in) {
+            r[i] = 0.0;
+            continue;
+        }
+        const double acc = (double)S + (double)C;
+        const double ri = b[i] - (d.diag[i] * x[i] - d.c.coef_lap * acc);
+        r[i] = ri;
+        part0 += ri * ri;
+        part1 += b[i] * b[i];
+    }
+    double v[2] = {part0, part1}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        d.scal[S_RR] = out[0];
+        d.scal[S_RNORM] = sqrt(out[0]);
+        d.scal[S_BNORM] = sqrt(out[1]);
     }
 }
 
@@ -879,12 +959,14 @@ __global__ void k_learned_apply(const __grid_constant__ Dev d, int use_scaling) 
     if (i >= d.n) return;
     if (!d.inner[i]) {
         d.z[i] = 0.0;
+        d.z32[i] = 0.f;
         d.minv[i] = 0.0;
         return;
     }
     const float y0 = d.mlp_out[2 * (size_t)i], y1 = d.mlp_out[2 * (size_t)i + 1];
     const double inc = (double)fminf(fmaxf(y0, -50.f), 50.f) * d.scal[S_PSCALE];
     d.z[i] = isfinite(inc) ? inc : 0.0;
+    d.z32[i] = (float)d.z[i];
     const double s = use_scaling ? exp((double)fminf(fmaxf(isfinite(y1) ? y1 : 0.f, -2.3f), 2.3f)) : 1.0;
     d.minv[i] = s / d.diag[i];
 }

@@ -194,6 +194,7 @@ struct Solver {
         e = e ? e : mk(&d.minv, N);
         e = e ? e : mk(&d.r32, N); e = e ? e : mk(&d.z32, N); e = e ? e : mk(&d.p32, N); e = e ? e : mk(&d.q32, N);
         e = e ? e : mk(&d.d32, N); e = e ? e : mk(&d.m32, N);
+        e = e ? e : mk(&d.xh, N); e = e ? e : mk(&d.xl, N);
         e = e ? e : mk(&d.feat_aux, 4 * N);
         e = e ? e : mk(&d.red, 4 * (size_t)kRedBlocks);
         e = e ? e : mk(&d.scal, (size_t)S_COUNT);
@@ -523,8 +524,7 @@ struct Solver {
                     MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
                                                                                   d.r, d.rhs, 2);
                 else
-                    MPS_COUNT_LAUNCH k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.press,
-                                                                                 d.r, d.rhs, 2);
+                    residual_df((const float*)d.nbrw);
                 MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
                 MPS_COUNT_LAUNCH k_features<<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 if (use_learned) {
@@ -533,9 +533,9 @@ struct Solver {
                     if (fp64())
                         MPS_COUNT_LAUNCH k_spmv<double, double, double, 2><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.z,
                                                                                       d.q, d.r, 6);
-                    else
-                        MPS_COUNT_LAUNCH k_spmv<float, double, double, 2><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.z, d.q,
-                                                                                     d.r, 6);
+                    else   // FP32 products: the line search needs no more
+                        MPS_COUNT_LAUNCH k_spmv<float, float, float, 2><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.z32,
+                                                                                   d.q32, d.r, 6);
                     MPS_COUNT_LAUNCH k_learned_finish<<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 }
                 timer.mark(PH_SETUP, st);
@@ -648,6 +648,12 @@ struct Solver {
         return CCT_NOERR;
     }
 
+    // r = rhs - A press (FP32 weights) in double-float arithmetic; norms to the scalars
+    void residual_df(const float* w) {
+        MPS_COUNT_LAUNCH k_split_x<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.xh, d.xl);
+        MPS_COUNT_LAUNCH k_residual_df<<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+    }
+
     // FP32 Jacobi-PCG inside FP64 iterative refinement
     CCTStatusType solve_ir(MpsStepStats& S) {
         const float* w = (const float*)d.nbrw;
@@ -660,7 +666,7 @@ struct Solver {
         double bnorm = 0.0;
         int outer = 0;
         for (;;) {
-            MPS_COUNT_LAUNCH k_spmv<float, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+            residual_df(w);
             if (pull_scal()) return CCT_CUDAERR;
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
@@ -840,6 +846,23 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
         }
     }
     return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_r, double* relres) {
+    if (!s) return CCT_PARAMERR;
+    mps::Solver& S = s->s;
+    mps::Dev& d = S.d;
+    if (S.fp64() || d.n <= 0) return CCT_PARAMERR;
+    const float* w = (const float*)d.nbrw;
+    if (variant == 0)
+        MPS_COUNT_LAUNCH mps::k_spmv<float, double, double, 1><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.press, d.r,
+                                                                                                  d.rhs, 2);
+    else
+        S.residual_df(w);
+    if (S.pull_scal()) return CCT_CUDAERR;
+    if (relres) *relres = S.h_scal[mps::S_BNORM] > 0 ? S.h_scal[mps::S_RNORM] / S.h_scal[mps::S_BNORM] : 0.0;
+    if (host_r) return mps::cuda_status(cudaMemcpy(host_r, d.r, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
+    return CCT_NOERR;
 }
 
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n) {

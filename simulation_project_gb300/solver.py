@@ -52,6 +52,7 @@ _SIGS = {
     "mps_solver_step": (C.c_int, [P, C.c_int, C.POINTER(MpsStepStats)]),
     "mps_solver_get_particles": (C.c_int, [P, C.POINTER(C.c_int), P, P, P, P, P]),
     "mps_solver_get_triangles": (C.c_int, [P, P]),
+    "mps_solver_debug_residual": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_double)]),
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
     "mps_solver_copy_pressure": (C.c_int, [P, P]),
     "mps_solver_stream": (C.c_int, [P, C.POINTER(P)]),
@@ -163,6 +164,14 @@ class Solver:
         out["id"] = ids[:n]
         out["nbr_count"] = cnt[:n]
         return out
+
+    def debug_residual(self, variant: int):
+        """(r, ||r|| / ||b||) of the current state: variant 0 FP64 kernel, 1 double-float."""
+        n = self.state(sort_by_id=False)["id"].shape[0]
+        r = np.zeros(max(n, 1))
+        rel = C.c_double()
+        _check(_lib().mps_solver_debug_residual(self.h, int(variant), _p(r), C.byref(rel)), "mps_solver_debug_residual")
+        return r[:n], rel.value
 
     def triangles(self) -> np.ndarray:
         v = np.zeros((self.scene.t, 9))
