@@ -9,15 +9,21 @@ lattice, no dataset.  One "step" is one full solver step (topology, walls, drag,
 predictor, topology, PND, PPE solve, pressure-gradient correction, wall motion).
 
 value       = particle-steps/s of the FP32-operator / FP64-refined solver with the
-              learned initial guess and scaling (trained on the GPU by the library's
-              own BF16 tensor-core kernels before the timed region), states resident
-              in HBM;
+              multilevel preconditioner and the learned initial guess (trained on the
+              GPU by the library's own BF16 tensor-core kernels before the timed
+              region), states resident in HBM;
 plain_fp64  = the same steps with every operator and Jacobi-PCG in FP64;
 e2e         = the learned solver driven through the public C-ABI from pinned host
               buffers: each step uploads the state, steps, and downloads it.
 roofline    = the PPE SpMV (the dominant kernel) timed with CUDA events on the solver
               stream inside the timed region; algorithmic bytes per launch = 8 B per
-              neighbour entry (int32 index + FP32 weight) + 25 B per interior row.
+              neighbour entry (int32 index + FP32 weight) + 25 B per interior row;
+              traffic = DRAM bytes per entry from one ncu capture at full size
+              (SPMV_DRAM_BYTES_PER_ENTRY) times the live entry count.
+sort        = SortUsingThrust (stable LSD radix sort of (cell key, index)) on the
+              particle count with keys in the cell-key range, keys/s and GB/s.
+accuracy    = the FP32-IR solver against the FP64 solver on the same scene after
+              10 steps: pressure, PND, velocity, kinetic energy, positions.
 cpu_baseline= the FP64 oracle solver with OpenMP on the host cores, on a bounded
               sample (the same bucket at l0 = 0.004, ~1e5 particles, 1 step).
 --impl reference: the reference's own explicit-schedule kernels compiled for the CPU
@@ -41,6 +47,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# DRAM bytes per neighbour entry of one k_spmv<float,float,float,0> launch, measured
+# with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on the default
+# workload: 1.80 GB for 201.4M entries (SELL-32 padding included)
+SPMV_DRAM_BYTES_PER_ENTRY = 1.803e9 / 201.36e6
 
 
 def load_peaks():
@@ -234,7 +244,8 @@ def run_gpu(args):
     roofline = {"bound": "hbm", "kernel": "k_spmv<float,float,float> (PPE SpMV, FP32 rows)",
                 "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
                 "frac": round(achieved / peak_gbs, 3), "peak_kind": peak_kind,
-                "traffic": None, "bytes_per_launch": int(bytes_launch), "launches": spmv_n,
+                "traffic": int(SPMV_DRAM_BYTES_PER_ENTRY * nnz), "traffic_source": "ncu dram bytes per entry x entries",
+                "bytes_per_launch": int(bytes_launch), "launches": spmv_n,
                 "avg_launch_us": round(avg_ms * 1e3, 2)}
     phases = {k: round(float(np.mean([s[k] for s in st_fast])), 3) for k in
               ("ms_grid", "ms_walls", "ms_predictor", "ms_list", "ms_ppe_setup", "ms_spmv", "ms_cg_vec",
@@ -243,6 +254,8 @@ def run_gpu(args):
     # end to end through the C-ABI from pinned host buffers
     e2e = run_e2e(fast, args)
     fast.close()
+    sort = sort_bench(n, scene.box.cell_num, peak_gbs)
+    accuracy = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
 
     result = {
         "metric": "particle-steps/s @1M on 1 GB300, learned-precond vs plain CG at 1e-8 PPE residual",
@@ -287,6 +300,8 @@ def run_gpu(args):
                         "phases_ms": phases},
         "learned_training": train_info,
         "roofline": roofline,
+        "sort": sort,
+        "accuracy_vs_fp64": accuracy,
         "e2e": e2e,
         "gpu_launches": int(st_fast[0]["launches_in_region"]),
         "clocks": clk,
@@ -296,6 +311,71 @@ def run_gpu(args):
     if log:
         result["notes"] = log
     return result
+
+
+def sort_bench(n, cells, peak_gbs, reps=10):
+    """SortUsingThrust on n keys uniform in [0, cells) (the cell-key range of the
+    workload), timed with CUDA events on the legacy stream the sort runs on."""
+    from simulation_project_gb300 import lib
+    rng = np.random.default_rng(9)
+    keys0 = rng.integers(0, cells, n, dtype=np.int32)
+    dk, dv = lib.DeviceArray((n,), np.int32), lib.DeviceArray((n,), np.int32)
+    L = lib.load()
+    L.SortUsingThrust.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+    idx = np.arange(n, dtype=np.int32)
+    ev0, ev1 = lib.Event(), lib.Event()
+    total = 0.0
+    for r in range(reps + 2):
+        dk.upload(keys0)
+        dv.upload(idx)
+        lib.call("mps_device_sync")
+        ev0.record(None)
+        if L.SortUsingThrust(n, dk.ptr, dv.ptr) != 0:
+            raise RuntimeError("SortUsingThrust failed")
+        ev1.record(None)
+        lib.call("mps_device_sync")
+        if r >= 2:
+            total += ev0.elapsed_ms(ev1)
+    ok = bool(np.array_equal(dk.download(), np.sort(keys0, kind="stable")))
+    ms = total / reps
+    passes = max(1, (int(cells - 1).bit_length() + 7) // 8)
+    gbs = 16.0 * n * passes / (ms / 1e3) / 1e9   # read + write of key and value per pass
+    dk.free()
+    dv.free()
+    return {"keys": n, "key_range": int(cells), "passes": passes, "ms": round(ms, 4),
+            "keys_per_s": n / (ms / 1e3), "achieved_gbs": round(gbs, 1), "peak_gbs": peak_gbs,
+            "frac": round(gbs / peak_gbs, 3), "sorted_correctly": ok}
+
+
+def accuracy_vs_fp64(scene, params, args, steps=10):
+    """The metric's solver (FP32 operators, FP64 refinement, multilevel, learned guess)
+    against the FP64 solver on the same scene after `steps` steps, over the particle
+    ids both still hold."""
+    from simulation_project_gb300.solver import Solver
+    a = Solver(scene, precision="fp64")
+    b = Solver(scene, precision="fp32_ir", preconditioner=args.precond,
+               learned=args.learned_mode if params is not None else 0)
+    if params is not None:
+        b.set_learned(params)
+    for i in range(steps):
+        a.step(i)
+        b.step(i)
+    sa, sb = a.state(), b.state()
+    a.close()
+    b.close()
+    common, ia, ib = np.intersect1d(sa["id"], sb["id"], return_indices=True)
+    pa, pb = sa["press"][ia], sb["press"][ib]
+    va, vb = sa["vel"][ia], sb["vel"][ib]
+    na, nb = sa["pnd"][ia], sb["pnd"][ib]
+    ke_a, ke_b = 0.5 * np.sum(va * va), 0.5 * np.sum(vb * vb)
+    l0 = scene.param.InitialParticleDistance
+    return {"steps": steps, "particles_compared": int(len(common)),
+            "pressure_max_rel": float(np.abs(pb - pa).max() / np.abs(pa).max()),
+            "pressure_rms_rel": float(np.sqrt(np.mean((pb - pa) ** 2)) / np.sqrt(np.mean(pa ** 2))),
+            "pnd_max_rel": float(np.abs(nb - na).max() / scene.n0_pnd),
+            "velocity_max_rel": float(np.abs(vb - va).max() / np.abs(va).max()),
+            "kinetic_energy_rel": float(abs(ke_b - ke_a) / ke_a),
+            "position_max_over_l0": float(np.abs(sb["pos"][ib] - sa["pos"][ia]).max() / l0)}
 
 
 def run_profile_case(args):
@@ -426,6 +506,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--learned-mode", type=int, default=1, help="bit 0 initial guess, bit 1 diagonal scaling")
     ap.add_argument("--precond", type=int, default=1, help="0 Jacobi, 1 multilevel (FP32 inner solve)")
+    ap.add_argument("--accuracy-steps", type=int, default=10, help="steps of the FP32-IR vs FP64 comparison")
     ap.add_argument("--profile-case", action="store_true", help="only the solver steps (for ncu captures)")
     ap.add_argument("--fp64", action="store_true", help="with --profile-case: the plain FP64 solver")
     args = ap.parse_args()

@@ -84,6 +84,7 @@ typedef struct MpsStepStats {
     float ms_precond;       /* multilevel setup and V-cycles */
     int mg_levels;          /* coarse levels of the multilevel preconditioner (0: Jacobi) */
     int mg_level1;          /* level-1 aggregates */
+    double r0_relres;       /* ||b - A p0|| / ||b|| of the start (warm start or learned guess) */
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);

@@ -349,7 +349,7 @@ struct Solver {
         if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
         const int smem = (2 * kMgMaxDense * kMgMaxDense + kMgMaxDense) * (int)sizeof(float);
         if (cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) return CCT_CUDAERR;
-        mg.omega = opt.mg_omega > 0 ? (float)opt.mg_omega : 0.85f;
+        mg.omega = opt.mg_omega > 0 ? (float)opt.mg_omega : 1.0f;
         mg_on = mg_grid_levels >= 1;
         return CCT_NOERR;
     }
@@ -633,6 +633,7 @@ struct Solver {
         h_nnz[0] = h_scal[S_NNZ0];
         h_nnz[1] = h_scal[S_NNZ1];
         const double bnorm = h_scal[S_BNORM];
+        S.r0_relres = bnorm > 0 ? h_scal[S_RNORM] / bnorm : 0.0;
         const double tol = opt.cg_rtol * bnorm;
         MPS_COUNT_LAUNCH k_cg_start<double><<<kRedBlocks, 256, 0, st>>>(d, d.r, d.z, d.p, nullptr, 1.0, d.minv, nullptr, nullptr, 3, tol,
                                                        opt.cg_max_iter);
@@ -671,6 +672,7 @@ struct Solver {
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
                 h_nnz[1] = h_scal[S_NNZ1];
+                S.r0_relres = h_scal[S_BNORM] > 0 ? h_scal[S_RNORM] / h_scal[S_BNORM] : 0.0;
             }
             bnorm = h_scal[S_BNORM];
             const double rn = h_scal[S_RNORM];
@@ -748,7 +750,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->check_every = 8;
     o->source_relaxation = 0.05;
     o->preconditioner = MPS_PRECOND_MULTILEVEL;
-    o->mg_omega = 0.85;
+    o->mg_omega = 1.0;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
