@@ -385,7 +385,13 @@ def run_profile_case(args):
     from simulation_project_gb300.solver import Solver
     lib.load()
     scene = build_scene(args.l0)
-    s = Solver(scene, precision="fp64" if args.fp64 else "fp32_ir", profile=1, preconditioner=args.precond)
+    params = None
+    if args.profile_learned:
+        params, _ = train_learned(Solver, scene, args.train_steps, [])
+    s = Solver(scene, precision="fp64" if args.fp64 else "fp32_ir", profile=1, preconditioner=args.precond,
+               learned=args.learned_mode if params is not None else 0)
+    if params is not None:
+        s.set_learned(params)
     ms, _, st = time_steps(s, args.steps, args.warmup)
     s.close()
     print(json.dumps({"profile_case": True, "particles": scene.n, "ms_per_step": ms / args.steps,
@@ -509,6 +515,7 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=10, help="steps of the FP32-IR vs FP64 comparison")
     ap.add_argument("--profile-case", action="store_true", help="only the solver steps (for ncu captures)")
     ap.add_argument("--fp64", action="store_true", help="with --profile-case: the plain FP64 solver")
+    ap.add_argument("--profile-learned", action="store_true", help="with --profile-case: train, then the learned solver")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank = int(os.environ.get("RANK", "0"))

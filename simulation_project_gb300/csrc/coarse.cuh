@@ -18,7 +18,7 @@ namespace mps {
 
 constexpr int kMgMaxLevels = 10;
 constexpr int kMgMaxDense = 128;
-constexpr int kMgAsmThreads = 128;
+constexpr int kMgAsmThreads = 64;      // a cell holds ~50-70 particles
 
 struct MgLevel {
     int n;             // aggregates
@@ -40,7 +40,8 @@ struct Mg {
     MgLevel L[kMgMaxLevels + 1];   // L[0] unused
     float* ainv;       // [n_last^2] inverse of the last level's matrix
     int* agg1;         // [n] particle -> level-1 aggregate
-    unsigned* pcc;     // [n] cell coordinates of the particle, 10 bits each (x<<20 | y<<10 | z)
+    unsigned* pcc;     // [n] cell coordinates of the particle, 10 bits each (x<<20 | y<<10 | z),
+                       //     bit 31 set for an interior particle
 };
 
 __device__ __forceinline__ void mg_decode(int c, int gy, int gz, int& x, int& y, int& z) {
@@ -105,12 +106,12 @@ __global__ void k_mg_particles(const __grid_constant__ Dev d, const __grid_const
     const int c = d.key[i];
     if (c < 0 || c >= d.cells) {
         mg.agg1[i] = -1;
-        mg.pcc[i] = 0xffffffffu;
+        mg.pcc[i] = 0x7fffffffu;   // not interior: never summed
         return;
     }
     int x, y, z;
     mg_decode(c, d.box.m_GridSize.y, d.box.m_GridSize.z, x, y, z);
-    mg.pcc[i] = ((unsigned)x << 20) | ((unsigned)y << 10) | (unsigned)z;
+    mg.pcc[i] = ((unsigned)x << 20) | ((unsigned)y << 10) | (unsigned)z | (d.inner[i] ? 0x80000000u : 0u);
     mg.agg1[i] = mg.L[1].cmap[c];
 }
 
@@ -138,14 +139,29 @@ __global__ void __launch_bounds__(kMgAsmThreads) k_mg_assemble1(const __grid_con
         if (!d.inner[i]) continue;
         ds += d.diag[i];
         const int cnt = d.nbr_cnt[i];
-        for (int k = 0; k < cnt; ++k) {
-            const size_t ek = sell_index(i, k, d.K);
-            const int j = d.nbr[ek];
-            if (!d.inner[j]) continue;
-            const unsigned pj = mg.pcc[j];
-            const int dx = (int)(pj >> 20) - cx, dy = (int)((pj >> 10) & 1023u) - cy, dz = (int)(pj & 1023u) - cz;
-            if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
-            acc[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)][tid] += (float)w[ek];
+        for (int k = 0; k < cnt; k += 4) {
+            // four entries' loads in flight before the dependent gathers
+            int jj[4];
+            float wv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const bool a = k + u < cnt;
+                const size_t ek = sell_index(i, a ? k + u : k, d.K);
+                jj[u] = a ? d.nbr[ek] : -1;
+                wv[u] = a ? (float)w[ek] : 0.f;
+            }
+            unsigned pq[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) pq[u] = jj[u] >= 0 ? mg.pcc[jj[u]] : 0u;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned pj = pq[u];
+                if (!(pj & 0x80000000u)) continue;   // not interior (or no entry)
+                const int dx = (int)((pj >> 20) & 1023u) - cx, dy = (int)((pj >> 10) & 1023u) - cy,
+                          dz = (int)(pj & 1023u) - cz;
+                if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
+                acc[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)][tid] += wv[u];
+            }
         }
     }
     dsum[tid] = ds;

@@ -8,7 +8,17 @@
 
 namespace mps {
 
-// radix sort (sort.cu)
+// radix sort (sort.cu).  Scratch: alternate key and value arrays, the digit counts
+// of every tile (digit-major), 8 spare words and per-pass digit totals.
+constexpr int kRadixSortTile = 2048;
+constexpr int kRadixBuckets = 256;
+constexpr int kRadixMaxPasses = 4;
+constexpr size_t radix_scratch_bytes_for(long long n) {
+    return sizeof(int) * 2 * (size_t)(n > 0 ? n : 0) +
+           sizeof(unsigned) * ((size_t)kRadixBuckets * (size_t)(((n > 0 ? n : 1) + kRadixSortTile - 1) / kRadixSortTile) +
+                               8 + (size_t)kRadixMaxPasses * kRadixBuckets) +
+           256;
+}
 size_t radix_scratch_bytes(int n);
 int radix_passes(unsigned range);
 cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, void* scratch, cudaStream_t st);

@@ -9,7 +9,9 @@
 //   k_digit_hist : each 2048-key tile counts its digits (warp-aggregated with
 //                  __match_any_sync, then shared-memory adds); counts stored
 //                  digit-major: counts[d * tiles + tile]
-//   k_scan_excl  : one CTA turns the counts into exclusive offsets
+//                  and adds its per-digit totals to dtot[pass][d]
+//   k_scan_digits: CTA per digit d: base(d) = sum of the totals of the smaller
+//                  digits, then the exclusive scan of counts[d][0..tiles) from base(d)
 //   k_scatter    : each tile re-reads its keys in index order (warp w owns keys
 //                  [w*256, w*256+256) of the tile, 32 per round), ranks them stably
 //                  with __match_any_sync + per-warp running digit counters, and
@@ -24,14 +26,16 @@ namespace mps {
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
-constexpr int kRadix = 256;
+constexpr int kRadix = kRadixBuckets;
+static_assert(kSortTile == kRadixSortTile, "tile size of the scratch formula");
 
 __device__ __forceinline__ unsigned digit_of(int key, int kmin, int shift) {
     return (((unsigned)key - (unsigned)kmin) >> shift) & 255u;
 }
 
 __global__ void __launch_bounds__(kSortThreads) k_digit_hist(const int* __restrict__ keys, int n, int kmin, int shift,
-                                                            int tiles, unsigned* __restrict__ counts) {
+                                                            int tiles, unsigned* __restrict__ counts,
+                                                            unsigned* __restrict__ dtot) {
     __shared__ unsigned h[kRadix];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -46,6 +50,7 @@ __global__ void __launch_bounds__(kSortThreads) k_digit_hist(const int* __restri
     }
     __syncthreads();
     counts[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+    if (h[threadIdx.x]) atomicAdd(&dtot[threadIdx.x], h[threadIdx.x]);
 }
 
 // Exclusive scan of len unsigned values, in place, by one CTA of 1024 threads.
@@ -115,6 +120,34 @@ __device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* ws, un
     const unsigned ex = x - v + (w > 0 ? ws[w - 1] : 0u);
     total = ws[31];
     return ex;
+}
+
+// CTA per digit: offsets[d][t] = base(d) + sum of counts[d][t' < t], in place
+__global__ void __launch_bounds__(kScanThreads) k_scan_digits(unsigned* __restrict__ counts, int tiles,
+                                                              const unsigned* __restrict__ dtot) {
+    __shared__ unsigned ws[32];
+    __shared__ unsigned carry;
+    const int d = blockIdx.x;
+    unsigned v = threadIdx.x < (unsigned)d ? dtot[threadIdx.x] : 0u;   // d < 256 <= blockDim
+    unsigned base;
+    (void)block_exclusive(v, ws, base);
+    if (threadIdx.x == 0) carry = base;
+    __syncthreads();
+    unsigned* row = counts + (size_t)d * tiles;
+    for (int c0 = 0; c0 < tiles; c0 += 4 * kScanThreads) {
+        const int o4 = c0 + 4 * threadIdx.x;
+        const unsigned v0 = o4 < tiles ? row[o4] : 0u, v1 = o4 + 1 < tiles ? row[o4 + 1] : 0u;
+        const unsigned v2 = o4 + 2 < tiles ? row[o4 + 2] : 0u, v3 = o4 + 3 < tiles ? row[o4 + 3] : 0u;
+        unsigned total;
+        const unsigned ex = block_exclusive(v0 + v1 + v2 + v3, ws, total) + carry;
+        if (o4 < tiles) row[o4] = ex;
+        if (o4 + 1 < tiles) row[o4 + 1] = ex + v0;
+        if (o4 + 2 < tiles) row[o4 + 2] = ex + v0 + v1;
+        if (o4 + 3 < tiles) row[o4 + 3] = ex + v0 + v1 + v2;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const unsigned* __restrict__ a, int len,
@@ -242,10 +275,7 @@ __global__ void k_minmax_init(int* mm) {
     mm[1] = INT_MIN;
 }
 
-size_t radix_scratch_bytes(int n) {
-    const int tiles = div_up(n > 0 ? n : 1, kSortTile);
-    return sizeof(int) * 2 * (size_t)n + sizeof(unsigned) * ((size_t)kRadix * tiles + 8) + 256;
-}
+size_t radix_scratch_bytes(int n) { return radix_scratch_bytes_for(n); }
 
 int radix_passes(unsigned range) {
     int bits = 0;
@@ -262,14 +292,18 @@ cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, 
     int* valt = (int*)p;
     p += sizeof(int) * (size_t)n;
     unsigned* counts = (unsigned*)p;
+    unsigned* dtot = counts + (size_t)kRadix * tiles + 8;   // [kRadixMaxPasses][kRadix]
+    if (passes > kRadixMaxPasses) return cudaErrorInvalidValue;
+    cudaMemsetAsync(dtot, 0, sizeof(unsigned) * kRadix * passes, st);
     int* ka = keys;
     int* va = vals;
     int* kb = kalt;
     int* vb = valt;
     for (int pass = 0; pass < passes; ++pass) {
         const int shift = pass * 8;
-        MPS_COUNT_LAUNCH k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts);
-        MPS_COUNT_LAUNCH k_scan_excl<<<1, 1024, 0, st>>>(counts, kRadix * tiles, nullptr);
+        unsigned* dt = dtot + (size_t)kRadix * pass;
+        MPS_COUNT_LAUNCH k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts, dt);
+        MPS_COUNT_LAUNCH k_scan_digits<<<kRadix, kScanThreads, 0, st>>>(counts, tiles, dt);
         MPS_COUNT_LAUNCH k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, kmin, shift, tiles, counts);
         int* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;

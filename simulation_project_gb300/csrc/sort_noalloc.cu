@@ -11,7 +11,7 @@
 // Limits and rules:
 //   * at most kNoAllocMaxKeys = 262,144 keys per call; larger n returns CCT_PARAMERR
 //     (mps_last_error() says why) without touching the arrays;
-//   * the array (2,228,768 bytes, about 2.1 MiB) lives in every GPU that loads the
+//   * the array (2,232,864 bytes, about 2.1 MiB) lives in every GPU that loads the
 //     library, until the process exits;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, with that device current); make that first
@@ -32,12 +32,8 @@ namespace mps {
 namespace {
 
 constexpr int kNoAllocMaxKeys = 1 << 18;
-constexpr int kNoAllocTile = 2048;      // keys per radix tile (sort.cu)
-constexpr int kNoAllocRadix = 256;      // digits per pass
 constexpr size_t kNoAllocHeader = 256;  // min/max words, padded to the array alignment
-constexpr size_t kNoAllocSortBytes =
-    sizeof(int) * 2 * (size_t)kNoAllocMaxKeys +
-    sizeof(unsigned) * ((size_t)kNoAllocRadix * ((kNoAllocMaxKeys + kNoAllocTile - 1) / kNoAllocTile) + 8) + 256;
+constexpr size_t kNoAllocSortBytes = radix_scratch_bytes_for(kNoAllocMaxKeys);
 constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocSortBytes;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
