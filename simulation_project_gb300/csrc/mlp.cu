@@ -187,6 +187,130 @@ __global__ void k_unpad_output(int M, const float* __restrict__ Yp, float* __res
     if (i >= M * FOUT) return;
     Y[i] = Yp[(size_t)(i / FOUT) * FOUTP + (i % FOUT)];
 }
+
+// ---------------------------------------------------------------------------
+// Fused inference: the whole 12 -> 128 -> 128 -> 128 -> 2 network in one
+// persistent kernel.  Each CTA stages the four weight matrices once in shared
+// memory, transposed to [n][k] with padded rows (conflict-free B fragments); each
+// warp takes 16 rows at a time through all layers with mma.m16n8k16 (BF16 in, FP32
+// accumulate).  Bias and SiLU are applied to the accumulator fragments in
+// registers, which are repacked directly as the next layer's BF16 A fragments
+// (the m16n8 accumulator of n-tiles 2k, 2k+1 is the m16k16 A tile of k-step k), so
+// activations never leave the registers.  Same rounding points as the layer-by-
+// layer path: FP32 sum + bias, SiLU in FP32, BF16 activations.
+// ---------------------------------------------------------------------------
+constexpr int kMiWarps = 8;
+constexpr int kMiS1 = 24;    // padded row (elements) of W1^T [128][16]
+constexpr int kMiS = 136;    // padded row of W2^T, W3^T [128][128] and W4^T [8][128]
+constexpr size_t kMiSmem = sizeof(bf16) * (128 * kMiS1 + 2 * 128 * kMiS + 8 * kMiS) + sizeof(float) * (3 * H + 8);
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// 16 x 128 accumulator (16 n-tiles) -> bias + SiLU -> A fragments of the next layer
+__device__ __forceinline__ void mi_activate(float (&acc)[16][4], const float* __restrict__ bias, int c,
+                                            uint32_t (&a)[8][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) {
+        const float b0 = bias[nt * 8 + 2 * c], b1 = bias[nt * 8 + 2 * c + 1];
+        acc[nt][0] = silu(acc[nt][0] + b0);
+        acc[nt][1] = silu(acc[nt][1] + b1);
+        acc[nt][2] = silu(acc[nt][2] + b0);
+        acc[nt][3] = silu(acc[nt][3] + b1);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        a[k][0] = pack_bf16(acc[2 * k][0], acc[2 * k][1]);
+        a[k][1] = pack_bf16(acc[2 * k][2], acc[2 * k][3]);
+        a[k][2] = pack_bf16(acc[2 * k + 1][0], acc[2 * k + 1][1]);
+        a[k][3] = pack_bf16(acc[2 * k + 1][2], acc[2 * k + 1][3]);
+    }
+}
+
+// hidden layer 128 -> 128 with weights W^T [128][kMiS] in shared memory
+__device__ __forceinline__ void mi_hidden(const uint32_t (&a)[8][4], const bf16* __restrict__ wt, int g, int c,
+                                          float (&acc)[16][4]) {
+#pragma unroll
+    for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            const bf16* row = wt + (nt * 8 + g) * kMiS + 16 * k + 2 * c;
+            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8)};
+            mma_bf16(acc[nt], a[k], b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kMiWarps * 32) k_mlp_infer(int M, const float* __restrict__ X, float* __restrict__ Y,
+                                                            Layers L) {
+    extern __shared__ __align__(16) unsigned char mi_smem[];
+    bf16* w1 = reinterpret_cast<bf16*>(mi_smem);   // [128][kMiS1]
+    bf16* w2 = w1 + 128 * kMiS1;                    // [128][kMiS]
+    bf16* w3 = w2 + 128 * kMiS;
+    bf16* w4 = w3 + 128 * kMiS;                     // [8][kMiS]
+    float* bs = reinterpret_cast<float*>(w4 + 8 * kMiS);   // b1, b2, b3 [128], b4 [8]
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int e = threadIdx.x; e < 128 * kMiS1; e += blockDim.x) {
+        const int n = e / kMiS1, k = e % kMiS1;
+        w1[e] = k < FINP ? L.W1[k * H + n] : zero;
+    }
+    for (int e = threadIdx.x; e < H * H; e += blockDim.x) {
+        const int k = e / H, n = e % H;   // W[k][n]
+        w2[n * kMiS + k] = L.W2[e];
+        w3[n * kMiS + k] = L.W3[e];
+    }
+    for (int e = threadIdx.x; e < 8 * H; e += blockDim.x) {
+        const int n = e / H, k = e % H;
+        w4[n * kMiS + k] = L.W4[k * FOUTP + n];
+    }
+    for (int e = threadIdx.x; e < 3 * H + 8; e += blockDim.x)
+        bs[e] = e < H ? L.b1[e] : e < 2 * H ? L.b2[e - H] : e < 3 * H ? L.b3[e - 2 * H] : L.b4[e - 3 * H];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, c = lane & 3;
+    const int tiles = (M + 15) / 16;
+    for (int t = blockIdx.x * kMiWarps + warp; t < tiles; t += gridDim.x * kMiWarps) {
+        const int r0 = t * 16 + g, r1 = r0 + 8;
+        // layer 1: A = features (12 of 16 columns), one k-step
+        auto feat2 = [&](int r, int col) -> uint32_t {
+            if (r >= M || col >= FIN) return 0u;
+            const float2 v = *reinterpret_cast<const float2*>(X + (size_t)r * FIN + col);
+            return pack_bf16(v.x, v.y);
+        };
+        const uint32_t a1[4] = {feat2(r0, 2 * c), feat2(r1, 2 * c), feat2(r0, 2 * c + 8), feat2(r1, 2 * c + 8)};
+        float acc[16][4];
+#pragma unroll
+        for (int nt = 0; nt < 16; ++nt) {
+            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+            const bf16* row = w1 + (nt * 8 + g) * kMiS1 + 2 * c;
+            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8)};
+            mma_bf16(acc[nt], a1, b);
+        }
+        uint32_t a[8][4];
+        mi_activate(acc, bs, c, a);
+        mi_hidden(a, w2, g, c, acc);
+        mi_activate(acc, bs + H, c, a);
+        mi_hidden(a, w3, g, c, acc);
+        mi_activate(acc, bs + 2 * H, c, a);
+        // output layer: one n-tile (columns 0..7, of which 0 and 1 are used)
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const bf16* row = w4 + g * kMiS + 16 * k + 2 * c;
+            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8)};
+            mma_bf16(o, a[k], b);
+        }
+        if (c == 0) {
+            const float b0 = bs[3 * H], b1 = bs[3 * H + 1];
+            if (r0 < M) *reinterpret_cast<float2*>(Y + (size_t)r0 * FOUT) = make_float2(o[0] + b0, o[1] + b1);
+            if (r1 < M) *reinterpret_cast<float2*>(Y + (size_t)r1 * FOUT) = make_float2(o[2] + b0, o[3] + b1);
+        }
+    }
+}
 // dY = d loss / d y for loss = mean((y0 - t0)^2 + w1 (y1 - t1)^2); loss partial sums
 __global__ void k_loss_grad(int M, const float* __restrict__ Yp, const float* __restrict__ T, float w1,
                             bf16* __restrict__ dYb, float* __restrict__ dY, double* __restrict__ loss) {
@@ -370,12 +494,19 @@ struct MpsMlp {
 namespace mps {
 // used by the solver: forward of a created MLP on M rows of features
 cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st) {
-    for (int r = 0; r < M; r += m->maxb) {
-        const int cnt = min(m->maxb, M - r);
-        cudaError_t e = m->forward(cnt, X + (size_t)r * FIN, st, false);
+    if (M <= 0) return cudaSuccess;
+    static bool smem_set = false;   // the attribute is per function, set once per process
+    if (!smem_set) {
+        const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMiSmem);
         if (e) return e;
-        MPS_COUNT_LAUNCH k_unpad_output<<<div_up(cnt * FOUT, 256), 256, 0, st>>>(cnt, m->Yp, Y + (size_t)r * FOUT);
+        smem_set = true;
     }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (M + 15) / 16;
+    const int grid = std::max(1, std::min(div_up(tiles, kMiWarps), 2 * std::max(sms, 1)));
+    MPS_COUNT_LAUNCH k_mlp_infer<<<grid, kMiWarps * 32, kMiSmem, st>>>(M, X, Y, m->L);
     return cudaGetLastError();
 }
 }  // namespace mps

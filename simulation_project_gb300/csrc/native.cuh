@@ -76,6 +76,7 @@ struct Dev {
     float *r32, *z32, *p32, *q32, *d32, *m32;  // FP32 inner CG vectors, m32 = preconditioner
     double* minv;              // FP64 preconditioner (1/diag or learned)
     float *xh, *xl;            // x = xh + xl (to ~2^-48): split pressure for the double-float residual
+    float* pf32;               // FP32 pressure (neighbour-pressure feature)
     double* feat_aux;          // per-particle auxiliaries for features (div, mean P, ...)
     double* red;               // block partial sums
     double* scal;              // device scalars

@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                             ((T*)d.nbrw)[e] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
-                        if constexpr (MODE == NB_LIST_FEAT) a1 += (T)d.press[j];   // neighbour pressure
+                        if constexpr (MODE == NB_LIST_FEAT) a1 += (T)d.pf32[j];    // neighbour pressure
                         if (rr < reg) {
                             gacc = true;
                             const T rg = rr > mindg ? rr : mindg;
@@ -711,6 +711,12 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
             d.scal[S_BNORM] = sqrt(out[1]);
         }
     }
+}
+
+// FP32 copy of the pressure (neighbour-pressure feature)
+__global__ void k_to_float_p(int n, const double* __restrict__ p, float* __restrict__ q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) q[i] = (float)p[i];
 }
 
 // x = xh + xl: the FP64 pressure split into two floats (representation error
@@ -925,31 +931,35 @@ __global__ void __launch_bounds__(256) k_pressure_scale(const __grid_constant__ 
 
 // 12 features per particle (FP32); r holds the FP64 initial residual b - A p_prev
 __global__ void k_features(const __grid_constant__ Dev d) {
+    // FP32 arithmetic (the FP64 pipe is narrow); FP64 only for the PND deviation
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
-    const double ps = d.scal[S_PSCALE];
+    const float ips = (float)(1.0 / d.scal[S_PSCALE]);
     float* f = d.feat + 12 * (size_t)i;
-    const double dg = d.diag[i];
-    f[0] = (float)((d.pnd[i] - d.c.n0_pnd) / d.c.n0_pnd * 10.0);
-    f[1] = (float)(d.feat_aux[4 * (size_t)i + 1] * d.c.dt * 10.0);
+    const float idg = 1.f / (float)d.diag[i];
+    f[0] = (float)(d.pnd[i] - d.c.n0_pnd) * (float)(10.0 / d.c.n0_pnd);
+    f[1] = (float)d.feat_aux[4 * (size_t)i + 1] * (float)(d.c.dt * 10.0);
     const int t = d.wid[i];
-    if (t >= 0 && d.wdist[i] < d.c.re_lap) {
+    const float wd = (float)d.wdist[i];
+    if (t >= 0 && wd < (float)d.c.re_lap) {
         const double* w = d.wdir + 3 * (size_t)i;
-        const double l = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-        f[2] = (float)(d.wdist[i] / d.c.re_lap);
-        f[3] = l > 0 ? (float)(w[0] / l) : 0.f;
-        f[4] = l > 0 ? (float)(w[1] / l) : 0.f;
-        f[5] = l > 0 ? (float)(w[2] / l) : 0.f;
+        const float wx = (float)w[0], wy = (float)w[1], wz = (float)w[2];
+        const float l = sqrtf(wx * wx + wy * wy + wz * wz);
+        const float il = l > 0.f ? 1.f / l : 0.f;
+        f[2] = wd * (float)(1.0 / d.c.re_lap);
+        f[3] = wx * il;
+        f[4] = wy * il;
+        f[5] = wz * il;
     } else {
         f[2] = 1.f; f[3] = 0.f; f[4] = 0.f; f[5] = 0.f;
     }
-    f[6] = (float)(d.press[i] / ps);
-    f[7] = (float)(d.feat_aux[4 * (size_t)i] / ps);
-    f[8] = (float)(d.rhs[i] / dg / ps);
-    f[9] = (float)(d.feat_aux[4 * (size_t)i + 2] / 250.0);
-    f[10] = (float)(d.inner[i] ? d.r[i] / dg / ps : 0.0);
-    const dbl4 v = d.vel[i];
-    f[11] = (float)(sqrt(v.x * v.x + v.y * v.y + v.z * v.z) * d.c.dt / d.c.l0 * 100.0);
+    f[6] = (float)d.press[i] * ips;
+    f[7] = (float)d.feat_aux[4 * (size_t)i] * ips;
+    f[8] = (float)d.rhs[i] * idg * ips;
+    f[9] = (float)d.feat_aux[4 * (size_t)i + 2] * (1.f / 250.f);
+    f[10] = d.inner[i] ? (float)d.r[i] * idg * ips : 0.f;
+    const float4 v = d.ovel[i];
+    f[11] = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z) * (float)(d.c.dt / d.c.l0 * 100.0);
 }
 
 // predicted increment dp = scale * y0 (into z), preconditioner M^-1 = exp(y1) / diag

@@ -192,9 +192,9 @@ struct Solver {
         e = e ? e : mk(&d.inner, N);
         e = e ? e : mk(&d.r, N); e = e ? e : mk(&d.z, N); e = e ? e : mk(&d.p, N); e = e ? e : mk(&d.q, N);
         e = e ? e : mk(&d.minv, N);
-        e = e ? e : mk(&d.r32, N); e = e ? e : mk(&d.z32, N); e = e ? e : mk(&d.p32, N); e = e ? e : mk(&d.q32, N);
+        e = e ? e : mk(&d.r32, N); e = e ? e : mk(&d.z32, N); e = e ? e : mk(&d.pf32, N); e = e ? e : mk(&d.q32, N);
         e = e ? e : mk(&d.d32, N); e = e ? e : mk(&d.m32, N);
-        e = e ? e : mk(&d.xh, N); e = e ? e : mk(&d.xl, N);
+        e = e ? e : mk(&d.xh, N); e = e ? e : mk(&d.xl, N); e = e ? e : mk(&d.p32, N);
         e = e ? e : mk(&d.feat_aux, 4 * N);
         e = e ? e : mk(&d.red, 4 * (size_t)kRedBlocks);
         e = e ? e : mk(&d.scal, (size_t)S_COUNT);
@@ -506,8 +506,10 @@ struct Solver {
         walls_distance<T>();
         timer.mark(PH_LIST, st);
         const int nb_cells = std::max(1, std::min(d.cells, d.n));
-        if ((learned_ready && opt.learned) || collect)
+        if ((learned_ready && opt.learned) || collect) {
+            MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
             MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST_FEAT><<<nb_cells, kNbThreads, 0, st>>>(d);
+        }
         else
             MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST><<<nb_cells, kNbThreads, 0, st>>>(d);
         timer.mark(PH_SETUP, st);
