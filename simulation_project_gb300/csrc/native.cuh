@@ -77,7 +77,6 @@ struct Dev {
     double* minv;              // FP64 preconditioner (1/diag or learned)
     float *xh, *xl;            // x = xh + xl (to ~2^-48): split pressure for the double-float residual
     float* pf32;               // FP32 pressure (neighbour-pressure feature)
-    double* feat_aux;          // per-particle auxiliaries for features (div, mean P, ...)
     double* red;               // block partial sums
     double* scal;              // device scalars
     unsigned* red_count;       // last-block counters

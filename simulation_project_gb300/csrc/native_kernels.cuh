@@ -19,7 +19,7 @@ constexpr int kStageCap = 2048;
 constexpr int kRedBlocks = 1216;   // 152 SMs x 8 resident CTAs of 256 threads
 constexpr int kVecThreads = 256;
 
-enum { NB_PREDICT = 0, NB_LIST = 1, NB_LIST_FEAT = 2 };
+enum { NB_PREDICT = 0, NB_LIST = 1 };
 
 template <class T> struct V3 { T x, y, z; };
 
@@ -404,11 +404,6 @@ __device__ __forceinline__ void nb_epilogue(const Dev& d, int i, T a0, T a1, T a
             pnd += exact_z<double>(d.c.dim == 2 ? c_zgrad2 : c_zgrad3, d.c.dim == 2 ? 23 : 21, riw, d.c.l0);
         d.pnd[i] = pnd;
         d.sumw[i] = (double)a0;
-        if constexpr (MODE == NB_LIST_FEAT) {
-            d.feat_aux[4 * (size_t)i] = cnt > 0 ? (double)a1 / cnt : 0.0;
-            d.feat_aux[4 * (size_t)i + 1] = (double)a3 * (double)d.c.dim / d.c.n0_pnd;
-            d.feat_aux[4 * (size_t)i + 2] = (double)cnt;
-        }
     }
 }
 
@@ -418,7 +413,6 @@ __device__ __forceinline__ void nb_epilogue(const Dev& d, int i, T a0, T a1, T a
 // its lanes test 32 candidates per round.  MODE:
 //   NB_PREDICT    Laplacian of the velocity -> viscosity/gravity/drag predictor
 //   NB_LIST       Laplacian rows (SELL-32), gradient rows, PND, sum of weights
-//   NB_LIST_FEAT  NB_LIST plus the learned features' neighbour aggregates
 // The warp's butterfly sums are parked in lane k%32 for its k-th target and the
 // epilogues run lane-parallel.
 template <class T, int MODE>
@@ -536,18 +530,11 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                             ((T*)d.nbrw)[e] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
-                        if constexpr (MODE == NB_LIST_FEAT) a1 += (T)d.pf32[j];    // neighbour pressure
                         if (rr < reg) {
                             gacc = true;
                             const T rg = rr > mindg ? rr : mindg;
                             const T wg = reg / rg - T(1);
                             a2 += wg;                              // PND
-                            if constexpr (MODE == NB_LIST_FEAT) {
-                                // velocity divergence (feature): sum (v_j - v_i).d w / r^2
-                                const float4 vj4 = d.ovel[j];
-                                a3 += ((T(vj4.x) - vi.x) * dv.x + (T(vj4.y) - vi.y) * dv.y +
-                                       (T(vj4.z) - vi.z) * dv.z) * wg / (rg * rg);
-                            }
                         }
                     }
                 }
@@ -930,6 +917,10 @@ __global__ void __launch_bounds__(256) k_pressure_scale(const __grid_constant__ 
 }
 
 // 12 features per particle (FP32); r holds the FP64 initial residual b - A p_prev
+// The network's neighbour aggregates come from the gradient-radius rows (index,
+// distance): mean previous pressure and velocity divergence
+// sum (v_j - v_i).(x_j - x_i) w_g / r^2 * d / n0 over the PND neighbours.
+template <class T>
 __global__ void k_features(const __grid_constant__ Dev d) {
     // FP32 arithmetic (the FP64 pipe is narrow); FP64 only for the PND deviation
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -937,8 +928,23 @@ __global__ void k_features(const __grid_constant__ Dev d) {
     const float ips = (float)(1.0 / d.scal[S_PSCALE]);
     float* f = d.feat + 12 * (size_t)i;
     const float idg = 1.f / (float)d.diag[i];
+    const float4 pi = d.opos[i], vi = d.ovel[i];
+    const float reg = (float)d.c.re_grad, mindg = (float)d.c.mind_grad;
+    const int gc = d.gcnt[i];
+    float psum = 0.f, div = 0.f;
+    for (int k = 0; k < gc; ++k) {
+        const size_t e = (size_t)i * d.KG + k;
+        const int j = d.gnbr[e];
+        const float r = (float)((const T*)d.gnbrr)[e];
+        const float4 pj = d.opos[j], vj = d.ovel[j];
+        const float rg = r > mindg ? r : mindg;
+        const float wg = reg / rg - 1.f;
+        psum += d.pf32[j];
+        div += ((vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) + (vj.z - vi.z) * (pj.z - pi.z)) * wg /
+               (rg * rg);
+    }
     f[0] = (float)(d.pnd[i] - d.c.n0_pnd) * (float)(10.0 / d.c.n0_pnd);
-    f[1] = (float)d.feat_aux[4 * (size_t)i + 1] * (float)(d.c.dt * 10.0);
+    f[1] = div * (float)(d.c.dim / d.c.n0_pnd * d.c.dt * 10.0);
     const int t = d.wid[i];
     const float wd = (float)d.wdist[i];
     if (t >= 0 && wd < (float)d.c.re_lap) {
@@ -954,12 +960,11 @@ __global__ void k_features(const __grid_constant__ Dev d) {
         f[2] = 1.f; f[3] = 0.f; f[4] = 0.f; f[5] = 0.f;
     }
     f[6] = (float)d.press[i] * ips;
-    f[7] = (float)d.feat_aux[4 * (size_t)i] * ips;
+    f[7] = gc > 0 ? psum / (float)gc * ips : 0.f;
     f[8] = (float)d.rhs[i] * idg * ips;
-    f[9] = (float)d.feat_aux[4 * (size_t)i + 2] * (1.f / 250.f);
+    f[9] = (float)d.nbr_cnt[i] * (1.f / 250.f);
     f[10] = d.inner[i] ? (float)d.r[i] * idg * ips : 0.f;
-    const float4 v = d.ovel[i];
-    f[11] = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z) * (float)(d.c.dt / d.c.l0 * 100.0);
+    f[11] = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * (float)(d.c.dt / d.c.l0 * 100.0);
 }
 
 // predicted increment dp = scale * y0 (into z), preconditioner M^-1 = exp(y1) / diag

@@ -195,7 +195,6 @@ struct Solver {
         e = e ? e : mk(&d.r32, N); e = e ? e : mk(&d.z32, N); e = e ? e : mk(&d.pf32, N); e = e ? e : mk(&d.q32, N);
         e = e ? e : mk(&d.d32, N); e = e ? e : mk(&d.m32, N);
         e = e ? e : mk(&d.xh, N); e = e ? e : mk(&d.xl, N); e = e ? e : mk(&d.p32, N);
-        e = e ? e : mk(&d.feat_aux, 4 * N);
         e = e ? e : mk(&d.red, 4 * (size_t)kRedBlocks);
         e = e ? e : mk(&d.scal, (size_t)S_COUNT);
         e = e ? e : mk(&d.red_count, 16);
@@ -506,12 +505,7 @@ struct Solver {
         walls_distance<T>();
         timer.mark(PH_LIST, st);
         const int nb_cells = std::max(1, std::min(d.cells, d.n));
-        if ((learned_ready && opt.learned) || collect) {
-            MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
-            MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST_FEAT><<<nb_cells, kNbThreads, 0, st>>>(d);
-        }
-        else
-            MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST><<<nb_cells, kNbThreads, 0, st>>>(d);
+        MPS_COUNT_LAUNCH k_neighbours<T, NB_LIST><<<nb_cells, kNbThreads, 0, st>>>(d);
         timer.mark(PH_SETUP, st);
         if (opt.pressure_mode == MPS_PRESSURE_EXPLICIT) {
             MPS_COUNT_LAUNCH k_eos<<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -528,7 +522,8 @@ struct Solver {
                 else
                     residual_df((const float*)d.nbrw);
                 MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
-                MPS_COUNT_LAUNCH k_features<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
+                MPS_COUNT_LAUNCH k_features<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 if (use_learned) {
                     if (mlp_forward(mlp, d.n, d.feat, d.mlp_out, st)) return CCT_CUDAERR;
                     MPS_COUNT_LAUNCH k_learned_apply<<<blocks_for(d.n), kBlock, 0, st>>>(d, (opt.learned & 2) ? 1 : 0);
