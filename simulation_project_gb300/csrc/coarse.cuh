@@ -334,33 +334,6 @@ __global__ void k_mg_down(const double* __restrict__ scal, MgLevel lo, MgLevel h
     }
 }
 
-// last level (one CTA of 32 warps): restriction from lo (if from_lo), then
-// e2 = A^-1 r with the explicit inverse, a warp per row, lanes over columns
-__global__ void __launch_bounds__(1024) k_mg_bottom(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
-                                                    int from_lo, const float* __restrict__ ainv) {
-    if (scal[S_CONV] != 0.0) return;
-    __shared__ float rs[kMgMaxDense];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int I = w; I < hi.n; I += nw) {
-        float s;
-        if (from_lo) {
-            s = mg_child_residual_warp(lo, hi, I, lane);
-            if (lane == 0) hi.r[I] = s;
-        } else {
-            s = hi.r[I];
-        }
-        if (lane == 0) rs[I] = s;
-    }
-    __syncthreads();
-    for (int I = w; I < hi.n; I += nw) {
-        float v = 0.f;
-        for (int J = lane; J < hi.n; J += 32) v += ainv[I * hi.n + J] * rs[J];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) hi.e2[I] = v;
-    }
-}
-
 // prolongation hi -> lo and the up sweep on lo: e' = e + P e_hi,
 // e2 = e' + omega D^-1 (r - A e'); warp per lo aggregate, lane per stencil slot
 __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi, float omega) {
@@ -375,6 +348,65 @@ __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     if (lane == 0) lo.e2[I] = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
+}
+
+// CG update fused with the level-1 restriction (multilevel path): warp per level-1
+// aggregate over its contiguous rows: x += alpha p, r -= alpha q on interior rows,
+// r1[I] = sum of r over the cell, the first down sweep e1 = omega D1^-1 r1, and
+// ||r||^2 with the convergence test (as k_cg_update with_z = 0).
+template <class TV, class TXA>
+__global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
+                                                            TXA* __restrict__ x, TV* __restrict__ r,
+                                                            const TV* __restrict__ p, const TV* __restrict__ q, int slot) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const MgLevel& L1 = mg.L[1];
+    const TV alpha = (TV)d.scal[S_ALPHA];
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    TV prr = TV(0);
+    for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < L1.n; I += nw) {
+        const int c = L1.ccell[I];
+        float s = 0.f;
+        for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) {
+            if (!d.inner[i]) continue;
+            x[i] = x[i] + (TXA)alpha * (TXA)p[i];
+            const TV ri = r[i] - alpha * q[i];
+            r[i] = ri;
+            prr += ri * ri;
+            s += (float)ri;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            L1.r[I] = s;
+            L1.e[I] = mg.omega * L1.dinv[I] * s;
+        }
+    }
+    double v[1] = {(double)prr}, out[1];
+    if (grid_reduce<1, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        const double rn = sqrt(out[0]);
+        d.scal[S_RNORM] = rn;
+        const double it = d.scal[S_ITER] + 1.0;
+        d.scal[S_ITER] = it;
+        if (rn <= d.scal[S_TOL] || it >= d.scal[S_MAXIT] || !(rn == rn)) d.scal[S_CONV] = 1.0;
+    }
+}
+
+// last level: e2 = A^-1 r with the explicit inverse (one CTA, warp per row)
+__global__ void __launch_bounds__(1024) k_mg_dense_solve(const double* __restrict__ scal, MgLevel lv,
+                                                         const float* __restrict__ ainv) {
+    if (scal[S_CONV] != 0.0) return;
+    __shared__ float rs[kMgMaxDense];
+    for (int I = threadIdx.x; I < lv.n; I += blockDim.x) rs[I] = lv.r[I];
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int I = w; I < lv.n; I += nw) {
+        float v = 0.f;
+        for (int J = lane; J < lv.n; J += 32) v += ainv[I * lv.n + J] * rs[J];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) lv.e2[I] = v;
+    }
 }
 
 // fine level: z = m r + e1[aggregate] on interior rows (0 elsewhere), rz = r.z;

@@ -389,21 +389,20 @@ struct Solver {
         return CCT_NOERR;
     }
 
-    // z = M^-1 r (interior rows), rz; mode 1 also sets p = z and S_RZ, mode 0 S_BETA
-    void mg_apply(const float* r, float* z, float* p, int mode) {
+    // z = M^-1 r (interior rows), rz; mode 1 also sets p = z and S_RZ, mode 0 S_BETA.
+    // restricted = true: level-1 r and the first sweep are already done (by
+    // k_mg_update_restrict)
+    void mg_apply(const float* r, float* z, float* p, int mode, bool restricted = false) {
         MgLevel* L = mg.L;
         const int lv = mg.levels;
         const float om = mg.omega;
-        MPS_COUNT_LAUNCH k_mg_restrict_fine<float><<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d, mg, r);
-        if (lv == 1) {
-            MPS_COUNT_LAUNCH k_mg_bottom<<<1, 1024, 0, st>>>(d.scal, L[1], L[1], 0, mg.ainv);
-        } else {
-            for (int l = 1; l + 1 < lv; ++l)
-                MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
-            MPS_COUNT_LAUNCH k_mg_bottom<<<1, 1024, 0, st>>>(d.scal, L[lv - 1], L[lv], 1, mg.ainv);
-            for (int l = lv - 1; l >= 1; --l)
-                MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
-        }
+        if (!restricted)
+            MPS_COUNT_LAUNCH k_mg_restrict_fine<float><<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d, mg, r);
+        for (int l = 1; l < lv; ++l)
+            MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+        MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
+        for (int l = lv - 1; l >= 1; --l)
+            MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
         MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7);
     }
 
@@ -603,12 +602,13 @@ struct Solver {
                 MPS_COUNT_LAUNCH k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
                 timer.mark(PH_VEC, st);
                 const bool use_mg = std::is_same<TV, float>::value && mg_ready;
-                MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1,
-                                                                                  use_mg ? 0 : 1);
+                if (!use_mg)
+                    MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1, 1);
                 if constexpr (std::is_same<TV, float>::value) {
                     if (use_mg) {
+                        MPS_COUNT_LAUNCH k_mg_update_restrict<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, mg, x, r, p, q, 1);
                         timer.mark(PH_PRECOND, st);
-                        mg_apply(r, z, p, 0);
+                        mg_apply(r, z, p, 0, true);
                         timer.mark(PH_VEC, st);
                     }
                 }
