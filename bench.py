@@ -114,9 +114,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def build_scene(l0, seed=4):
+def build_scene(l0, seed=4, workload="bucket"):
     from simulation_project_gb300 import scenes
+    if workload == "mixer":
+        # four rotating cylinders (radii 0.10-0.18 m, 20-45 rpm, seeded), 40 % fill, 512 drag spheres
+        return scenes.mixer(l0=l0, dt=5e-5, seed=6 + seed - 4)
     return scenes.rotating_bucket(l0=l0, dt=5e-5, seed=seed, n_drag=64, drag_seed=3)
+
+
+WORKLOADS = {
+    "bucket": "rotating bucket r=0.15 L=0.3, 35% fill, l0={l0}, 30 rpm, 4096 wall + 64 drag-sphere STL models, "
+              "dt=5e-5, PPE rtol 1e-8",
+    "mixer": "4-cylinder mixer (r 0.10-0.18 m, L=0.3, 20-45 rpm, seed 6), 40% fill, l0={l0}, 512 drag spheres, "
+             "dt=5e-5, PPE rtol 1e-8",
+}
 
 
 def barrier():
@@ -194,7 +205,7 @@ def run_gpu(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     lib.call("mps_set_device", local)
-    scene = build_scene(args.l0, seed=4 + rank)
+    scene = build_scene(args.l0, seed=4 + rank, workload=args.workload)
     n = scene.n
     log = []
     peak_gbs, peak_kind = load_peaks()
@@ -271,8 +282,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic (seeded jittered lattice in a triangulated rotating cylinder)",
-        "config": {"workload": f"rotating bucket r=0.15 L=0.3, 35% fill, l0={args.l0}, 30 rpm, 4096 wall + "
-                               "64 drag-sphere STL models, dt=5e-5, PPE rtol 1e-8",
+        "config": {"workload": WORKLOADS[args.workload].format(l0=args.l0),
                    "particles": n, "triangles": scene.t, "cells": scene.box.cell_num,
                    "l2": "inputs larger than L2 (neighbour rows ~8 B x nnz per SpMV)",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
@@ -347,12 +357,40 @@ def sort_bench(n, cells, peak_gbs, reps=10):
             "frac": round(gbs / peak_gbs, 3), "sorted_correctly": ok}
 
 
+def _compare_states(sa, sb, scene):
+    """Errors of state sb against state sa over the particle ids both still hold."""
+    common, ia, ib = np.intersect1d(sa["id"], sb["id"], return_indices=True)
+    pa, pb = sa["press"][ia], sb["press"][ib]
+    va, vb = sa["vel"][ia], sb["vel"][ib]
+    na, nb = sa["pnd"][ia], sb["pnd"][ib]
+    ke_a, ke_b = 0.5 * np.sum(va * va), 0.5 * np.sum(vb * vb)
+    l0 = scene.param.InitialParticleDistance
+    q = np.array([50, 90, 99])
+    return {"particles_compared": int(len(common)),
+            "pressure_max_rel": float(np.abs(pb - pa).max() / np.abs(pa).max()),
+            "pressure_rms_rel": float(np.sqrt(np.mean((pb - pa) ** 2)) / np.sqrt(np.mean(pa ** 2))),
+            "pressure_mean_rel": float(abs(pb.mean() - pa.mean()) / np.abs(pa).mean()),
+            "pressure_percentiles_rel": [float(x) for x in
+                                         np.abs(np.percentile(pb, q) - np.percentile(pa, q)) / np.abs(pa).max()],
+            "pnd_max_rel": float(np.abs(nb - na).max() / scene.n0_pnd),
+            "velocity_max_rel": float(np.abs(vb - va).max() / np.abs(va).max()),
+            "kinetic_energy_rel": float(abs(ke_b - ke_a) / ke_a),
+            "position_max_over_l0": float(np.abs(sb["pos"][ib] - sa["pos"][ia]).max() / l0)}
+
+
 def accuracy_vs_fp64(scene, params, args, steps=10):
     """The metric's solver (FP32 operators, FP64 refinement, multilevel, learned guess)
-    against the FP64 solver on the same scene after `steps` steps, over the particle
-    ids both still hold."""
+    against the FP64 solver on the same scene after `steps` steps, and a control:
+    the FP64 solver against itself started from positions moved by 5e-6 l0, about the
+    resolution of an FP32 coordinate in this box (the divergence that perturbations of
+    FP32 size reach in a free-surface particle flow)."""
+    import copy
     from simulation_project_gb300.solver import Solver
+    pert = copy.copy(scene)
+    rng = np.random.default_rng(11)
+    pert.pos = scene.pos + 5e-6 * scene.param.InitialParticleDistance * rng.standard_normal(scene.pos.shape)
     a = Solver(scene, precision="fp64")
+    c = Solver(pert, precision="fp64")
     b = Solver(scene, precision="fp32_ir", preconditioner=args.precond,
                learned=args.learned_mode if params is not None else 0)
     if params is not None:
@@ -360,22 +398,14 @@ def accuracy_vs_fp64(scene, params, args, steps=10):
     for i in range(steps):
         a.step(i)
         b.step(i)
-    sa, sb = a.state(), b.state()
-    a.close()
-    b.close()
-    common, ia, ib = np.intersect1d(sa["id"], sb["id"], return_indices=True)
-    pa, pb = sa["press"][ia], sb["press"][ib]
-    va, vb = sa["vel"][ia], sb["vel"][ib]
-    na, nb = sa["pnd"][ia], sb["pnd"][ib]
-    ke_a, ke_b = 0.5 * np.sum(va * va), 0.5 * np.sum(vb * vb)
-    l0 = scene.param.InitialParticleDistance
-    return {"steps": steps, "particles_compared": int(len(common)),
-            "pressure_max_rel": float(np.abs(pb - pa).max() / np.abs(pa).max()),
-            "pressure_rms_rel": float(np.sqrt(np.mean((pb - pa) ** 2)) / np.sqrt(np.mean(pa ** 2))),
-            "pnd_max_rel": float(np.abs(nb - na).max() / scene.n0_pnd),
-            "velocity_max_rel": float(np.abs(vb - va).max() / np.abs(va).max()),
-            "kinetic_energy_rel": float(abs(ke_b - ke_a) / ke_a),
-            "position_max_over_l0": float(np.abs(sb["pos"][ib] - sa["pos"][ia]).max() / l0)}
+        c.step(i)
+    sa, sb, sc_ = a.state(), b.state(), c.state()
+    for x in (a, b, c):
+        x.close()
+    out = {"steps": steps, "reference": "FP64 solver on the GPU (matches the FP64 oracle to 1e-6 on the parity cases)"}
+    out.update(_compare_states(sa, sb, scene))
+    out["control_fp64_perturbed_5e-6_l0"] = _compare_states(sa, sc_, scene)
+    return out
 
 
 def run_profile_case(args):
@@ -384,7 +414,7 @@ def run_profile_case(args):
     from simulation_project_gb300 import lib
     from simulation_project_gb300.solver import Solver
     lib.load()
-    scene = build_scene(args.l0)
+    scene = build_scene(args.l0, workload=args.workload)
     params = None
     if args.profile_learned:
         params, _ = train_learned(Solver, scene, args.train_steps, [])
@@ -398,6 +428,20 @@ def run_profile_case(args):
                       "phases": {k: st[-1][k] for k in st[-1] if k.startswith("ms_")},
                       "spmv_launches": st[-1]["spmv_launches"], "nnz": st[-1]["nnz"],
                       "cg_iterations": st[-1]["cg_iterations"], "mg_levels": st[-1]["mg_levels"]}))
+    return 0
+
+
+def run_accuracy_only(args):
+    """The FP32-IR learned solver against the FP64 solver after --accuracy-steps steps."""
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.solver import Solver
+    lib.load()
+    scene = build_scene(args.l0, workload=args.workload)
+    params, info = (None, {}) if args.no_learned else train_learned(Solver, scene, args.train_steps, [])
+    t0 = time.perf_counter()
+    acc = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
+    print(json.dumps({"accuracy_vs_fp64": acc, "workload": WORKLOADS[args.workload].format(l0=args.l0),
+                      "particles": scene.n, "learned": params is not None, "seconds": time.perf_counter() - t0}))
     return 0
 
 
@@ -513,6 +557,8 @@ def main():
     ap.add_argument("--learned-mode", type=int, default=1, help="bit 0 initial guess, bit 1 diagonal scaling")
     ap.add_argument("--precond", type=int, default=1, help="0 Jacobi, 1 multilevel (FP32 inner solve)")
     ap.add_argument("--accuracy-steps", type=int, default=10, help="steps of the FP32-IR vs FP64 comparison")
+    ap.add_argument("--accuracy-only", action="store_true", help="only the FP32-IR vs FP64 comparison")
+    ap.add_argument("--workload", default="bucket", choices=sorted(WORKLOADS), help="bucket (default) or mixer")
     ap.add_argument("--profile-case", action="store_true", help="only the solver steps (for ncu captures)")
     ap.add_argument("--fp64", action="store_true", help="with --profile-case: the plain FP64 solver")
     ap.add_argument("--profile-learned", action="store_true", help="with --profile-case: train, then the learned solver")
@@ -521,6 +567,8 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     if args.profile_case:
         return run_profile_case(args)
+    if args.accuracy_only:
+        return run_accuracy_only(args)
     if args.impl == "reference":
         if rank != 0:
             return 0

@@ -137,6 +137,45 @@ CCTStatusType mps_solver_learned_samples(MpsSolver* s, float* features, float* t
 /* 1: compute features and targets at every PPE solve (for mps_solver_learned_samples) */
 CCTStatusType mps_solver_collect(MpsSolver* s, int on);
 
+/* ---- reserved names of the reference and the precision / learned-part controls ----
+ *
+ * The reference declares CCellSet::CalculatePressureCG and CalculatePressureNJPCG
+ * (solver/MPS_SOLVER_WITH_ROTATION/PMMultiGPU/Source/CGPUCellSet.h:224-225) but never
+ * defines them.  Here they solve the pressure Poisson equation for the solver's current
+ * particle state: topology, wall distance, PND and PPE assembly at the current positions,
+ * then the solve from the previous pressure to cg_rtol (positions and velocities are
+ * unchanged, the state is re-sorted).  CG: Jacobi preconditioner, no network.  NJPCG:
+ * the multilevel preconditioner (FP32_IR) and the learned initial guess when one is
+ * installed.  The prototype CalcPoisson of the same tree's DeviceProcess.h:50 (AoS
+ * CParticle arrays of an older solver variant, undefined matrix arguments) is not
+ * provided. */
+CCTStatusType CalculatePressureCG(MpsSolver* s, MpsStepStats* stats);
+CCTStatusType CalculatePressureNJPCG(MpsSolver* s, MpsStepStats* stats);
+/* switches between MPS_PREC_FP64 and MPS_PREC_FP32_IR for the following steps */
+CCTStatusType mps_set_precision(MpsSolver* s, int precision);
+
+typedef struct MpsLearnedInfo {
+    int samples;            /* (state, converged pressure) pairs kept */
+    int val_samples;        /* of which held out for validation (10 %) */
+    int adam_steps;
+    int batch;
+    float val_loss_before;  /* validation loss of the initial network */
+    float val_loss_after;
+    double collect_ms, train_ms;
+} MpsLearnedInfo;
+/* Runs `steps` steps of the solver itself (step indices first_step ...; the simulation
+ * advances as usual and the PPE is solved without the network), keeps up to
+ * max_samples (<= 0: 400,000) randomly chosen (features, converged pressure) pairs of
+ * interior particles, trains the network on the GPU (Adam, `epochs` passes of `batch`
+ * rows, learning rate halved per pass, 10 % validation) and installs it with the
+ * learned initial guess enabled (options.learned |= 1). */
+CCTStatusType mps_learned_train(MpsSolver* s, int first_step, int steps, int max_samples, int epochs, int batch,
+                                float lr, unsigned long long seed, MpsLearnedInfo* info);
+/* Network outputs (pressure increment in units of the step's pressure scale, log
+ * diagonal scale; host array of 2 n floats, may be NULL) for the features of the last
+ * step; requires an installed network and a last step that computed features. */
+CCTStatusType mps_learned_infer(MpsSolver* s, float* out, int* n);
+
 #ifdef __cplusplus
 }
 #endif

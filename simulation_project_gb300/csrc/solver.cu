@@ -12,9 +12,11 @@
 // particle count after each compaction and the CG convergence word every
 // `check_every` iterations.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <random>
 #include <type_traits>
 #include <vector>
 
@@ -110,12 +112,14 @@ struct Solver {
     // learned parameters (optional)
     bool learned_ready = false;
     bool collect = false;
+    bool feat_valid = false;   // d.feat holds the features of the last step
     MpsMlp* mlp = nullptr;
     // multilevel preconditioner
     Mg mg{};
     int mg_grid_levels = 0;    // levels with a grid (1 .. mg_grid_levels)
     bool mg_on = false;        // enabled and supported by the grid
     bool mg_ready = false;     // set up for the current step
+    bool mg_init_done = false; // level buffers allocated
     unsigned* mg_flag = nullptr;
     unsigned* mg_counts = nullptr;
     unsigned* h_counts = nullptr;
@@ -171,7 +175,7 @@ struct Solver {
         timer.on = opt.profile != 0;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CCT_CUDAERR;
         const size_t N = nmax;
-        const size_t wsz = fp64() ? sizeof(double) : sizeof(float);
+        const size_t wsz = sizeof(double);   // room for FP64 rows: the precision can be switched
         cudaError_t e = cudaSuccess;
         e = e ? e : mk(&d.pos, N); e = e ? e : mk(&d.vel, N); e = e ? e : mk(&d.pos2, N); e = e ? e : mk(&d.vel2, N);
         e = e ? e : mk(&d.press, N); e = e ? e : mk(&d.press2, N); e = e ? e : mk(&d.visc, N); e = e ? e : mk(&d.visc2, N);
@@ -325,6 +329,8 @@ struct Solver {
     // level grids halve (rounding up) until one cell; cell coordinates are packed
     // in 10 bits, so every grid dimension must be below 1024
     CCTStatusType mg_init() {
+        if (mg_init_done) return CCT_NOERR;
+        mg_init_done = true;
         const CGridBox& b = d.box;
         if (b.m_GridSize.x >= 1024 || b.m_GridSize.y >= 1024 || b.m_GridSize.z >= 1024) return CCT_NOERR;
         int gx = b.m_GridSize.x, gy = b.m_GridSize.y, gz = b.m_GridSize.z;
@@ -357,7 +363,12 @@ struct Solver {
     // setup: needs interior flags, diagonals and the FP32 neighbour rows)
     CCTStatusType mg_setup() {
         mg_ready = false;
-        if (!mg_on || d.n <= 0) return CCT_NOERR;
+        if (opt.preconditioner != MPS_PRECOND_MULTILEVEL && !mg_init_done) return CCT_NOERR;
+        if (opt.preconditioner == MPS_PRECOND_MULTILEVEL && !mg_init_done) {
+            const CCTStatusType rc = mg_init();
+            if (rc != CCT_NOERR) return rc;
+        }
+        if (!mg_on || opt.preconditioner != MPS_PRECOND_MULTILEVEL || d.n <= 0) return CCT_NOERR;
         MgLevel* L = mg.L;
         MPS_COUNT_LAUNCH k_mg_flags1<<<blocks_for(d.cells), kBlock, 0, st>>>(d, mg_flag);
         for (int l = 1; l <= mg_grid_levels; ++l) {
@@ -478,29 +489,35 @@ struct Solver {
     }
 
     template <class T>
-    CCTStatusType run_step(int step, MpsStepStats* out) {
+    // One step; pressure_only: only topology, walls, PND and the PPE solve at the
+    // current positions (no predictor, no correction, walls do not move).
+    CCTStatusType run_step(int step, MpsStepStats* out, bool pressure_only = false) {
         MpsStepStats S{};
         spmv_launches = 0;
+        feat_valid = false;
         timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
         cudaMemsetAsync(d.istat, 0, sizeof(int), st);
         CCTStatusType rc;
+        if (!pressure_only) {
+            if ((rc = compact())) return rc;
+            if ((rc = grid())) return rc;
+            timer.mark(PH_WALLS, st);
+            if (d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
+            walls_distance<T>();
+            if (d.drag_n > 0 && d.tri_n > 0) MPS_COUNT_LAUNCH k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            else cudaMemsetAsync(d.dragv, 0, sizeof(double) * 3 * d.n, st);
+            timer.mark(PH_PRED, st);
+            const int nb_grid = std::max(1, std::min(d.cells, d.n));
+            MPS_COUNT_LAUNCH k_neighbours<T, NB_PREDICT><<<nb_grid, kNbThreads, 0, st>>>(d);
+            std::swap(d.pos, d.pos2);
+            std::swap(d.vel, d.vel2);
+            timer.mark(PH_GRID, st);
+        }
         if ((rc = compact())) return rc;
         if ((rc = grid())) return rc;
         timer.mark(PH_WALLS, st);
-        if (d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
-        walls_distance<T>();
-        if (d.drag_n > 0 && d.tri_n > 0) MPS_COUNT_LAUNCH k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
-        else cudaMemsetAsync(d.dragv, 0, sizeof(double) * 3 * d.n, st);
-        timer.mark(PH_PRED, st);
-        const int nb_grid = std::max(1, std::min(d.cells, d.n));
-        MPS_COUNT_LAUNCH k_neighbours<T, NB_PREDICT><<<nb_grid, kNbThreads, 0, st>>>(d);
-        std::swap(d.pos, d.pos2);
-        std::swap(d.vel, d.vel2);
-        timer.mark(PH_GRID, st);
-        if ((rc = compact())) return rc;
-        if ((rc = grid())) return rc;
-        timer.mark(PH_WALLS, st);
+        if (pressure_only && d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
         walls_distance<T>();
         timer.mark(PH_LIST, st);
         const int nb_cells = std::max(1, std::min(d.cells, d.n));
@@ -523,6 +540,7 @@ struct Solver {
                 MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
                 MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
                 MPS_COUNT_LAUNCH k_features<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                feat_valid = true;
                 if (use_learned) {
                     if (mlp_forward(mlp, d.n, d.feat, d.mlp_out, st)) return CCT_CUDAERR;
                     MPS_COUNT_LAUNCH k_learned_apply<<<blocks_for(d.n), kBlock, 0, st>>>(d, (opt.learned & 2) ? 1 : 0);
@@ -551,11 +569,13 @@ struct Solver {
             if (collect) MPS_COUNT_LAUNCH k_targets<<<blocks_for(d.n), kBlock, 0, st>>>(d);
         }
         timer.mark(PH_CORRECT, st);
-        MPS_COUNT_LAUNCH k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
-        std::swap(d.pos, d.pos2);
-        std::swap(d.vel, d.vel2);
+        if (!pressure_only) {
+            MPS_COUNT_LAUNCH k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            std::swap(d.pos, d.pos2);
+            std::swap(d.vel, d.vel2);
+        }
         timer.mark(PH_WALLS, st);
-        if (d.tri_n > 0 && walls_move) {
+        if (!pressure_only && d.tri_n > 0 && walls_move) {
             MPS_COUNT_LAUNCH k_walls_move<<<blocks_for(d.tri_n), kBlock, 0, st>>>(d, step);
             bins_dirty = 1;
         }
@@ -718,8 +738,8 @@ struct Solver {
         return cuda_status(e);
     }
 
-    CCTStatusType step(int stepi, MpsStepStats* out) {
-        return fp64() ? run_step<double>(stepi, out) : run_step<float>(stepi, out);
+    CCTStatusType step(int stepi, MpsStepStats* out, bool pressure_only = false) {
+        return fp64() ? run_step<double>(stepi, out, pressure_only) : run_step<float>(stepi, out, pressure_only);
     }
 };
 
@@ -920,6 +940,151 @@ CCTStatusType mps_solver_learned_samples(MpsSolver* s, float* features, float* t
     cudaError_t e = cudaStreamSynchronize(s->s.st);
     if (!e && features) e = cudaMemcpy(features, d.feat, sizeof(float) * 12 * d.n, cudaMemcpyDeviceToHost);
     if (!e && targets) e = cudaMemcpy(targets, d.targets, sizeof(float) * 2 * d.n, cudaMemcpyDeviceToHost);
+    return mps::cuda_status(e);
+}
+
+// ---------------------------------------------------------------------------
+// entry points under the reference's reserved names (S/CGPUCellSet.h:224-225)
+// and the precision / learned-part controls
+// ---------------------------------------------------------------------------
+static CCTStatusType pressure_solve(MpsSolver* s, MpsStepStats* stats, int precond, int learned) {
+    if (!s) return CCT_PARAMERR;
+    Solver& v = s->s;
+    if (v.opt.pressure_mode != MPS_PRESSURE_PPE) return CCT_PARAMERR;
+    const int p0 = v.opt.preconditioner, l0 = v.opt.learned;
+    v.opt.preconditioner = precond;
+    v.opt.learned = learned;
+    const CCTStatusType rc = v.step(0, stats, true);
+    v.opt.preconditioner = p0;
+    v.opt.learned = l0;
+    return rc;
+}
+
+CCTStatusType CalculatePressureCG(MpsSolver* s, MpsStepStats* stats) {
+    return pressure_solve(s, stats, MPS_PRECOND_JACOBI, 0);
+}
+
+CCTStatusType CalculatePressureNJPCG(MpsSolver* s, MpsStepStats* stats) {
+    if (!s) return CCT_PARAMERR;
+    const Solver& v = s->s;
+    return pressure_solve(s, stats, MPS_PRECOND_MULTILEVEL, v.learned_ready ? (v.opt.learned ? v.opt.learned : 1) : 0);
+}
+
+CCTStatusType mps_set_precision(MpsSolver* s, int precision) {
+    if (!s || (precision != MPS_PREC_FP64 && precision != MPS_PREC_FP32_IR)) return CCT_PARAMERR;
+    s->s.opt.precision = precision;
+    return CCT_NOERR;
+}
+
+CCTStatusType mps_learned_train(MpsSolver* s, int first_step, int steps, int max_samples, int epochs, int batch,
+                                float lr, unsigned long long seed, MpsLearnedInfo* info) {
+    if (!s || steps <= 0 || epochs <= 0 || batch <= 0 || !(lr > 0.f)) return CCT_PARAMERR;
+    Solver& v = s->s;
+    if (v.opt.pressure_mode != MPS_PRESSURE_PPE) return CCT_PARAMERR;
+    if (max_samples <= 0) max_samples = 400000;
+    const auto t0 = std::chrono::steady_clock::now();
+    std::mt19937_64 rng(seed);
+    const int per_step = std::max(1, max_samples / steps);
+    std::vector<float> F, T, f, t;
+    std::vector<int> cand;
+    const int learned0 = v.opt.learned;
+    v.opt.learned = 0;
+    v.collect = true;
+    CCTStatusType rc = CCT_NOERR;
+    for (int k = 0; k < steps && rc == CCT_NOERR; ++k) {
+        MpsStepStats st;
+        rc = v.step(first_step + k, &st);
+        if (rc) break;
+        const int n = v.d.n;
+        f.resize(12 * (size_t)n);
+        t.resize(2 * (size_t)n);
+        cudaError_t e = cudaMemcpy(f.data(), v.d.feat, sizeof(float) * 12 * n, cudaMemcpyDeviceToHost);
+        if (!e) e = cudaMemcpy(t.data(), v.d.targets, sizeof(float) * 2 * n, cudaMemcpyDeviceToHost);
+        if (e) { rc = mps::cuda_status(e); break; }
+        cand.clear();
+        for (int r = 0; r < n; ++r)
+            if (std::isfinite(t[2 * (size_t)r]) && std::isfinite(t[2 * (size_t)r + 1])) cand.push_back(r);
+        std::shuffle(cand.begin(), cand.end(), rng);
+        if ((int)cand.size() > per_step) cand.resize(per_step);
+        for (int r : cand) {
+            F.insert(F.end(), f.begin() + 12 * (size_t)r, f.begin() + 12 * (size_t)r + 12);
+            T.insert(T.end(), t.begin() + 2 * (size_t)r, t.begin() + 2 * (size_t)r + 2);
+        }
+    }
+    v.collect = false;
+    v.opt.learned = learned0;
+    if (rc) return rc;
+    const auto t1 = std::chrono::steady_clock::now();
+    const int S = (int)(T.size() / 2);
+    if (S < 2 * batch) return CCT_PARAMERR;
+    std::vector<int> idx(S);
+    for (int i = 0; i < S; ++i) idx[i] = i;
+    std::shuffle(idx.begin(), idx.end(), rng);
+    const int n_val = std::max(1, S / 10);
+    std::vector<float> Xv(12 * (size_t)n_val), Tv(2 * (size_t)n_val), Xb(12 * (size_t)batch), Tb(2 * (size_t)batch);
+    for (int i = 0; i < n_val; ++i) {
+        std::copy_n(F.begin() + 12 * (size_t)idx[i], 12, Xv.begin() + 12 * (size_t)i);
+        std::copy_n(T.begin() + 2 * (size_t)idx[i], 2, Tv.begin() + 2 * (size_t)i);
+    }
+    float *dXv = nullptr, *dTv = nullptr, *dXb = nullptr, *dTb = nullptr, *dg = nullptr;
+    MpsMlp* m = nullptr;
+    cudaError_t e = cudaMalloc(&dXv, sizeof(float) * Xv.size());
+    if (!e) e = cudaMalloc(&dTv, sizeof(float) * Tv.size());
+    if (!e) e = cudaMalloc(&dXb, sizeof(float) * Xb.size());
+    if (!e) e = cudaMalloc(&dTb, sizeof(float) * Tb.size());
+    if (!e) e = cudaMalloc(&dg, sizeof(float) * MPS_MLP_PARAMS);
+    if (!e) e = cudaMemcpy(dXv, Xv.data(), sizeof(float) * Xv.size(), cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(dTv, Tv.data(), sizeof(float) * Tv.size(), cudaMemcpyHostToDevice);
+    if (e) rc = CCT_MEMERR;
+    if (!rc) rc = mps_mlp_create(std::max(batch, n_val), seed, &m);
+    float loss0 = 0.f, loss1 = 0.f;
+    int adam = 0;
+    if (!rc) rc = mps_mlp_loss_grad(m, n_val, dXv, dTv, 0.25f, dg, &loss0, nullptr);
+    std::vector<int> tr(idx.begin() + n_val, idx.end());
+    for (int ep = 0; ep < epochs && !rc; ++ep) {
+        std::shuffle(tr.begin(), tr.end(), rng);
+        const float lr_ep = lr * std::pow(0.5f, (float)ep);
+        for (size_t b0 = 0; b0 + batch <= tr.size() && !rc; b0 += batch) {
+            for (int i = 0; i < batch; ++i) {
+                std::copy_n(F.begin() + 12 * (size_t)tr[b0 + i], 12, Xb.begin() + 12 * (size_t)i);
+                std::copy_n(T.begin() + 2 * (size_t)tr[b0 + i], 2, Tb.begin() + 2 * (size_t)i);
+            }
+            e = cudaMemcpy(dXb, Xb.data(), sizeof(float) * Xb.size(), cudaMemcpyHostToDevice);
+            if (!e) e = cudaMemcpy(dTb, Tb.data(), sizeof(float) * Tb.size(), cudaMemcpyHostToDevice);
+            if (e) { rc = CCT_CUDAERR; break; }
+            rc = mps_mlp_train_step(m, batch, dXb, dTb, 0.25f, lr_ep, nullptr, nullptr);
+            ++adam;
+        }
+    }
+    if (!rc) rc = mps_mlp_loss_grad(m, n_val, dXv, dTv, 0.25f, dg, &loss1, nullptr);
+    std::vector<float> params(MPS_MLP_PARAMS);
+    if (!rc) rc = mps_mlp_get_params(m, params.data());
+    if (!rc) rc = mps_solver_set_learned(s, params.data(), MPS_MLP_PARAMS);
+    if (!rc) v.opt.learned |= 1;
+    if (m) mps_mlp_destroy(m);
+    cudaFree(dXv); cudaFree(dTv); cudaFree(dXb); cudaFree(dTb); cudaFree(dg);
+    if (info) {
+        const auto t2 = std::chrono::steady_clock::now();
+        info->samples = S;
+        info->val_samples = n_val;
+        info->adam_steps = adam;
+        info->batch = batch;
+        info->val_loss_before = loss0;
+        info->val_loss_after = loss1;
+        info->collect_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        info->train_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    }
+    return rc;
+}
+
+CCTStatusType mps_learned_infer(MpsSolver* s, float* host_out, int* n) {
+    if (!s || !n) return CCT_PARAMERR;
+    Solver& v = s->s;
+    if (!v.learned_ready || !v.mlp || !v.feat_valid) return CCT_PARAMERR;
+    *n = v.d.n;
+    if (mps::mlp_forward(v.mlp, v.d.n, v.d.feat, v.d.mlp_out, v.st)) return CCT_CUDAERR;
+    cudaError_t e = cudaStreamSynchronize(v.st);
+    if (!e && host_out) e = cudaMemcpy(host_out, v.d.mlp_out, sizeof(float) * 2 * v.d.n, cudaMemcpyDeviceToHost);
     return mps::cuda_status(e);
 }
 

@@ -41,6 +41,12 @@ class MpsStepStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class MpsLearnedInfo(C.Structure):
+    _fields_ = [("samples", C.c_int), ("val_samples", C.c_int), ("adam_steps", C.c_int), ("batch", C.c_int),
+                ("val_loss_before", C.c_float), ("val_loss_after", C.c_float), ("collect_ms", C.c_double),
+                ("train_ms", C.c_double)]
+
+
 P = C.c_void_p
 _SIGS = {
     "mps_solver_default_options": (None, [C.POINTER(MpsSolverOptions)]),
@@ -61,6 +67,12 @@ _SIGS = {
     "mps_solver_download_state": (C.c_int, [P, P, P, P]),
     "mps_solver_set_learned": (C.c_int, [P, P, C.c_int]),
     "mps_solver_learned_samples": (C.c_int, [P, P, P, C.POINTER(C.c_int)]),
+    "CalculatePressureCG": (C.c_int, [P, C.POINTER(MpsStepStats)]),
+    "CalculatePressureNJPCG": (C.c_int, [P, C.POINTER(MpsStepStats)]),
+    "mps_set_precision": (C.c_int, [P, C.c_int]),
+    "mps_learned_train": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong,
+                                    C.POINTER(MpsLearnedInfo)]),
+    "mps_learned_infer": (C.c_int, [P, P, C.POINTER(C.c_int)]),
     "mps_solver_collect": (C.c_int, [P, C.c_int]),
 }
 _bound = False
@@ -173,6 +185,29 @@ class Solver:
         rel = C.c_double()
         _check(_lib().mps_solver_debug_residual(self.h, int(variant), _p(r), C.byref(rel)), "mps_solver_debug_residual")
         return r[:n], rel.value
+
+    def pressure(self, njp: bool = False) -> dict:
+        """PPE solve at the current state (CalculatePressureNJPCG if njp, else CalculatePressureCG)."""
+        st = MpsStepStats()
+        f = _lib().CalculatePressureNJPCG if njp else _lib().CalculatePressureCG
+        _check(f(self.h, C.byref(st)), "CalculatePressure" + ("NJPCG" if njp else "CG"))
+        return st.as_dict()
+
+    def set_precision(self, precision: str):
+        _check(_lib().mps_set_precision(self.h, PREC[precision]), "mps_set_precision")
+
+    def learned_train(self, first_step, steps, max_samples=400_000, epochs=4, batch=8192, lr=2e-3, seed=1) -> dict:
+        """mps_learned_train: collect from this solver's own next `steps` steps, train, install."""
+        info = MpsLearnedInfo()
+        _check(_lib().mps_learned_train(self.h, int(first_step), int(steps), int(max_samples), int(epochs), int(batch),
+                                        float(lr), int(seed), C.byref(info)), "mps_learned_train")
+        return {k: getattr(info, k) for k, _ in info._fields_}
+
+    def learned_infer(self) -> np.ndarray:
+        n = C.c_int()
+        out = np.zeros((max(self.scene.n, 1), 2), np.float32)
+        _check(_lib().mps_learned_infer(self.h, _p(out), C.byref(n)), "mps_learned_infer")
+        return out[:n.value]
 
     def triangles(self) -> np.ndarray:
         v = np.zeros((self.scene.t, 9))
