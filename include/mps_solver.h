@@ -64,6 +64,8 @@ typedef struct MpsSolverOptions {
     int profile;            /* 1: time every phase with CUDA events on the solver stream */
     int preconditioner;     /* MPS_PRECOND_* (FP32_IR) */
     double mg_omega;        /* Jacobi weight of the multilevel smoothing sweeps */
+    int compress_rows;      /* 1: 16-bit column offsets for the FP32 SpMV where a 32-row
+                               slice spans <= 65535 columns (same results, fewer bytes) */
 } MpsSolverOptions;
 
 typedef struct MpsStepStats {

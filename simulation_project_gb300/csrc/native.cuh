@@ -10,6 +10,9 @@
 //   nbr, nbrw       int / T [ceil(n/32)*32 * K]  Laplacian neighbour rows in SELL-32
 //                                                 layout: entry k of row i at
 //                                                 ((i/32)*K + k)*32 + i%32; nbr_cnt[i] entries
+//   nbr16, sbase    u16 [same] / int [slices]    the interior rows' columns as 16-bit
+//                                                 offsets from the slice's smallest column
+//                                                 (sbase -1: the slice spans > 65535)
 //   gnbr, gnbrr     int / T [n * KG]              gradient-radius rows (index, r)
 //   tri             double[9*T], tnrm double[3*T] walls; tcs[cells+1]/tids CSR bins
 // Kernels take the whole record as one __grid_constant__ parameter.
@@ -65,6 +68,9 @@ struct Dev {
     // neighbour rows
     int* nbr;
     void* nbrw;
+    unsigned short* nbr16;     // SELL-32 column offsets from the slice base (interior rows)
+    int* sbase;                // [slices] smallest column index of the slice, -1: 32-bit slice
+    int rows16;                // nbr16 / sbase are valid for the current rows
     int* nbr_cnt;
     int* gnbr;
     void* gnbrr;

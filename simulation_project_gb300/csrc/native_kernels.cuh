@@ -614,6 +614,70 @@ __global__ void k_eos(const __grid_constant__ Dev d) {
 // CG machinery: warp-per-row SpMV over the neighbour rows, vector updates with
 // fused FP64 dot products, convergence decided on the device.
 // ---------------------------------------------------------------------------
+// Column index of SELL entry e: a signed 16-bit offset from the slice's first row,
+// or the 32-bit index
+template <bool NARROW>
+__device__ __forceinline__ int sell_col(const Dev& d, size_t e, int sb) {
+    if constexpr (NARROW) return sb + (int)(short)__ldcs(d.nbr16 + e);
+    return __ldcs(d.nbr + e);
+}
+
+// Compressed columns of the interior rows, one read pass: warp per 32-row slice,
+// offsets j - 32*slice as signed 16 bits; a slice with an offset outside
+// [-32768, 32767] keeps its 32-bit columns (sbase = -1, found by a warp vote).
+__global__ void k_compress_rows(const __grid_constant__ Dev d) {
+    const int lane = threadIdx.x & 31;
+    const int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (sl >= (d.n + 31) >> 5) return;   // warp-uniform
+    const int i = sl * 32 + lane;
+    const int cnt = (i < d.n && d.inner[i]) ? d.nbr_cnt[i] : 0;
+    const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+    const size_t base = (size_t)sl * d.K * 32 + lane;
+    const int r0 = sl * 32;
+    bool fits = true;
+    for (int k = 0; k < kmax; k += 4) {
+        int j[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = k + u < cnt ? __ldcs(d.nbr + base + (size_t)(k + u) * 32) : r0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (k + u < cnt) {
+                const int off = j[u] - r0;
+                fits = fits && off >= -32768 && off <= 32767;
+                d.nbr16[base + (size_t)(k + u) * 32] = (unsigned short)(short)off;
+            }
+        }
+    }
+    const bool all = __all_sync(0xffffffffu, fits);
+    if (lane == 0) d.sbase[sl] = all ? r0 : -1;
+}
+
+// Dot of one SELL row with x (lane = row): four entries' loads in flight, evict-first
+template <bool NARROW, class TA, class TW, class TX>
+__device__ __forceinline__ TA sell_row_dot(const Dev& d, const TW* __restrict__ w, const TX* __restrict__ x,
+                                           size_t base, int cnt, int kmax, int sb) {
+    TA acc = TA(0);
+    int k = 0;
+    for (; k + 4 <= kmax; k += 4) {
+        int id[4];
+        TW wv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            id[u] = sell_col<NARROW>(d, base + (size_t)(k + u) * 32, sb);
+            wv[u] = __ldcs(w + base + (size_t)(k + u) * 32);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k + u < cnt) acc += (TA)wv[u] * (TA)x[id[u]];
+    }
+    for (; k < kmax; ++k) {
+        const int idk = sell_col<NARROW>(d, base + (size_t)k * 32, sb);
+        const TW wk = __ldcs(w + base + (size_t)k * 32);
+        if (k < cnt) acc += (TA)wk * (TA)x[idk];
+    }
+    return acc;
+}
+
 // y = A x for interior rows (y = 0 elsewhere); A = diag - coef * W.  MODE 0: plain
 // (+ dot x.y -> S_PQ, alpha = rz / pq); MODE 1: residual r = b - A x (FP64 out),
 // norms -> S_RR, S_BNORM; MODE 2: y = A x with dots x.y -> S_LS0 and x.b -> S_LS1.
@@ -643,25 +707,9 @@ __global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, con
         const int cnt = in ? d.nbr_cnt[i] : 0;
         const int kmax = __reduce_max_sync(0xffffffffu, cnt);
         const size_t base = (size_t)sl * d.K * 32 + lane;
-        TA acc = TA(0);
-        int k = 0;
-        for (; k + 4 <= kmax; k += 4) {
-            int id[4];
-            TW wv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                id[u] = __ldcs(d.nbr + base + (size_t)(k + u) * 32);
-                wv[u] = __ldcs(w + base + (size_t)(k + u) * 32);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (k + u < cnt) acc += (TA)wv[u] * (TA)x[id[u]];
-        }
-        for (; k < kmax; ++k) {
-            const int idk = __ldcs(d.nbr + base + (size_t)k * 32);
-            const TW wk = __ldcs(w + base + (size_t)k * 32);
-            if (k < cnt) acc += (TA)wk * (TA)x[idk];
-        }
+        const int sb = (sizeof(TW) == 4 && d.rows16) ? d.sbase[sl] : -1;
+        const TA acc = sb >= 0 ? sell_row_dot<true, TA>(d, w, x, base, cnt, kmax, sb)
+                               : sell_row_dot<false, TA>(d, w, x, base, cnt, kmax, sb);
         if (!row) continue;
         if (!in) {
             y[i] = TY(0);
@@ -717,6 +765,41 @@ __global__ void k_split_x(int n, const double* __restrict__ x, float* __restrict
     xl[i] = (float)(v - (double)h);
 }
 
+// double-float sum of w * (xh + xl) over one SELL row (lane = row), see k_residual_df
+template <bool NARROW>
+__device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict__ w, const float* __restrict__ xh,
+                                           const float* __restrict__ xl, size_t base, int cnt, int kmax, int sb,
+                                           float& S_out, float& C_out) {
+    float S = 0.f, C = 0.f;
+    for (int k = 0; k < kmax; k += 4) {
+        int id[4];
+        float wv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const bool a = k + u < kmax;
+            const size_t e = base + (size_t)(a ? k + u : k) * 32;
+            id[u] = sell_col<NARROW>(d, e, sb);
+            wv[u] = __ldcs(w + e);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (k + u < cnt) {
+                const float h = xh[id[u]], l = xl[id[u]];
+                const float p = __fmul_rn(wv[u], h);
+                const float pe = __fmaf_rn(wv[u], h, -p);
+                const float lo = __fmaf_rn(wv[u], l, pe);
+                const float s = __fadd_rn(S, p);
+                const float bb = __fsub_rn(s, S);
+                const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+                S = s;
+                C = __fadd_rn(C, __fadd_rn(err, lo));
+            }
+        }
+    }
+    S_out = S;
+    C_out = C;
+}
+
 // Refinement residual r = b - A x with FP32 weights, in double-float arithmetic:
 // every product w*xh is kept exactly as the pair (p, fma(w, xh, -p)), w*xl joins
 // the low word, and the row sum is a (hi, lo) float pair updated by TwoSum
@@ -741,31 +824,10 @@ __global__ void __launch_bounds__(256) k_residual_df(const __grid_constant__ Dev
         const int cnt = in ? d.nbr_cnt[i] : 0;
         const int kmax = __reduce_max_sync(0xffffffffu, cnt);
         const size_t base = (size_t)sl * d.K * 32 + lane;
-        float S = 0.f, C = 0.f;
-        for (int k = 0; k < kmax; k += 4) {
-            int id[4];
-            float wv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const bool a = k + u < kmax;
-                id[u] = a ? __ldcs(d.nbr + base + (size_t)(k + u) * 32) : 0;
-                wv[u] = a ? __ldcs(w + base + (size_t)(k + u) * 32) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                if (k + u < cnt) {
-                    const float h = xh[id[u]], l = xl[id[u]];
-                    const float p = __fmul_rn(wv[u], h);
-                    const float pe = __fmaf_rn(wv[u], h, -p);
-                    const float lo = __fmaf_rn(wv[u], l, pe);
-                    const float s = __fadd_rn(S, p);
-                    const float bb = __fsub_rn(s, S);
-                    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-                    S = s;
-                    C = __fadd_rn(C, __fadd_rn(err, lo));
-                }
-            }
-        }
+        float S, C;
+        // 32-bit columns: the residual is compute-heavy per entry, and the 16-bit
+        // form measured slower here than in the SpMV
+        df_row_sum<false>(d, w, xh, xl, base, cnt, kmax, -1, S, C);
         if (!row) continue;
         if (!in) {
             r[i] = 0.0;

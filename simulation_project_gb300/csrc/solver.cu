@@ -189,6 +189,7 @@ struct Solver {
         e = e ? e : mk(&d.tcs, 2 * (size_t)d.cells);
         const size_t N32 = (N + 31) / 32 * 32;
         e = e ? e : mk(&d.nbr, N32 * d.K); e = e ? e : mk((char**)&d.nbrw, N32 * d.K * wsz);
+        e = e ? e : mk(&d.nbr16, N32 * d.K); e = e ? e : mk(&d.sbase, N32 / 32 + 1);
         e = e ? e : mk(&d.nbr_cnt, N);
         e = e ? e : mk(&d.gnbr, N * d.KG); e = e ? e : mk((char**)&d.gnbrr, N * d.KG * wsz);
         e = e ? e : mk(&d.gcnt, N);
@@ -495,6 +496,7 @@ struct Solver {
         MpsStepStats S{};
         spmv_launches = 0;
         feat_valid = false;
+        d.rows16 = 0;
         timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
         cudaMemsetAsync(d.istat, 0, sizeof(int), st);
@@ -528,6 +530,10 @@ struct Solver {
         } else {
             MPS_COUNT_LAUNCH k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
             MPS_COUNT_LAUNCH k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
+            if (!fp64() && opt.compress_rows) {
+                MPS_COUNT_LAUNCH k_compress_rows<<<div_up((d.n + 31) / 32 * 32, 256), 256, 0, st>>>(d);
+                d.rows16 = 1;
+            }
             const bool use_learned = learned_ready && opt.learned;
             if (use_learned || collect) {
                 timer.mark(PH_LEARNED, st);
@@ -768,6 +774,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->source_relaxation = 0.05;
     o->preconditioner = MPS_PRECOND_MULTILEVEL;
     o->mg_omega = 1.0;
+    o->compress_rows = 1;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
