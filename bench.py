@@ -248,14 +248,17 @@ def run_gpu(args):
     spmv_ms = sum(s["ms_spmv"] for s in st_fast)
     spmv_n = sum(s["spmv_launches"] for s in st_fast)
     nnz = np.mean([s["nnz"] for s in st_fast])
+    nnz_wide = np.mean([s["nnz_wide"] if s["rows16"] else s["nnz"] for s in st_fast])
     interior = np.mean([s["interior"] for s in st_fast])
-    bytes_launch = 8.0 * nnz + 25.0 * interior
+    # 4 B weight + 2 B (16-bit offset) or 4 B column per entry, 25 B per interior row
+    bytes_launch = 6.0 * (nnz - nnz_wide) + 8.0 * nnz_wide + 25.0 * interior
     avg_ms = spmv_ms / max(spmv_n, 1)
     achieved = bytes_launch / (avg_ms / 1e3) / 1e9 if spmv_n else 0.0
     roofline = {"bound": "hbm", "kernel": "k_spmv<float,float,float> (PPE SpMV, FP32 rows)",
                 "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
                 "frac": round(achieved / peak_gbs, 3), "peak_kind": peak_kind,
                 "traffic": int(SPMV_DRAM_BYTES_PER_ENTRY * nnz), "traffic_source": "ncu dram bytes per entry x entries",
+                "entries": int(nnz), "entries_32bit_columns": int(nnz_wide),
                 "bytes_per_launch": int(bytes_launch), "launches": spmv_n,
                 "avg_launch_us": round(avg_ms * 1e3, 2)}
     phases = {k: round(float(np.mean([s[k] for s in st_fast])), 3) for k in

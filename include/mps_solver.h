@@ -68,6 +68,15 @@ typedef struct MpsSolverOptions {
                                slice spans <= 65535 columns (same results, fewer bytes) */
 } MpsSolverOptions;
 
+/* error_flags bits of MpsStepStats (set by kernels, read after the step) */
+#define MPS_ERR_KEY_RANGE 1u       /* a hash key fell outside [0, cells) */
+#define MPS_ERR_NEIGHBOUR_CAP 2u   /* a neighbour list overflowed its capacity */
+#define MPS_ERR_NONFINITE 4u       /* a non-finite value was produced */
+#define MPS_ERR_TRI_CAP 8u         /* a cell exceeded its triangle capacity */
+#define MPS_ERR_CG 16u             /* the CG solve did not converge */
+#define MPS_ERR_STAGE_TIMEOUT 32u  /* a bulk copy into shared memory did not complete in time
+                                      (the kernel fell back to global loads) */
+
 typedef struct MpsStepStats {
     int particles;
     int interior;           /* particles in the PPE (not free surface) */
@@ -87,6 +96,8 @@ typedef struct MpsStepStats {
     int mg_levels;          /* coarse levels of the multilevel preconditioner (0: Jacobi) */
     int mg_level1;          /* level-1 aggregates */
     double r0_relres;       /* ||b - A p0|| / ||b|| of the start (warm start or learned guess) */
+    long long nnz_wide;     /* interior entries stored with 32-bit columns (the rest: 16-bit) */
+    int rows16;             /* 1 if the FP32 SpMV used compressed columns this step */
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);

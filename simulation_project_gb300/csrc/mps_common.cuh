@@ -173,9 +173,6 @@ __device__ __forceinline__ float ref_zlap(int dim, float r, float l0) {
 
 }  // namespace mps
 
-// Error flag bits written by kernels into a device word (read by the host after a step).
-#define MPS_ERR_KEY_RANGE 1u      // a hash key fell outside [0, cells)
-#define MPS_ERR_NEIGHBOUR_CAP 2u  // a neighbour list overflowed its capacity
-#define MPS_ERR_NONFINITE 4u      // a non-finite value was produced
-#define MPS_ERR_TRI_CAP 8u        // a cell exceeded its triangle capacity
-#define MPS_ERR_CG 16u            // the CG solve did not converge
+// Error flag bits written by kernels into a device word (MPS_ERR_*, public in
+// include/mps_solver.h, read by the host after a step).
+#include "../../include/mps_solver.h"

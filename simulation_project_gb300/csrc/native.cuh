@@ -97,7 +97,7 @@ struct Dev {
 // device scalar slots
 enum {
     S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_BNORM, S_TOL, S_CONV, S_ITER, S_RZNEW, S_RNORM, S_R0NORM,
-    S_IRTOL, S_TMP0, S_TMP1, S_PSCALE, S_MAXIT, S_NNZ0, S_NNZ1, S_LS0, S_LS1, S_COUNT
+    S_IRTOL, S_TMP0, S_TMP1, S_PSCALE, S_MAXIT, S_NNZ0, S_NNZ1, S_LS0, S_LS1, S_NINT, S_COUNT
 };
 
 }  // namespace mps

@@ -23,6 +23,47 @@ enum { NB_PREDICT = 0, NB_LIST = 1 };
 
 template <class T> struct V3 { T x, y, z; };
 
+// ---- bulk (TMA) copies global -> shared, completed on an mbarrier ----
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// one arrival that also announces `bytes` of transactions
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_test_parity(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bytes (a multiple of 16) from a 16-byte-aligned global address to a 16-byte-aligned
+// shared address; completion is counted on bar
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// bounded wait on phase 0 of bar: false if it did not complete within `spins` polls
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, long long spins) {
+    for (long long k = 0; k < spins; ++k)
+        if (mbar_test_parity(bar, 0)) return true;
+    return false;
+}
+
+// a / b: IEEE division in FP64; in FP32 the fast approximate form (<= 2 ulp), which
+// the neighbour passes use for their weights (it is issued for every accepted pair)
+template <class T>
+__device__ __forceinline__ T wdiv(T a, T b) {
+    if constexpr (sizeof(T) == 4) return __fdividef(a, b);
+    return a / b;
+}
+
 // SELL-32 position of entry k of row i (row capacity K)
 __device__ __forceinline__ size_t sell_index(int i, int k, int K) {
     return ((size_t)(i >> 5) * K + k) * 32 + (i & 31);
@@ -417,7 +458,8 @@ __device__ __forceinline__ void nb_epilogue(const Dev& d, int i, T a0, T a1, T a
 // epilogues run lane-parallel.
 template <class T, int MODE>
 __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant__ Dev d) {
-    __shared__ float4 spos[kStageCap];
+    __shared__ __align__(16) float4 spos[kStageCap];
+    __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int rs[9], rl[9], rp[10];
     const int ci = blockIdx.x;
     if (ci >= *d.cell_count) return;
@@ -450,12 +492,24 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
     }
     __syncthreads();
     const int S = rp[9];
-    const bool staged = S <= kStageCap;
-    if (staged) {
-        for (int c = threadIdx.x; c < S; c += blockDim.x) {
-            int r = 0;
-            while (c >= rp[r + 1]) ++r;
-            spos[c] = d.opos[rs[r] + (c - rp[r])];
+    bool staged = S <= kStageCap;
+    if (staged && S > 0) {
+        // the 9 runs are contiguous float4 ranges: one bulk copy each (16-byte aligned
+        // addresses, sizes multiples of 16 bytes), completed on one mbarrier
+        if (threadIdx.x == 0) {
+            mbar_init(&stage_bar, 1);
+            mbar_arrive_expect_tx(&stage_bar, (unsigned)S * (unsigned)sizeof(float4));
+            for (int r = 0; r < 9; ++r)
+                if (rl[r] > 0)
+                    bulk_copy_g2s(&spos[rp[r]], d.opos + rs[r], (unsigned)rl[r] * (unsigned)sizeof(float4), &stage_bar);
+        }
+        __syncthreads();
+        if (!mbar_wait_bounded(&stage_bar, 1ll << 22)) {
+            // the copies did not land in time: flag it, wait (bounded) for the copies
+            // still in flight into this CTA's shared memory, and use global loads
+            if (threadIdx.x == 0) atomicOr(d.err, MPS_ERR_STAGE_TIMEOUT);
+            mbar_wait_bounded(&stage_bar, 1ll << 26);
+            staged = false;
         }
     }
     __syncthreads();
@@ -474,6 +528,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         const V3<T> vi = load_v<T>(d, i);
         T a0 = 0, a1 = 0, a2 = 0, a3 = 0;   // mode-specific accumulators
         int cnt = 0, gcnt = 0;
+        const size_t row0 = sell_index(i, 0, d.K);   // SELL position of the row's entry 0
         for (int r = 0; r < 9; ++r) {
             const int len = rl[r];
             for (int b = 0; b < len; b += 32) {
@@ -509,7 +564,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
                 if (acc) {
-                    const T w = re / (rr > mind ? rr : mind) - T(1);
+                    const T w = wdiv<T>(re, rr > mind ? rr : mind) - T(1);
                     if constexpr (MODE == NB_PREDICT) {
                         V3<T> vj;
                         if constexpr (sizeof(T) == 8) {
@@ -525,7 +580,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     } else {
                         const int slot = cnt + __popc(bal & lt);
                         if (slot < d.K) {
-                            const size_t e = sell_index(i, slot, d.K);
+                            const size_t e = row0 + (size_t)slot * 32;
                             d.nbr[e] = j;
                             ((T*)d.nbrw)[e] = w;
                         }
@@ -533,7 +588,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                         if (rr < reg) {
                             gacc = true;
                             const T rg = rr > mindg ? rr : mindg;
-                            const T wg = reg / rg - T(1);
+                            const T wg = wdiv<T>(reg, rg) - T(1);
                             a2 += wg;                              // PND
                         }
                     }
@@ -650,6 +705,11 @@ __global__ void k_compress_rows(const __grid_constant__ Dev d) {
     }
     const bool all = __all_sync(0xffffffffu, fits);
     if (lane == 0) d.sbase[sl] = all ? r0 : -1;
+    // interior entries kept at 32 bits (counted for the bytes-per-launch figure)
+    int wide = all ? 0 : cnt;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wide += __shfl_down_sync(0xffffffffu, wide, o);
+    if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
 }
 
 // Dot of one SELL row with x (lane = row): four entries' loads in flight, evict-first
@@ -926,18 +986,22 @@ __global__ void k_cg_p(const __grid_constant__ Dev d, TV* p, const TV* z) {
         p[i] = z[i] + beta * p[i];
 }
 
-// neighbour-entry counts: interior rows (PPE matrix) and all rows
+// neighbour-entry counts of interior rows (PPE matrix) and all rows; interior rows
 __global__ void __launch_bounds__(256) k_count_nnz(const __grid_constant__ Dev d, int slot) {
-    double a = 0.0, b = 0.0;
+    double a = 0.0, b = 0.0, m = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
         const double c = (double)d.nbr_cnt[i];
         b += c;
-        if (d.inner[i]) a += c;
+        if (d.inner[i]) {
+            a += c;
+            m += 1.0;
+        }
     }
-    double v[2] = {a, b}, out[2];
-    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+    double v[3] = {a, b, m}, out[3];
+    if (grid_reduce<3>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
         d.scal[S_NNZ0] = out[0];
         d.scal[S_NNZ1] = out[1];
+        d.scal[S_NINT] = out[2];
     }
 }
 

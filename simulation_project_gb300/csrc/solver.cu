@@ -499,7 +499,7 @@ struct Solver {
         d.rows16 = 0;
         timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
-        cudaMemsetAsync(d.istat, 0, sizeof(int), st);
+        cudaMemsetAsync(d.istat, 0, 2 * sizeof(int), st);
         CCTStatusType rc;
         if (!pressure_only) {
             if ((rc = compact())) return rc;
@@ -587,14 +587,17 @@ struct Solver {
         }
         timer.mark(PH_OTHER, st);
         cudaMemcpyAsync(h_int, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(h_int + 1, d.istat, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(h_int + 1, d.istat, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
         S.error_flags |= (unsigned)h_int[0];
         S.max_row = h_int[1];
+        S.nnz_wide = h_int[2];
+        S.rows16 = d.rows16;
         S.particles = d.n;
         if (opt.pressure_mode != MPS_PRESSURE_EXPLICIT) {
             S.nnz = (long long)h_nnz[0];
             S.pairs = (long long)h_nnz[1];
+            S.interior = (int)h_nnz[2];
         }
         if (timer.on) {
             float ms[PH_COUNT] = {0};
@@ -610,7 +613,7 @@ struct Solver {
         return CCT_NOERR;
     }
 
-    double h_nnz[2] = {0, 0};
+    double h_nnz[3] = {0, 0, 0};
     // read the device scalars
     CCTStatusType pull_scal() {
         cudaMemcpyAsync(h_scal, d.scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st);
@@ -655,6 +658,7 @@ struct Solver {
         if (pull_scal()) return CCT_CUDAERR;
         h_nnz[0] = h_scal[S_NNZ0];
         h_nnz[1] = h_scal[S_NNZ1];
+        h_nnz[2] = h_scal[S_NINT];
         const double bnorm = h_scal[S_BNORM];
         S.r0_relres = bnorm > 0 ? h_scal[S_RNORM] / bnorm : 0.0;
         const double tol = opt.cg_rtol * bnorm;
@@ -695,6 +699,7 @@ struct Solver {
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
                 h_nnz[1] = h_scal[S_NNZ1];
+                h_nnz[2] = h_scal[S_NINT];
                 S.r0_relres = h_scal[S_BNORM] > 0 ? h_scal[S_RNORM] / h_scal[S_BNORM] : 0.0;
             }
             bnorm = h_scal[S_BNORM];

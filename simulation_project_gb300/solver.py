@@ -35,7 +35,7 @@ class MpsStepStats(C.Structure):
                 ("ms_ppe_setup", C.c_float), ("ms_spmv", C.c_float), ("ms_cg_vec", C.c_float),
                 ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int),
                 ("ms_precond", C.c_float), ("mg_levels", C.c_int), ("mg_level1", C.c_int),
-                ("r0_relres", C.c_double)]
+                ("r0_relres", C.c_double), ("nnz_wide", C.c_longlong), ("rows16", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
