@@ -49,8 +49,8 @@ sys.path.insert(0, ROOT)
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # DRAM bytes per neighbour entry of one k_spmv<float,float,float,0> launch, measured
 # with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on the default
-# workload: 1.80 GB for 201.4M entries (SELL-32 padding included)
-SPMV_DRAM_BYTES_PER_ENTRY = 1.803e9 / 201.36e6
+# workload with 16-bit column offsets: 1.35 GB for 201.4M entries (padding included)
+SPMV_DRAM_BYTES_PER_ENTRY = 1.352e9 / 201.36e6
 
 
 def load_peaks():

@@ -825,12 +825,24 @@ __global__ void k_split_x(int n, const double* __restrict__ x, float* __restrict
     xl[i] = (float)(v - (double)h);
 }
 
-// double-float sum of w * (xh + xl) over one SELL row (lane = row), see k_residual_df
+// (S, C) += p + lo in double-float: TwoSum of the high words, low words added
+__device__ __forceinline__ void df_add(float& S, float& C, float p, float lo) {
+    const float s = __fadd_rn(S, p);
+    const float bb = __fsub_rn(s, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(err, lo));
+}
+
+// double-float sum of w * (xh + xl) over one SELL row (lane = row), see k_residual_df.
+// Two independent (hi, lo) accumulators (even / odd unrolled entries) so the TwoSum
+// chains overlap, merged with TwoSum at the end (a fixed order); two rather than four
+// keep the kernel at 32 registers (8 CTAs of 256 per SM).
 template <bool NARROW>
 __device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict__ w, const float* __restrict__ xh,
                                            const float* __restrict__ xl, size_t base, int cnt, int kmax, int sb,
                                            float& S_out, float& C_out) {
-    float S = 0.f, C = 0.f;
+    float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
     for (int k = 0; k < kmax; k += 4) {
         int id[4];
         float wv[4];
@@ -847,17 +859,14 @@ __device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict
                 const float h = xh[id[u]], l = xl[id[u]];
                 const float p = __fmul_rn(wv[u], h);
                 const float pe = __fmaf_rn(wv[u], h, -p);
-                const float lo = __fmaf_rn(wv[u], l, pe);
-                const float s = __fadd_rn(S, p);
-                const float bb = __fsub_rn(s, S);
-                const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-                S = s;
-                C = __fadd_rn(C, __fadd_rn(err, lo));
+                if (u & 1) df_add(S1, C1, p, __fmaf_rn(wv[u], l, pe));
+                else df_add(S0, C0, p, __fmaf_rn(wv[u], l, pe));
             }
         }
     }
-    S_out = S;
-    C_out = C;
+    df_add(S0, C0, S1, C1);
+    S_out = S0;
+    C_out = C0;
 }
 
 // Refinement residual r = b - A x with FP32 weights, in double-float arithmetic:
@@ -867,7 +876,7 @@ __device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict
 // term diag*x and the final difference are FP64, so the FP64 pipe does per-row
 // work instead of per-entry work.  Error: about 2^-44 of sum |w x| per row.
 // Norms ||r||^2 -> S_RR / S_RNORM and ||b|| -> S_BNORM as in k_spmv MODE 1.
-__global__ void __launch_bounds__(256) k_residual_df(const __grid_constant__ Dev d, const float* __restrict__ w,
+__global__ void __launch_bounds__(256, 8) k_residual_df(const __grid_constant__ Dev d, const float* __restrict__ w,
                                                      const double* __restrict__ x, double* __restrict__ r,
                                                      const double* __restrict__ b, int slot) {
     const int lane = threadIdx.x & 31;
