@@ -712,22 +712,25 @@ __global__ void k_compress_rows(const __grid_constant__ Dev d) {
     if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
 }
 
-// Dot of one SELL row with x (lane = row): four entries' loads in flight, evict-first
+// Dot of one SELL row with x (lane = row), evict-first loads.  U entries' loads are
+// in flight before their gathers: 8 for 16-bit columns (6 B per entry, so a warp
+// keeps about as many bytes in flight as with 4 entries of 8 B), 4 otherwise.
 template <bool NARROW, class TA, class TW, class TX>
 __device__ __forceinline__ TA sell_row_dot(const Dev& d, const TW* __restrict__ w, const TX* __restrict__ x,
                                            size_t base, int cnt, int kmax, int sb) {
+    constexpr int U = NARROW ? 8 : 4;
     TA acc = TA(0);
     int k = 0;
-    for (; k + 4 <= kmax; k += 4) {
-        int id[4];
-        TW wv[4];
+    for (; k + U <= kmax; k += U) {
+        int id[U];
+        TW wv[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             id[u] = sell_col<NARROW>(d, base + (size_t)(k + u) * 32, sb);
             wv[u] = __ldcs(w + base + (size_t)(k + u) * 32);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < U; ++u)
             if (k + u < cnt) acc += (TA)wv[u] * (TA)x[id[u]];
     }
     for (; k < kmax; ++k) {
@@ -747,7 +750,7 @@ __device__ __forceinline__ TA sell_row_dot(const Dev& d, const TW* __restrict__ 
 // The k loop runs to the slice's longest row, unrolled 4x so that eight line loads
 // are in flight per warp before the gathers; matrix loads are evict-first.
 template <class TW, class TX, class TY, int MODE>
-__global__ void __launch_bounds__(256) k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w,
+__global__ void __launch_bounds__(256, 8) k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w,
                                               const TX* __restrict__ x, TY* __restrict__ y, const double* __restrict__ b,
                                               int slot) {
     if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
