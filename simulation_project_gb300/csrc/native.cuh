@@ -56,6 +56,8 @@ struct Dev {
     int* cell_count;
     // walls
     double* tri;
+    float* tri32;              // FP32 copy of tri (FP32 wall distance and drag)
+    unsigned char* tdrag;      // 1 for triangles of drag models
     double* tnrm;
     int* tmodel;
     CTriangleParameters* tparams;

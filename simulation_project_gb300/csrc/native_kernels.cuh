@@ -280,10 +280,20 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
     md = T(1e8);
     mdir = v3(T(0), T(0), T(0));
     mid = -1;
-    const double cs = d.box.m_CellSize;
-    const int cx = f2i(((double)p.x - (double)d.box.m_BufferedZone.m_MinBound.x) / cs);
-    const int cy = f2i(((double)p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
-    const int cz = f2i(((double)p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs);
+    int cx, cy, cz;
+    if constexpr (sizeof(T) == 4) {
+        // FP32 path: cell of the candidate triangles in FP32 (the wall influence radius
+        // is at most one cell, so the 27 cells cover it either way)
+        const float inv = (float)(1.0 / (double)d.box.m_CellSize);
+        cx = f2i((p.x - d.box.m_BufferedZone.m_MinBound.x) * inv);
+        cy = f2i((p.y - d.box.m_BufferedZone.m_MinBound.y) * inv);
+        cz = f2i((p.z - d.box.m_BufferedZone.m_MinBound.z) * inv);
+    } else {
+        const double cs = d.box.m_CellSize;
+        cx = f2i(((double)p.x - (double)d.box.m_BufferedZone.m_MinBound.x) / cs);
+        cy = f2i(((double)p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
+        cz = f2i(((double)p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs);
+    }
     for (int k = -1; k <= 1; ++k)
         for (int j = -1; j <= 1; ++j)
             for (int i = -1; i <= 1; ++i) {
@@ -294,11 +304,16 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
                 const int e = d.tcs[d.cells + m];
                 for (int l = s; l < e; ++l) {
                     const int t = d.tids[l];
-                    if (drag_only != (bool)d.tparams[d.tmodel[t]].isDrag) continue;
+                    if (drag_only != (d.tdrag[t] != 0)) continue;
                     if (t == mid) continue;
-                    const double* v = d.tri + 9 * (size_t)t;
-                    const V3<T> q = closest_on_tri<T>(p, v3<T>((T)v[0], (T)v[1], (T)v[2]), v3<T>((T)v[3], (T)v[4], (T)v[5]),
-                                                      v3<T>((T)v[6], (T)v[7], (T)v[8]));
+                    V3<T> q;
+                    if constexpr (sizeof(T) == 4) {
+                        const float* v = d.tri32 + 9 * (size_t)t;
+                        q = closest_on_tri<T>(p, v3<T>(v[0], v[1], v[2]), v3<T>(v[3], v[4], v[5]), v3<T>(v[6], v[7], v[8]));
+                    } else {
+                        const double* v = d.tri + 9 * (size_t)t;
+                        q = closest_on_tri<T>(p, v3<T>(v[0], v[1], v[2]), v3<T>(v[3], v[4], v[5]), v3<T>(v[6], v[7], v[8]));
+                    }
                     const V3<T> dv = v3(p.x - q.x, p.y - q.y, p.z - q.z);
                     const T dd = sqrt(dv.x * dv.x + dv.y * dv.y + dv.z * dv.z);
                     if (dd < md) {
@@ -809,6 +824,12 @@ __global__ void __launch_bounds__(256, 8) k_spmv(const __grid_constant__ Dev d, 
             d.scal[S_BNORM] = sqrt(out[1]);
         }
     }
+}
+
+// FP32 copy of the wall vertices (after the walls moved)
+__global__ void k_tri_to_float(const __grid_constant__ Dev d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < 9 * d.tri_n) d.tri32[k] = (float)d.tri[k];
 }
 
 // FP32 copy of the pressure (neighbour-pressure feature)

@@ -240,6 +240,8 @@ struct Solver {
         if (d.tnrm) cudaFree(d.tnrm);
         if (d.tmodel) cudaFree(d.tmodel);
         if (d.tparams) cudaFree(d.tparams);
+        if (d.tri32) cudaFree(d.tri32);
+        if (d.tdrag) cudaFree(d.tdrag);
         if (d.drag) cudaFree(d.drag);
         if (h_scal) cudaFreeHost(h_scal);
         if (h_int) cudaFreeHost(h_int);
@@ -286,8 +288,8 @@ struct Solver {
     }
 
     CCTStatusType set_triangles(int t, const double* v, const int* model, int nmodels, const CTriangleParameters* tp) {
-        if (d.tri) { cudaFree(d.tri); cudaFree(d.tnrm); cudaFree(d.tmodel); cudaFree(d.tparams); }
-        d.tri = nullptr; d.tnrm = nullptr; d.tmodel = nullptr; d.tparams = nullptr;
+        if (d.tri) { cudaFree(d.tri); cudaFree(d.tnrm); cudaFree(d.tmodel); cudaFree(d.tparams); cudaFree(d.tri32); cudaFree(d.tdrag); }
+        d.tri = nullptr; d.tnrm = nullptr; d.tmodel = nullptr; d.tparams = nullptr; d.tri32 = nullptr; d.tdrag = nullptr;
         d.tri_n = t;
         models = nmodels;
         walls_move = 0;
@@ -308,11 +310,19 @@ struct Solver {
         if (!e) e = cudaMalloc(&d.tnrm, sizeof(double) * 3 * (size_t)t);
         if (!e) e = cudaMalloc(&d.tmodel, sizeof(int) * (size_t)t);
         if (!e) e = cudaMalloc(&d.tparams, sizeof(CTriangleParameters) * std::max(nmodels, 1));
+        if (!e) e = cudaMalloc(&d.tri32, sizeof(float) * 9 * (size_t)t);
+        if (!e) e = cudaMalloc(&d.tdrag, (size_t)t);
         if (e) return CCT_MEMERR;
+        std::vector<float> v32(9 * (size_t)t);
+        std::vector<unsigned char> fl((size_t)t);
+        for (size_t k = 0; k < v32.size(); ++k) v32[k] = (float)v[k];
+        for (int k = 0; k < t; ++k) fl[k] = (model[k] >= 0 && model[k] < nmodels && tp[model[k]].isDrag) ? 1 : 0;
         e = cudaMemcpy(d.tri, v, sizeof(double) * 9 * (size_t)t, cudaMemcpyHostToDevice);
         if (!e) e = cudaMemcpy(d.tnrm, nrm.data(), sizeof(double) * 3 * (size_t)t, cudaMemcpyHostToDevice);
         if (!e) e = cudaMemcpy(d.tmodel, model, sizeof(int) * (size_t)t, cudaMemcpyHostToDevice);
         if (!e) e = cudaMemcpy(d.tparams, tp, sizeof(CTriangleParameters) * nmodels, cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(d.tri32, v32.data(), sizeof(float) * v32.size(), cudaMemcpyHostToDevice);
+        if (!e) e = cudaMemcpy(d.tdrag, fl.data(), (size_t)t, cudaMemcpyHostToDevice);
         bins_dirty = 1;
         return cuda_status(e);
     }
@@ -583,6 +593,7 @@ struct Solver {
         timer.mark(PH_WALLS, st);
         if (!pressure_only && d.tri_n > 0 && walls_move) {
             MPS_COUNT_LAUNCH k_walls_move<<<blocks_for(d.tri_n), kBlock, 0, st>>>(d, step);
+            MPS_COUNT_LAUNCH k_tri_to_float<<<blocks_for(9 * d.tri_n), kBlock, 0, st>>>(d);
             bins_dirty = 1;
         }
         timer.mark(PH_OTHER, st);
