@@ -1156,6 +1156,34 @@ __global__ void k_learned_finish(const __grid_constant__ Dev d) {
     d.press[i] = d.inner[i] ? d.pprev[i] + a * d.z[i] : 0.0;
 }
 
+// FP32 path: the same update, and the refinement residual of the new start without a
+// second residual pass: r = r0 - alpha (A dp), with r0 = b - A p_prev (FP64-accurate,
+// already in d.r) and A dp the line search's FP32 product (q32); ||r|| -> S_RR, S_RNORM
+// (S_BNORM is r0's).  The FP32 error of alpha (A dp) only perturbs the first
+// refinement pass, which is followed by a freshly computed residual.
+__global__ void __launch_bounds__(256) k_learned_finish_r(const __grid_constant__ Dev d, int slot) {
+    const double dad = d.scal[S_LS0], dr = d.scal[S_LS1];
+    const double a = (dad > 0.0 && isfinite(dr / dad)) ? dr / dad : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) d.scal[S_IRTOL] = a;
+    double rr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        if (!d.inner[i]) {
+            d.press[i] = 0.0;
+            d.r[i] = 0.0;
+            continue;
+        }
+        d.press[i] = d.pprev[i] + a * d.z[i];
+        const double ri = d.r[i] - a * (double)d.q32[i];
+        d.r[i] = ri;
+        rr += ri * ri;
+    }
+    double v[1] = {rr}, out[1];
+    if (grid_reduce<1>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        d.scal[S_RR] = out[0];
+        d.scal[S_RNORM] = sqrt(out[0]);
+    }
+}
+
 // training targets after a plain solve: (p - p_prev) / scale and the log of the
 // diagonal scale that maps the initial residual onto the error, clamped to [0.1, 10]
 __global__ void k_targets(const __grid_constant__ Dev d) {

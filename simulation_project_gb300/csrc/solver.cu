@@ -113,6 +113,7 @@ struct Solver {
     bool learned_ready = false;
     bool collect = false;
     bool feat_valid = false;   // d.feat holds the features of the last step
+    bool residual_ready = false;   // d.r / S_RNORM / S_BNORM hold the start's residual
     MpsMlp* mlp = nullptr;
     // multilevel preconditioner
     Mg mg{};
@@ -506,6 +507,7 @@ struct Solver {
         MpsStepStats S{};
         spmv_launches = 0;
         feat_valid = false;
+        residual_ready = false;
         d.rows16 = 0;
         timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
@@ -566,7 +568,12 @@ struct Solver {
                     else   // FP32 products: the line search needs no more
                         MPS_COUNT_LAUNCH k_spmv<float, float, float, 2><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.z32,
                                                                                    d.q32, d.r, 6);
-                    MPS_COUNT_LAUNCH k_learned_finish<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                    if (fp64()) {
+                        MPS_COUNT_LAUNCH k_learned_finish<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+                    } else {
+                        MPS_COUNT_LAUNCH k_learned_finish_r<<<kRedBlocks, 256, 0, st>>>(d, 7);
+                        residual_ready = true;
+                    }
                 }
                 timer.mark(PH_SETUP, st);
             }
@@ -705,7 +712,8 @@ struct Solver {
         double bnorm = 0.0;
         int outer = 0;
         for (;;) {
-            residual_df(w);
+            if (!(outer == 0 && residual_ready)) residual_df(w);
+            residual_ready = false;
             if (pull_scal()) return CCT_CUDAERR;
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
