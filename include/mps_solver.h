@@ -66,6 +66,8 @@ typedef struct MpsSolverOptions {
     double mg_omega;        /* Jacobi weight of the multilevel smoothing sweeps */
     int compress_rows;      /* 1: 16-bit column offsets for the FP32 SpMV where a 32-row
                                slice spans <= 65535 columns (same results, fewer bytes) */
+    int mg_sweeps;          /* weighted-Jacobi sweeps on level 1 before the restriction and
+                               after the prolongation (coarser levels: 1) */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */

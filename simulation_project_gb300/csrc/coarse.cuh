@@ -334,6 +334,24 @@ __global__ void k_mg_down(const double* __restrict__ scal, MgLevel lo, MgLevel h
     }
 }
 
+// one more weighted-Jacobi sweep on a level: out = in + omega D^-1 (r - A in); warp per
+// aggregate, lane per stencil slot (level 1 runs as many before the restriction as
+// after the prolongation, so the V-cycle stays symmetric)
+__global__ void k_mg_smooth(const double* __restrict__ scal, MgLevel lv, const float* __restrict__ in,
+                            float* __restrict__ out, float omega) {
+    if (scal[S_CONV] != 0.0) return;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I >= lv.n) return;   // warp-uniform
+    float t = 0.f;
+    if (lane < 27) {
+        const int J = lv.nb[(size_t)I * 27 + lane];
+        if (J >= 0) t = lv.a[(size_t)I * 27 + lane] * in[J];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[I] = in[I] + omega * lv.dinv[I] * (lv.r[I] - t);
+}
+
 // prolongation hi -> lo and the up sweep on lo: e' = e + P e_hi,
 // e2 = e' + omega D^-1 (r - A e'); warp per lo aggregate, lane per stencil slot
 __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi, float omega) {

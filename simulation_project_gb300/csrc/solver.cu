@@ -421,11 +421,21 @@ struct Solver {
         const float om = mg.omega;
         if (!restricted)
             MPS_COUNT_LAUNCH k_mg_restrict_fine<float><<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d, mg, r);
+        // additional level-1 sweeps before the restriction and after the prolongation
+        const int extra = lv > 1 ? std::max(0, opt.mg_sweeps - 1) : 0;
+        for (int k = 0; k < extra; ++k) {
+            MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e, L[1].e2, om);
+            std::swap(L[1].e, L[1].e2);
+        }
         for (int l = 1; l < lv; ++l)
             MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
         MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
         for (int l = lv - 1; l >= 1; --l)
             MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+        for (int k = 0; k < extra; ++k) {
+            MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e2, L[1].e, om);
+            std::swap(L[1].e, L[1].e2);
+        }
         MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7);
     }
 
@@ -799,6 +809,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->preconditioner = MPS_PRECOND_MULTILEVEL;
     o->mg_omega = 1.0;
     o->compress_rows = 1;
+    o->mg_sweeps = 1;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,

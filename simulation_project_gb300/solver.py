@@ -24,7 +24,7 @@ class MpsSolverOptions(C.Structure):
                 ("cg_rtol", C.c_double), ("cg_max_iter", C.c_int), ("ir_inner_rtol", C.c_double),
                 ("ir_max_outer", C.c_int), ("max_neighbours", C.c_int), ("check_every", C.c_int),
                 ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
-                ("mg_omega", C.c_double), ("compress_rows", C.c_int)]
+                ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int)]
 
 
 class MpsStepStats(C.Structure):
