@@ -199,7 +199,7 @@ __global__ void k_unpad_output(int M, const float* __restrict__ Yp, float* __res
 // activations never leave the registers.  Same rounding points as the layer-by-
 // layer path: FP32 sum + bias, SiLU in FP32, BF16 activations.
 // ---------------------------------------------------------------------------
-constexpr int kMiWarps = 8;
+constexpr int kMiWarps = 16;
 constexpr int kMiS1 = 24;    // padded row (elements) of W1^T [128][16]
 constexpr int kMiS = 136;    // padded row of W2^T, W3^T [128][128] and W4^T [8][128]
 constexpr size_t kMiSmem = sizeof(bf16) * (128 * kMiS1 + 2 * 128 * kMiS + 8 * kMiS) + sizeof(float) * (3 * H + 8);
@@ -245,7 +245,7 @@ __device__ __forceinline__ void mi_hidden(const uint32_t (&a)[8][4], const bf16*
     }
 }
 
-__global__ void __launch_bounds__(kMiWarps * 32) k_mlp_infer(int M, const float* __restrict__ X, float* __restrict__ Y,
+__global__ void __launch_bounds__(kMiWarps * 32, 1) k_mlp_infer(int M, const float* __restrict__ X, float* __restrict__ Y,
                                                             Layers L) {
     extern __shared__ __align__(16) unsigned char mi_smem[];
     bf16* w1 = reinterpret_cast<bf16*>(mi_smem);   // [128][kMiS1]

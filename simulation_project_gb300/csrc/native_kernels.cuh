@@ -1081,27 +1081,48 @@ __global__ void __launch_bounds__(256) k_pressure_scale(const __grid_constant__ 
 // sum (v_j - v_i).(x_j - x_i) w_g / r^2 * d / n0 over the PND neighbours.
 template <class T>
 __global__ void k_features(const __grid_constant__ Dev d) {
-    // FP32 arithmetic (the FP64 pipe is narrow); FP64 only for the PND deviation
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    // A warp takes 32 consecutive particles: for each, the lanes read its gradient
+    // row together (coalesced) and the sums are shuffle-reduced and parked in the
+    // particle's lane; then every lane assembles its own particle's features (FP32
+    // arithmetic, FP64 only for the PND deviation), so nothing runs on one lane alone.
+    const int lane = threadIdx.x & 31;
+    const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    const float reg = (float)d.c.re_grad, mindg = (float)d.c.mind_grad;
+    float my_psum = 0.f, my_div = 0.f;
+    for (int q = 0; q < 32 && base + q < d.n; ++q) {   // warp-uniform
+        const int iq = base + q;
+        const float4 pi = d.opos[iq], vi = d.ovel[iq];
+        const int gc = d.gcnt[iq];
+        float psum = 0.f, div = 0.f;
+        for (int k = lane; k < gc; k += 32) {
+            const size_t e = (size_t)iq * d.KG + k;
+            const int j = d.gnbr[e];
+            const float r = (float)((const T*)d.gnbrr)[e];
+            const float4 pj = d.opos[j], vj = d.ovel[j];
+            const float rg = r > mindg ? r : mindg;
+            const float wg = reg / rg - 1.f;
+            psum += d.pf32[j];
+            div += ((vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) + (vj.z - vi.z) * (pj.z - pi.z)) *
+                   wg / (rg * rg);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            psum += __shfl_xor_sync(0xffffffffu, psum, o);
+            div += __shfl_xor_sync(0xffffffffu, div, o);
+        }
+        if (lane == q) {
+            my_psum = psum;
+            my_div = div;
+        }
+    }
+    const int i = base + lane;
     if (i >= d.n) return;
+    const float psum = my_psum, div = my_div;
+    const int gc = d.gcnt[i];
+    const float4 vi = d.ovel[i];
     const float ips = (float)(1.0 / d.scal[S_PSCALE]);
     float* f = d.feat + 12 * (size_t)i;
     const float idg = 1.f / (float)d.diag[i];
-    const float4 pi = d.opos[i], vi = d.ovel[i];
-    const float reg = (float)d.c.re_grad, mindg = (float)d.c.mind_grad;
-    const int gc = d.gcnt[i];
-    float psum = 0.f, div = 0.f;
-    for (int k = 0; k < gc; ++k) {
-        const size_t e = (size_t)i * d.KG + k;
-        const int j = d.gnbr[e];
-        const float r = (float)((const T*)d.gnbrr)[e];
-        const float4 pj = d.opos[j], vj = d.ovel[j];
-        const float rg = r > mindg ? r : mindg;
-        const float wg = reg / rg - 1.f;
-        psum += d.pf32[j];
-        div += ((vj.x - vi.x) * (pj.x - pi.x) + (vj.y - vi.y) * (pj.y - pi.y) + (vj.z - vi.z) * (pj.z - pi.z)) * wg /
-               (rg * rg);
-    }
     f[0] = (float)(d.pnd[i] - d.c.n0_pnd) * (float)(10.0 / d.c.n0_pnd);
     f[1] = div * (float)(d.c.dim / d.c.n0_pnd * d.c.dt * 10.0);
     const int t = d.wid[i];
