@@ -229,18 +229,31 @@ __device__ __forceinline__ void mi_activate(float (&acc)[16][4], const float* __
     }
 }
 
-// hidden layer 128 -> 128 with weights W^T [128][kMiS] in shared memory
-__device__ __forceinline__ void mi_hidden(const uint32_t (&a)[8][4], const bf16* __restrict__ wt, int g, int c,
+// four 8x8 BF16 matrices from shared memory; lane l gives the address of row l % 8 of
+// matrix l / 8 (16-byte aligned).  With W^T stored [n][k], an 8 (n) x 8 (k) matrix is
+// exactly one register of an m16n8k16 B fragment.
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16* p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"((unsigned)__cvta_generic_to_shared(p)));
+}
+
+// hidden layer 128 -> 128 with weights W^T [128][kMiS] in shared memory; one ldmatrix
+// brings the B fragments of two n-tiles
+__device__ __forceinline__ void mi_hidden(const uint32_t (&a)[8][4], const bf16* __restrict__ wt, int lane,
                                           float (&acc)[16][4]) {
 #pragma unroll
     for (int nt = 0; nt < 16; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+    const int m = lane >> 3, rr = lane & 7;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            const bf16* row = wt + (nt * 8 + g) * kMiS + 16 * k + 2 * c;
-            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8)};
-            mma_bf16(acc[nt], a[k], b);
+        for (int np = 0; np < 8; ++np) {
+            uint32_t b[4];
+            ldsm_x4(b, wt + ((2 * np + (m >> 1)) * 8 + rr) * kMiS + 16 * k + 8 * (m & 1));
+            const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+            mma_bf16(acc[2 * np], a[k], b0);
+            mma_bf16(acc[2 * np + 1], a[k], b1);
         }
     }
 }
@@ -283,26 +296,33 @@ __global__ void __launch_bounds__(kMiWarps * 32, 1) k_mlp_infer(int M, const flo
         };
         const uint32_t a1[4] = {feat2(r0, 2 * c), feat2(r1, 2 * c), feat2(r0, 2 * c + 8), feat2(r1, 2 * c + 8)};
         float acc[16][4];
+        const int m = lane >> 3, rr = lane & 7;
 #pragma unroll
-        for (int nt = 0; nt < 16; ++nt) {
-            acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
-            const bf16* row = w1 + (nt * 8 + g) * kMiS1 + 2 * c;
-            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8)};
-            mma_bf16(acc[nt], a1, b);
+        for (int np = 0; np < 8; ++np) {
+            uint32_t b[4];
+            ldsm_x4(b, w1 + ((2 * np + (m >> 1)) * 8 + rr) * kMiS1 + 8 * (m & 1));
+            const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[2 * np][q] = acc[2 * np + 1][q] = 0.f;
+            mma_bf16(acc[2 * np], a1, b0);
+            mma_bf16(acc[2 * np + 1], a1, b1);
         }
         uint32_t a[8][4];
         mi_activate(acc, bs, c, a);
-        mi_hidden(a, w2, g, c, acc);
+        mi_hidden(a, w2, lane, acc);
         mi_activate(acc, bs + H, c, a);
-        mi_hidden(a, w3, g, c, acc);
+        mi_hidden(a, w3, lane, acc);
         mi_activate(acc, bs + 2 * H, c, a);
-        // output layer: one n-tile (columns 0..7, of which 0 and 1 are used)
+        // output layer: one n-tile (columns 0..7, of which 0 and 1 are used); one
+        // ldmatrix brings the B fragments of two k-steps
         float o[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const bf16* row = w4 + g * kMiS + 16 * k + 2 * c;
-            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(row), *reinterpret_cast<const uint32_t*>(row + 8)};
-            mma_bf16(o, a[k], b);
+        for (int kp = 0; kp < 4; ++kp) {
+            uint32_t b[4];
+            ldsm_x4(b, w4 + rr * kMiS + 16 * (2 * kp + (m >> 1)) + 8 * (m & 1));
+            const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+            mma_bf16(o, a[2 * kp], b0);
+            mma_bf16(o, a[2 * kp + 1], b1);
         }
         if (c == 0) {
             const float b0 = bs[3 * H], b1 = bs[3 * H + 1];
