@@ -2,7 +2,8 @@
 //
 // Layout in HBM (all arrays indexed by the current cell-sorted particle order):
 //   pos, vel        dbl4  (x, y, z, unused)   FP64 master state, 32 B each
-//   opos, ovel      float4                        FP32 operator copies (FP32 mode)
+//   opos, ovel      float4                        FP32 operator copies; opos.w holds the
+//                                                 particle's global z bin (cell z * 64 + bin)
 //   press           double                        pressure (PPE solution)
 //   visc            float, type int, id int       carried per particle
 //   key, idx        int                           hash keys / sort permutation
@@ -51,6 +52,8 @@ struct Dev {
     int *type2, *id2;
     float4 *opos, *ovel;
     int *key, *idx;
+    int* skey;                 // sort key: cell << zbits | z bin of the particle inside its cell
+    int zbits;                 // z-bin bits of the sort key (6; 0 for grids too large for them)
     int *cstart, *cend;
     int* cell_list;
     int* cell_count;

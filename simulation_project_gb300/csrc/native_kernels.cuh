@@ -158,7 +158,15 @@ __global__ void k_hash(const __grid_constant__ Dev d) {
         atomicOr(d.err, MPS_ERR_KEY_RANGE);
         k = k < 0 ? 0 : d.cells - 1;
     }
-    d.key[i] = k;
+    // particles of a cell are ordered by a z bin (1/64 of the cell): each 3-cell z-run
+    // of the neighbour search is then sorted by z, so a target can clip it
+    int zq = 0;
+    if (d.zbits) {
+        const double fz = (p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs;
+        zq = f2i((fz - (double)c) * (double)(1 << d.zbits));
+        zq = zq < 0 ? 0 : (zq > (1 << d.zbits) - 1 ? (1 << d.zbits) - 1 : zq);
+    }
+    d.skey[i] = (k << d.zbits) | zq;
     d.idx[i] = i;
 }
 
@@ -174,12 +182,17 @@ __global__ void k_gather(const __grid_constant__ Dev d) {
     d.visc2[i] = d.visc[s];
     d.type2[i] = d.type[s];
     d.id2[i] = d.id[s];
-    d.opos[i] = make_float4((float)p.x, (float)p.y, (float)p.z, 0.f);
+    const int sk = d.skey[i];
+    const int h = sk >> d.zbits;
+    // global z bin (cell z * 64 + bin inside the cell), exact in a float
+    const float zbin = (float)((h % d.box.m_GridSize.z) * 64 + ((sk & ((1 << d.zbits) - 1)) << (6 - d.zbits)));
+    d.opos[i] = make_float4((float)p.x, (float)p.y, (float)p.z, zbin);
     d.ovel[i] = make_float4((float)v.x, (float)v.y, (float)v.z, 0.f);
-    const int h = d.key[i];
-    if (i == 0 || h != d.key[i - 1]) {
+    d.key[i] = h;
+    const int hp = i > 0 ? (d.skey[i - 1] >> d.zbits) : -1;
+    if (i == 0 || h != hp) {
         d.cstart[h] = i;
-        if (i > 0) d.cend[d.key[i - 1]] = i;
+        if (i > 0) d.cend[hp] = i;
         const int slot = atomicAdd(d.cell_count, 1);
         d.cell_list[slot] = h;
     }
@@ -544,9 +557,48 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         T a0 = 0, a1 = 0, a2 = 0, a3 = 0;   // mode-specific accumulators
         int cnt = 0, gcnt = 0;
         const size_t row0 = sell_index(i, 0, d.K);   // SELL position of the row's entry 0
+        // z window of each run for this target: the run (3 cells stacked in z) is sorted
+        // by z bin; the bins a neighbour can occupy are those within +-sqrt(re^2 - dxy^2)
+        // of the target, dxy its distance to the run's column in x-y (re^2 with a 2e-4
+        // margin, bounds widened by one bin: no neighbour is cut by FP32 round-off).
+        // Lanes 0..8 find the first candidate of run `lane`, lanes 16..24 the end.
+        int bound = 0;
+        {
+            const int r = lane & 15;
+            const bool upper = lane >= 16;
+            if (r < 9) {
+                const int len = rl[r];
+                bound = upper ? len : 0;
+                if (d.zbits && len > 0) {
+                    const float cs = d.box.m_CellSize;
+                    const float xlo = d.box.m_BufferedZone.m_MinBound.x + (float)(cx + r / 3 - 1) * cs;
+                    const float ylo = d.box.m_BufferedZone.m_MinBound.y + (float)(cy + r % 3 - 1) * cs;
+                    const float ddx = fmaxf(0.f, fmaxf(xlo - pf.x, pf.x - (xlo + cs)));
+                    const float ddy = fmaxf(0.f, fmaxf(ylo - pf.y, pf.y - (ylo + cs)));
+                    const float rem = re2f * 1.0001f - (ddx * ddx + ddy * ddy);
+                    if (rem <= 0.f) {
+                        bound = 0;
+                    } else {
+                        const float reff = sqrtf(rem);
+                        const float scale = 64.f / cs;
+                        const float zrel = pf.z - d.box.m_BufferedZone.m_MinBound.z;
+                        const float tb = upper ? floorf((zrel + reff) * scale) + 1.f : floorf((zrel - reff) * scale) - 1.f;
+                        int lo = 0, hi = len;
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            const float w = staged ? spos[rp[r] + mid].w : d.opos[rs[r] + mid].w;
+                            if (upper ? (w <= tb) : (w < tb)) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        bound = lo;
+                    }
+                }
+            }
+        }
         for (int r = 0; r < 9; ++r) {
-            const int len = rl[r];
-            for (int b = 0; b < len; b += 32) {
+            const int kb = __shfl_sync(0xffffffffu, bound, r);
+            const int len = max(kb, __shfl_sync(0xffffffffu, bound, 16 + r));
+            for (int b = kb; b < len; b += 32) {
                 const int o = b + lane;
                 const bool valid = o < len;
                 const int j = rs[r] + o;

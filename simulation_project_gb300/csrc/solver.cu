@@ -182,7 +182,8 @@ struct Solver {
         e = e ? e : mk(&d.press, N); e = e ? e : mk(&d.press2, N); e = e ? e : mk(&d.visc, N); e = e ? e : mk(&d.visc2, N);
         e = e ? e : mk(&d.type, N); e = e ? e : mk(&d.type2, N); e = e ? e : mk(&d.id, N); e = e ? e : mk(&d.id2, N);
         e = e ? e : mk(&d.opos, N); e = e ? e : mk(&d.ovel, N);
-        e = e ? e : mk(&d.key, N); e = e ? e : mk(&d.idx, N);
+        e = e ? e : mk(&d.key, N); e = e ? e : mk(&d.idx, N); e = e ? e : mk(&d.skey, N);
+        d.zbits = d.cells < (1 << 24) ? 6 : 0;   // the sort key stays below 2^30
         e = e ? e : mk(&d.cstart, (size_t)d.cells); e = e ? e : mk(&d.cend, (size_t)d.cells);
         e = e ? e : mk(&d.cell_list, (size_t)d.cells); e = e ? e : mk(&d.cell_count, 1);
         e = e ? e : mk(&d.wdist, N); e = e ? e : mk(&d.wdir, 3 * N); e = e ? e : mk(&d.wid, N);
@@ -458,7 +459,8 @@ struct Solver {
         const int n = d.n;
         if (n <= 0) return CCT_NOERR;
         MPS_COUNT_LAUNCH k_hash<<<blocks_for(n), kBlock, 0, st>>>(d);
-        if (radix_sort_pairs(n, d.key, d.idx, 0, radix_passes((unsigned)(d.cells - 1)), sort_scratch, st)) return CCT_CUDAERR;
+        const unsigned krange = ((unsigned)d.cells << d.zbits) - 1u;
+        if (radix_sort_pairs(n, d.skey, d.idx, 0, radix_passes(krange), sort_scratch, st)) return CCT_CUDAERR;
         cudaMemsetAsync(d.cstart, 0xff, sizeof(int) * d.cells, st);
         cudaMemsetAsync(d.cend, 0xff, sizeof(int) * d.cells, st);
         cudaMemsetAsync(d.cell_count, 0, sizeof(int), st);
