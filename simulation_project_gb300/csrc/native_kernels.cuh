@@ -546,6 +546,9 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
     const unsigned lt = (1u << lane) - 1u;
     const T re = (T)d.c.re_lap, reg = (T)d.c.re_grad, mind = (T)d.c.mind_lap, mindg = (T)d.c.mind_grad;
     const float re2f = (float)(d.c.re_lap * d.c.re_lap) * 1.0001f;
+    // FP32 path: one reciprocal square root per accepted pair gives r and both weights
+    const float re2s = (float)d.c.re_lap * (float)d.c.re_lap;
+    const float wmax = (float)(d.c.re_lap / d.c.mind_lap) - 1.f, wgmax = (float)(d.c.re_grad / d.c.mind_grad) - 1.f;
     // target parked in this lane for the lane-parallel epilogue
     int my_i = -1, my_cnt = 0, my_gcnt = 0;
     T m0 = 0, m1 = 0, m2 = 0, m3 = 0;
@@ -604,6 +607,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 const int j = rs[r] + o;
                 bool acc = false, gacc = false;
                 T rr = T(0);
+                float rinv = 0.f;   // 1 / r (FP32 path)
                 V3<T> dv = v3(T(0), T(0), T(0));
                 if (valid && j != i) {
                     const float4 q = staged ? spos[rp[r] + o] : d.opos[j];
@@ -620,10 +624,10 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                                 dv = v3<T>(dx, dy, dz);
                             }
                         } else {
-                            const float rf = sqrtf(d2f);
-                            if (rf < (float)re) {
+                            if (d2f < re2s) {
                                 acc = true;
-                                rr = rf;
+                                rinv = rsqrtf(fmaxf(d2f, 1e-30f));
+                                rr = d2f * rinv;
                                 dv = v3<T>(dxf, dyf, dzf);
                             }
                         }
@@ -631,7 +635,9 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
                 if (acc) {
-                    const T w = wdiv<T>(re, rr > mind ? rr : mind) - T(1);
+                    T w;
+                    if constexpr (sizeof(T) == 4) w = rr > mind ? re * rinv - 1.f : wmax;
+                    else w = wdiv<T>(re, rr > mind ? rr : mind) - T(1);
                     if constexpr (MODE == NB_PREDICT) {
                         V3<T> vj;
                         if constexpr (sizeof(T) == 8) {
@@ -654,8 +660,9 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                         a0 += w;                                   // sum of Laplacian weights
                         if (rr < reg) {
                             gacc = true;
-                            const T rg = rr > mindg ? rr : mindg;
-                            const T wg = wdiv<T>(reg, rg) - T(1);
+                            T wg;
+                            if constexpr (sizeof(T) == 4) wg = rr > mindg ? reg * rinv - 1.f : wgmax;
+                            else wg = wdiv<T>(reg, rr > mindg ? rr : mindg) - T(1);
                             a2 += wg;                              // PND
                         }
                     }
