@@ -47,10 +47,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# DRAM bytes per neighbour entry of one k_spmv<float,float,float,0> launch, measured
-# with ncu (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on the default
-# workload with 16-bit column offsets: 1.35 GB for 201.4M entries (padding included)
-SPMV_DRAM_BYTES_PER_ENTRY = 1.352e9 / 201.36e6
+# compulsory bytes per particle of one step, per FP32 CG iteration and per FP64
+# refinement pass (hash, sort, reorder, walls, predictor, PND/RHS, correction;
+# SpMV + dots + vector updates; residual)
+STEP_FIXED_B, STEP_ITER_B, STEP_IR_B = 760.0, 72.0, 48.0
+# DRAM bytes per neighbour entry of one k_spmv_stream launch, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum, one pass) on the default workload
+# with 16-bit column offsets: 1.3376 GB read + 2.2 MB written for 201.36M entries
+# (SELL padding included)
+SPMV_DRAM_BYTES_PER_ENTRY = (1.33758e9 + 2.24e6) / 201.362e6
 
 
 def load_peaks():
@@ -258,7 +263,7 @@ def run_gpu(args):
     bytes_launch = 6.0 * (nnz - nnz_wide) + 8.0 * nnz_wide + 25.0 * interior
     avg_ms = spmv_ms / max(spmv_n, 1)
     achieved = bytes_launch / (avg_ms / 1e3) / 1e9 if spmv_n else 0.0
-    roofline = {"bound": "hbm", "kernel": "k_spmv<float,float,float> (PPE SpMV, FP32 rows)",
+    roofline = {"bound": "hbm", "kernel": "k_spmv_stream<0,8,2,8,4> (PPE SpMV, FP32 rows streamed by bulk copies)",
                 "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
                 "frac": round(achieved / peak_gbs, 3), "peak_kind": peak_kind,
                 "traffic": int(SPMV_DRAM_BYTES_PER_ENTRY * nnz), "traffic_source": "ncu dram bytes per entry x entries",
@@ -268,6 +273,21 @@ def run_gpu(args):
     phases = {k: round(float(np.mean([s[k] for s in st_fast])), 3) for k in
               ("ms_grid", "ms_walls", "ms_predictor", "ms_list", "ms_ppe_setup", "ms_spmv", "ms_cg_vec",
                "ms_correct", "ms_learned", "ms_precond")}
+    # compulsory bytes of the whole step: N (760 + k_CG 72 + k_IR 48) B with the FP32
+    # operator recomputed from positions (the stored SELL rows are extra, reported beside)
+    k_cg = float(np.mean([s["cg_iterations"] for s in st_fast]))
+    k_ir = float(np.mean([s["ir_passes"] for s in st_fast]))
+    step_bytes = n * (STEP_FIXED_B + k_cg * STEP_ITER_B + k_ir * STEP_IR_B)
+    step_gbs = step_bytes / (ms_fast / args.steps / 1e3) / 1e9
+    step_model = {"model": "N*(760 + k_CG*72 + k_IR*48) bytes per step", "k_cg": k_cg, "k_ir": k_ir,
+                  "bytes_per_step": int(step_bytes), "achieved_gbs": round(step_gbs, 1),
+                  "frac": round(step_gbs / peak_gbs, 4),
+                  "stored_row_bytes_per_step": int(k_cg * bytes_launch)}
+    # accepted Laplacian pairs of the two neighbour passes (predictor and rows/PND)
+    pairs = float(np.mean([s["pairs"] for s in st_fast]))
+    nb_ms = phases["ms_predictor"] + phases["ms_list"]
+    pair_evals = {"accepted_pairs_per_pass": int(pairs), "accepted_per_particle": round(pairs / n, 1),
+                  "passes": 2, "pairs_per_s": 2.0 * pairs / (nb_ms / 1e3) if nb_ms > 0 else None}
 
     # end to end through the C-ABI from pinned host buffers
     e2e = run_e2e(fast, args)
@@ -317,6 +337,8 @@ def run_gpu(args):
                         "phases_ms": phases},
         "learned_training": train_info,
         "roofline": roofline,
+        "step_bytes": step_model,
+        "pair_evaluations": pair_evals,
         "sort": sort,
         "accuracy_vs_fp64": accuracy,
         "e2e": e2e,

@@ -68,6 +68,13 @@ typedef struct MpsSolverOptions {
                                slice spans <= 65535 columns (same results, fewer bytes) */
     int mg_sweeps;          /* weighted-Jacobi sweeps on level 1 before the restriction and
                                after the prolongation (coarser levels: 1) */
+    int matrix_free;        /* FP32 inner SpMV: 0 streams the stored FP32 weights; 4 or 8
+                               recompute each weight from the FP32 positions the neighbour
+                               pass used (same bits), 4 or 8 entries per unrolled group,
+                               streaming only the columns */
+    int spmv_stream;        /* FP32 inner SpMV over 16-bit slices: 0 register walk; 1 rows
+                               streamed through shared memory by bulk copies (a ring of 2
+                               stages of 8 entries per warp); same row values */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */
@@ -127,6 +134,11 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
  * array of n doubles, may be NULL) and ||r|| / ||b||: variant 0 with FP64
  * products and sums, variant 1 with the double-float kernel the solver uses */
 CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, double* relres);
+/* One FP32 inner SpMV y = A x over the current rows (FP32_IR solvers; host arrays of
+ * n floats in the solver's order): kernel 0 register walk, 1 rows streamed through
+ * shared memory (needs the 16-bit slices), 4 / 8 matrix-free.  Every kernel gives the
+ * same bits. */
+CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
 /* Device pointer of the pressure array (FP64, sorted order) and particle count. */
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);
 /* Pressure read back to a host buffer, in the solver's order (e2e output). */

@@ -75,6 +75,7 @@ struct Dev {
     void* nbrw;
     unsigned short* nbr16;     // SELL-32 column offsets from the slice base (interior rows)
     int* sbase;                // [slices] smallest column index of the slice, -1: 32-bit slice
+    int* skmax;                // [slices] longest interior row of a 16-bit slice, -1: 32-bit slice
     int rows16;                // nbr16 / sbase are valid for the current rows
     int* nbr_cnt;
     int* gnbr;

@@ -49,11 +49,37 @@ __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, unsign
                  ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+// L2 policy for streamed data read once: evict first (keeps the vectors that the
+// next kernels reuse resident in L2)
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+// bulk copy as bulk_copy_g2s with an L2 cache policy
+__device__ __forceinline__ void bulk_copy_g2s_hint(void* dst, const void* src, unsigned bytes, unsigned long long* bar,
+                                                   unsigned long long pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
 // bounded wait on phase 0 of bar: false if it did not complete within `spins` polls
 __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, long long spins) {
     for (long long k = 0; k < spins; ++k)
         if (mbar_test_parity(bar, 0)) return true;
     return false;
+}
+// bounded wait for the completion of the phase with the given parity
+__device__ __forceinline__ bool mbar_wait_parity_bounded(unsigned long long* bar, unsigned parity, long long spins) {
+    for (long long k = 0; k < spins; ++k)
+        if (mbar_test_parity(bar, parity)) return true;
+    return false;
+}
+// orders this thread's earlier generic-proxy accesses to shared memory (after a warp
+// barrier: the warp's reads of a stage) before later bulk copies into it
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // a / b: IEEE division in FP64; in FP32 the fast approximate form (<= 2 ulp), which
@@ -476,6 +502,19 @@ __device__ __forceinline__ void nb_epilogue(const Dev& d, int i, T a0, T a1, T a
     }
 }
 
+// FP32 squared distance and Laplacian weight of one pair, every rounding explicit:
+// the neighbour pass that stores the weights and the matrix-free SpMV that
+// recomputes them from the same positions get the same bits.
+__device__ __forceinline__ float dist2_f32(float dx, float dy, float dz) {
+    return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+// w = re / max(r, mind) - 1 from one reciprocal square root; rinv = 1 / r, rr = r
+__device__ __forceinline__ float lap_weight_f32(float d2, float re, float mind, float wmax, float& rinv, float& rr) {
+    rinv = rsqrtf(fmaxf(d2, 1e-30f));
+    rr = __fmul_rn(d2, rinv);
+    return rr > mind ? __fmaf_rn(re, rinv, -1.f) : wmax;
+}
+
 // Neighbour passes, CTA per non-empty cell.  The 9 (x, y) columns of the 27-cell
 // neighbourhood are contiguous z-runs in the sorted order; their positions are
 // staged in shared memory (float4), a warp takes one target particle at a time and
@@ -607,12 +646,12 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 const int j = rs[r] + o;
                 bool acc = false, gacc = false;
                 T rr = T(0);
-                float rinv = 0.f;   // 1 / r (FP32 path)
+                float rinv = 0.f, rrf = 0.f, wf = 0.f;   // 1 / r, r, Laplacian weight (FP32 path)
                 V3<T> dv = v3(T(0), T(0), T(0));
                 if (valid && j != i) {
                     const float4 q = staged ? spos[rp[r] + o] : d.opos[j];
                     const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
-                    const float d2f = dxf * dxf + dyf * dyf + dzf * dzf;
+                    const float d2f = dist2_f32(dxf, dyf, dzf);
                     if (d2f < re2f) {
                         if constexpr (sizeof(T) == 8) {
                             const dbl4 pj = d.pos[j];
@@ -626,8 +665,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                         } else {
                             if (d2f < re2s) {
                                 acc = true;
-                                rinv = rsqrtf(fmaxf(d2f, 1e-30f));
-                                rr = d2f * rinv;
+                                wf = lap_weight_f32(d2f, (float)re, (float)mind, wmax, rinv, rrf);
+                                rr = rrf;
                                 dv = v3<T>(dxf, dyf, dzf);
                             }
                         }
@@ -636,7 +675,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
                 if (acc) {
                     T w;
-                    if constexpr (sizeof(T) == 4) w = rr > mind ? re * rinv - 1.f : wmax;
+                    if constexpr (sizeof(T) == 4) w = wf;
                     else w = wdiv<T>(re, rr > mind ? rr : mind) - T(1);
                     if constexpr (MODE == NB_PREDICT) {
                         V3<T> vj;
@@ -661,7 +700,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                         if (rr < reg) {
                             gacc = true;
                             T wg;
-                            if constexpr (sizeof(T) == 4) wg = rr > mindg ? reg * rinv - 1.f : wgmax;
+                            if constexpr (sizeof(T) == 4) wg = rr > mindg ? __fmaf_rn(reg, rinv, -1.f) : wgmax;
                             else wg = wdiv<T>(reg, rr > mindg ? rr : mindg) - T(1);
                             a2 += wg;                              // PND
                         }
@@ -778,13 +817,20 @@ __global__ void k_compress_rows(const __grid_constant__ Dev d) {
         }
     }
     const bool all = __all_sync(0xffffffffu, fits);
-    if (lane == 0) d.sbase[sl] = all ? r0 : -1;
+    if (lane == 0) {
+        d.sbase[sl] = all ? r0 : -1;
+        d.skmax[sl] = all ? kmax : -1;
+    }
     // interior entries kept at 32 bits (counted for the bytes-per-launch figure)
     int wide = all ? 0 : cnt;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) wide += __shfl_down_sync(0xffffffffu, wide, o);
     if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
 }
+
+// acc + a * b with one rounding (no contraction left to the compiler)
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 // Dot of one SELL row with x (lane = row), evict-first loads.  U entries' loads are
 // in flight before their gathers: 8 for 16-bit columns (6 B per entry, so a warp
@@ -805,12 +851,59 @@ __device__ __forceinline__ TA sell_row_dot(const Dev& d, const TW* __restrict__ 
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            if (k + u < cnt) acc += (TA)wv[u] * (TA)x[id[u]];
+            if (k + u < cnt) acc = fma_t((TA)wv[u], (TA)x[id[u]], acc);
     }
     for (; k < kmax; ++k) {
         const int idk = sell_col<NARROW>(d, base + (size_t)k * 32, sb);
         const TW wk = __ldcs(w + base + (size_t)k * 32);
-        if (k < cnt) acc += (TA)wk * (TA)x[idk];
+        if (k < cnt) acc = fma_t((TA)wk, (TA)x[idk], acc);
+    }
+    return acc;
+}
+
+// Matrix-free FP32 row dot (lane = row): only the columns are streamed; each weight
+// is recomputed from the FP32 positions the neighbour pass used, by the same
+// expression (dist2_f32, lap_weight_f32), so the sum is bit-identical to the
+// stored-weight walk.  U entries' columns are loaded, then their position and x
+// gathers (a padded entry gathers the row itself and is not accumulated).
+template <bool NARROW, int U>
+__device__ __forceinline__ float sell_row_dot_mf(const Dev& d, const float* __restrict__ x, size_t base, int cnt,
+                                                 int kmax, int sb, int i, float4 pi, float re, float mind,
+                                                 float wmax) {
+    float acc = 0.f;
+    int k = 0;
+    for (; k + U <= kmax; k += U) {
+        int id[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            id[u] = sell_col<NARROW>(d, base + (size_t)(k + u) * 32, sb);
+            if (k + u >= cnt) id[u] = i;
+        }
+        float4 q[U];
+        float xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            q[u] = __ldg(d.opos + id[u]);
+            xv[u] = __ldg(x + id[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            float rinv, rr;
+            const float wk = lap_weight_f32(dist2_f32(__fsub_rn(q[u].x, pi.x), __fsub_rn(q[u].y, pi.y),
+                                                      __fsub_rn(q[u].z, pi.z)),
+                                            re, mind, wmax, rinv, rr);
+            if (k + u < cnt) acc = __fmaf_rn(wk, xv[u], acc);
+        }
+    }
+    for (; k < kmax; ++k) {
+        int j = sell_col<NARROW>(d, base + (size_t)k * 32, sb);
+        if (k >= cnt) j = i;
+        const float4 q = __ldg(d.opos + j);
+        const float xj = __ldg(x + j);
+        float rinv, rr;
+        const float wk = lap_weight_f32(dist2_f32(__fsub_rn(q.x, pi.x), __fsub_rn(q.y, pi.y), __fsub_rn(q.z, pi.z)),
+                                        re, mind, wmax, rinv, rr);
+        if (k < cnt) acc = __fmaf_rn(wk, xj, acc);
     }
     return acc;
 }
@@ -823,10 +916,13 @@ __device__ __forceinline__ TA sell_row_dot(const Dev& d, const TW* __restrict__ 
 // full 128-byte line (256 for FP64 weights) and no cross-lane reduction is needed.
 // The k loop runs to the slice's longest row, unrolled 4x so that eight line loads
 // are in flight per warp before the gathers; matrix loads are evict-first.
-template <class TW, class TX, class TY, int MODE>
-__global__ void __launch_bounds__(256, 8) k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w,
-                                              const TX* __restrict__ x, TY* __restrict__ y, const double* __restrict__ b,
-                                              int slot) {
+// MF > 0 (FP32 weights, FP32 x): matrix-free rows, MF entries per unrolled group; the
+// weight array is not read.
+template <class TW, class TX, class TY, int MODE, int MF = 0>
+__global__ void __launch_bounds__(256, MF == 0 ? 8 : (MF <= 4 ? 5 : 3))
+    k_spmv(const __grid_constant__ Dev d, const TW* __restrict__ w, const TX* __restrict__ x, TY* __restrict__ y,
+           const double* __restrict__ b, int slot) {
+    static_assert(MF == 0 || (sizeof(TW) == 4 && sizeof(TX) == 4 && MODE != 1), "matrix-free rows: FP32 only");
     if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -845,8 +941,18 @@ __global__ void __launch_bounds__(256, 8) k_spmv(const __grid_constant__ Dev d, 
         const int kmax = __reduce_max_sync(0xffffffffu, cnt);
         const size_t base = (size_t)sl * d.K * 32 + lane;
         const int sb = (sizeof(TW) == 4 && d.rows16) ? d.sbase[sl] : -1;
-        const TA acc = sb >= 0 ? sell_row_dot<true, TA>(d, w, x, base, cnt, kmax, sb)
-                               : sell_row_dot<false, TA>(d, w, x, base, cnt, kmax, sb);
+        TA acc;
+        if constexpr (MF > 0) {
+            const float4 pi = in ? d.opos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float re = (float)d.c.re_lap, mind = (float)d.c.mind_lap;
+            const float wmax = (float)(d.c.re_lap / d.c.mind_lap) - 1.f;
+            const int ii = row ? i : 0;
+            acc = sb >= 0 ? sell_row_dot_mf<true, MF>(d, (const float*)x, base, cnt, kmax, sb, ii, pi, re, mind, wmax)
+                          : sell_row_dot_mf<false, MF>(d, (const float*)x, base, cnt, kmax, sb, ii, pi, re, mind, wmax);
+        } else {
+            acc = sb >= 0 ? sell_row_dot<true, TA>(d, w, x, base, cnt, kmax, sb)
+                          : sell_row_dot<false, TA>(d, w, x, base, cnt, kmax, sb);
+        }
         if (!row) continue;
         if (!in) {
             y[i] = TY(0);
@@ -881,6 +987,162 @@ __global__ void __launch_bounds__(256, 8) k_spmv(const __grid_constant__ Dev d, 
             d.scal[S_RR] = out[0];
             d.scal[S_RNORM] = sqrt(out[0]);
             d.scal[S_BNORM] = sqrt(out[1]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Streamed FP32 SpMV of the inner CG: the 16-bit columns and FP32 weights of each
+// slice reach shared memory by bulk (TMA) copies, so the loads in flight do not
+// hold registers.  Every warp owns a ring of SS stages of SC entries (SC x 64 B of
+// columns + SC x 128 B of weights per stage, one mbarrier each); lane 0 keeps the
+// ring full, running ahead across the warp's slices (gw, gw + nw, ...), while all
+// lanes gather x and accumulate the stage in entry order, so every row value is
+// bit-identical to the register walk.  32-bit slices (skmax = -1) take the register
+// walk.  A stage that does not land within the poll limit sets
+// MPS_ERR_STAGE_TIMEOUT; the warp then waits (bounded) for its copies in flight and
+// finishes on the register walk.  MODE 0 / 2 as in k_spmv.
+// ---------------------------------------------------------------------------
+template <int SC> constexpr int stream_stage_bytes() { return SC * 192; }
+template <int SC, int SS, int W> constexpr int stream_smem_bytes() { return W * SS * stream_stage_bytes<SC>(); }
+
+template <int MODE, int SC, int SS, int W, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_constant__ Dev d,
+                                                                  const float* __restrict__ w,
+                                                                  const float* __restrict__ x, float* __restrict__ y,
+                                                                  const double* __restrict__ b, int slot) {
+    static_assert(MODE == 0 || MODE == 2, "FP32 modes only");
+    static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
+    if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
+    extern __shared__ __align__(128) unsigned char stream_smem[];
+    __shared__ __align__(8) unsigned long long bars[W][SS];
+    constexpr int SB = stream_stage_bytes<SC>();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* ring = stream_smem + warp * SS * SB;
+    unsigned long long* bar = bars[warp];
+    if (lane == 0)
+        for (int st = 0; st < SS; ++st) mbar_init(&bar[st], 1);
+    __syncwarp();
+
+    const int gw = blockIdx.x * W + warp;
+    const int nw = gridDim.x * W;
+    const int nsl = (d.n + 31) >> 5;
+    const int K = d.K;
+    // producer: next chunk to copy is chunk pc of slice ps (pk entries, pn chunks)
+    int ps = gw - nw, pc = 0, pk = 0, pn = 0;
+    auto next_slice = [&]() {
+        do {
+            ps += nw;
+            pk = ps < nsl ? d.skmax[ps] : 0;
+        } while (ps < nsl && pk <= 0);
+        pc = 0;
+        pn = (pk + SC - 1) / SC;
+    };
+    next_slice();
+    unsigned q_issue = 0, q_cons = 0;
+    bool streaming = true;
+    const unsigned long long pol = l2_evict_first_policy();
+    auto refill = [&]() {
+        while (streaming && ps < nsl && q_issue - q_cons < (unsigned)SS) {
+            const int st = (int)(q_issue % SS);
+            const int k0 = pc * SC;
+            const int ne = min(SC, pk - k0);
+            if (lane == 0) {
+                const size_t e0 = ((size_t)ps * K + k0) * 32;
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * 192u);
+                bulk_copy_g2s_hint(ring + st * SB, d.nbr16 + e0, (unsigned)ne * 64u, &bar[st], pol);
+                bulk_copy_g2s_hint(ring + st * SB + SC * 64, w + e0, (unsigned)ne * 128u, &bar[st], pol);
+            }
+            ++q_issue;
+            if (++pc == pn) next_slice();
+        }
+    };
+    // gives up streaming: bounded wait for the copies still in flight into this ring
+    auto abandon = [&]() {
+        if (lane == 0) atomicOr(d.err, MPS_ERR_STAGE_TIMEOUT);
+        for (unsigned q = q_cons; q != q_issue; ++q)
+            mbar_wait_parity_bounded(&bar[q % SS], (q / SS) & 1u, 1ll << 24);
+        streaming = false;
+        q_cons = q_issue;
+    };
+
+    const double coef = d.c.coef_lap;
+    double part0 = 0.0, part1 = 0.0;
+    float partw = 0.f;
+    for (int sl = gw; sl < nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int km = d.skmax[sl];
+        const size_t base = (size_t)sl * K * 32 + lane;
+        float acc = 0.f;
+        bool done = false;
+        if (km >= 0 && streaming) {
+            if (km > 0) {
+                const int nc = (km + SC - 1) / SC;
+                const int r0 = sl * 32;
+                for (int c = 0; c < nc; ++c) {
+                    refill();
+                    const int st = (int)(q_cons % SS);
+                    if (!__all_sync(0xffffffffu, mbar_wait_parity_bounded(&bar[st], (q_cons / SS) & 1u, 1ll << 20))) {
+                        abandon();
+                        break;
+                    }
+                    const unsigned short* cs = (const unsigned short*)(ring + st * SB);
+                    const float* ws = (const float*)(ring + st * SB + SC * 64);
+                    const int k0 = c * SC;
+#pragma unroll
+                    for (int g = 0; g < SC; g += 8) {
+                        int j[8];
+                        float wv[8];
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) {
+                            j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
+                            wv[u] = ws[(g + u) * 32 + lane];
+                        }
+#pragma unroll
+                        for (int u = 0; u < 8; ++u)
+                            if (k0 + g + u < cnt) acc = __fmaf_rn(wv[u], __ldg(x + j[u]), acc);
+                    }
+                    __syncwarp();
+                    ++q_cons;
+                }
+            }
+            done = streaming;
+        }
+        if (!done) {
+            // 32-bit slice, or streaming given up: the register walk
+            const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+            const int sb = (km >= 0) ? sl * 32 : -1;
+            acc = sb >= 0 ? sell_row_dot<true, float>(d, w, x, base, cnt, kmax, sb)
+                          : sell_row_dot<false, float>(d, w, x, base, cnt, kmax, sb);
+        }
+        if (!row) continue;
+        if (!in) {
+            y[i] = 0.f;
+            continue;
+        }
+        const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
+        y[i] = (float)yi;
+        if (MODE == 0) {
+            partw += x[i] * (float)yi;
+        } else {
+            part0 += (double)x[i] * yi;
+            part1 += (double)x[i] * b[i];
+        }
+    }
+    if (MODE == 0) part0 = (double)partw;
+    double v[2] = {part0, part1}, out[2];
+    if (grid_reduce<2, typename std::conditional<MODE == 0, float, double>::type>(v, d.red, d.red_count + slot, out) &&
+        threadIdx.x == 0) {
+        if (MODE == 0) {
+            d.scal[S_PQ] = out[0];
+            d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
+        } else {
+            d.scal[S_LS0] = out[0];
+            d.scal[S_LS1] = out[1];
         }
     }
 }

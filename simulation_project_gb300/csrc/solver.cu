@@ -192,6 +192,7 @@ struct Solver {
         const size_t N32 = (N + 31) / 32 * 32;
         e = e ? e : mk(&d.nbr, N32 * d.K); e = e ? e : mk((char**)&d.nbrw, N32 * d.K * wsz);
         e = e ? e : mk(&d.nbr16, N32 * d.K); e = e ? e : mk(&d.sbase, N32 / 32 + 1);
+        e = e ? e : mk(&d.skmax, N32 / 32 + 1);
         e = e ? e : mk(&d.nbr_cnt, N);
         e = e ? e : mk(&d.gnbr, N * d.KG); e = e ? e : mk((char**)&d.gnbrr, N * d.KG * wsz);
         e = e ? e : mk(&d.gcnt, N);
@@ -578,8 +579,8 @@ struct Solver {
                         MPS_COUNT_LAUNCH k_spmv<double, double, double, 2><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.z,
                                                                                       d.q, d.r, 6);
                     else   // FP32 products: the line search needs no more
-                        MPS_COUNT_LAUNCH k_spmv<float, float, float, 2><<<kRedBlocks, 256, 0, st>>>(d, (const float*)d.nbrw, d.z32,
-                                                                                   d.q32, d.r, 6);
+                        spmv_ls((const float*)d.nbrw);
+                    if (stream_failed) return CCT_CUDAERR;
                     if (fp64()) {
                         MPS_COUNT_LAUNCH k_learned_finish<<<blocks_for(d.n), kBlock, 0, st>>>(d);
                     } else {
@@ -651,6 +652,77 @@ struct Solver {
         return CCT_NOERR;
     }
 
+    // streamed SpMV: ring of 2 stages of 8 entries per warp, CTAs of 8 warps, at least
+    // 4 CTAs per SM (5 resident at 48 registers).  Measured on the 882k-particle
+    // bucket against rings of 3-4 stages, 16 entries, and 6-8 or 16-32-warp CTAs:
+    // more shared memory costs more in L1 hits of the x gathers than it gains in
+    // copies in flight.  Dynamic shared memory opt-in and a persistent grid of
+    // SMs x resident CTAs, set up on first use.
+    static constexpr int kSsEntries = 8, kSsStages = 2, kSsWarps = 8, kSsMinBlocks = 4;
+    int stream_grid = 0;
+    bool stream_failed = false;
+    int stream_blocks() {
+        if (stream_grid == 0) {
+            constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps>();
+            auto k0 = k_spmv_stream<0, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            auto k2 = k_spmv_stream<2, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            if (cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) ||
+                cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
+                return -1;
+            int dev = 0, sms = 0, per_sm = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k0, kSsWarps * 32, smem)) return -1;
+            // the reduction buffer holds 2 partials per CTA for up to 2 x kRedBlocks CTAs
+            stream_grid = std::max(1, std::min(sms * std::max(per_sm, 1), 2 * kRedBlocks));
+        }
+        return stream_grid;
+    }
+    template <int MODE>
+    void spmv_stream(const float* w, const float* x, float* y, const double* b, int slot) {
+        const int g = stream_blocks();
+        if (g < 0) {
+            stream_failed = true;
+            return;
+        }
+        constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps>();
+        MPS_COUNT_LAUNCH k_spmv_stream<MODE, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>
+            <<<g, kSsWarps * 32, smem, st>>>(d, w, x, y, b, slot);
+    }
+    // the streamed kernel needs the 16-bit slices of this step
+    bool use_stream() const { return opt.spmv_stream != 0 && d.rows16; }
+
+    // q = A p of the inner CG (MODE 0): stored weights, or matrix-free FP32 rows
+    template <class TW, class TV>
+    void spmv_cg(const TW* w, const TV* p, TV* q) {
+        if constexpr (std::is_same<TW, float>::value && std::is_same<TV, float>::value) {
+            if (opt.matrix_free == 0 && use_stream()) {
+                spmv_stream<0>(w, p, q, nullptr, 0);
+                return;
+            }
+            if (opt.matrix_free == 4) {
+                MPS_COUNT_LAUNCH k_spmv<float, float, float, 0, 4><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+                return;
+            }
+            if (opt.matrix_free == 8) {
+                MPS_COUNT_LAUNCH k_spmv<float, float, float, 0, 8><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+                return;
+            }
+        }
+        MPS_COUNT_LAUNCH k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+    }
+    // q32 = A z32 with the line-search dots (MODE 2) of the learned guess, FP32
+    void spmv_ls(const float* w) {
+        if (opt.matrix_free == 0 && use_stream())
+            spmv_stream<2>(w, d.z32, d.q32, d.r, 6);
+        else if (opt.matrix_free == 4)
+            MPS_COUNT_LAUNCH k_spmv<float, float, float, 2, 4><<<kRedBlocks, 256, 0, st>>>(d, w, d.z32, d.q32, d.r, 6);
+        else if (opt.matrix_free == 8)
+            MPS_COUNT_LAUNCH k_spmv<float, float, float, 2, 8><<<kRedBlocks, 256, 0, st>>>(d, w, d.z32, d.q32, d.r, 6);
+        else
+            MPS_COUNT_LAUNCH k_spmv<float, float, float, 2><<<kRedBlocks, 256, 0, st>>>(d, w, d.z32, d.q32, d.r, 6);
+    }
+
     template <class TW, class TV, class TXA>
     int cg_loop(TXA* x, TV* r, TV* z, TV* p, TV* q, const TW* w, const double* m64, const float* m32, int maxit) {
         const int every = opt.check_every > 0 ? opt.check_every : 8;
@@ -658,7 +730,7 @@ struct Solver {
         while (done < maxit + every) {
             for (int k = 0; k < every; ++k) {
                 timer.mark(PH_SPMV, st);
-                MPS_COUNT_LAUNCH k_spmv<TW, TV, TV, 0><<<kRedBlocks, 256, 0, st>>>(d, w, p, q, nullptr, 0);
+                spmv_cg<TW, TV>(w, p, q);
                 timer.mark(PH_VEC, st);
                 const bool use_mg = std::is_same<TV, float>::value && mg_ready;
                 if (!use_mg)
@@ -675,7 +747,7 @@ struct Solver {
                 ++spmv_launches;
             }
             done += every;
-            if (pull_scal()) return -1;
+            if (stream_failed || pull_scal()) return -1;
             if (h_scal[S_CONV] != 0.0) break;
         }
         return (int)h_scal[S_ITER];
@@ -812,6 +884,8 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->mg_omega = 1.0;
     o->compress_rows = 1;
     o->mg_sweeps = 1;
+    o->matrix_free = 0;
+    o->spmv_stream = 1;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -819,6 +893,8 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (!param || !box || !out) return CCT_PARAMERR;
     MpsSolverOptions o;
     if (opt) o = *opt; else mps_solver_default_options(&o);
+    if (o.matrix_free != 0 && o.matrix_free != 4 && o.matrix_free != 8) return CCT_PARAMERR;
+    if (o.spmv_stream != 0 && o.spmv_stream != 1) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {
@@ -926,6 +1002,32 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_
     if (relres) *relres = S.h_scal[mps::S_BNORM] > 0 ? S.h_scal[mps::S_RNORM] / S.h_scal[mps::S_BNORM] : 0.0;
     if (host_r) return mps::cuda_status(cudaMemcpy(host_r, d.r, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
     return CCT_NOERR;
+}
+
+CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_x, float* host_y) {
+    if (!s || !host_x || !host_y) return CCT_PARAMERR;
+    mps::Solver& S = s->s;
+    mps::Dev& d = S.d;
+    if (S.fp64() || d.n <= 0) return CCT_PARAMERR;
+    if (kernel != 0 && kernel != 1 && kernel != 4 && kernel != 8) return CCT_PARAMERR;
+    if (kernel == 1 && !d.rows16) return CCT_PARAMERR;
+    const float* w = (const float*)d.nbrw;
+    cudaError_t e = cudaMemcpyAsync(d.p32, host_x, sizeof(float) * d.n, cudaMemcpyHostToDevice, S.st);
+    // MODE 0 returns at once after a converged solve: clear the flag (the next CG start sets it)
+    if (!e) e = cudaMemsetAsync(d.scal + mps::S_CONV, 0, sizeof(double), S.st);
+    if (e) return CCT_CUDAERR;
+    if (kernel == 0)
+        MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
+    else if (kernel == 1)
+        S.spmv_stream<0>(w, d.p32, d.q32, nullptr, 0);
+    else if (kernel == 4)
+        MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0, 4><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
+    else
+        MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0, 8><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
+    if (S.stream_failed) return CCT_CUDAERR;
+    e = cudaMemcpyAsync(host_y, d.q32, sizeof(float) * d.n, cudaMemcpyDeviceToHost, S.st);
+    if (!e) e = cudaStreamSynchronize(S.st);
+    return mps::cuda_status(e);
 }
 
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n) {

@@ -24,7 +24,8 @@ class MpsSolverOptions(C.Structure):
                 ("cg_rtol", C.c_double), ("cg_max_iter", C.c_int), ("ir_inner_rtol", C.c_double),
                 ("ir_max_outer", C.c_int), ("max_neighbours", C.c_int), ("check_every", C.c_int),
                 ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
-                ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int)]
+                ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int),
+                ("matrix_free", C.c_int), ("spmv_stream", C.c_int)]
 
 
 class MpsStepStats(C.Structure):
@@ -61,6 +62,7 @@ _SIGS = {
     "mps_solver_get_triangles": (C.c_int, [P, P]),
     "mps_solver_debug_residual": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_double)]),
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
+    "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
     "mps_solver_copy_pressure": (C.c_int, [P, P]),
     "mps_solver_stream": (C.c_int, [P, C.POINTER(P)]),
     "mps_solver_upload_state": (C.c_int, [P, P, P, P]),
@@ -185,6 +187,17 @@ class Solver:
         rel = C.c_double()
         _check(_lib().mps_solver_debug_residual(self.h, int(variant), _p(r), C.byref(rel)), "mps_solver_debug_residual")
         return r[:n], rel.value
+
+    def debug_spmv(self, kernel: int, x: np.ndarray) -> np.ndarray:
+        """One FP32 inner SpMV y = A x over the current rows with the named kernel
+        (0 register walk, 1 streamed, 4 / 8 matrix-free), solver order."""
+        n = self.state(sort_by_id=False)["id"].shape[0]
+        xs = np.ascontiguousarray(x, dtype=np.float32)
+        if xs.shape != (n,):
+            raise ValueError(f"x must have shape ({n},)")
+        y = np.zeros(n, np.float32)
+        _check(_lib().mps_solver_debug_spmv(self.h, int(kernel), _p(xs), _p(y)), "mps_solver_debug_spmv")
+        return y
 
     def pressure(self, njp: bool = False) -> dict:
         """PPE solve at the current state (CalculatePressureNJPCG if njp, else CalculatePressureCG)."""

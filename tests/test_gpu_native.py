@@ -10,6 +10,7 @@ import pytest
 import orc
 from simulation_project_gb300 import scenes
 from simulation_project_gb300.solver import Solver
+from simulation_project_gb300.types import MpsError
 
 pytestmark = pytest.mark.gpu
 
@@ -144,12 +145,66 @@ def test_double_float_residual_matches_fp64_residual():
     assert abs(reldf - rel64) <= 1e-3 * rel64 + 1e-12
 
 
+@pytest.mark.parametrize("mf", [4, 8])
+def test_matrix_free_spmv_gives_identical_results(mf):
+    """Matrix-free inner SpMV: each weight recomputed from the FP32 positions by the
+    neighbour pass's own expression, summed in the same order, so the FP32-IR step is
+    bit-identical to the stored-weight SpMV."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=4, drag_index=0.5)
+    a = Solver(sc, precision="fp32_ir", matrix_free=mf)
+    b = Solver(sc, precision="fp32_ir", matrix_free=0, spmv_stream=0)
+    for i in range(3):
+        sa, sb = a.step(i), b.step(i)
+        assert sa["error_flags"] == 0 and sa["cg_relres"] <= 1e-8
+        assert sa["cg_iterations"] == sb["cg_iterations"] and sa["cg_relres"] == sb["cg_relres"]
+    x, y = a.state(), b.state()
+    assert np.array_equal(x["press"], y["press"]) and np.array_equal(x["pos"], y["pos"])
+
+
+def test_spmv_kernels_give_identical_rows():
+    """The register walk, the streamed kernel and both matrix-free unrolls compute
+    every row of y = A x in the same order: bit-identical y."""
+    sc = scenes.rotating_bucket(l0=0.006, n_drag=4, drag_index=0.5)
+    s = Solver(sc, precision="fp32_ir")
+    for i in range(2):
+        s.step(i)
+    n = s.state(sort_by_id=False)["id"].shape[0]
+    x = np.random.default_rng(7).standard_normal(n).astype(np.float32)
+    y0 = s.debug_spmv(0, x)
+    assert np.isfinite(y0).all() and np.count_nonzero(y0) > n // 2
+    for k in (1, 4, 8):
+        yk = s.debug_spmv(k, x)
+        assert np.array_equal(y0.view(np.uint32), yk.view(np.uint32)), (k, np.abs(yk - y0).max())
+
+
+def test_streamed_spmv_step_matches():
+    """FP32-IR steps with the streamed SpMV: same row values, the CG's p.q sums in
+    another order (persistent grid), so the step agrees to the solve tolerance."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=4, drag_index=0.5)
+    a = Solver(sc, precision="fp32_ir", spmv_stream=1)
+    b = Solver(sc, precision="fp32_ir", spmv_stream=0)
+    for i in range(3):
+        sa, sb = a.step(i), b.step(i)
+        assert sa["error_flags"] == 0 and sa["cg_relres"] <= 1e-8, sa
+        assert abs(sa["cg_iterations"] - sb["cg_iterations"]) <= 2
+    pa, pb = a.state()["press"], b.state()["press"]
+    assert np.abs(pa - pb).max() <= 1e-6 * np.abs(pb).max()
+
+
+def test_spmv_options_are_checked():
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=0)
+    for bad in ({"matrix_free": 3}, {"spmv_stream": 2}):
+        with pytest.raises(MpsError) as e:
+            Solver(sc, precision="fp32_ir", **bad)
+        assert e.value.status == 2   # CCT_PARAMERR
+
+
 def test_compressed_rows_give_identical_results():
     """16-bit column offsets (the default) and 32-bit columns: same columns in the same
     order, so the FP32-IR step is bit-identical."""
     sc = scenes.rotating_bucket(l0=0.008, n_drag=4, drag_index=0.5)
-    a = Solver(sc, precision="fp32_ir", compress_rows=1)
-    b = Solver(sc, precision="fp32_ir", compress_rows=0)
+    a = Solver(sc, precision="fp32_ir", compress_rows=1, spmv_stream=0)
+    b = Solver(sc, precision="fp32_ir", compress_rows=0, spmv_stream=0)
     for i in range(3):
         sa, sb = a.step(i), b.step(i)
         assert sa["cg_iterations"] == sb["cg_iterations"] and sa["cg_relres"] == sb["cg_relres"]
