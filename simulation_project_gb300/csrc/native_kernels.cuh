@@ -991,162 +991,6 @@ __global__ void __launch_bounds__(256, MF == 0 ? 8 : (MF <= 4 ? 5 : 3))
     }
 }
 
-// ---------------------------------------------------------------------------
-// Streamed FP32 SpMV of the inner CG: the 16-bit columns and FP32 weights of each
-// slice reach shared memory by bulk (TMA) copies, so the loads in flight do not
-// hold registers.  Every warp owns a ring of SS stages of SC entries (SC x 64 B of
-// columns + SC x 128 B of weights per stage, one mbarrier each); lane 0 keeps the
-// ring full, running ahead across the warp's slices (gw, gw + nw, ...), while all
-// lanes gather x and accumulate the stage in entry order, so every row value is
-// bit-identical to the register walk.  32-bit slices (skmax = -1) take the register
-// walk.  A stage that does not land within the poll limit sets
-// MPS_ERR_STAGE_TIMEOUT; the warp then waits (bounded) for its copies in flight and
-// finishes on the register walk.  MODE 0 / 2 as in k_spmv.
-// ---------------------------------------------------------------------------
-template <int SC> constexpr int stream_stage_bytes() { return SC * 192; }
-template <int SC, int SS, int W> constexpr int stream_smem_bytes() { return W * SS * stream_stage_bytes<SC>(); }
-
-template <int MODE, int SC, int SS, int W, int MINB>
-__global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_constant__ Dev d,
-                                                                  const float* __restrict__ w,
-                                                                  const float* __restrict__ x, float* __restrict__ y,
-                                                                  const double* __restrict__ b, int slot) {
-    static_assert(MODE == 0 || MODE == 2, "FP32 modes only");
-    static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
-    if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
-    extern __shared__ __align__(128) unsigned char stream_smem[];
-    __shared__ __align__(8) unsigned long long bars[W][SS];
-    constexpr int SB = stream_stage_bytes<SC>();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned char* ring = stream_smem + warp * SS * SB;
-    unsigned long long* bar = bars[warp];
-    if (lane == 0)
-        for (int st = 0; st < SS; ++st) mbar_init(&bar[st], 1);
-    __syncwarp();
-
-    const int gw = blockIdx.x * W + warp;
-    const int nw = gridDim.x * W;
-    const int nsl = (d.n + 31) >> 5;
-    const int K = d.K;
-    // producer: next chunk to copy is chunk pc of slice ps (pk entries, pn chunks)
-    int ps = gw - nw, pc = 0, pk = 0, pn = 0;
-    auto next_slice = [&]() {
-        do {
-            ps += nw;
-            pk = ps < nsl ? d.skmax[ps] : 0;
-        } while (ps < nsl && pk <= 0);
-        pc = 0;
-        pn = (pk + SC - 1) / SC;
-    };
-    next_slice();
-    unsigned q_issue = 0, q_cons = 0;
-    bool streaming = true;
-    const unsigned long long pol = l2_evict_first_policy();
-    auto refill = [&]() {
-        while (streaming && ps < nsl && q_issue - q_cons < (unsigned)SS) {
-            const int st = (int)(q_issue % SS);
-            const int k0 = pc * SC;
-            const int ne = min(SC, pk - k0);
-            if (lane == 0) {
-                const size_t e0 = ((size_t)ps * K + k0) * 32;
-                fence_proxy_async_smem();
-                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * 192u);
-                bulk_copy_g2s_hint(ring + st * SB, d.nbr16 + e0, (unsigned)ne * 64u, &bar[st], pol);
-                bulk_copy_g2s_hint(ring + st * SB + SC * 64, w + e0, (unsigned)ne * 128u, &bar[st], pol);
-            }
-            ++q_issue;
-            if (++pc == pn) next_slice();
-        }
-    };
-    // gives up streaming: bounded wait for the copies still in flight into this ring
-    auto abandon = [&]() {
-        if (lane == 0) atomicOr(d.err, MPS_ERR_STAGE_TIMEOUT);
-        for (unsigned q = q_cons; q != q_issue; ++q)
-            mbar_wait_parity_bounded(&bar[q % SS], (q / SS) & 1u, 1ll << 24);
-        streaming = false;
-        q_cons = q_issue;
-    };
-
-    const double coef = d.c.coef_lap;
-    double part0 = 0.0, part1 = 0.0;
-    float partw = 0.f;
-    for (int sl = gw; sl < nsl; sl += nw) {
-        const int i = sl * 32 + lane;
-        const bool row = i < d.n;
-        const bool in = row && d.inner[i];
-        const int cnt = in ? d.nbr_cnt[i] : 0;
-        const int km = d.skmax[sl];
-        const size_t base = (size_t)sl * K * 32 + lane;
-        float acc = 0.f;
-        bool done = false;
-        if (km >= 0 && streaming) {
-            if (km > 0) {
-                const int nc = (km + SC - 1) / SC;
-                const int r0 = sl * 32;
-                for (int c = 0; c < nc; ++c) {
-                    refill();
-                    const int st = (int)(q_cons % SS);
-                    if (!__all_sync(0xffffffffu, mbar_wait_parity_bounded(&bar[st], (q_cons / SS) & 1u, 1ll << 20))) {
-                        abandon();
-                        break;
-                    }
-                    const unsigned short* cs = (const unsigned short*)(ring + st * SB);
-                    const float* ws = (const float*)(ring + st * SB + SC * 64);
-                    const int k0 = c * SC;
-#pragma unroll
-                    for (int g = 0; g < SC; g += 8) {
-                        int j[8];
-                        float wv[8];
-#pragma unroll
-                        for (int u = 0; u < 8; ++u) {
-                            j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
-                            wv[u] = ws[(g + u) * 32 + lane];
-                        }
-#pragma unroll
-                        for (int u = 0; u < 8; ++u)
-                            if (k0 + g + u < cnt) acc = __fmaf_rn(wv[u], __ldg(x + j[u]), acc);
-                    }
-                    __syncwarp();
-                    ++q_cons;
-                }
-            }
-            done = streaming;
-        }
-        if (!done) {
-            // 32-bit slice, or streaming given up: the register walk
-            const int kmax = __reduce_max_sync(0xffffffffu, cnt);
-            const int sb = (km >= 0) ? sl * 32 : -1;
-            acc = sb >= 0 ? sell_row_dot<true, float>(d, w, x, base, cnt, kmax, sb)
-                          : sell_row_dot<false, float>(d, w, x, base, cnt, kmax, sb);
-        }
-        if (!row) continue;
-        if (!in) {
-            y[i] = 0.f;
-            continue;
-        }
-        const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
-        y[i] = (float)yi;
-        if (MODE == 0) {
-            partw += x[i] * (float)yi;
-        } else {
-            part0 += (double)x[i] * yi;
-            part1 += (double)x[i] * b[i];
-        }
-    }
-    if (MODE == 0) part0 = (double)partw;
-    double v[2] = {part0, part1}, out[2];
-    if (grid_reduce<2, typename std::conditional<MODE == 0, float, double>::type>(v, d.red, d.red_count + slot, out) &&
-        threadIdx.x == 0) {
-        if (MODE == 0) {
-            d.scal[S_PQ] = out[0];
-            d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
-        } else {
-            d.scal[S_LS0] = out[0];
-            d.scal[S_LS1] = out[1];
-        }
-    }
-}
-
 // FP32 copy of the wall vertices (after the walls moved)
 __global__ void k_tri_to_float(const __grid_constant__ Dev d) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1248,6 +1092,289 @@ __global__ void __launch_bounds__(256, 8) k_residual_df(const __grid_constant__ 
             continue;
         }
         const double acc = (double)S + (double)C;
+        const double ri = b[i] - (d.diag[i] * x[i] - d.c.coef_lap * acc);
+        r[i] = ri;
+        part0 += ri * ri;
+        part1 += b[i] * b[i];
+    }
+    double v[2] = {part0, part1}, out[2];
+    if (grid_reduce<2>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        d.scal[S_RR] = out[0];
+        d.scal[S_RNORM] = sqrt(out[0]);
+        d.scal[S_BNORM] = sqrt(out[1]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Streamed SELL rows: the 16-bit columns and FP32 weights of each slice reach shared
+// memory by bulk (TMA) copies, so the loads in flight hold no registers and the
+// matrix does not pass through L1 (the x gathers keep it).  Every warp owns a ring of
+// SS stages of SC entries (SC x 64 B of columns + SC x 128 B of weights per stage,
+// one mbarrier each); lane 0 keeps the ring full, running ahead across the warp's
+// slices (gw, gw + nw, ...), and all lanes consume a stage in entry order.  The
+// copies carry an L2 evict-first policy (the CG vectors and the multilevel data stay
+// resident).  A stage that does not land within the poll limit sets
+// MPS_ERR_STAGE_TIMEOUT; the warp then waits (bounded) for its copies in flight and
+// finishes on the register walk.  32-bit slices (skmax = -1) take the register walk.
+// ---------------------------------------------------------------------------
+template <int SC> constexpr int stream_stage_bytes() { return SC * 192; }
+template <int SC, int SS, int W> constexpr int stream_smem_bytes() { return W * SS * stream_stage_bytes<SC>(); }
+
+template <int SC, int SS>
+struct SliceRing {
+    static constexpr int SB = stream_stage_bytes<SC>();
+    unsigned char* ring;
+    unsigned long long* bar;
+    const unsigned short* cols;
+    const float* w;
+    const int* skmax;
+    unsigned* err;
+    int nsl, nw, K, lane;
+    int ps, pc, pk, pn;          // producer: next chunk pc of slice ps (pk entries, pn chunks)
+    unsigned q_issue, q_cons;
+    bool streaming;
+    unsigned long long pol;
+
+    __device__ void init(const Dev& d, const float* w_, unsigned char* ring_, unsigned long long* bar_, int gw,
+                         int nw_) {
+        ring = ring_;
+        bar = bar_;
+        cols = d.nbr16;
+        w = w_;
+        skmax = d.skmax;
+        err = d.err;
+        nsl = (d.n + 31) >> 5;
+        nw = nw_;
+        K = d.K;
+        lane = threadIdx.x & 31;
+        if (lane == 0)
+            for (int st = 0; st < SS; ++st) mbar_init(&bar[st], 1);
+        __syncwarp();
+        ps = gw - nw;
+        q_issue = q_cons = 0;
+        streaming = true;
+        pol = l2_evict_first_policy();
+        next_slice();
+    }
+    __device__ void next_slice() {
+        do {
+            ps += nw;
+            pk = ps < nsl ? skmax[ps] : 0;
+        } while (ps < nsl && pk <= 0);
+        pc = 0;
+        pn = (pk + SC - 1) / SC;
+    }
+    // issue copies until SS stages are in flight or the warp's slices are exhausted
+    __device__ void refill() {
+        while (streaming && ps < nsl && q_issue - q_cons < (unsigned)SS) {
+            const int st = (int)(q_issue % SS);
+            const int k0 = pc * SC;
+            const int ne = min(SC, pk - k0);
+            if (lane == 0) {
+                const size_t e0 = ((size_t)ps * K + k0) * 32;
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * 192u);
+                bulk_copy_g2s_hint(ring + st * SB, cols + e0, (unsigned)ne * 64u, &bar[st], pol);
+                bulk_copy_g2s_hint(ring + st * SB + SC * 64, w + e0, (unsigned)ne * 128u, &bar[st], pol);
+            }
+            ++q_issue;
+            if (++pc == pn) next_slice();
+        }
+    }
+    // waits for the next stage; false: streaming abandoned (the caller recomputes the
+    // slice on the register walk)
+    __device__ bool acquire(const unsigned short*& cs, const float*& ws) {
+        refill();
+        const int st = (int)(q_cons % SS);
+        if (!__all_sync(0xffffffffu, mbar_wait_parity_bounded(&bar[st], (q_cons / SS) & 1u, 1ll << 20))) {
+            if (lane == 0) atomicOr(err, MPS_ERR_STAGE_TIMEOUT);
+            for (unsigned q = q_cons; q != q_issue; ++q)
+                mbar_wait_parity_bounded(&bar[q % SS], (q / SS) & 1u, 1ll << 24);
+            streaming = false;
+            q_cons = q_issue;
+            return false;
+        }
+        cs = (const unsigned short*)(ring + st * SB);
+        ws = (const float*)(ring + st * SB + SC * 64);
+        return true;
+    }
+    // the warp is done reading the stage
+    __device__ void release() {
+        __syncwarp();
+        ++q_cons;
+    }
+};
+
+// FP32 SpMV of the inner CG over streamed rows, MODE 0 / 2 as in k_spmv.  Each row
+// accumulates its entries in order with one FMA each, so every row value is
+// bit-identical to the register walk.
+template <int MODE, int SC, int SS, int W, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_constant__ Dev d,
+                                                             const float* __restrict__ w,
+                                                             const float* __restrict__ x, float* __restrict__ y,
+                                                             const double* __restrict__ b, int slot) {
+    static_assert(MODE == 0 || MODE == 2, "FP32 modes only");
+    static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
+    if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
+    extern __shared__ __align__(128) unsigned char stream_smem[];
+    __shared__ __align__(8) unsigned long long bars[W][SS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
+    SliceRing<SC, SS> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS>::SB, bars[warp], gw, nw);
+
+    const double coef = d.c.coef_lap;
+    double part0 = 0.0, part1 = 0.0;
+    float partw = 0.f;
+    for (int sl = gw; sl < R.nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int km = d.skmax[sl];
+        float acc = 0.f;
+        bool done = false;
+        if (km >= 0 && R.streaming) {
+            const int nc = (km + SC - 1) / SC;
+            const int r0 = sl * 32;
+            for (int c = 0; c < nc; ++c) {
+                const unsigned short* cs;
+                const float* ws;
+                if (!R.acquire(cs, ws)) break;
+                const int k0 = c * SC;
+#pragma unroll
+                for (int g = 0; g < SC; g += 8) {
+                    int j[8];
+                    float wv[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
+                        wv[u] = ws[(g + u) * 32 + lane];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u)
+                        if (k0 + g + u < cnt) acc = __fmaf_rn(wv[u], __ldg(x + j[u]), acc);
+                }
+                R.release();
+            }
+            done = R.streaming;
+        }
+        if (!done) {
+            // 32-bit slice, or streaming given up: the register walk
+            const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+            const size_t base = (size_t)sl * d.K * 32 + lane;
+            acc = km >= 0 ? sell_row_dot<true, float>(d, w, x, base, cnt, kmax, sl * 32)
+                          : sell_row_dot<false, float>(d, w, x, base, cnt, kmax, -1);
+        }
+        if (!row) continue;
+        if (!in) {
+            y[i] = 0.f;
+            continue;
+        }
+        const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
+        y[i] = (float)yi;
+        if (MODE == 0) {
+            partw += x[i] * (float)yi;
+        } else {
+            part0 += (double)x[i] * yi;
+            part1 += (double)x[i] * b[i];
+        }
+    }
+    if (MODE == 0) part0 = (double)partw;
+    double v[2] = {part0, part1}, out[2];
+    if (grid_reduce<2, typename std::conditional<MODE == 0, float, double>::type>(v, d.red, d.red_count + slot, out) &&
+        threadIdx.x == 0) {
+        if (MODE == 0) {
+            d.scal[S_PQ] = out[0];
+            d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
+        } else {
+            d.scal[S_LS0] = out[0];
+            d.scal[S_LS1] = out[1];
+        }
+    }
+}
+
+// Refinement residual r = b - A x over streamed rows in double-float arithmetic, the
+// same per-entry operations and accumulator order as k_residual_df (entries of even
+// index into the first (hi, lo) pair, odd into the second, merged at the end), so r
+// is bit-identical to it.  Norms -> S_RR / S_RNORM and ||b|| -> S_BNORM.
+template <int SC, int SS, int W, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_constant__ Dev d,
+                                                                 const float* __restrict__ w,
+                                                                 const double* __restrict__ x,
+                                                                 double* __restrict__ r,
+                                                                 const double* __restrict__ b, int slot) {
+    static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
+    extern __shared__ __align__(128) unsigned char stream_smem[];
+    __shared__ __align__(8) unsigned long long bars[W][SS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
+    SliceRing<SC, SS> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS>::SB, bars[warp], gw, nw);
+    const float* __restrict__ xh = d.xh;
+    const float* __restrict__ xl = d.xl;
+
+    double part0 = 0.0, part1 = 0.0;
+    for (int sl = gw; sl < R.nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int km = d.skmax[sl];
+        float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
+        bool done = false;
+        if (km >= 0 && R.streaming) {
+            const int nc = (km + SC - 1) / SC;
+            const int r0 = sl * 32;
+            for (int c = 0; c < nc; ++c) {
+                const unsigned short* cs;
+                const float* ws;
+                if (!R.acquire(cs, ws)) break;
+                const int k0 = c * SC;
+#pragma unroll
+                for (int g = 0; g < SC; g += 8) {
+                    int j[8];
+                    float wv[8], h[8], l[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
+                        wv[u] = ws[(g + u) * 32 + lane];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const bool a = k0 + g + u < cnt;
+                        h[u] = a ? xh[j[u]] : 0.f;
+                        l[u] = a ? xl[j[u]] : 0.f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        if (k0 + g + u < cnt) {
+                            const float p = __fmul_rn(wv[u], h[u]);
+                            const float pe = __fmaf_rn(wv[u], h[u], -p);
+                            if (u & 1) df_add(S1, C1, p, __fmaf_rn(wv[u], l[u], pe));
+                            else df_add(S0, C0, p, __fmaf_rn(wv[u], l[u], pe));
+                        }
+                    }
+                }
+                R.release();
+            }
+            if (R.streaming) {
+                df_add(S0, C0, S1, C1);
+                done = true;
+            }
+        }
+        if (!done) {
+            const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+            const size_t base = (size_t)sl * d.K * 32 + lane;
+            if (km >= 0) df_row_sum<true>(d, w, xh, xl, base, cnt, kmax, sl * 32, S0, C0);
+            else df_row_sum<false>(d, w, xh, xl, base, cnt, kmax, -1, S0, C0);
+        }
+        if (!row) continue;
+        if (!in) {
+            r[i] = 0.0;
+            continue;
+        }
+        const double acc = (double)S0 + (double)C0;
         const double ri = b[i] - (d.diag[i] * x[i] - d.c.coef_lap * acc);
         r[i] = ri;
         part0 += ri * ri;

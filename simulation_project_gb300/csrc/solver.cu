@@ -659,24 +659,40 @@ struct Solver {
     // copies in flight.  Dynamic shared memory opt-in and a persistent grid of
     // SMs x resident CTAs, set up on first use.
     static constexpr int kSsEntries = 8, kSsStages = 2, kSsWarps = 8, kSsMinBlocks = 4;
-    int stream_grid = 0;
+    static constexpr int kSsSmem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps>();
+    int spmv_grid = 0, resid_grid = 0;
     bool stream_failed = false;
-    int stream_blocks() {
-        if (stream_grid == 0) {
-            constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps>();
-            auto k0 = k_spmv_stream<0, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
-            auto k2 = k_spmv_stream<2, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
-            if (cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) ||
-                cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
-                return -1;
+    // SMs x resident CTAs of a streamed kernel (after its shared-memory opt-in)
+    template <class F>
+    int persistent_grid(F kernel, int& cached) {
+        if (cached == 0) {
             int dev = 0, sms = 0, per_sm = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k0, kSsWarps * 32, smem)) return -1;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSsWarps * 32, kSsSmem)) return -1;
             // the reduction buffer holds 2 partials per CTA for up to 2 x kRedBlocks CTAs
-            stream_grid = std::max(1, std::min(sms * std::max(per_sm, 1), 2 * kRedBlocks));
+            cached = std::max(1, std::min(sms * std::max(per_sm, 1), 2 * kRedBlocks));
         }
-        return stream_grid;
+        return cached;
+    }
+    int stream_blocks() {
+        if (spmv_grid == 0) {
+            auto k0 = k_spmv_stream<0, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            auto k2 = k_spmv_stream<2, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            if (cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, kSsSmem) ||
+                cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, kSsSmem))
+                return -1;
+            return persistent_grid(k0, spmv_grid);
+        }
+        return spmv_grid;
+    }
+    int resid_blocks() {
+        if (resid_grid == 0) {
+            auto k = k_residual_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kSsSmem)) return -1;
+            return persistent_grid(k, resid_grid);
+        }
+        return resid_grid;
     }
     template <int MODE>
     void spmv_stream(const float* w, const float* x, float* y, const double* b, int slot) {
@@ -685,9 +701,8 @@ struct Solver {
             stream_failed = true;
             return;
         }
-        constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps>();
         MPS_COUNT_LAUNCH k_spmv_stream<MODE, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>
-            <<<g, kSsWarps * 32, smem, st>>>(d, w, x, y, b, slot);
+            <<<g, kSsWarps * 32, kSsSmem, st>>>(d, w, x, y, b, slot);
     }
     // the streamed kernel needs the 16-bit slices of this step
     bool use_stream() const { return opt.spmv_stream != 0 && d.rows16; }
@@ -779,9 +794,20 @@ struct Solver {
     }
 
     // r = rhs - A press (FP32 weights) in double-float arithmetic; norms to the scalars
-    void residual_df(const float* w) {
+    // (rows streamed through shared memory over the 16-bit slices, else the register walk)
+    void residual_df(const float* w, bool stream = true) {
         MPS_COUNT_LAUNCH k_split_x<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.xh, d.xl);
-        MPS_COUNT_LAUNCH k_residual_df<<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        if (stream && use_stream()) {
+            const int g = resid_blocks();
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH k_residual_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>
+                <<<g, kSsWarps * 32, kSsSmem, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        } else {
+            MPS_COUNT_LAUNCH k_residual_df<<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        }
     }
 
     // FP32 Jacobi-PCG inside FP64 iterative refinement
@@ -798,7 +824,7 @@ struct Solver {
         for (;;) {
             if (!(outer == 0 && residual_ready)) residual_df(w);
             residual_ready = false;
-            if (pull_scal()) return CCT_CUDAERR;
+            if (stream_failed || pull_scal()) return CCT_CUDAERR;
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
                 h_nnz[1] = h_scal[S_NNZ1];
@@ -997,8 +1023,8 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_
         MPS_COUNT_LAUNCH mps::k_spmv<float, double, double, 1><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.press, d.r,
                                                                                                   d.rhs, 2);
     else
-        S.residual_df(w);
-    if (S.pull_scal()) return CCT_CUDAERR;
+        S.residual_df(w, variant == 1);
+    if (S.stream_failed || S.pull_scal()) return CCT_CUDAERR;
     if (relres) *relres = S.h_scal[mps::S_BNORM] > 0 ? S.h_scal[mps::S_RNORM] / S.h_scal[mps::S_BNORM] : 0.0;
     if (host_r) return mps::cuda_status(cudaMemcpy(host_r, d.r, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
     return CCT_NOERR;

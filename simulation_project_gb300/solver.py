@@ -181,7 +181,8 @@ class Solver:
         return out
 
     def debug_residual(self, variant: int):
-        """(r, ||r|| / ||b||) of the current state: variant 0 FP64 kernel, 1 double-float."""
+        """(r, ||r|| / ||b||) of the current state: variant 0 FP64 kernel, 1 the
+        double-float kernel the solver uses, 2 the double-float register walk."""
         n = self.state(sort_by_id=False)["id"].shape[0]
         r = np.zeros(max(n, 1))
         rel = C.c_double()

@@ -177,6 +177,20 @@ def test_spmv_kernels_give_identical_rows():
         assert np.array_equal(y0.view(np.uint32), yk.view(np.uint32)), (k, np.abs(yk - y0).max())
 
 
+def test_streamed_residual_is_bit_identical():
+    """The double-float refinement residual over streamed rows does the register
+    walk's operations in the same order: identical r and norms."""
+    sc = scenes.rotating_bucket(l0=0.006, n_drag=4, drag_index=0.5)
+    s = Solver(sc, precision="fp32_ir")
+    for i in range(2):
+        s.step(i)
+    r1, rel1 = s.debug_residual(1)
+    r2, rel2 = s.debug_residual(2)
+    assert np.array_equal(r1, r2) and rel1 == rel2
+    r0, rel0 = s.debug_residual(0)
+    assert np.abs(r1 - r0).max() <= 1e-10 * np.abs(s.debug_ppe()["rhs"]).max()
+
+
 def test_streamed_spmv_step_matches():
     """FP32-IR steps with the streamed SpMV: same row values, the CG's p.q sums in
     another order (persistent grid), so the step agrees to the solve tolerance."""
