@@ -18,7 +18,6 @@ namespace mps {
 
 constexpr int kMgMaxLevels = 10;
 constexpr int kMgMaxDense = 128;
-constexpr int kMgAsmThreads = 64;      // a cell holds ~50-70 particles
 
 struct MgLevel {
     int n;             // aggregates
@@ -42,6 +41,9 @@ struct Mg {
     int* agg1;         // [n] particle -> level-1 aggregate
     unsigned* pcc;     // [n] cell coordinates of the particle, 10 bits each (x<<20 | y<<10 | z),
                        //     bit 31 set for an interior particle
+    float* part;       // [27 n] level-1 assembly: slot sums of a (slice, cell) row segment,
+                       //     stored at the segment's first row
+    double* partd;     // [n] diagonal sum of that segment
 };
 
 __device__ __forceinline__ void mg_decode(int c, int gy, int gz, int& x, int& y, int& z) {
@@ -115,79 +117,113 @@ __global__ void k_mg_particles(const __grid_constant__ Dev d, const __grid_const
     mg.agg1[i] = mg.L[1].cmap[c];
 }
 
-// Level-1 Galerkin stencil: CTA per aggregate (cell).  A1[I, J] = sum over interior
-// i in I and interior neighbours j in J of A_ij; A1[I, I] adds the diagonals.  Each
-// thread owns one shared-memory column of 27 partial sums (no atomics, fixed order).
+// Level-1 Galerkin stencil, pass 1 of 2: warp per 32-row slice, lane per row (the
+// SELL walk: 8 entries' columns and weights in flight, 16-bit columns where the slice
+// has them).  Each lane sums its row's interior-interior entries per stencil slot in
+// its own shared-memory column; the slot follows from one subtraction of packed cell
+// coordinates (each field offset by one, so a neighbour cell gives fields 0..2 and no
+// borrow).  The lanes of each cell (contiguous rows) are then summed by a segmented
+// shuffle tree, and the segment's first lane stores the 27 slot sums and the
+// diagonal sum at its row.  Fixed orders: deterministic.
+constexpr int kMgAsmWarps = 4;
 template <class TW>
-__global__ void __launch_bounds__(kMgAsmThreads) k_mg_assemble1(const __grid_constant__ Dev d,
-                                                               const __grid_constant__ Mg mg,
-                                                               const TW* __restrict__ w) {
-    __shared__ float acc[27][kMgAsmThreads];
-    __shared__ double dsum[kMgAsmThreads];
-    __shared__ float slot_sum[28];
+__global__ void __launch_bounds__(kMgAsmWarps * 32) k_mg_assemble_rows(const __grid_constant__ Dev d,
+                                                                       const __grid_constant__ Mg mg,
+                                                                       const TW* __restrict__ w) {
+    __shared__ float acc[kMgAsmWarps][27][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    float (*A)[32] = acc[wib];
+    const int gw = blockIdx.x * kMgAsmWarps + wib, nw = gridDim.x * kMgAsmWarps;
+    const int nsl = (d.n + 31) >> 5;
+    for (int sl = gw; sl < nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+        const unsigned pi = (row ? mg.pcc[i] : 0u) & 0x3fffffffu;
+        const int seg = row ? mg.agg1[i] : -1;
+        const int sb = (sizeof(TW) == 4 && d.rows16) ? d.sbase[sl] : -1;
+        const size_t base = (size_t)sl * d.K * 32 + lane;
+#pragma unroll
+        for (int t = 0; t < 27; ++t) A[t][lane] = 0.f;
+        __syncwarp();
+        for (int k = 0; k < kmax; k += 8) {
+            int jj[8];
+            float wv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const size_t e = base + (size_t)min(k + u, kmax - 1) * 32;
+                jj[u] = sb >= 0 ? sell_col<true>(d, e, sb) : sell_col<false>(d, e, sb);
+                wv[u] = (float)__ldcs(w + e);
+            }
+            unsigned pq[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) pq[u] = k + u < cnt ? mg.pcc[jj[u]] : 0u;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                if (!(pq[u] & 0x80000000u)) continue;   // not interior, or no entry
+                const unsigned dd = (pq[u] & 0x3fffffffu) + 0x00100401u - pi;
+                const unsigned fx = dd >> 20, fy = (dd >> 10) & 1023u, fz = dd & 1023u;
+                if (fx <= 2u && fy <= 2u && fz <= 2u) A[fx * 9 + fy * 3 + fz][lane] += wv[u];
+            }
+        }
+        __syncwarp();
+        // segmented sums over the lanes of each cell, into the segment's first lane
+        const int prev = __shfl_up_sync(0xffffffffu, seg, 1);
+        const bool head = row && seg >= 0 && (lane == 0 || prev != seg);
+        bool same[5];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const int o = 1 << q;
+            const int sn = __shfl_down_sync(0xffffffffu, seg, o);
+            same[q] = lane + o < 32 && sn == seg;
+        }
+        double ds = in ? d.diag[i] : 0.0;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const double t = __shfl_down_sync(0xffffffffu, ds, 1 << q);
+            if (same[q]) ds += t;
+        }
+        if (head) mg.partd[i] = ds;
+        for (int t = 0; t < 27; ++t) {
+            float v = A[t][lane];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) {
+                const float x = __shfl_down_sync(0xffffffffu, v, 1 << q);
+                if (same[q]) v += x;
+            }
+            if (head) mg.part[(size_t)i * 27 + t] = v;
+        }
+        __syncwarp();
+    }
+}
+
+// Level-1 Galerkin stencil, pass 2 of 2: warp per level-1 aggregate (cell) sums the
+// segments of its rows in slice order (lane s: slot s, lane 27: the diagonals) and
+// stores A1[I, .] = -coef * slot sums, with the diagonal sum added to the centre.
+__global__ void k_mg_assemble_cells(const __grid_constant__ Dev d, const __grid_constant__ Mg mg) {
     const MgLevel& L1 = mg.L[1];
-    const int I = blockIdx.x;
-    if (I >= L1.n) return;
-    const int tid = threadIdx.x;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I >= L1.n) return;   // warp-uniform
     const int c = L1.ccell[I];
-    int cx, cy, cz;
-    mg_decode(c, d.box.m_GridSize.y, d.box.m_GridSize.z, cx, cy, cz);
-    for (int s = 0; s < 27; ++s) acc[s][tid] = 0.f;
-    double ds = 0.0;
     const int b = d.cstart[c], e = d.cend[c];
-    for (int i = b + tid; i < e; i += kMgAsmThreads) {
-        if (!d.inner[i]) continue;
-        ds += d.diag[i];
-        const int cnt = d.nbr_cnt[i];
-        for (int k = 0; k < cnt; k += 4) {
-            // four entries' loads in flight before the dependent gathers
-            int jj[4];
-            float wv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const bool a = k + u < cnt;
-                const size_t ek = sell_index(i, a ? k + u : k, d.K);
-                jj[u] = a ? d.nbr[ek] : -1;
-                wv[u] = a ? (float)w[ek] : 0.f;
-            }
-            unsigned pq[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) pq[u] = jj[u] >= 0 ? mg.pcc[jj[u]] : 0u;
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const unsigned pj = pq[u];
-                if (!(pj & 0x80000000u)) continue;   // not interior (or no entry)
-                const int dx = (int)((pj >> 20) & 1023u) - cx, dy = (int)((pj >> 10) & 1023u) - cy,
-                          dz = (int)(pj & 1023u) - cz;
-                if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;
-                acc[(dx + 1) * 9 + (dy + 1) * 3 + (dz + 1)][tid] += wv[u];
-            }
+    float v = 0.f;
+    double ds = 0.0;
+    if (e > b) {
+        for (int sl = b >> 5; sl <= (e - 1) >> 5; ++sl) {
+            const int h = sl == (b >> 5) ? b : sl * 32;
+            if (lane < 27) v += mg.part[(size_t)h * 27 + lane];
+            else if (lane == 27) ds += mg.partd[h];
         }
     }
-    dsum[tid] = ds;
-    __syncthreads();
-    const int warp = tid >> 5, lane = tid & 31;
-    for (int s = warp; s < 28; s += kMgAsmThreads / 32) {
-        if (s < 27) {
-            float v = 0.f;
-            for (int q = lane; q < kMgAsmThreads; q += 32) v += acc[s][q];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) slot_sum[s] = v;
-        } else {
-            double v = 0.0;
-            for (int q = lane; q < kMgAsmThreads; q += 32) v += dsum[q];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) slot_sum[27] = (float)v;
-        }
-    }
-    __syncthreads();
-    if (tid < 27) {
+    const float dsum = (float)__shfl_sync(0xffffffffu, ds, 27);
+    const float centre = __shfl_sync(0xffffffffu, v, 13);
+    if (lane < 27) {
         const float coef = (float)d.c.coef_lap;
-        const float v = tid == 13 ? slot_sum[27] - coef * slot_sum[13] : -coef * slot_sum[tid];
-        L1.a[(size_t)I * 27 + tid] = v;
-        if (tid == 13) L1.dinv[I] = v > 0.f ? 1.f / v : 0.f;
+        const float a = lane == 13 ? dsum - coef * centre : -coef * v;
+        L1.a[(size_t)I * 27 + lane] = a;
+        if (lane == 13) L1.dinv[I] = a > 0.f ? 1.f / a : 0.f;
     }
 }
 

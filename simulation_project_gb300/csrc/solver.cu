@@ -363,6 +363,7 @@ struct Solver {
         mg_grid_levels = std::min(l, kMgMaxLevels);
         e = e ? e : mk(&mg.ainv, (size_t)kMgMaxDense * kMgMaxDense);
         e = e ? e : mk(&mg.agg1, (size_t)nmax); e = e ? e : mk(&mg.pcc, (size_t)nmax);
+        e = e ? e : mk(&mg.part, 27 * (size_t)nmax); e = e ? e : mk(&mg.partd, (size_t)nmax);
         e = e ? e : mk(&mg_flag, (size_t)d.cells + 1); e = e ? e : mk(&mg_counts, (size_t)kMgMaxLevels + 1);
         if (e) return CCT_MEMERR;
         if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
@@ -404,7 +405,8 @@ struct Solver {
         for (int l = 1; l <= levels; ++l)
             MPS_COUNT_LAUNCH k_mg_links<<<blocks_for(L[l].n), kBlock, 0, st>>>(L[l], L[l < levels ? l + 1 : l], l < levels);
         MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, st>>>(d, mg);
-        MPS_COUNT_LAUNCH k_mg_assemble1<float><<<L[1].n, kMgAsmThreads, 0, st>>>(d, mg, (const float*)d.nbrw);
+        MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, st>>>(d, mg, (const float*)d.nbrw);
+        MPS_COUNT_LAUNCH k_mg_assemble_cells<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d, mg);
         for (int l = 1; l < levels; ++l)
             MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, st>>>(L[l], L[l + 1]);
         const int nd = L[levels].n;
