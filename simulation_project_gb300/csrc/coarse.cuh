@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(kMgCoarsenWarps * 32) k_mg_coarsen(MgLevel lo,
 __global__ void __launch_bounds__(1024) k_mg_dense_inverse(MgLevel lv, float* __restrict__ ainv) {
     extern __shared__ float sm[];
     const int n = lv.n, w2 = 2 * n;
+    if (n <= 0 || n > kMgMaxDense) return;
     float* M = sm;              // [n][2n]: [A | I]
     float* f = sm + n * w2;     // [n] elimination factors
     for (int t = threadIdx.x; t < n * w2; t += blockDim.x) M[t] = 0.f;
@@ -291,6 +292,10 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(MgLevel lv, float* __
     for (int I = threadIdx.x; I < n; I += blockDim.x)
         if (!(M[I * w2 + I] > 0.f)) M[I * w2 + I] = 1.f;
     __syncthreads();
+    // each thread owns one column (col < w2) and the rows row0, row0 + rstep, ...: no
+    // index division in the elimination loop (same operations as an element loop)
+    const int col = (int)threadIdx.x % w2, row0 = (int)threadIdx.x / w2, rstep = (int)blockDim.x / w2;
+    const bool owner = (int)threadIdx.x < rstep * w2;
     for (int k = 0; k < n; ++k) {
         const float piv = M[k * w2 + k];
         __syncthreads();
@@ -298,9 +303,10 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(MgLevel lv, float* __
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = i == k ? 0.f : M[i * w2 + k];
         __syncthreads();
-        for (int t = threadIdx.x; t < n * w2; t += blockDim.x) {
-            const int i = t / w2, col = t % w2;
-            if (i != k) M[t] -= f[i] * M[k * w2 + col];
+        if (owner) {
+            const float mk = M[k * w2 + col];
+            for (int i = row0; i < n; i += rstep)
+                if (i != k) M[i * w2 + col] -= f[i] * mk;
         }
         __syncthreads();
     }
