@@ -56,6 +56,9 @@ STEP_FIXED_B, STEP_ITER_B, STEP_IR_B = 760.0, 72.0, 48.0
 # with 16-bit column offsets: 1.3376 GB read + 2.2 MB written for 201.36M entries
 # (SELL padding included)
 SPMV_DRAM_BYTES_PER_ENTRY = (1.33758e9 + 2.24e6) / 201.362e6
+# the same for the FP16-weight kernel of the inner CG (k_spmv_stream<..., __half>):
+# 898.3 MB read + 1.8 MB written for 201.36M entries
+SPMV16_DRAM_BYTES_PER_ENTRY = (898.3e6 + 1.8e6) / 201.362e6
 
 
 def load_peaks():
@@ -259,14 +262,21 @@ def run_gpu(args):
     nnz = np.mean([s["nnz"] for s in st_fast])
     nnz_wide = np.mean([s["nnz_wide"] if s["rows16"] else s["nnz"] for s in st_fast])
     interior = np.mean([s["interior"] for s in st_fast])
-    # 4 B weight + 2 B (16-bit offset) or 4 B column per entry, 25 B per interior row
-    bytes_launch = 6.0 * (nnz - nnz_wide) + 8.0 * nnz_wide + 25.0 * interior
+    inner16 = all(s["inner16"] for s in st_fast)
+    # weight (2 B FP16 or 4 B FP32) + 2 B (16-bit offset) or 4 B column per entry, 25 B
+    # per interior row
+    wb = 2.0 if inner16 else 4.0
+    bytes_launch = (wb + 2.0) * (nnz - nnz_wide) + (wb + 4.0) * nnz_wide + 25.0 * interior
     avg_ms = spmv_ms / max(spmv_n, 1)
     achieved = bytes_launch / (avg_ms / 1e3) / 1e9 if spmv_n else 0.0
-    roofline = {"bound": "hbm", "kernel": "k_spmv_stream<0,8,2,8,4> (PPE SpMV, FP32 rows streamed by bulk copies)",
+    kname = ("k_spmv_stream<0,16,2,8,4,__half> (inner-CG SpMV, FP16 weights + 16-bit columns streamed by bulk copies)"
+             if inner16 else "k_spmv_stream<0,8,2,8,4> (inner-CG SpMV, FP32 weights + 16-bit columns streamed by bulk copies)")
+    per_entry = SPMV16_DRAM_BYTES_PER_ENTRY if inner16 else SPMV_DRAM_BYTES_PER_ENTRY
+    roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
                 "frac": round(achieved / peak_gbs, 3), "peak_kind": peak_kind,
-                "traffic": int(SPMV_DRAM_BYTES_PER_ENTRY * nnz), "traffic_source": "ncu dram bytes per entry x entries",
+                "traffic": int(per_entry * nnz) if per_entry else None,
+                "traffic_source": "ncu dram bytes per entry x entries",
                 "entries": int(nnz), "entries_32bit_columns": int(nnz_wide),
                 "bytes_per_launch": int(bytes_launch), "launches": spmv_n, "launches_issued": spmv_issued,
                 "avg_launch_us": round(avg_ms * 1e3, 2)}

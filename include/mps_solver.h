@@ -56,7 +56,9 @@ typedef struct MpsSolverOptions {
     double compressibility; /* artificial compressibility alpha [1/Pa] (Ikeda et al.) */
     double cg_rtol;         /* PPE relative residual target (||b - A p|| / ||b||) */
     int cg_max_iter;        /* CG iteration cap (per solve) */
-    double ir_inner_rtol;   /* FP32 inner CG tolerance relative to the refinement residual */
+    double ir_inner_rtol;   /* floor of the FP32 inner CG tolerance relative to the refinement
+                               residual; <= 0: automatic (1e-4 for the FP16-weight operator
+                               under the multilevel preconditioner, else 2e-6) */
     int ir_max_outer;       /* refinement pass cap */
     int max_neighbours;     /* capacity of a Laplacian neighbour row */
     int check_every;        /* CG convergence is read back every this many iterations */
@@ -75,6 +77,12 @@ typedef struct MpsSolverOptions {
     int spmv_stream;        /* FP32 inner SpMV over 16-bit slices: 0 register walk; 1 rows
                                streamed through shared memory by bulk copies (a ring of 2
                                stages of 8 entries per warp); same row values */
+    int inner_weights;      /* 16 (default): the inner CG uses FP16 copies of the FP32 weights
+                               with the diagonal recomputed from the rounded weights (a
+                               consistent Laplacian within ~5e-4 of the FP32 one; the
+                               refinement still drives the FP32-weight residual to cg_rtol);
+                               needs spmv_stream = 1 and matrix_free = 0.  32: the inner CG
+                               uses the FP32 weights (the refinement's operator) */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */
@@ -107,6 +115,7 @@ typedef struct MpsStepStats {
     double r0_relres;       /* ||b - A p0|| / ||b|| of the start (warm start or learned guess) */
     long long nnz_wide;     /* interior entries stored with 32-bit columns (the rest: 16-bit) */
     int rows16;             /* 1 if the FP32 SpMV used compressed columns this step */
+    int inner16;            /* 1 if the inner CG ran on the FP16-weight operator this step */
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);
@@ -138,8 +147,8 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
 CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, double* relres);
 /* One FP32 inner SpMV y = A x over the current rows (FP32_IR solvers; host arrays of
  * n floats in the solver's order): kernel 0 register walk, 1 rows streamed through
- * shared memory (needs the 16-bit slices), 4 / 8 matrix-free.  Every kernel gives the
- * same bits. */
+ * shared memory (needs the 16-bit slices), 4 / 8 matrix-free: all give the same bits;
+ * 2 the streamed FP16-weight operator (inner_weights = 16). */
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
 /* Device pointer of the pressure array (FP64, sorted order) and particle count. */
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);

@@ -19,6 +19,8 @@
 // Kernels take the whole record as one __grid_constant__ parameter.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "mps_common.cuh"
 #include "mps_internal.h"
 #include "../../include/mps_solver.h"
@@ -77,6 +79,9 @@ struct Dev {
     int* sbase;                // [slices] smallest column index of the slice, -1: 32-bit slice
     int* skmax;                // [slices] longest interior row of a 16-bit slice, -1: 32-bit slice
     int rows16;                // nbr16 / sbase are valid for the current rows
+    __half* w16;               // FP16 copies of the FP32 weights (interior rows; inner CG operator)
+    double* diag16;            // diagonal of the FP16-weight operator: coef * sum of FP16 weights + kappa
+    int rows_w16;              // w16 / diag16 are valid for the current rows
     int* nbr_cnt;
     int* gnbr;
     void* gnbrr;

@@ -793,7 +793,10 @@ __device__ __forceinline__ int sell_col(const Dev& d, size_t e, int sb) {
 // Compressed columns of the interior rows, one read pass: warp per 32-row slice,
 // offsets j - 32*slice as signed 16 bits; a slice with an offset outside
 // [-32768, 32767] keeps its 32-bit columns (sbase = -1, found by a warp vote).
-__global__ void k_compress_rows(const __grid_constant__ Dev d) {
+// With w16: also the FP16 copy of each FP32 weight (round to nearest) and the
+// diagonal of that operator, coef * (sum of the FP16 weights in entry order, in FP32)
+// + kappa, so the FP16-weight operator is again a Laplacian plus kappa.
+__global__ void k_compress_rows(const __grid_constant__ Dev d, int w16) {
     const int lane = threadIdx.x & 31;
     const int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (sl >= (d.n + 31) >> 5) return;   // warp-uniform
@@ -802,20 +805,32 @@ __global__ void k_compress_rows(const __grid_constant__ Dev d) {
     const int kmax = __reduce_max_sync(0xffffffffu, cnt);
     const size_t base = (size_t)sl * d.K * 32 + lane;
     const int r0 = sl * 32;
+    const float* __restrict__ w = (const float*)d.nbrw;
     bool fits = true;
+    float sw16 = 0.f;
     for (int k = 0; k < kmax; k += 4) {
         int j[4];
+        float wv[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = k + u < cnt ? __ldcs(d.nbr + base + (size_t)(k + u) * 32) : r0;
+        for (int u = 0; u < 4; ++u) {
+            j[u] = k + u < cnt ? __ldcs(d.nbr + base + (size_t)(k + u) * 32) : r0;
+            wv[u] = (w16 && k + u < cnt) ? __ldcs(w + base + (size_t)(k + u) * 32) : 0.f;
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (k + u < cnt) {
                 const int off = j[u] - r0;
                 fits = fits && off >= -32768 && off <= 32767;
                 d.nbr16[base + (size_t)(k + u) * 32] = (unsigned short)(short)off;
+                if (w16) {
+                    const __half h = __float2half_rn(wv[u]);
+                    d.w16[base + (size_t)(k + u) * 32] = h;
+                    sw16 += __half2float(h);
+                }
             }
         }
     }
+    if (w16 && cnt > 0) d.diag16[i] = d.c.coef_lap * (double)sw16 + d.c.kappa;
     const bool all = __all_sync(0xffffffffu, fits);
     if (lane == 0) {
         d.sbase[sl] = all ? r0 : -1;
@@ -828,6 +843,10 @@ __global__ void k_compress_rows(const __grid_constant__ Dev d) {
     if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
 }
 
+// a stored weight as a float or double (FP16 weights widen to float)
+__device__ __forceinline__ float to_wt(float v) { return v; }
+__device__ __forceinline__ double to_wt(double v) { return v; }
+__device__ __forceinline__ float to_wt(__half v) { return __half2float(v); }
 // acc + a * b with one rounding (no contraction left to the compiler)
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return __fma_rn(a, b, c); }
@@ -851,12 +870,12 @@ __device__ __forceinline__ TA sell_row_dot(const Dev& d, const TW* __restrict__ 
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            if (k + u < cnt) acc = fma_t((TA)wv[u], (TA)x[id[u]], acc);
+            if (k + u < cnt) acc = fma_t((TA)to_wt(wv[u]), (TA)x[id[u]], acc);
     }
     for (; k < kmax; ++k) {
         const int idk = sell_col<NARROW>(d, base + (size_t)k * 32, sb);
         const TW wk = __ldcs(w + base + (size_t)k * 32);
-        if (k < cnt) acc = fma_t((TA)wk, (TA)x[idk], acc);
+        if (k < cnt) acc = fma_t((TA)to_wt(wk), (TA)x[idk], acc);
     }
     return acc;
 }
@@ -1117,16 +1136,22 @@ __global__ void __launch_bounds__(256, 8) k_residual_df(const __grid_constant__ 
 // MPS_ERR_STAGE_TIMEOUT; the warp then waits (bounded) for its copies in flight and
 // finishes on the register walk.  32-bit slices (skmax = -1) take the register walk.
 // ---------------------------------------------------------------------------
-template <int SC> constexpr int stream_stage_bytes() { return SC * 192; }
-template <int SC, int SS, int W> constexpr int stream_smem_bytes() { return W * SS * stream_stage_bytes<SC>(); }
+// stage: SC x 64 B of 16-bit columns, then SC x 32 weights of type TW
+template <int SC, class TW = float> constexpr int stream_stage_bytes() { return SC * (64 + 32 * (int)sizeof(TW)); }
+template <int SC, int SS, int W, class TW = float> constexpr int stream_smem_bytes() {
+    return W * SS * stream_stage_bytes<SC, TW>();
+}
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
 
-template <int SC, int SS>
+template <int SC, int SS, class TW = float>
 struct SliceRing {
-    static constexpr int SB = stream_stage_bytes<SC>();
+    static constexpr int SB = stream_stage_bytes<SC, TW>();
+    static constexpr unsigned WB = (unsigned)sizeof(TW) * 32u;   // weight bytes per entry
     unsigned char* ring;
     unsigned long long* bar;
     const unsigned short* cols;
-    const float* w;
+    const TW* w;
     const int* skmax;
     unsigned* err;
     int nsl, nw, K, lane;
@@ -1135,7 +1160,7 @@ struct SliceRing {
     bool streaming;
     unsigned long long pol;
 
-    __device__ void init(const Dev& d, const float* w_, unsigned char* ring_, unsigned long long* bar_, int gw,
+    __device__ void init(const Dev& d, const TW* w_, unsigned char* ring_, unsigned long long* bar_, int gw,
                          int nw_) {
         ring = ring_;
         bar = bar_;
@@ -1173,9 +1198,9 @@ struct SliceRing {
             if (lane == 0) {
                 const size_t e0 = ((size_t)ps * K + k0) * 32;
                 fence_proxy_async_smem();
-                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * 192u);
+                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * (64u + WB));
                 bulk_copy_g2s_hint(ring + st * SB, cols + e0, (unsigned)ne * 64u, &bar[st], pol);
-                bulk_copy_g2s_hint(ring + st * SB + SC * 64, w + e0, (unsigned)ne * 128u, &bar[st], pol);
+                bulk_copy_g2s_hint(ring + st * SB + SC * 64, w + e0, (unsigned)ne * WB, &bar[st], pol);
             }
             ++q_issue;
             if (++pc == pn) next_slice();
@@ -1183,7 +1208,7 @@ struct SliceRing {
     }
     // waits for the next stage; false: streaming abandoned (the caller recomputes the
     // slice on the register walk)
-    __device__ bool acquire(const unsigned short*& cs, const float*& ws) {
+    __device__ bool acquire(const unsigned short*& cs, const TW*& ws) {
         refill();
         const int st = (int)(q_cons % SS);
         if (!__all_sync(0xffffffffu, mbar_wait_parity_bounded(&bar[st], (q_cons / SS) & 1u, 1ll << 20))) {
@@ -1195,7 +1220,7 @@ struct SliceRing {
             return false;
         }
         cs = (const unsigned short*)(ring + st * SB);
-        ws = (const float*)(ring + st * SB + SC * 64);
+        ws = (const TW*)(ring + st * SB + SC * 64);
         return true;
     }
     // the warp is done reading the stage
@@ -1207,10 +1232,11 @@ struct SliceRing {
 
 // FP32 SpMV of the inner CG over streamed rows, MODE 0 / 2 as in k_spmv.  Each row
 // accumulates its entries in order with one FMA each, so every row value is
-// bit-identical to the register walk.
-template <int MODE, int SC, int SS, int W, int MINB>
+// bit-identical to the register walk.  TW = __half: the FP16-weight operator (w16,
+// diag16), accumulated in FP32.
+template <int MODE, int SC, int SS, int W, int MINB, class TW = float>
 __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_constant__ Dev d,
-                                                             const float* __restrict__ w,
+                                                             const TW* __restrict__ w,
                                                              const float* __restrict__ x, float* __restrict__ y,
                                                              const double* __restrict__ b, int slot) {
     static_assert(MODE == 0 || MODE == 2, "FP32 modes only");
@@ -1220,8 +1246,9 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
     __shared__ __align__(8) unsigned long long bars[W][SS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
-    SliceRing<SC, SS> R;
-    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS>::SB, bars[warp], gw, nw);
+    SliceRing<SC, SS, TW> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, TW>::SB, bars[warp], gw, nw);
+    const double* __restrict__ diag = sizeof(TW) == 2 ? d.diag16 : d.diag;
 
     const double coef = d.c.coef_lap;
     double part0 = 0.0, part1 = 0.0;
@@ -1239,7 +1266,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
             const int r0 = sl * 32;
             for (int c = 0; c < nc; ++c) {
                 const unsigned short* cs;
-                const float* ws;
+                const TW* ws;
                 if (!R.acquire(cs, ws)) break;
                 const int k0 = c * SC;
 #pragma unroll
@@ -1249,7 +1276,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
-                        wv[u] = ws[(g + u) * 32 + lane];
+                        wv[u] = to_f32(ws[(g + u) * 32 + lane]);
                     }
 #pragma unroll
                     for (int u = 0; u < 8; ++u)
@@ -1271,7 +1298,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
             y[i] = 0.f;
             continue;
         }
-        const double yi = d.diag[i] * (double)x[i] - coef * (double)acc;
+        const double yi = diag[i] * (double)x[i] - coef * (double)acc;
         y[i] = (float)yi;
         if (MODE == 0) {
             partw += x[i] * (float)yi;
@@ -1309,8 +1336,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
     __shared__ __align__(8) unsigned long long bars[W][SS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
-    SliceRing<SC, SS> R;
-    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS>::SB, bars[warp], gw, nw);
+    SliceRing<SC, SS, float> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, float>::SB, bars[warp], gw, nw);
     const float* __restrict__ xh = d.xh;
     const float* __restrict__ xl = d.xl;
 

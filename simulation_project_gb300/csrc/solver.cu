@@ -193,6 +193,10 @@ struct Solver {
         e = e ? e : mk(&d.nbr, N32 * d.K); e = e ? e : mk((char**)&d.nbrw, N32 * d.K * wsz);
         e = e ? e : mk(&d.nbr16, N32 * d.K); e = e ? e : mk(&d.sbase, N32 / 32 + 1);
         e = e ? e : mk(&d.skmax, N32 / 32 + 1);
+        if (opt.inner_weights == 16) {
+            e = e ? e : mk(&d.w16, N32 * d.K);
+            e = e ? e : mk(&d.diag16, N);
+        }
         e = e ? e : mk(&d.nbr_cnt, N);
         e = e ? e : mk(&d.gnbr, N * d.KG); e = e ? e : mk((char**)&d.gnbrr, N * d.KG * wsz);
         e = e ? e : mk(&d.gcnt, N);
@@ -524,6 +528,7 @@ struct Solver {
         feat_valid = false;
         residual_ready = false;
         d.rows16 = 0;
+        d.rows_w16 = 0;
         timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
         cudaMemsetAsync(d.istat, 0, 2 * sizeof(int), st);
@@ -558,8 +563,10 @@ struct Solver {
             MPS_COUNT_LAUNCH k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
             MPS_COUNT_LAUNCH k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
             if (!fp64() && opt.compress_rows) {
-                MPS_COUNT_LAUNCH k_compress_rows<<<div_up((d.n + 31) / 32 * 32, 256), 256, 0, st>>>(d);
+                const int w16 = (want_inner16() && d.w16) ? 1 : 0;
+                MPS_COUNT_LAUNCH k_compress_rows<<<div_up((d.n + 31) / 32 * 32, 256), 256, 0, st>>>(d, w16);
                 d.rows16 = 1;
+                d.rows_w16 = w16;
             }
             const bool use_learned = learned_ready && opt.learned;
             if (use_learned || collect) {
@@ -626,6 +633,7 @@ struct Solver {
         S.max_row = h_int[1];
         S.nnz_wide = h_int[2];
         S.rows16 = d.rows16;
+        S.inner16 = inner16() ? 1 : 0;
         S.particles = d.n;
         if (opt.pressure_mode != MPS_PRESSURE_EXPLICIT) {
             S.nnz = (long long)h_nnz[0];
@@ -666,12 +674,12 @@ struct Solver {
     bool stream_failed = false;
     // SMs x resident CTAs of a streamed kernel (after its shared-memory opt-in)
     template <class F>
-    int persistent_grid(F kernel, int& cached) {
+    int persistent_grid(F kernel, int& cached, int smem = kSsSmem) {
         if (cached == 0) {
             int dev = 0, sms = 0, per_sm = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSsWarps * 32, kSsSmem)) return -1;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSsWarps * 32, smem)) return -1;
             // the reduction buffer holds 2 partials per CTA for up to 2 x kRedBlocks CTAs
             cached = std::max(1, std::min(sms * std::max(per_sm, 1), 2 * kRedBlocks));
         }
@@ -706,15 +714,36 @@ struct Solver {
         MPS_COUNT_LAUNCH k_spmv_stream<MODE, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>
             <<<g, kSsWarps * 32, kSsSmem, st>>>(d, w, x, y, b, slot);
     }
+    // the inner CG's SpMV over FP16 weights (w16, diag16): stages of 16 entries (2 KB,
+    // the bytes in flight of the FP32 ring's 8), 2 stages, CTAs of 8 warps, at least 4
+    // per SM (measured against 8 x 2-3, 24 x 2, 32 x 2 and 5 CTAs per SM)
+    static constexpr int kS16Entries = 16;
+    static constexpr int kS16Smem = stream_smem_bytes<kS16Entries, kSsStages, kSsWarps, __half>();
+    int spmv16_grid = 0;
+    void spmv_stream16(const float* x, float* y) {
+        auto k = k_spmv_stream<0, kS16Entries, kSsStages, kSsWarps, kSsMinBlocks, __half>;
+        if (spmv16_grid == 0) {
+            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kS16Smem) ||
+                persistent_grid(k, spmv16_grid, kS16Smem) < 0) {
+                stream_failed = true;
+                return;
+            }
+        }
+        MPS_COUNT_LAUNCH k<<<spmv16_grid, kSsWarps * 32, kS16Smem, st>>>(d, d.w16, x, y, nullptr, 0);
+    }
     // the streamed kernel needs the 16-bit slices of this step
     bool use_stream() const { return opt.spmv_stream != 0 && d.rows16; }
+    // the inner CG runs on the FP16-weight operator (streamed, not matrix-free)
+    bool want_inner16() const { return opt.inner_weights == 16 && opt.spmv_stream != 0 && opt.matrix_free == 0; }
+    bool inner16() const { return want_inner16() && d.rows_w16 && use_stream(); }
 
     // q = A p of the inner CG (MODE 0): stored weights, or matrix-free FP32 rows
     template <class TW, class TV>
     void spmv_cg(const TW* w, const TV* p, TV* q) {
         if constexpr (std::is_same<TW, float>::value && std::is_same<TV, float>::value) {
             if (opt.matrix_free == 0 && use_stream()) {
-                spmv_stream<0>(w, p, q, nullptr, 0);
+                if (inner16()) spmv_stream16(p, q);
+                else spmv_stream<0>(w, p, q, nullptr, 0);
                 return;
             }
             if (opt.matrix_free == 4) {
@@ -812,6 +841,14 @@ struct Solver {
         }
     }
 
+    // inner-solve floor: the option, or automatically 1e-4 for the FP16-weight operator
+    // under the multilevel preconditioner (a pass contracts the FP32-weight residual by
+    // at most ~5e-4 then; measured fastest) and 2e-6 otherwise
+    double ir_inner_rtol() const {
+        if (opt.ir_inner_rtol > 0) return opt.ir_inner_rtol;
+        return inner16() && mg_ready ? 1e-4 : 2e-6;
+    }
+
     // FP32 Jacobi-PCG inside FP64 iterative refinement
     CCTStatusType solve_ir(MpsStepStats& S) {
         const float* w = (const float*)d.nbrw;
@@ -840,7 +877,7 @@ struct Solver {
             // inner FP32 solve of A d = r / ||r||: to the reduction still needed (with a
             // 0.3 margin), but not below what FP32 CG reliably reaches (ir_inner_rtol)
             const double need = 0.3 * opt.cg_rtol * bnorm / rn;
-            const double inner_tol = std::max(need, opt.ir_inner_rtol);
+            const double inner_tol = std::max(need, ir_inner_rtol());
             MPS_COUNT_LAUNCH k_cg_start<float><<<kRedBlocks, 256, 0, st>>>(d, d.r32, d.z32, d.p32, d.r, 1.0 / rn, nullptr, d.m32, d.d32, 3,
                                                           inner_tol, opt.cg_max_iter);
             if (mg_ready) {
@@ -903,7 +940,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->compressibility = 1e-9;
     o->cg_rtol = 1e-8;
     o->cg_max_iter = 5000;
-    o->ir_inner_rtol = 2e-6;
+    o->ir_inner_rtol = 0.0;
     o->ir_max_outer = 12;
     o->max_neighbours = 384;
     o->check_every = 8;
@@ -914,6 +951,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->mg_sweeps = 1;
     o->matrix_free = 0;
     o->spmv_stream = 1;
+    o->inner_weights = 16;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -923,6 +961,7 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (opt) o = *opt; else mps_solver_default_options(&o);
     if (o.matrix_free != 0 && o.matrix_free != 4 && o.matrix_free != 8) return CCT_PARAMERR;
     if (o.spmv_stream != 0 && o.spmv_stream != 1) return CCT_PARAMERR;
+    if (o.inner_weights != 32 && o.inner_weights != 16) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {
@@ -1037,8 +1076,9 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     mps::Solver& S = s->s;
     mps::Dev& d = S.d;
     if (S.fp64() || d.n <= 0) return CCT_PARAMERR;
-    if (kernel != 0 && kernel != 1 && kernel != 4 && kernel != 8) return CCT_PARAMERR;
+    if (kernel != 0 && kernel != 1 && kernel != 2 && kernel != 4 && kernel != 8) return CCT_PARAMERR;
     if (kernel == 1 && !d.rows16) return CCT_PARAMERR;
+    if (kernel == 2 && !(d.rows16 && d.rows_w16)) return CCT_PARAMERR;
     const float* w = (const float*)d.nbrw;
     cudaError_t e = cudaMemcpyAsync(d.p32, host_x, sizeof(float) * d.n, cudaMemcpyHostToDevice, S.st);
     // MODE 0 returns at once after a converged solve: clear the flag (the next CG start sets it)
@@ -1048,6 +1088,8 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
         MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
     else if (kernel == 1)
         S.spmv_stream<0>(w, d.p32, d.q32, nullptr, 0);
+    else if (kernel == 2)
+        S.spmv_stream16(d.p32, d.q32);
     else if (kernel == 4)
         MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0, 4><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
     else

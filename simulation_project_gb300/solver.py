@@ -25,7 +25,7 @@ class MpsSolverOptions(C.Structure):
                 ("ir_max_outer", C.c_int), ("max_neighbours", C.c_int), ("check_every", C.c_int),
                 ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
                 ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int),
-                ("matrix_free", C.c_int), ("spmv_stream", C.c_int)]
+                ("matrix_free", C.c_int), ("spmv_stream", C.c_int), ("inner_weights", C.c_int)]
 
 
 class MpsStepStats(C.Structure):
@@ -36,7 +36,8 @@ class MpsStepStats(C.Structure):
                 ("ms_ppe_setup", C.c_float), ("ms_spmv", C.c_float), ("ms_cg_vec", C.c_float),
                 ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int),
                 ("ms_precond", C.c_float), ("mg_levels", C.c_int), ("mg_level1", C.c_int),
-                ("r0_relres", C.c_double), ("nnz_wide", C.c_longlong), ("rows16", C.c_int)]
+                ("r0_relres", C.c_double), ("nnz_wide", C.c_longlong), ("rows16", C.c_int),
+                ("inner16", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -191,7 +192,8 @@ class Solver:
 
     def debug_spmv(self, kernel: int, x: np.ndarray) -> np.ndarray:
         """One FP32 inner SpMV y = A x over the current rows with the named kernel
-        (0 register walk, 1 streamed, 4 / 8 matrix-free), solver order."""
+        (0 register walk, 1 streamed, 4 / 8 matrix-free; 2 the FP16-weight operator),
+        solver order."""
         n = self.state(sort_by_id=False)["id"].shape[0]
         xs = np.ascontiguousarray(x, dtype=np.float32)
         if xs.shape != (n,):

@@ -191,11 +191,31 @@ def test_streamed_residual_is_bit_identical():
     assert np.abs(r1 - r0).max() <= 1e-10 * np.abs(s.debug_ppe()["rhs"]).max()
 
 
+def test_fp16_inner_operator():
+    """FP16 copies of the weights for the inner CG (diagonal recomputed from them):
+    the SpMV is within the FP16 rounding of the FP32 one, and the refinement still
+    drives the FP32-weight residual to the tolerance."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=4, drag_index=0.5)
+    a = Solver(sc, precision="fp32_ir", inner_weights=16)
+    b = Solver(sc, precision="fp32_ir", inner_weights=32)
+    for i in range(3):
+        sa, sb = a.step(i), b.step(i)
+        assert sa["error_flags"] == 0 and sa["cg_relres"] <= 1e-8, sa
+        assert sa["cg_iterations"] <= 1.5 * sb["cg_iterations"] + 8, (sa["cg_iterations"], sb["cg_iterations"])
+    pa, pb = a.state()["press"], b.state()["press"]
+    assert np.abs(pa - pb).max() <= 1e-5 * np.abs(pb).max()
+    n = a.state(sort_by_id=False)["id"].shape[0]
+    x = np.random.default_rng(3).standard_normal(n).astype(np.float32)
+    y32, y16 = a.debug_spmv(0, x), a.debug_spmv(2, x)
+    assert np.linalg.norm(y16 - y32) <= 1e-3 * np.linalg.norm(y32)
+    assert not np.array_equal(y16, y32)
+
+
 def test_streamed_spmv_step_matches():
     """FP32-IR steps with the streamed SpMV: same row values, the CG's p.q sums in
     another order (persistent grid), so the step agrees to the solve tolerance."""
     sc = scenes.rotating_bucket(l0=0.008, n_drag=4, drag_index=0.5)
-    a = Solver(sc, precision="fp32_ir", spmv_stream=1)
+    a = Solver(sc, precision="fp32_ir", spmv_stream=1, inner_weights=32)
     b = Solver(sc, precision="fp32_ir", spmv_stream=0)
     for i in range(3):
         sa, sb = a.step(i), b.step(i)
@@ -207,7 +227,7 @@ def test_streamed_spmv_step_matches():
 
 def test_spmv_options_are_checked():
     sc = scenes.rotating_bucket(l0=0.008, n_drag=0)
-    for bad in ({"matrix_free": 3}, {"spmv_stream": 2}):
+    for bad in ({"matrix_free": 3}, {"spmv_stream": 2}, {"inner_weights": 8}):
         with pytest.raises(MpsError) as e:
             Solver(sc, precision="fp32_ir", **bad)
         assert e.value.status == 2   # CCT_PARAMERR
