@@ -410,6 +410,54 @@ __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
     if (lane == 0) lo.e2[I] = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
 }
 
+// the last prolongation and up sweep (level 2 -> level 1) fused with the fine level:
+// warp per level-1 aggregate computes e1[I] as k_mg_up, then z = m r + e1[I] over the
+// cell's rows (every row lies in one cell), p = z in mode 1, and r.z as k_mg_fine_z
+// (S_RZ, or S_BETA and S_RZ); one pass over the rows instead of two launches
+template <class TV>
+__global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
+                                                      const TV* __restrict__ r, TV* __restrict__ z,
+                                                      TV* __restrict__ p, const float* __restrict__ m32, int mode,
+                                                      int slot) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const MgLevel& lo = mg.L[1];
+    const MgLevel& hi = mg.L[2];
+    const float omega = mg.omega;
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    TV prz = TV(0);
+    if (I < lo.n) {   // warp-uniform; every thread reaches the grid reduction
+        float t = 0.f;
+        if (lane < 27) {
+            const int J = lo.nb[(size_t)I * 27 + lane];
+            if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.par[J]]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        const float e1 = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
+        if (lane == 0) lo.e2[I] = e1;
+        const int c = lo.ccell[I];
+        for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) {
+            TV zi = TV(0);
+            if (d.inner[i]) {
+                zi = (TV)m32[i] * r[i] + (TV)e1;
+                prz += r[i] * zi;
+            }
+            z[i] = zi;
+            if (mode == 1) p[i] = zi;
+        }
+    }
+    double v[1] = {(double)prz}, out[1];
+    if (grid_reduce<1, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        if (mode == 1) {
+            d.scal[S_RZ] = out[0];
+        } else {
+            const double rz = d.scal[S_RZ];
+            d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
+            d.scal[S_RZ] = out[0];
+        }
+    }
+}
+
 // CG update fused with the level-1 restriction (multilevel path): warp per level-1
 // aggregate over its contiguous rows: x += alpha p, r -= alpha q on interior rows,
 // r1[I] = sum of r over the cell, the first down sweep e1 = omega D1^-1 r1, and

@@ -438,8 +438,16 @@ struct Solver {
         for (int l = 1; l < lv; ++l)
             MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
         MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
-        for (int l = lv - 1; l >= 1; --l)
+        // the level-2 -> level-1 up sweep carries the fine level when no extra level-1
+        // sweeps follow it (and the reduction buffer holds its CTAs' partials)
+        const int up1_blocks = div_up(L[1].n * 32, 256);
+        const bool fuse = lv >= 2 && extra == 0 && up1_blocks <= 4 * kRedBlocks;
+        for (int l = lv - 1; l >= (fuse ? 2 : 1); --l)
             MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+        if (fuse) {
+            MPS_COUNT_LAUNCH k_mg_up_fine_z<float><<<up1_blocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7);
+            return;
+        }
         for (int k = 0; k < extra; ++k) {
             MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e2, L[1].e, om);
             std::swap(L[1].e, L[1].e2);
