@@ -269,14 +269,22 @@ def run_gpu(args):
     bytes_launch = (wb + 2.0) * (nnz - nnz_wide) + (wb + 4.0) * nnz_wide + 25.0 * interior
     avg_ms = spmv_ms / max(spmv_n, 1)
     achieved = bytes_launch / (avg_ms / 1e3) / 1e9 if spmv_n else 0.0
-    kname = ("k_spmv_stream<0,16,2,8,4,__half> (inner-CG SpMV, FP16 weights + 16-bit columns streamed by bulk copies)"
-             if inner16 else "k_spmv_stream<0,8,2,8,4> (inner-CG SpMV, FP32 weights + 16-bit columns streamed by bulk copies)")
-    per_entry = SPMV16_DRAM_BYTES_PER_ENTRY if inner16 else SPMV_DRAM_BYTES_PER_ENTRY
+    wide = nnz_wide * 2 > nnz   # the solver streams every slice's 32-bit columns then
+    if wide:
+        kname = ("k_spmv_stream<0,8,2,8,4,%s,true> (inner-CG SpMV, %s weights + 32-bit columns streamed by bulk copies)"
+                 % (("__half", "FP16") if inner16 else ("float", "FP32")))
+    else:
+        kname = ("k_spmv_stream<0,16,2,8,4,__half> (inner-CG SpMV, FP16 weights + 16-bit columns streamed by bulk copies)"
+                 if inner16 else
+                 "k_spmv_stream<0,8,2,8,4> (inner-CG SpMV, FP32 weights + 16-bit columns streamed by bulk copies)")
+    # DRAM bytes per entry were captured for the 16-bit-column kernels only
+    per_entry = None if wide else (SPMV16_DRAM_BYTES_PER_ENTRY if inner16 else SPMV_DRAM_BYTES_PER_ENTRY)
     roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
                 "frac": round(achieved / peak_gbs, 3), "peak_kind": peak_kind,
                 "traffic": int(per_entry * nnz) if per_entry else None,
-                "traffic_source": "ncu dram bytes per entry x entries",
+                "traffic_source": ("ncu dram bytes per entry x entries" if per_entry else
+                                   "not captured for the 32-bit-column layout"),
                 "entries": int(nnz), "entries_32bit_columns": int(nnz_wide),
                 "bytes_per_launch": int(bytes_launch), "launches": spmv_n, "launches_issued": spmv_issued,
                 "avg_launch_us": round(avg_ms * 1e3, 2)}

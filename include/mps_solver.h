@@ -83,6 +83,9 @@ typedef struct MpsSolverOptions {
                                refinement still drives the FP32-weight residual to cg_rtol);
                                needs spmv_stream = 1 and matrix_free = 0.  32: the inner CG
                                uses the FP32 weights (the refinement's operator) */
+    int spmv_wide;          /* streamed SpMV columns: 0 automatic (32-bit columns of every
+                               slice when most entries of the last step needed them, else the
+                               16-bit slices), 1 always 32-bit, -1 never; same row values */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */
@@ -147,8 +150,10 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
 CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, double* relres);
 /* One FP32 inner SpMV y = A x over the current rows (FP32_IR solvers; host arrays of
  * n floats in the solver's order): kernel 0 register walk, 1 rows streamed through
- * shared memory (needs the 16-bit slices), 4 / 8 matrix-free: all give the same bits;
- * 2 the streamed FP16-weight operator (inner_weights = 16). */
+ * shared memory (16-bit columns; needs the 16-bit slices), 3 streamed with the 32-bit
+ * columns, 4 / 8 matrix-free: all give the same bits; 2 / 6 the streamed FP16-weight
+ * operator (inner_weights = 16) with 16-bit / 32-bit columns, the same bits as each
+ * other. */
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
 /* Device pointer of the pressure array (FP64, sorted order) and particle count. */
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);

@@ -834,7 +834,7 @@ __global__ void k_compress_rows(const __grid_constant__ Dev d, int w16) {
     const bool all = __all_sync(0xffffffffu, fits);
     if (lane == 0) {
         d.sbase[sl] = all ? r0 : -1;
-        d.skmax[sl] = all ? kmax : -1;
+        d.skmax[sl] = all ? kmax : -1 - kmax;
     }
     // interior entries kept at 32 bits (counted for the bytes-per-launch figure)
     int wide = all ? 0 : cnt;
@@ -1136,21 +1136,28 @@ __global__ void __launch_bounds__(256, 8) k_residual_df(const __grid_constant__ 
 // MPS_ERR_STAGE_TIMEOUT; the warp then waits (bounded) for its copies in flight and
 // finishes on the register walk.  32-bit slices (skmax = -1) take the register walk.
 // ---------------------------------------------------------------------------
-// stage: SC x 64 B of 16-bit columns, then SC x 32 weights of type TW
-template <int SC, class TW = float> constexpr int stream_stage_bytes() { return SC * (64 + 32 * (int)sizeof(TW)); }
-template <int SC, int SS, int W, class TW = float> constexpr int stream_smem_bytes() {
-    return W * SS * stream_stage_bytes<SC, TW>();
+// stage: SC x 32 columns (16-bit offsets, or 32-bit indices when WIDE), then SC x 32
+// weights of type TW
+template <int SC, class TW = float, bool WIDE = false> constexpr int stream_stage_bytes() {
+    return SC * ((WIDE ? 128 : 64) + 32 * (int)sizeof(TW));
 }
+template <int SC, int SS, int W, class TW = float, bool WIDE = false> constexpr int stream_smem_bytes() {
+    return W * SS * stream_stage_bytes<SC, TW, WIDE>();
+}
+// longest interior row of a slice from skmax (kmax for a 16-bit slice, -1 - kmax for
+// a 32-bit one)
+__device__ __forceinline__ int slice_kmax(int v) { return v >= 0 ? v : -1 - v; }
 __device__ __forceinline__ float to_f32(float v) { return v; }
 __device__ __forceinline__ float to_f32(__half v) { return __half2float(v); }
 
-template <int SC, int SS, class TW = float>
+template <int SC, int SS, class TW = float, bool WIDE = false>
 struct SliceRing {
-    static constexpr int SB = stream_stage_bytes<SC, TW>();
+    static constexpr int SB = stream_stage_bytes<SC, TW, WIDE>();
+    static constexpr unsigned CB = WIDE ? 128u : 64u;            // column bytes per entry
     static constexpr unsigned WB = (unsigned)sizeof(TW) * 32u;   // weight bytes per entry
     unsigned char* ring;
     unsigned long long* bar;
-    const unsigned short* cols;
+    const unsigned char* cols;
     const TW* w;
     const int* skmax;
     unsigned* err;
@@ -1164,7 +1171,7 @@ struct SliceRing {
                          int nw_) {
         ring = ring_;
         bar = bar_;
-        cols = d.nbr16;
+        cols = WIDE ? (const unsigned char*)d.nbr : (const unsigned char*)d.nbr16;
         w = w_;
         skmax = d.skmax;
         err = d.err;
@@ -1185,6 +1192,7 @@ struct SliceRing {
         do {
             ps += nw;
             pk = ps < nsl ? skmax[ps] : 0;
+            if (WIDE) pk = slice_kmax(pk);   // every slice; else 16-bit slices only
         } while (ps < nsl && pk <= 0);
         pc = 0;
         pn = (pk + SC - 1) / SC;
@@ -1198,9 +1206,9 @@ struct SliceRing {
             if (lane == 0) {
                 const size_t e0 = ((size_t)ps * K + k0) * 32;
                 fence_proxy_async_smem();
-                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * (64u + WB));
-                bulk_copy_g2s_hint(ring + st * SB, cols + e0, (unsigned)ne * 64u, &bar[st], pol);
-                bulk_copy_g2s_hint(ring + st * SB + SC * 64, w + e0, (unsigned)ne * WB, &bar[st], pol);
+                mbar_arrive_expect_tx(&bar[st], (unsigned)ne * (CB + WB));
+                bulk_copy_g2s_hint(ring + st * SB, cols + e0 * (CB / 32u), (unsigned)ne * CB, &bar[st], pol);
+                bulk_copy_g2s_hint(ring + st * SB + SC * CB, w + e0, (unsigned)ne * WB, &bar[st], pol);
             }
             ++q_issue;
             if (++pc == pn) next_slice();
@@ -1208,7 +1216,7 @@ struct SliceRing {
     }
     // waits for the next stage; false: streaming abandoned (the caller recomputes the
     // slice on the register walk)
-    __device__ bool acquire(const unsigned short*& cs, const TW*& ws) {
+    __device__ bool acquire(const unsigned char*& cs, const TW*& ws) {
         refill();
         const int st = (int)(q_cons % SS);
         if (!__all_sync(0xffffffffu, mbar_wait_parity_bounded(&bar[st], (q_cons / SS) & 1u, 1ll << 20))) {
@@ -1219,8 +1227,8 @@ struct SliceRing {
             q_cons = q_issue;
             return false;
         }
-        cs = (const unsigned short*)(ring + st * SB);
-        ws = (const TW*)(ring + st * SB + SC * 64);
+        cs = ring + st * SB;
+        ws = (const TW*)(ring + st * SB + SC * CB);
         return true;
     }
     // the warp is done reading the stage
@@ -1234,7 +1242,7 @@ struct SliceRing {
 // accumulates its entries in order with one FMA each, so every row value is
 // bit-identical to the register walk.  TW = __half: the FP16-weight operator (w16,
 // diag16), accumulated in FP32.
-template <int MODE, int SC, int SS, int W, int MINB, class TW = float>
+template <int MODE, int SC, int SS, int W, int MINB, class TW = float, bool WIDE = false>
 __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_constant__ Dev d,
                                                              const TW* __restrict__ w,
                                                              const float* __restrict__ x, float* __restrict__ y,
@@ -1246,8 +1254,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
     __shared__ __align__(8) unsigned long long bars[W][SS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
-    SliceRing<SC, SS, TW> R;
-    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, TW>::SB, bars[warp], gw, nw);
+    SliceRing<SC, SS, TW, WIDE> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, TW, WIDE>::SB, bars[warp], gw, nw);
     const double* __restrict__ diag = sizeof(TW) == 2 ? d.diag16 : d.diag;
 
     const double coef = d.c.coef_lap;
@@ -1261,11 +1269,12 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
         const int km = d.skmax[sl];
         float acc = 0.f;
         bool done = false;
-        if (km >= 0 && R.streaming) {
-            const int nc = (km + SC - 1) / SC;
+        if ((WIDE || km >= 0) && R.streaming) {
+            const int kms = slice_kmax(km);
+            const int nc = (kms + SC - 1) / SC;
             const int r0 = sl * 32;
             for (int c = 0; c < nc; ++c) {
-                const unsigned short* cs;
+                const unsigned char* cs;
                 const TW* ws;
                 if (!R.acquire(cs, ws)) break;
                 const int k0 = c * SC;
@@ -1275,7 +1284,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
                     float wv[8];
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
-                        j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
+                        if constexpr (WIDE) j[u] = ((const int*)cs)[(g + u) * 32 + lane];
+                        else j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
                         wv[u] = to_f32(ws[(g + u) * 32 + lane]);
                     }
 #pragma unroll
@@ -1354,7 +1364,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
             const int nc = (km + SC - 1) / SC;
             const int r0 = sl * 32;
             for (int c = 0; c < nc; ++c) {
-                const unsigned short* cs;
+                const unsigned char* cs;
                 const float* ws;
                 if (!R.acquire(cs, ws)) break;
                 const int k0 = c * SC;
@@ -1364,7 +1374,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
                     float wv[8], h[8], l[8];
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
-                        j[u] = r0 + (int)(short)cs[(g + u) * 32 + lane];
+                        j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
                         wv[u] = ws[(g + u) * 32 + lane];
                     }
 #pragma unroll

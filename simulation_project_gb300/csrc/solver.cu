@@ -534,6 +534,7 @@ struct Solver {
         MpsStepStats S{};
         spmv_launches = 0;
         feat_valid = false;
+        prefer_wide = opt.spmv_wide == 1 || (opt.spmv_wide == 0 && last.nnz > 0 && 2 * last.nnz_wide > last.nnz);
         residual_ready = false;
         d.rows16 = 0;
         d.rows_w16 = 0;
@@ -712,8 +713,34 @@ struct Solver {
         }
         return resid_grid;
     }
+    // a streamed kernel's persistent grid, after its shared-memory opt-in (cached)
+    template <class K>
+    int stream_grid_for(K kernel, int smem, int& cache) {
+        if (cache == 0) {
+            if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) return -1;
+            int c = 0;
+            if (persistent_grid(kernel, c, smem) < 0) return -1;
+            cache = c;
+        }
+        return cache;
+    }
+    // most entries of the last step had 32-bit columns (a grid whose x planes span more
+    // than the 16-bit offsets reach): stream the 32-bit columns of every slice instead
+    bool prefer_wide = false;
+    int spmv_wide_grid[2] = {0, 0}, spmv16_wide_grid = 0;
     template <int MODE>
     void spmv_stream(const float* w, const float* x, float* y, const double* b, int slot) {
+        if (prefer_wide) {
+            auto k = k_spmv_stream<MODE, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks, float, true>;
+            constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps, float, true>();
+            const int g = stream_grid_for(k, smem, spmv_wide_grid[MODE == 0 ? 0 : 1]);
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, smem, st>>>(d, w, x, y, b, slot);
+            return;
+        }
         const int g = stream_blocks();
         if (g < 0) {
             stream_failed = true;
@@ -729,6 +756,18 @@ struct Solver {
     static constexpr int kS16Smem = stream_smem_bytes<kS16Entries, kSsStages, kSsWarps, __half>();
     int spmv16_grid = 0;
     void spmv_stream16(const float* x, float* y) {
+        if (prefer_wide) {
+            // 8 entries of 32-bit column + FP16 weight per stage: the FP32 ring's 1.5 KB
+            auto kw = k_spmv_stream<0, kSsEntries, kSsStages, kSsWarps, kSsMinBlocks, __half, true>;
+            constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps, __half, true>();
+            const int g = stream_grid_for(kw, smem, spmv16_wide_grid);
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH kw<<<g, kSsWarps * 32, smem, st>>>(d, d.w16, x, y, nullptr, 0);
+            return;
+        }
         auto k = k_spmv_stream<0, kS16Entries, kSsStages, kSsWarps, kSsMinBlocks, __half>;
         if (spmv16_grid == 0) {
             if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kS16Smem) ||
@@ -960,6 +999,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->matrix_free = 0;
     o->spmv_stream = 1;
     o->inner_weights = 16;
+    o->spmv_wide = 0;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -970,6 +1010,7 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (o.matrix_free != 0 && o.matrix_free != 4 && o.matrix_free != 8) return CCT_PARAMERR;
     if (o.spmv_stream != 0 && o.spmv_stream != 1) return CCT_PARAMERR;
     if (o.inner_weights != 32 && o.inner_weights != 16) return CCT_PARAMERR;
+    if (o.spmv_wide < -1 || o.spmv_wide > 1) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {
@@ -1084,9 +1125,9 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     mps::Solver& S = s->s;
     mps::Dev& d = S.d;
     if (S.fp64() || d.n <= 0) return CCT_PARAMERR;
-    if (kernel != 0 && kernel != 1 && kernel != 2 && kernel != 4 && kernel != 8) return CCT_PARAMERR;
-    if (kernel == 1 && !d.rows16) return CCT_PARAMERR;
-    if (kernel == 2 && !(d.rows16 && d.rows_w16)) return CCT_PARAMERR;
+    if (kernel < 0 || kernel > 8 || kernel == 5 || kernel == 7) return CCT_PARAMERR;
+    if ((kernel == 1 || kernel == 3) && !d.rows16) return CCT_PARAMERR;
+    if ((kernel == 2 || kernel == 6) && !(d.rows16 && d.rows_w16)) return CCT_PARAMERR;
     const float* w = (const float*)d.nbrw;
     cudaError_t e = cudaMemcpyAsync(d.p32, host_x, sizeof(float) * d.n, cudaMemcpyHostToDevice, S.st);
     // MODE 0 returns at once after a converged solve: clear the flag (the next CG start sets it)
@@ -1094,10 +1135,13 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     if (e) return CCT_CUDAERR;
     if (kernel == 0)
         MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
-    else if (kernel == 1)
-        S.spmv_stream<0>(w, d.p32, d.q32, nullptr, 0);
-    else if (kernel == 2)
-        S.spmv_stream16(d.p32, d.q32);
+    else if (kernel == 1 || kernel == 2 || kernel == 3 || kernel == 6) {
+        const bool keep = S.prefer_wide;
+        S.prefer_wide = kernel == 3 || kernel == 6;
+        if (kernel == 1 || kernel == 3) S.spmv_stream<0>(w, d.p32, d.q32, nullptr, 0);
+        else S.spmv_stream16(d.p32, d.q32);
+        S.prefer_wide = keep;
+    }
     else if (kernel == 4)
         MPS_COUNT_LAUNCH mps::k_spmv<float, float, float, 0, 4><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.p32, d.q32, nullptr, 0);
     else

@@ -25,7 +25,8 @@ class MpsSolverOptions(C.Structure):
                 ("ir_max_outer", C.c_int), ("max_neighbours", C.c_int), ("check_every", C.c_int),
                 ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
                 ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int),
-                ("matrix_free", C.c_int), ("spmv_stream", C.c_int), ("inner_weights", C.c_int)]
+                ("matrix_free", C.c_int), ("spmv_stream", C.c_int), ("inner_weights", C.c_int),
+                ("spmv_wide", C.c_int)]
 
 
 class MpsStepStats(C.Structure):
@@ -192,8 +193,8 @@ class Solver:
 
     def debug_spmv(self, kernel: int, x: np.ndarray) -> np.ndarray:
         """One FP32 inner SpMV y = A x over the current rows with the named kernel
-        (0 register walk, 1 streamed, 4 / 8 matrix-free; 2 the FP16-weight operator),
-        solver order."""
+        (0 register walk, 1 streamed, 3 streamed 32-bit columns, 4 / 8 matrix-free; 2 / 6
+        the FP16-weight operator with 16-bit / 32-bit columns), solver order."""
         n = self.state(sort_by_id=False)["id"].shape[0]
         xs = np.ascontiguousarray(x, dtype=np.float32)
         if xs.shape != (n,):

@@ -172,7 +172,7 @@ def test_spmv_kernels_give_identical_rows():
     x = np.random.default_rng(7).standard_normal(n).astype(np.float32)
     y0 = s.debug_spmv(0, x)
     assert np.isfinite(y0).all() and np.count_nonzero(y0) > n // 2
-    for k in (1, 4, 8):
+    for k in (1, 3, 4, 8):
         yk = s.debug_spmv(k, x)
         assert np.array_equal(y0.view(np.uint32), yk.view(np.uint32)), (k, np.abs(yk - y0).max())
 
@@ -209,6 +209,22 @@ def test_fp16_inner_operator():
     y32, y16 = a.debug_spmv(0, x), a.debug_spmv(2, x)
     assert np.linalg.norm(y16 - y32) <= 1e-3 * np.linalg.norm(y32)
     assert not np.array_equal(y16, y32)
+    assert np.array_equal(y16.view(np.uint32), a.debug_spmv(6, x).view(np.uint32))
+
+
+@pytest.mark.parametrize("inner", [16, 32])
+def test_wide_column_streaming_step(inner):
+    """Streaming every slice's 32-bit columns (the choice for grids whose x planes
+    exceed the 16-bit offsets) converges like the 16-bit slices."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=4, drag_index=0.5)
+    a = Solver(sc, precision="fp32_ir", inner_weights=inner, spmv_wide=1)
+    b = Solver(sc, precision="fp32_ir", inner_weights=inner, spmv_wide=-1)
+    for i in range(3):
+        sa, sb = a.step(i), b.step(i)
+        assert sa["error_flags"] == 0 and sa["cg_relres"] <= 1e-8, sa
+        assert abs(sa["cg_iterations"] - sb["cg_iterations"]) <= 2
+    pa, pb = a.state()["press"], b.state()["press"]
+    assert np.abs(pa - pb).max() <= 1e-5 * np.abs(pb).max()
 
 
 def test_streamed_spmv_step_matches():
@@ -227,7 +243,7 @@ def test_streamed_spmv_step_matches():
 
 def test_spmv_options_are_checked():
     sc = scenes.rotating_bucket(l0=0.008, n_drag=0)
-    for bad in ({"matrix_free": 3}, {"spmv_stream": 2}, {"inner_weights": 8}):
+    for bad in ({"matrix_free": 3}, {"spmv_stream": 2}, {"inner_weights": 8}, {"spmv_wide": 2}):
         with pytest.raises(MpsError) as e:
             Solver(sc, precision="fp32_ir", **bad)
         assert e.value.status == 2   # CCT_PARAMERR
