@@ -146,7 +146,7 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
  * array of n doubles, may be NULL) and ||r|| / ||b||: variant 0 with FP64
  * products and sums, variant 1 with the double-float kernel the solver uses (rows
  * streamed through shared memory when spmv_stream is on), variant 2 the double-float
- * register walk */
+ * register walk, variant 3 the double-float kernel streaming 32-bit columns */
 CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, double* relres);
 /* One FP32 inner SpMV y = A x over the current rows (FP32_IR solvers; host arrays of
  * n floats in the solver's order): kernel 0 register walk, 1 rows streamed through

@@ -1335,7 +1335,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
 // same per-entry operations and accumulator order as k_residual_df (entries of even
 // index into the first (hi, lo) pair, odd into the second, merged at the end), so r
 // is bit-identical to it.  Norms -> S_RR / S_RNORM and ||b|| -> S_BNORM.
-template <int SC, int SS, int W, int MINB>
+template <int SC, int SS, int W, int MINB, bool WIDE = false>
 __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_constant__ Dev d,
                                                                  const float* __restrict__ w,
                                                                  const double* __restrict__ x,
@@ -1346,8 +1346,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
     __shared__ __align__(8) unsigned long long bars[W][SS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
-    SliceRing<SC, SS, float> R;
-    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, float>::SB, bars[warp], gw, nw);
+    SliceRing<SC, SS, float, WIDE> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, float, WIDE>::SB, bars[warp], gw, nw);
     const float* __restrict__ xh = d.xh;
     const float* __restrict__ xl = d.xl;
 
@@ -1360,8 +1360,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
         const int km = d.skmax[sl];
         float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
         bool done = false;
-        if (km >= 0 && R.streaming) {
-            const int nc = (km + SC - 1) / SC;
+        if ((WIDE || km >= 0) && R.streaming) {
+            const int nc = (slice_kmax(km) + SC - 1) / SC;
             const int r0 = sl * 32;
             for (int c = 0; c < nc; ++c) {
                 const unsigned char* cs;
@@ -1374,7 +1374,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
                     float wv[8], h[8], l[8];
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
-                        j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
+                        if constexpr (WIDE) j[u] = ((const int*)cs)[(g + u) * 32 + lane];
+                        else j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
                         wv[u] = ws[(g + u) * 32 + lane];
                     }
 #pragma unroll

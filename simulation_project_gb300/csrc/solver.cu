@@ -727,7 +727,7 @@ struct Solver {
     // most entries of the last step had 32-bit columns (a grid whose x planes span more
     // than the 16-bit offsets reach): stream the 32-bit columns of every slice instead
     bool prefer_wide = false;
-    int spmv_wide_grid[2] = {0, 0}, spmv16_wide_grid = 0;
+    int spmv_wide_grid[2] = {0, 0}, spmv16_wide_grid = 0, resid_wide_grid = 0;
     template <int MODE>
     void spmv_stream(const float* w, const float* x, float* y, const double* b, int slot) {
         if (prefer_wide) {
@@ -875,7 +875,16 @@ struct Solver {
     // (rows streamed through shared memory over the 16-bit slices, else the register walk)
     void residual_df(const float* w, bool stream = true) {
         MPS_COUNT_LAUNCH k_split_x<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.xh, d.xl);
-        if (stream && use_stream()) {
+        if (stream && use_stream() && prefer_wide) {
+            auto k = k_residual_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks, true>;
+            constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps, float, true>();
+            const int g = stream_grid_for(k, smem, resid_wide_grid);
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, smem, st>>>(d, w, d.press, d.r, d.rhs, 2);
+        } else if (stream && use_stream()) {
             const int g = resid_blocks();
             if (g < 0) {
                 stream_failed = true;
@@ -1107,13 +1116,17 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_
     if (!s) return CCT_PARAMERR;
     mps::Solver& S = s->s;
     mps::Dev& d = S.d;
-    if (S.fp64() || d.n <= 0) return CCT_PARAMERR;
+    if (S.fp64() || d.n <= 0 || variant < 0 || variant > 3) return CCT_PARAMERR;
     const float* w = (const float*)d.nbrw;
     if (variant == 0)
         MPS_COUNT_LAUNCH mps::k_spmv<float, double, double, 1><<<mps::kRedBlocks, 256, 0, S.st>>>(d, w, d.press, d.r,
                                                                                                   d.rhs, 2);
-    else
-        S.residual_df(w, variant == 1);
+    else {
+        const bool keep = S.prefer_wide;
+        if (variant == 3) S.prefer_wide = true;
+        S.residual_df(w, variant == 1 || variant == 3);
+        S.prefer_wide = keep;
+    }
     if (S.stream_failed || S.pull_scal()) return CCT_CUDAERR;
     if (relres) *relres = S.h_scal[mps::S_BNORM] > 0 ? S.h_scal[mps::S_RNORM] / S.h_scal[mps::S_BNORM] : 0.0;
     if (host_r) return mps::cuda_status(cudaMemcpy(host_r, d.r, sizeof(double) * d.n, cudaMemcpyDeviceToHost));

@@ -186,7 +186,10 @@ def test_streamed_residual_is_bit_identical():
         s.step(i)
     r1, rel1 = s.debug_residual(1)
     r2, rel2 = s.debug_residual(2)
-    assert np.array_equal(r1, r2) and rel1 == rel2
+    r3, rel3 = s.debug_residual(3)
+    # rows bit-identical; the norms are grid reductions over different grids
+    assert np.array_equal(r1, r2) and abs(rel1 - rel2) <= 1e-12 * rel1
+    assert np.array_equal(r1, r3) and abs(rel1 - rel3) <= 1e-12 * rel1
     r0, rel0 = s.debug_residual(0)
     assert np.abs(r1 - r0).max() <= 1e-10 * np.abs(s.debug_ppe()["rhs"]).max()
 
