@@ -92,6 +92,10 @@ struct Solver {
     int models = 0;
     int walls_move = 0;
     cudaStream_t st = nullptr;
+    // second stream: the multilevel setup runs there beside the learned guess
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_rows = nullptr, ev_mg = nullptr;
+    bool mg_setup_done = false;   // this step's hierarchy is already built
     std::vector<void*> allocs;
     void* sort_scratch = nullptr;
     size_t sort_scratch_bytes = 0;
@@ -175,6 +179,10 @@ struct Solver {
         c.explicit_pressure = opt.pressure_mode == MPS_PRESSURE_EXPLICIT;
         timer.on = opt.profile != 0;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CCT_CUDAERR;
+        if (cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_rows, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_mg, cudaEventDisableTiming) != cudaSuccess)
+            return CCT_CUDAERR;
         const size_t N = nmax;
         const size_t wsz = sizeof(double);   // room for FP64 rows: the precision can be switched
         cudaError_t e = cudaSuccess;
@@ -257,6 +265,9 @@ struct Solver {
         if (mlp) mps_mlp_destroy(mlp);
         mlp = nullptr;
         if (st) cudaStreamDestroy(st);
+        if (st2) cudaStreamDestroy(st2);
+        if (ev_rows) cudaEventDestroy(ev_rows);
+        if (ev_mg) cudaEventDestroy(ev_mg);
     }
 
     void swap_state() {
@@ -380,7 +391,7 @@ struct Solver {
 
     // aggregates, links and operators of the current particle order (after the PPE
     // setup: needs interior flags, diagonals and the FP32 neighbour rows)
-    CCTStatusType mg_setup() {
+    CCTStatusType mg_setup(cudaStream_t ss) {
         mg_ready = false;
         if (opt.preconditioner != MPS_PRECOND_MULTILEVEL && !mg_init_done) return CCT_NOERR;
         if (opt.preconditioner == MPS_PRECOND_MULTILEVEL && !mg_init_done) {
@@ -389,16 +400,16 @@ struct Solver {
         }
         if (!mg_on || opt.preconditioner != MPS_PRECOND_MULTILEVEL || d.n <= 0) return CCT_NOERR;
         MgLevel* L = mg.L;
-        MPS_COUNT_LAUNCH k_mg_flags1<<<blocks_for(d.cells), kBlock, 0, st>>>(d, mg_flag);
+        MPS_COUNT_LAUNCH k_mg_flags1<<<blocks_for(d.cells), kBlock, 0, ss>>>(d, mg_flag);
         for (int l = 1; l <= mg_grid_levels; ++l) {
             const int nc = L[l].gx * L[l].gy * L[l].gz;
-            if (l > 1) MPS_COUNT_LAUNCH k_mg_flags_up<<<blocks_for(nc), kBlock, 0, st>>>(L[l - 1], L[l], mg_flag);
-            if (scan_exclusive(mg_flag, nc, mg_flag + nc, st, scan_sums)) return CCT_CUDAERR;
-            MPS_COUNT_LAUNCH k_mg_fill<<<blocks_for(nc), kBlock, 0, st>>>(L[l], mg_flag);
-            cudaMemcpyAsync(mg_counts + l, mg_flag + nc, sizeof(unsigned), cudaMemcpyDeviceToDevice, st);
+            if (l > 1) MPS_COUNT_LAUNCH k_mg_flags_up<<<blocks_for(nc), kBlock, 0, ss>>>(L[l - 1], L[l], mg_flag);
+            if (scan_exclusive(mg_flag, nc, mg_flag + nc, ss, scan_sums)) return CCT_CUDAERR;
+            MPS_COUNT_LAUNCH k_mg_fill<<<blocks_for(nc), kBlock, 0, ss>>>(L[l], mg_flag);
+            cudaMemcpyAsync(mg_counts + l, mg_flag + nc, sizeof(unsigned), cudaMemcpyDeviceToDevice, ss);
         }
-        cudaMemcpyAsync(h_counts, mg_counts, sizeof(unsigned) * (kMgMaxLevels + 1), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
+        cudaMemcpyAsync(h_counts, mg_counts, sizeof(unsigned) * (kMgMaxLevels + 1), cudaMemcpyDeviceToHost, ss);
+        if (cudaStreamSynchronize(ss)) return CCT_CUDAERR;
         int levels = 0;
         for (int l = 1; l <= mg_grid_levels; ++l) {
             L[l].n = (int)h_counts[l];
@@ -407,14 +418,14 @@ struct Solver {
         if (!levels || L[1].n <= 0) return CCT_NOERR;   // no small enough level: Jacobi this step
         mg.levels = levels;
         for (int l = 1; l <= levels; ++l)
-            MPS_COUNT_LAUNCH k_mg_links<<<blocks_for(L[l].n), kBlock, 0, st>>>(L[l], L[l < levels ? l + 1 : l], l < levels);
-        MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, st>>>(d, mg);
-        MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, st>>>(d, mg, (const float*)d.nbrw);
-        MPS_COUNT_LAUNCH k_mg_assemble_cells<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d, mg);
+            MPS_COUNT_LAUNCH k_mg_links<<<blocks_for(L[l].n), kBlock, 0, ss>>>(L[l], L[l < levels ? l + 1 : l], l < levels);
+        MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, ss>>>(d, mg);
+        MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, ss>>>(d, mg, (const float*)d.nbrw);
+        MPS_COUNT_LAUNCH k_mg_assemble_cells<<<div_up(L[1].n * 32, 256), 256, 0, ss>>>(d, mg);
         for (int l = 1; l < levels; ++l)
-            MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, st>>>(L[l], L[l + 1]);
+            MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, ss>>>(L[l], L[l + 1]);
         const int nd = L[levels].n;
-        MPS_COUNT_LAUNCH k_mg_dense_inverse<<<1, 1024, (2 * nd * nd + nd) * sizeof(float), st>>>(L[levels], mg.ainv);
+        MPS_COUNT_LAUNCH k_mg_dense_inverse<<<1, 1024, (2 * nd * nd + nd) * sizeof(float), ss>>>(L[levels], mg.ainv);
         if (cudaGetLastError()) return CCT_CUDAERR;
         mg_ready = true;
         return CCT_NOERR;
@@ -578,6 +589,11 @@ struct Solver {
                 d.rows_w16 = w16;
             }
             const bool use_learned = learned_ready && opt.learned;
+            // the multilevel setup only needs the rows: with the learned guess it runs on
+            // the second stream meanwhile (enqueued after the learned kernels below)
+            const bool overlap_mg = use_learned && !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
+            mg_setup_done = false;
+            if (overlap_mg) cudaEventRecord(ev_rows, st);
             if (use_learned || collect) {
                 timer.mark(PH_LEARNED, st);
                 cudaMemcpyAsync(d.pprev, d.press, sizeof(double) * d.n, cudaMemcpyDeviceToDevice, st);
@@ -607,6 +623,13 @@ struct Solver {
                     }
                 }
                 timer.mark(PH_SETUP, st);
+            }
+            if (overlap_mg) {
+                cudaStreamWaitEvent(st2, ev_rows, 0);
+                if (mg_setup(st2)) return CCT_CUDAERR;
+                cudaEventRecord(ev_mg, st2);
+                cudaStreamWaitEvent(st, ev_mg, 0);
+                mg_setup_done = true;
             }
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
             if (use_learned && S.cg_relres > opt.cg_rtol) {
@@ -910,7 +933,8 @@ struct Solver {
         const float* w = (const float*)d.nbrw;
         MPS_COUNT_LAUNCH k_to_float<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.minv, d.m32);
         timer.mark(PH_PRECOND, st);
-        if (mg_setup()) return CCT_CUDAERR;
+        if (!mg_setup_done && mg_setup(st)) return CCT_CUDAERR;
+        mg_setup_done = false;
         S.mg_levels = mg_ready ? mg.levels : 0;
         S.mg_level1 = mg_ready ? mg.L[1].n : 0;
         timer.mark(PH_VEC, st);
