@@ -314,6 +314,7 @@ def run_gpu(args):
 
     # end to end through the C-ABI from pinned host buffers
     e2e = run_e2e(fast, args)
+    frames = frames_bench(fast, n, args)
     fast.close()
     sort = sort_bench(n, scene.box.cell_num, peak_gbs)
     accuracy = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
@@ -365,6 +366,7 @@ def run_gpu(args):
         "sort": sort,
         "accuracy_vs_fp64": accuracy,
         "e2e": e2e,
+        "frames": frames,
         "gpu_launches": int(st_fast[0]["launches_in_region"]),
         "clocks": clk,
     }
@@ -495,6 +497,50 @@ def run_accuracy_only(args):
     print(json.dumps({"accuracy_vs_fp64": acc, "workload": WORKLOADS[args.workload].format(l0=args.l0),
                       "particles": scene.n, "learned": params is not None, "seconds": time.perf_counter() - t0}))
     return 0
+
+
+def frames_bench(solver, n, args, steps=5):
+    """Output frames (reference format, mps_solver_save_frame) outside the timed region:
+    wall time per step with and without a binary frame after every step (the pack, the
+    pinned copy and the file write overlap the next steps), and the latency of one frame
+    in each format.  Files go to a temporary directory."""
+    import shutil
+    import tempfile
+    from simulation_project_gb300 import lib
+    tmp = tempfile.mkdtemp(prefix="mps_frames_")
+    try:
+        first = 10_000
+        def run(with_frames):
+            lib.call("mps_device_sync")
+            t0 = time.perf_counter()
+            for k in range(steps):
+                solver.step(first + k)
+                if with_frames:
+                    solver.save_frame(os.path.join(tmp, f"f{k % 2}.dat"), ascii=False, time=k * 5e-5)
+            solver.wait_frames()
+            lib.call("mps_device_sync")
+            return (time.perf_counter() - t0) * 1e3 / steps
+        run(False)
+        base = run(False)
+        first += steps
+        with_f = run(True)
+        out = {"particles": n, "steps": steps, "wall_ms_per_step": round(base, 3),
+               "wall_ms_per_step_binary_frame_each_step": round(with_f, 3),
+               "overhead_ms_per_step": round(with_f - base, 3),
+               "binary_bytes": 4 + 48 * n + 8}
+        for ascii in (False, True):
+            lib.call("mps_device_sync")
+            t0 = time.perf_counter()
+            solver.save_frame(os.path.join(tmp, "one.dat"), ascii=ascii)
+            solver.wait_frames()
+            out["ascii_frame_ms" if ascii else "binary_frame_ms"] = round((time.perf_counter() - t0) * 1e3, 2)
+            if ascii:
+                out["ascii_bytes"] = os.path.getsize(os.path.join(tmp, "one.dat"))
+        return out
+    except Exception as e:  # pragma: no cover - reported, not fatal for the metric
+        return {"error": str(e)}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
 
 
 def run_e2e(solver, args):

@@ -21,6 +21,14 @@
  *   mps_grid_box             CCellSet::SetComputeZone, CGPUCellSet.cpp:109-152.
  *   mps_lattice_constants    n0 and lambda of the cubic lattice for a radius (FP64);
  *                            no reference counterpart (it reads n0 from the file).
+ *   mps_write_frame          IO::Save / SaveAscii / SaveBinary, IO.cpp:649-756: an output
+ *                            frame.  ASCII: count; "x y z vx vy vz P n T nu solidRate
+ *                            type" per particle (%g, 6 significant digits, as the
+ *                            reference's std::ostream); time; model count; "x\ty\tz\t
+ *                            angle" per model.  Binary: int32 count, 48-byte records
+ *                            (3+3+5 floats, int32 type), float time, int32 model count,
+ *                            4 floats per model.  temperature / solid_rate may be NULL
+ *                            (written as 0).
  * All return CCT_NOERR, CCT_FILEERR (cannot open / malformed) or CCT_PARAMERR.
  */
 #ifndef MPS_IO_H
@@ -39,6 +47,10 @@ CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset
 float mps_lambda_table(float l0);
 CCTStatusType mps_grid_box(const CBox* compute_zone, const CParameter* param, CGridBox* out);
 CCTStatusType mps_lattice_constants(double re_coefficient, double l0, int dimension, double* n0, double* lambda);
+CCTStatusType mps_write_frame(const char* path, int ascii, int n, const Scalar3* pos, const Scalar3* vel,
+                              const Scalar* pressure, const Scalar* density, const Scalar* temperature,
+                              const Scalar* viscosity, const Scalar* solid_rate, const ParticleType* type,
+                              Scalar time, int models, const Scalar3* model_pos, const Scalar* model_angle);
 
 #ifdef __cplusplus
 }

@@ -155,6 +155,17 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, do
  * operator (inner_weights = 16) with 16-bit / 32-bit columns, the same bits as each
  * other. */
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
+/* Output frame of the current state in the reference's format (IO::Save,
+ * radix/SPVSOLVER/MultiGPUSolver/IO.cpp:649-756; see mps_write_frame in mps_io.h):
+ * particles in ID order with position, velocity, pressure, PND as the density,
+ * viscosity and type (temperature and solid rate, not modelled here, are written as 0),
+ * the time and `models` model positions / rotation angles.  The state is packed on the
+ * solver stream at this point of the step sequence and copied to pinned host memory on
+ * a stream of its own; a host thread writes the file while later steps run (two frames
+ * in flight).  mps_solver_wait_frames waits for them and returns the first write error. */
+CCTStatusType mps_solver_save_frame(MpsSolver* s, const char* path, int ascii, double time, int models,
+                                    const Scalar3* model_pos, const Scalar* model_angle);
+CCTStatusType mps_solver_wait_frames(MpsSolver* s);
 /* Device pointer of the pressure array (FP64, sorted order) and particle count. */
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n);
 /* Pressure read back to a host buffer, in the solver's order (e2e output). */

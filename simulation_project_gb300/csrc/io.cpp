@@ -1,5 +1,8 @@
 // io.cpp - the reference's input formats (include/mps_io.h), host C++ without Boost.
+#include <algorithm>
 #include <cfloat>
+#include <charconv>
+#include <cstdio>
 #include <climits>
 #include <cmath>
 #include <cstdint>
@@ -7,6 +10,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/mps_io.h"
@@ -336,3 +340,142 @@ CCTStatusType mps_lattice_constants(double re, double l0, int dim, double* n0, d
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Output frames: IO::Save / SaveAscii / SaveBinary, radix/SPVSOLVER/MultiGPUSolver/
+// IO.cpp:649-756.  ASCII: the count, one line per particle "x y z vx vy vz P n T nu
+// solidRate type" (std::ostream defaults: %g with 6 significant digits, the type as an
+// integer), the time, the model count and "x\ty\tz\tangle" per model.  Binary: int32
+// count, per particle 3 + 3 + 5 floats and an int32 type (48 bytes), the float time,
+// int32 model count and 3 + 1 floats per model.  Built in one host buffer, one write.
+// ---------------------------------------------------------------------------
+static_assert(sizeof(ParticleType) == 4 && sizeof(Scalar3) == 12, "ParticleType is an int32, Scalar3 3 floats");
+
+namespace {
+
+// %g with 6 significant digits, as std::ostream's defaults and printf("%g") print a
+// float; std::to_chars in chars_format::general with a precision is specified to give
+// printf's %.*g text and is much faster than snprintf
+void put_g(std::string& b, double v) {
+    char t[32];
+    const std::to_chars_result r = std::to_chars(t, t + sizeof t, v, std::chars_format::general, 6);
+    b.append(t, (size_t)(r.ptr - t));
+}
+void put_i(std::string& b, long long v) {
+    char t[24];
+    const int k = std::snprintf(t, sizeof t, "%lld", v);
+    b.append(t, (size_t)(k > 0 ? k : 0));
+}
+
+}  // namespace
+
+namespace {
+
+struct FrameRecord {   // one binary record of IO::SaveBinary (IO.cpp:729-739)
+    Scalar3 pos, vel;
+    Scalar pressure, density, temperature, viscosity, solid;
+    Integer type;
+};
+static_assert(sizeof(FrameRecord) == 48, "binary frame records are 48 bytes");
+
+// the ASCII lines of particles [a, b)
+void ascii_lines(std::string& b, int a, int e, const Scalar3* pos, const Scalar3* vel, const Scalar* pressure,
+                 const Scalar* density, const Scalar* temperature, const Scalar* viscosity, const Scalar* solid_rate,
+                 const ParticleType* type) {
+    b.reserve((size_t)(e - a) * 96);
+    for (int i = a; i < e; ++i) {
+        put_g(b, pos[i].x); b += ' ';
+        put_g(b, pos[i].y); b += ' ';
+        put_g(b, pos[i].z); b += ' ';
+        put_g(b, vel[i].x); b += ' ';
+        put_g(b, vel[i].y); b += ' ';
+        put_g(b, vel[i].z); b += ' ';
+        put_g(b, pressure[i]); b += ' ';
+        put_g(b, density[i]); b += ' ';
+        put_g(b, temperature ? temperature[i] : 0.0f); b += ' ';
+        put_g(b, viscosity[i]); b += ' ';
+        put_g(b, solid_rate ? solid_rate[i] : 0.0f); b += ' ';
+        put_i(b, (long long)type[i]);
+        b += '\n';
+    }
+}
+
+}  // namespace
+
+extern "C" CCTStatusType mps_write_frame(const char* path, int ascii, int n, const Scalar3* pos, const Scalar3* vel,
+                                         const Scalar* pressure, const Scalar* density, const Scalar* temperature,
+                                         const Scalar* viscosity, const Scalar* solid_rate, const ParticleType* type,
+                                         Scalar time, int models, const Scalar3* model_pos,
+                                         const Scalar* model_angle) {
+    if (!path || n < 0 || models < 0) return CCT_PARAMERR;
+    if (n > 0 && (!pos || !vel || !pressure || !density || !viscosity || !type)) return CCT_PARAMERR;
+    if (models > 0 && (!model_pos || !model_angle)) return CCT_PARAMERR;
+    FILE* f = std::fopen(path, ascii ? "w" : "wb");
+    if (!f) return CCT_FILEERR;
+    bool ok = true;
+    auto put = [&](const void* p, size_t bytes) { ok = ok && std::fwrite(p, 1, bytes, f) == bytes; };
+    if (ascii) {
+        std::string head;
+        put_i(head, n);
+        head += '\n';
+        put(head.data(), head.size());
+        // particle lines formatted by up to 16 host threads in contiguous chunks, written
+        // in order (the bytes do not depend on the split)
+        const int nt = n < 4096 ? 1 : (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+        std::vector<std::string> part((size_t)nt);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t) {
+            const int a = (int)((long long)n * t / nt), e = (int)((long long)n * (t + 1) / nt);
+            auto job = [&, t, a, e]() {
+                ascii_lines(part[(size_t)t], a, e, pos, vel, pressure, density, temperature, viscosity, solid_rate,
+                            type);
+            };
+            if (t + 1 < nt) th.emplace_back(job);
+            else job();
+        }
+        for (std::thread& x : th) x.join();
+        for (const std::string& p : part) put(p.data(), p.size());
+        std::string tail;
+        put_g(tail, time);
+        tail += '\n';
+        put_i(tail, models);
+        tail += '\n';
+        for (int m = 0; m < models; ++m) {
+            put_g(tail, model_pos[m].x); tail += '\t';
+            put_g(tail, model_pos[m].y); tail += '\t';
+            put_g(tail, model_pos[m].z); tail += '\t';
+            put_g(tail, model_angle[m]);
+            tail += '\n';
+        }
+        put(tail.data(), tail.size());
+    } else {
+        const Integer cnt = n;
+        put(&cnt, sizeof cnt);
+        constexpr int kChunk = 16384;   // records per write (768 KB)
+        std::vector<FrameRecord> rec((size_t)std::min(n, kChunk));
+        for (int a = 0; a < n && ok; a += kChunk) {
+            const int e = std::min(n, a + kChunk);
+            for (int i = a; i < e; ++i) {
+                FrameRecord& r = rec[(size_t)(i - a)];
+                r.pos = pos[i];
+                r.vel = vel[i];
+                r.pressure = pressure[i];
+                r.density = density[i];
+                r.temperature = temperature ? temperature[i] : 0.0f;
+                r.viscosity = viscosity[i];
+                r.solid = solid_rate ? solid_rate[i] : 0.0f;
+                r.type = (Integer)type[i];
+            }
+            put(rec.data(), sizeof(FrameRecord) * (size_t)(e - a));
+        }
+        put(&time, sizeof time);
+        const Integer mc = models;
+        put(&mc, sizeof mc);
+        for (int m = 0; m < models; ++m) {
+            put(&model_pos[m], sizeof(Scalar3));
+            put(&model_angle[m], sizeof(Scalar));
+        }
+    }
+    const int c = std::fclose(f);
+    return (ok && c == 0) ? CCT_NOERR : CCT_FILEERR;
+}

@@ -1532,6 +1532,30 @@ __global__ void k_pack_state(const __grid_constant__ Dev d, const double* p3, co
     d.vel[i] = make_dbl4(v3[3 * (size_t)i], v3[3 * (size_t)i + 1], v3[3 * (size_t)i + 2], 0.0);
     d.press[i] = pr[i];
 }
+// output frames in particle-ID order: mark the IDs present (the exclusive scan of the
+// marks is each ID's row), then pack position, velocity, pressure, PND, viscosity
+// (FP32) and type at that row: out = [pos 3n | vel 3n | press n | pnd n | visc n]
+__global__ void k_frame_mark(const __grid_constant__ Dev d, unsigned* flag, int idcap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int id = d.id[i];
+    if (id >= 0 && id < idcap) flag[id] = 1u;
+}
+__global__ void k_frame_pack(const __grid_constant__ Dev d, const unsigned* rank, int idcap, float* out, int* otype) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int id = d.id[i];
+    if (id < 0 || id >= idcap) return;
+    const size_t n = (size_t)d.n, r = rank[id];
+    if (r >= n) return;
+    const dbl4 p = d.pos[i], v = d.vel[i];
+    out[3 * r] = (float)p.x; out[3 * r + 1] = (float)p.y; out[3 * r + 2] = (float)p.z;
+    out[3 * n + 3 * r] = (float)v.x; out[3 * n + 3 * r + 1] = (float)v.y; out[3 * n + 3 * r + 2] = (float)v.z;
+    out[6 * n + r] = (float)d.press[i];
+    out[7 * n + r] = (float)d.pnd[i];
+    out[8 * n + r] = d.visc[i];
+    otype[r] = d.type[i];
+}
 __global__ void k_unpack_state(const __grid_constant__ Dev d, double* p3, double* v3, double* pr) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;

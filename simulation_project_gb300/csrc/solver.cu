@@ -17,9 +17,12 @@
 #include <cstdio>
 #include <cstring>
 #include <random>
+#include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
+#include "../../include/mps_io.h"
 #include "native_kernels.cuh"
 #include "coarse.cuh"
 #include "../../include/mps_learned.h"
@@ -245,6 +248,15 @@ struct Solver {
     }
 
     void destroy() {
+        frames_wait();
+        for (FrameSlot& f : fslot) {
+            if (f.h) cudaFreeHost(f.h);
+            if (f.ht) cudaFreeHost(f.ht);
+            if (f.copied) cudaEventDestroy(f.copied);
+        }
+        // d_frame, d_ftype and d_fflag come from mk(): freed with `allocs` below
+        if (ev_packed) cudaEventDestroy(ev_packed);
+        if (st_io) cudaStreamDestroy(st_io);
         cudaDeviceSynchronize();
         for (void* p : allocs) cudaFree(p);
         allocs.clear();
@@ -997,6 +1009,97 @@ struct Solver {
         return cuda_status(e);
     }
 
+    // ---- output frames: packed on the solver stream, copied to pinned host memory on
+    // a stream of their own, written to the file by a host thread (two slots) ----
+    struct FrameSlot {
+        float* h = nullptr;        // pinned: [pos 3n | vel 3n | press n | pnd n | visc n]
+        int* ht = nullptr;         // pinned: type
+        cudaEvent_t copied = nullptr;
+        std::thread th;
+        CCTStatusType rc = CCT_NOERR;
+        std::vector<Scalar3> mpos;
+        std::vector<Scalar> mang;
+    };
+    FrameSlot fslot[2];
+    int fnext = 0;
+    cudaStream_t st_io = nullptr;
+    float* d_frame = nullptr;
+    int* d_ftype = nullptr;
+    unsigned* d_fflag = nullptr;
+    CCTStatusType frame_rc = CCT_NOERR;   // first error of a finished write
+
+    CCTStatusType frames_init() {
+        if (d_frame) return CCT_NOERR;
+        const size_t N = nmax;
+        cudaError_t e = cudaStreamCreateWithFlags(&st_io, cudaStreamNonBlocking);
+        e = e ? e : mk(&d_frame, 9 * N); e = e ? e : mk(&d_ftype, N); e = e ? e : mk(&d_fflag, N + 1);
+        for (FrameSlot& f : fslot) {
+            e = e ? e : cudaMallocHost((void**)&f.h, sizeof(float) * 9 * N);
+            e = e ? e : cudaMallocHost((void**)&f.ht, sizeof(int) * N);
+            e = e ? e : cudaEventCreateWithFlags(&f.copied, cudaEventDisableTiming);
+        }
+        return e ? CCT_MEMERR : CCT_NOERR;
+    }
+    void frame_join(FrameSlot& f) {
+        if (f.th.joinable()) f.th.join();
+        if (frame_rc == CCT_NOERR && f.rc != CCT_NOERR) frame_rc = f.rc;
+        f.rc = CCT_NOERR;
+    }
+    CCTStatusType frames_wait() {
+        for (FrameSlot& f : fslot) frame_join(f);
+        const CCTStatusType rc = frame_rc;
+        frame_rc = CCT_NOERR;
+        return rc;
+    }
+    CCTStatusType save_frame(const char* path, int ascii, double time, int models, const Scalar3* mp, const Scalar* ma) {
+        if (!path || models < 0 || (models > 0 && (!mp || !ma))) return CCT_PARAMERR;
+        CCTStatusType rc = frames_init();
+        if (rc != CCT_NOERR) return rc;
+        FrameSlot& f = fslot[fnext];
+        frame_join(f);                         // its previous write is done: reuse the buffers
+        const int n = d.n;
+        const int idcap = (int)nmax;
+        // the previous frame's copy has left the device staging before it is repacked
+        cudaStreamWaitEvent(st, fslot[fnext ^ 1].copied, 0);
+        cudaMemsetAsync(d_fflag, 0, sizeof(unsigned) * ((size_t)idcap + 1), st);
+        if (n > 0) {
+            MPS_COUNT_LAUNCH k_frame_mark<<<blocks_for(n), kBlock, 0, st>>>(d, d_fflag, idcap);
+            scan_exclusive(d_fflag, idcap, d_fflag + idcap, st, scan_sums);
+            MPS_COUNT_LAUNCH k_frame_pack<<<blocks_for(n), kBlock, 0, st>>>(d, d_fflag, idcap, d_frame, d_ftype);
+        }
+        cudaEventRecord(ev_frame_packed(), st);
+        cudaStreamWaitEvent(st_io, ev_frame_packed(), 0);
+        cudaError_t e = cudaSuccess;
+        if (n > 0) {
+            e = cudaMemcpyAsync(f.h, d_frame, sizeof(float) * 9 * (size_t)n, cudaMemcpyDeviceToHost, st_io);
+            if (!e) e = cudaMemcpyAsync(f.ht, d_ftype, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, st_io);
+        }
+        if (!e) e = cudaEventRecord(f.copied, st_io);
+        if (e) return CCT_CUDAERR;
+        f.mpos.assign(mp, mp + models);
+        f.mang.assign(ma, ma + models);
+        const std::string fpath(path);
+        FrameSlot* fp = &f;
+        fp->th = std::thread([fp, fpath, ascii, n, time, models]() {
+            if (cudaEventSynchronize(fp->copied) != cudaSuccess) {
+                fp->rc = CCT_CUDAERR;
+                return;
+            }
+            const float* h = fp->h;
+            const size_t m = (size_t)n;
+            fp->rc = mps_write_frame(fpath.c_str(), ascii, n, (const Scalar3*)h, (const Scalar3*)(h + 3 * m), h + 6 * m,
+                                     h + 7 * m, nullptr, h + 8 * m, nullptr, (const ParticleType*)fp->ht, (Scalar)time,
+                                     models, fp->mpos.data(), fp->mang.data());
+        });
+        fnext ^= 1;
+        return CCT_NOERR;
+    }
+    cudaEvent_t ev_packed = nullptr;
+    cudaEvent_t ev_frame_packed() {
+        if (!ev_packed) cudaEventCreateWithFlags(&ev_packed, cudaEventDisableTiming);
+        return ev_packed;
+    }
+
     CCTStatusType step(int stepi, MpsStepStats* out, bool pressure_only = false) {
         return fp64() ? run_step<double>(stepi, out, pressure_only) : run_step<float>(stepi, out, pressure_only);
     }
@@ -1187,6 +1290,17 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     e = cudaMemcpyAsync(host_y, d.q32, sizeof(float) * d.n, cudaMemcpyDeviceToHost, S.st);
     if (!e) e = cudaStreamSynchronize(S.st);
     return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_save_frame(MpsSolver* s, const char* path, int ascii, double time, int models,
+                                    const Scalar3* model_pos, const Scalar* model_angle) {
+    if (!s) return CCT_PARAMERR;
+    return s->s.save_frame(path, ascii, time, models, model_pos, model_angle);
+}
+
+CCTStatusType mps_solver_wait_frames(MpsSolver* s) {
+    if (!s) return CCT_PARAMERR;
+    return s->s.frames_wait();
 }
 
 CCTStatusType mps_solver_device_pressure(MpsSolver* s, const double** press, int* n) {

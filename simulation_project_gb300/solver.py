@@ -65,6 +65,8 @@ _SIGS = {
     "mps_solver_debug_residual": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_double)]),
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
     "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
+    "mps_solver_save_frame": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, P, P]),
+    "mps_solver_wait_frames": (C.c_int, [P]),
     "mps_solver_copy_pressure": (C.c_int, [P, P]),
     "mps_solver_stream": (C.c_int, [P, C.POINTER(P)]),
     "mps_solver_upload_state": (C.c_int, [P, P, P, P]),
@@ -202,6 +204,19 @@ class Solver:
         y = np.zeros(n, np.float32)
         _check(_lib().mps_solver_debug_spmv(self.h, int(kernel), _p(xs), _p(y)), "mps_solver_debug_spmv")
         return y
+
+    def save_frame(self, path, ascii=False, time=0.0, model_pos=None, model_angle=None):
+        """Output frame of the current state (reference format, particles in ID order),
+        written by a host thread while later steps run; wait_frames() waits for it."""
+        mp = np.ascontiguousarray(np.zeros((0, 3)) if model_pos is None else model_pos, dtype=np.float32).reshape(-1, 3)
+        ma = np.ascontiguousarray(np.zeros(0) if model_angle is None else model_angle, dtype=np.float32)
+        if len(ma) != len(mp):
+            raise ValueError("one angle per model position")
+        _check(_lib().mps_solver_save_frame(self.h, str(path).encode(), int(bool(ascii)), float(time), len(ma),
+                                            _p(mp), _p(ma)), "mps_solver_save_frame")
+
+    def wait_frames(self):
+        _check(_lib().mps_solver_wait_frames(self.h), "mps_solver_wait_frames")
 
     def pressure(self, njp: bool = False) -> dict:
         """PPE solve at the current state (CalculatePressureNJPCG if njp, else CalculatePressureCG)."""
