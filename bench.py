@@ -499,7 +499,7 @@ def run_accuracy_only(args):
     return 0
 
 
-def frames_bench(solver, n, args, steps=5):
+def frames_bench(solver, n, args, steps=10):
     """Output frames (reference format, mps_solver_save_frame) outside the timed region:
     wall time per step with and without a binary frame after every step (the pack, the
     pinned copy and the file write overlap the next steps), and the latency of one frame
@@ -517,16 +517,17 @@ def frames_bench(solver, n, args, steps=5):
                 solver.step(first + k)
                 if with_frames:
                     solver.save_frame(os.path.join(tmp, f"f{k % 2}.dat"), ascii=False, time=k * 5e-5)
-            solver.wait_frames()
+            t1 = time.perf_counter()
+            solver.wait_frames()   # the last frame's write, after the last step
             lib.call("mps_device_sync")
-            return (time.perf_counter() - t0) * 1e3 / steps
+            return (t1 - t0) * 1e3 / steps, (time.perf_counter() - t1) * 1e3
         run(False)
-        base = run(False)
+        base, _ = run(False)
         first += steps
-        with_f = run(True)
+        with_f, tail = run(True)
         out = {"particles": n, "steps": steps, "wall_ms_per_step": round(base, 3),
                "wall_ms_per_step_binary_frame_each_step": round(with_f, 3),
-               "overhead_ms_per_step": round(with_f - base, 3),
+               "overhead_ms_per_step": round(with_f - base, 3), "last_frame_wait_ms": round(tail, 2),
                "binary_bytes": 4 + 48 * n + 8}
         for ascii in (False, True):
             lib.call("mps_device_sync")
