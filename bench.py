@@ -315,6 +315,7 @@ def run_gpu(args):
     # end to end through the C-ABI from pinned host buffers
     e2e = run_e2e(fast, args)
     frames = frames_bench(fast, n, args)
+    inflow = inflow_bench(scene, n)
     fast.close()
     sort = sort_bench(n, scene.box.cell_num, peak_gbs)
     accuracy = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
@@ -367,6 +368,7 @@ def run_gpu(args):
         "accuracy_vs_fp64": accuracy,
         "e2e": e2e,
         "frames": frames,
+        "inflow": inflow,
         "gpu_launches": int(st_fast[0]["launches_in_region"]),
         "clocks": clk,
     }
@@ -497,6 +499,35 @@ def run_accuracy_only(args):
     print(json.dumps({"accuracy_vs_fp64": acc, "workload": WORKLOADS[args.workload].format(l0=args.l0),
                       "particles": scene.n, "learned": params is not None, "seconds": time.perf_counter() - t0}))
     return 0
+
+
+def inflow_bench(scene, n, bucket=10_000):
+    """Device-side inflow (mps_solver_add_particles, InsertBucket semantics) outside the
+    timed region: a separate solver of the same scene with room for the bucket, warmed
+    up; the time to insert a bucket (hole scan over the IDs, count read-back, upload,
+    insert kernel) and the next step (which sorts the new particles in; the bucket sits
+    outside the compute zone, so that step also removes it again)."""
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.solver import Solver
+    try:
+        s = Solver(scene, precision="fp32_ir", max_particles=n + 2 * bucket)
+        for k in range(3):
+            s.step(k)
+        b = np.full((bucket, 3), 10.0, np.float32) + np.arange(bucket, dtype=np.float32)[:, None] * 1e-3
+        lib.call("mps_device_sync")
+        t0 = time.perf_counter()
+        added = s.add_particles(b)
+        t1 = time.perf_counter()
+        st = s.step(3)
+        lib.call("mps_device_sync")
+        t2 = time.perf_counter()
+        out = {"particles": n, "bucket": bucket, "added": added, "add_ms": round((t1 - t0) * 1e3, 3),
+               "next_step_ms": round((t2 - t1) * 1e3, 3), "next_step_error_flags": int(st["error_flags"]),
+               "particles_after_next_step": int(st["particles"])}
+        s.close()
+        return out
+    except Exception as e:  # pragma: no cover - reported, not fatal for the metric
+        return {"error": str(e)}
 
 
 def frames_bench(solver, n, args, steps=10):

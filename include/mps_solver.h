@@ -155,6 +155,14 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, do
  * operator (inner_weights = 16) with 16-bit / 32-bit columns, the same bits as each
  * other. */
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
+/* Particle inflow (CMultiGPUHandler::AddBucketParticles / InsertBucket,
+ * radix/SPVSOLVER/MultiGPUSolver/MultiGPUHandler.cpp:1156-1210) on the device state:
+ * the bucket's particles (reference CParticle records; ID, Density, Temperature and
+ * SolidPhaseRate are not used) take the IDs below the ID extent that no particle
+ * carries (removed by the compute-zone compaction), in increasing order; the rest are
+ * appended at the extent when all of them fit under max_particles, else dropped, as
+ * the reference does.  *added = particles inserted.  The next step sorts them in. */
+CCTStatusType mps_solver_add_particles(MpsSolver* s, int count, const CParticle* bucket, int* added);
 /* Output frame of the current state in the reference's format (IO::Save,
  * radix/SPVSOLVER/MultiGPUSolver/IO.cpp:649-756; see mps_write_frame in mps_io.h):
  * particles in ID order with position, velocity, pressure, PND as the density,

@@ -1532,6 +1532,38 @@ __global__ void k_pack_state(const __grid_constant__ Dev d, const double* p3, co
     d.vel[i] = make_dbl4(v3[3 * (size_t)i], v3[3 * (size_t)i + 1], v3[3 * (size_t)i + 2], 0.0);
     d.press[i] = pr[i];
 }
+// particle inflow (CMultiGPUHandler::InsertBucket, MultiGPUHandler.cpp:1163-1210): the
+// IDs below the extent that no particle carries are the holes, filled in increasing
+// order; the rest of a bucket goes on at the extent
+__global__ void k_fill_u32(unsigned* a, int n, unsigned v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+__global__ void k_clear_present(const __grid_constant__ Dev d, unsigned* hole, int idext) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int id = d.id[i];
+    if (id >= 0 && id < idext) hole[id] = 0u;
+}
+__global__ void k_hole_list(const unsigned* hole, const unsigned* rank, int idext, int* holes) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id < idext && hole[id]) holes[rank[id]] = id;
+}
+// bucket particle j -> state slot d.n + j with the j-th hole's ID, or the extent + (j - holes)
+__global__ void k_insert(const __grid_constant__ Dev d, const CParticle* __restrict__ b, int added, int nholes,
+                         const int* __restrict__ holes, int idext) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= added) return;
+    const size_t s = (size_t)d.n + (size_t)j;
+    const CParticle q = b[j];
+    d.pos[s] = make_dbl4(q.Position.x, q.Position.y, q.Position.z, 0.0);
+    d.vel[s] = make_dbl4(q.Velocity.x, q.Velocity.y, q.Velocity.z, 0.0);
+    d.press[s] = q.Pressure;
+    d.visc[s] = q.KineticViscosity;
+    d.type[s] = (int)q.Type;
+    d.id[s] = j < nholes ? holes[j] : idext + (j - nholes);
+}
+
 // output frames in particle-ID order: mark the IDs present (the exclusive scan of the
 // marks is each ID's row), then pack position, velocity, pressure, PND, viscosity
 // (FP32) and type at that row: out = [pos 3n | vel 3n | press n | pnd n | visc n]

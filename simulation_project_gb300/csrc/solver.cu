@@ -254,7 +254,10 @@ struct Solver {
             if (f.ht) cudaFreeHost(f.ht);
             if (f.copied) cudaEventDestroy(f.copied);
         }
-        // d_frame, d_ftype and d_fflag come from mk(): freed with `allocs` below
+        // d_frame, d_ftype, d_fflag and the inflow buffers come from mk(): freed with
+        // `allocs` below; the bucket staging does not
+        if (d_bucket) cudaFree(d_bucket);
+        d_bucket = nullptr;
         if (ev_packed) cudaEventDestroy(ev_packed);
         if (st_io) cudaStreamDestroy(st_io);
         cudaDeviceSynchronize();
@@ -307,6 +310,7 @@ struct Solver {
             id[i] = i;
         }
         d.n = n;
+        idext = n;
         cudaError_t e = cudaMemcpyAsync(d.pos, P.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.vel, V.data(), sizeof(dbl4) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.press, pr.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st);
@@ -1009,6 +1013,62 @@ struct Solver {
         return cuda_status(e);
     }
 
+    // ---- particle inflow ----
+    int idext = 0;                 // ID extent: IDs in use lie below it (holes: removed ones)
+    unsigned *d_hole = nullptr, *d_hrank = nullptr;
+    int* d_holes = nullptr;
+    CParticle* d_bucket = nullptr;
+    size_t bucket_cap = 0;
+    // InsertBucket (MultiGPUHandler.cpp:1163-1210) on the device state: bucket particles
+    // take the missing IDs below the extent in increasing order; the rest are appended at
+    // the extent only if all of them fit under max_particles (else they are dropped)
+    CCTStatusType add_particles(int count, const CParticle* bucket, int* added_out) {
+        if (count < 0 || (count > 0 && !bucket)) return CCT_PARAMERR;
+        if (added_out) *added_out = 0;
+        if (count == 0) return CCT_NOERR;
+        cudaError_t e = cudaSuccess;
+        if (!d_hole) {
+            e = e ? e : mk(&d_hole, (size_t)nmax + 1);
+            e = e ? e : mk(&d_hrank, (size_t)nmax + 1);
+            e = e ? e : mk(&d_holes, (size_t)nmax);
+            if (e) return CCT_MEMERR;
+        }
+        if ((size_t)count > bucket_cap) {
+            if (d_bucket) cudaFree(d_bucket);
+            d_bucket = nullptr;
+            if (cudaMalloc(&d_bucket, sizeof(CParticle) * (size_t)count)) {
+                bucket_cap = 0;
+                return CCT_MEMERR;
+            }
+            bucket_cap = (size_t)count;
+        }
+        int nholes = 0;
+        if (idext > 0) {
+            MPS_COUNT_LAUNCH k_fill_u32<<<blocks_for(idext), kBlock, 0, st>>>(d_hole, idext, 1u);
+            if (d.n > 0) MPS_COUNT_LAUNCH k_clear_present<<<blocks_for(d.n), kBlock, 0, st>>>(d, d_hole, idext);
+            cudaMemcpyAsync(d_hrank, d_hole, sizeof(unsigned) * (size_t)idext, cudaMemcpyDeviceToDevice, st);
+            scan_exclusive(d_hrank, idext, d_hrank + idext, st, scan_sums);
+            MPS_COUNT_LAUNCH k_hole_list<<<blocks_for(idext), kBlock, 0, st>>>(d_hole, d_hrank, idext, d_holes);
+            cudaMemcpyAsync(h_int, d_hrank + idext, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
+            nholes = (int)h_int[0];
+        }
+        const int fill = std::min(count, nholes);
+        const int rest = count - fill;
+        const int app = ((long long)idext + rest <= (long long)nmax) ? rest : 0;
+        const int added = fill + app;
+        if (added > 0) {
+            e = cudaMemcpyAsync(d_bucket, bucket, sizeof(CParticle) * (size_t)added, cudaMemcpyHostToDevice, st);
+            if (e) return CCT_CUDAERR;
+            MPS_COUNT_LAUNCH k_insert<<<blocks_for(added), kBlock, 0, st>>>(d, d_bucket, added, nholes, d_holes, idext);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
+            d.n += added;
+            idext += app;
+        }
+        if (added_out) *added_out = added;
+        return cuda_status(cudaGetLastError());
+    }
+
     // ---- output frames: packed on the solver stream, copied to pinned host memory on
     // a stream of their own, written to the file by a host thread (two slots) ----
     struct FrameSlot {
@@ -1290,6 +1350,11 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     e = cudaMemcpyAsync(host_y, d.q32, sizeof(float) * d.n, cudaMemcpyDeviceToHost, S.st);
     if (!e) e = cudaStreamSynchronize(S.st);
     return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_add_particles(MpsSolver* s, int count, const CParticle* bucket, int* added) {
+    if (!s) return CCT_PARAMERR;
+    return s->s.add_particles(count, bucket, added);
 }
 
 CCTStatusType mps_solver_save_frame(MpsSolver* s, const char* path, int ascii, double time, int models,

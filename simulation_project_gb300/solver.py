@@ -66,6 +66,7 @@ _SIGS = {
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
     "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
     "mps_solver_save_frame": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, P, P]),
+    "mps_solver_add_particles": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_int)]),
     "mps_solver_wait_frames": (C.c_int, [P]),
     "mps_solver_copy_pressure": (C.c_int, [P, P]),
     "mps_solver_stream": (C.c_int, [P, C.POINTER(P)]),
@@ -128,7 +129,10 @@ class Solver:
         self.options = o
         self.scene = scene
         h = P()
-        _check(L.mps_solver_create(C.byref(scene.param), C.byref(scene.box), int(max_particles or scene.n),
+        # host buffers of the state are sized for this capacity: inflow can raise the
+        # particle count above the scene's
+        self.capacity = int(max_particles or scene.n)
+        _check(L.mps_solver_create(C.byref(scene.param), C.byref(scene.box), self.capacity,
                                    C.byref(o), C.byref(h)), "mps_solver_create")
         self.h = h
         pos = np.ascontiguousarray(scene.pos, dtype=np.float64)
@@ -155,7 +159,7 @@ class Solver:
 
     def state(self, sort_by_id=True) -> dict:
         L = _lib()
-        nmax = self.scene.n
+        nmax = self.capacity
         n = C.c_int()
         pos = np.zeros((nmax, 3))
         vel = np.zeros((nmax, 3))
@@ -172,7 +176,7 @@ class Solver:
         return out
 
     def debug_ppe(self) -> dict:
-        nmax = self.scene.n
+        nmax = self.capacity
         arr = {k: np.zeros(nmax) for k in ("pnd", "diag", "rhs", "sol", "nbr_idsum")}
         ids = np.zeros(nmax, np.int32)
         cnt = np.zeros(nmax, np.int32)
@@ -204,6 +208,28 @@ class Solver:
         y = np.zeros(n, np.float32)
         _check(_lib().mps_solver_debug_spmv(self.h, int(kernel), _p(xs), _p(y)), "mps_solver_debug_spmv")
         return y
+
+    def add_particles(self, pos, vel=None, press=None, visc=None, ptype=None) -> int:
+        """Inflow of a bucket of particles (InsertBucket semantics: the missing IDs first,
+        the rest appended if it fits); returns how many were inserted."""
+        from .types import CParticle
+        pos = np.asarray(pos, dtype=np.float32).reshape(-1, 3)
+        k = len(pos)
+        vel = np.zeros((k, 3), np.float32) if vel is None else np.asarray(vel, np.float32).reshape(k, 3)
+        press = np.zeros(k, np.float32) if press is None else np.asarray(press, np.float32)
+        visc = np.full(k, 1e-6, np.float32) if visc is None else np.asarray(visc, np.float32)
+        ptype = np.zeros(k, np.int32) if ptype is None else np.asarray(ptype, np.int32)
+        b = (CParticle * max(k, 1))()
+        for j in range(k):
+            r = b[j]
+            r.ID = -1
+            r.Position.x, r.Position.y, r.Position.z = (float(v) for v in pos[j])
+            r.Velocity.x, r.Velocity.y, r.Velocity.z = (float(v) for v in vel[j])
+            r.Pressure, r.KineticViscosity, r.Type = float(press[j]), float(visc[j]), int(ptype[j])
+        added = C.c_int()
+        _check(_lib().mps_solver_add_particles(self.h, k, C.cast(b, C.c_void_p), C.byref(added)),
+               "mps_solver_add_particles")
+        return added.value
 
     def save_frame(self, path, ascii=False, time=0.0, model_pos=None, model_angle=None):
         """Output frame of the current state (reference format, particles in ID order),
@@ -237,7 +263,7 @@ class Solver:
 
     def learned_infer(self) -> np.ndarray:
         n = C.c_int()
-        out = np.zeros((max(self.scene.n, 1), 2), np.float32)
+        out = np.zeros((max(self.capacity, 1), 2), np.float32)
         _check(_lib().mps_learned_infer(self.h, _p(out), C.byref(n)), "mps_learned_infer")
         return out[:n.value]
 
@@ -256,7 +282,7 @@ class Solver:
 
     def learned_samples(self):
         """(features [n,12], targets [n,2]) of the last PPE solve, interior rows only."""
-        nmax = self.scene.n
+        nmax = self.capacity
         f = np.zeros((nmax, 12), np.float32)
         t = np.zeros((nmax, 2), np.float32)
         n = C.c_int()

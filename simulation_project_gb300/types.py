@@ -255,3 +255,11 @@ assert DISTANCE_DTYPE.itemsize == C.sizeof(CDistance)
 assert CELL_DTYPE.itemsize == C.sizeof(CCell)
 
 CParticle_size = 52   # sizeof(CParticle) (DataType.h:220-240)
+
+
+class CParticle(C.Structure):
+    """One particle record of the reference (DataType.h:220-240): the particle-file and
+    bucket format."""
+    _fields_ = [("ID", C.c_int), ("Position", Scalar3), ("Velocity", Scalar3), ("Pressure", C.c_float),
+                ("Density", C.c_float), ("Temperature", C.c_float), ("KineticViscosity", C.c_float),
+                ("SolidPhaseRate", C.c_float), ("Type", C.c_int)]

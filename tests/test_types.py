@@ -39,3 +39,10 @@ def test_grid_box_geometry_follows_setcomputezone():
     assert abs(b.m_CellSize - 0.04) < 1e-9
     assert (b.m_GridSize.x, b.m_GridSize.y, b.m_GridSize.z) == (24, 9, 19)
     assert abs(b.m_BufferedZone.m_MinBound.x + 0.08) < 1e-7
+
+
+def test_cparticle_record_size():
+    import ctypes as C
+    from simulation_project_gb300.types import CParticle, CParticle_size
+    assert C.sizeof(CParticle) == CParticle_size == 52
+    assert CParticle.Position.offset == 4 and CParticle.Type.offset == 48
