@@ -111,6 +111,12 @@ def default_options(precision="fp32_ir", **kw) -> MpsSolverOptions:
     return o
 
 
+# numpy view of the reference's CParticle record (DataType.h:220-240)
+CPARTICLE_DTYPE = np.dtype([("ID", "<i4"), ("Position", "<f4", 3), ("Velocity", "<f4", 3), ("Pressure", "<f4"),
+                            ("Density", "<f4"), ("Temperature", "<f4"), ("KineticViscosity", "<f4"),
+                            ("SolidPhaseRate", "<f4"), ("Type", "<i4")])
+
+
 def _p(a):
     return None if a is None else a.ctypes.data
 
@@ -212,23 +218,20 @@ class Solver:
     def add_particles(self, pos, vel=None, press=None, visc=None, ptype=None) -> int:
         """Inflow of a bucket of particles (InsertBucket semantics: the missing IDs first,
         the rest appended if it fits); returns how many were inserted."""
-        from .types import CParticle
         pos = np.asarray(pos, dtype=np.float32).reshape(-1, 3)
         k = len(pos)
-        vel = np.zeros((k, 3), np.float32) if vel is None else np.asarray(vel, np.float32).reshape(k, 3)
-        press = np.zeros(k, np.float32) if press is None else np.asarray(press, np.float32)
-        visc = np.full(k, 1e-6, np.float32) if visc is None else np.asarray(visc, np.float32)
-        ptype = np.zeros(k, np.int32) if ptype is None else np.asarray(ptype, np.int32)
-        b = (CParticle * max(k, 1))()
-        for j in range(k):
-            r = b[j]
-            r.ID = -1
-            r.Position.x, r.Position.y, r.Position.z = (float(v) for v in pos[j])
-            r.Velocity.x, r.Velocity.y, r.Velocity.z = (float(v) for v in vel[j])
-            r.Pressure, r.KineticViscosity, r.Type = float(press[j]), float(visc[j]), int(ptype[j])
+        b = np.zeros(max(k, 1), CPARTICLE_DTYPE)   # CParticle records (52 bytes)
+        b["ID"][:k] = -1
+        b["Position"][:k] = pos
+        if vel is not None:
+            b["Velocity"][:k] = np.asarray(vel, np.float32).reshape(k, 3)
+        if press is not None:
+            b["Pressure"][:k] = press
+        b["KineticViscosity"][:k] = 1e-6 if visc is None else np.asarray(visc, np.float32)
+        if ptype is not None:
+            b["Type"][:k] = ptype
         added = C.c_int()
-        _check(_lib().mps_solver_add_particles(self.h, k, C.cast(b, C.c_void_p), C.byref(added)),
-               "mps_solver_add_particles")
+        _check(_lib().mps_solver_add_particles(self.h, k, b.ctypes.data, C.byref(added)), "mps_solver_add_particles")
         return added.value
 
     def save_frame(self, path, ascii=False, time=0.0, model_pos=None, model_angle=None):

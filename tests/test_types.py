@@ -44,5 +44,8 @@ def test_grid_box_geometry_follows_setcomputezone():
 def test_cparticle_record_size():
     import ctypes as C
     from simulation_project_gb300.types import CParticle, CParticle_size
-    assert C.sizeof(CParticle) == CParticle_size == 52
+    from simulation_project_gb300.solver import CPARTICLE_DTYPE
+    assert C.sizeof(CParticle) == CParticle_size == 52 == CPARTICLE_DTYPE.itemsize
     assert CParticle.Position.offset == 4 and CParticle.Type.offset == 48
+    for name, _ in CParticle._fields_:
+        assert CPARTICLE_DTYPE.fields[name][1] == getattr(CParticle, name).offset
