@@ -21,6 +21,9 @@
  *   mps_grid_box             CCellSet::SetComputeZone, CGPUCellSet.cpp:109-152.
  *   mps_lattice_constants    n0 and lambda of the cubic lattice for a radius (FP64);
  *                            no reference counterpart (it reads n0 from the file).
+ *   mps_read_dt_file         DtFrame::Load, DtFrame.cpp:11-35: the dt schedule.
+ *   mps_dt_schedule_next     CMultiGPUHandler::CheckAndUpdateDt, MultiGPUHandler.cpp:
+ *                            1256-1275: applies the next due schedule row to a CParameter.
  *   mps_write_frame          IO::Save / SaveAscii / SaveBinary, IO.cpp:649-756: an output
  *                            frame.  ASCII: count; "x y z vx vy vz P n T nu solidRate
  *                            type" per particle (%g, 6 significant digits, as the
@@ -47,6 +50,28 @@ CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset
 float mps_lambda_table(float l0);
 CCTStatusType mps_grid_box(const CBox* compute_zone, const CParameter* param, CGridBox* out);
 CCTStatusType mps_lattice_constants(double re_coefficient, double l0, int dimension, double* n0, double* lambda);
+/* One row of the dt schedule file (DtFrame::Load, radix/SPVSOLVER/MultiGPUSolver/
+ * DtFrame.cpp:11-35; DeltaTime, DataType.h:565-571): from `step` on, Dt, CourantNumber,
+ * ParticleGenerationStep (inflow_step) and OutputStep take these values. */
+typedef struct MpsDtRow {
+    Integer step;
+    Scalar dt;
+    Scalar courant;
+    Scalar inflow_step;
+    Scalar output_step;
+} MpsDtRow;
+/* Reads the rows "Step Dt CourantNumber InflowStep OutputStep" with the reference's
+ * stream semantics: reading stops at the first field that does not parse or at the end
+ * of the file, and a row counts only if the stream is still good after its fifth field
+ * (a last row not followed by whitespace is dropped, as DtFrame::Load drops it).
+ * rows = NULL counts. */
+CCTStatusType mps_read_dt_file(const char* path, int* count, MpsDtRow* rows, int capacity);
+/* CMultiGPUHandler::CheckAndUpdateDt (MultiGPUHandler.cpp:1256-1275): if row *next is
+ * due (current_step >= its step), copies it into param (Dt, CourantNumber,
+ * ParticleGenerationStep, OutputStep as an integer) and advances *next; one row per
+ * call.  *applied = 1 when a row was applied. */
+CCTStatusType mps_dt_schedule_next(const MpsDtRow* rows, int count, int* next, int current_step, CParameter* param,
+                                   int* applied);
 CCTStatusType mps_write_frame(const char* path, int ascii, int n, const Scalar3* pos, const Scalar3* vel,
                               const Scalar* pressure, const Scalar* density, const Scalar* temperature,
                               const Scalar* viscosity, const Scalar* solid_rate, const ParticleType* type,

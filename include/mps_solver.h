@@ -155,6 +155,11 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, do
  * operator (inner_weights = 16) with 16-bit / 32-bit columns, the same bits as each
  * other. */
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
+/* Time step from the next step on (a dt schedule row, mps_dt_schedule_next in
+ * mps_io.h): Dt, and CourantNumber when courant > 0; the constants that depend on them
+ * are recomputed as at creation, so the solver continues exactly as one created with
+ * these values. */
+CCTStatusType mps_solver_set_time_step(MpsSolver* s, double dt, double courant);
 /* Particle inflow (CMultiGPUHandler::AddBucketParticles / InsertBucket,
  * radix/SPVSOLVER/MultiGPUSolver/MultiGPUHandler.cpp:1156-1210) on the device state:
  * the bucket's particles (reference CParticle records; ID, Density, Temperature and

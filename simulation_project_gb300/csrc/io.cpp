@@ -479,3 +479,48 @@ extern "C" CCTStatusType mps_write_frame(const char* path, int ascii, int n, con
     const int c = std::fclose(f);
     return (ok && c == 0) ? CCT_NOERR : CCT_FILEERR;
 }
+
+// ---------------------------------------------------------------------------
+// dt schedule: DtFrame::Load (DtFrame.cpp:11-35) and CheckAndUpdateDt
+// (MultiGPUHandler.cpp:1256-1275)
+// ---------------------------------------------------------------------------
+extern "C" CCTStatusType mps_read_dt_file(const char* path, int* count, MpsDtRow* rows, int capacity) {
+    if (!path || !count) return CCT_PARAMERR;
+    std::ifstream f(path);
+    if (!f.is_open()) return CCT_FILEERR;
+    int k = 0;
+    while (f.is_open() && f.good()) {
+        Integer step = 0;
+        Scalar dt = 0, cr = 0, inflow = 0, out = 0;
+        f >> step;
+        f >> dt;
+        f >> cr;
+        f >> inflow;
+        f >> out;
+        if (f.good()) {
+            if (rows) {
+                if (k >= capacity) return CCT_PARAMERR;
+                rows[k] = MpsDtRow{step, dt, cr, inflow, out};
+            }
+            ++k;
+        }
+    }
+    *count = k;
+    return CCT_NOERR;
+}
+
+extern "C" CCTStatusType mps_dt_schedule_next(const MpsDtRow* rows, int count, int* next, int current_step,
+                                              CParameter* param, int* applied) {
+    if (!next || !param || (count > 0 && !rows)) return CCT_PARAMERR;
+    if (applied) *applied = 0;
+    const int k = *next;
+    if (k >= 0 && k < count && current_step >= rows[k].step) {
+        param->Dt = rows[k].dt;
+        param->CourantNumber = rows[k].courant;
+        param->ParticleGenerationStep = rows[k].inflow_step;
+        param->OutputStep = static_cast<Integer>(rows[k].output_step);
+        *next = k + 1;
+        if (applied) *applied = 1;
+    }
+    return CCT_NOERR;
+}

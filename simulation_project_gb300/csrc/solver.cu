@@ -1013,6 +1013,20 @@ struct Solver {
         return cuda_status(e);
     }
 
+    // ---- time step (the dt schedule, CheckAndUpdateDt) ----
+    // the constants that depend on dt, computed from the float Dt as at creation
+    CCTStatusType set_time_step(double dt, double courant) {
+        if (!(dt > 0.0) || !std::isfinite(dt)) return CCT_PARAMERR;
+        param.Dt = (Scalar)dt;
+        if (courant > 0.0) param.CourantNumber = (Scalar)courant;
+        Consts& c = d.c;
+        c.dt = param.Dt;
+        c.kappa = opt.compressibility * c.rho / (c.dt * c.dt);
+        c.c2 = c.rho / (c.dt * c.dt);
+        c.vmax = c.l0 * (double)param.CourantNumber / c.dt;
+        return CCT_NOERR;
+    }
+
     // ---- particle inflow ----
     int idext = 0;                 // ID extent: IDs in use lie below it (holes: removed ones)
     unsigned *d_hole = nullptr, *d_hrank = nullptr;
@@ -1350,6 +1364,11 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     e = cudaMemcpyAsync(host_y, d.q32, sizeof(float) * d.n, cudaMemcpyDeviceToHost, S.st);
     if (!e) e = cudaStreamSynchronize(S.st);
     return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_set_time_step(MpsSolver* s, double dt, double courant) {
+    if (!s) return CCT_PARAMERR;
+    return s->s.set_time_step(dt, courant);
 }
 
 CCTStatusType mps_solver_add_particles(MpsSolver* s, int count, const CParticle* bucket, int* added) {

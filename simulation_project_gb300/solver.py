@@ -67,6 +67,7 @@ _SIGS = {
     "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
     "mps_solver_save_frame": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, P, P]),
     "mps_solver_add_particles": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_int)]),
+    "mps_solver_set_time_step": (C.c_int, [P, C.c_double, C.c_double]),
     "mps_solver_wait_frames": (C.c_int, [P]),
     "mps_solver_copy_pressure": (C.c_int, [P, P]),
     "mps_solver_stream": (C.c_int, [P, C.POINTER(P)]),
@@ -214,6 +215,10 @@ class Solver:
         y = np.zeros(n, np.float32)
         _check(_lib().mps_solver_debug_spmv(self.h, int(kernel), _p(xs), _p(y)), "mps_solver_debug_spmv")
         return y
+
+    def set_time_step(self, dt, courant=0.0):
+        """Dt (and CourantNumber when > 0) from the next step on (a dt schedule row)."""
+        _check(_lib().mps_solver_set_time_step(self.h, float(dt), float(courant)), "mps_solver_set_time_step")
 
     def add_particles(self, pos, vel=None, press=None, visc=None, ptype=None) -> int:
         """Inflow of a bucket of particles (InsertBucket semantics: the missing IDs first,
