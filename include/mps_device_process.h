@@ -27,8 +27,11 @@
  *     does on the host (CGPUCellSet.cpp:1160-1202), in the same order; ParticleNum is a
  *     HOST pointer (in: count, out: remaining count) and the call synchronises Stream.
  *     It works on the output-order arrays bound by InitializeDeviceConstOutPutParticles.
- *   - CalcTemperatureFactor / CalcTurbulenceViscosity are not implemented: they
- *     return CCT_PARAMERR when the parameter enables them and CCT_NOERR otherwise.
+ *   - CalcTemperatureFactor (DeviceProcess_Kernel.h:705-852) and CalcTurbulenceViscosity
+ *     (:1273-1476) run whatever the parameter's switches say, as the reference's
+ *     launchers do; the caller calls them only when bUpdateTemperature / bTurbulance
+ *     is on.  CalcTurbulenceViscosity and a turbulent CalcExplicitly need the last two
+ *     arrays of InitializeDeviceConstInputParticles (CCT_PARAMERR when they are null).
  *   - CalcExplicitPressureGradient returns CCT_PARAMERR when bNegativePressure is on.
  */
 #ifndef MPS_DEVICE_PROCESS_H

@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -631,10 +632,12 @@ int orc_calc_drag_effect(OrcBindings* b, int n) {
 }
 
 /* CalcExplicitly_Kernel, DeviceProcess_Kernel.h:390-582 (viscosity + gravity
- * predictor; artificial-pressure and collision terms when bExplicitPressure). */
+ * predictor; artificial-pressure and collision terms when bExplicitPressure; with
+ * bTurbulance the laminar plus turbulent viscosity scales the Laplacian (:545-552) and
+ * the gradient of the strain product is accumulated (:477-485) but multiplied by the
+ * integer quotient 2/3 = 0 before it reaches the velocity (:558-562)). */
 int orc_calc_explicitly(OrcBindings* b, int n) {
     const CParameter& P = b->param;
-    if (P.bTurbulance) return CCT_PARAMERR;
     for (int id = 0; id < n; ++id) {
         const int orig = b->id[id];
         const float rho = P.Density;
@@ -648,8 +651,10 @@ int orc_calc_explicitly(OrcBindings* b, int n) {
         const int cid = cell_q(b->box, tp, cx, cy, cz);
         S3 lap = mk(0, 0, 0), art = mk(0, 0, 0), col = mk(0, 0, 0);
         S3 v0 = b->vel[id];
+        S3 tke = mk(0, 0, 0);
         const float re = P.LaplacianInfluenceRadiusCoefficient * P.InitialParticleDistance;
         const float rc = P.r_coeff * P.InitialParticleDistance;
+        const float reg = P.GradientInfluenceRadiusCoefficient * P.InitialParticleDistance;
         if (cid >= 0 && cid < b->cell_num) {
             const float mind = (float)(re * 1e-3);
             for (int k = -1; k <= 1; ++k)
@@ -671,6 +676,11 @@ int orc_calc_explicitly(OrcBindings* b, int n) {
                             lap.x += (v1.x - v0.x) * w;
                             lap.y += (v1.y - v0.y) * w;
                             lap.z += (v1.z - v0.z) * w;
+                            if (P.bTurbulance && d < reg) {
+                                const float w1 = weight_q(reg, d);
+                                const float sc = (b->strain[x] - b->strain[id]) * w1 / (d * d);
+                                tke = add(tke, mul(sub(b->pos[x], tp), sc));
+                            }
                             if (P.bExplicitPressure && d < rc) {
                                 const float a = P.ArtificialPressure * w / (d * d);
                                 art = add(art, mul(sub(b->pos[x], tp), a));
@@ -695,9 +705,14 @@ int orc_calc_explicitly(OrcBindings* b, int n) {
         S3 dragv = mk(0, 0, 0);
         S3 acc = add(mk(0, 0, 0), P.GravityConstant);
         if (b->drag_num > 0) dragv = b->drag_acc[id];
-        lap = mul(lap, b->kin_visc[id]);
+        if (P.bTurbulance) lap = mul(lap, b->kin_visc[id] + b->turb_visc[id]);
+        else lap = mul(lap, b->kin_visc[id]);
         acc = add(acc, lap);
         v0 = sub(add(v0, mul(acc, P.Dt)), dragv);
+        if (P.bTurbulance) {
+            tke = mul(tke, (float)(2 / 3));
+            v0 = sub(v0, mul(tke, P.Dt));
+        }
         if (P.bExplicitPressure) {
             const float c = (float)(-P.Dimension) / (P.ConstantParticleDensity * rho);
             acc = add(mul(art, c), mul(col, (float)0.01));
@@ -709,6 +724,159 @@ int orc_calc_explicitly(OrcBindings* b, int n) {
             b->out_pos[orig].z = tp.z + P.Dt * v0.z;
             b->out_vel[orig] = v0;
         }
+    }
+    return CCT_NOERR;
+}
+
+/* CalcTemperatureFactor_Kernel, DeviceProcess_Kernel.h:705-852: heat conduction
+ * over the neighbours within the temperature radius (distance <= re, clamped below at
+ * 1e-3 re; conductance 1 / (1/k + R/r) over r^2), the nearest wall through its
+ * gradient Z function with the harmonic mean of the fluid and wall conductivities, the
+ * drag heating; both sums enter only when larger than FLT_EPSILON in magnitude; the
+ * result clamped to [MinWallTemperature, MaxWallTemperature] and the viscosity updated
+ * linearly in it (output arrays at the original index). */
+int orc_calc_temperature_factor(OrcBindings* b, int n) {
+    const CParameter& P = b->param;
+    for (int id = 0; id < n; ++id) {
+        const float rho = P.Density;
+        const float ecoef = P.Dt * 2 * P.Dimension / (P.ConstantParticleDensity * rho * P.FruidSpecificHeat);
+        float hf = 0.0f, hw = 0.0f;
+        const float ret = P.TemperatureInfluenceRadiusCoefficient * P.InitialParticleDistance;
+        float num = 0, den = 0;
+        const S3 tp = b->pos[id];
+        float tt = b->temperature[id];
+        const int orig = b->id[id];
+        if (!include_q(b->box, tp, P.Tolerance)) {
+            b->out_id[orig] = -1;
+            continue;
+        }
+        int cx, cy, cz;
+        const int cid = cell_q(b->box, tp, cx, cy, cz);
+        if (cid < 0 || cid >= b->cell_num) continue;
+        const float mind = (float)(ret * 1e-3);
+        for (int k = -1; k <= 1; ++k)
+            for (int j = -1; j <= 1; ++j)
+                for (int i = -1; i <= 1; ++i) {
+                    const int m = key_of(b->box, cx + i, cy + j, cz + k);
+                    if (m < 0 || m >= b->cell_num) continue;
+                    const int s = b->cell_start[m];
+                    if ((unsigned)s == 0xffffffffu) continue;
+                    const int e = b->cell_end[m];
+                    for (int x = s; x < e; ++x) {
+                        if (b->out_id[x] < 0) continue;
+                        if (x == id) continue;
+                        float d = dist_q(tp, b->pos[x]);
+                        if (!(d <= ret)) continue;
+                        if (d < mind) d = mind;
+                        num = (b->temperature[x] - tt) * weight_q(ret, d);
+                        den = d * d * (1 / P.FruidThermalConductivity + P.FruidThermalResistance / d);
+                        hf += num / den;
+                    }
+                }
+        const float wd = b->stl_distance[id].Magnitude;
+        const int tri = b->stl_id[id];
+        if (tri >= 0 && tri < b->triangle_num && wd > 0 && wd < ret) {
+            const CTriangleParameters& tq = b->tri_params[b->triangles[tri].ModelIDNumber];
+            const float res = tq.WallThermalResistivity;
+            const float cond = (2 * P.FruidThermalConductivity * tq.WallThermalConductivity) /
+                               (P.FruidThermalConductivity + tq.WallThermalConductivity);
+            const float ww = (2 == P.Dimension) ? zeval_q(kZGrad2, wd, P.InitialParticleDistance)
+                                                : zeval_q(kZGrad3, wd, P.InitialParticleDistance);
+            num = (tq.Temperature - tt) * ww;
+            den = wd * wd * (1 / cond + res / wd);
+            hw = num / den;
+        }
+        if (b->drag_num > 0) tt += b->drag_temperature[id];
+        float comb = 0.0f;
+        if (std::fabs(hf) > FLT_EPSILON) comb += hf;
+        if (std::fabs(hw) > FLT_EPSILON) comb += hw;
+        tt += (ecoef * (comb));
+        if (tt > P.MaxWallTemperature) tt = P.MaxWallTemperature;
+        if (tt < P.MinWallTemperature) tt = P.MinWallTemperature;
+        b->out_temperature[orig] = tt;
+        b->out_kin_visc[orig] = P.ViscosityUpdateParameterA * tt + P.ViscosityUpdateParameterB;
+    }
+    return CCT_NOERR;
+}
+
+/* CalcTurbulenceViscosity_Kernel, DeviceProcess_Kernel.h:1273-1476: the velocity
+ * gradient tensor over the neighbours within the gradient radius (scaled by d / n0),
+ * the strain-rate product S = A^2 + B^2 + C^2 + 2 (D^2 + E^2 + F^2) of its diagonal and
+ * symmetrised off-diagonal parts, a Smagorinsky viscosity with the wall damping
+ * 1 - exp(-r_w / re) capped at TurbulanViscosityRatio, and the turbulent kinetic
+ * energy S 2 Cnue l0^2 / Cepsilon capped at TurbulanceIntensity (sorted-order arrays).
+ * The kernel's vorticity and neighbour PND are never read (its vorticity uses a
+ * distance vector that stays zero) and are left out. */
+int orc_calc_turbulence_viscosity(OrcBindings* b, int n) {
+    const CParameter& P = b->param;
+    for (int id = 0; id < n; ++id) {
+        const int orig = b->id[id];
+        const S3 tp = b->pos[id];
+        const S3 v0 = b->vel[id];
+        if (!include_q(b->box, tp, P.Tolerance)) {
+            b->turb_visc[id] = 0.0f;
+            b->out_id[orig] = -1;
+            continue;
+        }
+        S3 X = mk(0, 0, 0), Y = mk(0, 0, 0), Z = mk(0, 0, 0), D = mk(0, 0, 0);
+        float strain = 0.0f, coef = 0.0f;
+        int cx, cy, cz;
+        const int cid = cell_q(b->box, tp, cx, cy, cz);
+        if (cid < 0 || cid >= b->cell_num) {
+            b->pressure[id] = 0.0f;
+            continue;
+        }
+        const float re = P.GradientInfluenceRadiusCoefficient * P.InitialParticleDistance;
+        const float mind = (float)(re * 1e-3);
+        for (int k = -1; k <= 1; ++k)
+            for (int j = -1; j <= 1; ++j)
+                for (int i = -1; i <= 1; ++i) {
+                    const int m = key_of(b->box, cx + i, cy + j, cz + k);
+                    if (m < 0 || m >= b->cell_num) continue;
+                    const int s = b->cell_start[m];
+                    if ((unsigned)s == 0xffffffffu) continue;
+                    const int e = b->cell_end[m];
+                    for (int x = s; x < e; ++x) {
+                        if (b->out_id[x] < 0) continue;
+                        if (x == id) continue;
+                        float d = dist_q(tp, b->pos[x]);
+                        if (!(d < re)) continue;
+                        if (d < mind) d = mind;
+                        const float w = weight_q(re, d);
+                        const S3 v1 = b->vel[x];
+                        const S3 q = b->pos[x];
+                        X.x += ((v1.x - v0.x) * (q.x - tp.x) * w) / (d * d);
+                        X.y += ((v1.x - v0.x) * (q.y - tp.y) * w) / (d * d);
+                        X.z += ((v1.x - v0.x) * (q.z - tp.z) * w) / (d * d);
+                        Y.x += ((v1.y - v0.y) * (q.x - tp.x) * w) / (d * d);
+                        Y.y += ((v1.y - v0.y) * (q.y - tp.y) * w) / (d * d);
+                        Y.z += ((v1.y - v0.y) * (q.z - tp.z) * w) / (d * d);
+                        Z.x += ((v1.z - v0.z) * (q.x - tp.x) * w) / (d * d);
+                        Z.y += ((v1.z - v0.z) * (q.y - tp.y) * w) / (d * d);
+                        Z.z += ((v1.z - v0.z) * (q.z - tp.z) * w) / (d * d);
+                    }
+                }
+        const float g = P.Dimension / P.ConstantParticleDensity;
+        X.x = g * X.x; X.y = g * X.y; X.z = g * X.z;
+        Y.x = g * Y.x; Y.y = g * Y.y; Y.z = g * Y.z;
+        Z.x = g * Z.x; Z.y = g * Z.y; Z.z = g * Z.z;
+        D.x = (float)(0.5 * (X.y + Y.x));
+        D.y = (float)(0.5 * (X.z + Z.x));
+        D.z = (float)(0.5 * (Y.z + Z.y));
+        strain = X.x * X.x + Y.y * Y.y + Z.z * Z.z + 2 * D.x * D.x + 2 * D.y * D.y + 2 * D.z * D.z;
+        const float riw = b->stl_distance[id].Magnitude;
+        const float ratio = -(riw / re);
+        const float damp = 1 - std::exp(ratio);
+        const float smag = P.SmagorinskyConstant * damp;
+        coef = (smag * P.FilterWidth) * (smag * P.FilterWidth);
+        float tv = 0;
+        if (strain > 0) tv = coef * std::sqrt(2 * strain);
+        if (tv > P.TurbulanViscosityRatio) tv = P.TurbulanViscosityRatio;
+        b->turb_visc[id] = tv;
+        const float tkc = 2 * P.Cnue * P.InitialParticleDistance * P.InitialParticleDistance / P.Cepsilon;
+        float tke = strain * tkc;
+        if (tke > P.TurbulanceIntensity) tke = P.TurbulanceIntensity;
+        b->strain[id] = tke;
     }
     return CCT_NOERR;
 }

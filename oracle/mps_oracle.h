@@ -67,6 +67,9 @@ typedef struct OrcBindings {
     Scalar3* drag_acc;
     float* drag_temperature;
     int* magnifier_count;
+    /* turbulence (c_daParticleTurbulaceViscosity, c_daParticleStrainTensorProduct) */
+    float* turb_visc;
+    float* strain;
 } OrcBindings;
 
 /* ---- math helpers (reference float arithmetic) ---- */
@@ -100,6 +103,8 @@ int orc_calc_drag_effect(OrcBindings* b, int n);
 
 /* ---- particle operators (explicit schedule) ---- */
 int orc_calc_explicitly(OrcBindings* b, int n);
+int orc_calc_temperature_factor(OrcBindings* b, int n);
+int orc_calc_turbulence_viscosity(OrcBindings* b, int n);
 int orc_calc_explicit_pressure(OrcBindings* b, int n);
 int orc_calc_explicit_pressure_gradient(OrcBindings* b, int n);
 

@@ -53,6 +53,10 @@ static inline void __syncthreads() {}
 using std::isfinite;
 using std::max;
 using std::min;
+/* device code's abs(float) and sqrt(float) are the float overloads: the same here
+ * (the C library's ::abs(int) and ::sqrt(double) would convert) */
+using std::abs;
+using std::sqrt;
 
 #include "DataType.h"
 #include "DeviceProcess_Kernel.h"
@@ -96,6 +100,8 @@ struct HarnessBindings {
     Scalar3* drag_acc;
     Scalar* drag_temperature;
     Integer* magnifier_count;
+    Scalar* turb_visc;
+    Scalar* strain;
 };
 
 /* Equivalent of InitializeDeviceMemConst / InitializeDeviceConst{Input,OutPut}
@@ -137,6 +143,8 @@ static void bind(const HarnessBindings* b) {
     c_daDragAcc = b->drag_acc;
     c_daDragTemperature = b->drag_temperature;
     c_daMagnifierCount = b->magnifier_count;
+    c_daParticleTurbulaceViscosity = b->turb_visc;
+    c_daParticleStrainTensorProduct = b->strain;
 }
 
 /* Run a one-thread-per-item kernel: block size 1, block index = item.  Items are
@@ -247,6 +255,18 @@ int orc_calc_drag_effect(HarnessBindings* b, int n) {
 int orc_calc_explicitly(HarnessBindings* b, int n) {
     bind(b);
     run_items(n, [&] { CalcExplicitly_Kernel(n); });
+    return CCT_NOERR;
+}
+
+int orc_calc_temperature_factor(HarnessBindings* b, int n) {
+    bind(b);
+    run_items(n, [&] { CalcTemperatureFactor_Kernel(n); });
+    return CCT_NOERR;
+}
+
+int orc_calc_turbulence_viscosity(HarnessBindings* b, int n) {
+    bind(b);
+    run_items(n, [&] { CalcTurbulenceViscosity_Kernel(n); });
     return CCT_NOERR;
 }
 

@@ -16,6 +16,7 @@
 // bounds skip keys outside [0, cells) instead of writing out of bounds, and a cell's
 // triangle list is filled in ascending triangle id (the reference's atomics give an
 // arbitrary order).
+#include <cfloat>
 #include <stdio.h>
 
 #include "mps_common.cuh"
@@ -63,6 +64,8 @@ struct RefBind {
     float* drag_temperature;
     int* magnifier_count;
     CDragTriangle* drag_triangles;
+    float* turb_visc;   // c_daParticleTurbulaceViscosity (sorted order)
+    float* strain;      // c_daParticleStrainTensorProduct (sorted order)
 };
 
 static RefBind g_bind;
@@ -466,7 +469,8 @@ __global__ void k_ref_drag(int n, const __grid_constant__ RefBind b) {
 // 27-cell traversal in the reference order: k outer, j, i inner; particles of a
 // cell in sorted order; neighbours whose out_id (indexed by sorted position, as in
 // the reference) is negative are skipped.
-template <class F>
+// LE: neighbours at distance <= re (the temperature operator), else < re
+template <bool LE = false, class F>
 __device__ __forceinline__ void ref_neighbours(const RefBind& b, int id, const Scalar3& tp, int cx, int cy, int cz,
                                                float re, F&& f) {
     const float mind = (float)(re * 1e-3);
@@ -483,7 +487,7 @@ __device__ __forceinline__ void ref_neighbours(const RefBind& b, int id, const S
                     if (x == id) continue;
                     const Scalar3 q = b.pos[x];
                     float d = ref_dist(tp, q);
-                    if (!(d < re)) continue;
+                    if (!(LE ? d <= re : d < re)) continue;
                     if (d < mind) d = mind;
                     f(x, d, q);
                 }
@@ -506,9 +510,12 @@ __global__ void k_ref_explicitly(int n, const __grid_constant__ RefBind b) {
     const int cid = ref_cell(b.box, tp, cx, cy, cz);
     Scalar3 lap = s3(0, 0, 0), art = s3(0, 0, 0), col = s3(0, 0, 0);
     Scalar3 v0 = b.vel[id];
+    Scalar3 tke = s3(0, 0, 0);
     const float re = P.LaplacianInfluenceRadiusCoefficient * P.InitialParticleDistance;
     const float rc = P.r_coeff * P.InitialParticleDistance;
+    const float reg = P.GradientInfluenceRadiusCoefficient * P.InitialParticleDistance;
     const bool ep = P.bExplicitPressure;
+    const bool turb = P.bTurbulance;
     if (cid >= 0 && cid < b.cell_num) {
         ref_neighbours(b, id, tp, cx, cy, cz, re, [&](int x, float d, const Scalar3& q) {
             const float w = weight(re, d);
@@ -516,6 +523,12 @@ __global__ void k_ref_explicitly(int n, const __grid_constant__ RefBind b) {
             lap.x += (v1.x - v0.x) * w;
             lap.y += (v1.y - v0.y) * w;
             lap.z += (v1.z - v0.z) * w;
+            // turbulent kinetic energy gradient (:477-485)
+            if (turb && d < reg) {
+                const float w1 = weight(reg, d);
+                const float sc = (b.strain[x] - b.strain[id]) * w1 / (d * d);
+                tke = s3add(tke, s3mul(s3sub(q, tp), sc));
+            }
             if (ep && d < rc) {
                 const float a = P.ArtificialPressure * w / (d * d);
                 art = s3add(art, s3mul(s3sub(q, tp), a));
@@ -538,9 +551,15 @@ __global__ void k_ref_explicitly(int n, const __grid_constant__ RefBind b) {
     Scalar3 dragv = s3(0, 0, 0);
     Scalar3 acc = s3add(s3(0, 0, 0), P.GravityConstant);
     if (b.drag_num > 0) dragv = b.drag_acc[id];
-    lap = s3mul(lap, b.kin_visc[id]);
+    // laminar + turbulent viscosity (:545-552)
+    lap = s3mul(lap, turb ? b.kin_visc[id] + b.turb_visc[id] : b.kin_visc[id]);
     acc = s3add(acc, lap);
     v0 = s3sub(s3add(v0, s3mul(acc, P.Dt)), dragv);
+    if (turb) {
+        // (2/3) is the integer quotient 0 in the reference (:560): the term vanishes
+        tke = s3mul(tke, (float)(2 / 3));
+        v0 = s3sub(v0, s3mul(tke, P.Dt));
+    }
     if (ep) {
         const float c = (float)(-P.Dimension) / (P.ConstantParticleDensity * P.Density);
         acc = s3add(s3mul(art, c), s3mul(col, (float)0.01));
@@ -550,6 +569,116 @@ __global__ void k_ref_explicitly(int n, const __grid_constant__ RefBind b) {
         b.out_pos[orig] = s3(tp.x + P.Dt * v0.x, tp.y + P.Dt * v0.y, tp.z + P.Dt * v0.z);
         b.out_vel[orig] = v0;
     }
+}
+
+// CalcTemperatureFactor_Kernel (DeviceProcess_Kernel.h:705-852): conduction over the
+// neighbours within the temperature radius (distance <= re), the nearest wall through
+// its gradient Z function, the drag heating; each sum counted only above FLT_EPSILON
+// in magnitude; clamped; viscosity linear in the temperature (original index)
+__global__ void k_ref_temperature(int n, const __grid_constant__ RefBind b) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const CParameter& P = b.param;
+    const float rho = P.Density;
+    const float ecoef = P.Dt * 2 * P.Dimension / (P.ConstantParticleDensity * rho * P.FruidSpecificHeat);
+    float hf = 0.0f, hw = 0.0f;
+    const float ret = P.TemperatureInfluenceRadiusCoefficient * P.InitialParticleDistance;
+    const Scalar3 tp = b.pos[id];
+    float tt = b.temperature[id];
+    const int orig = b.id[id];
+    if (!in_zone<float>(b.box, tp.x, tp.y, tp.z, P.Tolerance)) {
+        b.out_id[orig] = -1;
+        return;
+    }
+    int cx, cy, cz;
+    const int cid = ref_cell(b.box, tp, cx, cy, cz);
+    if (cid < 0 || cid >= b.cell_num) return;
+    ref_neighbours<true>(b, id, tp, cx, cy, cz, ret, [&](int x, float d, const Scalar3&) {
+        const float num = (b.temperature[x] - tt) * weight(ret, d);
+        const float den = d * d * (1 / P.FruidThermalConductivity + P.FruidThermalResistance / d);
+        hf += num / den;
+    });
+    const float wd = b.stl_distance[id].Magnitude;
+    const int tri = b.stl_id[id];
+    if (tri >= 0 && tri < b.triangle_num && wd > 0 && wd < ret) {
+        const CTriangleParameters& tq = b.tri_params[b.triangles[tri].ModelIDNumber];
+        const float res = tq.WallThermalResistivity;
+        const float cond = (2 * P.FruidThermalConductivity * tq.WallThermalConductivity) /
+                           (P.FruidThermalConductivity + tq.WallThermalConductivity);
+        const float ww = ref_zgrad(P.Dimension, wd, P.InitialParticleDistance);
+        const float num = (tq.Temperature - tt) * ww;
+        const float den = wd * wd * (1 / cond + res / wd);
+        hw = num / den;
+    }
+    if (b.drag_num > 0) tt += b.drag_temperature[id];
+    float comb = 0.0f;
+    if (fabsf(hf) > FLT_EPSILON) comb += hf;
+    if (fabsf(hw) > FLT_EPSILON) comb += hw;
+    tt += (ecoef * (comb));
+    if (tt > P.MaxWallTemperature) tt = P.MaxWallTemperature;
+    if (tt < P.MinWallTemperature) tt = P.MinWallTemperature;
+    b.out_temperature[orig] = tt;
+    b.out_kin_visc[orig] = P.ViscosityUpdateParameterA * tt + P.ViscosityUpdateParameterB;
+}
+
+// CalcTurbulenceViscosity_Kernel (DeviceProcess_Kernel.h:1273-1476): velocity gradient
+// tensor within the gradient radius, strain-rate product, wall-damped Smagorinsky
+// viscosity (capped) and turbulent kinetic energy (capped), sorted order.  The
+// kernel's vorticity and PND are never read and are left out.
+__global__ void k_ref_turbulence(int n, const __grid_constant__ RefBind b) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    const CParameter& P = b.param;
+    const int orig = b.id[id];
+    const Scalar3 tp = b.pos[id];
+    const Scalar3 v0 = b.vel[id];
+    if (!in_zone<float>(b.box, tp.x, tp.y, tp.z, P.Tolerance)) {
+        b.turb_visc[id] = 0.0f;
+        b.out_id[orig] = -1;
+        return;
+    }
+    Scalar3 X = s3(0, 0, 0), Y = s3(0, 0, 0), Z = s3(0, 0, 0), D = s3(0, 0, 0);
+    int cx, cy, cz;
+    const int cid = ref_cell(b.box, tp, cx, cy, cz);
+    if (cid < 0 || cid >= b.cell_num) {
+        b.pressure[id] = 0.0f;
+        return;
+    }
+    const float re = P.GradientInfluenceRadiusCoefficient * P.InitialParticleDistance;
+    ref_neighbours(b, id, tp, cx, cy, cz, re, [&](int x, float d, const Scalar3& q) {
+        const float w = weight(re, d);
+        const Scalar3 v1 = b.vel[x];
+        X.x += ((v1.x - v0.x) * (q.x - tp.x) * w) / (d * d);
+        X.y += ((v1.x - v0.x) * (q.y - tp.y) * w) / (d * d);
+        X.z += ((v1.x - v0.x) * (q.z - tp.z) * w) / (d * d);
+        Y.x += ((v1.y - v0.y) * (q.x - tp.x) * w) / (d * d);
+        Y.y += ((v1.y - v0.y) * (q.y - tp.y) * w) / (d * d);
+        Y.z += ((v1.y - v0.y) * (q.z - tp.z) * w) / (d * d);
+        Z.x += ((v1.z - v0.z) * (q.x - tp.x) * w) / (d * d);
+        Z.y += ((v1.z - v0.z) * (q.y - tp.y) * w) / (d * d);
+        Z.z += ((v1.z - v0.z) * (q.z - tp.z) * w) / (d * d);
+    });
+    const float g = P.Dimension / P.ConstantParticleDensity;
+    X.x = g * X.x; X.y = g * X.y; X.z = g * X.z;
+    Y.x = g * Y.x; Y.y = g * Y.y; Y.z = g * Y.z;
+    Z.x = g * Z.x; Z.y = g * Z.y; Z.z = g * Z.z;
+    D.x = (float)(0.5 * (X.y + Y.x));
+    D.y = (float)(0.5 * (X.z + Z.x));
+    D.z = (float)(0.5 * (Y.z + Z.y));
+    const float strain = X.x * X.x + Y.y * Y.y + Z.z * Z.z + 2 * D.x * D.x + 2 * D.y * D.y + 2 * D.z * D.z;
+    const float riw = b.stl_distance[id].Magnitude;
+    const float ratio = -(riw / re);
+    const float damp = 1 - expf(ratio);
+    const float smag = P.SmagorinskyConstant * damp;
+    const float coef = (smag * P.FilterWidth) * (smag * P.FilterWidth);
+    float tv = 0;
+    if (strain > 0) tv = coef * sqrtf(2 * strain);
+    if (tv > P.TurbulanViscosityRatio) tv = P.TurbulanViscosityRatio;
+    b.turb_visc[id] = tv;
+    const float tkc = 2 * P.Cnue * P.InitialParticleDistance * P.InitialParticleDistance / P.Cepsilon;
+    float tke = strain * tkc;
+    if (tke > P.TurbulanceIntensity) tke = P.TurbulanceIntensity;
+    b.strain[id] = tke;
 }
 
 // CalcExplicitPressure_Kernel (DeviceProcess_Kernel.h:921-1054)
@@ -707,8 +836,8 @@ CCTStatusType InitializeDeviceConstInputParticles(Integer* InputParticleID, Scal
                                                   Scalar* InputParticleSolidPhaseRate, ParticleType* InputParticleType,
                                                   Scalar* ParticleTurbulaceViscosity,
                                                   Scalar* ParticleStrainTensorProduct) {
-    (void)ParticleTurbulaceViscosity;
-    (void)ParticleStrainTensorProduct;
+    g_bind.turb_visc = ParticleTurbulaceViscosity;
+    g_bind.strain = ParticleStrainTensorProduct;
     g_bind.id = InputParticleID;
     g_bind.pos = InputParticlePosition;
     g_bind.vel = InputParticleVelocity;
@@ -872,7 +1001,7 @@ CCTStatusType CalcDragEffect(cudaStream_t& Stream, Integer ComputeParticleNum) {
 
 CCTStatusType CalcExplicitly(cudaStream_t& Stream, Integer ParticleNum) {
     if (ParticleNum <= 0) return CCT_NOERR;
-    if (g_bind.param.bTurbulance) return CCT_PARAMERR;
+    if (g_bind.param.bTurbulance && (!g_bind.turb_visc || !g_bind.strain)) return CCT_PARAMERR;
     MPS_COUNT_LAUNCH k_ref_explicitly<<<grid_of(ParticleNum), kBlock, 0, Stream>>>(ParticleNum, g_bind);
     return launch_status();
 }
@@ -890,16 +1019,18 @@ CCTStatusType CalcExplicitPressureGradient(cudaStream_t& Stream, Integer Compute
     return launch_status();
 }
 
-// Temperature and turbulence operators are not part of this library.
 CCTStatusType CalcTemperatureFactor(cudaStream_t& Stream, Integer ComputeParticleNum) {
-    (void)Stream;
-    (void)ComputeParticleNum;
-    return g_bind.param.bUpdateTemperature ? CCT_PARAMERR : CCT_NOERR;
+    if (ComputeParticleNum <= 0) return CCT_NOERR;
+    if (!g_bind.temperature || !g_bind.out_temperature || !g_bind.out_kin_visc) return CCT_PARAMERR;
+    MPS_COUNT_LAUNCH k_ref_temperature<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    return launch_status();
 }
+
 CCTStatusType CalcTurbulenceViscosity(cudaStream_t& Stream, Integer ComputeParticleNum) {
-    (void)Stream;
-    (void)ComputeParticleNum;
-    return g_bind.param.bTurbulance ? CCT_PARAMERR : CCT_NOERR;
+    if (ComputeParticleNum <= 0) return CCT_NOERR;
+    if (!g_bind.turb_visc || !g_bind.strain) return CCT_PARAMERR;
+    MPS_COUNT_LAUNCH k_ref_turbulence<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    return launch_status();
 }
 
 }  // extern "C"

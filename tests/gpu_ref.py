@@ -11,7 +11,7 @@ from simulation_project_gb300.lib import DeviceArray, call
 ARRAYS = ["id", "pos", "vel", "pressure", "density", "temperature", "kin_visc", "solid_rate", "type",
           "out_id", "out_pos", "out_vel", "out_pressure", "out_density", "out_temperature", "out_kin_visc",
           "out_solid_rate", "out_type", "triangles", "stl_distance", "stl_id", "cells", "cell_start", "cell_end",
-          "drag_acc", "drag_temperature", "magnifier_count", "hash", "index"]
+          "drag_acc", "drag_temperature", "magnifier_count", "turb_visc", "strain", "hash", "index"]
 
 
 class GpuRef:
@@ -36,8 +36,8 @@ class GpuRef:
              ["out_id", "out_pos", "out_vel", "out_pressure", "out_density", "out_temperature", "out_kin_visc",
               "out_solid_rate", "out_type"]])
         call("InitializeDeviceConstInputParticles", *[self.p(k) for k in
-             ["id", "pos", "vel", "pressure", "density", "temperature", "kin_visc", "solid_rate", "type"]],
-             None, None)
+             ["id", "pos", "vel", "pressure", "density", "temperature", "kin_visc", "solid_rate", "type",
+              "turb_visc", "strain"]])
         call("DragParametersToConst", self.dp.ptr, self.p("drag_acc"), self.p("drag_temperature"), st.drag_num,
              self.p("magnifier_count"), None)
 

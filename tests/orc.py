@@ -26,7 +26,7 @@ class OrcBindings(C.Structure):
         ("triangles", P), ("triangle_num", C.c_int), ("tri_params", P), ("stl_distance", P), ("stl_id", P),
         ("cells", P), ("cell_num", C.c_int), ("cell_start", P), ("cell_end", P),
         ("drag_params", P), ("drag_num", C.c_int), ("drag_acc", P), ("drag_temperature", P),
-        ("magnifier_count", P),
+        ("magnifier_count", P), ("turb_visc", P), ("strain", P),
     ]
 
 
@@ -66,6 +66,8 @@ _FUNCS = {
     "orc_calc_stl_distance": (C.c_int, [P, C.c_int]),
     "orc_calc_drag_effect": (C.c_int, [P, C.c_int]),
     "orc_calc_explicitly": (C.c_int, [P, C.c_int]),
+    "orc_calc_temperature_factor": (C.c_int, [P, C.c_int]),
+    "orc_calc_turbulence_viscosity": (C.c_int, [P, C.c_int]),
     "orc_calc_explicit_pressure": (C.c_int, [P, C.c_int]),
     "orc_calc_explicit_pressure_gradient": (C.c_int, [P, C.c_int]),
     "orc_sim_create": (P, [P, C.c_int]),
@@ -173,6 +175,8 @@ class RefState:
         self.drag_acc = f3()
         self.drag_temperature = np.zeros(m, np.float32)
         self.magnifier_count = np.zeros(m, np.int32)
+        self.turb_visc = np.zeros(m, np.float32)
+        self.strain = np.zeros(m, np.float32)
         self.hash = np.zeros(m, np.int32)
         self.index = np.zeros(m, np.int32)
         self.param = scene.param
@@ -188,7 +192,8 @@ class RefState:
         for name in ["id", "pos", "vel", "pressure", "density", "temperature", "kin_visc", "solid_rate", "type",
                      "out_id", "out_pos", "out_vel", "out_pressure", "out_density", "out_temperature",
                      "out_kin_visc", "out_solid_rate", "out_type", "triangles", "stl_distance", "stl_id", "cells",
-                     "cell_start", "cell_end", "drag_acc", "drag_temperature", "magnifier_count"]:
+                     "cell_start", "cell_end", "drag_acc", "drag_temperature", "magnifier_count", "turb_visc",
+                     "strain"]:
             setattr(b, name, getattr(self, name).ctypes.data)
         b.tri_params = C.addressof(self.tri_params)
         b.drag_params = C.addressof(self.drag_params)
@@ -314,3 +319,35 @@ class OracleSim:
         if self.h:
             self.lib.sim_destroy(self.h)
             self.h = None
+
+
+def thermal_scene(sc, seed):
+    """Turns on the temperature operator of `sc` with conductivities, wall temperatures
+    and clamps that give a visible heat step on a small block; returns a setup hook
+    that draws the initial temperatures (out_temperature, original order)."""
+    p = sc.param
+    p.bUpdateTemperature = True
+    p.TemperatureInfluenceRadiusCoefficient = 2.1
+    p.FruidThermalConductivity, p.FruidThermalResistance = 0.6, 2e-4
+    p.WallThermalConductivity, p.WallThermalResistance = 16.0, 1e-3
+    p.FruidSpecificHeat = 4186.0
+    p.MaxWallTemperature, p.MinWallTemperature = 330.0, 290.0
+    p.ViscosityUpdateParameterA, p.ViscosityUpdateParameterB = -2e-8, 7e-6
+    p.Dt = 0.01
+    for tp in sc.tri_params:
+        tp.Temperature, tp.WallThermalConductivity, tp.WallThermalResistivity = 340.0, 20.0, 5e-4
+
+    def setup(st):
+        rng = np.random.default_rng(seed)
+        st.out_temperature[:st.n] = rng.uniform(295, 325, st.n).astype(np.float32)
+    return setup
+
+
+def turbulent_scene(sc, seed):
+    """Turns on the Smagorinsky turbulence model of `sc` (viscosity cap reached on a
+    block with random velocities of 0.5 m/s)."""
+    p = sc.param
+    p.bTurbulance = True
+    p.SmagorinskyConstant, p.FilterWidth = 0.12, 0.02
+    p.TurbulanViscosityRatio, p.Cnue, p.Cepsilon, p.TurbulanceIntensity = 2e-5, 0.094, 1.048, 0.5
+    sc.vel = np.random.default_rng(seed + 7).normal(0, 0.5, sc.pos.shape)

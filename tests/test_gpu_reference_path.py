@@ -1,8 +1,9 @@
 """GPU parity of the reference-named launcher API against the oracle: hash keys,
-sort permutation, cell tables, reorder, triangle binning, wall distance, drag and the
-three explicit-schedule particle kernels must be bit-identical to the oracle (itself
-pinned to the reference's kernel code).  Wall rotation uses cosf/sinf on both sides
-and is compared with an absolute tolerance of 2e-6 m."""
+sort permutation, cell tables, reorder, triangle binning, wall distance, drag, the
+three explicit-schedule particle kernels and the temperature operator must be
+bit-identical to the oracle (itself pinned to the reference's kernel code).  Wall
+rotation uses cosf/sinf and the turbulence model's wall damping expf on both sides:
+those are compared with tolerances stated in their tests."""
 import ctypes as C
 
 import numpy as np
@@ -152,8 +153,102 @@ def test_triangle_motion_close():
 
 def test_unsupported_features_report_paramerr():
     sc = scenes.random_block(4)
-    sc.param.bTurbulance = True
+    sc.param.bNegativePressure = True
     st = orc.RefState(sc)
     g = _gpu().GpuRef(st)
-    assert lib.load().CalcTurbulenceViscosity(g.stream.ref(), st.n) == 2
-    assert lib.load().CalcExplicitly(g.stream.ref(), st.n) == 2
+    assert lib.load().CalcExplicitPressureGradient(g.stream.ref(), st.n) == 2
+
+
+HEAT = ["out_id", "out_temperature", "out_kin_visc", "temperature", "stl_distance", "stl_id", "drag_acc",
+        "drag_temperature", "out_solid_rate"]
+
+
+POWF = ["drag_temperature", "out_solid_rate", "out_temperature", "out_kin_visc"]
+
+
+def _heat_pipeline(sc, setup, with_drag):
+    st = orc.RefState(sc)
+    setup(st)
+    g = _gpu().GpuRef(st)
+    b = oracle_topology_walls(st)
+    ORC.calc_stl_distance(C.byref(b), st.n)
+    if with_drag:
+        ORC.calc_drag_effect(C.byref(b), st.n)
+    assert ORC.calc_temperature_factor(C.byref(b), st.n) == 0
+    g.topology(st.n)
+    g.walls()
+    g.run("CalcSTLDistance", st.n)
+    if with_drag:
+        g.run("CalcDragEffect", st.n)
+    assert call("CalcTemperatureFactor", g.stream.ref(), st.n) == 0
+    g.stream.sync()
+    got = g.download()
+    if not with_drag:
+        assert_same(st, got, HEAT)
+        return st
+    # the drag heating raises the slip speed to TempExponential with powf, CUDA's on the
+    # GPU and the host library's on the CPU (last-bit differences): those fields and the
+    # temperatures they heat are compared with tolerances, the rest bit for bit
+    assert_same(st, got, [f for f in HEAT if f not in POWF])
+    n = st.n
+    np.testing.assert_allclose(got["drag_temperature"][:n], st.drag_temperature[:n], rtol=1e-6, atol=0)
+    np.testing.assert_allclose(got["out_solid_rate"][:n], st.out_solid_rate[:n], rtol=1e-6, atol=0)
+    np.testing.assert_allclose(got["out_temperature"][:n], st.out_temperature[:n], rtol=0, atol=1e-4)
+    np.testing.assert_allclose(got["out_kin_visc"][:n], st.out_kin_visc[:n], rtol=1e-6, atol=0)
+    return st
+
+
+@pytest.mark.parametrize("n_side,seed", [(9, 0), (24, 2)])
+def test_temperature_bit_exact(n_side, seed):
+    sc = scenes.random_block(n_side, seed=seed)
+    st = _heat_pipeline(sc, orc.thermal_scene(sc, seed), with_drag=False)
+    t = st.out_temperature[:st.n]
+    assert (t <= 330.0).all() and (t >= 290.0).all() and len(np.unique(t)) > st.n // 2
+
+
+def test_temperature_with_drag_heating_bit_exact():
+    sc = scenes.rotating_bucket(l0=0.02, n_drag=6, drag_index=5.0)
+    sc.vel = np.random.default_rng(5).normal(0, 0.2, sc.pos.shape)
+    for d in sc.drag:
+        d.InputVelocityToken1 = b"T"
+        d.TempIndex, d.TempExponential, d.TempDragPermiabilityConstant = 2.0, 1.5, 0.5
+    sc.param.ThermalStep = 1
+    st = _heat_pipeline(sc, orc.thermal_scene(sc, 3), with_drag=True)
+    assert (st.drag_temperature[:st.n] != 0).any()
+
+
+@pytest.mark.parametrize("n_side,seed", [(9, 0), (20, 1)])
+def test_turbulence_and_explicit_step(n_side, seed):
+    """Strain-rate products and everything that does not depend on the wall damping
+    are bit-identical; the damping factor 1 - expf(-r/re) uses CUDA's expf (2 ulp) on the
+    GPU and the host library's on the CPU.  An error of k ulp in e = expf(-r/re) moves
+    damp by k ulp * e/(1-e) relative, and the viscosity carries damp squared: the
+    viscosity is compared against that bound per particle (k = 4), the predicted
+    velocities and positions to 1e-6 relative (the viscosity term is Dt-scaled)."""
+    sc = scenes.random_block(n_side, seed=seed)
+    orc.turbulent_scene(sc, seed)
+    st = orc.RefState(sc)
+    g = _gpu().GpuRef(st)
+    b = oracle_topology_walls(st)
+    ORC.calc_stl_distance(C.byref(b), st.n)
+    assert ORC.calc_turbulence_viscosity(C.byref(b), st.n) == 0
+    tv_o = st.turb_visc.copy()
+    assert ORC.calc_explicitly(C.byref(b), st.n) == 0
+    g.topology(st.n)
+    g.walls()
+    g.run("CalcSTLDistance", st.n)
+    assert call("CalcTurbulenceViscosity", g.stream.ref(), st.n) == 0
+    g.stream.sync()
+    tv_g = g.download()["turb_visc"]
+    assert call("CalcExplicitly", g.stream.ref(), st.n) == 0
+    g.stream.sync()
+    got = g.download()
+    assert_same(st, got, ["strain", "out_id", "stl_distance", "stl_id", "pressure", "id", "hash", "index"])
+    n = st.n
+    re = np.float64(sc.param.GradientInfluenceRadiusCoefficient) * sc.param.InitialParticleDistance
+    e = np.exp(-st.stl_distance["Magnitude"][:n].astype(np.float64) / re)
+    bound = tv_o[:n].astype(np.float64) * (2 * 4 * 2.0 ** -24 * e / np.maximum(1 - e, 1e-30) + 4 * 2.0 ** -24)
+    assert (np.abs(tv_g[:n].astype(np.float64) - tv_o[:n]) <= bound).all()
+    assert (tv_o[:n] > 0).any() and (tv_o[:n] == np.float32(2e-5)).any()
+    for f in ["out_vel", "out_pos", "vel", "pos"]:
+        np.testing.assert_allclose(got[f][:n], getattr(st, f)[:n], rtol=1e-6, atol=1e-9, err_msg=f)

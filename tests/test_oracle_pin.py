@@ -159,3 +159,44 @@ def test_triangle_motion():
     # cosf/sinf vs the host math library differ in the last bits: tolerance
     np.testing.assert_allclose(so.triangles["Vertex"], sr.triangles["Vertex"], rtol=0, atol=2e-6)
     assert np.abs(so.triangles["Vertex"] - orc.RefState(sc).triangles["Vertex"]).max() > 1e-3
+
+
+FIELDS_HEAT = ["out_id", "out_temperature", "out_kin_visc", "temperature", "stl_distance", "stl_id", "drag_acc",
+               "out_solid_rate"]
+FIELDS_TURB = ["turb_visc", "strain", "out_id", "out_pos", "out_vel", "pressure"]
+
+
+@pytest.mark.parametrize("seed", [0, 2])
+def test_temperature_kernel(seed):
+    sc = scenes.random_block(9, seed=seed)
+    setup = orc.thermal_scene(sc, seed)
+    so, sr = _run_both(sc, ["calc_stl_distance", "calc_temperature_factor"], setup)
+    for f in FIELDS_HEAT:
+        assert bits_equal(getattr(so, f), getattr(sr, f)), f
+    t = so.out_temperature[:so.n]
+    assert (t != np.float32(0)).all() and (t <= 330.0).all() and (t >= 290.0).all()
+
+
+def test_temperature_with_drag_heating():
+    sc = scenes.rotating_bucket(l0=0.02, n_drag=6, drag_index=5.0)
+    sc.vel = np.random.default_rng(5).normal(0, 0.2, sc.pos.shape)
+    for d in sc.drag:
+        d.InputVelocityToken1 = b"T"
+        d.TempIndex, d.TempExponential, d.TempDragPermiabilityConstant = 2.0, 1.5, 0.5
+    sc.param.ThermalStep = 1
+    setup = orc.thermal_scene(sc, 3)
+    so, sr = _run_both(sc, ["calc_stl_distance", "calc_drag_effect", "calc_temperature_factor"], setup)
+    for f in FIELDS_HEAT:
+        assert bits_equal(getattr(so, f), getattr(sr, f)), f
+    assert (so.drag_temperature[:so.n] != 0).any()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_turbulence_kernels(seed):
+    sc = scenes.random_block(9, seed=seed)
+    orc.turbulent_scene(sc, seed)
+    so, sr = _run_both(sc, ["calc_stl_distance", "calc_turbulence_viscosity", "calc_explicitly"])
+    for f in FIELDS_TURB:
+        assert bits_equal(getattr(so, f), getattr(sr, f)), f
+    assert (so.turb_visc[:so.n] > 0).any() and (so.strain[:so.n] > 0).any()
+    assert (so.turb_visc[:so.n] == np.float32(2e-5)).any()   # the cap is reached
