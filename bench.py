@@ -228,8 +228,8 @@ def run_gpu(args):
     if not args.no_learned:
         params, train_info = train_learned(Solver, scene, args.train_steps, log)
 
-    # plain FP64 Jacobi-CG (metric denominator)
-    plain = Solver(scene, precision="fp64", profile=0)
+    # plain FP64 Jacobi-CG (metric denominator), from the previous pressure
+    plain = Solver(scene, precision="fp64", profile=0, warm_start=0)
     ms_plain, _, st_plain = time_steps(plain, args.steps, args.warmup)
     plain.close()
     pps_plain = n * args.steps / (ms_plain / 1e3)
@@ -243,6 +243,11 @@ def run_gpu(args):
     ms_irm, _, st_irm = time_steps(irm, args.steps, args.warmup)
     irm.close()
     pps_irm = n * args.steps / (ms_irm / 1e3)
+    # the same from the previous pressure (no extrapolation of the pressure history)
+    irm0 = Solver(scene, precision="fp32_ir", profile=0, preconditioner=1, warm_start=0)
+    ms_irm0, _, st_irm0 = time_steps(irm0, args.steps, args.warmup)
+    irm0.close()
+    pps_irm0 = n * args.steps / (ms_irm0 / 1e3)
 
     # learned FP32 / FP64-refined solver (metric numerator), with phase timing
     fast = Solver(scene, precision="fp32_ir", profile=1, preconditioner=args.precond,
@@ -349,6 +354,12 @@ def run_gpu(args):
             "value": pps_irm, "ms_per_step": ms_irm / args.steps,
             "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_irm])),
             "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_irm]))},
+        "fp32_ir_multilevel_previous_pressure": {
+            "value": pps_irm0, "ms_per_step": ms_irm0 / args.steps,
+            "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_irm0])),
+            "ir_passes_per_step": float(np.mean([s["ir_passes"] for s in st_irm0]))},
+        "extrapolation_iterations_saved_per_step": float(
+            np.mean([s["cg_iterations"] for s in st_irm0]) - np.mean([s["cg_iterations"] for s in st_irm])),
         "network_iterations_saved_per_step": float(
             np.mean([s["cg_iterations"] for s in (st_irm if args.precond else st_ir)]) -
             np.mean([s["cg_iterations"] for s in st_fast])),
@@ -358,6 +369,7 @@ def run_gpu(args):
                         "fallbacks": int(sum(s["fallback"] for s in st_fast)),
                         "error_flags": int(np.bitwise_or.reduce([s["error_flags"] for s in st_fast])),
                         "learned": params is not None, "preconditioner": ["jacobi", "multilevel"][args.precond],
+                        "warm_start_order": int(st_fast[-1]["warm_start"]),
                         "mg_levels": int(st_fast[-1]["mg_levels"]), "mg_level1": int(st_fast[-1]["mg_level1"]),
                         "phases_ms": phases},
         "learned_training": train_info,

@@ -86,6 +86,12 @@ typedef struct MpsSolverOptions {
     int spmv_wide;          /* streamed SpMV columns: 0 automatic (32-bit columns of every
                                slice when most entries of the last step needed them, else the
                                16-bit slices), 1 always 32-bit, -1 never; same row values */
+    int warm_start;         /* start of the PPE solve from each particle's pressure history
+                               (interior rows): 0 the previous pressure P_{n-1}; 1 linear in
+                               time, 2 P_{n-1} - P_{n-2}; 2 quadratic, 3 P_{n-1} - 3 P_{n-2} +
+                               P_{n-3}; -1 (default) 2 in FP32_IR, 0 in FP64.  Limited to the
+                               history held (reset by mps_solver_set_particles and
+                               mps_solver_set_time_step) */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */
@@ -119,6 +125,7 @@ typedef struct MpsStepStats {
     long long nnz_wide;     /* interior entries stored with 32-bit columns (the rest: 16-bit) */
     int rows16;             /* 1 if the FP32 SpMV used compressed columns this step */
     int inner16;            /* 1 if the inner CG ran on the FP16-weight operator this step */
+    int warm_start;         /* extrapolation order of this step's warm start (0: P_{n-1}) */
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);
@@ -142,6 +149,12 @@ CCTStatusType mps_solver_get_triangles(MpsSolver* s, double* vertices);
  * solution, particle id, Laplacian neighbour count, sum of neighbour ids */
 CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, double* rhs, double* sol, int* id,
                                    int* nbr_count, double* nbr_idsum);
+/* Pressure history of the warm start (solver order, n entries each): the particles'
+ * last two increments P_n - P_{n-1} and P_{n-1} - P_{n-2} (0 where a particle was not
+ * interior), the interior flags of the last solve, the ids, and how many increments
+ * are held (0..2). */
+CCTStatusType mps_solver_debug_history(MpsSolver* s, float* dph1, float* dph2, unsigned char* inner, int* id,
+                                       int* held);
 /* refinement residual r = b - A p of the current state (FP32_IR solvers; host
  * array of n doubles, may be NULL) and ||r|| / ||b||: variant 0 with FP64
  * products and sums, variant 1 with the double-float kernel the solver uses (rows

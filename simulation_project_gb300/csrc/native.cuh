@@ -99,7 +99,10 @@ struct Dev {
     unsigned* red_count;       // last-block counters
     unsigned* err;
     int* istat;                // [0] longest neighbour row
-    double* pprev;             // warm-start pressure of the step (learned path)
+    double* pprev;             // the particle's pressure before this step's solve (P_{n-1})
+    float *dph1, *dph2;        // the particle's last two pressure increments P_{n-1} - P_{n-2}
+                               // and P_{n-2} - P_{n-3} (warm-start extrapolation)
+    float *dph1b, *dph2b;      // their permutation buffers (sort, compaction)
     float* feat;               // [n][12] learned features
     float* mlp_out;            // [n][2] network outputs
     float* targets;            // [n][2] training targets

@@ -169,6 +169,8 @@ __global__ void k_compact(const __grid_constant__ Dev d, const unsigned* keep, c
     d.visc2[o] = d.visc[i];
     d.type2[o] = d.type[i];
     d.id2[o] = d.id[i];
+    d.dph1b[o] = d.dph1[i];
+    d.dph2b[o] = d.dph2[i];
 }
 
 __global__ void k_hash(const __grid_constant__ Dev d) {
@@ -208,6 +210,8 @@ __global__ void k_gather(const __grid_constant__ Dev d) {
     d.visc2[i] = d.visc[s];
     d.type2[i] = d.type[s];
     d.id2[i] = d.id[s];
+    d.dph1b[i] = d.dph1[s];
+    d.dph2b[i] = d.dph2[s];
     const int sk = d.skey[i];
     const int h = sk >> d.zbits;
     // global z bin (cell z * 64 + bin inside the cell), exact in a float
@@ -1562,6 +1566,8 @@ __global__ void k_insert(const __grid_constant__ Dev d, const CParticle* __restr
     d.visc[s] = q.KineticViscosity;
     d.type[s] = (int)q.Type;
     d.id[s] = j < nholes ? holes[j] : idext + (j - nholes);
+    d.dph1[s] = 0.f;
+    d.dph2[s] = 0.f;
 }
 
 // output frames in particle-ID order: mark the IDs present (the exclusive scan of the
@@ -1617,7 +1623,7 @@ __global__ void __launch_bounds__(256) k_pressure_scale(const __grid_constant__ 
     }
 }
 
-// 12 features per particle (FP32); r holds the FP64 initial residual b - A p_prev
+// 12 features per particle (FP32); r holds the FP64 initial residual b - A p0 of the warm start p0
 // The network's neighbour aggregates come from the gradient-radius rows (index,
 // distance): mean previous pressure and velocity divergence
 // sum (v_j - v_i).(x_j - x_i) w_g / r^2 * d / n0 over the PND neighbours.
@@ -1689,6 +1695,33 @@ __global__ void k_features(const __grid_constant__ Dev d) {
     f[11] = sqrtf(vi.x * vi.x + vi.y * vi.y + vi.z * vi.z) * (float)(d.c.dt / d.c.l0 * 100.0);
 }
 
+// Extrapolated pressure increment of particle i from its last two increments: order 1
+// repeats the last one (linear in time), order 2 adds its change (quadratic:
+// P_n ~ 3 P_{n-1} - 3 P_{n-2} + P_{n-3}); order 0: none.
+__device__ __forceinline__ double warm_increment(const Dev& d, int i, int order) {
+    if (order <= 0) return 0.0;
+    const double a = (double)d.dph1[i];
+    return order >= 2 ? 2.0 * a - (double)d.dph2[i] : a;
+}
+
+// Warm start of the PPE solve: pprev = P_{n-1}, the particle's pressure after the last
+// step, and the start p0 = P_{n-1} + the extrapolated increment on interior rows.
+__global__ void k_warm_start(const __grid_constant__ Dev d, int order) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const double p = d.press[i];
+    d.pprev[i] = p;
+    if (order > 0 && d.inner[i]) d.press[i] = p + warm_increment(d, i, order);
+}
+
+// after the solve: shift the increment history (P_n - P_{n-1} on interior rows, else 0)
+__global__ void k_history(const __grid_constant__ Dev d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    d.dph2[i] = d.dph1[i];
+    d.dph1[i] = d.inner[i] ? (float)(d.press[i] - d.pprev[i]) : 0.f;
+}
+
 // predicted increment dp = scale * y0 (into z), preconditioner M^-1 = exp(y1) / diag
 // when the scaling output is used (else Jacobi)
 __global__ void k_learned_apply(const __grid_constant__ Dev d, int use_scaling) {
@@ -1708,19 +1741,19 @@ __global__ void k_learned_apply(const __grid_constant__ Dev d, int use_scaling) 
     d.minv[i] = s / d.diag[i];
 }
 
-// p = p_prev + alpha dp with alpha = (dp . r0) / (dp . A dp), the A-norm-optimal step
-// along the predicted increment (so the start is never worse than p_prev in A-norm)
+// p = p0 + alpha dp with alpha = (dp . r0) / (dp . A dp), the A-norm-optimal step
+// along the predicted increment (so the start is never worse than the warm start p0)
 __global__ void k_learned_finish(const __grid_constant__ Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const double dad = d.scal[S_LS0], dr = d.scal[S_LS1];
     double a = (dad > 0.0 && isfinite(dr / dad)) ? dr / dad : 0.0;
     if (i == 0) d.scal[S_IRTOL] = a;
-    d.press[i] = d.inner[i] ? d.pprev[i] + a * d.z[i] : 0.0;
+    d.press[i] = d.inner[i] ? d.press[i] + a * d.z[i] : 0.0;
 }
 
 // FP32 path: the same update, and the refinement residual of the new start without a
-// second residual pass: r = r0 - alpha (A dp), with r0 = b - A p_prev (FP64-accurate,
+// second residual pass: r = r0 - alpha (A dp), with r0 = b - A p0 (FP64-accurate,
 // already in d.r) and A dp the line search's FP32 product (q32); ||r|| -> S_RR, S_RNORM
 // (S_BNORM is r0's).  The FP32 error of alpha (A dp) only perturbs the first
 // refinement pass, which is followed by a freshly computed residual.
@@ -1735,7 +1768,7 @@ __global__ void __launch_bounds__(256) k_learned_finish_r(const __grid_constant_
             d.r[i] = 0.0;
             continue;
         }
-        d.press[i] = d.pprev[i] + a * d.z[i];
+        d.press[i] = d.press[i] + a * d.z[i];
         const double ri = d.r[i] - a * (double)d.q32[i];
         d.r[i] = ri;
         rr += ri * ri;
@@ -1747,9 +1780,10 @@ __global__ void __launch_bounds__(256) k_learned_finish_r(const __grid_constant_
     }
 }
 
-// training targets after a plain solve: (p - p_prev) / scale and the log of the
+// training targets after a plain solve: (p - p0) / scale, p0 the warm start the features
+// were computed at (P_{n-1} + the extrapolated increment of `order`), and the log of the
 // diagonal scale that maps the initial residual onto the error, clamped to [0.1, 10]
-__global__ void k_targets(const __grid_constant__ Dev d) {
+__global__ void k_targets(const __grid_constant__ Dev d, int order) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     float* t = d.targets + 2 * (size_t)i;
@@ -1759,7 +1793,7 @@ __global__ void k_targets(const __grid_constant__ Dev d) {
         return;
     }
     const double ps = d.scal[S_PSCALE];
-    const double e = d.press[i] - d.pprev[i];
+    const double e = d.press[i] - (d.pprev[i] + warm_increment(d, i, order));
     t[0] = (float)(e / ps);
     const double r0n = (double)d.feat[12 * (size_t)i + 10];   // r0 / (diag ps)
     const double en = e / ps;

@@ -140,6 +140,15 @@ struct Solver {
     }
 
     bool fp64() const { return opt.precision == MPS_PREC_FP64; }
+    // pressure increments recorded for the particles (0..2); reset with a new particle
+    // set or time step
+    int hist = 0;
+    // warm-start extrapolation order of this step: the option, or automatically
+    // quadratic in FP32_IR and the previous pressure in FP64; at most the history held
+    int warm_order() const {
+        const int w = opt.warm_start < 0 ? (fp64() ? 0 : 2) : opt.warm_start;
+        return std::min(w, hist);
+    }
 
     CCTStatusType init(const CParameter* prm, const CGridBox* box, int max_particles, const MpsSolverOptions* o) {
         opt = *o;
@@ -191,6 +200,7 @@ struct Solver {
         cudaError_t e = cudaSuccess;
         e = e ? e : mk(&d.pos, N); e = e ? e : mk(&d.vel, N); e = e ? e : mk(&d.pos2, N); e = e ? e : mk(&d.vel2, N);
         e = e ? e : mk(&d.press, N); e = e ? e : mk(&d.press2, N); e = e ? e : mk(&d.visc, N); e = e ? e : mk(&d.visc2, N);
+        e = e ? e : mk(&d.dph1, N); e = e ? e : mk(&d.dph2, N); e = e ? e : mk(&d.dph1b, N); e = e ? e : mk(&d.dph2b, N);
         e = e ? e : mk(&d.type, N); e = e ? e : mk(&d.type2, N); e = e ? e : mk(&d.id, N); e = e ? e : mk(&d.id2, N);
         e = e ? e : mk(&d.opos, N); e = e ? e : mk(&d.ovel, N);
         e = e ? e : mk(&d.key, N); e = e ? e : mk(&d.idx, N); e = e ? e : mk(&d.skey, N);
@@ -292,6 +302,8 @@ struct Solver {
         std::swap(d.visc, d.visc2);
         std::swap(d.type, d.type2);
         std::swap(d.id, d.id2);
+        std::swap(d.dph1, d.dph1b);
+        std::swap(d.dph2, d.dph2b);
     }
 
     CCTStatusType set_particles(int n, const double* pos, const double* vel, const double* press, const double* visc,
@@ -317,7 +329,10 @@ struct Solver {
         if (!e) e = cudaMemcpyAsync(d.visc, vi.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.type, ty.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
         if (!e) e = cudaMemcpyAsync(d.id, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+        if (!e) e = cudaMemsetAsync(d.dph1, 0, sizeof(float) * std::max(n, 1), st);
+        if (!e) e = cudaMemsetAsync(d.dph2, 0, sizeof(float) * std::max(n, 1), st);
         if (!e) e = cudaStreamSynchronize(st);
+        hist = 0;
         return cuda_status(e);
     }
 
@@ -610,9 +625,11 @@ struct Solver {
             const bool overlap_mg = use_learned && !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
             mg_setup_done = false;
             if (overlap_mg) cudaEventRecord(ev_rows, st);
+            const int warm = warm_order();
+            MPS_COUNT_LAUNCH k_warm_start<<<blocks_for(d.n), kBlock, 0, st>>>(d, warm);
+            S.warm_start = warm;
             if (use_learned || collect) {
                 timer.mark(PH_LEARNED, st);
-                cudaMemcpyAsync(d.pprev, d.press, sizeof(double) * d.n, cudaMemcpyDeviceToDevice, st);
                 if (fp64())
                     MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
                                                                                   d.r, d.rhs, 2);
@@ -659,7 +676,9 @@ struct Solver {
                 S.error_flags = (S.error_flags & ~MPS_ERR_CG) | S2.error_flags;
                 S.fallback = 1;
             }
-            if (collect) MPS_COUNT_LAUNCH k_targets<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            if (collect) MPS_COUNT_LAUNCH k_targets<<<blocks_for(d.n), kBlock, 0, st>>>(d, warm);
+            MPS_COUNT_LAUNCH k_history<<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            hist = std::min(hist + 1, 2);
         }
         timer.mark(PH_CORRECT, st);
         if (!pressure_only) {
@@ -1024,6 +1043,7 @@ struct Solver {
         c.kappa = opt.compressibility * c.rho / (c.dt * c.dt);
         c.c2 = c.rho / (c.dt * c.dt);
         c.vmax = c.l0 * (double)param.CourantNumber / c.dt;
+        hist = 0;   // the increments were taken over the old step
         return CCT_NOERR;
     }
 
@@ -1210,6 +1230,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->spmv_stream = 1;
     o->inner_weights = 16;
     o->spmv_wide = 0;
+    o->warm_start = -1;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -1221,6 +1242,7 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (o.spmv_stream != 0 && o.spmv_stream != 1) return CCT_PARAMERR;
     if (o.inner_weights != 32 && o.inner_weights != 16) return CCT_PARAMERR;
     if (o.spmv_wide < -1 || o.spmv_wide > 1) return CCT_PARAMERR;
+    if (o.warm_start < -1 || o.warm_start > 2) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {
@@ -1310,6 +1332,20 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
             cudaFree(tmp);
         }
     }
+    return mps::cuda_status(e);
+}
+
+CCTStatusType mps_solver_debug_history(MpsSolver* s, float* dph1, float* dph2, unsigned char* inner, int* id,
+                                       int* held) {
+    if (!s || !dph1 || !dph2 || !inner || !id || !held) return CCT_PARAMERR;
+    mps::Dev& d = s->s.d;
+    const int n = d.n;
+    cudaError_t e = cudaStreamSynchronize(s->s.st);
+    if (!e && n > 0) e = cudaMemcpy(dph1, d.dph1, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    if (!e && n > 0) e = cudaMemcpy(dph2, d.dph2, sizeof(float) * n, cudaMemcpyDeviceToHost);
+    if (!e && n > 0) e = cudaMemcpy(inner, d.inner, n, cudaMemcpyDeviceToHost);
+    if (!e && n > 0) e = cudaMemcpy(id, d.id, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    *held = s->s.hist;
     return mps::cuda_status(e);
 }
 

@@ -96,12 +96,14 @@ class Mlp:
             pass
 
 
-def collect_samples(scene, steps, precision="fp64", max_rows=400_000, seed=0):
+def collect_samples(scene, steps, precision="fp64", max_rows=400_000, seed=0, warm_start=2):
     """Runs the plain solver for `steps` steps and returns (features, targets) of its
     PPE solves: the network learns from (state, converged pressure) pairs of the
-    plain solver itself."""
+    plain solver itself.  The solver starts each solve from the warm start the learned
+    solver will use (`warm_start`, the quadratic extrapolation of the FP32_IR default),
+    so the features are taken there and the targets are the corrections to it."""
     from .solver import Solver
-    s = Solver(scene, precision=precision)
+    s = Solver(scene, precision=precision, warm_start=warm_start)
     s.collect(True)
     fs, ts = [], []
     rng = np.random.default_rng(seed)
@@ -156,7 +158,8 @@ def train(features, targets, epochs=4, batch=8192, lr=2e-3, seed=1, log=None, ma
 
 
 def train_on_scene(scene, steps=6, log=None):
-    """Data from `steps` plain FP64 steps of the scene, then GPU training."""
+    """Data from `steps` plain FP64 steps of the scene (started as the learned solver
+    starts, see collect_samples), then GPU training."""
     t0 = time.perf_counter()
     f, t = collect_samples(scene, steps)
     p, info = train(f, t, log=log)

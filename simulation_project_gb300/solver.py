@@ -26,7 +26,7 @@ class MpsSolverOptions(C.Structure):
                 ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
                 ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int),
                 ("matrix_free", C.c_int), ("spmv_stream", C.c_int), ("inner_weights", C.c_int),
-                ("spmv_wide", C.c_int)]
+                ("spmv_wide", C.c_int), ("warm_start", C.c_int)]
 
 
 class MpsStepStats(C.Structure):
@@ -38,7 +38,7 @@ class MpsStepStats(C.Structure):
                 ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int),
                 ("ms_precond", C.c_float), ("mg_levels", C.c_int), ("mg_level1", C.c_int),
                 ("r0_relres", C.c_double), ("nnz_wide", C.c_longlong), ("rows16", C.c_int),
-                ("inner16", C.c_int)]
+                ("inner16", C.c_int), ("warm_start", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -64,6 +64,7 @@ _SIGS = {
     "mps_solver_get_triangles": (C.c_int, [P, P]),
     "mps_solver_debug_residual": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_double)]),
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
+    "mps_solver_debug_history": (C.c_int, [P, P, P, P, P, P]),
     "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
     "mps_solver_save_frame": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, P, P]),
     "mps_solver_add_particles": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_int)]),
@@ -194,6 +195,18 @@ class Solver:
         out["id"] = ids[:n]
         out["nbr_count"] = cnt[:n]
         return out
+
+    def debug_history(self) -> dict:
+        """Warm-start pressure history in solver order: dph1 = P_n - P_{n-1}, dph2 =
+        P_{n-1} - P_{n-2} (FP32), the interior flags, ids and the number held."""
+        n = self.state(sort_by_id=False)["id"].shape[0]
+        d1, d2 = np.zeros(max(n, 1), np.float32), np.zeros(max(n, 1), np.float32)
+        inner = np.zeros(max(n, 1), np.uint8)
+        ids = np.zeros(max(n, 1), np.int32)
+        held = C.c_int()
+        _check(_lib().mps_solver_debug_history(self.h, _p(d1), _p(d2), _p(inner), _p(ids), C.byref(held)),
+               "mps_solver_debug_history")
+        return {"dph1": d1[:n], "dph2": d2[:n], "inner": inner[:n].astype(bool), "id": ids[:n], "held": held.value}
 
     def debug_residual(self, variant: int):
         """(r, ||r|| / ||b||) of the current state: variant 0 FP64 kernel, 1 the
