@@ -42,6 +42,12 @@ CCTStatusType mps_mlp_set_params(MpsMlp* m, const float* host_params);
 CCTStatusType mps_mlp_get_params(MpsMlp* m, float* host_params);
 /* Y[M][2] = MLP(X[M][12]) (device FP32) */
 CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* stream);
+/* the same with a chosen kernel: 0 the tcgen05 kernel mps_mlp_forward uses, 1 the
+ * warp-level mma.sync kernel (a cross-check) */
+CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, int variant, void* stream);
+/* nonzero if an MMA completion wait of the tcgen05 kernel ever ran out (the kernel then
+ * stops early; its outputs are incomplete) */
+CCTStatusType mps_mlp_tc_timeouts(unsigned* out);
 /* loss = mean over rows of (y0-t0)^2 + w1 (y1-t1)^2 and the gradient of every
  * parameter (device FP32, MPS_MLP_PARAMS floats) by the tensor-core backward pass */
 CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T, float w1, float* grad,

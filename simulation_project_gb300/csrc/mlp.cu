@@ -159,6 +159,8 @@ __global__ void k_pack_input(int M, const float* __restrict__ X, bf16* __restric
 struct Layers {
     bf16 *W1, *W2, *W3, *W4;      // [16][128], [128][128], [128][128], [128][16]
     float *b1, *b2, *b3, *b4;     // [128] x3, [16]
+    unsigned char* tc;            // shared-memory image of the tcgen05 inference kernel:
+                                  // W1^T .. W4^T (canonical K-major) and the biases
 };
 __global__ void k_params_to_layers(const float* __restrict__ p, Layers L) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -331,6 +333,299 @@ __global__ void __launch_bounds__(kMiWarps * 32, 1) k_mlp_infer(int M, const flo
         }
     }
 }
+// ---------------------------------------------------------------------------
+// Fused inference on the 5th-generation tensor cores (tcgen05): a persistent CTA of
+// 4 warps takes 128 rows at a time through the four layers.  Operands live in
+// shared memory in the canonical K-major layout without swizzle (core matrices of
+// 8 rows x 16 bytes; the two core matrices of one 16-wide k-step 128 bytes apart,
+// 8-row groups K/8 x 128 bytes apart): the weights W^T [n][k], staged once per CTA
+// by one bulk copy of an image prepared at each parameter update (k_layers_to_tc),
+// and the layer input [row][k].  One thread issues the MMAs of a layer
+// (tcgen05.mma.cta_group::1.kind::f16, BF16 in, FP32 accumulate, M = 128, N = 128 or
+// 16, one instruction per k-step) into 128 TMEM columns and commits them to an
+// mbarrier; after the (bounded) wait each warp reads its 32 TMEM lanes (= rows) with
+// tcgen05.ld, adds the bias, applies SiLU (silu_fast) and writes the BF16 activations
+// as the next layer's A operand.  The rows of the next tile are loaded while the
+// current one runs.  FP32 accumulate + bias and BF16 activations as k_mlp_infer.
+// ---------------------------------------------------------------------------
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 128;
+constexpr unsigned kTcTmemCols = 128;
+// byte offsets of the dynamic shared memory
+constexpr int kTcX = 0;                          // [128][16] layer-1 input
+constexpr int kTcA = kTcX + 128 * 16 * 2;        // [128][128] hidden activations
+constexpr int kTcW1 = kTcA + 128 * 128 * 2;      // W1^T [128][16]
+constexpr int kTcW2 = kTcW1 + 128 * 16 * 2;      // W2^T [128][128]
+constexpr int kTcW3 = kTcW2 + 128 * 128 * 2;     // W3^T [128][128]
+constexpr int kTcW4 = kTcW3 + 128 * 128 * 2;     // W4^T [16][128]
+constexpr int kTcB = kTcW4 + 16 * 128 * 2;       // b1, b2, b3 [128], b4 [16] (FP32)
+constexpr int kTcBar = kTcB + (3 * H + 16) * 4;  // 2 mbarriers (16 B) + TMEM address (4 B)
+constexpr size_t kTcSmem = kTcBar + 32 + 1024;   // + room to align the base to 1024 B
+
+constexpr int kTcImage = kTcBar - kTcW1;         // bytes of the weight + bias image
+static_assert(kTcImage % 16 == 0 && kTcW1 % 16 == 0, "bulk copy of the image needs 16-byte multiples");
+
+__device__ unsigned g_mlp_tc_timeout;   // set when an MMA completion wait ran out
+
+// canonical K-major offset (bytes) of element (r, k) of an operand with K columns
+__device__ __forceinline__ int tc_off(int r, int k, int K) {
+    return (r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+// shared-memory matrix descriptor: start address, leading (K) and stride (8-row)
+// byte offsets, fixed version bits 46..48 = 0b001, no swizzle
+__device__ __forceinline__ unsigned long long tc_desc(unsigned saddr, unsigned lbo, unsigned sbo) {
+    return (unsigned long long)((saddr & 0x3FFFFu) >> 4) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor of kind::f16: FP32 D, BF16 A and B, both K-major, N, M
+__host__ __device__ constexpr unsigned tc_idesc(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+__device__ __forceinline__ unsigned tc_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void tc_mma(unsigned tmem_d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                       int accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(unsigned long long* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(tc_smem(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool tc_bar_test(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(tc_smem(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool tc_bar_wait(unsigned long long* bar, unsigned parity, long long spins) {
+    for (long long k = 0; k < spins; ++k)
+        if (tc_bar_test(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy writes of shared memory -> visible to the tensor cores (async proxy)
+__device__ __forceinline__ void tc_fence_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// 32 consecutive TMEM columns of this thread's lane
+__device__ __forceinline__ void tc_ld32(unsigned taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_ld2(unsigned taddr, uint32_t& a, uint32_t& b) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=r"(a), "=r"(b) : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// the shared-memory image of W^T (canonical layout) and the biases, built once per
+// parameter update so every CTA stages it with one bulk copy
+__global__ void k_layers_to_tc(Layers L) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned char* img = L.tc - kTcW1;   // offsets below are those of the kernel's shared memory
+    if (e < FINP * H) {
+        const int k = e / H, n = e % H;
+        *reinterpret_cast<bf16*>(img + kTcW1 + tc_off(n, k, FINP)) = L.W1[e];
+    }
+    if (e < H * H) {
+        const int k = e / H, n = e % H;
+        *reinterpret_cast<bf16*>(img + kTcW2 + tc_off(n, k, H)) = L.W2[e];
+        *reinterpret_cast<bf16*>(img + kTcW3 + tc_off(n, k, H)) = L.W3[e];
+    }
+    if (e < H * FOUTP) {
+        const int k = e / FOUTP, n = e % FOUTP;
+        *reinterpret_cast<bf16*>(img + kTcW4 + tc_off(n, k, H)) = L.W4[e];
+    }
+    if (e < 3 * H + 16) {
+        float* bs = reinterpret_cast<float*>(img + kTcB);
+        bs[e] = e < H ? L.b1[e] : e < 2 * H ? L.b2[e - H] : e < 3 * H ? L.b3[e - 2 * H] : L.b4[e - 3 * H];
+    }
+}
+
+// SiLU as z/2 (1 + tanh(z/2)) with the hardware tanh approximation (one MUFU op; its
+// relative error ~2^-11 gives an absolute error <= |z| 2.5e-4, below the BF16 rounding
+// of the activation that follows for |z| < 16)
+__device__ __forceinline__ float tanh_approx(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float silu_fast(float z) {
+    const float h = 0.5f * z;
+    return fmaf(h, tanh_approx(h), h);
+}
+
+// hidden-layer epilogue: this thread's row of the 128 accumulator columns + bias,
+// SiLU, BF16 -> the A operand (row r, canonical K-major, K = 128)
+__device__ __forceinline__ void tc_epilogue_hidden(unsigned tmem_row, const float* __restrict__ bias,
+                                                   unsigned char* __restrict__ A, int r) {
+#pragma unroll 1
+    for (int c = 0; c < 4; ++c) {
+        uint32_t v[32];
+        tc_ld32(tmem_row + 32 * c, v);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint4 o;
+            uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int j = 8 * q + 2 * e;
+                w[e] = pack_bf16(silu_fast(__uint_as_float(v[j]) + bias[32 * c + j]),
+                                 silu_fast(__uint_as_float(v[j + 1]) + bias[32 * c + j + 1]));
+            }
+            *reinterpret_cast<uint4*>(A + tc_off(r, 32 * c + 8 * q, 128)) = o;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(int M, const float* __restrict__ X,
+                                                                 float* __restrict__ Y, Layers L, unsigned* err) {
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
+    unsigned char* Xs = sm + kTcX;
+    unsigned char* As = sm + kTcA;
+    float* bs = reinterpret_cast<float*>(sm + kTcB);
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + kTcBar);
+    unsigned long long* wbar = bar + 1;
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(sm + kTcBar + 16);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights and biases: one bulk copy of the prepared image (16-byte aligned, a
+    // multiple of 16 bytes), completed on wbar
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(wbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_smem(wbar)),
+                     "r"((unsigned)kTcImage)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(tc_smem(sm + kTcW1)), "l"(L.tc), "r"((unsigned)kTcImage), "r"(tc_smem(wbar))
+                     : "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
+                     "r"(kTcTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    __syncthreads();   // wbar initialised before anyone polls it
+    bool timed_out = !tc_bar_wait(wbar, 0, 1ll << 22);
+    if (__syncthreads_or(timed_out)) {
+        if (tid == 0) {
+            atomicOr(&g_mlp_tc_timeout, 1u);
+            if (err) atomicOr(err, MPS_ERR_STAGE_TIMEOUT);
+        }
+        tc_bar_wait(wbar, 0, 1ll << 24);   // the copy may still land: wait (bounded) for it
+        timed_out = true;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tmem_slot;
+    const unsigned tmem_row = tmem + ((unsigned)(32 * warp) << 16);   // this warp's lanes
+    const unsigned xa = tc_smem(Xs), aa = tc_smem(As);
+    const unsigned w1a = tc_smem(sm + kTcW1), w2a = tc_smem(sm + kTcW2), w3a = tc_smem(sm + kTcW3),
+                   w4a = tc_smem(sm + kTcW4);
+    const unsigned id128 = tc_idesc(128, 128), id16 = tc_idesc(128, 16);
+    unsigned phase = 0;
+    const int tiles = (M + kTcRows - 1) / kTcRows;
+    // this thread's row of the next tile, loaded one tile ahead
+    auto load_row = [&](int t, float4 (&x)[3]) {
+        const int row = t * kTcRows + tid;
+        if (t < tiles && row < M) {
+            const float4* xr = reinterpret_cast<const float4*>(X + (size_t)row * FIN);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) x[q] = xr[q];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) x[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    };
+    float4 xn[3];
+    load_row(blockIdx.x, xn);
+    for (int t = blockIdx.x; t < tiles && !timed_out; t += gridDim.x) {
+        const int r = tid, row = t * kTcRows + r;
+        // layer-1 input: this thread's row (12 features, BF16, zero padded to 16)
+        {
+            float f[16];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                f[4 * q] = xn[q].x; f[4 * q + 1] = xn[q].y; f[4 * q + 2] = xn[q].z; f[4 * q + 3] = xn[q].w;
+            }
+#pragma unroll
+            for (int k = 12; k < 16; ++k) f[k] = 0.f;
+            load_row(t + gridDim.x, xn);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                uint4 o;
+                o.x = pack_bf16(f[8 * h], f[8 * h + 1]);
+                o.y = pack_bf16(f[8 * h + 2], f[8 * h + 3]);
+                o.z = pack_bf16(f[8 * h + 4], f[8 * h + 5]);
+                o.w = pack_bf16(f[8 * h + 6], f[8 * h + 7]);
+                *reinterpret_cast<uint4*>(Xs + tc_off(r, 8 * h, FINP)) = o;
+            }
+        }
+        // four layers: MMAs by one thread, completion on the mbarrier, epilogue by all
+        for (int layer = 0; layer < 4 && !timed_out; ++layer) {
+            tc_fence_smem();
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                if (layer == 0) {
+                    tc_mma(tmem, tc_desc(xa, 128, 256), tc_desc(w1a, 128, 256), id128, 0);
+                } else {
+                    const unsigned wa = layer == 1 ? w2a : layer == 2 ? w3a : w4a;
+                    const unsigned idesc = layer == 3 ? id16 : id128;
+#pragma unroll 1
+                    for (int s = 0; s < 8; ++s)
+                        tc_mma(tmem, tc_desc(aa + 256 * s, 128, 2048), tc_desc(wa + 256 * s, 128, 2048), idesc, s > 0);
+                }
+                tc_commit(bar);
+            }
+            const bool ok = tc_bar_wait(bar, phase, 1ll << 22);
+            if (__syncthreads_or(!ok)) {
+                // flag it, wait (bounded) for the MMAs in flight, then leave
+                if (tid == 0) {
+                    atomicOr(&g_mlp_tc_timeout, 1u);
+                    if (err) atomicOr(err, MPS_ERR_STAGE_TIMEOUT);
+                }
+                tc_bar_wait(bar, phase, 1ll << 26);
+                timed_out = true;
+                break;
+            }
+            phase ^= 1u;
+            tc_fence_after();
+            if (layer < 3) {
+                tc_epilogue_hidden(tmem_row, bs + layer * H, As, r);
+            } else {
+                uint32_t y0, y1;
+                tc_ld2(tmem_row, y0, y1);
+                if (row < M)
+                    *reinterpret_cast<float2*>(Y + (size_t)row * FOUT) =
+                        make_float2(__uint_as_float(y0) + bs[3 * H], __uint_as_float(y1) + bs[3 * H + 1]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+    }
+}
+
 // dY = d loss / d y for loss = mean((y0 - t0)^2 + w1 (y1 - t1)^2); loss partial sums
 __global__ void k_loss_grad(int M, const float* __restrict__ Yp, const float* __restrict__ T, float w1,
                             bf16* __restrict__ dYb, float* __restrict__ dY, double* __restrict__ loss) {
@@ -430,6 +725,7 @@ struct MpsMlp {
         e = e ? e : mk(&L.W1, FINP * H); e = e ? e : mk(&L.W2, H * H); e = e ? e : mk(&L.W3, H * H);
         e = e ? e : mk(&L.W4, H * FOUTP);
         e = e ? e : mk(&L.b1, H); e = e ? e : mk(&L.b2, H); e = e ? e : mk(&L.b3, H); e = e ? e : mk(&L.b4, FOUTP);
+        e = e ? e : mk(&L.tc, (size_t)kTcImage);
         e = e ? e : mk(&Xb, B * FINP); e = e ? e : mk(&H1, B * H); e = e ? e : mk(&H2, B * H); e = e ? e : mk(&H3, B * H);
         e = e ? e : mk(&Z1, B * H); e = e ? e : mk(&Z2, B * H); e = e ? e : mk(&Z3, B * H);
         e = e ? e : mk(&Yp, B * FOUTP); e = e ? e : mk(&dY, B * FOUTP); e = e ? e : mk(&dYb, B * FOUTP);
@@ -452,6 +748,7 @@ struct MpsMlp {
     }
     cudaError_t sync_layers(cudaStream_t st) {
         MPS_COUNT_LAUNCH k_params_to_layers<<<div_up(H * H, 256), 256, 0, st>>>(p, L);
+        MPS_COUNT_LAUNCH k_layers_to_tc<<<div_up(H * H, 256), 256, 0, st>>>(L);
         return cudaGetLastError();
     }
     // forward over M rows (M <= maxb); keep pre-activations when train
@@ -512,22 +809,40 @@ struct MpsMlp {
 };
 
 namespace mps {
-// used by the solver: forward of a created MLP on M rows of features
-cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st) {
+// forward of a created MLP on M rows of features: variant 0 the tcgen05 kernel (the
+// solver's), 1 the mma.sync kernel (kept as a cross-check of the former)
+cudaError_t mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st, int variant,
+                                unsigned* err) {
     if (M <= 0) return cudaSuccess;
-    static bool smem_set = false;   // the attribute is per function, set once per process
+    static bool smem_set = false, tc_set = false;   // the attribute is per function, set once
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (variant == 0) {
+        if (!tc_set) {
+            const cudaError_t e =
+                cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+            if (e) return e;
+            tc_set = true;
+        }
+        const int tiles = (M + kTcRows - 1) / kTcRows;
+        const int grid = std::max(1, std::min(tiles, 2 * std::max(sms, 1)));
+        MPS_COUNT_LAUNCH k_mlp_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(M, X, Y, m->L, err);
+        return cudaGetLastError();
+    }
     if (!smem_set) {
         const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMiSmem);
         if (e) return e;
         smem_set = true;
     }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int tiles = (M + 15) / 16;
     const int grid = std::max(1, std::min(div_up(tiles, kMiWarps), 2 * std::max(sms, 1)));
     MPS_COUNT_LAUNCH k_mlp_infer<<<grid, kMiWarps * 32, kMiSmem, st>>>(M, X, Y, m->L);
     return cudaGetLastError();
+}
+// used by the solver (err: its error word)
+cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st, unsigned* err) {
+    return mlp_forward_variant(m, M, X, Y, st, 0, err);
 }
 }  // namespace mps
 
@@ -598,7 +913,18 @@ CCTStatusType mps_mlp_get_params(MpsMlp* m, float* host_params) {
 CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* stream) {
     if (!m || M < 0) return CCT_PARAMERR;
     if (M == 0) return CCT_NOERR;
-    return cuda_status(mlp_forward(m, M, X, Y, (cudaStream_t)stream));
+    return cuda_status(mlp_forward(m, M, X, Y, (cudaStream_t)stream, nullptr));
+}
+
+CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, int variant, void* stream) {
+    if (!m || M < 0 || variant < 0 || variant > 1) return CCT_PARAMERR;
+    if (M == 0) return CCT_NOERR;
+    return cuda_status(mlp_forward_variant(m, M, X, Y, (cudaStream_t)stream, variant, nullptr));
+}
+
+CCTStatusType mps_mlp_tc_timeouts(unsigned* out) {
+    if (!out) return CCT_PARAMERR;
+    return cuda_status(cudaMemcpyFromSymbol(out, g_mlp_tc_timeout, sizeof(unsigned)));
 }
 
 CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T, float w1, float* grad,

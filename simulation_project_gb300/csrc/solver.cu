@@ -28,7 +28,7 @@
 #include "../../include/mps_learned.h"
 
 namespace mps {
-cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st);
+cudaError_t mlp_forward(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st, unsigned* err);
 
 namespace {
 
@@ -640,7 +640,7 @@ struct Solver {
                 MPS_COUNT_LAUNCH k_features<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
                 feat_valid = true;
                 if (use_learned) {
-                    if (mlp_forward(mlp, d.n, d.feat, d.mlp_out, st)) return CCT_CUDAERR;
+                    if (mlp_forward(mlp, d.n, d.feat, d.mlp_out, st, d.err)) return CCT_CUDAERR;
                     MPS_COUNT_LAUNCH k_learned_apply<<<blocks_for(d.n), kBlock, 0, st>>>(d, (opt.learned & 2) ? 1 : 0);
                     if (fp64())
                         MPS_COUNT_LAUNCH k_spmv<double, double, double, 2><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.z,
@@ -1621,7 +1621,7 @@ CCTStatusType mps_learned_infer(MpsSolver* s, float* host_out, int* n) {
     Solver& v = s->s;
     if (!v.learned_ready || !v.mlp || !v.feat_valid) return CCT_PARAMERR;
     *n = v.d.n;
-    if (mps::mlp_forward(v.mlp, v.d.n, v.d.feat, v.d.mlp_out, v.st)) return CCT_CUDAERR;
+    if (mps::mlp_forward(v.mlp, v.d.n, v.d.feat, v.d.mlp_out, v.st, v.d.err)) return CCT_CUDAERR;
     cudaError_t e = cudaStreamSynchronize(v.st);
     if (!e && host_out) e = cudaMemcpy(host_out, v.d.mlp_out, sizeof(float) * 2 * v.d.n, cudaMemcpyDeviceToHost);
     return mps::cuda_status(e);

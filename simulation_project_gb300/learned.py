@@ -23,6 +23,8 @@ _SIGS = {
     "mps_mlp_set_params": (C.c_int, [P, P]),
     "mps_mlp_get_params": (C.c_int, [P, P]),
     "mps_mlp_forward": (C.c_int, [P, C.c_int, P, P, P]),
+    "mps_mlp_forward_variant": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
+    "mps_mlp_tc_timeouts": (C.c_int, [C.POINTER(C.c_uint)]),
     "mps_mlp_loss_grad": (C.c_int, [P, C.c_int, P, P, C.c_float, P, C.POINTER(C.c_float), P]),
     "mps_mlp_train_step": (C.c_int, [P, C.c_int, P, P, C.c_float, C.c_float, C.POINTER(C.c_float), P]),
 }
@@ -69,8 +71,19 @@ class Mlp:
         p = np.ascontiguousarray(p, np.float32)
         _check(_lib().mps_mlp_set_params(self.h, p.ctypes.data), "mps_mlp_set_params")
 
-    def forward(self, X_dev, Y_dev, M):
-        _check(_lib().mps_mlp_forward(self.h, M, X_dev, Y_dev, None), "mps_mlp_forward")
+    def forward(self, X_dev, Y_dev, M, variant=None):
+        """Y = MLP(X) on the device; variant None: the library's kernel (tcgen05), 0 the
+        same, 1 the mma.sync cross-check kernel."""
+        if variant is None:
+            _check(_lib().mps_mlp_forward(self.h, M, X_dev, Y_dev, None), "mps_mlp_forward")
+        else:
+            _check(_lib().mps_mlp_forward_variant(self.h, M, X_dev, Y_dev, variant, None), "mps_mlp_forward_variant")
+
+    @staticmethod
+    def tc_timeouts() -> int:
+        v = C.c_uint()
+        _check(_lib().mps_mlp_tc_timeouts(C.byref(v)), "mps_mlp_tc_timeouts")
+        return int(v.value)
 
     def loss_grad(self, X_dev, T_dev, M, grad_dev, w1=0.25):
         loss = C.c_float()

@@ -58,6 +58,27 @@ def test_mlp_forward_matches_oracle():
     assert np.abs(got - ref).max() <= 2e-2 * np.abs(ref).max() + 1e-4
 
 
+@pytest.mark.parametrize("rows", [1, 127, 128, 1000, 50021])
+def test_tcgen05_inference_matches_mma_sync_and_oracle(rows):
+    """The tcgen05 kernel (TMEM accumulators, 128-row tiles, ragged last tile) against
+    the mma.sync kernel and the FP64 oracle: same rounding points (FP32 accumulate +
+    bias, SiLU, BF16 activations), so both within the oracle tolerance of the forward
+    test and within 1e-2 of max |y| of each other."""
+    m, p = _net(seed=7)
+    X = np.random.default_rng(rows).normal(0, 1, (rows, 12)).astype(np.float32)
+    dX = DeviceArray.from_host(X)
+    dY0, dY1 = DeviceArray((rows, 2), np.float32), DeviceArray((rows, 2), np.float32)
+    m.forward(dX.ptr, dY0.ptr, rows, variant=0)
+    m.forward(dX.ptr, dY1.ptr, rows, variant=1)
+    y0, y1 = dY0.download(), dY1.download()
+    ref = mo.forward(p, X)
+    scale = np.abs(ref).max()
+    assert np.isfinite(y0).all()
+    assert np.abs(y0 - ref).max() <= 2e-2 * scale + 1e-4
+    assert np.abs(y0 - y1).max() <= 1e-2 * scale + 1e-4
+    assert Mlp.tc_timeouts() == 0
+
+
 def test_mlp_gradient_matches_oracle():
     m, p = _net(seed=5)
     rng = np.random.default_rng(2)
