@@ -490,9 +490,16 @@ def run_profile_case(args):
                learned=args.learned_mode if params is not None else 0)
     if params is not None:
         s.set_learned(params)
-    ms, _, st = time_steps(s, args.steps, args.warmup)
+    # the last step separately, with the library's launch count before it (the -s of an
+    # ncu launch list of that step)
+    ms, _, st = time_steps(s, args.steps - 1, args.warmup) if args.steps > 1 else (0.0, None, [])
+    before = lib.kernel_launches()
+    ms1, _, st1 = time_steps(s, 1, 0, first_step=args.warmup + args.steps - 1)
+    after = lib.kernel_launches()
+    ms, st = ms + ms1, st + st1
     s.close()
     print(json.dumps({"profile_case": True, "particles": scene.n, "ms_per_step": ms / args.steps,
+                      "launches_before_last_step": before, "launches_last_step": after - before,
                       "phases": {k: st[-1][k] for k in st[-1] if k.startswith("ms_")},
                       "spmv_launches": st[-1]["spmv_launches"], "nnz": st[-1]["nnz"],
                       "cg_iterations": st[-1]["cg_iterations"], "mg_levels": st[-1]["mg_levels"]}))

@@ -26,6 +26,8 @@ struct MgLevel {
     int* ccell;        // [n] aggregate -> cell
     int* nb;           // [27 n] neighbour aggregates (-1: none), slot (dx+1)*9+(dy+1)*3+(dz+1)
     int* par;          // [n] aggregate of the next level containing it (-1 on the last level)
+    int* child;        // [8 n] aggregates of the level below inside this one, octant order
+                       //     ((x & 1) << 2 | (y & 1) << 1 | (z & 1)), -1: none (levels >= 2)
     float* a;          // [27 n] Galerkin stencil
     float* dinv;       // [n] 1 / diagonal (0 for an aggregate without interior particles)
     float* r;          // [n] restricted residual
@@ -44,6 +46,8 @@ struct Mg {
     float* part;       // [27 n] level-1 assembly: slot sums of a (slice, cell) row segment,
                        //     stored at the segment's first row
     double* partd;     // [n] diagonal sum of that segment
+    int* rb;           // [n1 + 1] rows of level-1 aggregate I: [rb[I], rb[I + 1]) (aggregates are
+                       //     numbered in cell order and the rows are sorted by cell)
 };
 
 __device__ __forceinline__ void mg_decode(int c, int gy, int gz, int& x, int& y, int& z) {
@@ -98,7 +102,19 @@ __global__ void k_mg_links(MgLevel lv, MgLevel up, int has_up) {
         const bool in = xx >= 0 && yy >= 0 && zz >= 0 && xx < lv.gx && yy < lv.gy && zz < lv.gz;
         lv.nb[(size_t)I * 27 + s] = in ? lv.cmap[(xx * lv.gy + yy) * lv.gz + zz] : -1;
     }
-    lv.par[I] = has_up ? up.cmap[((x >> 1) * up.gy + (y >> 1)) * up.gz + (z >> 1)] : -1;
+    const int P = has_up ? up.cmap[((x >> 1) * up.gy + (y >> 1)) * up.gz + (z >> 1)] : -1;
+    lv.par[I] = P;
+    if (P >= 0) up.child[(size_t)P * 8 + (((x & 1) << 2) | ((y & 1) << 1) | (z & 1))] = I;
+}
+
+// row ranges of the level-1 aggregates
+__global__ void k_mg_rows(const __grid_constant__ Dev d, const __grid_constant__ Mg mg) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const MgLevel& L1 = mg.L[1];
+    if (I >= L1.n) return;
+    const int c = L1.ccell[I];
+    mg.rb[I] = d.cstart[c];
+    if (I == L1.n - 1) mg.rb[L1.n] = d.cend[c];
 }
 
 // per particle: level-1 aggregate and packed cell coordinates
@@ -325,9 +341,8 @@ __global__ void k_mg_restrict_fine(const __grid_constant__ Dev d, const __grid_c
     const MgLevel& L1 = mg.L[1];
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (I >= L1.n) return;
-    const int c = L1.ccell[I];
     float s = 0.f;
-    for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) s += (float)r[i];
+    for (int i = mg.rb[I] + lane; i < mg.rb[I + 1]; i += 32) s += (float)r[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
     if (lane == 0) {
@@ -337,27 +352,41 @@ __global__ void k_mg_restrict_fine(const __grid_constant__ Dev d, const __grid_c
 }
 
 // Residual of the level-lo iterate summed over the children of level-hi aggregate I2,
-// by one warp: the 8 x 28 (child, slot) terms, 7 per lane, then a fixed shuffle tree
-// (every lane returns the sum).  Slot 27 is the child's own restricted residual.
+// by one warp: the 8 x 28 (child, slot) terms, 7 per lane (t = lane + 32 q), then a
+// fixed shuffle tree (every lane returns the sum).  Slot 27 is the child's own
+// restricted residual.  The loads are issued in three waves (children; their stencil
+// entries and residuals; the neighbours' corrections) instead of one dependent chain
+// per term, and the terms are summed in the same order.
 __device__ __forceinline__ float mg_child_residual_warp(const MgLevel& lo, const MgLevel& hi, int I2, int lane) {
-    int X, Y, Z;
-    mg_decode(hi.ccell[I2], hi.gy, hi.gz, X, Y, Z);
-    int child = -1;
-    if (lane < 8) {
-        const int x = 2 * X + (lane >> 2), y = 2 * Y + ((lane >> 1) & 1), z = 2 * Z + (lane & 1);
-        if (x < lo.gx && y < lo.gy && z < lo.gz) child = lo.cmap[(x * lo.gy + y) * lo.gz + z];
-    }
-    float v = 0.f;
-    for (int t = lane; t < 224; t += 32) {
-        const int q = t / 28, s = t % 28;
-        const int I = __shfl_sync(0xffffffffu, child, q);
-        if (I < 0) continue;
-        if (s == 27) {
-            v += lo.r[I];
-        } else {
-            const int J = lo.nb[(size_t)I * 27 + s];
-            if (J >= 0) v -= lo.a[(size_t)I * 27 + s] * lo.e[J];
+    const int child = lane < 8 ? hi.child[(size_t)I2 * 8 + lane] : -1;
+    int I[7], J[7];
+    float a[7], x[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) I[q] = __shfl_sync(0xffffffffu, child, (lane + 32 * q) / 28);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const int s = (lane + 32 * q) % 28;
+        J[q] = -1;
+        a[q] = 0.f;
+        x[q] = 0.f;
+        if (I[q] >= 0) {
+            if (s == 27) {
+                x[q] = lo.r[I[q]];
+            } else {
+                J[q] = lo.nb[(size_t)I[q] * 27 + s];
+                a[q] = lo.a[(size_t)I[q] * 27 + s];
+            }
         }
+    }
+#pragma unroll
+    for (int q = 0; q < 7; ++q)
+        if (J[q] >= 0) x[q] = lo.e[J[q]];
+    float v = 0.f;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        if (I[q] < 0) continue;
+        if ((lane + 32 * q) % 28 == 27) v += x[q];
+        else if (J[q] >= 0) v -= a[q] * x[q];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -435,8 +464,7 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
         const float e1 = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
         if (lane == 0) lo.e2[I] = e1;
-        const int c = lo.ccell[I];
-        for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) {
+        for (int i = mg.rb[I] + lane; i < mg.rb[I + 1]; i += 32) {
             TV zi = TV(0);
             if (d.inner[i]) {
                 zi = (TV)m32[i] * r[i] + (TV)e1;
@@ -473,9 +501,8 @@ __global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constan
     const int nw = (gridDim.x * blockDim.x) >> 5;
     TV prr = TV(0);
     for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < L1.n; I += nw) {
-        const int c = L1.ccell[I];
         float s = 0.f;
-        for (int i = d.cstart[c] + lane; i < d.cend[c]; i += 32) {
+        for (int i = mg.rb[I] + lane; i < mg.rb[I + 1]; i += 32) {
             if (!d.inner[i]) continue;
             x[i] = x[i] + (TXA)alpha * (TXA)p[i];
             const TV ri = r[i] - alpha * q[i];

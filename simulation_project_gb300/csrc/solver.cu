@@ -403,6 +403,7 @@ struct Solver {
             e = e ? e : mk(&L.cmap, nc); e = e ? e : mk(&L.ccell, nc); e = e ? e : mk(&L.nb, 27 * nc);
             e = e ? e : mk(&L.par, nc); e = e ? e : mk(&L.a, 27 * nc); e = e ? e : mk(&L.dinv, nc);
             e = e ? e : mk(&L.r, nc); e = e ? e : mk(&L.e, nc); e = e ? e : mk(&L.e2, nc);
+            e = e ? e : mk(&L.child, 8 * nc);
             if (nc == 1) break;
             gx = (gx + 1) / 2; gy = (gy + 1) / 2; gz = (gz + 1) / 2;
         }
@@ -410,6 +411,7 @@ struct Solver {
         e = e ? e : mk(&mg.ainv, (size_t)kMgMaxDense * kMgMaxDense);
         e = e ? e : mk(&mg.agg1, (size_t)nmax); e = e ? e : mk(&mg.pcc, (size_t)nmax);
         e = e ? e : mk(&mg.part, 27 * (size_t)nmax); e = e ? e : mk(&mg.partd, (size_t)nmax);
+        e = e ? e : mk(&mg.rb, (size_t)d.cells + 1);
         e = e ? e : mk(&mg_flag, (size_t)d.cells + 1); e = e ? e : mk(&mg_counts, (size_t)kMgMaxLevels + 1);
         if (e) return CCT_MEMERR;
         if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
@@ -448,9 +450,11 @@ struct Solver {
         }
         if (!levels || L[1].n <= 0) return CCT_NOERR;   // no small enough level: Jacobi this step
         mg.levels = levels;
+        for (int l = 2; l <= levels; ++l) cudaMemsetAsync(L[l].child, 0xff, sizeof(int) * 8 * (size_t)L[l].n, ss);
         for (int l = 1; l <= levels; ++l)
             MPS_COUNT_LAUNCH k_mg_links<<<blocks_for(L[l].n), kBlock, 0, ss>>>(L[l], L[l < levels ? l + 1 : l], l < levels);
         MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, ss>>>(d, mg);
+        MPS_COUNT_LAUNCH k_mg_rows<<<blocks_for(L[1].n), kBlock, 0, ss>>>(d, mg);
         MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, ss>>>(d, mg, (const float*)d.nbrw);
         MPS_COUNT_LAUNCH k_mg_assemble_cells<<<div_up(L[1].n * 32, 256), 256, 0, ss>>>(d, mg);
         for (int l = 1; l < levels; ++l)
