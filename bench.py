@@ -70,6 +70,15 @@ def load_peaks():
         return 6800.0, "fallback"
 
 
+def load_bf16_peak():
+    """Measured dense BF16 tensor throughput (burst) in TFLOP/s, else the fallback 1900."""
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except Exception:
+        return 1900.0
+
+
 class ClockSampler:
     """nvidia-smi samples (SM clock, max clock, throttle reasons) during the timed region."""
 
@@ -323,6 +332,7 @@ def run_gpu(args):
     inflow = inflow_bench(scene, n)
     fast.close()
     sort = sort_bench(n, scene.box.cell_num, peak_gbs)
+    mlp = mlp_bench(params, n, load_bf16_peak())
     accuracy = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
 
     result = {
@@ -377,6 +387,7 @@ def run_gpu(args):
         "step_bytes": step_model,
         "pair_evaluations": pair_evals,
         "sort": sort,
+        "mlp_inference": mlp,
         "accuracy_vs_fp64": accuracy,
         "e2e": e2e,
         "frames": frames,
@@ -389,6 +400,40 @@ def run_gpu(args):
     if log:
         result["notes"] = log
     return result
+
+
+def mlp_bench(params, n, tflops_peak, reps=20):
+    """The learned guess's MLP inference on n rows of features: the tcgen05 kernel the
+    solver runs (variant 0) and the mma.sync cross-check kernel (variant 1), CUDA events
+    on the legacy stream around `reps` launches after 3 warm-up launches."""
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.learned import Mlp
+    if params is None:
+        return None
+    m = Mlp(max_batch=8192, seed=1)
+    m.set_params(params)
+    X = lib.DeviceArray.from_host(np.random.default_rng(11).normal(0, 1, (n, 12)).astype(np.float32))
+    Y = lib.DeviceArray((n, 2), np.float32)
+    out = {"rows": n, "flop_per_row_padded": 73728}
+    ev0, ev1 = lib.Event(), lib.Event()
+    for v, name in ((0, "tcgen05"), (1, "mma_sync")):
+        for _ in range(3):
+            m.forward(X.ptr, Y.ptr, n, variant=v)
+        lib.call("mps_device_sync")
+        ev0.record(None)
+        for _ in range(reps):
+            m.forward(X.ptr, Y.ptr, n, variant=v)
+        ev1.record(None)
+        lib.call("mps_device_sync")
+        us = ev0.elapsed_ms(ev1) / reps * 1e3
+        tf = 73728.0 * n / (us / 1e6) / 1e12
+        out[name] = {"us_per_launch": round(us, 1), "tflops": round(tf, 1),
+                     "frac_of_bf16_peak": round(tf / tflops_peak, 3) if tflops_peak else None}
+    out["timeouts"] = Mlp.tc_timeouts()
+    X.free()
+    Y.free()
+    m.close()
+    return out
 
 
 def sort_bench(n, cells, peak_gbs, reps=10):
