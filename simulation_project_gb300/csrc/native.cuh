@@ -92,7 +92,8 @@ struct Dev {
     double *r, *z, *p, *q;     // FP64 CG vectors
     float *r32, *z32, *p32, *q32, *d32, *m32;  // FP32 inner CG vectors, m32 = preconditioner
     double* minv;              // FP64 preconditioner (1/diag or learned)
-    float *xh, *xl;            // x = xh + xl (to ~2^-48): split pressure for the double-float residual
+    float2* xs;                // x = xs.x + xs.y (to ~2^-48): split pressure for the double-float
+                               // residual, both words of a row in one 8-byte gather
     float* pf32;               // FP32 pressure (neighbour-pressure feature)
     double* red;               // block partial sums
     double* scal;              // device scalars

@@ -1026,15 +1026,14 @@ __global__ void k_to_float_p(int n, const double* __restrict__ p, float* __restr
     if (i < n) q[i] = (float)p[i];
 }
 
-// x = xh + xl: the FP64 pressure split into two floats (representation error
+// x = xs.x + xs.y: the FP64 pressure split into two floats (representation error
 // about 2^-48 |x|) for the double-float residual
-__global__ void k_split_x(int n, const double* __restrict__ x, float* __restrict__ xh, float* __restrict__ xl) {
+__global__ void k_split_x(int n, const double* __restrict__ x, float2* __restrict__ xs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double v = x[i];
     const float h = (float)v;
-    xh[i] = h;
-    xl[i] = (float)(v - (double)h);
+    xs[i] = make_float2(h, (float)(v - (double)h));
 }
 
 // (S, C) += p + lo in double-float: TwoSum of the high words, low words added
@@ -1051,9 +1050,8 @@ __device__ __forceinline__ void df_add(float& S, float& C, float p, float lo) {
 // chains overlap, merged with TwoSum at the end (a fixed order); two rather than four
 // keep the kernel at 32 registers (8 CTAs of 256 per SM).
 template <bool NARROW>
-__device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict__ w, const float* __restrict__ xh,
-                                           const float* __restrict__ xl, size_t base, int cnt, int kmax, int sb,
-                                           float& S_out, float& C_out) {
+__device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict__ w, const float2* __restrict__ xs,
+                                           size_t base, int cnt, int kmax, int sb, float& S_out, float& C_out) {
     float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
     for (int k = 0; k < kmax; k += 4) {
         int id[4];
@@ -1068,7 +1066,8 @@ __device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (k + u < cnt) {
-                const float h = xh[id[u]], l = xl[id[u]];
+                const float2 v = xs[id[u]];
+                const float h = v.x, l = v.y;
                 const float p = __fmul_rn(wv[u], h);
                 const float pe = __fmaf_rn(wv[u], h, -p);
                 if (u & 1) df_add(S1, C1, p, __fmaf_rn(wv[u], l, pe));
@@ -1095,8 +1094,7 @@ __global__ void __launch_bounds__(256, 8) k_residual_df(const __grid_constant__ 
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     const int nslices = (d.n + 31) >> 5;
-    const float* __restrict__ xh = d.xh;
-    const float* __restrict__ xl = d.xl;
+    const float2* __restrict__ xs = d.xs;
     double part0 = 0.0, part1 = 0.0;
     for (int sl = gw; sl < nslices; sl += nw) {
         const int i = sl * 32 + lane;
@@ -1108,7 +1106,7 @@ __global__ void __launch_bounds__(256, 8) k_residual_df(const __grid_constant__ 
         float S, C;
         // 32-bit columns: the residual is compute-heavy per entry, and the 16-bit
         // form measured slower here than in the SpMV
-        df_row_sum<false>(d, w, xh, xl, base, cnt, kmax, -1, S, C);
+        df_row_sum<false>(d, w, xs, base, cnt, kmax, -1, S, C);
         if (!row) continue;
         if (!in) {
             r[i] = 0.0;
@@ -1352,8 +1350,7 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
     const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
     SliceRing<SC, SS, float, WIDE> R;
     R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, float, WIDE>::SB, bars[warp], gw, nw);
-    const float* __restrict__ xh = d.xh;
-    const float* __restrict__ xl = d.xl;
+    const float2* __restrict__ xs = d.xs;
 
     double part0 = 0.0, part1 = 0.0;
     for (int sl = gw; sl < R.nsl; sl += nw) {
@@ -1385,8 +1382,9 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
                         const bool a = k0 + g + u < cnt;
-                        h[u] = a ? xh[j[u]] : 0.f;
-                        l[u] = a ? xl[j[u]] : 0.f;
+                        const float2 v = a ? xs[j[u]] : make_float2(0.f, 0.f);
+                        h[u] = v.x;
+                        l[u] = v.y;
                     }
 #pragma unroll
                     for (int u = 0; u < 8; ++u) {
@@ -1408,8 +1406,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
         if (!done) {
             const int kmax = __reduce_max_sync(0xffffffffu, cnt);
             const size_t base = (size_t)sl * d.K * 32 + lane;
-            if (km >= 0) df_row_sum<true>(d, w, xh, xl, base, cnt, kmax, sl * 32, S0, C0);
-            else df_row_sum<false>(d, w, xh, xl, base, cnt, kmax, -1, S0, C0);
+            if (km >= 0) df_row_sum<true>(d, w, xs, base, cnt, kmax, sl * 32, S0, C0);
+            else df_row_sum<false>(d, w, xs, base, cnt, kmax, -1, S0, C0);
         }
         if (!row) continue;
         if (!in) {

@@ -227,7 +227,7 @@ struct Solver {
         e = e ? e : mk(&d.minv, N);
         e = e ? e : mk(&d.r32, N); e = e ? e : mk(&d.z32, N); e = e ? e : mk(&d.pf32, N); e = e ? e : mk(&d.q32, N);
         e = e ? e : mk(&d.d32, N); e = e ? e : mk(&d.m32, N);
-        e = e ? e : mk(&d.xh, N); e = e ? e : mk(&d.xl, N); e = e ? e : mk(&d.p32, N);
+        e = e ? e : mk(&d.xs, N); e = e ? e : mk(&d.p32, N);
         e = e ? e : mk(&d.red, 4 * (size_t)kRedBlocks);
         e = e ? e : mk(&d.scal, (size_t)S_COUNT);
         e = e ? e : mk(&d.red_count, 16);
@@ -936,7 +936,7 @@ struct Solver {
     // r = rhs - A press (FP32 weights) in double-float arithmetic; norms to the scalars
     // (rows streamed through shared memory over the 16-bit slices, else the register walk)
     void residual_df(const float* w, bool stream = true) {
-        MPS_COUNT_LAUNCH k_split_x<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.xh, d.xl);
+        MPS_COUNT_LAUNCH k_split_x<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.xs);
         if (stream && use_stream() && prefer_wide) {
             auto k = k_residual_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks, true>;
             constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps, float, true>();
