@@ -15,7 +15,8 @@
 //                                                 offsets from the slice's smallest column
 //                                                 (sbase -1: the slice spans > 65535)
 //   gnbr, gnbrr     int / T [n * KG]              gradient-radius rows (index, r)
-//   tri             double[9*T], tnrm double[3*T] walls; tcs[cells+1]/tids CSR bins
+//   tri             double[9*T], tnrm double[3*T] walls; tcs[4*cells]/tids: per cell key
+//                   2*cell + (drag), the triangles whose cell box (grown by one cell) holds it
 // Kernels take the whole record as one __grid_constant__ parameter.
 #pragma once
 

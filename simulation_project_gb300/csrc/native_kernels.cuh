@@ -248,6 +248,14 @@ __device__ __forceinline__ void tri_cell_box(const Dev& d, int t, int& i0, int& 
     i1 = min(f2i((hi[0] - (double)B.m_MinBound.x) / cs), d.box.m_GridSize.x - 1);
     j1 = min(f2i((hi[1] - (double)B.m_MinBound.y) / cs), d.box.m_GridSize.y - 1);
     k1 = min(f2i((hi[2] - (double)B.m_MinBound.z) / cs), d.box.m_GridSize.z - 1);
+    // halo: the cells whose 27-cell neighbourhood meets the triangle's cells (a cell's
+    // list is then the union of its neighbours' box lists, each triangle once)
+    if (i0 <= i1 && j0 <= j1 && k0 <= k1) {
+        i0 = max(i0 - 1, 0); j0 = max(j0 - 1, 0); k0 = max(k0 - 1, 0);
+        i1 = min(i1 + 1, d.box.m_GridSize.x - 1);
+        j1 = min(j1 + 1, d.box.m_GridSize.y - 1);
+        k1 = min(k1 + 1, d.box.m_GridSize.z - 1);
+    }
 }
 __global__ void k_bin_count(const __grid_constant__ Dev d, unsigned* cnt) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -264,11 +272,12 @@ __global__ void k_bin_fill(const __grid_constant__ Dev d, const unsigned* off, i
     tri_cell_box(d, t, i0, j0, k0, i1, j1, k1);
     unsigned o = off[t];
     const unsigned e = off[t + 1];
+    const int kind = d.tdrag[t] != 0 ? 1 : 0;   // wall and drag triangles in separate lists
     for (int i = i0; i <= i1; ++i)
         for (int j = j0; j <= j1; ++j)
             for (int k = k0; k <= k1; ++k) {
                 if (o >= e) return;
-                vcell[o] = cell_key(d.box.m_GridSize, i, j, k);
+                vcell[o] = 2 * cell_key(d.box.m_GridSize, i, j, k) + kind;
                 vtri[o] = t;
                 ++o;
             }
@@ -326,7 +335,7 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
     int cx, cy, cz;
     if constexpr (sizeof(T) == 4) {
         // FP32 path: cell of the candidate triangles in FP32 (the wall influence radius
-        // is at most one cell, so the 27 cells cover it either way)
+        // is at most one cell, so the 27-cell neighbourhood covers it either way)
         const float inv = (float)(1.0 / (double)d.box.m_CellSize);
         cx = f2i((p.x - d.box.m_BufferedZone.m_MinBound.x) * inv);
         cy = f2i((p.y - d.box.m_BufferedZone.m_MinBound.y) * inv);
@@ -337,35 +346,34 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
         cy = f2i(((double)p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
         cz = f2i(((double)p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs);
     }
-    for (int k = -1; k <= 1; ++k)
-        for (int j = -1; j <= 1; ++j)
-            for (int i = -1; i <= 1; ++i) {
-                const int m = cell_key(d.box.m_GridSize, cx + i, cy + j, cz + k);
-                if (m < 0 || m >= d.cells) continue;
-                const int s = d.tcs[m];
-                if (s < 0) continue;
-                const int e = d.tcs[d.cells + m];
-                for (int l = s; l < e; ++l) {
-                    const int t = d.tids[l];
-                    if (drag_only != (d.tdrag[t] != 0)) continue;
-                    if (t == mid) continue;
-                    V3<T> q;
-                    if constexpr (sizeof(T) == 4) {
-                        const float* v = d.tri32 + 9 * (size_t)t;
-                        q = closest_on_tri<T>(p, v3<T>(v[0], v[1], v[2]), v3<T>(v[3], v[4], v[5]), v3<T>(v[6], v[7], v[8]));
-                    } else {
-                        const double* v = d.tri + 9 * (size_t)t;
-                        q = closest_on_tri<T>(p, v3<T>(v[0], v[1], v[2]), v3<T>(v[3], v[4], v[5]), v3<T>(v[6], v[7], v[8]));
-                    }
-                    const V3<T> dv = v3(p.x - q.x, p.y - q.y, p.z - q.z);
-                    const T dd = sqrt(dv.x * dv.x + dv.y * dv.y + dv.z * dv.z);
-                    if (dd < md) {
-                        md = dd;
-                        mdir = dv;
-                        mid = t;
-                    }
-                }
-            }
+    // the triangles binned around the particle's cell (clamped to the grid): the halo
+    // list of that cell, walls or drag bodies, each triangle once
+    const Integer3 G = d.box.m_GridSize;
+    cx = min(max(cx, 0), G.x - 1);
+    cy = min(max(cy, 0), G.y - 1);
+    cz = min(max(cz, 0), G.z - 1);
+    const int key = 2 * cell_key(G, cx, cy, cz) + (drag_only ? 1 : 0);
+    const int s = d.tcs[key];
+    if (s < 0) return;
+    const int e = d.tcs[2 * d.cells + key];
+    for (int l = s; l < e; ++l) {
+        const int t = d.tids[l];
+        V3<T> q;
+        if constexpr (sizeof(T) == 4) {
+            const float* v = d.tri32 + 9 * (size_t)t;
+            q = closest_on_tri<T>(p, v3<T>(v[0], v[1], v[2]), v3<T>(v[3], v[4], v[5]), v3<T>(v[6], v[7], v[8]));
+        } else {
+            const double* v = d.tri + 9 * (size_t)t;
+            q = closest_on_tri<T>(p, v3<T>(v[0], v[1], v[2]), v3<T>(v[3], v[4], v[5]), v3<T>(v[6], v[7], v[8]));
+        }
+        const V3<T> dv = v3(p.x - q.x, p.y - q.y, p.z - q.z);
+        const T dd = sqrt(dv.x * dv.x + dv.y * dv.y + dv.z * dv.z);
+        if (dd < md) {
+            md = dd;
+            mdir = dv;
+            mid = t;
+        }
+    }
 }
 
 template <class T>

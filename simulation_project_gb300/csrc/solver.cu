@@ -209,7 +209,7 @@ struct Solver {
         e = e ? e : mk(&d.cell_list, (size_t)d.cells); e = e ? e : mk(&d.cell_count, 1);
         e = e ? e : mk(&d.wdist, N); e = e ? e : mk(&d.wdir, 3 * N); e = e ? e : mk(&d.wid, N);
         e = e ? e : mk(&d.dragv, 3 * N);
-        e = e ? e : mk(&d.tcs, 2 * (size_t)d.cells);
+        e = e ? e : mk(&d.tcs, 4 * (size_t)d.cells);   // list bounds of the 2 cells keys (walls, drag)
         const size_t N32 = (N + 31) / 32 * 32;
         e = e ? e : mk(&d.nbr, N32 * d.K); e = e ? e : mk((char**)&d.nbrw, N32 * d.K * wsz);
         e = e ? e : mk(&d.nbr16, N32 * d.K); e = e ? e : mk(&d.sbase, N32 / 32 + 1);
@@ -540,7 +540,7 @@ struct Solver {
         if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
         const unsigned nv = (unsigned)h_int[0];
         if (nv == 0) {
-            cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 2 * d.cells, st);
+            cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, st);
             bins_dirty = 0;
             return CCT_NOERR;
         }
@@ -556,10 +556,11 @@ struct Solver {
         int* vcell = bin_visit;
         d.tids = bin_visit + bin_visit_cap;
         MPS_COUNT_LAUNCH k_bin_fill<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, vcell, d.tids);
-        if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(d.cells - 1)), bin_sort, st))
+        if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(2 * d.cells - 1)), bin_sort, st))
             return CCT_CUDAERR;
-        cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 2 * d.cells, st);
-        MPS_COUNT_LAUNCH k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, st>>>((int)nv, vcell, d.tcs, d.tcs + d.cells);
+        cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, st);
+        MPS_COUNT_LAUNCH k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, st>>>((int)nv, vcell, d.tcs,
+                                                                               d.tcs + 2 * d.cells);
         bins_dirty = 0;
         return cuda_status(cudaGetLastError());
     }
