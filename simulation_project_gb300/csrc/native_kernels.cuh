@@ -177,10 +177,13 @@ __global__ void k_hash(const __grid_constant__ Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const dbl4 p = d.pos[i];
-    const double cs = d.box.m_CellSize;
-    const int a = f2i((p.x - (double)d.box.m_BufferedZone.m_MinBound.x) / cs);
-    const int b = f2i((p.y - (double)d.box.m_BufferedZone.m_MinBound.y) / cs);
-    const int c = f2i((p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs);
+    // cell coordinates from one reciprocal (FP64 divisions are slow on GB300's narrow
+    // FP64 pipe); only a coordinate within an ulp of a cell face can land otherwise
+    const double ics = 1.0 / (double)d.box.m_CellSize;
+    const double fz = (p.z - (double)d.box.m_BufferedZone.m_MinBound.z) * ics;
+    const int a = f2i((p.x - (double)d.box.m_BufferedZone.m_MinBound.x) * ics);
+    const int b = f2i((p.y - (double)d.box.m_BufferedZone.m_MinBound.y) * ics);
+    const int c = f2i(fz);
     int k = cell_key(d.box.m_GridSize, a, b, c);
     if (k < 0 || k >= d.cells) {
         atomicOr(d.err, MPS_ERR_KEY_RANGE);
@@ -190,7 +193,6 @@ __global__ void k_hash(const __grid_constant__ Dev d) {
     // of the neighbour search is then sorted by z, so a target can clip it
     int zq = 0;
     if (d.zbits) {
-        const double fz = (p.z - (double)d.box.m_BufferedZone.m_MinBound.z) / cs;
         zq = f2i((fz - (double)c) * (double)(1 << d.zbits));
         zq = zq < 0 ? 0 : (zq > (1 << d.zbits) - 1 ? (1 << d.zbits) - 1 : zq);
     }
@@ -787,7 +789,9 @@ __global__ void k_eos(const __grid_constant__ Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const double pnd = d.pnd[i];
-    d.press[i] = pnd > d.c.beta * d.c.n0_pnd ? d.c.sonic2 * d.c.rho / d.c.n0_pnd * (pnd - d.c.n0_pnd) : 0.0;
+    const double p = pnd > d.c.beta * d.c.n0_pnd ? d.c.sonic2 * d.c.rho / d.c.n0_pnd * (pnd - d.c.n0_pnd) : 0.0;
+    d.press[i] = p;
+    d.pf32[i] = (float)p;
 }
 
 // ---------------------------------------------------------------------------
@@ -1726,6 +1730,7 @@ __global__ void k_history(const __grid_constant__ Dev d) {
     if (i >= d.n) return;
     d.dph2[i] = d.dph1[i];
     d.dph1[i] = d.inner[i] ? (float)(d.press[i] - d.pprev[i]) : 0.f;
+    d.pf32[i] = (float)d.press[i];   // FP32 copy for the correction's pair terms
 }
 
 // predicted increment dp = scale * y0 (into z), preconditioner M^-1 = exp(y1) / diag
@@ -1834,6 +1839,9 @@ __global__ void k_axpy_ir(const __grid_constant__ Dev d, double* x, const float*
 // pressure-gradient correction (CalcExplicitPressureGradient_Kernel semantics)
 // ---------------------------------------------------------------------------
 template <class T>
+__device__ void correct_finish(const Dev& d, int i, T gx, T gy, T gz);
+
+template <class T>
 __global__ void k_correct(const __grid_constant__ Dev d) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
@@ -1853,6 +1861,57 @@ __global__ void k_correct(const __grid_constant__ Dev d) {
         gy += (pj.y - pi.y) * pc;
         gz += (pj.z - pi.z) * pc;
     }
+    correct_finish<T>(d, i, gx, gy, gz);
+}
+
+// FP32 path of the correction: a warp takes 32 consecutive particles; for each, the
+// lanes read its gradient row together (coalesced) with the pair pressures from the
+// FP32 copy of the solved pressure (no FP64 arithmetic per pair: GB300's FP64 pipe is
+// narrow), the sums are shuffle-reduced and parked in the particle's lane, and every
+// lane then finishes its own particle (correct_finish, FP64 state update).
+__global__ void k_correct_warp(const __grid_constant__ Dev d) {
+    const int lane = threadIdx.x & 31;
+    const int base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    const float reg = (float)d.c.re_grad, mindg = (float)d.c.mind_grad;
+    float mx = 0.f, my = 0.f, mz = 0.f;
+    for (int q = 0; q < 32 && base + q < d.n; ++q) {   // warp-uniform
+        const int iq = base + q;
+        const float4 pi = d.opos[iq];
+        const float Pi = d.pf32[iq];
+        const int gc = d.gcnt[iq];
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+        for (int k = lane; k < gc; k += 32) {
+            const size_t e = (size_t)iq * d.KG + k;
+            const int j = d.gnbr[e];
+            const float r = ((const float*)d.gnbrr)[e];
+            const float4 pj = d.opos[j];
+            const float rr = r > mindg ? r : mindg;
+            const float pc = 0.5f * (d.pf32[j] + Pi) * (reg / rr - 1.f) / (rr * rr);
+            gx += (pj.x - pi.x) * pc;
+            gy += (pj.y - pi.y) * pc;
+            gz += (pj.z - pi.z) * pc;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            gx += __shfl_xor_sync(0xffffffffu, gx, o);
+            gy += __shfl_xor_sync(0xffffffffu, gy, o);
+            gz += __shfl_xor_sync(0xffffffffu, gz, o);
+        }
+        if (lane == q) {
+            mx = gx;
+            my = gy;
+            mz = gz;
+        }
+    }
+    const int i = base + lane;
+    if (i < d.n) correct_finish<float>(d, i, mx, my, mz);
+}
+
+// the per-particle end of the correction: FP64 gradient with the wall terms, velocity
+// update with the Courant clamp, position update (CalcExplicitPressureGradient_Kernel)
+template <class T>
+__device__ void correct_finish(const Dev& d, int i, T gx, T gy, T gz) {
+    const double Pi = d.press[i];
     double g[3] = {(double)gx * d.c.c1, (double)gy * d.c.c1, (double)gz * d.c.c1};
     if (d.wid[i] >= 0) {
         const double m = d.wdist[i];

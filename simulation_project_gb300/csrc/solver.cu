@@ -687,7 +687,10 @@ struct Solver {
         }
         timer.mark(PH_CORRECT, st);
         if (!pressure_only) {
-            MPS_COUNT_LAUNCH k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
+            if constexpr (sizeof(T) == 4)
+                MPS_COUNT_LAUNCH k_correct_warp<<<div_up((d.n + 31) / 32, 8), 256, 0, st>>>(d);
+            else
+                MPS_COUNT_LAUNCH k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
             std::swap(d.pos, d.pos2);
             std::swap(d.vel, d.vel2);
         }
