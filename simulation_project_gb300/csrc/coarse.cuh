@@ -26,6 +26,7 @@ struct MgLevel {
     int* ccell;        // [n] aggregate -> cell
     int* nb;           // [27 n] neighbour aggregates (-1: none), slot (dx+1)*9+(dy+1)*3+(dz+1)
     int* par;          // [n] aggregate of the next level containing it (-1 on the last level)
+    int* nbp;          // [27 n] par of each stencil neighbour, loaded beside nb by the up sweeps
     int* child;        // [8 n] aggregates of the level below inside this one, octant order
                        //     ((x & 1) << 2 | (y & 1) << 1 | (z & 1)), -1: none (levels >= 2)
     float* a;          // [27 n] Galerkin stencil
@@ -40,6 +41,7 @@ struct Mg {
     float omega;       // Jacobi weight of the smoothing sweeps
     MgLevel L[kMgMaxLevels + 1];   // L[0] unused
     float* ainv;       // [n_last^2] inverse of the last level's matrix
+    unsigned* done;    // CTAs of the last restriction that finished (k_mg_down; reset to 0)
     int* agg1;         // [n] particle -> level-1 aggregate
     unsigned* pcc;     // [n] cell coordinates of the particle, 10 bits each (x<<20 | y<<10 | z),
                        //     bit 31 set for an interior particle
@@ -115,6 +117,14 @@ __global__ void k_mg_rows(const __grid_constant__ Dev d, const __grid_constant__
     const int c = L1.ccell[I];
     mg.rb[I] = d.cstart[c];
     if (I == L1.n - 1) mg.rb[L1.n] = d.cend[c];
+}
+
+// parent of every stencil neighbour (after the level's links)
+__global__ void k_mg_nbpar(MgLevel lv) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 27 * lv.n) return;
+    const int J = lv.nb[e];
+    lv.nbp[e] = J >= 0 ? lv.par[J] : -1;
 }
 
 // per particle: level-1 aggregate and packed cell coordinates
@@ -393,16 +403,46 @@ __device__ __forceinline__ float mg_child_residual_warp(const MgLevel& lo, const
     return v;
 }
 
-// restriction lo -> hi and the first down sweep on hi: warp per hi aggregate
-__global__ void k_mg_down(const double* __restrict__ scal, MgLevel lo, MgLevel hi, float omega) {
-    if (scal[S_CONV] != 0.0) return;
-    const int I2 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (I2 >= hi.n) return;   // warp-uniform
-    const float s = mg_child_residual_warp(lo, hi, I2, lane);
-    if (lane == 0) {
-        hi.r[I2] = s;
-        hi.e[I2] = omega * hi.dinv[I2] * s;
+// last level: e2 = A^-1 r with the explicit inverse, by one CTA (warp per row; r read
+// through L2, it was written by other CTAs)
+__device__ __forceinline__ void mg_dense_solve_cta(const MgLevel& lv, const float* __restrict__ ainv) {
+    __shared__ float rs[kMgMaxDense];
+    for (int I = threadIdx.x; I < lv.n; I += blockDim.x) rs[I] = __ldcg(lv.r + I);
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int I = w; I < lv.n; I += nw) {
+        float v = 0.f;
+        for (int J = lane; J < lv.n; J += 32) v += ainv[I * lv.n + J] * rs[J];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) lv.e2[I] = v;
     }
+}
+
+// restriction lo -> hi and the first down sweep on hi: warp per hi aggregate.  With
+// ainv (hi is the last level) the CTA that finishes last (counted on `done`, reset by
+// it) also solves hi with the explicit inverse, one launch less per V-cycle.
+__global__ void k_mg_down(const double* __restrict__ scal, MgLevel lo, MgLevel hi, float omega,
+                          const float* __restrict__ ainv, unsigned* __restrict__ done) {
+    if (scal[S_CONV] != 0.0) return;   // the same for every CTA of the launch
+    const int I2 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (I2 < hi.n) {   // warp-uniform
+        const float s = mg_child_residual_warp(lo, hi, I2, lane);
+        if (lane == 0) {
+            hi.r[I2] = s;
+            hi.e[I2] = omega * hi.dinv[I2] * s;
+        }
+    }
+    if (!ainv) return;
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    mg_dense_solve_cta(hi, ainv);
+    if (threadIdx.x == 0) *done = 0u;
 }
 
 // one more weighted-Jacobi sweep on a level: out = in + omega D^-1 (r - A in); warp per
@@ -432,7 +472,7 @@ __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
     float t = 0.f;
     if (lane < 27) {
         const int J = lo.nb[(size_t)I * 27 + lane];
-        if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.par[J]]);
+        if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.nbp[(size_t)I * 27 + lane]]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
@@ -458,7 +498,7 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
         float t = 0.f;
         if (lane < 27) {
             const int J = lo.nb[(size_t)I * 27 + lane];
-            if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.par[J]]);
+            if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.nbp[(size_t)I * 27 + lane]]);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
@@ -531,17 +571,7 @@ __global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constan
 __global__ void __launch_bounds__(1024) k_mg_dense_solve(const double* __restrict__ scal, MgLevel lv,
                                                          const float* __restrict__ ainv) {
     if (scal[S_CONV] != 0.0) return;
-    __shared__ float rs[kMgMaxDense];
-    for (int I = threadIdx.x; I < lv.n; I += blockDim.x) rs[I] = lv.r[I];
-    __syncthreads();
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int I = w; I < lv.n; I += nw) {
-        float v = 0.f;
-        for (int J = lane; J < lv.n; J += 32) v += ainv[I * lv.n + J] * rs[J];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) lv.e2[I] = v;
-    }
+    mg_dense_solve_cta(lv, ainv);
 }
 
 // fine level: z = m r + e1[aggregate] on interior rows (0 elsewhere), rz = r.z;

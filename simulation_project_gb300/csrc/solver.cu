@@ -403,12 +403,14 @@ struct Solver {
             e = e ? e : mk(&L.cmap, nc); e = e ? e : mk(&L.ccell, nc); e = e ? e : mk(&L.nb, 27 * nc);
             e = e ? e : mk(&L.par, nc); e = e ? e : mk(&L.a, 27 * nc); e = e ? e : mk(&L.dinv, nc);
             e = e ? e : mk(&L.r, nc); e = e ? e : mk(&L.e, nc); e = e ? e : mk(&L.e2, nc);
-            e = e ? e : mk(&L.child, 8 * nc);
+            e = e ? e : mk(&L.child, 8 * nc); e = e ? e : mk(&L.nbp, 27 * nc);
             if (nc == 1) break;
             gx = (gx + 1) / 2; gy = (gy + 1) / 2; gz = (gz + 1) / 2;
         }
         mg_grid_levels = std::min(l, kMgMaxLevels);
         e = e ? e : mk(&mg.ainv, (size_t)kMgMaxDense * kMgMaxDense);
+        e = e ? e : mk(&mg.done, 1);
+        if (!e) e = cudaMemset(mg.done, 0, sizeof(unsigned));
         e = e ? e : mk(&mg.agg1, (size_t)nmax); e = e ? e : mk(&mg.pcc, (size_t)nmax);
         e = e ? e : mk(&mg.part, 27 * (size_t)nmax); e = e ? e : mk(&mg.partd, (size_t)nmax);
         e = e ? e : mk(&mg.rb, (size_t)d.cells + 1);
@@ -453,6 +455,8 @@ struct Solver {
         for (int l = 2; l <= levels; ++l) cudaMemsetAsync(L[l].child, 0xff, sizeof(int) * 8 * (size_t)L[l].n, ss);
         for (int l = 1; l <= levels; ++l)
             MPS_COUNT_LAUNCH k_mg_links<<<blocks_for(L[l].n), kBlock, 0, ss>>>(L[l], L[l < levels ? l + 1 : l], l < levels);
+        for (int l = 1; l < levels; ++l)
+            MPS_COUNT_LAUNCH k_mg_nbpar<<<blocks_for(27 * L[l].n), kBlock, 0, ss>>>(L[l]);
         MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, ss>>>(d, mg);
         MPS_COUNT_LAUNCH k_mg_rows<<<blocks_for(L[1].n), kBlock, 0, ss>>>(d, mg);
         MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, ss>>>(d, mg, (const float*)d.nbrw);
@@ -481,9 +485,14 @@ struct Solver {
             MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e, L[1].e2, om);
             std::swap(L[1].e, L[1].e2);
         }
-        for (int l = 1; l < lv; ++l)
-            MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
-        MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
+        // the last restriction also solves the last level densely (its last CTA, of
+        // 1024 threads like the stand-alone dense solve)
+        for (int l = 1; l < lv; ++l) {
+            const int tpb = l + 1 == lv ? 1024 : 256;
+            MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, tpb), tpb, 0, st>>>(
+                d.scal, L[l], L[l + 1], om, l + 1 == lv ? mg.ainv : nullptr, mg.done);
+        }
+        if (lv == 1) MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
         // the level-2 -> level-1 up sweep carries the fine level when no extra level-1
         // sweeps follow it (and the reduction buffer holds its CTAs' partials)
         const int up1_blocks = div_up(L[1].n * 32, 256);
