@@ -57,8 +57,9 @@ typedef struct MpsSolverOptions {
     double cg_rtol;         /* PPE relative residual target (||b - A p|| / ||b||) */
     int cg_max_iter;        /* CG iteration cap (per solve) */
     double ir_inner_rtol;   /* floor of the FP32 inner CG tolerance relative to the refinement
-                               residual; <= 0: automatic (1e-4 for the FP16-weight operator
-                               under the multilevel preconditioner, else 2e-6) */
+                               residual; <= 0: automatic (7e-4 for the FP16-weight operator
+                               under the multilevel preconditioner, about the contraction a
+                               refinement pass can reach with that operator; else 2e-6) */
     int ir_max_outer;       /* refinement pass cap */
     int max_neighbours;     /* capacity of a Laplacian neighbour row */
     int check_every;        /* CG convergence is read back every this many iterations */

@@ -613,6 +613,11 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         T a0 = 0, a1 = 0, a2 = 0, a3 = 0;   // mode-specific accumulators
         int cnt = 0, gcnt = 0;
         const size_t row0 = sell_index(i, 0, d.K);   // SELL position of the row's entry 0
+        // the row's first entries (SELL row, gradient row): one wide multiply-add per store
+        int* const nrow = d.nbr + row0;
+        T* const wrow = (T*)d.nbrw + row0;
+        int* const grow = d.gnbr + (size_t)i * d.KG;
+        T* const grrow = (T*)d.gnbrr + (size_t)i * d.KG;
         // z window of each run for this target: the run (3 cells stacked in z) is sorted
         // by z bin; the bins a neighbour can occupy are those within +-sqrt(re^2 - dxy^2)
         // of the target, dxy its distance to the run's column in x-y (re^2 with a 2e-4
@@ -706,9 +711,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     } else {
                         const int slot = cnt + __popc(bal & lt);
                         if (slot < d.K) {
-                            const size_t e = row0 + (size_t)slot * 32;
-                            d.nbr[e] = j;
-                            ((T*)d.nbrw)[e] = w;
+                            nrow[slot * 32] = j;
+                            wrow[slot * 32] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
                         if (rr < reg) {
@@ -726,8 +730,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     if (gacc) {
                         const int slot = gcnt + __popc(gb & lt);
                         if (slot < d.KG) {
-                            d.gnbr[(size_t)i * d.KG + slot] = j;
-                            ((T*)d.gnbrr)[(size_t)i * d.KG + slot] = rr;
+                            grow[slot] = j;
+                            grrow[slot] = rr;
                         }
                     }
                     gcnt += __popc(gb);

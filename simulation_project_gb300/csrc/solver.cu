@@ -972,12 +972,15 @@ struct Solver {
         }
     }
 
-    // inner-solve floor: the option, or automatically 1e-4 for the FP16-weight operator
-    // under the multilevel preconditioner (a pass contracts the FP32-weight residual by
-    // at most ~5e-4 then; measured fastest) and 2e-6 otherwise
+    // inner-solve floor: the option, or automatically 7e-4 for the FP16-weight operator
+    // under the multilevel preconditioner and 2e-6 otherwise.  With the FP16 weights a
+    // refinement pass contracts the FP32-weight residual only down to about the weights'
+    // relative rounding (2^-11 ~ 4.9e-4), so inner iterations past it are lost; measured
+    // at 882k particles: 1e-4 -> 28.0, 7e-4 -> 27.0 CG iterations per step, 2 passes
+    // either way (1e-3 and above add third passes)
     double ir_inner_rtol() const {
         if (opt.ir_inner_rtol > 0) return opt.ir_inner_rtol;
-        return inner16() && mg_ready ? 1e-4 : 2e-6;
+        return inner16() && mg_ready ? 7e-4 : 2e-6;
     }
 
     // FP32 Jacobi-PCG inside FP64 iterative refinement
