@@ -267,22 +267,24 @@ __global__ void k_bin_count(const __grid_constant__ Dev d, unsigned* cnt) {
     const long long c = (long long)max(i1 - i0 + 1, 0) * max(j1 - j0 + 1, 0) * max(k1 - k0 + 1, 0);
     cnt[t] = (unsigned)min(c, (long long)1 << 20);
 }
+// warp per triangle: its lanes write the (cell key, triangle) entries of its cell box,
+// entry q = ((i - i0) nj + (j - j0)) nk + (k - k0) at off[t] + q (at most the counted ones)
 __global__ void k_bin_fill(const __grid_constant__ Dev d, const unsigned* off, int* vcell, int* vtri) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= d.tri_n) return;
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (t >= d.tri_n) return;   // warp-uniform
     int i0, j0, k0, i1, j1, k1;
     tri_cell_box(d, t, i0, j0, k0, i1, j1, k1);
-    unsigned o = off[t];
-    const unsigned e = off[t + 1];
+    const unsigned o = off[t];
+    const unsigned cnt = off[t + 1] - o;
+    const int nj = j1 - j0 + 1, nk = k1 - k0 + 1;
     const int kind = d.tdrag[t] != 0 ? 1 : 0;   // wall and drag triangles in separate lists
-    for (int i = i0; i <= i1; ++i)
-        for (int j = j0; j <= j1; ++j)
-            for (int k = k0; k <= k1; ++k) {
-                if (o >= e) return;
-                vcell[o] = 2 * cell_key(d.box.m_GridSize, i, j, k) + kind;
-                vtri[o] = t;
-                ++o;
-            }
+    for (unsigned q = lane; q < cnt; q += 32) {
+        const int k = k0 + (int)(q % (unsigned)nk);
+        const int j = j0 + (int)((q / (unsigned)nk) % (unsigned)nj);
+        const int i = i0 + (int)(q / ((unsigned)nk * (unsigned)nj));
+        vcell[o + q] = 2 * cell_key(d.box.m_GridSize, i, j, k) + kind;
+        vtri[o + q] = t;
+    }
 }
 __global__ void k_bin_bounds(int nv, const int* vcell, int* ts, int* te) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -564,7 +564,7 @@ struct Solver {
         }
         int* vcell = bin_visit;
         d.tids = bin_visit + bin_visit_cap;
-        MPS_COUNT_LAUNCH k_bin_fill<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, vcell, d.tids);
+        MPS_COUNT_LAUNCH k_bin_fill<<<div_up(t * 32, 256), 256, 0, st>>>(d, bin_off, vcell, d.tids);
         if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(2 * d.cells - 1)), bin_sort, st))
             return CCT_CUDAERR;
         cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, st);
