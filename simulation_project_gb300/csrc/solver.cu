@@ -140,6 +140,9 @@ struct Solver {
     }
 
     bool fp64() const { return opt.precision == MPS_PREC_FP64; }
+    // inner CG iterations of each refinement pass in the last step (first batch sizes)
+    static constexpr int kPassMemory = 4;
+    int pass_its[kPassMemory] = {0, 0, 0, 0};
     // pressure increments recorded for the particles (0..2); reset with a new particle
     // set or time step
     int hist = 0;
@@ -891,12 +894,18 @@ struct Solver {
             MPS_COUNT_LAUNCH k_spmv<float, float, float, 2><<<kRedBlocks, 256, 0, st>>>(d, w, d.z32, d.q32, d.r, 6);
     }
 
+    // CG iterations in batches with one convergence read-back after each (the kernels
+    // of a batch return at once after convergence).  predict > 2 (the same pass's count
+    // in the last step): a first batch of predict - 1 iterations, then batches of 2, so
+    // few launches run past convergence; else batches of check_every.
     template <class TW, class TV, class TXA>
-    int cg_loop(TXA* x, TV* r, TV* z, TV* p, TV* q, const TW* w, const double* m64, const float* m32, int maxit) {
+    int cg_loop(TXA* x, TV* r, TV* z, TV* p, TV* q, const TW* w, const double* m64, const float* m32, int maxit,
+                int predict = 0) {
         const int every = opt.check_every > 0 ? opt.check_every : 8;
+        int batch = predict > 2 ? predict - 1 : every;
         int done = 0;
         while (done < maxit + every) {
-            for (int k = 0; k < every; ++k) {
+            for (int k = 0; k < batch; ++k) {
                 timer.mark(PH_SPMV, st);
                 spmv_cg<TW, TV>(w, p, q);
                 timer.mark(PH_VEC, st);
@@ -914,9 +923,10 @@ struct Solver {
                 MPS_COUNT_LAUNCH k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
                 ++spmv_launches;
             }
-            done += every;
+            done += batch;
             if (stream_failed || pull_scal()) return -1;
             if (h_scal[S_CONV] != 0.0) break;
+            batch = predict > 2 ? 2 : every;
         }
         return (int)h_scal[S_ITER];
     }
@@ -1020,9 +1030,11 @@ struct Solver {
                 mg_apply(d.r32, d.z32, d.p32, 1);
                 timer.mark(PH_VEC, st);
             }
+            const int pi = outer < kPassMemory ? outer : kPassMemory - 1;
             const int it = cg_loop<float, float, float>(d.d32, d.r32, d.z32, d.p32, d.q32, w, nullptr, d.m32,
-                                                        opt.cg_max_iter);
+                                                        opt.cg_max_iter, pass_its[pi]);
             if (it < 0) return CCT_CUDAERR;
+            pass_its[pi] = it;
             S.cg_iterations += it;
             MPS_COUNT_LAUNCH k_axpy_ir<<<kRedBlocks, 256, 0, st>>>(d, d.press, d.d32, rn);
             ++outer;
