@@ -10,7 +10,9 @@
 // and writes FP32 and/or BF16; split-K CTAs accumulate with FP32 atomics.
 // The network is tiny (69 kFLOP per particle per forward), so these kernels are a
 // small part of a solver step; they exist so the network is trained on the GPU by
-// this library's own kernels.
+// this library's own kernels.  The solver's inference runs on the 5th-generation
+// tensor cores (k_mlp_infer_tc: tcgen05.mma into TMEM, weights staged by one bulk
+// copy); the fused mma.sync inference kernel (k_mlp_infer) is kept as its cross-check.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <stdio.h>
