@@ -66,7 +66,9 @@ typedef struct MpsSolverOptions {
     double source_relaxation; /* gamma in b = gamma rho/dt^2 (n* - n0)/n0 (Tanaka & Masunaga 2010) */
     int profile;            /* 1: time every phase with CUDA events on the solver stream */
     int preconditioner;     /* MPS_PRECOND_* (FP32_IR) */
-    double mg_omega;        /* Jacobi weight of the multilevel smoothing sweeps */
+    double mg_omega;        /* Jacobi weight of the multilevel smoothing sweeps (default 1.3;
+                               the V-cycle stops being a positive definite preconditioner
+                               above about 1.6 on the MPS Laplacians measured) */
     int compress_rows;      /* 1: 16-bit column offsets for the FP32 SpMV where a 32-row
                                slice spans <= 65535 columns (same results, fewer bytes) */
     int mg_sweeps;          /* weighted-Jacobi sweeps on level 1 before the restriction and

@@ -422,7 +422,7 @@ struct Solver {
         if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
         const int smem = (2 * kMgMaxDense * kMgMaxDense + kMgMaxDense) * (int)sizeof(float);
         if (cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) return CCT_CUDAERR;
-        mg.omega = opt.mg_omega > 0 ? (float)opt.mg_omega : 1.0f;
+        mg.omega = opt.mg_omega > 0 ? (float)opt.mg_omega : 1.3f;
         mg_on = mg_grid_levels >= 1;
         return CCT_NOERR;
     }
@@ -1255,7 +1255,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->check_every = 8;
     o->source_relaxation = 0.05;
     o->preconditioner = MPS_PRECOND_MULTILEVEL;
-    o->mg_omega = 1.0;
+    o->mg_omega = 1.3;   // over-relaxed: measured 27.2 -> 25.9 CG iterations at 882k; 1.7 diverges
     o->compress_rows = 1;
     o->mg_sweeps = 1;
     o->matrix_free = 0;
