@@ -48,3 +48,21 @@ def test_library_is_built_for_sm103a():
     path = build.build()
     blob = open(path, "rb").read()
     assert b"sm_103a" in blob
+
+
+def test_default_options_through_the_python_mirror(so):
+    """mps_solver_default_options (host code, no GPU) read through the ctypes mirror of
+    MpsSolverOptions: every field lands where the header puts it, with the documented
+    defaults (FP32 inner solve on FP16 weights streamed by bulk copies, multilevel
+    preconditioner with smoothing weight 1.3, automatic warm start and inner floor)."""
+    from simulation_project_gb300.solver import default_options, MpsSolverOptions
+    o = default_options()
+    # 14 ints and 9 doubles in header order, naturally aligned (four 4-byte pads)
+    assert C.sizeof(MpsSolverOptions) == 144
+    assert o.precision == 1 and o.pressure_mode == 0 and o.learned == 0
+    assert o.compressibility == 1e-9 and o.cg_rtol == 1e-8 and o.cg_max_iter == 5000
+    assert o.ir_inner_rtol == 0.0 and o.ir_max_outer == 12 and o.max_neighbours == 384
+    assert o.check_every == 8 and o.source_relaxation == 0.05
+    assert o.preconditioner == 1 and o.mg_omega == 1.3 and o.compress_rows == 1 and o.mg_sweeps == 1
+    assert o.matrix_free == 0 and o.spmv_stream == 1 and o.inner_weights == 16 and o.spmv_wide == 0
+    assert o.warm_start == -1
