@@ -135,6 +135,27 @@ def test_explicit_step_kernels(seed):
     assert np.abs(so.out_pressure[:so.n]).max() > 0
 
 
+@pytest.mark.parametrize("seed", [0, 2])
+def test_explicit_step_kernels_2d_branches(seed):
+    """Dimension = 2 on the same block: the 2D Z tables (gradient and Laplacian), the
+    2-dimensional coefficients of the Laplacian, PND, gradient and temperature terms."""
+    sc = scenes.random_block(9, seed=seed)
+    sc.param.Dimension = 2
+    setup = orc.thermal_scene(sc, seed)
+    so, sr = _run_both(sc, ["calc_stl_distance", "calc_explicitly", "calc_temperature_factor"], setup)
+    _compare(so, sr)
+    for f in FIELDS_HEAT:
+        assert bits_equal(getattr(so, f), getattr(sr, f)), f
+    for lib, st in ((ORC, so), (REF, sr)):
+        b = st.bindings()
+        orc.ref_topology(lib, st, b)
+        assert lib.calc_stl_distance(C.byref(b), st.n) == 0
+        assert lib.calc_explicit_pressure(C.byref(b), st.n) == 0
+        assert lib.calc_explicit_pressure_gradient(C.byref(b), st.n) == 0
+    _compare(so, sr)
+    assert np.abs(so.out_pressure[:so.n]).max() > 0
+
+
 def test_drag_kernel():
     sc = scenes.rotating_bucket(l0=0.02, n_drag=6, drag_index=5.0)
     sc.vel = np.random.default_rng(5).normal(0, 0.2, sc.pos.shape)
