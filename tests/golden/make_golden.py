@@ -44,6 +44,35 @@ def explicit_step(lib, scene):
     return after_predictor, final
 
 
+HEAT_FIELDS = OUT_FIELDS + ["temperature", "out_temperature", "out_kin_visc", "turb_visc", "strain"]
+
+
+def thermal_turbulent_step(lib, scene, temps):
+    """Wall distance, the temperature operator, the Smagorinsky viscosity and the
+    turbulent predictor (CalcTemperatureFactor, CalcTurbulenceViscosity, CalcExplicitly)
+    from the initial temperatures `temps` (original order)."""
+    st = orc.RefState(scene)
+    st.out_temperature[:st.n] = temps
+    b = st.bindings()
+    orc.ref_topology(lib, st, b)
+    lib.reset_triangle_topology(st.cells_n, orc.ptr(st.cells))
+    lib.register_triangle_topology(C.byref(b), orc.ptr(st.triangles), st.t, orc.ptr(st.cells), st.cells_n)
+    lib.calc_stl_distance(C.byref(b), st.n)
+    lib.calc_temperature_factor(C.byref(b), st.n)
+    lib.calc_turbulence_viscosity(C.byref(b), st.n)
+    lib.calc_explicitly(C.byref(b), st.n)
+    return {f: getattr(st, f).copy() for f in HEAT_FIELDS}
+
+
+def thermal_turbulent_scene():
+    sc = scenes.random_block(9, seed=5)
+    hook = orc.thermal_scene(sc, 5)
+    orc.turbulent_scene(sc, 5)
+    probe = orc.RefState(sc)
+    hook(probe)
+    return sc, probe.out_temperature[:probe.n].copy()
+
+
 def golden_scenes():
     s1 = scenes.random_block(8, seed=11)
     s2 = scenes.rotating_bucket(l0=0.025, n_drag=4, drag_index=5.0)
@@ -116,6 +145,11 @@ def main():
         arrays.update({f"final_{k}": v for k, v in final.items()})
         np.savez_compressed(os.path.join(HERE, f"ref_explicit_{name}.npz"), **arrays)
     np.savez_compressed(os.path.join(HERE, "ref_math.npz"), **math_cases(ref))
+    sc, temps = thermal_turbulent_scene()
+    arrays = scene_to_arrays(sc)
+    arrays["in_temp"] = temps
+    arrays.update({f"out_{k}": v for k, v in thermal_turbulent_step(ref, sc, temps).items()})
+    np.savez_compressed(os.path.join(HERE, "ref_thermal_turbulent.npz"), **arrays)
     print("written")
 
 

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import orc
-from golden.make_golden import explicit_step, math_cases, scene_from_arrays
+from golden.make_golden import explicit_step, math_cases, scene_from_arrays, thermal_turbulent_step
 
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -21,6 +21,15 @@ def test_explicit_step_matches_reference_golden(name):
         for k, v in arrays.items():
             ref = g[f"{stage}_{k}"]
             assert v.tobytes() == ref.tobytes(), f"{stage}_{k}"
+
+
+def test_thermal_turbulent_step_matches_reference_golden():
+    """Temperature operator, Smagorinsky viscosity and the turbulent predictor."""
+    g = np.load(os.path.join(GOLD, "ref_thermal_turbulent.npz"))
+    mine = thermal_turbulent_step(orc.oracle(), scene_from_arrays(g), g["in_temp"])
+    for k, v in mine.items():
+        assert v.tobytes() == g[f"out_{k}"].tobytes(), k
+    assert (g["out_turb_visc"] > 0).any() and (g["out_out_temperature"] != g["in_temp"][0]).any()
 
 
 def test_math_matches_reference_golden():
