@@ -53,14 +53,15 @@ def test_hash_sort_cells_reorder(n_side, seed):
                                    "kin_visc", "type"])
 
 
+@pytest.mark.parametrize("entry", ["SortUsingThrust", "StableSortUsingThrust"])
 @pytest.mark.parametrize("n,lo,hi", [(1, 0, 5), (2, 3, 3), (1000, -50, 50), (70000, 0, 1 << 17),
                                      (300000, -(1 << 30), 1 << 30), (65536, 7, 7), (4097, 0, 255)])
-def test_radix_sort_is_stable_sort(n, lo, hi):
+def test_radix_sort_is_stable_sort(n, lo, hi, entry):
     rng = np.random.default_rng(n)
     keys = rng.integers(lo, hi + 1, size=n, dtype=np.int64).astype(np.int32)
     vals = np.arange(n, dtype=np.int32)
     dk, dv = DeviceArray.from_host(keys), DeviceArray.from_host(vals)
-    call("SortUsingThrust", n, dk.ptr, dv.ptr)
+    call(entry, n, dk.ptr, dv.ptr)
     order = np.argsort(keys, kind="stable")
     assert np.array_equal(dk.download(), keys[order])
     assert np.array_equal(dv.download(), vals[order])
