@@ -516,6 +516,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(int M, const flo
                      : "memory");
     }
     if (warp == 0) {
+        __syncwarp();   // .aligned: the whole warp, converged (thread 0 just left its branch)
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
                      "r"(kTcTmemCols)
                      : "memory");
@@ -609,6 +610,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(int M, const flo
             }
             phase ^= 1u;
             tc_fence_after();
+            __syncwarp();   // the tcgen05.ld below are .aligned (the polls above diverge)
             if (layer < 3) {
                 tc_epilogue_hidden(tmem_row, bs + layer * H, As, r);
             } else {
@@ -623,6 +625,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(int M, const flo
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
+        __syncwarp();
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
     }
