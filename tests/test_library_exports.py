@@ -66,3 +66,17 @@ def test_default_options_through_the_python_mirror(so):
     assert o.preconditioner == 1 and o.mg_omega == 1.3 and o.compress_rows == 1 and o.mg_sweeps == 1
     assert o.matrix_free == 0 and o.spmv_stream == 1 and o.inner_weights == 16 and o.spmv_wide == 0
     assert o.warm_start == -1
+
+
+@pytest.mark.parametrize("bad", [{"matrix_free": 3}, {"spmv_stream": 2}, {"inner_weights": 8}, {"spmv_wide": 2},
+                                 {"warm_start": 3}, {"warm_start": -2}])
+def test_invalid_solver_options_are_rejected_before_any_device_work(so, bad):
+    """mps_solver_create checks its options before it touches the device: an invalid
+    value returns CCT_PARAMERR (2) and no solver, with or without a GPU."""
+    from simulation_project_gb300 import scenes
+    from simulation_project_gb300.solver import default_options, _lib
+    sc = scenes.random_block(4)
+    o = default_options(**bad)
+    h = C.c_void_p()
+    rc = _lib().mps_solver_create(C.byref(sc.param), C.byref(sc.box), sc.n, C.byref(o), C.byref(h))
+    assert rc == 2 and not h.value
