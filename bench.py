@@ -27,8 +27,9 @@ accuracy    = the FP32-IR solver against the FP64 solver on the same scene after
 cpu_baseline= the FP64 oracle solver with OpenMP on the host cores, on a bounded
               sample (the same bucket at l0 = 0.004, ~1e5 particles, 1 step).
 --impl reference: the reference's own explicit-schedule kernels compiled for the CPU
-              (oracle/_ref/libref.so, OpenMP over particles), timed on the same
-              bucket at l0 = 0.004 (a bounded sample), per step.
+              (oracle/_ref/libref.so, OpenMP over particles), timed per step on the
+              same scene as the GPU arm (the reference has no PPE solver: its scheme
+              is the explicit equation-of-state pressure).
 Multi-GPU: replicas only (each rank runs its own scene; value = sum over ranks).
 """
 import argparse
@@ -349,10 +350,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic (seeded jittered lattice in a triangulated rotating cylinder)",
-        "config": {"workload": WORKLOADS[args.workload].format(l0=args.l0),
-                   "particles": n, "triangles": scene.t, "cells": scene.box.cell_num,
-                   "l2": "inputs larger than L2 (neighbour rows ~8 B x nnz per SpMV)",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "config": gpu_config(args, scene, world),
         "plain_fp64": {"value": pps_plain, "ms_per_step": ms_plain / args.steps,
                        "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_plain])),
                        "relres_max": float(max(s["cg_relres"] for s in st_plain))},
@@ -682,8 +680,17 @@ def cpu_baseline(args):
             "sample": f"FP64 oracle PPE step (OpenMP) on the bucket at l0=0.004 ({sc.n} particles), 1 step"}
 
 
+def gpu_config(args, scene, world=1):
+    """The `config` object of a bench line (the same for both arms)."""
+    return {"workload": WORKLOADS[args.workload].format(l0=args.l0),
+            "particles": scene.n, "triangles": scene.t, "cells": scene.box.cell_num,
+            "l2": "inputs larger than L2 (neighbour rows ~8 B x nnz per SpMV)",
+            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
+
+
 def run_reference(args):
-    """The reference's explicit-schedule kernels compiled for the CPU (oracle/_ref)."""
+    """The reference's explicit-schedule kernels compiled for the CPU (oracle/_ref), on
+    the same scene as the GPU arm."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import orc
@@ -692,7 +699,8 @@ def run_reference(args):
     if ref is None:
         ref = orc.oracle()
         kind = "port"
-    sc = build_scene(0.004)
+    sc = build_scene(args.l0, workload=args.workload)
+    config = gpu_config(args, sc)
     sc.param.bExplicitPressure = True
     sc.param.SonicVelocity = 20.0
     st = orc.RefState(sc)
@@ -727,11 +735,12 @@ def run_reference(args):
             "PPE residual", "value": v, "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "rotating bucket r=0.15 L=0.3, 35% fill, 30 rpm, 4096 wall + 64 drag-sphere STL "
-                                   "models; bounded sample at l0=0.004", "particles": st.n},
+            "config": config,
+            "reference_scheme": "the reference's only pressure scheme: explicit (equation of state), no PPE solve; "
+                                "its kernels compiled for the host CPU, OpenMP over particles",
             "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": _threads(), "kind": kind,
                              "sample": f"reference explicit schedule (EOS pressure, its own kernels on the CPU) "
-                                       f"on the bucket at l0=0.004 ({st.n} particles) per step"},
+                                       f"on the GPU arm's scene ({st.n} particles), every step of the run"},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -77,8 +77,10 @@ CCTStatusType StableSortUsingThrust(Integer MaxParticleNum, Integer* daNumberHas
  * device memory (an allocator hook, a pre-reserved memory pool, a real-time path):
  * same result, but its scratch is one static __device__ array of about 2.1 MiB held by
  * every GPU that loads the library.  At most 262,144 keys (more: CCT_PARAMERR, arrays
- * untouched).  The first call on a device looks up the array's address; make it before
- * any stream capture.  Calls share the array: calls that overlap on the GPU race. */
+ * untouched).  Every call looks up the array's device address on the current device
+ * (nothing cached, so a device reset leaves no stale address); the first call on a device
+ * also loads the library's module there: make it before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race. */
 CCTStatusType SortUsingThrustNoAlloc(Integer MaxParticleNum, Integer* daNumberHash, Integer* daNumberIndex);
 
 /* one-time binding calls */

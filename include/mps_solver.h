@@ -158,6 +158,14 @@ CCTStatusType mps_solver_debug_ppe(MpsSolver* s, double* pnd, double* diag, doub
  * are held (0..2). */
 CCTStatusType mps_solver_debug_history(MpsSolver* s, float* dph1, float* dph2, unsigned char* inner, int* id,
                                        int* held);
+/* Wall bins of the current triangles (binned first if they moved or changed): for every
+ * list key c = 2 * cell + kind (kind 0 walls, 1 drag bodies) bounds[c] / bounds[2 cells + c]
+ * are the start and end of its entries (-1 / -1: empty), tids the triangle of each entry
+ * (cap entries at most; NULL: not copied), *entries how many there are.  A cell's list
+ * holds the triangles whose cell box, grown by one cell, holds the cell, in increasing
+ * triangle order (the 27-cell candidate set of the cell; CCell lists of
+ * RegisterTriangleTopology, Utility_Inline.h:1745-1855, in the reference). */
+CCTStatusType mps_solver_debug_wall_bins(MpsSolver* s, int* bounds, int* tids, int cap, int* entries);
 /* refinement residual r = b - A p of the current state (FP32_IR solvers; host
  * array of n doubles, may be NULL) and ||r|| / ||b||: variant 0 with FP64
  * products and sums, variant 1 with the double-float kernel the solver uses (rows
@@ -229,11 +237,30 @@ CCTStatusType mps_solver_collect(MpsSolver* s, int on);
  * then the solve from the previous pressure to cg_rtol (positions and velocities are
  * unchanged, the state is re-sorted).  CG: Jacobi preconditioner, no network.  NJPCG:
  * the multilevel preconditioner (FP32_IR) and the learned initial guess when one is
- * installed.  The prototype CalcPoisson of the same tree's DeviceProcess.h:50 (AoS
- * CParticle arrays of an older solver variant, undefined matrix arguments) is not
- * provided. */
+ * installed. */
 CCTStatusType CalculatePressureCG(MpsSolver* s, MpsStepStats* stats);
 CCTStatusType CalculatePressureNJPCG(MpsSolver* s, MpsStepStats* stats);
+/* CalcPoisson: the reserved prototype of the same tree's DeviceProcess.h:50-53
+ * (CalcPoisson(cudaStream_t&, ParticleNum, CParticle*, Scalar* distance, Integer* ID,
+ * TriangleNum, CTriangle*, CDistance*, Scalar* dA, Scalar* dB, Scalar* dX, Scalar* dX0),
+ * declared there but never defined), as a context-handle variant: the particles, walls,
+ * drag bodies and their distances are the solver's, in place of the AoS particle and
+ * wall arguments; the solver's buffers carry the old variant's per-particle A_ii, B, X
+ * and X0 (CGPUCellSet.h:69-81 of that tree).  It solves the PPE of the solver's current
+ * state as CalculatePressureCG does (topology, wall distance, PND and assembly at the
+ * current positions, Jacobi-PCG to cg_rtol at the solver's precision) and writes device
+ * arrays of ParticleNum Scalars indexed by particle ID:
+ *   dA  the PPE diagonal A_ii (0 for particles outside the PPE: free surface, P = 0),
+ *   dB  the right-hand side (0 outside the PPE),
+ *   dX  the solved pressure;
+ * dX0 (may be NULL: the solver's pressure history) is the start of the solve, read by
+ * ID; any of dA, dB, dX may be NULL.  Entries of IDs no particle carries are left as
+ * they are.  Stream (a cudaStream_t, may be NULL): the solve starts after the work
+ * already queued there (which may write dX0); the outputs are complete on return.
+ * CCT_PARAMERR for a particle ID >= ParticleNum, CCT_CALCERR when CG misses cg_rtol
+ * (stats, may be NULL, has the details). */
+CCTStatusType CalcPoisson(void* Stream, MpsSolver* s, Integer ParticleNum, Scalar* dA, Scalar* dB, Scalar* dX,
+                          const Scalar* dX0, MpsStepStats* stats);
 /* switches between MPS_PREC_FP64 and MPS_PREC_FP32_IR for the following steps */
 CCTStatusType mps_set_precision(MpsSolver* s, int precision);
 

@@ -7,7 +7,8 @@ oracle/_ref/libref.so - the reference solver's own kernel header compiled for th
     by oracle/ref_harness.cpp.  Its sources are decoded copies of four files of the
     reference tree (radix/SPVSOLVER/MultiGPUSolver/{DataType.h, Constant.h,
     Utility_Inline.h, DeviceProcess_Kernel.h}; DataType.h is UTF-16 with a BOM) that
-    this script writes to oracle/_ref/src/ when the reference checkout is present.
+    this script writes to oracle/_ref/src/ when the reference checkout is present
+    (at $MPS_REFERENCE_ROOT, by default /root/reference).
     oracle/_ref/ is git-ignored; on a machine without the reference checkout the
     copies already in oracle/_ref/src/ (if any) are compiled, otherwise the reference
     harness is skipped and the pin tests fall back to the committed golden vectors.
@@ -21,7 +22,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = "/root/reference/radix/SPVSOLVER/MultiGPUSolver"
+# checkout of the reference project: MPS_REFERENCE_ROOT, by default /root/reference
+REF_ROOT = os.environ.get("MPS_REFERENCE_ROOT", "/root/reference")
+REF_TREE = os.path.join(REF_ROOT, "radix", "SPVSOLVER", "MultiGPUSolver")
 REF_FILES = ["DataType.h", "Constant.h", "Utility_Inline.h", "DeviceProcess_Kernel.h"]
 CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared"]
 

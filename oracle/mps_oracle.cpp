@@ -509,6 +509,21 @@ int orc_update_triangle_position(OrcBindings* b, int t) {
     return CCT_NOERR;
 }
 
+/* ResetWallPosition_Kernel, DeviceProcess_Kernel.h:690-704: a triangle of a linearly
+ * moving model (LinearMovableOrNot) is copied back whole from the original triangles
+ * every LinearResetInterval steps, at the steps with (step + 1) % interval == 0.  The
+ * reference's modulo is undefined for an interval of 0; here such a model is never
+ * reset (the library does the same). */
+int orc_reset_wall_position(OrcBindings* b, int t, int step, const CTriangle* orig) {
+    for (int id = 0; id < t; ++id) {
+        const CTriangleParameters& tp = b->tri_params[b->triangles[id].ModelIDNumber];
+        if (!tp.LinearMovableOrNot) continue;
+        if (tp.LinearResetInterval == 0) continue;
+        if ((step + 1) % tp.LinearResetInterval == 0) std::memcpy(&b->triangles[id], &orig[id], sizeof(CTriangle));
+    }
+    return CCT_NOERR;
+}
+
 /* RotateTrianglePosition_Kernel, DeviceProcess_Kernel.h:622-689: incremental
  * rotation by the per-step angle about the axis CenterOfRotation ->
  * SecondPointOfRotation, ramped linearly between RotationStartTime and

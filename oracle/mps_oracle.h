@@ -98,6 +98,7 @@ int orc_reset_triangle_topology(int cells, CCell* cell);
 int orc_register_triangle_topology(OrcBindings* b, const CTriangle* tri, int t, CCell* cell, int cells);
 int orc_update_triangle_position(OrcBindings* b, int t);
 int orc_rotate_triangle_position(OrcBindings* b, int t, int step);
+int orc_reset_wall_position(OrcBindings* b, int t, int step, const CTriangle* orig);
 int orc_calc_stl_distance(OrcBindings* b, int n);
 int orc_calc_drag_effect(OrcBindings* b, int n);
 

@@ -239,6 +239,12 @@ int orc_rotate_triangle_position(HarnessBindings* b, int t, int step) {
     return CCT_NOERR;
 }
 
+int orc_reset_wall_position(HarnessBindings* b, int t, int step, const CTriangle* orig) {
+    bind(b);
+    run_items(t, [&] { ResetWallPosition_Kernel(t, step, orig); });
+    return CCT_NOERR;
+}
+
 int orc_calc_stl_distance(HarnessBindings* b, int n) {
     bind(b);
     for (int i = 0; i < n; ++i) b->stl_id[i] = -1;

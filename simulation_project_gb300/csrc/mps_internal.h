@@ -34,6 +34,8 @@ size_t scan_tile_sums_capacity();
 void* scratch_get(int slot, size_t bytes);
 // records "where: CUDA error string" for mps_last_error()
 void note_error(const char* where, cudaError_t e);
+// records a message of the library's own for mps_last_error()
+void note_message(const char* msg);
 
 // Kernel launches issued by this library since load (every launch site is written as
 // MPS_COUNT_LAUNCH k<<<...>>>(...); read by mps_kernel_launches()).

@@ -259,13 +259,17 @@ __device__ __forceinline__ void tri_cell_box(const Dev& d, int t, int& i0, int& 
         k1 = min(k1 + 1, d.box.m_GridSize.z - 1);
     }
 }
-__global__ void k_bin_count(const __grid_constant__ Dev d, unsigned* cnt) {
+// entries of each triangle's (grown) cell box; a box holds at most the grid's cells, so
+// one count fits 32 bits, and the 64-bit total tells the host whether the 32-bit
+// offsets of the scan (and the int entry indices of the sort) can hold them all
+__global__ void k_bin_count(const __grid_constant__ Dev d, unsigned* cnt, unsigned long long* total) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= d.tri_n) return;
     int i0, j0, k0, i1, j1, k1;
     tri_cell_box(d, t, i0, j0, k0, i1, j1, k1);
     const long long c = (long long)max(i1 - i0 + 1, 0) * max(j1 - j0 + 1, 0) * max(k1 - k0 + 1, 0);
-    cnt[t] = (unsigned)min(c, (long long)1 << 20);
+    cnt[t] = (unsigned)c;
+    atomicAdd(total, (unsigned long long)c);
 }
 // warp per triangle: its lanes write the (cell key, triangle) entries of its cell box,
 // entry q = ((i - i0) nj + (j - j0)) nk + (k - k0) at off[t] + q (at most the counted ones)
@@ -1728,6 +1732,34 @@ __global__ void k_warm_start(const __grid_constant__ Dev d, int order) {
     const double p = d.press[i];
     d.pprev[i] = p;
     if (order > 0 && d.inner[i]) d.press[i] = p + warm_increment(d, i, order);
+}
+
+// CalcPoisson's start: p0 of each particle from the caller's ID-indexed array (an ID at
+// or above `cap` sets MPS_ERR_KEY_RANGE and keeps the particle's own pressure)
+__global__ void k_poisson_start(const __grid_constant__ Dev d, int cap, const float* __restrict__ x0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int id = d.id[i];
+    if (id < 0 || id >= cap) {
+        atomicOr(d.err, MPS_ERR_KEY_RANGE);
+        return;
+    }
+    d.press[i] = (double)x0[id];
+}
+// CalcPoisson's outputs, ID-indexed: diagonal and right-hand side of the PPE row (0 for
+// particles outside the PPE: free surface, Dirichlet P = 0) and the solved pressure
+__global__ void k_poisson_out(const __grid_constant__ Dev d, int cap, float* a, float* b, float* x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const int id = d.id[i];
+    if (id < 0 || id >= cap) {
+        atomicOr(d.err, MPS_ERR_KEY_RANGE);
+        return;
+    }
+    const bool in = d.inner[i] != 0;
+    if (a) a[id] = in ? (float)d.diag[i] : 0.f;
+    if (b) b[id] = in ? (float)d.rhs[i] : 0.f;
+    if (x) x[id] = (float)d.press[i];
 }
 
 // after the solve: shift the increment history (P_n - P_{n-1} on interior rows, else 0)

@@ -31,6 +31,7 @@ unsigned long long g_kernel_launches = 0;
 void note_error(const char* where, cudaError_t e) {
     snprintf(g_err, sizeof(g_err), "%s: %s", where, cudaGetErrorString(e));
 }
+void note_message(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
 
 void* scratch_get(int slot, size_t bytes) {
     if (slot < 0 || slot >= kSlots) return nullptr;

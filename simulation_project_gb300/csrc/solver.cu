@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <random>
@@ -108,6 +109,8 @@ struct Solver {
     int* h_int = nullptr;       // pinned small ints
     // wall-bin scratch
     unsigned* bin_off = nullptr;
+    size_t bin_off_cap = 0;
+    int bin_entries = 0;   // (cell, triangle) entries of the last binning
     int* bin_visit = nullptr;
     size_t bin_visit_cap = 0;
     void* bin_sort = nullptr;
@@ -545,12 +548,33 @@ struct Solver {
     CCTStatusType bin_walls() {
         const int t = d.tri_n;
         if (t <= 0) return CCT_NOERR;
-        if (!bin_off && cudaMalloc(&bin_off, sizeof(unsigned) * ((size_t)t + 2))) return CCT_MEMERR;
-        MPS_COUNT_LAUNCH k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off);
+        // counts (t + 1 with the scan's total) and the 64-bit sum of the counts behind them
+        if ((size_t)t > bin_off_cap) {   // sized for the largest wall set seen
+            if (bin_off) cudaFree(bin_off);
+            bin_off = nullptr;
+            bin_off_cap = 0;
+            if (cudaMalloc(&bin_off, sizeof(unsigned) * ((size_t)t + 2) + sizeof(unsigned long long) * 2))
+                return CCT_MEMERR;
+            bin_off_cap = (size_t)t;
+        }
+        unsigned long long* total = (unsigned long long*)(bin_off + ((size_t)t + 3) / 2 * 2);
+        cudaMemsetAsync(total, 0, sizeof(unsigned long long), st);
+        MPS_COUNT_LAUNCH k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, total);
+        cudaMemcpyAsync(h_int + 4, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
+        unsigned long long total_h = 0;
+        std::memcpy(&total_h, h_int + 4, sizeof(total_h));
+        // every (cell, triangle) entry is indexed by an int in the sort and by the 32-bit
+        // scan: a wall whose boxes hold more entries is refused, never truncated
+        if (total_h > (unsigned long long)INT32_MAX) {
+            note_message("wall bins: the triangles' cell boxes hold more than 2^31 - 1 (cell, triangle) entries");
+            return CCT_MEMERR;
+        }
         scan_exclusive(bin_off, t + 1, nullptr, st, scan_sums);
         cudaMemcpyAsync(h_int, bin_off + t, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
         const unsigned nv = (unsigned)h_int[0];
+        bin_entries = (int)nv;
         if (nv == 0) {
             cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, st);
             bins_dirty = 0;
@@ -559,7 +583,7 @@ struct Solver {
         if (nv > bin_visit_cap) {
             if (bin_visit) cudaFree(bin_visit);
             if (bin_sort) cudaFree(bin_sort);
-            bin_visit_cap = nv + nv / 2;
+            bin_visit_cap = std::min<size_t>((size_t)nv + nv / 2, (size_t)INT32_MAX);
             if (cudaMalloc(&bin_visit, sizeof(int) * 2 * bin_visit_cap)) return CCT_MEMERR;
             bin_sort_bytes = radix_scratch_bytes((int)bin_visit_cap);
             if (cudaMalloc(&bin_sort, bin_sort_bytes)) return CCT_MEMERR;
@@ -1381,6 +1405,30 @@ CCTStatusType mps_solver_debug_history(MpsSolver* s, float* dph1, float* dph2, u
     return mps::cuda_status(e);
 }
 
+CCTStatusType mps_solver_debug_wall_bins(MpsSolver* s, int* bounds, int* tids, int cap, int* entries) {
+    if (!s || !entries) return CCT_PARAMERR;
+    mps::Solver& S = s->s;
+    mps::Dev& d = S.d;
+    *entries = 0;
+    if (d.tri_n <= 0) return CCT_NOERR;
+    if (S.bins_dirty) {
+        const CCTStatusType rc = S.bin_walls();
+        if (rc != CCT_NOERR) return rc;
+    }
+    if (cudaStreamSynchronize(S.st)) return CCT_CUDAERR;
+    const int nv = S.bin_entries;
+    *entries = nv;
+    if (bounds) {
+        const cudaError_t e = cudaMemcpy(bounds, d.tcs, sizeof(int) * 4 * (size_t)d.cells, cudaMemcpyDeviceToHost);
+        if (e) return CCT_CUDAERR;
+    }
+    if (tids && nv > 0) {
+        if (cap < nv) return CCT_PARAMERR;
+        if (cudaMemcpy(tids, d.tids, sizeof(int) * (size_t)nv, cudaMemcpyDeviceToHost)) return CCT_CUDAERR;
+    }
+    return CCT_NOERR;
+}
+
 CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_r, double* relres) {
     if (!s) return CCT_PARAMERR;
     mps::Solver& S = s->s;
@@ -1539,6 +1587,45 @@ CCTStatusType CalculatePressureNJPCG(MpsSolver* s, MpsStepStats* stats) {
     if (!s) return CCT_PARAMERR;
     const Solver& v = s->s;
     return pressure_solve(s, stats, MPS_PRECOND_MULTILEVEL, v.learned_ready ? (v.opt.learned ? v.opt.learned : 1) : 0);
+}
+
+CCTStatusType CalcPoisson(void* Stream, MpsSolver* s, Integer ParticleNum, Scalar* dA, Scalar* dB, Scalar* dX,
+                          const Scalar* dX0, MpsStepStats* stats) {
+    if (!s || ParticleNum < 0) return CCT_PARAMERR;
+    Solver& v = s->s;
+    if (v.opt.pressure_mode != MPS_PRESSURE_PPE) return CCT_PARAMERR;
+    if (v.d.n > 0 && ParticleNum == 0) return CCT_PARAMERR;
+    // the solve follows the caller's earlier work on Stream (it may have written dX0)
+    if (Stream) {
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) return CCT_CUDAERR;
+        cudaError_t e = cudaEventRecord(ev, (cudaStream_t)Stream);
+        if (!e) e = cudaStreamWaitEvent(v.st, ev, 0);
+        cudaEventDestroy(ev);
+        if (e) return CCT_CUDAERR;
+    }
+    if (dX0 && v.d.n > 0) {
+        MPS_COUNT_LAUNCH mps::k_poisson_start<<<mps::blocks_for(v.d.n), mps::kBlock, 0, v.st>>>(v.d, ParticleNum, dX0);
+        v.hist = 0;   // the start replaces the pressure history
+    }
+    MpsStepStats st{};
+    CCTStatusType rc = pressure_solve(s, &st, MPS_PRECOND_JACOBI, 0);
+    if (rc != CCT_NOERR) return rc;
+    if (dX0) v.hist = 0;
+    if (v.d.n > 0) {
+        cudaMemsetAsync(v.d.err, 0, sizeof(unsigned), v.st);
+        MPS_COUNT_LAUNCH mps::k_poisson_out<<<mps::blocks_for(v.d.n), mps::kBlock, 0, v.st>>>(v.d, ParticleNum, dA, dB,
+                                                                                              dX);
+        cudaMemcpyAsync(v.h_int, v.d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, v.st);
+        if (cudaStreamSynchronize(v.st)) return CCT_CUDAERR;
+        st.error_flags |= (unsigned)v.h_int[0];
+    }
+    if (stats) *stats = st;
+    if (st.error_flags & MPS_ERR_KEY_RANGE) {
+        mps::note_message("CalcPoisson: a particle ID lies at or above ParticleNum");
+        return CCT_PARAMERR;
+    }
+    return (st.error_flags & MPS_ERR_CG) ? CCT_CALCERR : CCT_NOERR;
 }
 
 CCTStatusType mps_set_precision(MpsSolver* s, int precision) {

@@ -13,9 +13,12 @@
 //     (mps_last_error() says why) without touching the arrays;
 //   * the array (2,232,864 bytes, about 2.1 MiB) lives in every GPU that loads the
 //     library, until the process exits;
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, with that device current); make that first
-//     call before any stream capture;
+//   * every call looks up the array's device address on the current device with
+//     cudaGetSymbolAddress (no allocation; nothing is cached, so a device reset or a
+//     re-created context cannot leave a stale address behind, and concurrent first
+//     calls from several host threads share no unsynchronised state); the first call
+//     on a device also makes the runtime load the library's module there, so make that
+//     first call before any stream capture;
 //   * every call shares the array, and it keeps the last call's contents: the sort
 //     writes each scratch word before it reads it (min/max re-initialised, histograms
 //     fully rewritten per pass), so nothing is stale -- but calls that overlap on the
@@ -38,28 +41,17 @@ constexpr size_t kNoAllocBytes = kNoAllocHeader + kNoAllocSortBytes;
 
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
-void* g_noalloc_addr[kMaxDevices];
-
-// device address of the array for the current device (looked up once per device)
+// device address of the array on the current device, looked up on every call: the
+// host-side symbol g_noalloc_scratch is only a stand-in for it and must never reach a
+// kernel
 CCTStatusType noalloc_scratch(void** out) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        note_error("SortUsingThrustNoAlloc: cudaGetDevice", e);
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        note_error("SortUsingThrustNoAlloc: cudaGetSymbolAddress", e);
         return CCT_CUDAERR;
     }
-    if (dev < 0 || dev >= kMaxDevices) return CCT_PARAMERR;
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            note_error("SortUsingThrustNoAlloc: cudaGetSymbolAddress", e);
-            return CCT_CUDAERR;
-        }
-        g_noalloc_addr[dev] = p;
-    }
-    *out = g_noalloc_addr[dev];
+    *out = p;
     return CCT_NOERR;
 }
 

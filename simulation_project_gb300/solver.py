@@ -66,6 +66,7 @@ _SIGS = {
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
     "mps_solver_debug_history": (C.c_int, [P, P, P, P, P, P]),
     "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
+    "mps_solver_debug_wall_bins": (C.c_int, [P, P, P, C.c_int, C.POINTER(C.c_int)]),
     "mps_solver_save_frame": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, P, P]),
     "mps_solver_add_particles": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_int)]),
     "mps_solver_set_time_step": (C.c_int, [P, C.c_double, C.c_double]),
@@ -79,6 +80,7 @@ _SIGS = {
     "CalculatePressureCG": (C.c_int, [P, C.POINTER(MpsStepStats)]),
     "CalculatePressureNJPCG": (C.c_int, [P, C.POINTER(MpsStepStats)]),
     "mps_set_precision": (C.c_int, [P, C.c_int]),
+    "CalcPoisson": (C.c_int, [P, P, C.c_int, P, P, P, P, C.POINTER(MpsStepStats)]),
     "mps_learned_train": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_ulonglong,
                                     C.POINTER(MpsLearnedInfo)]),
     "mps_learned_infer": (C.c_int, [P, P, C.POINTER(C.c_int)]),
@@ -229,6 +231,23 @@ class Solver:
         _check(_lib().mps_solver_debug_spmv(self.h, int(kernel), _p(xs), _p(y)), "mps_solver_debug_spmv")
         return y
 
+    def debug_wall_bins(self) -> dict:
+        """Per-cell triangle lists of the wall search: {(cell, kind): [triangle ids]} for
+        the non-empty lists (kind 0 walls, 1 drag bodies)."""
+        L = _lib()
+        cells = int(self.scene.box.cell_num)
+        nv = C.c_int()
+        _check(L.mps_solver_debug_wall_bins(self.h, None, None, 0, C.byref(nv)), "mps_solver_debug_wall_bins")
+        bounds = np.zeros(4 * cells, np.int32)
+        tids = np.zeros(max(nv.value, 1), np.int32)
+        _check(L.mps_solver_debug_wall_bins(self.h, _p(bounds), _p(tids), len(tids), C.byref(nv)),
+               "mps_solver_debug_wall_bins")
+        ts, te = bounds[:2 * cells], bounds[2 * cells:]
+        out = {}
+        for c in np.flatnonzero(ts >= 0):
+            out[(int(c) // 2, int(c) % 2)] = tids[ts[c]:te[c]].tolist()
+        return out
+
     def set_time_step(self, dt, courant=0.0):
         """Dt (and CourantNumber when > 0) from the next step on (a dt schedule row)."""
         _check(_lib().mps_solver_set_time_step(self.h, float(dt), float(courant)), "mps_solver_set_time_step")
@@ -270,6 +289,13 @@ class Solver:
         st = MpsStepStats()
         f = _lib().CalculatePressureNJPCG if njp else _lib().CalculatePressureCG
         _check(f(self.h, C.byref(st)), "CalculatePressure" + ("NJPCG" if njp else "CG"))
+        return st.as_dict()
+
+    def calc_poisson(self, n_ids, d_a, d_b, d_x, d_x0=None, stream=None) -> dict:
+        """CalcPoisson on device arrays of n_ids floats indexed by particle ID (device
+        pointers as ints; any may be None)."""
+        st = MpsStepStats()
+        _check(_lib().CalcPoisson(stream, self.h, int(n_ids), d_a, d_b, d_x, d_x0, C.byref(st)), "CalcPoisson")
         return st.as_dict()
 
     def set_precision(self, precision: str):

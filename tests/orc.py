@@ -63,6 +63,7 @@ _FUNCS = {
     "orc_register_triangle_topology": (C.c_int, [P, P, C.c_int, P, C.c_int]),
     "orc_update_triangle_position": (C.c_int, [P, C.c_int]),
     "orc_rotate_triangle_position": (C.c_int, [P, C.c_int, C.c_int]),
+    "orc_reset_wall_position": (C.c_int, [P, C.c_int, C.c_int, P]),
     "orc_calc_stl_distance": (C.c_int, [P, C.c_int]),
     "orc_calc_drag_effect": (C.c_int, [P, C.c_int]),
     "orc_calc_explicitly": (C.c_int, [P, C.c_int]),
@@ -351,3 +352,21 @@ def turbulent_scene(sc, seed):
     p.SmagorinskyConstant, p.FilterWidth = 0.12, 0.02
     p.TurbulanViscosityRatio, p.Cnue, p.Cepsilon, p.TurbulanceIntensity = 2e-5, 0.094, 1.048, 0.5
     sc.vel = np.random.default_rng(seed + 7).normal(0, 0.5, sc.pos.shape)
+
+
+def linear_walls_scene(seed=0):
+    """A block whose box walls are split over three models: model 0 fixed, models 1
+    and 2 moving linearly (LinearMovableOrNot) with reset intervals 3 and 5; for
+    ResetWallPosition (DeviceProcess_Kernel.h:690-704)."""
+    from simulation_project_gb300 import scenes
+    sc = scenes.random_block(6, seed=seed)
+    rng = np.random.default_rng(seed)
+    sc.tri_model = rng.integers(0, 3, size=sc.t).astype(np.int32)
+    tps = [scenes._tri_normal_params(dt=sc.param.Dt) for _ in range(3)]
+    for m, (vel, interval) in ((1, ((0.3, -0.1, 0.05), 3)), (2, ((-0.2, 0.0, 0.4), 5))):
+        tps[m].Velocity = Scalar3(*vel)
+        tps[m].LinearMovableOrNot = True
+        tps[m].LinearResetInterval = interval
+    tps[0].LinearResetInterval = 2   # not movable: never reset
+    sc.tri_params = tps
+    return sc

@@ -1,0 +1,146 @@
+"""Parity at the benchmark configurations, not only on small scenes.
+
+* Config 1: the full dam break (0.2 x 0.2 x 0.4 m column at l0 = 0.01, 16,000
+  particles, 12-triangle tank) and config 2: the rotating bucket at l0 = 0.004
+  (108,186 particles, 4096-triangle cylinder, 64 drag spheres of radius 3 l0, 30 rpm),
+  both in FP64 against the FP64 oracle solver for 10 steps: identical Laplacian
+  neighbour sets (count and id checksum per particle), pressure within 1e-6 (max-norm,
+  relative to max |P|), positions within 1e-6 l0.
+* Config 2 with FP32 operators inside FP64 refinement against the same FP64 oracle
+  after 10 steps: pressure within 2e-3 (max-norm relative), PND 1e-5 relative, velocity
+  2e-3 of the largest speed, kinetic energy 1e-4 relative, positions 1e-4 l0; the
+  measured errors are printed.
+* The reference-named explicit schedule (CalcSTLDistance, CalcDragEffect,
+  CalcExplicitly, then CalcExplicitPressure and CalcExplicitPressureGradient on the
+  predicted positions) on the config-2 scene, bit-identical to the oracle, and the
+  oracle bit-identical to the reference's own kernel code compiled for the CPU where
+  its sources are present.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import orc
+from simulation_project_gb300 import scenes
+from simulation_project_gb300.solver import Solver
+
+pytestmark = pytest.mark.gpu
+STEPS = 10
+
+
+def _run_pair(sc, precision, steps=STEPS, **opts):
+    o = orc.OracleSim(sc)
+    g = Solver(sc, precision=precision, **opts)
+    for i in range(steps):
+        rc, ost = o.step(i)
+        st = g.step(i)
+        assert rc == 0 and st["error_flags"] == 0, (i, st)
+        assert st["cg_relres"] <= 1e-8 and ost["cg_relres"] <= 1e-8, (i, st, ost)
+    return o, g
+
+
+def _fp64_bar(sc, o, g):
+    gp = g.debug_ppe()
+    og = np.argsort(gp["id"], kind="stable")
+    on = o.neighbours()
+    assert np.array_equal(gp["id"][og], on["id"])
+    assert np.array_equal(gp["nbr_count"][og], on["nbr_count"])
+    assert np.array_equal(gp["nbr_idsum"][og], on["nbr_idsum"])
+    a, b = g.state(), o.state()
+    assert np.array_equal(a["id"], b["id"])
+    pmax = np.abs(b["press"]).max()
+    assert pmax > 0
+    err_p = np.abs(a["press"] - b["press"]).max() / pmax
+    err_x = np.abs(a["pos"] - b["pos"]).max() / sc.param.InitialParticleDistance
+    print(f"\n{sc.name} n={sc.n} FP64 after {STEPS} steps: pressure {err_p:.2e}, positions {err_x:.2e} l0")
+    assert err_p <= 1e-6, err_p
+    assert err_x <= 1e-6, err_x
+
+
+def test_config1_dam_break_fp64_ten_steps():
+    sc = scenes.dam_break(l0=0.01, seed=1)
+    assert sc.n == 16000 and sc.t == 12
+    o, g = _run_pair(sc, "fp64")
+    _fp64_bar(sc, o, g)
+    g.close()
+    o.close()
+
+
+def _bucket():
+    sc = scenes.rotating_bucket(l0=0.004, seed=2)
+    assert sc.n > 100_000 and len(sc.drag) == 1
+    assert int((sc.tri_model == 0).sum()) == 4096 and int((sc.tri_model == 1).sum()) == 64 * 80
+    return sc
+
+
+def test_config2_bucket_fp64_ten_steps():
+    sc = _bucket()
+    o, g = _run_pair(sc, "fp64")
+    _fp64_bar(sc, o, g)
+    np.testing.assert_allclose(g.triangles().reshape(-1, 9), _oracle_triangles(o, sc), rtol=0, atol=1e-12)
+    g.close()
+    o.close()
+
+
+def _oracle_triangles(o, sc):
+    v = np.zeros((sc.t, 9))
+    o.lib.sim_get_triangles(o.h, orc.ptr(v))
+    return v
+
+
+def test_config2_bucket_fp32_ir_against_fp64_oracle():
+    sc = _bucket()
+    o, g = _run_pair(sc, "fp32_ir")
+    a, b = g.state(), o.state()
+    assert np.array_equal(a["id"], b["id"])
+    l0 = sc.param.InitialParticleDistance
+    err = {
+        "pressure": np.abs(a["press"] - b["press"]).max() / np.abs(b["press"]).max(),
+        "pressure_rms": np.sqrt(np.mean((a["press"] - b["press"]) ** 2)) / np.sqrt(np.mean(b["press"] ** 2)),
+        "pnd": np.abs(a["pnd"] - b["pnd"]).max() / np.abs(b["pnd"]).max(),
+        "velocity": np.abs(a["vel"] - b["vel"]).max() / np.abs(b["vel"]).max(),
+        "kinetic_energy": abs((a["vel"] ** 2).sum() - (b["vel"] ** 2).sum()) / (b["vel"] ** 2).sum(),
+        "position_l0": np.abs(a["pos"] - b["pos"]).max() / l0,
+    }
+    print(f"\nconfig 2 FP32-IR vs FP64 oracle after {STEPS} steps: " +
+          ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
+    assert err["pressure"] <= 2e-3, err
+    assert err["pnd"] <= 1e-5, err
+    assert err["velocity"] <= 2e-3, err
+    assert err["kinetic_energy"] <= 1e-4, err
+    assert err["position_l0"] <= 1e-4, err
+    g.close()
+    o.close()
+
+
+def test_config2_reference_named_explicit_step_bit_exact():
+    from test_gpu_reference_path import _explicit_pipeline
+    sc = _bucket()
+    sc.vel = np.random.default_rng(5).normal(0, 0.05, sc.pos.shape)
+    st = _explicit_pipeline(sc, with_drag=True)
+    n = st.n
+    assert np.abs(st.out_pressure[:n]).max() > 0
+    assert (st.stl_id[:n] >= 0).sum() > n // 10
+    assert (np.abs(st.drag_acc[:n]).sum(1) > 0).any()
+    ref = orc.reference()
+    if ref is None:
+        return
+    # one step of the same schedule by the reference's own kernel code on the CPU
+    ORC = orc.oracle()
+    so = orc.RefState(sc)
+    sr = so.copy()
+    for lib, s in ((ORC, so), (ref, sr)):
+        b = s.bindings()
+        orc.ref_topology(lib, s, b)
+        lib.reset_triangle_topology(s.cells_n, orc.ptr(s.cells))
+        lib.register_triangle_topology(C.byref(b), orc.ptr(s.triangles), s.t, orc.ptr(s.cells), s.cells_n)
+        for fn in ("calc_stl_distance", "calc_drag_effect", "calc_explicitly"):
+            assert getattr(lib, fn)(C.byref(b), s.n) == 0
+        b = s.bindings()
+        orc.ref_topology(lib, s, b)
+        for fn in ("calc_stl_distance", "calc_explicit_pressure", "calc_explicit_pressure_gradient"):
+            assert getattr(lib, fn)(C.byref(b), s.n) == 0
+    for f in ("out_pos", "out_vel", "out_pressure", "out_density", "stl_distance", "stl_id", "drag_acc", "cells"):
+        assert getattr(so, f).tobytes() == getattr(sr, f).tobytes(), f
+        assert getattr(so, f).tobytes() == getattr(st, f).tobytes(), f

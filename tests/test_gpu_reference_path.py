@@ -152,6 +152,26 @@ def test_triangle_motion_close():
     np.testing.assert_allclose(got["Vertex"], st.triangles["Vertex"], rtol=0, atol=2e-6)
 
 
+def test_linear_wall_reset_bit_exact():
+    """UpdateTrianglePosition + ResetWallPosition (DeviceProcess_Kernel.h:603-621,
+    690-704) over 17 steps: the triangles equal the oracle's bit for bit."""
+    sc = orc.linear_walls_scene(seed=4)
+    st = orc.RefState(sc)
+    orig = st.triangles.copy()
+    g = _gpu().GpuRef(st)
+    d_orig = DeviceArray.from_host(orig)
+    b = st.bindings()
+    for step in range(17):
+        ORC.update_triangle_position(C.byref(b), st.t)
+        ORC.reset_wall_position(C.byref(b), st.t, step, orc.ptr(orig))
+        assert call("UpdateTrianglePosition", g.stream.ref(), st.t, g.p("triangles")) == 0
+        assert call("ResetWallPosition", g.stream.ref(), st.t, step, d_orig.ptr) == 0
+    g.stream.sync()
+    got = g.download()["triangles"]
+    assert got.tobytes() == st.triangles.tobytes()
+    assert got.tobytes() != orig.tobytes()
+
+
 def test_unsupported_features_report_paramerr():
     sc = scenes.random_block(4)
     sc.param.bNegativePressure = True

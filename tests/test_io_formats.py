@@ -12,7 +12,9 @@ from simulation_project_gb300 import build
 from simulation_project_gb300.types import CParameter, CGridBox, CBox, Scalar3, CTriangle, CParticle_size
 from simulation_project_gb300 import scenes
 
-TD = "/root/reference/solver/TESTDATA/velocity simulation in evaporator and heater.zip"
+# input deck of the reference checkout ($MPS_REFERENCE_ROOT, by default /root/reference)
+REF_ROOT = os.environ.get("MPS_REFERENCE_ROOT", "/root/reference")
+TD = os.path.join(REF_ROOT, "solver", "TESTDATA", "velocity simulation in evaporator and heater.zip")
 
 
 @pytest.fixture(scope="module")

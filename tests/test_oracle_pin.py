@@ -182,6 +182,29 @@ def test_triangle_motion():
     assert np.abs(so.triangles["Vertex"] - orc.RefState(sc).triangles["Vertex"]).max() > 1e-3
 
 
+def test_linear_wall_reset():
+    """UpdateTrianglePosition each step, then ResetWallPosition: movable models return
+    to the original triangles at the steps with (step + 1) % interval == 0."""
+    sc = orc.linear_walls_scene(seed=4)
+    so = orc.RefState(sc)
+    sr = so.copy()
+    orig = so.triangles.copy()
+    resets = 0
+    for lib, st in ((ORC, so), (REF, sr)):
+        b = st.bindings()
+        for step in range(17):
+            assert lib.update_triangle_position(C.byref(b), st.t) == 0
+            assert lib.reset_wall_position(C.byref(b), st.t, step, orc.ptr(orig)) == 0
+            if lib is ORC:
+                resets += int(((step + 1) % 3 == 0) or ((step + 1) % 5 == 0))
+    assert bits_equal(so.triangles, sr.triangles)
+    # model 0 moved with velocity 0: unchanged; models 1 and 2 moved since their last reset
+    m = so.triangles["ModelIDNumber"][:so.t]
+    assert bits_equal(so.triangles[:so.t][m == 0], orig[:so.t][m == 0])
+    assert (so.triangles["Vertex"][:so.t][m == 1] != orig["Vertex"][:so.t][m == 1]).any()
+    assert resets > 0
+
+
 FIELDS_HEAT = ["out_id", "out_temperature", "out_kin_visc", "temperature", "stl_distance", "stl_id", "drag_acc",
                "out_solid_rate"]
 FIELDS_TURB = ["turb_visc", "strain", "out_id", "out_pos", "out_vel", "pressure"]
