@@ -12,7 +12,9 @@ value       = particle-steps/s of the FP32-operator / FP64-refined solver with t
               multilevel preconditioner and the learned initial guess (trained on the
               GPU by the library's own BF16 tensor-core kernels before the timed
               region), states resident in HBM;
-plain_fp64  = the same steps with every operator and Jacobi-PCG in FP64;
+plain_fp64  = the same steps with every operator and Jacobi-PCG in FP64 (its CG SpMV
+              streamed as the FP32 one, over FP64 weights), with the roofline of
+              that SpMV;
 e2e         = the learned solver driven through the public C-ABI from pinned host
               buffers: each step uploads the state, steps, and downloads it.
 roofline    = the PPE SpMV (the dominant kernel) timed with CUDA events on the solver
@@ -243,6 +245,7 @@ def run_gpu(args):
     ms_plain, _, st_plain = time_steps(plain, args.steps, args.warmup)
     plain.close()
     pps_plain = n * args.steps / (ms_plain / 1e3)
+    plain_roof = plain_fp64_roofline(scene, args, peak_gbs)
 
     # FP32 / FP64-refined solver without the network: Jacobi, then multilevel
     ir = Solver(scene, precision="fp32_ir", profile=0, preconditioner=0)
@@ -353,7 +356,8 @@ def run_gpu(args):
         "config": gpu_config(args, scene, world),
         "plain_fp64": {"value": pps_plain, "ms_per_step": ms_plain / args.steps,
                        "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_plain])),
-                       "relres_max": float(max(s["cg_relres"] for s in st_plain))},
+                       "relres_max": float(max(s["cg_relres"] for s in st_plain)),
+                       "roofline": plain_roof},
         "speedup_vs_plain_fp64": pps_fast / pps_plain,
         "fp32_ir_jacobi_without_network": {"value": pps_ir, "ms_per_step": ms_ir / args.steps,
                                            "cg_iterations_per_step": float(np.mean([s["cg_iterations"] for s in st_ir])),
@@ -398,6 +402,36 @@ def run_gpu(args):
     if log:
         result["notes"] = log
     return result
+
+
+def plain_fp64_roofline(scene, args, peak_gbs, steps=3):
+    """Roofline of the plain FP64 solver's CG SpMV (k_spmv_stream64 over 16-bit columns
+    and FP64 weights, or the register walk where no slice fits 16 bits): a separate
+    profiled run of `steps` steps after the warm-up (phase events on the solver stream),
+    so that the timed denominator carries no event overhead.  Algorithmic bytes per
+    launch: 8 B weight + 2 B (16-bit) or 4 B (32-bit) column per neighbour entry, and
+    33 B per interior row (x, y, diagonal: 8 B each; count 4 B; interior flag 1 B)."""
+    from simulation_project_gb300.solver import Solver
+    s = Solver(scene, precision="fp64", profile=1, warm_start=0)
+    _, _, st = time_steps(s, steps, args.warmup)
+    s.close()
+    spmv_ms = sum(x["ms_spmv"] for x in st)
+    its = sum(x["cg_iterations"] for x in st)
+    nnz = float(np.mean([x["nnz"] for x in st]))
+    rows16 = all(x["rows16"] for x in st)
+    nnz_wide = float(np.mean([x["nnz_wide"] for x in st])) if rows16 else nnz
+    interior = float(np.mean([x["interior"] for x in st]))
+    wide = nnz_wide * 2 > nnz
+    bytes_launch = 10.0 * (nnz - nnz_wide) + 12.0 * nnz_wide + 33.0 * interior
+    avg_ms = spmv_ms / max(its, 1)
+    achieved = bytes_launch / (avg_ms / 1e3) / 1e9 if its else 0.0
+    kname = ("k_spmv_stream64<0,8,2,8,4%s> (FP64 CG SpMV, FP64 weights + %s columns streamed by bulk copies)"
+             % ((",true", "32-bit") if wide else ("", "16-bit"))) if rows16 else \
+        "k_spmv<double,double,double,0> (FP64 CG SpMV, register walk)"
+    return {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+            "frac": round(achieved / peak_gbs, 3), "bytes_per_launch": int(bytes_launch), "entries": int(nnz),
+            "entries_32bit_columns": int(nnz_wide), "launches": its, "avg_launch_us": round(avg_ms * 1e3, 2),
+            "fp64_flop_per_launch": int(2 * nnz), "steps_profiled": steps}
 
 
 def mlp_bench(params, n, tflops_peak, reps=20):

@@ -77,9 +77,11 @@ typedef struct MpsSolverOptions {
                                recompute each weight from the FP32 positions the neighbour
                                pass used (same bits), 4 or 8 entries per unrolled group,
                                streaming only the columns */
-    int spmv_stream;        /* FP32 inner SpMV over 16-bit slices: 0 register walk; 1 rows
-                               streamed through shared memory by bulk copies (a ring of 2
-                               stages of 8 entries per warp); same row values */
+    int spmv_stream;        /* SpMV over 16-bit slices: 0 register walk; 1 rows streamed
+                               through shared memory by bulk copies (a ring of 2 stages of
+                               8 entries per warp); same row values.  Both solvers: the
+                               FP32 inner CG, and the FP64 solver's CG products and
+                               residuals over its FP64 weights */
     int inner_weights;      /* 16 (default): the inner CG uses FP16 copies of the FP32 weights
                                with the diagonal recomputed from the rounded weights (a
                                consistent Laplacian within ~5e-4 of the FP32 one; the

@@ -199,15 +199,17 @@ CCTStatusType mps_read_particle_file(const char* path, int* count, CParticle* ou
     return CCT_NOERR;
 }
 
-CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset, int* count, CTriangle* out,
-                           int capacity) {
-    if (!path || !count) return CCT_PARAMERR;
+}  // extern "C"
+
+namespace mps_io {
+// The triangles of one STL file with the file's normals (CSTLSerializer::Load,
+// STLSerializer.cpp:225-357): ASCII when the first token is "solid", else binary.
+CCTStatusType stl_load_raw(const char* path, std::vector<CTriangle>& tris) {
     std::ifstream probe(path);
     if (!probe.is_open()) return CCT_FILEERR;
     std::string first;
     probe >> first;
     probe.close();
-    std::vector<CTriangle> tris;
     if (first == "solid") {
         std::ifstream f(path);
         std::string w;
@@ -251,6 +253,18 @@ CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset
             tris.push_back(T);
         }
     }
+    return CCT_NOERR;
+}
+}  // namespace mps_io
+
+extern "C" {
+
+CCTStatusType mps_read_stl(const char* path, int model_id, const Scalar3* offset, int* count, CTriangle* out,
+                           int capacity) {
+    if (!path || !count) return CCT_PARAMERR;
+    std::vector<CTriangle> tris;
+    const CCTStatusType rc = mps_io::stl_load_raw(path, tris);
+    if (rc != CCT_NOERR) return rc;
     for (auto& T : tris) {
         T.ModelIDNumber = model_id;
         if (offset)

@@ -1355,6 +1355,100 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
     }
 }
 
+// FP64 SpMV of the plain FP64 solver over streamed rows: the columns (16-bit offsets,
+// or 32-bit indices when WIDE) and FP64 weights of each slice reach shared memory by
+// bulk copies as in k_spmv_stream, and every row accumulates its entries in order with
+// one FP64 FMA each, so every row value is bit-identical to the register walk
+// k_spmv<double, double, double, MODE>.  MODE 0: y = A x (CG, S_CONV early exit) and
+// x.y -> S_PQ / S_ALPHA; MODE 1: y = b - A x with ||y||^2 -> S_RR / S_RNORM and ||b||
+// -> S_BNORM.
+template <int MODE, int SC, int SS, int W, int MINB, bool WIDE = false>
+__global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream64(const __grid_constant__ Dev d,
+                                                               const double* __restrict__ w,
+                                                               const double* __restrict__ x, double* __restrict__ y,
+                                                               const double* __restrict__ b, int slot) {
+    static_assert(MODE == 0 || MODE == 1, "CG product or residual");
+    static_assert(SC % 4 == 0, "stages hold whole groups of 4 entries");
+    if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
+    extern __shared__ __align__(128) unsigned char stream_smem[];
+    __shared__ __align__(8) unsigned long long bars[W][SS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
+    SliceRing<SC, SS, double, WIDE> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, double, WIDE>::SB, bars[warp], gw, nw);
+    const double coef = d.c.coef_lap;
+    double part0 = 0.0, part1 = 0.0;
+    for (int sl = gw; sl < R.nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int km = d.skmax[sl];
+        double acc = 0.0;
+        bool done = false;
+        if ((WIDE || km >= 0) && R.streaming) {
+            const int nc = (slice_kmax(km) + SC - 1) / SC;
+            const int r0 = sl * 32;
+            for (int c = 0; c < nc; ++c) {
+                const unsigned char* cs;
+                const double* ws;
+                if (!R.acquire(cs, ws)) break;
+                const int k0 = c * SC;
+#pragma unroll
+                for (int g = 0; g < SC; g += 4) {
+                    int j[4];
+                    double wv[4], xv[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if constexpr (WIDE) j[u] = ((const int*)cs)[(g + u) * 32 + lane];
+                        else j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
+                        wv[u] = ws[(g + u) * 32 + lane];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) xv[u] = k0 + g + u < cnt ? __ldg(x + j[u]) : 0.0;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (k0 + g + u < cnt) acc = __fma_rn(wv[u], xv[u], acc);
+                }
+                R.release();
+            }
+            done = R.streaming;
+        }
+        if (!done) {
+            // 32-bit slice (16-bit ring), or streaming given up: the register walk
+            const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+            const size_t base = (size_t)sl * d.K * 32 + lane;
+            acc = sell_row_dot<false, double>(d, w, x, base, cnt, kmax, -1);
+        }
+        if (!row) continue;
+        if (!in) {
+            y[i] = 0.0;
+            continue;
+        }
+        const double yi = d.diag[i] * x[i] - coef * acc;
+        if (MODE == 0) {
+            y[i] = yi;
+            part0 += x[i] * yi;
+        } else {
+            const double ri = b[i] - yi;
+            y[i] = ri;
+            part0 += ri * ri;
+            part1 += b[i] * b[i];
+        }
+    }
+    double v[2] = {part0, part1}, out[2];
+    if (grid_reduce<2, double>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        if (MODE == 0) {
+            d.scal[S_PQ] = out[0];
+            d.scal[S_ALPHA] = out[0] != 0.0 ? d.scal[S_RZ] / out[0] : 0.0;
+        } else {
+            d.scal[S_RR] = out[0];
+            d.scal[S_RNORM] = sqrt(out[0]);
+            d.scal[S_BNORM] = sqrt(out[1]);
+        }
+    }
+}
+
 // Refinement residual r = b - A x over streamed rows in double-float arithmetic, the
 // same per-entry operations and accumulator order as k_residual_df (entries of even
 // index into the first (hi, lo) pair, odd into the second, merged at the end), so r

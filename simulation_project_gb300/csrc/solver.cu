@@ -654,8 +654,10 @@ struct Solver {
         } else {
             MPS_COUNT_LAUNCH k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
             MPS_COUNT_LAUNCH k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
-            if (!fp64() && opt.compress_rows) {
-                const int w16 = (want_inner16() && d.w16) ? 1 : 0;
+            // 16-bit column offsets for the streamed SpMVs (the FP64 solver streams them
+            // with its FP64 weights; FP16 weight copies only for the FP32 inner CG)
+            if (opt.compress_rows && (!fp64() || opt.spmv_stream)) {
+                const int w16 = (!fp64() && want_inner16() && d.w16) ? 1 : 0;
                 MPS_COUNT_LAUNCH k_compress_rows<<<div_up((d.n + 31) / 32 * 32, 256), 256, 0, st>>>(d, w16);
                 d.rows16 = 1;
                 d.rows_w16 = w16;
@@ -886,9 +888,48 @@ struct Solver {
     bool want_inner16() const { return opt.inner_weights == 16 && opt.spmv_stream != 0 && opt.matrix_free == 0; }
     bool inner16() const { return want_inner16() && d.rows_w16 && use_stream(); }
 
+    // FP64 rows streamed through shared memory (the plain FP64 solver): stages of 8
+    // entries (512 B of 16-bit columns + 2 KB of FP64 weights), 2 stages, CTAs of 8
+    // warps, at least 4 per SM
+    static constexpr int kS64Entries = 8;
+    int spmv64_grid[2] = {0, 0}, spmv64_wide_grid[2] = {0, 0};
+    template <int MODE>
+    void spmv_stream64(const double* w, const double* x, double* y, const double* b, int slot) {
+        if (prefer_wide) {
+            auto k = k_spmv_stream64<MODE, kS64Entries, kSsStages, kSsWarps, kSsMinBlocks, true>;
+            constexpr int smem = stream_smem_bytes<kS64Entries, kSsStages, kSsWarps, double, true>();
+            const int g = stream_grid_for(k, smem, spmv64_wide_grid[MODE]);
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, smem, st>>>(d, w, x, y, b, slot);
+            return;
+        }
+        auto k = k_spmv_stream64<MODE, kS64Entries, kSsStages, kSsWarps, kSsMinBlocks>;
+        constexpr int smem = stream_smem_bytes<kS64Entries, kSsStages, kSsWarps, double>();
+        const int g = stream_grid_for(k, smem, spmv64_grid[MODE]);
+        if (g < 0) {
+            stream_failed = true;
+            return;
+        }
+        MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, smem, st>>>(d, w, x, y, b, slot);
+    }
+    // r = rhs - A press of the FP64 solver with its norms (streamed rows when available)
+    void residual64(const double* w) {
+        if (use_stream()) spmv_stream64<1>(w, d.press, d.r, d.rhs, 2);
+        else MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
+    }
+
     // q = A p of the inner CG (MODE 0): stored weights, or matrix-free FP32 rows
     template <class TW, class TV>
     void spmv_cg(const TW* w, const TV* p, TV* q) {
+        if constexpr (std::is_same<TW, double>::value && std::is_same<TV, double>::value) {
+            if (use_stream()) {
+                spmv_stream64<0>(w, p, q, nullptr, 0);
+                return;
+            }
+        }
         if constexpr (std::is_same<TW, float>::value && std::is_same<TV, float>::value) {
             if (opt.matrix_free == 0 && use_stream()) {
                 if (inner16()) spmv_stream16(p, q);
@@ -958,8 +999,8 @@ struct Solver {
     // plain FP64 Jacobi-PCG from the warm start in press
     CCTStatusType solve_fp64(MpsStepStats& S) {
         const double* w = (const double*)d.nbrw;
-        MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
-        if (pull_scal()) return CCT_CUDAERR;
+        residual64(w);
+        if (stream_failed || pull_scal()) return CCT_CUDAERR;
         h_nnz[0] = h_scal[S_NNZ0];
         h_nnz[1] = h_scal[S_NNZ1];
         h_nnz[2] = h_scal[S_NINT];
@@ -971,8 +1012,8 @@ struct Solver {
         const int it = cg_loop<double, double, double>(d.press, d.r, d.z, d.p, d.q, w, d.minv, nullptr, opt.cg_max_iter);
         if (it < 0) return CCT_CUDAERR;
         // true residual
-        MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, w, d.press, d.r, d.rhs, 2);
-        if (pull_scal()) return CCT_CUDAERR;
+        residual64(w);
+        if (stream_failed || pull_scal()) return CCT_CUDAERR;
         S.cg_iterations += it;
         S.b_norm = bnorm;
         S.cg_relres = bnorm > 0 ? h_scal[S_RNORM] / bnorm : 0.0;
