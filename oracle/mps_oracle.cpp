@@ -1124,6 +1124,8 @@ struct OrcSim {
     std::vector<D3> dragv;
     /* last PPE (sorted order) */
     std::vector<double> l_pnd, l_diag, l_rhs, l_sol, l_idsum;
+    std::vector<int> l_rowptr, l_col;
+    std::vector<double> l_val;
     std::vector<int> l_sid, l_cnt, l_id;
 
     double l0() const { return cfg.param.InitialParticleDistance; }
@@ -1230,11 +1232,16 @@ struct OrcSim {
             std::copy(lists[c].begin(), lists[c].end(), tcell_ids.begin() + tcell_start[c]);
     }
 
+    /* Nearest triangle of the 27 cells around p: the candidates (each triangle once)
+     * in increasing id, a candidate replacing the current nearest only when closer by
+     * more than 1e-12 l0, so that triangles at the same distance (closest point on a
+     * shared edge or vertex) resolve to the lowest id rather than to rounding. */
     void nearest(const D3& p, bool drag_only, double& md, D3& mdir, int& mid) const {
         md = 1e8; mdir = d3(0, 0, 0); mid = -1;
         int cx, cy, cz;
         const int cid = cell_of(p, cx, cy, cz);
         if (!(cid >= 0 && cid < cells)) return;
+        std::vector<int> cand;
         for (int k = -1; k <= 1; ++k)
             for (int j = -1; j <= 1; ++j)
                 for (int i = -1; i <= 1; ++i) {
@@ -1242,14 +1249,18 @@ struct OrcSim {
                     if (m < 0 || m >= cells) continue;
                     for (int l = tcell_start[m]; l < tcell_start[m + 1]; ++l) {
                         const int t = tcell_ids[l];
-                        if (drag_only != (bool)tparams[tris[t].model].isDrag) continue;
-                        if (t == mid) continue;
-                        const D3 q = closest_on_triangle(p, tris[t].v[0], tris[t].v[1], tris[t].v[2]);
-                        const D3 dv = dsub(p, q);
-                        const double d = dlen(dv);
-                        if (d < md) { md = d; mdir = dv; mid = t; }
+                        if (drag_only == (bool)tparams[tris[t].model].isDrag) cand.push_back(t);
                     }
                 }
+        std::sort(cand.begin(), cand.end());
+        cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+        const double tol = 1e-12 * l0();
+        for (const int t : cand) {
+            const D3 q = closest_on_triangle(p, tris[t].v[0], tris[t].v[1], tris[t].v[2]);
+            const D3 dv = dsub(p, q);
+            const double d = dlen(dv);
+            if (d < md - tol) { md = d; mdir = dv; mid = t; }
+        }
     }
 
     void wall_distance() {
@@ -1420,6 +1431,23 @@ struct OrcSim {
         for (int s = 0; s < n; ++s) spress[s] = inner[s] ? x[s] : 0.0;
         for (int s = 0; s < n; ++s) { press[sid[s]] = spress[s]; pnd[sid[s]] = npnd[s]; }
         l_pnd = npnd; l_diag = diag; l_rhs = rhs; l_sol = spress; l_sid = sid;
+        /* the PPE operator of this solve as CSR rows in the solver order: interior rows
+         * hold their diagonal and -c w_ij of every interior neighbour; other rows the
+         * identity (P = 0) */
+        l_rowptr.assign(n + 1, 0);
+        l_col.clear();
+        l_val.clear();
+        for (int s = 0; s < n; ++s) {
+            l_col.push_back(s);
+            l_val.push_back(inner[s] ? diag[s] : 1.0);
+            if (inner[s])
+                for (auto& e : nb[s])
+                    if (inner[e.first]) {
+                        l_col.push_back(e.first);
+                        l_val.push_back(-c * e.second);
+                    }
+            l_rowptr[s + 1] = (int)l_col.size();
+        }
         l_cnt.resize(n); l_idsum.resize(n); l_id.resize(n);
         for (int s = 0; s < n; ++s) {
             double acc = 0.0;
@@ -1627,6 +1655,15 @@ int orc_sim_last_nbr(OrcSim* s, int* cnt, double* idsum, int* pid) {
         pid[i] = s->l_id[i];
     }
     return (int)n;
+}
+
+/* The last solve's PPE operator (CSR, solver order; rows of particles outside the PPE
+ * are identity rows): returns the entry count; arrays may be NULL. */
+long long orc_sim_last_matrix(OrcSim* s, int* rowptr, int* col, double* val) {
+    if (rowptr) std::copy(s->l_rowptr.begin(), s->l_rowptr.end(), rowptr);
+    if (col) std::copy(s->l_col.begin(), s->l_col.end(), col);
+    if (val) std::copy(s->l_val.begin(), s->l_val.end(), val);
+    return (long long)s->l_col.size();
 }
 
 int orc_sim_last_ppe(OrcSim* s, double* pnd, double* diag, double* rhs, double* sol, int* sorted_id) {

@@ -148,6 +148,9 @@ int orc_sim_last_nbr(OrcSim* s, int* cnt, double* idsum, int* pid);
 /* One PPE solve on the current state's sorted arrays (for operator tests):
  * writes the per-particle PND, diagonal, rhs and solution in sorted order. */
 int orc_sim_last_ppe(OrcSim* s, double* pnd, double* diag, double* rhs, double* sol, int* sorted_id);
+/* The last solve's PPE operator as CSR rows in the solver order (identity rows for
+ * particles outside the PPE); returns the entry count, arrays may be NULL. */
+long long orc_sim_last_matrix(OrcSim* s, int* rowptr, int* col, double* val);
 
 #ifdef __cplusplus
 }

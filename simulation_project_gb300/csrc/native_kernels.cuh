@@ -335,8 +335,15 @@ __device__ V3<T> closest_on_tri(const V3<T>& p, const V3<T>& a, const V3<T>& b, 
     return v3(a.x + ab.x * v + ac.x * w, a.y + ab.y * v + ac.y * w, a.z + ab.z * v + ac.z * w);
 }
 
+// Nearest triangle of a particle.  Candidates are visited in increasing triangle id and
+// one replaces the current nearest only when it is closer by more than a tolerance
+// (1e-12 l0 in FP64, 1e-5 l0 in FP32): triangles at the same distance (a closest point
+// on a shared edge or vertex, whose distances differ only by rounding) resolve to the
+// lowest id instead of to the rounding of one implementation.  The choice matters for
+// drag bodies, whose drag acts along the chosen triangle's normal.
 template <class T>
 __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md, V3<T>& mdir, int& mid) {
+    const T tol = sizeof(T) == 8 ? T(1e-12 * d.c.l0) : T(1e-5 * d.c.l0);
     md = T(1e8);
     mdir = v3(T(0), T(0), T(0));
     mid = -1;
@@ -376,7 +383,7 @@ __device__ void nearest_tri(const Dev& d, const V3<T>& p, bool drag_only, T& md,
         }
         const V3<T> dv = v3(p.x - q.x, p.y - q.y, p.z - q.z);
         const T dd = sqrt(dv.x * dv.x + dv.y * dv.y + dv.z * dv.z);
-        if (dd < md) {
+        if (dd < md - tol) {
             md = dd;
             mdir = dv;
             mid = t;

@@ -82,6 +82,7 @@ _FUNCS = {
     "orc_sim_last_ppe": (C.c_int, [P, P, P, P, P, P]),
     "orc_sim_get_ids": (C.c_int, [P, P]),
     "orc_sim_last_nbr": (C.c_int, [P, P, P, P]),
+    "orc_sim_last_matrix": (C.c_longlong, [P, P, P, P]),
 }
 
 
@@ -306,6 +307,32 @@ class OracleSim:
         k = n.value
         o = np.argsort(ids[:k], kind="stable")
         return {"pos": pos[:k][o], "vel": vel[:k][o], "press": press[:k][o], "pnd": pnd[:k][o], "id": ids[:k][o]}
+
+    def matrix(self):
+        """The last solve's PPE operator (scipy CSR, solver order), the right-hand side
+        and the solver-order particle ids and positions."""
+        import scipy.sparse as sp
+        n0 = self.scene.n
+        nnz = int(self.lib.sim_last_matrix(self.h, None, None, None))
+        rowptr = np.zeros(n0 + 1, np.int32)
+        col = np.zeros(nnz, np.int32)
+        val = np.zeros(nnz)
+        self.lib.sim_last_matrix(self.h, ptr(rowptr), ptr(col), ptr(val))
+        n = int(np.flatnonzero(rowptr[1:] == nnz)[0]) + 1 if nnz else 0
+        pnd, diag, rhs, sol = (np.zeros(n0) for _ in range(4))
+        sid = np.zeros(n0, np.int32)
+        self.lib.sim_last_ppe(self.h, ptr(pnd), ptr(diag), ptr(rhs), ptr(sol), ptr(sid))
+        nb = self.neighbours_sorted()
+        A = sp.csr_matrix((val, col, rowptr[:n + 1]), shape=(n, n))
+        return A, rhs[:n], sol[:n], nb[:n]
+
+    def neighbours_sorted(self):
+        n0 = self.scene.n
+        cnt = np.zeros(n0, np.int32)
+        idsum = np.zeros(n0)
+        pid = np.zeros(n0, np.int32)
+        k = self.lib.sim_last_nbr(self.h, ptr(cnt), ptr(idsum), ptr(pid))
+        return pid[:k]
 
     def neighbours(self):
         n0 = self.scene.n

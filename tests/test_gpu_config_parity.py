@@ -5,11 +5,18 @@
   (108,186 particles, 4096-triangle cylinder, 64 drag spheres of radius 3 l0, 30 rpm),
   both in FP64 against the FP64 oracle solver for 10 steps: identical Laplacian
   neighbour sets (count and id checksum per particle), pressure within 1e-6 (max-norm,
-  relative to max |P|), positions within 1e-6 l0.
+  relative to max |P|), positions within 1e-6 l0 (measured on a GB300: 1.8e-13 /
+  5.5e-11 l0 and 1.9e-13 / 1.4e-14 l0).  The nearest wall or drag triangle of a
+  particle resolves ties (distances within 1e-12 l0) to the lowest triangle id on both
+  sides: without that rule the drag direction (the chosen triangle's normal) of
+  particles next to a drag sphere's shared edges followed each implementation's
+  rounding, and this flow amplifies such differences (a 4e-16 m perturbation of the
+  initial positions grows to 4e-7 in pressure after 10 steps in the oracle itself).
 * Config 2 with FP32 operators inside FP64 refinement against the same FP64 oracle
   after 10 steps: pressure within 2e-3 (max-norm relative), PND 1e-5 relative, velocity
   2e-3 of the largest speed, kinetic energy 1e-4 relative, positions 1e-4 l0; the
-  measured errors are printed.
+  measured errors are printed (GB300: pressure 3.4e-4, PND 6.2e-6, velocity 1.6e-4,
+  kinetic energy 6.2e-5, positions 2.7e-6 l0).
 * The reference-named explicit schedule (CalcSTLDistance, CalcDragEffect,
   CalcExplicitly, then CalcExplicitPressure and CalcExplicitPressureGradient on the
   predicted positions) on the config-2 scene, bit-identical to the oracle, and the
