@@ -381,6 +381,14 @@ def run_gpu(args):
                         "fallbacks": int(sum(s["fallback"] for s in st_fast)),
                         "error_flags": int(np.bitwise_or.reduce([s["error_flags"] for s in st_fast])),
                         "learned": params is not None, "preconditioner": ["jacobi", "multilevel"][args.precond],
+                        "learned_gate": {
+                            "steps_with_learned_guess": int(sum(s["learned_applied"] for s in st_fast)),
+                            "steps": len(st_fast),
+                            "saved_its_when_applied": [round(s["learned_saved_its"], 3) for s in st_fast
+                                                       if s["learned_applied"]],
+                            "cost_its_when_applied": [round(s["learned_cost_its"], 3) for s in st_fast
+                                                      if s["learned_applied"]]},
+                        "flexible_cg": bool(all(s["flexible"] for s in st_fast)),
                         "warm_start_order": int(st_fast[-1]["warm_start"]),
                         "mg_levels": int(st_fast[-1]["mg_levels"]), "mg_level1": int(st_fast[-1]["mg_level1"]),
                         "phases_ms": phases},

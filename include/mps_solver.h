@@ -97,6 +97,18 @@ typedef struct MpsSolverOptions {
                                P_{n-3}; -1 (default) 2 in FP32_IR, 0 in FP64.  Limited to the
                                history held (reset by mps_solver_set_particles and
                                mps_solver_set_time_step) */
+    int flexible;           /* inner CG: 1 flexible CG (Notay, one direction kept: beta =
+                               -(z.q) / (p.q), q = A p of the last direction), -1 plain PCG,
+                               0 (default) flexible while the learned diagonal scaling
+                               (learned bit 1) shapes the preconditioner, else plain */
+    int learned_gate;       /* 1 (default): the learned initial guess runs only while it
+                               pays: after each learned step the solver compares the CG
+                               iterations it saved (the residual reduction it gave, at the
+                               step's own contraction per iteration) with its cost (its
+                               kernels' CUDA-event time less the multilevel setup it
+                               overlaps, in iterations of the same step); when it costs more,
+                               it is skipped for 1, 2, 4, ... 64 steps before the next trial.
+                               0: it runs every step */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */
@@ -131,6 +143,10 @@ typedef struct MpsStepStats {
     int rows16;             /* 1 if the FP32 SpMV used compressed columns this step */
     int inner16;            /* 1 if the inner CG ran on the FP16-weight operator this step */
     int warm_start;         /* extrapolation order of this step's warm start (0: P_{n-1}) */
+    int learned_applied;    /* 1 if the learned initial guess ran this step */
+    float learned_saved_its;/* CG iterations it saved (estimate, see learned_gate) */
+    float learned_cost_its; /* its cost in CG iterations of this step (CUDA events) */
+    int flexible;           /* 1 if the inner CG ran as flexible CG */
 } MpsStepStats;
 
 void mps_solver_default_options(MpsSolverOptions* opt);

@@ -483,17 +483,20 @@ __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
 // warp per level-1 aggregate computes e1[I] as k_mg_up, then z = m r + e1[I] over the
 // cell's rows (every row lies in one cell), p = z in mode 1, and r.z as k_mg_fine_z
 // (S_RZ, or S_BETA and S_RZ); one pass over the rows instead of two launches
+// With qf (flexible CG, mode 0): also z.q of the last direction's product q = A p, and
+// S_BETA = -(z.q) / (p.q) (Notay's flexible CG keeping one direction) instead of the
+// ratio of successive r.z.
 template <class TV>
 __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
                                                       const TV* __restrict__ r, TV* __restrict__ z,
                                                       TV* __restrict__ p, const float* __restrict__ m32, int mode,
-                                                      int slot) {
+                                                      int slot, const TV* __restrict__ qf = nullptr) {
     if (d.scal[S_CONV] != 0.0) return;
     const MgLevel& lo = mg.L[1];
     const MgLevel& hi = mg.L[2];
     const float omega = mg.omega;
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    TV prz = TV(0);
+    TV prz = TV(0), pzq = TV(0);
     if (I < lo.n) {   // warp-uniform; every thread reaches the grid reduction
         float t = 0.f;
         if (lane < 27) {
@@ -509,14 +512,19 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
             if (d.inner[i]) {
                 zi = (TV)m32[i] * r[i] + (TV)e1;
                 prz += r[i] * zi;
+                if (qf) pzq += zi * qf[i];
             }
             z[i] = zi;
             if (mode == 1) p[i] = zi;
         }
     }
-    double v[1] = {(double)prz}, out[1];
-    if (grid_reduce<1, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+    double v[2] = {(double)prz, (double)pzq}, out[2];
+    if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
         if (mode == 1) {
+            d.scal[S_RZ] = out[0];
+        } else if (qf) {
+            const double pq = d.scal[S_PQ];
+            d.scal[S_BETA] = pq != 0.0 ? -out[1] / pq : 0.0;
             d.scal[S_RZ] = out[0];
         } else {
             const double rz = d.scal[S_RZ];
@@ -579,23 +587,29 @@ __global__ void __launch_bounds__(1024) k_mg_dense_solve(const double* __restric
 template <class TV>
 __global__ void __launch_bounds__(256) k_mg_fine_z(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
                                                    const TV* __restrict__ r, TV* __restrict__ z, TV* __restrict__ p,
-                                                   const float* __restrict__ m32, int mode, int slot) {
+                                                   const float* __restrict__ m32, int mode, int slot,
+                                                   const TV* __restrict__ qf = nullptr) {
     if (d.scal[S_CONV] != 0.0) return;
     const float* e1 = mg.L[1].e2;
-    TV prz = TV(0);
+    TV prz = TV(0), pzq = TV(0);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
         TV zi = TV(0);
         if (d.inner[i]) {
             const int a = mg.agg1[i];
             zi = (TV)m32[i] * r[i] + (a >= 0 ? (TV)e1[a] : TV(0));
             prz += r[i] * zi;
+            if (qf) pzq += zi * qf[i];
         }
         z[i] = zi;
         if (mode == 1) p[i] = zi;
     }
-    double v[1] = {(double)prz}, out[1];
-    if (grid_reduce<1, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+    double v[2] = {(double)prz, (double)pzq}, out[2];
+    if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
         if (mode == 1) {
+            d.scal[S_RZ] = out[0];
+        } else if (qf) {
+            const double pq = d.scal[S_PQ];
+            d.scal[S_BETA] = pq != 0.0 ? -out[1] / pq : 0.0;
             d.scal[S_RZ] = out[0];
         } else {
             const double rz = d.scal[S_RZ];

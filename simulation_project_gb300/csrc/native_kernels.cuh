@@ -1587,13 +1587,15 @@ __global__ void __launch_bounds__(256) k_cg_start(const __grid_constant__ Dev d,
 // x += alpha p; r -= alpha q; z = M r; rz, rr; then beta, convergence.
 // with_z = 0: the preconditioner is applied by separate kernels (z, rz and beta
 // are theirs); only x, r and the convergence test here.
+// flexible (with_z only): beta = -(z.q) / (p.q) of flexible CG instead of the ratio of
+// successive r.z.
 template <class TV, class TXA>
 __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d, TXA* x, TV* r, TV* z, const TV* p,
                                                    const TV* q, const double* m64, const float* m32, int slot,
-                                                   int with_z) {
+                                                   int with_z, int flexible = 0) {
     if (d.scal[S_CONV] != 0.0) return;
     const TV alpha = (TV)d.scal[S_ALPHA];
-    TV prz = TV(0), prr = TV(0);
+    TV prz = TV(0), prr = TV(0), pzq = TV(0);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
         if (!d.inner[i]) continue;
         x[i] = x[i] + (TXA)alpha * (TXA)p[i];
@@ -1604,12 +1606,17 @@ __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d
             const TV zi = ri * mi;
             z[i] = zi;
             prz += ri * zi;
+            if (flexible) pzq += zi * q[i];
         }
         prr += ri * ri;
     }
-    double v[2] = {(double)prz, (double)prr}, out[2];
-    if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
-        if (with_z) {
+    double v[3] = {(double)prz, (double)prr, (double)pzq}, out[3];
+    if (grid_reduce<3, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        if (with_z && flexible) {
+            const double pq = d.scal[S_PQ];
+            d.scal[S_BETA] = pq != 0.0 ? -out[2] / pq : 0.0;
+            d.scal[S_RZ] = out[0];
+        } else if (with_z) {
             const double rz = d.scal[S_RZ];
             d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
             d.scal[S_RZ] = out[0];
@@ -1910,7 +1917,10 @@ __global__ void k_learned_finish(const __grid_constant__ Dev d) {
 __global__ void __launch_bounds__(256) k_learned_finish_r(const __grid_constant__ Dev d, int slot) {
     const double dad = d.scal[S_LS0], dr = d.scal[S_LS1];
     const double a = (dad > 0.0 && isfinite(dr / dad)) ? dr / dad : 0.0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) d.scal[S_IRTOL] = a;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        d.scal[S_IRTOL] = a;
+        d.scal[S_TMP1] = d.scal[S_RNORM];   // ||r|| of the warm start, before the update
+    }
     double rr = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
         if (!d.inner[i]) {

@@ -143,6 +143,37 @@ struct Solver {
     }
 
     bool fp64() const { return opt.precision == MPS_PREC_FP64; }
+
+    // ---- gate of the learned initial guess (MpsSolverOptions::learned_gate) ----
+    // events: learned kernels [0, 1] (solver stream), the multilevel setup they overlap
+    // [2, 3] (second stream), the solve [4, 5]
+    cudaEvent_t gate_ev[6] = {};
+    int gate_skip = 0, gate_period = 1;
+    double gate_rb = 0.0, gate_ra = 0.0;
+    void gate_update(MpsStepStats& S, bool overlapped) {
+        if (cudaStreamSynchronize(st) || cudaStreamSynchronize(st2)) return;
+        float t_l = 0.f, t_m = 0.f, t_s = 0.f;
+        cudaEventElapsedTime(&t_l, gate_ev[0], gate_ev[1]);
+        if (overlapped) cudaEventElapsedTime(&t_m, gate_ev[2], gate_ev[3]);
+        cudaEventElapsedTime(&t_s, gate_ev[4], gate_ev[5]);
+        const int its = S.cg_iterations;
+        if (its <= 0 || !(gate_rb > 0.0) || !(gate_ra > 0.0) || !(S.cg_relres > 0.0) || !(S.r0_relres > S.cg_relres))
+            return;
+        // contraction per iteration of this solve, and the iterations the guess's
+        // residual reduction is worth at that rate
+        const double per_it = std::log(S.r0_relres / S.cg_relres) / its;
+        const double saved = std::log(gate_rb / gate_ra) / per_it;
+        const double t_it = (double)t_s / its;
+        const double cost = std::max(0.0, (double)t_l - (double)t_m) / t_it;
+        S.learned_saved_its = (float)saved;
+        S.learned_cost_its = (float)cost;
+        if (saved < cost) {
+            gate_skip = gate_period;
+            gate_period = std::min(2 * gate_period, 64);
+        } else {
+            gate_period = 1;
+        }
+    }
     // inner CG iterations of each refinement pass in the last step (first batch sizes)
     static constexpr int kPassMemory = 4;
     int pass_its[kPassMemory] = {0, 0, 0, 0};
@@ -197,6 +228,8 @@ struct Solver {
         c.explicit_pressure = opt.pressure_mode == MPS_PRESSURE_EXPLICIT;
         timer.on = opt.profile != 0;
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CCT_CUDAERR;
+        for (auto& e : gate_ev)
+            if (cudaEventCreate(&e) != cudaSuccess) return CCT_CUDAERR;
         if (cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_rows, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_mg, cudaEventDisableTiming) != cudaSuccess)
@@ -299,6 +332,8 @@ struct Solver {
         if (st2) cudaStreamDestroy(st2);
         if (ev_rows) cudaEventDestroy(ev_rows);
         if (ev_mg) cudaEventDestroy(ev_mg);
+        for (auto& e : gate_ev)
+            if (e) cudaEventDestroy(e);
     }
 
     void swap_state() {
@@ -476,6 +511,12 @@ struct Solver {
         return CCT_NOERR;
     }
 
+    // flexible CG for this step's inner solve (see MpsSolverOptions::flexible)
+    bool flex_step = false;
+    bool flexible_now() const {
+        if (opt.flexible != 0) return opt.flexible > 0;
+        return learned_ready && (opt.learned & 2) != 0;
+    }
     // z = M^-1 r (interior rows), rz; mode 1 also sets p = z and S_RZ, mode 0 S_BETA.
     // restricted = true: level-1 r and the first sweep are already done (by
     // k_mg_update_restrict)
@@ -502,18 +543,20 @@ struct Solver {
         // the level-2 -> level-1 up sweep carries the fine level when no extra level-1
         // sweeps follow it (and the reduction buffer holds its CTAs' partials)
         const int up1_blocks = div_up(L[1].n * 32, 256);
-        const bool fuse = lv >= 2 && extra == 0 && up1_blocks <= 4 * kRedBlocks;
+        // the reduction buffer holds 2 partials per CTA of the fused kernel
+        const bool fuse = lv >= 2 && extra == 0 && up1_blocks <= 2 * kRedBlocks;
+        const float* qf = (flex_step && mode == 0) ? d.q32 : nullptr;
         for (int l = lv - 1; l >= (fuse ? 2 : 1); --l)
             MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
         if (fuse) {
-            MPS_COUNT_LAUNCH k_mg_up_fine_z<float><<<up1_blocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7);
+            MPS_COUNT_LAUNCH k_mg_up_fine_z<float><<<up1_blocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
             return;
         }
         for (int k = 0; k < extra; ++k) {
             MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e2, L[1].e, om);
             std::swap(L[1].e, L[1].e2);
         }
-        MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7);
+        MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
     }
 
     // ---- phases ----
@@ -662,7 +705,16 @@ struct Solver {
                 d.rows16 = 1;
                 d.rows_w16 = w16;
             }
-            const bool use_learned = learned_ready && opt.learned;
+            bool use_learned = learned_ready && opt.learned;
+            // the gate: a learned guess that cost more than it saved sits out a few steps
+            if (use_learned && opt.learned_gate && !fp64() && gate_skip > 0) {
+                --gate_skip;
+                use_learned = false;
+            }
+            const bool gate_measure = use_learned && opt.learned_gate && !fp64();
+            S.learned_applied = use_learned ? 1 : 0;
+            flex_step = flexible_now();
+            S.flexible = flex_step ? 1 : 0;
             // the multilevel setup only needs the rows: with the learned guess it runs on
             // the second stream meanwhile (enqueued after the learned kernels below)
             const bool overlap_mg = use_learned && !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
@@ -678,6 +730,7 @@ struct Solver {
                                                                                   d.r, d.rhs, 2);
                 else
                     residual_df((const float*)d.nbrw);
+                if (gate_measure) cudaEventRecord(gate_ev[0], st);
                 MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
                 MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
                 MPS_COUNT_LAUNCH k_features<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -696,18 +749,26 @@ struct Solver {
                     } else {
                         MPS_COUNT_LAUNCH k_learned_finish_r<<<kRedBlocks, 256, 0, st>>>(d, 7);
                         residual_ready = true;
+                        if (gate_measure) cudaEventRecord(gate_ev[1], st);
                     }
                 }
                 timer.mark(PH_SETUP, st);
             }
             if (overlap_mg) {
                 cudaStreamWaitEvent(st2, ev_rows, 0);
+                if (gate_measure) cudaEventRecord(gate_ev[2], st2);
                 if (mg_setup(st2)) return CCT_CUDAERR;
+                if (gate_measure) cudaEventRecord(gate_ev[3], st2);
                 cudaEventRecord(ev_mg, st2);
                 cudaStreamWaitEvent(st, ev_mg, 0);
                 mg_setup_done = true;
             }
+            if (gate_measure) cudaEventRecord(gate_ev[4], st);
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
+            if (gate_measure) {
+                cudaEventRecord(gate_ev[5], st);
+                gate_update(S, overlap_mg);
+            }
             if (use_learned && S.cg_relres > opt.cg_rtol) {
                 // the learned solve did not reach the tolerance: plain Jacobi-CG from the warm start
                 MPS_COUNT_LAUNCH k_restore_plain<<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -976,7 +1037,8 @@ struct Solver {
                 timer.mark(PH_VEC, st);
                 const bool use_mg = std::is_same<TV, float>::value && mg_ready;
                 if (!use_mg)
-                    MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1, 1);
+                    MPS_COUNT_LAUNCH k_cg_update<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, x, r, z, p, q, m64, m32, 1, 1,
+                                                                                    flex_step ? 1 : 0);
                 if constexpr (std::is_same<TV, float>::value) {
                     if (use_mg) {
                         MPS_COUNT_LAUNCH k_mg_update_restrict<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, mg, x, r, p, q, 1);
@@ -1071,15 +1133,20 @@ struct Solver {
         double bnorm = 0.0;
         int outer = 0;
         for (;;) {
-            if (!(outer == 0 && residual_ready)) residual_df(w);
-            residual_ready = false;
+            const bool from_learned = outer == 0 && residual_ready;
+            if (!from_learned) residual_df(w);
+            residual_ready = from_learned;
             if (stream_failed || pull_scal()) return CCT_CUDAERR;
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
                 h_nnz[1] = h_scal[S_NNZ1];
                 h_nnz[2] = h_scal[S_NINT];
                 S.r0_relres = h_scal[S_BNORM] > 0 ? h_scal[S_RNORM] / h_scal[S_BNORM] : 0.0;
+                // the learned guess's residual norms before / after its update
+                gate_rb = residual_ready ? h_scal[S_TMP1] : 0.0;
+                gate_ra = h_scal[S_RNORM];
             }
+            residual_ready = false;
             bnorm = h_scal[S_BNORM];
             const double rn = h_scal[S_RNORM];
             S.cg_relres = bnorm > 0 ? rn / bnorm : 0.0;
@@ -1306,6 +1373,9 @@ struct MpsSolver {
 
 extern "C" {
 
+static_assert(sizeof(MpsSolverOptions) == 152 && sizeof(MpsStepStats) == 168,
+              "the option and statistics records are part of the C ABI");
+
 void mps_solver_default_options(MpsSolverOptions* o) {
     std::memset(o, 0, sizeof(*o));
     o->precision = MPS_PREC_FP32_IR;
@@ -1328,6 +1398,8 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->inner_weights = 16;
     o->spmv_wide = 0;
     o->warm_start = -1;
+    o->flexible = 0;
+    o->learned_gate = 1;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -1340,6 +1412,7 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (o.inner_weights != 32 && o.inner_weights != 16) return CCT_PARAMERR;
     if (o.spmv_wide < -1 || o.spmv_wide > 1) return CCT_PARAMERR;
     if (o.warm_start < -1 || o.warm_start > 2) return CCT_PARAMERR;
+    if (o.flexible < -1 || o.flexible > 1 || o.learned_gate < 0 || o.learned_gate > 1) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {

@@ -26,7 +26,8 @@ class MpsSolverOptions(C.Structure):
                 ("source_relaxation", C.c_double), ("profile", C.c_int), ("preconditioner", C.c_int),
                 ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int),
                 ("matrix_free", C.c_int), ("spmv_stream", C.c_int), ("inner_weights", C.c_int),
-                ("spmv_wide", C.c_int), ("warm_start", C.c_int)]
+                ("spmv_wide", C.c_int), ("warm_start", C.c_int), ("flexible", C.c_int),
+                ("learned_gate", C.c_int)]
 
 
 class MpsStepStats(C.Structure):
@@ -38,7 +39,8 @@ class MpsStepStats(C.Structure):
                 ("ms_correct", C.c_float), ("ms_learned", C.c_float), ("spmv_launches", C.c_int),
                 ("ms_precond", C.c_float), ("mg_levels", C.c_int), ("mg_level1", C.c_int),
                 ("r0_relres", C.c_double), ("nnz_wide", C.c_longlong), ("rows16", C.c_int),
-                ("inner16", C.c_int), ("warm_start", C.c_int)]
+                ("inner16", C.c_int), ("warm_start", C.c_int), ("learned_applied", C.c_int),
+                ("learned_saved_its", C.c_float), ("learned_cost_its", C.c_float), ("flexible", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

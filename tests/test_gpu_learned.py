@@ -117,9 +117,9 @@ def test_learned_solver_converges_and_reports_gain():
     p, info = train(f, t, epochs=6, batch=4096, lr=2e-3)
     assert info["val_loss_after"] < info["val_loss_before"]
     plain = Solver(sc, precision="fp32_ir")
-    learned = Solver(sc, precision="fp32_ir", learned=1)
+    learned = Solver(sc, precision="fp32_ir", learned=1, learned_gate=0)
     learned.set_learned(p)
-    scaled = Solver(sc, precision="fp32_ir", learned=3)
+    scaled = Solver(sc, precision="fp32_ir", learned=3, learned_gate=0)
     scaled.set_learned(p)
     it_p, it_l, it_s = 0, 0, 0
     for i in range(8):
@@ -141,3 +141,51 @@ def test_learned_solver_converges_and_reports_gain():
     pm = np.abs(a["press"]).max()
     # both converged to 1e-8 residual: pressures agree to the solve tolerance
     assert np.abs(a["press"] - b["press"]).max() <= 1e-3 * pm
+
+
+@pytest.mark.parametrize("precond", [0, 1], ids=["jacobi", "multilevel"])
+def test_flexible_cg_matches_pcg_for_a_fixed_preconditioner(precond):
+    """Flexible CG (beta = -(z.q)/(p.q), one direction kept) equals PCG in exact
+    arithmetic for a fixed SPD preconditioner: same 1e-8 residual, iterations within a
+    few per step, pressures within the solve tolerance."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=8)
+    a = Solver(sc, precision="fp32_ir", preconditioner=precond, flexible=-1)
+    b = Solver(sc, precision="fp32_ir", preconditioner=precond, flexible=1)
+    ia = ib = 0
+    for i in range(5):
+        sa, sb = a.step(i), b.step(i)
+        assert sa["cg_relres"] <= 1e-8 and sb["cg_relres"] <= 1e-8, (sa, sb)
+        assert sa["flexible"] == 0 and sb["flexible"] == 1
+        ia += sa["cg_iterations"]
+        ib += sb["cg_iterations"]
+    assert abs(ia - ib) <= max(3, ia // 10), (ia, ib)
+    pa, pb = a.state()["press"], b.state()["press"]
+    assert np.abs(pa - pb).max() <= 1e-3 * np.abs(pa).max()
+
+
+def test_learned_scaling_runs_flexible_cg_and_the_gate_skips_a_guess_that_does_not_pay():
+    """The learned diagonal scaling makes the inner solve flexible CG by default; the
+    gate measures each learned guess (iterations saved against its cost in iterations,
+    both from the step's own CUDA events and residuals) and skips the guess in the
+    following steps when it cost more than it saved."""
+    sc = scenes.rotating_bucket(l0=0.008, n_drag=8)
+    f, t = collect_samples(sc, steps=4, precision="fp64")
+    p, _ = train(f, t, epochs=4, batch=4096, lr=2e-3)
+    s = Solver(sc, precision="fp32_ir", learned=3)
+    s.set_learned(p)
+    rows = []
+    for i in range(12):
+        st = s.step(i)
+        assert st["cg_relres"] <= 1e-8 and st["error_flags"] == 0, st
+        assert st["flexible"] == 1
+        rows.append(st)
+    print("\nstep applied saved_its cost_its iterations")
+    for i, st in enumerate(rows):
+        print(i, st["learned_applied"], round(st["learned_saved_its"], 2), round(st["learned_cost_its"], 2),
+              st["cg_iterations"])
+    assert rows[0]["learned_applied"] == 1 and rows[0]["learned_cost_its"] > 0
+    for a, b in zip(rows, rows[1:]):
+        if a["learned_applied"] and a["learned_saved_its"] < a["learned_cost_its"]:
+            assert b["learned_applied"] == 0   # a guess that did not pay sits out the next step
+        if not b["learned_applied"]:
+            assert b["learned_saved_its"] == 0 and b["learned_cost_its"] == 0
