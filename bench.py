@@ -337,6 +337,7 @@ def run_gpu(args):
     fast.close()
     sort = sort_bench(n, scene.box.cell_num, peak_gbs)
     mlp = mlp_bench(params, n, load_bf16_peak())
+    training_gemms = gemm_bench(load_bf16_peak())
     accuracy = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
 
     result = {
@@ -398,6 +399,7 @@ def run_gpu(args):
         "pair_evaluations": pair_evals,
         "sort": sort,
         "mlp_inference": mlp,
+        "mlp_training_gemms": training_gemms,
         "accuracy_vs_fp64": accuracy,
         "e2e": e2e,
         "frames": frames,
@@ -473,6 +475,51 @@ def mlp_bench(params, n, tflops_peak, reps=20):
     X.free()
     Y.free()
     m.close()
+    return out
+
+
+def gemm_bench(tflops_peak, reps=20):
+    """The MLP's training GEMMs (mps_gemm_bf16_variant) on the shapes of one Adam step of
+    8192 rows: a hidden layer's forward (8192 x 128 x 128, bias + SiLU epilogue) and a
+    weight gradient (128 x 128 over K = 8192, split 16); the tcgen05 kernel training
+    uses (variant 0) and the mma.sync cross-check (variant 1), CUDA events on the legacy
+    stream around `reps` launches after 3 warm-up launches."""
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.learned import gemm_bf16
+    rng = np.random.default_rng(3)
+    Mb, H = 8192, 128
+    X = lib.DeviceArray.from_host(rng.integers(0, 1 << 15, (Mb, H), dtype=np.uint16))
+    W = lib.DeviceArray.from_host(rng.integers(0, 1 << 15, (H, H), dtype=np.uint16))
+    G = lib.DeviceArray.from_host(rng.integers(0, 1 << 15, (Mb, H), dtype=np.uint16))
+    bias = lib.DeviceArray.from_host(np.zeros(H, np.float32))
+    Y = lib.DeviceArray((Mb, H), np.float32)
+    Yb = lib.DeviceArray((Mb, H), np.uint16)
+    dW = lib.DeviceArray((H, H), np.float32)
+    ev0, ev1 = lib.Event(), lib.Event()
+    out = {}
+    shapes = {
+        "forward_8192x128x128": (lambda v: gemm_bf16(Mb, H, H, X.ptr, H, 0, W.ptr, H, 0, None, H, Cb=Yb.ptr, ldcb=H,
+                                                      Cz=Y.ptr, bias=bias.ptr, act=1, variant=v), 2.0 * Mb * H * H),
+        "weight_grad_128x128_k8192": (lambda v: gemm_bf16(H, H, Mb, X.ptr, H, 1, G.ptr, H, 0, dW.ptr, H, beta=1.0,
+                                                           split=16, variant=v), 2.0 * Mb * H * H),
+    }
+    for name, (fn, flop) in shapes.items():
+        out[name] = {}
+        for v, vname in ((0, "tcgen05"), (1, "mma_sync")):
+            for _ in range(3):
+                fn(v)
+            lib.call("mps_device_sync")
+            ev0.record(None)
+            for _ in range(reps):
+                fn(v)
+            ev1.record(None)
+            lib.call("mps_device_sync")
+            us = ev0.elapsed_ms(ev1) / reps * 1e3
+            tf = flop / (us / 1e6) / 1e12
+            out[name][vname] = {"us_per_launch": round(us, 2), "tflops": round(tf, 1),
+                                "frac_of_bf16_peak": round(tf / tflops_peak, 4)}
+    for a in (X, W, G, bias, Y, Yb, dW):
+        a.free()
     return out
 
 

@@ -7,6 +7,8 @@
  * Network: 12 features -> 128 -> 128 -> 128 (SiLU) -> 2 outputs (pressure increment
  * in units of the step's pressure scale, log of the diagonal preconditioner scale).
  * Weights are BF16 on the tensor cores, accumulation and the master copy are FP32.
+ * Training (forward with kept pre-activations, backward, Adam) and inference run on
+ * the 5th-generation tensor cores (tcgen05).
  * Parameter vector layout (FP32, MPS_MLP_PARAMS = 34,946 floats):
  *   W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[128][2] b4[2]
  * (W[k][n]: input k, output n).
@@ -29,10 +31,17 @@ extern "C" {
  * (transB = 1).  Any K (tiles are zero-filled).  C (FP32, ldc) and/or Cb (BF16, ldcb)
  * may be NULL.  act: 0 none, 1 SiLU (Cz, if given, receives the pre-activation FP32).
  * split_k > 1 splits the K loop over CTAs and accumulates into C with atomics
- * (beta must be 1 and act 0 then). */
+ * (beta must be 1 and act 0 then).  Runs on the 5th-generation tensor cores
+ * (tcgen05.mma into TMEM, 128 x 16..128 tiles, K in stages of 64); the MLP's forward
+ * and backward passes of training use it. */
 CCTStatusType mps_gemm_bf16(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb,
                             int transB, float* C, int ldc, void* Cb, int ldcb, float* Cz, const float* bias, int act,
                             float beta, int split_k, void* stream);
+/* the same with a chosen kernel: 0 the tcgen05 kernel of mps_gemm_bf16, 1 the
+ * warp-level mma.sync kernel (a cross-check) */
+CCTStatusType mps_gemm_bf16_variant(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb,
+                                    int transB, float* C, int ldc, void* Cb, int ldcb, float* Cz, const float* bias,
+                                    int act, float beta, int split_k, int variant, void* stream);
 
 typedef struct MpsMlp MpsMlp;
 CCTStatusType mps_mlp_create(int max_batch, unsigned long long seed, MpsMlp** out);

@@ -1,7 +1,9 @@
 // mlp.cu - BF16 tensor-core GEMM and the learned-preconditioner MLP (forward,
 // backward, Adam) of the GB300 MPS library (include/mps_learned.h).
 //
-// GEMM: one CTA of 4 warps computes a 64x64 FP32 tile of C with warp-level
+// GEMM (training): k_gemm_tc on the 5th-generation tensor cores (tcgen05.mma into
+// TMEM, see below).  Cross-check variant k_gemm_bf16: one CTA of 4 warps computes a
+// 64x64 FP32 tile of C with warp-level
 // mma.sync.m16n8k16 (BF16 in, FP32 accumulate); each warp owns a 32x32 sub-tile
 // (2 x 4 MMA tiles).  K advances 32 at a time through padded shared-memory tiles
 // As[m][k] and Bs[n][k], so every A and B fragment register is one 32-bit shared
@@ -136,8 +138,10 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
             }
 }
 
-cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, int ta, const bf16* B, int ldb, int tb, float* C, int ldc,
-                 bf16* Cb, int ldcb, float* Cz, const float* bias, int act, float beta, int split, cudaStream_t st) {
+// the mma.sync GEMM (variant 1, a cross-check of the tcgen05 one)
+cudaError_t gemm_mma_sync(int M, int N, int K, const bf16* A, int lda, int ta, const bf16* B, int ldb, int tb, float* C,
+                          int ldc, bf16* Cb, int ldcb, float* Cz, const float* bias, int act, float beta, int split,
+                          cudaStream_t st) {
     if (M <= 0 || N <= 0 || K <= 0) return cudaErrorInvalidValue;
     split = max(1, split);
     int kchunk = (K + split - 1) / split;
@@ -429,6 +433,203 @@ __device__ __forceinline__ void tc_ld32(unsigned taddr, uint32_t (&v)[32]) {
 __device__ __forceinline__ void tc_ld2(unsigned taddr, uint32_t& a, uint32_t& b) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=r"(a), "=r"(b) : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(unsigned taddr, uint32_t (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
+// BF16 GEMM on the 5th-generation tensor cores, the training path of the MLP:
+// C[M x N] (+)= op(A)[M x K] op(B)[K x N], FP32 accumulate, with the epilogue of
+// k_gemm_bf16 (bias, FP32 pre-activation Cz, SiLU, FP32 C with beta, BF16 Cb;
+// split-K CTAs add into C with FP32 atomics).  A CTA of 4 warps owns a 128 x BN tile
+// (BN = 16..128, a multiple of 16) whose accumulator lives in TMEM (128 lanes x BN
+// FP32 columns).  K advances 64 at a time through two shared-memory stages holding
+// the A tile [128][64] and the B^T tile [BN][64] in the canonical K-major layout
+// without swizzle (tc_off); every thread loads one row of each (rows of A and of B^T
+// that are K-contiguous in memory as 16-byte vectors, transposed operands element by
+// element, coalesced across the warp), zero-filling outside the matrix.  One thread
+// issues the four tcgen05.mma (M = 128, N = BN, K = 16 each) of a stage and commits
+// them to the stage's mbarrier; a stage is refilled only after its MMAs completed
+// (bounded wait).  The epilogue reads each warp's 32 TMEM lanes (= rows) with
+// tcgen05.ld.  Bounded waits that run out set g_mlp_tc_timeout, wait (bounded) for
+// the MMAs in flight and skip the epilogue.
+// ---------------------------------------------------------------------------
+constexpr int kGtBM = 128, kGtBK = 64, kGtMaxBN = 128, kGtThreads = 128;
+constexpr int kGtStageA = kGtBM * kGtBK * 2;                 // 16 KB
+constexpr int kGtStageB = kGtMaxBN * kGtBK * 2;              // 16 KB
+constexpr int kGtStage = kGtStageA + kGtStageB;
+constexpr size_t kGtSmem = 2 * kGtStage + 64 + 1024;         // 2 stages, barriers, TMEM slot, alignment
+
+// one row (64 k) of a K-major tile from row `row` of a matrix stored with K contiguous
+// (ld elements apart) or transposed (K rows, ld elements apart); zero outside
+__device__ __forceinline__ void gt_load_row(unsigned char* tile, int r, const bf16* __restrict__ X, int ld, int trans,
+                                            int row, int rows, int k0, int kend) {
+    const bf16 zero = __float2bfloat16(0.f);
+    const bool in = row < rows;
+#pragma unroll 1
+    for (int c = 0; c < kGtBK / 8; ++c) {
+        const int kb = k0 + 8 * c;
+        uint4 o = make_uint4(0u, 0u, 0u, 0u);
+        if (in && kb < kend) {
+            if (!trans && kb + 8 <= kend && ((((uintptr_t)(X + (size_t)row * ld + kb)) & 15u) == 0)) {
+                o = *reinterpret_cast<const uint4*>(X + (size_t)row * ld + kb);
+            } else {
+                uint32_t w[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int k = kb + 2 * q;
+                    const bf16 lo = k < kend ? (trans ? X[(size_t)k * ld + row] : X[(size_t)row * ld + k]) : zero;
+                    const bf16 hi =
+                        k + 1 < kend ? (trans ? X[(size_t)(k + 1) * ld + row] : X[(size_t)row * ld + k + 1]) : zero;
+                    w[q] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+                }
+                o = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        *reinterpret_cast<uint4*>(tile + tc_off(r, 8 * c, kGtBK)) = o;
+    }
+}
+
+__global__ void __launch_bounds__(kGtThreads) k_gemm_tc(int M, int N, int K, const bf16* __restrict__ A, int lda, int ta,
+                                                        const bf16* __restrict__ B, int ldb, int tb, float* C, int ldc,
+                                                        bf16* Cb, int ldcb, float* Cz, const float* __restrict__ bias,
+                                                        int act, float beta, int kchunk, int BN) {
+    extern __shared__ unsigned char gt_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)gt_raw + 1023) & ~(uintptr_t)1023);
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + 2 * kGtStage);   // [2]
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(sm + 2 * kGtStage + 16);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.y * kGtBM, n0 = blockIdx.x * BN;
+    const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+    const unsigned cols = BN <= 32 ? 32u : (BN <= 64 ? 64u : 128u);   // TMEM columns: a power of 2 >= 32
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar + 1)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        __syncwarp();
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
+                     "r"(cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tmem_slot;
+    const unsigned idesc = tc_idesc(kGtBM, BN);
+    const int nk = kend > kbeg ? (kend - kbeg + kGtBK - 1) / kGtBK : 0;
+    unsigned phases = 0u;   // bit s: parity of the next completion of stage s's barrier
+    bool timed_out = false;
+    for (int kt = 0; kt < nk; ++kt) {
+        const int s = kt & 1;
+        unsigned char* As = sm + s * kGtStage;
+        unsigned char* Bs = As + kGtStageA;
+        if (kt >= 2) {   // the MMAs that read this stage two tiles ago are done
+            const bool ok = tc_bar_wait(bar + s, (phases >> s) & 1u, 1ll << 22);
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(&g_mlp_tc_timeout, 1u);
+                tc_bar_wait(bar + s, (phases >> s) & 1u, 1ll << 24);
+                tc_bar_wait(bar + (s ^ 1), (phases >> (s ^ 1)) & 1u, 1ll << 24);
+                timed_out = true;
+                break;
+            }
+            phases ^= 1u << s;
+        }
+        const int k0 = kbeg + kt * kGtBK;
+        gt_load_row(As, tid, A, lda, ta, m0 + tid, M, k0, kend);
+        if (tid < BN) gt_load_row(Bs, tid, B, ldb, tb ? 0 : 1, n0 + tid, N, k0, kend);
+        tc_fence_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const unsigned aa = tc_smem(As), ba = tc_smem(Bs);
+#pragma unroll
+            for (int q = 0; q < kGtBK / 16; ++q)
+                tc_mma(tmem, tc_desc(aa + 256 * q, 128, 1024), tc_desc(ba + 256 * q, 128, 1024), idesc,
+                       (kt > 0 || q > 0) ? 1 : 0);
+            tc_commit(bar + s);
+        }
+    }
+    // all MMAs done: the last stage's commit tracks every earlier MMA of this thread
+    if (!timed_out && nk > 0) {
+        const int s = (nk - 1) & 1;
+        const bool ok = tc_bar_wait(bar + s, (phases >> s) & 1u, 1ll << 22);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) atomicOr(&g_mlp_tc_timeout, 1u);
+            tc_bar_wait(bar + s, (phases >> s) & 1u, 1ll << 24);
+            timed_out = true;
+        }
+    }
+    tc_fence_after();
+    __syncwarp();
+    if (!timed_out) {
+        const bool split = gridDim.z > 1;
+        const int row = m0 + 32 * warp + (tid & 31);
+        const unsigned trow = tmem + ((unsigned)(32 * warp) << 16);
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            uint32_t v[16];
+            if (nk > 0) tc_ld16(trow + c0, v);
+            else
+#pragma unroll
+                for (int q = 0; q < 16; ++q) v[q] = 0u;
+            if (row >= M) continue;
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                const int col = n0 + c0 + q;
+                if (col >= N) continue;
+                float x = __uint_as_float(v[q]);
+                if (split) {
+                    atomicAdd(C + (size_t)row * ldc + col, x);
+                    continue;
+                }
+                if (bias) x += bias[col];
+                if (Cz) Cz[(size_t)row * ldc + col] = x;
+                if (act == 1) x = silu(x);
+                if (C) C[(size_t)row * ldc + col] = beta != 0.f ? beta * C[(size_t)row * ldc + col] + x : x;
+                if (Cb) Cb[(size_t)row * ldcb + col] = __float2bfloat16(x);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(cols) : "memory");
+    }
+}
+
+// the training GEMM on tcgen05 (variant 0): BN = N rounded up to 16, at most 128
+cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, int ta, const bf16* B, int ldb, int tb, float* C, int ldc,
+                 bf16* Cb, int ldcb, float* Cz, const float* bias, int act, float beta, int split, cudaStream_t st) {
+    if (M <= 0 || N <= 0 || K <= 0) return cudaErrorInvalidValue;
+    static bool smem_set = false;
+    if (!smem_set) {
+        const cudaError_t e = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGtSmem);
+        if (e) return e;
+        smem_set = true;
+    }
+    split = max(1, split);
+    int kchunk = (K + split - 1) / split;
+    kchunk = (kchunk + kGtBK - 1) / kGtBK * kGtBK;
+    split = (K + kchunk - 1) / kchunk;
+    const int BN = std::min(kGtMaxBN, (N + 15) / 16 * 16);
+    dim3 grid(div_up(N, BN), div_up(M, kGtBM), split);
+    MPS_COUNT_LAUNCH k_gemm_tc<<<grid, kGtThreads, kGtSmem, st>>>(M, N, K, A, lda, ta, B, ldb, tb, C, ldc, Cb, ldcb, Cz,
+                                                                  bias, act, beta, kchunk, BN);
+    return cudaGetLastError();
 }
 
 // the shared-memory image of W^T (canonical layout) and the biases, built once per
@@ -859,6 +1060,19 @@ CCTStatusType mps_gemm_bf16(int M, int N, int K, const void* A, int lda, int tra
     if (split_k > 1 && (act != 0 || beta != 1.f || !C)) return CCT_PARAMERR;
     cudaError_t e = gemm(M, N, K, (const bf16*)A, lda, transA, (const bf16*)B, ldb, transB, C, ldc, (bf16*)Cb, ldcb, Cz,
                          bias, act, beta, split_k, (cudaStream_t)stream);
+    return e == cudaErrorInvalidValue ? CCT_PARAMERR : cuda_status(e);
+}
+
+CCTStatusType mps_gemm_bf16_variant(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb,
+                                    int transB, float* C, int ldc, void* Cb, int ldcb, float* Cz, const float* bias,
+                                    int act, float beta, int split_k, int variant, void* stream) {
+    if (variant < 0 || variant > 1) return CCT_PARAMERR;
+    if (variant == 0)
+        return mps_gemm_bf16(M, N, K, A, lda, transA, B, ldb, transB, C, ldc, Cb, ldcb, Cz, bias, act, beta, split_k,
+                             stream);
+    if (split_k > 1 && (act != 0 || beta != 1.f || !C)) return CCT_PARAMERR;
+    cudaError_t e = gemm_mma_sync(M, N, K, (const bf16*)A, lda, transA, (const bf16*)B, ldb, transB, C, ldc, (bf16*)Cb,
+                                  ldcb, Cz, bias, act, beta, split_k, (cudaStream_t)stream);
     return e == cudaErrorInvalidValue ? CCT_PARAMERR : cuda_status(e);
 }
 

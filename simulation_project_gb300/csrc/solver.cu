@@ -145,17 +145,29 @@ struct Solver {
     bool fp64() const { return opt.precision == MPS_PREC_FP64; }
 
     // ---- gate of the learned initial guess (MpsSolverOptions::learned_gate) ----
-    // events: learned kernels [0, 1] (solver stream), the multilevel setup they overlap
-    // [2, 3] (second stream), the solve [4, 5]
+    // events on the solver stream: [0] rows ready (warm start, learned guess, multilevel
+    // setup on either stream follow), [1, 2] the first residual of a learned step (the
+    // refinement reuses it, so it is no cost of the guess), [4, 5] the solve.  The span
+    // [0, 4] of a step without the guess (warm start + multilevel setup) is kept as the
+    // baseline; the guess costs what its step's span, less that residual, adds to it.
     cudaEvent_t gate_ev[6] = {};
     int gate_skip = 0, gate_period = 1;
     double gate_rb = 0.0, gate_ra = 0.0;
-    void gate_update(MpsStepStats& S, bool overlapped) {
-        if (cudaStreamSynchronize(st) || cudaStreamSynchronize(st2)) return;
-        float t_l = 0.f, t_m = 0.f, t_s = 0.f;
-        cudaEventElapsedTime(&t_l, gate_ev[0], gate_ev[1]);
-        if (overlapped) cudaEventElapsedTime(&t_m, gate_ev[2], gate_ev[3]);
+    double gate_span_off = -1.0;   // span of the last step without the guess [ms] (< 0: none yet)
+    void gate_update(MpsStepStats& S, bool learned) {
+        if (cudaStreamSynchronize(st)) return;
+        float t_span = 0.f, t_res = 0.f, t_s = 0.f;
+        cudaEventElapsedTime(&t_span, gate_ev[0], gate_ev[4]);
         cudaEventElapsedTime(&t_s, gate_ev[4], gate_ev[5]);
+        if (!learned) {
+            gate_span_off = t_span;
+            return;
+        }
+        cudaEventElapsedTime(&t_res, gate_ev[1], gate_ev[2]);
+        if (gate_span_off < 0.0) {   // no baseline yet: measure one step without the guess
+            gate_skip = 1;
+            return;
+        }
         const int its = S.cg_iterations;
         if (its <= 0 || !(gate_rb > 0.0) || !(gate_ra > 0.0) || !(S.cg_relres > 0.0) || !(S.r0_relres > S.cg_relres))
             return;
@@ -164,7 +176,7 @@ struct Solver {
         const double per_it = std::log(S.r0_relres / S.cg_relres) / its;
         const double saved = std::log(gate_rb / gate_ra) / per_it;
         const double t_it = (double)t_s / its;
-        const double cost = std::max(0.0, (double)t_l - (double)t_m) / t_it;
+        const double cost = ((double)t_span - (double)t_res - gate_span_off) / t_it;
         S.learned_saved_its = (float)saved;
         S.learned_cost_its = (float)cost;
         if (saved < cost) {
@@ -711,7 +723,10 @@ struct Solver {
                 --gate_skip;
                 use_learned = false;
             }
-            const bool gate_measure = use_learned && opt.learned_gate && !fp64();
+            // gated steps time the span from here to the solve (with and without the guess)
+            const bool gated = learned_ready && opt.learned && opt.learned_gate && !fp64();
+            const bool gate_measure = gated && use_learned;
+            if (gated) cudaEventRecord(gate_ev[0], st);
             S.learned_applied = use_learned ? 1 : 0;
             flex_step = flexible_now();
             S.flexible = flex_step ? 1 : 0;
@@ -725,12 +740,13 @@ struct Solver {
             S.warm_start = warm;
             if (use_learned || collect) {
                 timer.mark(PH_LEARNED, st);
+                if (gate_measure) cudaEventRecord(gate_ev[1], st);
                 if (fp64())
                     MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
                                                                                   d.r, d.rhs, 2);
                 else
                     residual_df((const float*)d.nbrw);
-                if (gate_measure) cudaEventRecord(gate_ev[0], st);
+                if (gate_measure) cudaEventRecord(gate_ev[2], st);   // the first residual: the refinement's
                 MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
                 MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
                 MPS_COUNT_LAUNCH k_features<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -749,25 +765,28 @@ struct Solver {
                     } else {
                         MPS_COUNT_LAUNCH k_learned_finish_r<<<kRedBlocks, 256, 0, st>>>(d, 7);
                         residual_ready = true;
-                        if (gate_measure) cudaEventRecord(gate_ev[1], st);
                     }
                 }
                 timer.mark(PH_SETUP, st);
             }
             if (overlap_mg) {
                 cudaStreamWaitEvent(st2, ev_rows, 0);
-                if (gate_measure) cudaEventRecord(gate_ev[2], st2);
                 if (mg_setup(st2)) return CCT_CUDAERR;
-                if (gate_measure) cudaEventRecord(gate_ev[3], st2);
                 cudaEventRecord(ev_mg, st2);
                 cudaStreamWaitEvent(st, ev_mg, 0);
                 mg_setup_done = true;
             }
-            if (gate_measure) cudaEventRecord(gate_ev[4], st);
+            if (gated && !use_learned && !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL) {
+                // the step without the guess sets the multilevel preconditioner up here (it
+                // would at the start of the solve), inside the span the gate compares
+                if (mg_setup(st)) return CCT_CUDAERR;
+                mg_setup_done = true;
+            }
+            if (gated) cudaEventRecord(gate_ev[4], st);
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
-            if (gate_measure) {
+            if (gated) {
                 cudaEventRecord(gate_ev[5], st);
-                gate_update(S, overlap_mg);
+                gate_update(S, use_learned);
             }
             if (use_learned && S.cg_relres > opt.cg_rtol) {
                 // the learned solve did not reach the tolerance: plain Jacobi-CG from the warm start

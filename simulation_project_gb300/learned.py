@@ -18,6 +18,8 @@ P = C.c_void_p
 _SIGS = {
     "mps_gemm_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, P, C.c_int, C.c_int, P, C.c_int, P,
                                 C.c_int, P, P, C.c_int, C.c_float, C.c_int, P]),
+    "mps_gemm_bf16_variant": (C.c_int, [C.c_int, C.c_int, C.c_int, P, C.c_int, C.c_int, P, C.c_int, C.c_int, P,
+                                        C.c_int, P, C.c_int, P, P, C.c_int, C.c_float, C.c_int, C.c_int, P]),
     "mps_mlp_create": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(P)]),
     "mps_mlp_destroy": (None, [P]),
     "mps_mlp_set_params": (C.c_int, [P, P]),
@@ -49,10 +51,14 @@ def _check(rc, what):
 
 
 def gemm_bf16(M, N, K, A, lda, ta, B, ldb, tb, C_, ldc, Cb=None, ldcb=0, Cz=None, bias=None, act=0, beta=0.0,
-              split=1, stream=None):
-    """Device pointers in, see mps_gemm_bf16."""
-    _check(_lib().mps_gemm_bf16(M, N, K, A, lda, ta, B, ldb, tb, C_, ldc, Cb, ldcb, Cz, bias, act, beta, split,
-                                stream), "mps_gemm_bf16")
+              split=1, stream=None, variant=None):
+    """Device pointers in, see mps_gemm_bf16 (variant 0 tcgen05, 1 mma.sync)."""
+    if variant is None:
+        _check(_lib().mps_gemm_bf16(M, N, K, A, lda, ta, B, ldb, tb, C_, ldc, Cb, ldcb, Cz, bias, act, beta, split,
+                                    stream), "mps_gemm_bf16")
+    else:
+        _check(_lib().mps_gemm_bf16_variant(M, N, K, A, lda, ta, B, ldb, tb, C_, ldc, Cb, ldcb, Cz, bias, act, beta,
+                                            split, variant, stream), "mps_gemm_bf16_variant")
 
 
 class Mlp:

@@ -24,9 +24,11 @@ def to_bf16_bits(a):
     return (((b + 0x7FFF + ((b >> 16) & 1)) >> 16) & 0xFFFF).astype(np.uint16)
 
 
+@pytest.mark.parametrize("variant", [0, 1], ids=["tcgen05", "mma_sync"])
 @pytest.mark.parametrize("M,N,K,ta,tb,split", [(64, 64, 32, 0, 0, 1), (100, 128, 48, 0, 0, 1), (128, 16, 1000, 1, 0, 8),
-                                               (333, 128, 16, 0, 1, 1), (16, 128, 517, 1, 0, 4)])
-def test_gemm_bf16_matches_numpy(M, N, K, ta, tb, split):
+                                               (333, 128, 16, 0, 1, 1), (16, 128, 517, 1, 0, 4),
+                                               (1000, 48, 200, 1, 1, 1), (8192, 128, 128, 0, 0, 1)])
+def test_gemm_bf16_matches_numpy(M, N, K, ta, tb, split, variant):
     rng = np.random.default_rng(M + N + K)
     A = rng.normal(0, 1, (K, M) if ta else (M, K)).astype(np.float32)
     B = rng.normal(0, 1, (N, K) if tb else (K, N)).astype(np.float32)
@@ -34,12 +36,35 @@ def test_gemm_bf16_matches_numpy(M, N, K, ta, tb, split):
     C = DeviceArray((M, N), np.float32)
     C.fill_bytes(0)
     gemm_bf16(M, N, K, dA.ptr, M if ta else K, ta, dB.ptr, K if tb else N, tb, C.ptr, N, beta=1.0 if split > 1 else 0.0,
-              split=split)
+              split=split, variant=variant)
     Am = mo.bf16(A.T if ta else A)
     Bm = mo.bf16(B.T if tb else B)
     ref = Am @ Bm
     got = C.download()
     assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max() + 1e-3 * np.sqrt(K) * 1e-2
+
+
+@pytest.mark.parametrize("variant", [0, 1], ids=["tcgen05", "mma_sync"])
+def test_gemm_bf16_epilogue(variant):
+    """Bias, FP32 pre-activation, SiLU, FP32 and BF16 outputs of one GEMM (the forward
+    layer of training) against numpy."""
+    M, N, K = 300, 128, 128
+    rng = np.random.default_rng(7)
+    A = rng.normal(0, 1, (M, K)).astype(np.float32)
+    B = rng.normal(0, 0.1, (K, N)).astype(np.float32)
+    bias = rng.normal(0, 0.5, N).astype(np.float32)
+    dA, dB = DeviceArray.from_host(to_bf16_bits(A)), DeviceArray.from_host(to_bf16_bits(B))
+    dbias = DeviceArray.from_host(bias)
+    C, Z = DeviceArray((M, N), np.float32), DeviceArray((M, N), np.float32)
+    Cb = DeviceArray((M, N), np.uint16)
+    gemm_bf16(M, N, K, dA.ptr, K, 0, dB.ptr, N, 0, C.ptr, N, Cb=Cb.ptr, ldcb=N, Cz=Z.ptr, bias=dbias.ptr, act=1,
+              variant=variant)
+    z = mo.bf16(A) @ mo.bf16(B) + bias
+    y = z / (1 + np.exp(-z))
+    assert np.abs(Z.download() - z).max() <= 1e-3 * np.abs(z).max()
+    assert np.abs(C.download() - y).max() <= 1e-3 * np.abs(y).max()
+    yb = (Cb.download().astype(np.uint32) << 16).view(np.float32)
+    assert np.abs(yb - y).max() <= 1e-2 * np.abs(y).max()
 
 
 def _net(seed=3):
@@ -183,8 +208,11 @@ def test_learned_scaling_runs_flexible_cg_and_the_gate_skips_a_guess_that_does_n
     for i, st in enumerate(rows):
         print(i, st["learned_applied"], round(st["learned_saved_its"], 2), round(st["learned_cost_its"], 2),
               st["cg_iterations"])
-    assert rows[0]["learned_applied"] == 1 and rows[0]["learned_cost_its"] > 0
-    for a, b in zip(rows, rows[1:]):
+    # step 0 runs the guess, step 1 measures the span without it (the baseline)
+    assert rows[0]["learned_applied"] == 1 and rows[1]["learned_applied"] == 0
+    measured = [st for st in rows[2:] if st["learned_applied"]]
+    assert measured and all(st["learned_cost_its"] != 0 for st in measured)
+    for a, b in zip(rows[2:], rows[3:]):
         if a["learned_applied"] and a["learned_saved_its"] < a["learned_cost_its"]:
             assert b["learned_applied"] == 0   # a guess that did not pay sits out the next step
         if not b["learned_applied"]:
