@@ -104,11 +104,14 @@ typedef struct MpsSolverOptions {
     int learned_gate;       /* 1 (default): the learned initial guess runs only while it
                                pays: after each learned step the solver compares the CG
                                iterations it saved (the residual reduction it gave, at the
-                               step's own contraction per iteration) with its cost (its
-                               kernels' CUDA-event time less the multilevel setup it
-                               overlaps, in iterations of the same step); when it costs more,
-                               it is skipped for 1, 2, 4, ... 64 steps before the next trial.
-                               0: it runs every step */
+                               step's own contraction per iteration) with its cost: the
+                               CUDA-event time from the rows' assembly to the solve, less
+                               the first refinement residual it computes for the solve,
+                               minus the same span of the last step without the guess, in
+                               iterations of the same step; when it costs more,
+                               it is skipped for 2, 8, 32, 64 steps before the next trial.
+                               The first step with the guess is followed by one without it
+                               (the span it is compared with).  0: it runs every step */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */

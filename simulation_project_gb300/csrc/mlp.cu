@@ -468,33 +468,59 @@ constexpr int kGtStageB = kGtMaxBN * kGtBK * 2;              // 16 KB
 constexpr int kGtStage = kGtStageA + kGtStageB;
 constexpr size_t kGtSmem = 2 * kGtStage + 64 + 1024;         // 2 stages, barriers, TMEM slot, alignment
 
-// one row (64 k) of a K-major tile from row `row` of a matrix stored with K contiguous
-// (ld elements apart) or transposed (K rows, ld elements apart); zero outside
-__device__ __forceinline__ void gt_load_row(unsigned char* tile, int r, const bf16* __restrict__ X, int ld, int trans,
-                                            int row, int rows, int k0, int kend) {
+// A tile [R][64 k] (K-major, canonical) of a matrix whose rows r0.. (`rows` in all)
+// are K-contiguous in memory (trans = 0: X[row*ld + k]) or row-contiguous (trans = 1:
+// X[k*ld + row]); zero outside the matrix and beyond kend.  The CTA's threads take
+// 16-byte pieces: K-contiguous rows as 8 lanes per 128-byte row piece (coalesced),
+// transposed ones as 8 consecutive rows at one k (coalesced along the rows) written to
+// the 8 rows' K-major slots; pieces that leave the matrix or are misaligned go element
+// by element.
+template <int R>
+__device__ __forceinline__ void gt_load_tile(unsigned char* tile, const bf16* __restrict__ X, int ld, int trans, int r0,
+                                             int rows, int k0, int kend) {
     const bf16 zero = __float2bfloat16(0.f);
-    const bool in = row < rows;
+    auto elem = [&](int row, int k) -> bf16 {
+        return (row < rows && k < kend) ? (trans ? X[(size_t)k * ld + row] : X[(size_t)row * ld + k]) : zero;
+    };
+    constexpr int kPieces = R * kGtBK / 8;   // 16-byte pieces of the tile
 #pragma unroll 1
-    for (int c = 0; c < kGtBK / 8; ++c) {
-        const int kb = k0 + 8 * c;
-        uint4 o = make_uint4(0u, 0u, 0u, 0u);
-        if (in && kb < kend) {
-            if (!trans && kb + 8 <= kend && ((((uintptr_t)(X + (size_t)row * ld + kb)) & 15u) == 0)) {
-                o = *reinterpret_cast<const uint4*>(X + (size_t)row * ld + kb);
-            } else {
-                uint32_t w[4];
+    for (int pc = threadIdx.x; pc < kPieces; pc += kGtThreads) {
+        if (!trans) {
+            const int r = pc >> 3, c = pc & 7;   // row r, k chunk c of 8
+            const int row = r0 + r, kb = k0 + 8 * c;
+            uint4 o = make_uint4(0u, 0u, 0u, 0u);
+            if (row < rows && kb < kend) {
+                const bf16* src = X + (size_t)row * ld + kb;
+                if (kb + 8 <= kend && (((uintptr_t)src) & 15u) == 0) {
+                    o = *reinterpret_cast<const uint4*>(src);
+                } else {
+                    uint32_t w[4];
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int k = kb + 2 * q;
-                    const bf16 lo = k < kend ? (trans ? X[(size_t)k * ld + row] : X[(size_t)row * ld + k]) : zero;
-                    const bf16 hi =
-                        k + 1 < kend ? (trans ? X[(size_t)(k + 1) * ld + row] : X[(size_t)row * ld + k + 1]) : zero;
-                    w[q] = (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+                    for (int q = 0; q < 4; ++q)
+                        w[q] = (uint32_t)__bfloat16_as_ushort(elem(row, kb + 2 * q)) |
+                               ((uint32_t)__bfloat16_as_ushort(elem(row, kb + 2 * q + 1)) << 16);
+                    o = make_uint4(w[0], w[1], w[2], w[3]);
                 }
-                o = make_uint4(w[0], w[1], w[2], w[3]);
             }
+            *reinterpret_cast<uint4*>(tile + tc_off(r, 8 * c, kGtBK)) = o;
+        } else {
+            const int k = pc / (R / 8), g = pc % (R / 8);   // k, group of 8 rows
+            const int row = r0 + 8 * g, kk = k0 + k;
+            uint16_t v[8];
+            const bf16* src = X + (size_t)kk * ld + row;
+            if (kk < kend && row + 8 <= rows && (((uintptr_t)src) & 15u) == 0) {
+                const uint4 o = *reinterpret_cast<const uint4*>(src);
+                v[0] = (uint16_t)(o.x & 0xFFFFu); v[1] = (uint16_t)(o.x >> 16);
+                v[2] = (uint16_t)(o.y & 0xFFFFu); v[3] = (uint16_t)(o.y >> 16);
+                v[4] = (uint16_t)(o.z & 0xFFFFu); v[5] = (uint16_t)(o.z >> 16);
+                v[6] = (uint16_t)(o.w & 0xFFFFu); v[7] = (uint16_t)(o.w >> 16);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) v[q] = __bfloat16_as_ushort(elem(row + q, kk));
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) *reinterpret_cast<uint16_t*>(tile + tc_off(8 * g + q, k, kGtBK)) = v[q];
         }
-        *reinterpret_cast<uint4*>(tile + tc_off(r, 8 * c, kGtBK)) = o;
     }
 }
 
@@ -546,8 +572,18 @@ __global__ void __launch_bounds__(kGtThreads) k_gemm_tc(int M, int N, int K, con
             phases ^= 1u << s;
         }
         const int k0 = kbeg + kt * kGtBK;
-        gt_load_row(As, tid, A, lda, ta, m0 + tid, M, k0, kend);
-        if (tid < BN) gt_load_row(Bs, tid, B, ldb, tb ? 0 : 1, n0 + tid, N, k0, kend);
+        gt_load_tile<kGtBM>(As, A, lda, ta, m0, M, k0, kend);
+        // B^T tile: rows are the n of op(B); B[k*ldb + n] (transB = 0) is row-contiguous
+        switch (BN) {
+            case 16: gt_load_tile<16>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            case 32: gt_load_tile<32>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            case 48: gt_load_tile<48>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            case 64: gt_load_tile<64>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            case 80: gt_load_tile<80>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            case 96: gt_load_tile<96>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            case 112: gt_load_tile<112>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+            default: gt_load_tile<128>(Bs, B, ldb, tb ? 0 : 1, n0, N, k0, kend); break;
+        }
         tc_fence_smem();
         tc_fence_before();
         __syncthreads();

@@ -151,11 +151,11 @@ struct Solver {
     // [0, 4] of a step without the guess (warm start + multilevel setup) is kept as the
     // baseline; the guess costs what its step's span, less that residual, adds to it.
     cudaEvent_t gate_ev[6] = {};
-    int gate_skip = 0, gate_period = 1;
+    int gate_skip = 0, gate_period = 2;
     double gate_rb = 0.0, gate_ra = 0.0;
     double gate_span_off = -1.0;   // span of the last step without the guess [ms] (< 0: none yet)
+    int gate_pending = 0;          // 1 / 2: this step's events (without / with the guess) await reading
     void gate_update(MpsStepStats& S, bool learned) {
-        if (cudaStreamSynchronize(st)) return;
         float t_span = 0.f, t_res = 0.f, t_s = 0.f;
         cudaEventElapsedTime(&t_span, gate_ev[0], gate_ev[4]);
         cudaEventElapsedTime(&t_s, gate_ev[4], gate_ev[5]);
@@ -181,9 +181,9 @@ struct Solver {
         S.learned_cost_its = (float)cost;
         if (saved < cost) {
             gate_skip = gate_period;
-            gate_period = std::min(2 * gate_period, 64);
+            gate_period = std::min(4 * gate_period, 64);
         } else {
-            gate_period = 1;
+            gate_period = 2;
         }
     }
     // inner CG iterations of each refinement pass in the last step (first batch sizes)
@@ -786,7 +786,7 @@ struct Solver {
             if ((rc = fp64() ? solve_fp64(S) : solve_ir(S))) return rc;
             if (gated) {
                 cudaEventRecord(gate_ev[5], st);
-                gate_update(S, use_learned);
+                gate_pending = use_learned ? 2 : 1;   // read after the step's final synchronisation
             }
             if (use_learned && S.cg_relres > opt.cg_rtol) {
                 // the learned solve did not reach the tolerance: plain Jacobi-CG from the warm start
@@ -822,6 +822,10 @@ struct Solver {
         cudaMemcpyAsync(h_int, d.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(h_int + 1, d.istat, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
+        if (gate_pending) {
+            gate_update(S, gate_pending == 2);
+            gate_pending = 0;
+        }
         S.error_flags |= (unsigned)h_int[0];
         S.max_row = h_int[1];
         S.nnz_wide = h_int[2];
