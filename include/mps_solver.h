@@ -99,8 +99,9 @@ typedef struct MpsSolverOptions {
                                mps_solver_set_time_step) */
     int flexible;           /* inner CG: 1 flexible CG (Notay, one direction kept: beta =
                                -(z.q) / (p.q), q = A p of the last direction), -1 plain PCG,
-                               0 (default) flexible while the learned diagonal scaling
-                               (learned bit 1) shapes the preconditioner, else plain */
+                               0 (default) flexible while the preconditioner is not a fixed
+                               symmetric one (fine_smoother 1, or the learned diagonal
+                               scaling, learned bit 1), else plain */
     int learned_gate;       /* 1 (default): the learned initial guess runs only while it
                                pays: after each learned step the solver compares the CG
                                iterations it saved (the residual reduction it gave, at the
@@ -112,6 +113,13 @@ typedef struct MpsSolverOptions {
                                it is skipped for 2, 8, 32, 64 steps before the next trial.
                                The first step with the guess is followed by one without it
                                (the span it is compared with).  0: it runs every step */
+    int fine_smoother;      /* fine level of the multilevel preconditioner: 0 additive Jacobi
+                               (z = m r + P e1); 1 (default) post-smoothing of the coarse
+                               correction through the short-range couplings (the neighbours
+                               within the gradient radius): z = P e1 + w m (r - A_s P e1),
+                               a diagonal-plus-neighbour fine operator, not symmetric, so
+                               the inner solve runs as flexible CG */
+    double smoother_weight; /* w of fine_smoother 1 (default 0.8) */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */

@@ -575,6 +575,113 @@ __global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constan
     }
 }
 
+// ---------------------------------------------------------------------------
+// Post-smoothing of the coarse correction through the short-range couplings
+// (MpsSolverOptions::fine_smoother = 1): z = P e1 + omega m (r - A_s P e1), where A_s
+// is the PPE operator restricted to the neighbours within the gradient radius (its
+// diagonal the full one) and m the fine diagonal preconditioner (1 / A_ii, or the
+// learned scaling of it).  P e1 is constant per cell, so A_s P e1 at row i is a sum over
+// the at most 27 neighbouring cells of the row's couplings lumped per cell: the rows
+// R[slot][i] below, built once per step.  The preconditioner is not symmetric; the
+// inner solve runs as flexible CG.
+// ---------------------------------------------------------------------------
+constexpr int kMgSmThreads = 128;
+// R[s * n + i] = -(sum of c w_ij over interior j of the gradient row of i whose cell is
+// at slot s of i's cell), plus A_ii at the centre slot 13; mask bit s for the nonzero
+// slots.  Slot sums are kept in a per-thread shared-memory column.
+__global__ void __launch_bounds__(kMgSmThreads) k_mg_smoother_rows(const __grid_constant__ Dev d,
+                                                                   const __grid_constant__ Mg mg, float* R,
+                                                                   unsigned* mask) {
+    __shared__ float acc[27 * kMgSmThreads];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    if (!d.inner[i]) {
+        mask[i] = 0u;
+        return;
+    }
+    float* a = acc + threadIdx.x;
+#pragma unroll
+    for (int s = 0; s < 27; ++s) a[s * kMgSmThreads] = 0.f;
+    const unsigned pi = mg.pcc[i];
+    const float re = (float)d.c.re_lap, mind = (float)d.c.mind_lap, c = (float)d.c.coef_lap;
+    const int cnt = min(d.gcnt[i], d.KG);
+    const int* __restrict__ gj = d.gnbr + (size_t)i * d.KG;
+    const float* __restrict__ gr = (const float*)d.gnbrr + (size_t)i * d.KG;
+    for (int k = 0; k < cnt; ++k) {
+        const int j = gj[k];
+        if (!d.inner[j]) continue;
+        const unsigned pj = mg.pcc[j];
+        const int dx = (int)((pj >> 20) & 1023u) - (int)((pi >> 20) & 1023u);
+        const int dy = (int)((pj >> 10) & 1023u) - (int)((pi >> 10) & 1023u);
+        const int dz = (int)(pj & 1023u) - (int)(pi & 1023u);
+        if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1) continue;   // beyond one cell: none
+        const int s = (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1);
+        a[s * kMgSmThreads] -= c * (re / fmaxf(gr[k], mind) - 1.f);
+    }
+    a[13 * kMgSmThreads] += (float)d.diag[i];
+    unsigned m = 0u;
+    const size_t n = (size_t)d.n;
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+        const float v = a[s * kMgSmThreads];
+        R[s * n + i] = v;
+        if (v != 0.f) m |= 1u << s;
+    }
+    mask[i] = m;
+}
+
+// fine level with post-smoothing: z = e1[a] + omega m32 (r - sum_s R[s][i] e1[nb(a, s)])
+// on interior rows (0 elsewhere); r.z (and z.q with qf) as k_mg_fine_z
+template <class TV>
+__global__ void __launch_bounds__(256) k_mg_fine_post(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
+                                                      const TV* __restrict__ r, TV* __restrict__ z, TV* __restrict__ p,
+                                                      const float* __restrict__ m32, int mode, int slot,
+                                                      const TV* __restrict__ qf, const float* __restrict__ R,
+                                                      const unsigned* __restrict__ mask, float omega) {
+    if (d.scal[S_CONV] != 0.0) return;
+    const MgLevel& L1 = mg.L[1];
+    const float* e1 = L1.e2;
+    const size_t n = (size_t)d.n;
+    TV prz = TV(0), pzq = TV(0);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x) {
+        TV zi = TV(0);
+        if (d.inner[i] && mg.agg1[i] < 0) {   // no aggregate: the diagonal term alone
+            zi = (TV)m32[i] * r[i];
+            prz += r[i] * zi;
+            if (qf) pzq += zi * qf[i];
+        } else if (d.inner[i]) {
+            const int a = mg.agg1[i];
+            float t = 0.f;
+            unsigned msk = mask[i];
+            while (msk) {
+                const int s = __ffs(msk) - 1;
+                msk &= msk - 1u;
+                const int b = s == 13 ? a : L1.nb[(size_t)a * 27 + s];
+                if (b >= 0) t = fmaf(R[s * n + i], e1[b], t);
+            }
+            zi = (TV)(e1[a] + omega * m32[i] * ((float)r[i] - t));
+            prz += r[i] * zi;
+            if (qf) pzq += zi * qf[i];
+        }
+        z[i] = zi;
+        if (mode == 1) p[i] = zi;
+    }
+    double v[2] = {(double)prz, (double)pzq}, out[2];
+    if (grid_reduce<2, TV>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        if (mode == 1) {
+            d.scal[S_RZ] = out[0];
+        } else if (qf) {
+            const double pq = d.scal[S_PQ];
+            d.scal[S_BETA] = pq != 0.0 ? -out[1] / pq : 0.0;
+            d.scal[S_RZ] = out[0];
+        } else {
+            const double rz = d.scal[S_RZ];
+            d.scal[S_BETA] = rz != 0.0 ? out[0] / rz : 0.0;
+            d.scal[S_RZ] = out[0];
+        }
+    }
+}
+
 // last level: e2 = A^-1 r with the explicit inverse (one CTA, warp per row)
 __global__ void __launch_bounds__(1024) k_mg_dense_solve(const double* __restrict__ scal, MgLevel lv,
                                                          const float* __restrict__ ainv) {

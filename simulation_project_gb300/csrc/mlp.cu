@@ -610,8 +610,12 @@ __global__ void __launch_bounds__(kGtThreads) k_gemm_tc(int M, int N, int K, con
     tc_fence_after();
     __syncwarp();
     if (!timed_out) {
+        // each warp's 32 rows x 16 columns go through a padded shared-memory block (the
+        // stage buffers are free now) so that a store instruction writes two 16-column
+        // row pieces (64 B each) instead of 32 rows one column apart
         const bool split = gridDim.z > 1;
-        const int row = m0 + 32 * warp + (tid & 31);
+        const int lane = tid & 31;
+        float* blk = reinterpret_cast<float*>(sm) + warp * 32 * 17;
         const unsigned trow = tmem + ((unsigned)(32 * warp) << 16);
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 16) {
@@ -620,12 +624,15 @@ __global__ void __launch_bounds__(kGtThreads) k_gemm_tc(int M, int N, int K, con
             else
 #pragma unroll
                 for (int q = 0; q < 16; ++q) v[q] = 0u;
-            if (row >= M) continue;
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                const int col = n0 + c0 + q;
-                if (col >= N) continue;
-                float x = __uint_as_float(v[q]);
+            for (int q = 0; q < 16; ++q) blk[lane * 17 + q] = __uint_as_float(v[q]);
+            __syncwarp();
+            const int cq = lane & 15, col = n0 + c0 + cq;
+#pragma unroll 4
+            for (int rr = lane >> 4; rr < 32; rr += 2) {
+                const int row = m0 + 32 * warp + rr;
+                if (row >= M || col >= N) continue;
+                float x = blk[rr * 17 + cq];
                 if (split) {
                     atomicAdd(C + (size_t)row * ldc + col, x);
                     continue;
@@ -636,6 +643,7 @@ __global__ void __launch_bounds__(kGtThreads) k_gemm_tc(int M, int N, int K, con
                 if (C) C[(size_t)row * ldc + col] = beta != 0.f ? beta * C[(size_t)row * ldc + col] + x : x;
                 if (Cb) Cb[(size_t)row * ldcb + col] = __float2bfloat16(x);
             }
+            __syncwarp();
         }
     }
     tc_fence_before();

@@ -550,8 +550,11 @@ __device__ __forceinline__ float lap_weight_f32(float d2, float re, float mind, 
 //   NB_LIST       Laplacian rows (SELL-32), gradient rows, PND, sum of weights
 // The warp's butterfly sums are parked in lane k%32 for its k-th target and the
 // epilogues run lane-parallel.
+// FP32 passes are asked to fit 5 CTAs per SM (<= 51 registers): the passes stall on
+// dependent latencies (shared loads, reciprocal square roots), so more resident warps
+// hide more of them
 template <class T, int MODE>
-__global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant__ Dev d) {
+__global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 5 : 1) k_neighbours(const __grid_constant__ Dev d) {
     __shared__ __align__(16) float4 spos[kStageCap];
     __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int rs[9], rl[9], rp[10];
@@ -672,16 +675,17 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         for (int r = 0; r < 9; ++r) {
             const int kb = __shfl_sync(0xffffffffu, bound, r);
             const int len = max(kb, __shfl_sync(0xffffffffu, bound, 16 + r));
+            const int rsr = rs[r], rpr = rp[r];   // run start (global) and stage offset
             for (int b = kb; b < len; b += 32) {
                 const int o = b + lane;
                 const bool valid = o < len;
-                const int j = rs[r] + o;
+                const int j = rsr + o;
                 bool acc = false, gacc = false;
                 T rr = T(0);
                 float rinv = 0.f, rrf = 0.f, wf = 0.f;   // 1 / r, r, Laplacian weight (FP32 path)
                 V3<T> dv = v3(T(0), T(0), T(0));
                 if (valid && j != i) {
-                    const float4 q = staged ? spos[rp[r] + o] : d.opos[j];
+                    const float4 q = staged ? spos[rpr + o] : d.opos[j];
                     const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
                     const float d2f = dist2_f32(dxf, dyf, dzf);
                     if (d2f < re2f) {
@@ -740,7 +744,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 cnt += __popc(bal);
                 if constexpr (MODE != NB_PREDICT) {
                     const unsigned gb = __ballot_sync(0xffffffffu, gacc);
-                    if (gacc) {
+                    if (gb != 0u && gacc) {
                         const int slot = gcnt + __popc(gb & lt);
                         if (slot < d.KG) {
                             grow[slot] = j;

@@ -468,6 +468,10 @@ struct Solver {
         e = e ? e : mk(&mg.part, 27 * (size_t)nmax); e = e ? e : mk(&mg.partd, (size_t)nmax);
         e = e ? e : mk(&mg.rb, (size_t)d.cells + 1);
         e = e ? e : mk(&mg_flag, (size_t)d.cells + 1); e = e ? e : mk(&mg_counts, (size_t)kMgMaxLevels + 1);
+        if (opt.fine_smoother == 1) {
+            e = e ? e : mk(&sm_R, 27 * (size_t)nmax);
+            e = e ? e : mk(&sm_mask, (size_t)nmax);
+        }
         if (e) return CCT_MEMERR;
         if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
         const int smem = (2 * kMgMaxDense * kMgMaxDense + kMgMaxDense) * (int)sizeof(float);
@@ -518,6 +522,9 @@ struct Solver {
             MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, ss>>>(L[l], L[l + 1]);
         const int nd = L[levels].n;
         MPS_COUNT_LAUNCH k_mg_dense_inverse<<<1, 1024, (2 * nd * nd + nd) * sizeof(float), ss>>>(L[levels], mg.ainv);
+        if (fine_post())
+            MPS_COUNT_LAUNCH k_mg_smoother_rows<<<blocks_for(d.n, kMgSmThreads), kMgSmThreads, 0, ss>>>(d, mg, sm_R,
+                                                                                                       sm_mask);
         if (cudaGetLastError()) return CCT_CUDAERR;
         mg_ready = true;
         return CCT_NOERR;
@@ -527,8 +534,12 @@ struct Solver {
     bool flex_step = false;
     bool flexible_now() const {
         if (opt.flexible != 0) return opt.flexible > 0;
-        return learned_ready && (opt.learned & 2) != 0;
+        return fine_post() || (learned_ready && (opt.learned & 2) != 0);
     }
+    // post-smoothing fine level of the multilevel preconditioner (fine_smoother 1)
+    float* sm_R = nullptr;       // [27 n] couplings lumped per neighbouring cell
+    unsigned* sm_mask = nullptr; // [n] nonzero slots
+    bool fine_post() const { return opt.fine_smoother == 1 && sm_R && mg_on && !fp64(); }
     // z = M^-1 r (interior rows), rz; mode 1 also sets p = z and S_RZ, mode 0 S_BETA.
     // restricted = true: level-1 r and the first sweep are already done (by
     // k_mg_update_restrict)
@@ -555,8 +566,9 @@ struct Solver {
         // the level-2 -> level-1 up sweep carries the fine level when no extra level-1
         // sweeps follow it (and the reduction buffer holds its CTAs' partials)
         const int up1_blocks = div_up(L[1].n * 32, 256);
+        const bool post = fine_post();
         // the reduction buffer holds 2 partials per CTA of the fused kernel
-        const bool fuse = lv >= 2 && extra == 0 && up1_blocks <= 2 * kRedBlocks;
+        const bool fuse = !post && lv >= 2 && extra == 0 && up1_blocks <= 2 * kRedBlocks;
         const float* qf = (flex_step && mode == 0) ? d.q32 : nullptr;
         for (int l = lv - 1; l >= (fuse ? 2 : 1); --l)
             MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
@@ -568,7 +580,11 @@ struct Solver {
             MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e2, L[1].e, om);
             std::swap(L[1].e, L[1].e2);
         }
-        MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
+        if (post)
+            MPS_COUNT_LAUNCH k_mg_fine_post<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf, sm_R,
+                                                                                sm_mask, (float)opt.smoother_weight);
+        else
+            MPS_COUNT_LAUNCH k_mg_fine_z<float><<<kRedBlocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
     }
 
     // ---- phases ----
@@ -1396,7 +1412,7 @@ struct MpsSolver {
 
 extern "C" {
 
-static_assert(sizeof(MpsSolverOptions) == 152 && sizeof(MpsStepStats) == 168,
+static_assert(sizeof(MpsSolverOptions) == 160 && sizeof(MpsStepStats) == 168,
               "the option and statistics records are part of the C ABI");
 
 void mps_solver_default_options(MpsSolverOptions* o) {
@@ -1423,6 +1439,8 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->warm_start = -1;
     o->flexible = 0;
     o->learned_gate = 1;
+    o->fine_smoother = 1;
+    o->smoother_weight = 0.8;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -1436,6 +1454,7 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (o.spmv_wide < -1 || o.spmv_wide > 1) return CCT_PARAMERR;
     if (o.warm_start < -1 || o.warm_start > 2) return CCT_PARAMERR;
     if (o.flexible < -1 || o.flexible > 1 || o.learned_gate < 0 || o.learned_gate > 1) return CCT_PARAMERR;
+    if (o.fine_smoother < 0 || o.fine_smoother > 1 || !(o.smoother_weight >= 0.0)) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {
