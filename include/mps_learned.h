@@ -32,7 +32,7 @@ extern "C" {
  * may be NULL.  act: 0 none, 1 SiLU (Cz, if given, receives the pre-activation FP32).
  * split_k > 1 splits the K loop over CTAs and accumulates into C with atomics
  * (beta must be 1 and act 0 then).  Runs on the 5th-generation tensor cores
- * (tcgen05.mma into TMEM, 128 x 16..128 tiles, K in stages of 64); the MLP's forward
+ * (tcgen05.mma into TMEM, 128 x 16..64 tiles, K in stages of 64); the MLP's forward
  * and backward passes of training use it. */
 CCTStatusType mps_gemm_bf16(int M, int N, int K, const void* A, int lda, int transA, const void* B, int ldb,
                             int transB, float* C, int ldc, void* Cb, int ldcb, float* Cz, const float* bias, int act,

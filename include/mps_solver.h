@@ -113,8 +113,8 @@ typedef struct MpsSolverOptions {
                                it is skipped for 2, 8, 32, 64 steps before the next trial.
                                The first step with the guess is followed by one without it
                                (the span it is compared with).  0: it runs every step */
-    int fine_smoother;      /* fine level of the multilevel preconditioner: 0 additive Jacobi
-                               (z = m r + P e1); 1 (default) post-smoothing of the coarse
+    int fine_smoother;      /* fine level of the multilevel preconditioner: 0 (default)
+                               additive Jacobi (z = m r + P e1); 1 post-smoothing of the coarse
                                correction through the short-range couplings (the neighbours
                                within the gradient radius): z = P e1 + w m (r - A_s P e1),
                                a diagonal-plus-neighbour fine operator, not symmetric, so

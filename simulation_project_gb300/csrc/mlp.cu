@@ -450,7 +450,7 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, uint32_t (&v)[16]) {
 // C[M x N] (+)= op(A)[M x K] op(B)[K x N], FP32 accumulate, with the epilogue of
 // k_gemm_bf16 (bias, FP32 pre-activation Cz, SiLU, FP32 C with beta, BF16 Cb;
 // split-K CTAs add into C with FP32 atomics).  A CTA of 4 warps owns a 128 x BN tile
-// (BN = 16..128, a multiple of 16) whose accumulator lives in TMEM (128 lanes x BN
+// (BN = 16..64, a multiple of 16) whose accumulator lives in TMEM (128 lanes x BN
 // FP32 columns).  K advances 64 at a time through two shared-memory stages holding
 // the A tile [128][64] and the B^T tile [BN][64] in the canonical K-major layout
 // without swizzle (tc_off); every thread loads one row of each (rows of A and of B^T
@@ -462,9 +462,11 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, uint32_t (&v)[16]) {
 // tcgen05.ld.  Bounded waits that run out set g_mlp_tc_timeout, wait (bounded) for
 // the MMAs in flight and skip the epilogue.
 // ---------------------------------------------------------------------------
-constexpr int kGtBM = 128, kGtBK = 64, kGtMaxBN = 128, kGtThreads = 128;
+// BN at most 64: twice the CTAs of 128-column tiles on the MLP's 128-wide layers (the
+// training GEMMs are small, so their time is latency, not tensor throughput)
+constexpr int kGtBM = 128, kGtBK = 64, kGtMaxBN = 64, kGtThreads = 128;
 constexpr int kGtStageA = kGtBM * kGtBK * 2;                 // 16 KB
-constexpr int kGtStageB = kGtMaxBN * kGtBK * 2;              // 16 KB
+constexpr int kGtStageB = kGtMaxBN * kGtBK * 2;              // 8 KB
 constexpr int kGtStage = kGtStageA + kGtStageB;
 constexpr size_t kGtSmem = 2 * kGtStage + 64 + 1024;         // 2 stages, barriers, TMEM slot, alignment
 
@@ -655,7 +657,7 @@ __global__ void __launch_bounds__(kGtThreads) k_gemm_tc(int M, int N, int K, con
     }
 }
 
-// the training GEMM on tcgen05 (variant 0): BN = N rounded up to 16, at most 128
+// the training GEMM on tcgen05 (variant 0): BN = N rounded up to 16, at most 64
 cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, int ta, const bf16* B, int ldb, int tb, float* C, int ldc,
                  bf16* Cb, int ldcb, float* Cz, const float* bias, int act, float beta, int split, cudaStream_t st) {
     if (M <= 0 || N <= 0 || K <= 0) return cudaErrorInvalidValue;

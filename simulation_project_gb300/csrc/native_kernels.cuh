@@ -550,11 +550,8 @@ __device__ __forceinline__ float lap_weight_f32(float d2, float re, float mind, 
 //   NB_LIST       Laplacian rows (SELL-32), gradient rows, PND, sum of weights
 // The warp's butterfly sums are parked in lane k%32 for its k-th target and the
 // epilogues run lane-parallel.
-// FP32 passes are asked to fit 5 CTAs per SM (<= 51 registers): the passes stall on
-// dependent latencies (shared loads, reciprocal square roots), so more resident warps
-// hide more of them
 template <class T, int MODE>
-__global__ void __launch_bounds__(kNbThreads, sizeof(T) == 4 ? 5 : 1) k_neighbours(const __grid_constant__ Dev d) {
+__global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant__ Dev d) {
     __shared__ __align__(16) float4 spos[kStageCap];
     __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int rs[9], rl[9], rp[10];

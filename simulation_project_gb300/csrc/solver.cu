@@ -1439,7 +1439,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->warm_start = -1;
     o->flexible = 0;
     o->learned_gate = 1;
-    o->fine_smoother = 1;
+    o->fine_smoother = 0;
     o->smoother_weight = 0.8;
 }
 

@@ -132,8 +132,8 @@ def test_multilevel_cuts_iterations_and_is_deterministic():
 
 def test_post_smoother_cuts_iterations_with_flexible_cg():
     """The fine level's post-smoothing through the short-range couplings (fine_smoother
-    1, the default) reaches the same 1e-8 residual in fewer inner iterations than the
-    additive Jacobi fine level, runs as flexible CG, and is deterministic."""
+    1) reaches the same 1e-8 residual in fewer inner iterations than the additive Jacobi
+    fine level (the default), runs as flexible CG, and is deterministic."""
     sc = scenes.rotating_bucket(l0=0.006, n_drag=4, drag_index=0.5)
     its, press = {}, []
     for fs in (0, 1, 1):

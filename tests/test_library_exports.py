@@ -66,7 +66,7 @@ def test_default_options_through_the_python_mirror(so):
     assert o.preconditioner == 1 and o.mg_omega == 1.3 and o.compress_rows == 1 and o.mg_sweeps == 1
     assert o.matrix_free == 0 and o.spmv_stream == 1 and o.inner_weights == 16 and o.spmv_wide == 0
     assert o.warm_start == -1 and o.flexible == 0 and o.learned_gate == 1
-    assert o.fine_smoother == 1 and o.smoother_weight == 0.8
+    assert o.fine_smoother == 0 and o.smoother_weight == 0.8
 
 
 @pytest.mark.parametrize("bad", [{"matrix_free": 3}, {"spmv_stream": 2}, {"inner_weights": 8}, {"spmv_wide": 2},
