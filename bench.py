@@ -248,16 +248,18 @@ def run_gpu(args):
     plain_roof = plain_fp64_roofline(scene, args, peak_gbs)
 
     # FP32 / FP64-refined solver without the network: Jacobi, then multilevel
-    ir = Solver(scene, precision="fp32_ir", profile=0, preconditioner=0)
+    # the FP32 arms all run with the phase timers on, as the metric's solver does (its
+    # SpMV roofline needs them), so that they compare like for like
+    ir = Solver(scene, precision="fp32_ir", profile=1, preconditioner=0)
     ms_ir, _, st_ir = time_steps(ir, args.steps, args.warmup)
     ir.close()
     pps_ir = n * args.steps / (ms_ir / 1e3)
-    irm = Solver(scene, precision="fp32_ir", profile=0, preconditioner=1)
+    irm = Solver(scene, precision="fp32_ir", profile=1, preconditioner=1)
     ms_irm, _, st_irm = time_steps(irm, args.steps, args.warmup)
     irm.close()
     pps_irm = n * args.steps / (ms_irm / 1e3)
     # the same from the previous pressure (no extrapolation of the pressure history)
-    irm0 = Solver(scene, precision="fp32_ir", profile=0, preconditioner=1, warm_start=0)
+    irm0 = Solver(scene, precision="fp32_ir", profile=1, preconditioner=1, warm_start=0)
     ms_irm0, _, st_irm0 = time_steps(irm0, args.steps, args.warmup)
     irm0.close()
     pps_irm0 = n * args.steps / (ms_irm0 / 1e3)
@@ -338,6 +340,7 @@ def run_gpu(args):
     sort = sort_bench(n, scene.box.cell_num, peak_gbs)
     mlp = mlp_bench(params, n, load_bf16_peak())
     training_gemms = gemm_bench(load_bf16_peak())
+    ref_named = reference_named_bench()
     accuracy = accuracy_vs_fp64(scene, params, args, steps=args.accuracy_steps)
 
     result = {
@@ -400,6 +403,7 @@ def run_gpu(args):
         "sort": sort,
         "mlp_inference": mlp,
         "mlp_training_gemms": training_gemms,
+        "reference_named_step": ref_named,
         "accuracy_vs_fp64": accuracy,
         "e2e": e2e,
         "frames": frames,
@@ -475,6 +479,33 @@ def mlp_bench(params, n, tflops_peak, reps=20):
     X.free()
     Y.free()
     m.close()
+    return out
+
+
+def reference_named_bench(steps=5, warmup=2):
+    """The reference's explicit schedule through the reference-named launchers
+    (simulation_project_gb300.refpath.RefStep: CCellSet's device arrays bound once, one
+    step of CMultiGPUHandler::Calculate per call): wall time per step, including the
+    host synchronisations the reference's launcher API implies (compaction count, the
+    sort on the legacy stream), on the bench bucket at l0 = 0.002 and 0.004."""
+    from simulation_project_gb300 import lib
+    from simulation_project_gb300.refpath import RefStep
+    out = {"scheme": "explicit (equation-of-state) pressure, the reference's own schedule and kernels' arithmetic"}
+    for name, l0 in (("l0_0.002", 0.002), ("l0_0.004", 0.004)):
+        sc = build_scene(l0)
+        g = RefStep(sc)
+        for i in range(warmup):
+            g.step(i)
+        g.sync()
+        lib.call("mps_device_sync")
+        t0 = time.perf_counter()
+        for i in range(steps):
+            g.step(warmup + i)
+        g.sync()
+        dt = time.perf_counter() - t0
+        out[name] = {"particles": sc.n, "steps": steps, "ms_per_step": round(dt * 1e3 / steps, 3),
+                     "particle_steps_per_s": sc.n * steps / dt}
+        g.close()
     return out
 
 
