@@ -149,3 +149,35 @@ class RefStep:
         self.tp.free()
         self.dp.free()
         self.d = {}
+
+
+def main(argv=None):
+    """python -m simulation_project_gb300.refpath [--l0 L] [--steps K] [--warmup W]: the
+    explicit reference schedule on the rotating bucket through the reference-named
+    launchers, wall time per step (the command the launch-list profile runs)."""
+    import argparse
+    import json
+    import time
+    from . import scenes
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--l0", type=float, default=0.002)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=2)
+    a = ap.parse_args(argv)
+    sc = scenes.rotating_bucket(l0=a.l0, dt=5e-5, seed=4, n_drag=64, drag_seed=3)
+    g = RefStep(sc)
+    for i in range(a.warmup):
+        g.step(i)
+    g.sync()
+    t0 = time.perf_counter()
+    for i in range(a.steps):
+        g.step(a.warmup + i)
+    g.sync()
+    dt = time.perf_counter() - t0
+    g.close()
+    print(json.dumps({"particles": sc.n, "steps": a.steps, "ms_per_step": dt * 1e3 / max(a.steps, 1)}))
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
