@@ -545,7 +545,8 @@ __device__ __forceinline__ float lap_weight_f32(float d2, float re, float mind, 
 // Neighbour passes, CTA per non-empty cell.  The 9 (x, y) columns of the 27-cell
 // neighbourhood are contiguous z-runs in the sorted order; their positions are
 // staged in shared memory (float4), a warp takes one target particle at a time and
-// its lanes test 32 candidates per round.  MODE:
+// its lanes test 32 candidates per round, in a z window of each run found by binary
+// search on the global z bin (w of opos).  MODE:
 //   NB_PREDICT    Laplacian of the velocity -> viscosity/gravity/drag predictor
 //   NB_LIST       Laplacian rows (SELL-32), gradient rows, PND, sum of weights
 // The warp's butterfly sums are parked in lane k%32 for its k-th target and the
@@ -555,6 +556,10 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
     __shared__ __align__(16) float4 spos[kStageCap];
     __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int rs[9], rl[9], rp[10];
+    // per-warp queues of accepted candidates (FP32 path): index and squared distance;
+    // a round adds at most 32 to fewer than 32 waiting entries
+    __shared__ int nb_qj[kNbThreads / 32][64];
+    __shared__ float nb_qd[kNbThreads / 32][64];
     const int ci = blockIdx.x;
     if (ci >= *d.cell_count) return;
     const int cell = d.cell_list[ci];
@@ -565,9 +570,7 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         const int x = cx + (int)threadIdx.x / 3 - 1, y = cy + (int)threadIdx.x % 3 - 1;
         int first = -1, last = -1;
         if (x >= 0 && x < G.x && y >= 0 && y < G.y) {
-            for (int dk = -1; dk <= 1; ++dk) {
-                const int z = cz + dk;
-                if (z < 0 || z >= G.z) continue;
+            for (int z = max(cz - 1, 0); z <= min(cz + 1, G.z - 1); ++z) {
                 const int c = cell_key(G, x, y, z);
                 const int st = d.cstart[c];
                 if (st >= 0) {
@@ -669,86 +672,154 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                 }
             }
         }
-        for (int r = 0; r < 9; ++r) {
-            const int kb = __shfl_sync(0xffffffffu, bound, r);
-            const int len = max(kb, __shfl_sync(0xffffffffu, bound, 16 + r));
-            const int rsr = rs[r], rpr = rp[r];   // run start (global) and stage offset
-            for (int b = kb; b < len; b += 32) {
-                const int o = b + lane;
-                const bool valid = o < len;
-                const int j = rsr + o;
-                bool acc = false, gacc = false;
-                T rr = T(0);
-                float rinv = 0.f, rrf = 0.f, wf = 0.f;   // 1 / r, r, Laplacian weight (FP32 path)
-                V3<T> dv = v3(T(0), T(0), T(0));
-                if (valid && j != i) {
-                    const float4 q = staged ? spos[rpr + o] : d.opos[j];
-                    const float dxf = q.x - pf.x, dyf = q.y - pf.y, dzf = q.z - pf.z;
-                    const float d2f = dist2_f32(dxf, dyf, dzf);
-                    if (d2f < re2f) {
-                        if constexpr (sizeof(T) == 8) {
-                            const dbl4 pj = d.pos[j];
-                            const double dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                            const double rd = exact_r(dx, dy, dz);
-                            if (rd < re) {
-                                acc = true;
-                                rr = rd;
-                                dv = v3<T>(dx, dy, dz);
-                            }
-                        } else {
-                            if (d2f < re2s) {
-                                acc = true;
-                                wf = lap_weight_f32(d2f, (float)re, (float)mind, wmax, rinv, rrf);
-                                rr = rrf;
-                                dv = v3<T>(dxf, dyf, dzf);
-                            }
-                        }
+        if constexpr (sizeof(T) == 4) {
+            // FP32: the candidates a round accepts queue up in candidate order; the
+            // weight, the sums and the row stores run on full batches of 32 entries,
+            // so the expensive path executes ~accepted/32 times per target instead of
+            // once per 32-candidate round.  Entry order (hence every row) is unchanged.
+            int* const qj = nb_qj[warp];
+            float* const qd = nb_qd[warp];
+            int qn = 0;
+            auto flush = [&](int nq) {   // the first nq <= 32 entries (nq warp-uniform)
+                const bool on = lane < nq;
+                const int j = on ? qj[lane] : 0;
+                float rinv = 0.f, rrf = 0.f, w = 0.f;
+                if (on) w = lap_weight_f32(qd[lane], (float)re, (float)mind, wmax, rinv, rrf);
+                bool gacc = false;
+                if constexpr (MODE == NB_PREDICT) {
+                    if (on) {
+                        const float4 v = d.ovel[j];
+                        a0 += (v.x - vi.x) * w;
+                        a1 += (v.y - vi.y) * w;
+                        a2 += (v.z - vi.z) * w;
                     }
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, acc);
-                if (acc) {
-                    T w;
-                    if constexpr (sizeof(T) == 4) w = wf;
-                    else w = wdiv<T>(re, rr > mind ? rr : mind) - T(1);
-                    if constexpr (MODE == NB_PREDICT) {
-                        V3<T> vj;
-                        if constexpr (sizeof(T) == 8) {
-                            const dbl4 v = d.vel[j];
-                            vj = v3<T>(v.x, v.y, v.z);
-                        } else {
-                            const float4 v = d.ovel[j];
-                            vj = v3<T>(v.x, v.y, v.z);
-                        }
-                        a0 += (vj.x - vi.x) * w;
-                        a1 += (vj.y - vi.y) * w;
-                        a2 += (vj.z - vi.z) * w;
-                    } else {
-                        const int slot = cnt + __popc(bal & lt);
+                } else {
+                    if (on) {
+                        const int slot = cnt + lane;
                         if (slot < d.K) {
                             nrow[slot * 32] = j;
                             wrow[slot * 32] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
-                        if (rr < reg) {
+                        if (rrf < reg) {
                             gacc = true;
-                            T wg;
-                            if constexpr (sizeof(T) == 4) wg = rr > mindg ? __fmaf_rn(reg, rinv, -1.f) : wgmax;
-                            else wg = wdiv<T>(reg, rr > mindg ? rr : mindg) - T(1);
-                            a2 += wg;                              // PND
+                            a2 += rrf > mindg ? __fmaf_rn(reg, rinv, -1.f) : wgmax;   // PND
                         }
                     }
-                }
-                cnt += __popc(bal);
-                if constexpr (MODE != NB_PREDICT) {
                     const unsigned gb = __ballot_sync(0xffffffffu, gacc);
                     if (gb != 0u && gacc) {
                         const int slot = gcnt + __popc(gb & lt);
                         if (slot < d.KG) {
                             grow[slot] = j;
-                            grrow[slot] = rr;
+                            grrow[slot] = rrf;
                         }
                     }
                     gcnt += __popc(gb);
+                }
+                cnt += nq;
+            };
+            for (int r = 0; r < 9; ++r) {
+                const int kb = __shfl_sync(0xffffffffu, bound, r);
+                const int len = max(kb, __shfl_sync(0xffffffffu, bound, 16 + r));
+                const int rsr = rs[r], rpr = rp[r];   // run start (global) and stage offset
+                for (int b = kb; b < len; b += 32) {
+                    const int o = b + lane;
+                    const int j = rsr + o;
+                    bool acc = false;
+                    float d2f = 0.f;
+                    if (o < len && j != i) {
+                        const float4 q = staged ? spos[rpr + o] : d.opos[j];
+                        d2f = dist2_f32(q.x - pf.x, q.y - pf.y, q.z - pf.z);
+                        acc = d2f < re2s;
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, acc);
+                    if (acc) {
+                        const int pos = qn + __popc(bal & lt);
+                        qj[pos] = j;
+                        qd[pos] = d2f;
+                    }
+                    qn += __popc(bal);
+                    if (qn >= 32) {
+                        __syncwarp();
+                        flush(32);
+                        // the entries past the batch move to the front of the queue
+                        const int rest = qn - 32;
+                        int mj = 0;
+                        float md = 0.f;
+                        if (lane < rest) {
+                            mj = qj[32 + lane];
+                            md = qd[32 + lane];
+                        }
+                        __syncwarp();
+                        if (lane < rest) {
+                            qj[lane] = mj;
+                            qd[lane] = md;
+                        }
+                        __syncwarp();
+                        qn = rest;
+                    }
+                }
+            }
+            __syncwarp();
+            if (qn > 0) flush(qn);
+            __syncwarp();   // the queue is reused for the warp's next target
+        } else {
+            // FP64: the FP32 distance screens, the exact FP64 distance decides
+            for (int r = 0; r < 9; ++r) {
+                const int kb = __shfl_sync(0xffffffffu, bound, r);
+                const int len = max(kb, __shfl_sync(0xffffffffu, bound, 16 + r));
+                const int rsr = rs[r], rpr = rp[r];   // run start (global) and stage offset
+                for (int b = kb; b < len; b += 32) {
+                    const int o = b + lane;
+                    const bool valid = o < len;
+                    const int j = rsr + o;
+                    bool acc = false, gacc = false;
+                    T rr = T(0);
+                    if (valid && j != i) {
+                        const float4 q = staged ? spos[rpr + o] : d.opos[j];
+                        const float d2f = dist2_f32(q.x - pf.x, q.y - pf.y, q.z - pf.z);
+                        if (d2f < re2f) {
+                            const dbl4 pj = d.pos[j];
+                            const double rd = exact_r(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
+                            if (rd < re) {
+                                acc = true;
+                                rr = rd;
+                            }
+                        }
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, acc);
+                    if (acc) {
+                        const T w = wdiv<T>(re, rr > mind ? rr : mind) - T(1);
+                        if constexpr (MODE == NB_PREDICT) {
+                            const dbl4 v = d.vel[j];
+                            a0 += (v.x - vi.x) * w;
+                            a1 += (v.y - vi.y) * w;
+                            a2 += (v.z - vi.z) * w;
+                        } else {
+                            const int slot = cnt + __popc(bal & lt);
+                            if (slot < d.K) {
+                                nrow[slot * 32] = j;
+                                wrow[slot * 32] = w;
+                            }
+                            a0 += w;                                   // sum of Laplacian weights
+                            if (rr < reg) {
+                                gacc = true;
+                                a2 += wdiv<T>(reg, rr > mindg ? rr : mindg) - T(1);   // PND
+                            }
+                        }
+                    }
+                    cnt += __popc(bal);
+                    if constexpr (MODE != NB_PREDICT) {
+                        const unsigned gb = __ballot_sync(0xffffffffu, gacc);
+                        if (gb != 0u && gacc) {
+                            const int slot = gcnt + __popc(gb & lt);
+                            if (slot < d.KG) {
+                                grow[slot] = j;
+                                grrow[slot] = rr;
+                            }
+                        }
+                        gcnt += __popc(gb);
+                    }
                 }
             }
         }

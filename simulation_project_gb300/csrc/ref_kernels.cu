@@ -888,6 +888,9 @@ CCTStatusType reorderDataAndFindCellStart(cudaStream_t& Stream, Integer numParti
     return launch_status();
 }
 
+// tile sums of the multi-CTA scan (NULL when the slot cannot be had: one-CTA scan)
+static unsigned* scan_sums() { return (unsigned*)scratch_get(8, sizeof(unsigned) * scan_tile_sums_capacity()); }
+
 // thrust::sort_by_key replacement: stable LSD radix sort on the legacy default
 // stream, keys of any int range (one min/max pass picks the digits to sort).
 CCTStatusType SortUsingThrust(Integer MaxParticleNum, Integer* daNumberHash, Integer* daNumberIndex) {
@@ -924,7 +927,7 @@ CCTStatusType CheckParticleOutsideComputeZone(cudaStream_t& Stream, Integer* Par
     MPS_CUDA_TRY(cudaMemsetAsync(removed, 0, sizeof(int), Stream));
     MPS_COUNT_LAUNCH k_ref_outside_flags<<<grid_of(n), kBlock, 0, Stream>>>(n, g_bind, flag);
     MPS_CUDA_TRY(cudaMemcpyAsync(rank, flag, sizeof(unsigned) * (size_t)n, cudaMemcpyDeviceToDevice, Stream));
-    MPS_CUDA_TRY(scan_exclusive(rank, n, nullptr, Stream));
+    MPS_CUDA_TRY(scan_exclusive(rank, n, nullptr, Stream, scan_sums()));
     MPS_COUNT_LAUNCH k_ref_compact<<<grid_of(n), kBlock, 0, Stream>>>(n, g_bind, flag, rank, removed);
     int r = 0;
     MPS_CUDA_TRY(cudaMemcpyAsync(&r, removed, sizeof(int), cudaMemcpyDeviceToHost, Stream));
@@ -948,7 +951,7 @@ CCTStatusType RegisterTriangleTopology(cudaStream_t& Stream, CTriangle* daTriang
     if (!off) return CCT_MEMERR;
     unsigned* total_dev = off + t;
     MPS_COUNT_LAUNCH k_tri_count<<<grid_of(t), kBlock, 0, Stream>>>(t, daTriangle, g_bind.box, CellNum, off);
-    MPS_CUDA_TRY(scan_exclusive(off, t, total_dev, Stream));
+    MPS_CUDA_TRY(scan_exclusive(off, t, total_dev, Stream, scan_sums()));
     unsigned nv = 0;
     MPS_CUDA_TRY(cudaMemcpyAsync(&nv, total_dev, sizeof(unsigned), cudaMemcpyDeviceToHost, Stream));
     MPS_CUDA_TRY(cudaStreamSynchronize(Stream));
