@@ -6,9 +6,12 @@
  *
  * Network: 12 features -> 128 -> 128 -> 128 (SiLU) -> 2 outputs (pressure increment
  * in units of the step's pressure scale, log of the diagonal preconditioner scale).
- * Weights are BF16 on the tensor cores, accumulation and the master copy are FP32.
- * Training (forward with kept pre-activations, backward, Adam) and inference run on
- * the 5th-generation tensor cores (tcgen05).
+ * Training (forward with kept pre-activations, backward, Adam) runs on the
+ * 5th-generation tensor cores (tcgen05) with BF16 weights and activations, FP32
+ * accumulation and an FP32 master copy.  Inference (mps_mlp_forward) runs on them too,
+ * in FP16: weights, activations and the hidden layers' accumulators FP16 (11
+ * significant bits against BF16's 8), the biases carried in the MMA through columns of
+ * ones (split into two FP16 parts), the output layer accumulated in FP32.
  * Parameter vector layout (FP32, MPS_MLP_PARAMS = 34,946 floats):
  *   W1[12][128] b1[128] W2[128][128] b2[128] W3[128][128] b3[128] W4[128][2] b4[2]
  * (W[k][n]: input k, output n).
@@ -51,8 +54,9 @@ CCTStatusType mps_mlp_set_params(MpsMlp* m, const float* host_params);
 CCTStatusType mps_mlp_get_params(MpsMlp* m, float* host_params);
 /* Y[M][2] = MLP(X[M][12]) (device FP32) */
 CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* stream);
-/* the same with a chosen kernel: 0 the tcgen05 kernel mps_mlp_forward uses, 1 the
- * warp-level mma.sync kernel (a cross-check) */
+/* the same with a chosen kernel: 0 the tcgen05 FP16 kernel mps_mlp_forward uses, 1 the
+ * warp-level mma.sync kernel with the BF16 / FP32 rounding points of training (a
+ * cross-check) */
 CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, int variant, void* stream);
 /* nonzero if an MMA completion wait of the tcgen05 kernel ever ran out (the kernel then
  * stops early; its outputs are incomplete) */

@@ -13,9 +13,12 @@
 // The network is tiny (69 kFLOP per particle per forward), so these kernels are a
 // small part of a solver step; they exist so the network is trained on the GPU by
 // this library's own kernels.  The solver's inference runs on the 5th-generation
-// tensor cores (k_mlp_infer_tc: tcgen05.mma into TMEM, weights staged by one bulk
-// copy); the fused mma.sync inference kernel (k_mlp_infer) is kept as its cross-check.
+// tensor cores in FP16 (k_mlp_infer_tc: tcgen05.mma into TMEM, four 128-row tiles in
+// flight per SM, weights staged by one bulk copy, biases inside the MMAs, SiLU in
+// packed FP16); the fused mma.sync inference kernel (k_mlp_infer, BF16 and FP32 like
+// training) is kept as its cross-check.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdint.h>
@@ -340,36 +343,63 @@ __global__ void __launch_bounds__(kMiWarps * 32, 1) k_mlp_infer(int M, const flo
     }
 }
 // ---------------------------------------------------------------------------
-// Fused inference on the 5th-generation tensor cores (tcgen05): a persistent CTA of
-// 4 warps takes 128 rows at a time through the four layers.  Operands live in
-// shared memory in the canonical K-major layout without swizzle (core matrices of
-// 8 rows x 16 bytes; the two core matrices of one 16-wide k-step 128 bytes apart,
-// 8-row groups K/8 x 128 bytes apart): the weights W^T [n][k], staged once per CTA
-// by one bulk copy of an image prepared at each parameter update (k_layers_to_tc),
-// and the layer input [row][k].  One thread issues the MMAs of a layer
-// (tcgen05.mma.cta_group::1.kind::f16, BF16 in, FP32 accumulate, M = 128, N = 128 or
-// 16, one instruction per k-step) into 128 TMEM columns and commits them to an
-// mbarrier; after the (bounded) wait each warp reads its 32 TMEM lanes (= rows) with
-// tcgen05.ld, adds the bias, applies SiLU (silu_fast) and writes the BF16 activations
-// as the next layer's A operand.  The rows of the next tile are loaded while the
-// current one runs.  FP32 accumulate + bias and BF16 activations as k_mlp_infer.
+// Fused inference on the 5th-generation tensor cores (tcgen05).  A persistent CTA
+// keeps kTcSlots 128-row tiles in flight, each with its own TMEM accumulator (128
+// columns), its own layer input in shared memory and its own 4 warps (warp w reads
+// TMEM lanes 32 (w % 4) ..): the slot's first thread issues the MMAs of a layer and
+// commits them to the slot's mbarrier mma_done[s]; the 4 warps wait on it, read their
+// rows of the accumulator with tcgen05.ld, apply SiLU and write the FP16 activations as
+// the next layer's A operand, meet at the slot's named barrier, and the first thread
+// issues the next layer.  The slots run independently, so the tensor cores work on
+// one slot's layer while other slots' epilogues run.
+// Operands use the canonical K-major layout without swizzle (core matrices of 8 rows
+// x 16 bytes; the two core matrices of one 16-wide k-step 128 bytes apart, 8-row
+// groups K/8 x 128 bytes apart): the weights W^T [n][k], staged once per CTA by one
+// bulk copy of an image prepared from the FP32 parameters at each update
+// (k_layers_to_tc), and the layer input [row][k] (one [128][144] buffer per slot; the
+// 12 features of layer 1, two ones and two zeros sit in its first 16 columns, read as
+// a K = 16 operand).  MMAs:
+// tcgen05.mma.cta_group::1.kind::f16 with FP16 A and B, FP32 accumulate, M = 128,
+// N = 128 (hidden layers) or 16 (output), one per k-step of 16.
+// The biases ride in the MMAs: every layer input carries two columns of ones (input
+// columns 12 and 13; hidden columns 128 and 129, K = 144) against the bias split into
+// an FP16 high part and the FP16 rounding of its remainder (about 21 significant
+// bits).  The hidden layers accumulate in FP16 (9 k-steps: the partial sums are
+// rounded to 11 significant bits 9 times, about the error of the BF16 activations the
+// FP32-accumulating kernels keep), read two per register (tcgen05.ld .pack::16b); the
+// output layer accumulates in FP32.  SiLU(z) = h (1 + tanh h) with h = z / 2: the
+// image holds the hidden layers' weights and biases times 1/2, so the accumulator is
+// h; tanh is the hardware approximation on two values at once (tanh.approx.f16x2) and
+// h + h tanh h one packed FP16 multiply-add: two instructions per pair of activations
+// and no conversion (the SFU pipe runs only the tanh), FP16 activations.  Every
+// mbarrier wait is bounded; a slot whose wait ran out (any of its threads: the
+// outcome is made uniform with a barrier reduction) sets g_mlp_tc_timeout and the
+// caller's error word and stops, its first thread waiting (bounded) for the MMAs it
+// issued before TMEM is freed.
 // ---------------------------------------------------------------------------
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 128;
-constexpr unsigned kTcTmemCols = 128;
-// byte offsets of the dynamic shared memory
-constexpr int kTcX = 0;                          // [128][16] layer-1 input
-constexpr int kTcA = kTcX + 128 * 16 * 2;        // [128][128] hidden activations
-constexpr int kTcW1 = kTcA + 128 * 128 * 2;      // W1^T [128][16]
-constexpr int kTcW2 = kTcW1 + 128 * 16 * 2;      // W2^T [128][128]
-constexpr int kTcW3 = kTcW2 + 128 * 128 * 2;     // W3^T [128][128]
-constexpr int kTcW4 = kTcW3 + 128 * 128 * 2;     // W4^T [16][128]
-constexpr int kTcB = kTcW4 + 16 * 128 * 2;       // b1, b2, b3 [128], b4 [16] (FP32)
-constexpr int kTcBar = kTcB + (3 * H + 16) * 4;  // 2 mbarriers (16 B) + TMEM address (4 B)
-constexpr size_t kTcSmem = kTcBar + 32 + 1024;   // + room to align the base to 1024 B
-
-constexpr int kTcImage = kTcBar - kTcW1;         // bytes of the weight + bias image
-static_assert(kTcImage % 16 == 0 && kTcW1 % 16 == 0, "bulk copy of the image needs 16-byte multiples");
+constexpr int kTcSlots = 4;
+constexpr int kTcK = H + 16;   // hidden layer input: 128 activations, 2 ones, 14 zeros
+// the weight image (FP16, byte offsets)
+constexpr int kImW1 = 0;                           // W1^T [128][16]  (x 1/2, bias in k = 12, 13)
+constexpr int kImW2 = kImW1 + 128 * FINP * 2;      // W2^T [128][144] (x 1/2, bias in k = 128, 129)
+constexpr int kImW3 = kImW2 + 128 * kTcK * 2;      // W3^T [128][144] (x 1/2)
+constexpr int kImW4 = kImW3 + 128 * kTcK * 2;      // W4^T [16][144]
+constexpr int kTcImage = kImW4 + FOUTP * kTcK * 2; // bytes of the image
+constexpr int kTcABytes = 128 * kTcK * 2;          // one slot's layer input [128][144]
+// shared memory and launch shape of the kernel with NS slots: the slots' layer inputs
+// (the features of layer 1 in the first 16 columns), the image, the mbarriers and the
+// TMEM address; 4 warps per slot
+template <int NS>
+struct TcShape {
+    static constexpr int W = NS * kTcABytes;
+    static constexpr int Bar = W + kTcImage;
+    static constexpr size_t Smem = Bar + 128 + 1024;   // + room to align the base to 1024 B
+    static constexpr int Threads = 4 * NS * 32;
+    static constexpr unsigned TmemCols = 128 * NS <= 256 ? 256u : 512u;   // a power of 2
+    static_assert(kTcImage % 16 == 0 && W % 16 == 0 && Bar % 8 == 0, "bulk copy and mbarrier alignment");
+    static_assert(Smem <= 227 * 1024 && 128 * NS <= 512, "shared memory and TMEM of one CTA");
+};
 
 __device__ unsigned g_mlp_tc_timeout;   // set when an MMA completion wait ran out
 
@@ -386,6 +416,10 @@ __device__ __forceinline__ unsigned long long tc_desc(unsigned saddr, unsigned l
 // instruction descriptor of kind::f16: FP32 D, BF16 A and B, both K-major, N, M
 __host__ __device__ constexpr unsigned tc_idesc(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+// FP16 A and B (format 0), D FP32 (f32acc) or FP16
+__host__ __device__ constexpr unsigned tc_idesc_f16(int M, int N, bool f32acc) {
+    return (f32acc ? (1u << 4) : 0u) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
 }
 __device__ __forceinline__ unsigned tc_smem(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void tc_mma(unsigned tmem_d, unsigned long long a, unsigned long long b, unsigned idesc,
@@ -678,121 +712,192 @@ cudaError_t gemm(int M, int N, int K, const bf16* A, int lda, int ta, const bf16
     return cudaGetLastError();
 }
 
-// the shared-memory image of W^T (canonical layout) and the biases, built once per
-// parameter update so every CTA stages it with one bulk copy
-__global__ void k_layers_to_tc(Layers L) {
+// the shared-memory image of the tcgen05 inference (W^T in the canonical layout, FP16,
+// the biases as high and low FP16 parts in the ones columns), built from the FP32
+// parameters once per update so every CTA stages it with one bulk copy
+__device__ __forceinline__ void put_f16(unsigned char* img, int off, float v) {
+    *reinterpret_cast<__half*>(img + off) = __float2half_rn(v);
+}
+__device__ __forceinline__ void put_bias_f16(unsigned char* img, int off_hi, int off_lo, float b) {
+    const __half hi = __float2half_rn(b);
+    *reinterpret_cast<__half*>(img + off_hi) = hi;
+    *reinterpret_cast<__half*>(img + off_lo) = __float2half_rn(b - __half2float(hi));
+}
+__global__ void k_layers_to_tc(const float* __restrict__ p, Layers L) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned char* img = L.tc - kTcW1;   // offsets below are those of the kernel's shared memory
-    if (e < FINP * H) {
-        const int k = e / H, n = e % H;
-        *reinterpret_cast<bf16*>(img + kTcW1 + tc_off(n, k, FINP)) = L.W1[e];
+    const int o1 = FIN * H, o2 = o1 + H, o3 = o2 + H * H, o4 = o3 + H, o5 = o4 + H * H, o6 = o5 + H, o7 = o6 + H * FOUT;
+    unsigned char* img = L.tc;
+    if (e < FINP * H) {   // W1^T [n][k]
+        const int n = e / FINP, k = e % FINP;
+        const int off = kImW1 + tc_off(n, k, FINP);
+        if (k < FIN) put_f16(img, off, 0.5f * p[k * H + n]);
+        else if (k == FIN) put_bias_f16(img, off, kImW1 + tc_off(n, k + 1, FINP), 0.5f * p[o1 + n]);
+        else if (k > FIN + 1) put_f16(img, off, 0.f);
     }
-    if (e < H * H) {
-        const int k = e / H, n = e % H;
-        *reinterpret_cast<bf16*>(img + kTcW2 + tc_off(n, k, H)) = L.W2[e];
-        *reinterpret_cast<bf16*>(img + kTcW3 + tc_off(n, k, H)) = L.W3[e];
+    if (e < kTcK * H) {   // W2^T, W3^T [n][k]
+        const int n = e / kTcK, k = e % kTcK;
+        const int off2 = kImW2 + tc_off(n, k, kTcK), off3 = kImW3 + tc_off(n, k, kTcK);
+        if (k < H) {
+            put_f16(img, off2, 0.5f * p[o2 + k * H + n]);
+            put_f16(img, off3, 0.5f * p[o4 + k * H + n]);
+        } else if (k == H) {
+            put_bias_f16(img, off2, kImW2 + tc_off(n, k + 1, kTcK), 0.5f * p[o3 + n]);
+            put_bias_f16(img, off3, kImW3 + tc_off(n, k + 1, kTcK), 0.5f * p[o5 + n]);
+        } else if (k > H + 1) {
+            put_f16(img, off2, 0.f);
+            put_f16(img, off3, 0.f);
+        }
     }
-    if (e < H * FOUTP) {
-        const int k = e / FOUTP, n = e % FOUTP;
-        *reinterpret_cast<bf16*>(img + kTcW4 + tc_off(n, k, H)) = L.W4[e];
-    }
-    if (e < 3 * H + 16) {
-        float* bs = reinterpret_cast<float*>(img + kTcB);
-        bs[e] = e < H ? L.b1[e] : e < 2 * H ? L.b2[e - H] : e < 3 * H ? L.b3[e - 2 * H] : L.b4[e - 3 * H];
+    if (e < kTcK * FOUTP) {   // W4^T [n][k], outputs n >= 2 zero
+        const int n = e / kTcK, k = e % kTcK;
+        const int off = kImW4 + tc_off(n, k, kTcK);
+        if (n >= FOUT) put_f16(img, off, 0.f);
+        else if (k < H) put_f16(img, off, p[o6 + k * FOUT + n]);
+        else if (k == H) put_bias_f16(img, off, kImW4 + tc_off(n, k + 1, kTcK), p[o7 + n]);
+        else if (k > H + 1) put_f16(img, off, 0.f);
     }
 }
 
-// SiLU as z/2 (1 + tanh(z/2)) with the hardware tanh approximation (one MUFU op; its
-// relative error ~2^-11 gives an absolute error <= |z| 2.5e-4, below the BF16 rounding
-// of the activation that follows for |z| < 16)
-__device__ __forceinline__ float tanh_approx(float x) {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float silu_fast(float z) {
-    const float h = 0.5f * z;
-    return fmaf(h, tanh_approx(h), h);
+// SiLU of two FP16 pre-activations given as h = z / 2: h (1 + tanh h) with
+// tanh.approx.f16x2 and one FP16x2 multiply-add
+__device__ __forceinline__ uint32_t silu2_f16(uint32_t h) {
+    uint32_t t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(h));
+    asm("fma.rn.f16x2 %0, %1, %2, %1;" : "=r"(t) : "r"(h), "r"(t));
+    return t;
 }
 
-// hidden-layer epilogue: this thread's row of the 128 accumulator columns + bias,
-// SiLU, BF16 -> the A operand (row r, canonical K-major, K = 128)
-__device__ __forceinline__ void tc_epilogue_hidden(unsigned tmem_row, const float* __restrict__ bias,
-                                                   unsigned char* __restrict__ A, int r) {
-#pragma unroll 1
-    for (int c = 0; c < 4; ++c) {
-        uint32_t v[32];
-        tc_ld32(tmem_row + 32 * c, v);
+// 64 consecutive FP16 TMEM columns of this thread's lane, two per register, without
+// waiting (tcgen05.wait::ld before the registers are read)
+__device__ __forceinline__ void tc_ld32_pack16_nowait(unsigned taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.pack::16b.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+        "%13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr));
+}
+// hidden-layer epilogue: this thread's row of the 128 FP16 accumulator columns (both
+// halves loaded before one wait), SiLU -> FP16 A operand of the next layer (row r,
+// canonical K-major, K = 144)
+__device__ __forceinline__ void tc_epilogue_hidden(unsigned tmem_row, unsigned char* __restrict__ A, int r) {
+    uint32_t v[2][32];
+    tc_ld32_pack16_nowait(tmem_row, v[0]);
+    tc_ld32_pack16_nowait(tmem_row + 64, v[1]);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            uint4 o;
-            uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+    for (int c = 0; c < 2; ++c) {
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int j = 8 * q + 2 * e;
-                w[e] = pack_bf16(silu_fast(__uint_as_float(v[j]) + bias[32 * c + j]),
-                                 silu_fast(__uint_as_float(v[j + 1]) + bias[32 * c + j + 1]));
-            }
-            *reinterpret_cast<uint4*>(A + tc_off(r, 32 * c + 8 * q, 128)) = o;
+        for (int q = 0; q < 8; ++q) {
+            const uint4 o = make_uint4(silu2_f16(v[c][4 * q]), silu2_f16(v[c][4 * q + 1]),
+                                       silu2_f16(v[c][4 * q + 2]), silu2_f16(v[c][4 * q + 3]));
+            *reinterpret_cast<uint4*>(A + tc_off(r, 64 * c + 8 * q, kTcK)) = o;
         }
     }
 }
+// two features -> FP16 pair (saturating: the input stays finite)
+__device__ __forceinline__ uint32_t pack_f16(float lo, float hi) {
+    uint32_t h;
+    asm("cvt.rn.satfinite.f16x2.f32 %0, %1, %2;" : "=r"(h) : "f"(hi), "f"(lo));
+    return h;
+}
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(int M, const float* __restrict__ X,
-                                                                 float* __restrict__ Y, Layers L, unsigned* err) {
+// the 128 threads of a slot: a named barrier (ids 1.. ; 0 is __syncthreads) and the
+// same with an OR over a predicate
+__device__ __forceinline__ void slot_sync(int id) { asm volatile("barrier.cta.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool slot_any(int id, bool v) {
+    unsigned r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n barrier.cta.red.or.pred p, %2, 128, q;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((unsigned)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(TcShape<NS>::Threads, 1) k_mlp_infer_tc(int M, const float* __restrict__ X,
+                                                                          float* __restrict__ Y, Layers L,
+                                                                          unsigned* err) {
+    using S = TcShape<NS>;
     extern __shared__ unsigned char tc_raw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>(((uintptr_t)tc_raw + 1023) & ~(uintptr_t)1023);
-    unsigned char* Xs = sm + kTcX;
-    unsigned char* As = sm + kTcA;
-    float* bs = reinterpret_cast<float*>(sm + kTcB);
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + kTcBar);
-    unsigned long long* wbar = bar + 1;
-    unsigned* tmem_slot = reinterpret_cast<unsigned*>(sm + kTcBar + 16);
-    const int tid = threadIdx.x, warp = tid >> 5;
-    // weights and biases: one bulk copy of the prepared image (16-byte aligned, a
-    // multiple of 16 bytes), completed on wbar
+    unsigned long long* mma_done = reinterpret_cast<unsigned long long*>(sm + S::Bar);   // [NS]
+    unsigned long long* drain = mma_done + NS;                                          // [NS]
+    unsigned long long* wbar = mma_done + 2 * NS;
+    unsigned* tmem_slot = reinterpret_cast<unsigned*>(sm + S::Bar + 8 * (2 * NS + 1));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(bar)) : "memory");
+        for (int s = 0; s < NS; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(mma_done + s)) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(drain + s)) : "memory");
+        }
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(wbar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // the weight image: one bulk copy (16-byte aligned, a multiple of 16 bytes),
+        // completed on wbar
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(tc_smem(wbar)),
                      "r"((unsigned)kTcImage)
                      : "memory");
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(tc_smem(sm + kTcW1)), "l"(L.tc), "r"((unsigned)kTcImage), "r"(tc_smem(wbar))
+                     ::"r"(tc_smem(sm + S::W)), "l"(L.tc), "r"((unsigned)kTcImage), "r"(tc_smem(wbar))
                      : "memory");
     }
     if (warp == 0) {
         __syncwarp();   // .aligned: the whole warp, converged (thread 0 just left its branch)
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tmem_slot)),
-                     "r"(kTcTmemCols)
+                     "r"(S::TmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    __syncthreads();   // wbar initialised before anyone polls it
-    bool timed_out = !tc_bar_wait(wbar, 0, 1ll << 22);
-    if (__syncthreads_or(timed_out)) {
+    __syncthreads();   // barriers initialised before anyone polls them
+    bool failed = !tc_bar_wait(wbar, 0, 1ll << 22);
+    if (__syncthreads_or(failed)) {
         if (tid == 0) {
             atomicOr(&g_mlp_tc_timeout, 1u);
             if (err) atomicOr(err, MPS_ERR_STAGE_TIMEOUT);
         }
         tc_bar_wait(wbar, 0, 1ll << 24);   // the copy may still land: wait (bounded) for it
-        timed_out = true;
+        failed = true;
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const unsigned tmem = *tmem_slot;
-    const unsigned tmem_row = tmem + ((unsigned)(32 * warp) << 16);   // this warp's lanes
-    const unsigned xa = tc_smem(Xs), aa = tc_smem(As);
-    const unsigned w1a = tc_smem(sm + kTcW1), w2a = tc_smem(sm + kTcW2), w3a = tc_smem(sm + kTcW3),
-                   w4a = tc_smem(sm + kTcW4);
-    const unsigned id128 = tc_idesc(128, 128), id16 = tc_idesc(128, 16);
-    unsigned phase = 0;
     const int tiles = (M + kTcRows - 1) / kTcRows;
-    // this thread's row of the next tile, loaded one tile ahead
+    const int stride = NS * gridDim.x;   // tiles t = NS * blockIdx.x + s + k * stride
+    constexpr unsigned sbo = kTcK / 8 * 128;   // 8-row group stride of the [128][144] operands
+
+    const int s = warp >> 2, r = 32 * (warp & 3) + lane, bar_id = 1 + s;
+    const bool leader = r == 0;   // issues the slot's MMAs
+    const unsigned tslot = tmem + 128u * (unsigned)s;
+    const unsigned trow = tslot + ((unsigned)(32 * (warp & 3)) << 16);
+    unsigned char* As = sm + s * kTcABytes;
+    const unsigned aa = tc_smem(As);
+    // hidden layers accumulate in FP16, the output layer in FP32
+    const unsigned id128 = tc_idesc_f16(128, 128, false), id16 = tc_idesc_f16(128, 16, true);
+    auto issue = [&](int layer) {   // by the leader, after the slot's barrier
+        tc_fence_after();
+        if (layer == 0) {
+            tc_mma(tslot, tc_desc(aa, 128, sbo), tc_desc(tc_smem(sm + S::W + kImW1), 128, 256), id128, 0);
+        } else {
+            const unsigned wa = tc_smem(sm + S::W + (layer == 1 ? kImW2 : layer == 2 ? kImW3 : kImW4));
+            const unsigned idesc = layer == 3 ? id16 : id128;
+#pragma unroll
+            for (int k = 0; k < kTcK / 16; ++k)
+                tc_mma(tslot, tc_desc(aa + 256 * k, 128, sbo), tc_desc(wa + 256 * k, 128, sbo), idesc, k > 0);
+        }
+        tc_commit(mma_done + s);
+    };
+    // the ones columns of the hidden inputs (written once)
+    *reinterpret_cast<uint4*>(As + tc_off(r, H, kTcK)) = make_uint4(0x3C003C00u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(As + tc_off(r, H + 8, kTcK)) = make_uint4(0u, 0u, 0u, 0u);
+    unsigned ph = 0u;   // parity of the next phase of mma_done[s]
     auto load_row = [&](int t, float4 (&x)[3]) {
-        const int row = t * kTcRows + tid;
+        const int row = t * kTcRows + r;
         if (t < tiles && row < M) {
             const float4* xr = reinterpret_cast<const float4*>(X + (size_t)row * FIN);
 #pragma unroll
@@ -803,78 +908,73 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_infer_tc(int M, const flo
         }
     };
     float4 xn[3];
-    load_row(blockIdx.x, xn);
-    for (int t = blockIdx.x; t < tiles && !timed_out; t += gridDim.x) {
-        const int r = tid, row = t * kTcRows + r;
-        // layer-1 input: this thread's row (12 features, BF16, zero padded to 16)
+    int t = NS * blockIdx.x + s;
+    load_row(t, xn);
+    // a wait of this warp ran out: the slot stops at its next barrier (the barriers
+    // carry the OR of the flag, so every warp of the slot stops there)
+    bool bad = failed;
+    bool stop = false;   // uniform over the slot: taken from a barrier's OR
+    for (; t < tiles && !stop; t += stride) {
+        const int row = t * kTcRows + r;
+        // layer-1 input in the first 16 columns: 12 features (FP16), two ones, two zeros
         {
-            float f[16];
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                f[4 * q] = xn[q].x; f[4 * q + 1] = xn[q].y; f[4 * q + 2] = xn[q].z; f[4 * q + 3] = xn[q].w;
-            }
-#pragma unroll
-            for (int k = 12; k < 16; ++k) f[k] = 0.f;
-            load_row(t + gridDim.x, xn);
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                uint4 o;
-                o.x = pack_bf16(f[8 * h], f[8 * h + 1]);
-                o.y = pack_bf16(f[8 * h + 2], f[8 * h + 3]);
-                o.z = pack_bf16(f[8 * h + 4], f[8 * h + 5]);
-                o.w = pack_bf16(f[8 * h + 6], f[8 * h + 7]);
-                *reinterpret_cast<uint4*>(Xs + tc_off(r, 8 * h, FINP)) = o;
-            }
+            uint4 o0, o1;
+            o0.x = pack_f16(xn[0].x, xn[0].y);
+            o0.y = pack_f16(xn[0].z, xn[0].w);
+            o0.z = pack_f16(xn[1].x, xn[1].y);
+            o0.w = pack_f16(xn[1].z, xn[1].w);
+            o1.x = pack_f16(xn[2].x, xn[2].y);
+            o1.y = pack_f16(xn[2].z, xn[2].w);
+            o1.z = 0x3C003C00u;
+            o1.w = 0u;
+            load_row(t + stride, xn);
+            *reinterpret_cast<uint4*>(As + tc_off(r, 0, kTcK)) = o0;
+            *reinterpret_cast<uint4*>(As + tc_off(r, 8, kTcK)) = o1;
         }
-        // four layers: MMAs by one thread, completion on the mbarrier, epilogue by all
-        for (int layer = 0; layer < 4 && !timed_out; ++layer) {
-            tc_fence_smem();
-            tc_fence_before();
-            __syncthreads();
-            if (tid == 0) {
-                tc_fence_after();
-                if (layer == 0) {
-                    tc_mma(tmem, tc_desc(xa, 128, 256), tc_desc(w1a, 128, 256), id128, 0);
-                } else {
-                    const unsigned wa = layer == 1 ? w2a : layer == 2 ? w3a : w4a;
-                    const unsigned idesc = layer == 3 ? id16 : id128;
-#pragma unroll 1
-                    for (int s = 0; s < 8; ++s)
-                        tc_mma(tmem, tc_desc(aa + 256 * s, 128, 2048), tc_desc(wa + 256 * s, 128, 2048), idesc, s > 0);
-                }
-                tc_commit(bar);
-            }
-            const bool ok = tc_bar_wait(bar, phase, 1ll << 22);
-            if (__syncthreads_or(!ok)) {
-                // flag it, wait (bounded) for the MMAs in flight, then leave
-                if (tid == 0) {
+        tc_fence_smem();
+        tc_fence_before();
+        if ((stop = slot_any(bar_id, bad))) break;
+        if (leader) issue(0);
+        for (int layer = 0; layer < 4; ++layer) {
+            const bool ok = __all_sync(0xffffffffu, tc_bar_wait(mma_done + s, ph, 1ll << 22));
+            if (!ok) {
+                if (lane == 0) {
                     atomicOr(&g_mlp_tc_timeout, 1u);
                     if (err) atomicOr(err, MPS_ERR_STAGE_TIMEOUT);
                 }
-                tc_bar_wait(bar, phase, 1ll << 26);
-                timed_out = true;
-                break;
-            }
-            phase ^= 1u;
-            tc_fence_after();
-            __syncwarp();   // the tcgen05.ld below are .aligned (the polls above diverge)
-            if (layer < 3) {
-                tc_epilogue_hidden(tmem_row, bs + layer * H, As, r);
+                bad = true;
             } else {
-                uint32_t y0, y1;
-                tc_ld2(tmem_row, y0, y1);
-                if (row < M)
-                    *reinterpret_cast<float2*>(Y + (size_t)row * FOUT) =
-                        make_float2(__uint_as_float(y0) + bs[3 * H], __uint_as_float(y1) + bs[3 * H + 1]);
+                ph ^= 1u;
+                tc_fence_after();
+                if (layer < 3) {
+                    tc_epilogue_hidden(trow, As, r);
+                } else {
+                    uint32_t y0, y1;
+                    tc_ld2(trow, y0, y1);
+                    if (row < M)
+                        *reinterpret_cast<float2*>(Y + (size_t)row * FOUT) =
+                            make_float2(__uint_as_float(y0), __uint_as_float(y1));
+                }
+            }
+            tc_fence_smem();
+            tc_fence_before();   // the next MMAs overwrite the accumulator these warps read
+            if (layer < 3) {
+                if ((stop = slot_any(bar_id, bad))) break;
+                if (leader) issue(layer + 1);
             }
         }
+    }
+    if (leader) {
+        // every MMA this thread issued has completed before TMEM is freed
+        tc_commit(drain + s);
+        tc_bar_wait(drain + s, 0, 1ll << 26);
     }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
         __syncwarp();
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTmemCols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TmemCols) : "memory");
     }
 }
 
@@ -1000,7 +1100,7 @@ struct MpsMlp {
     }
     cudaError_t sync_layers(cudaStream_t st) {
         MPS_COUNT_LAUNCH k_params_to_layers<<<div_up(H * H, 256), 256, 0, st>>>(p, L);
-        MPS_COUNT_LAUNCH k_layers_to_tc<<<div_up(H * H, 256), 256, 0, st>>>(L);
+        MPS_COUNT_LAUNCH k_layers_to_tc<<<div_up(kTcK * H, 256), 256, 0, st>>>(p, L);
         return cudaGetLastError();
     }
     // forward over M rows (M <= maxb); keep pre-activations when train
@@ -1072,14 +1172,16 @@ cudaError_t mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, cuda
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (variant == 0) {
         if (!tc_set) {
-            const cudaError_t e =
-                cudaFuncSetAttribute(k_mlp_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+            const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc<kTcSlots>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)TcShape<kTcSlots>::Smem);
             if (e) return e;
             tc_set = true;
         }
         const int tiles = (M + kTcRows - 1) / kTcRows;
-        const int grid = std::max(1, std::min(tiles, 2 * std::max(sms, 1)));
-        MPS_COUNT_LAUNCH k_mlp_infer_tc<<<grid, kTcThreads, kTcSmem, st>>>(M, X, Y, m->L, err);
+        const int grid = std::max(1, std::min(div_up(tiles, kTcSlots), std::max(sms, 1)));   // one CTA per SM
+        MPS_COUNT_LAUNCH k_mlp_infer_tc<kTcSlots>
+            <<<grid, TcShape<kTcSlots>::Threads, TcShape<kTcSlots>::Smem, st>>>(M, X, Y, m->L, err);
         return cudaGetLastError();
     }
     if (!smem_set) {
