@@ -469,11 +469,29 @@ __global__ void k_ref_drag(int n, const __grid_constant__ RefBind b) {
 // 27-cell traversal in the reference order: k outer, j, i inner; particles of a
 // cell in sorted order; neighbours whose out_id (indexed by sorted position, as in
 // the reference) is negative are skipped.
-// LE: neighbours at distance <= re (the temperature operator), else < re
+// LE: neighbours at distance <= re (the temperature operator), else < re.
+// Screen: ref_sqrt never returns less than sqrt(x) (1 - 3e-7) (its Newton step from
+// below gives y <= 1/sqrt(x), the float roundings cost a few ulps), so a finite squared
+// distance >= re^2 (1 + 1e-5) is rejected by the reference's own test and is skipped
+// before the square root; the others take the reference's arithmetic unchanged
+// (+inf is not screened: the reference's sqrt of it is -0, which it accepts).
+__device__ __forceinline__ float ref_screen2(float re) { return re * re * 1.00001f; }
+template <bool LE, class F>
+__device__ __forceinline__ void ref_candidate(int x, const Scalar3& tp, const Scalar3& q, float re, float re2x, float mind,
+                                              F& f) {
+    const float dx = tp.x - q.x, dy = tp.y - q.y, dz = tp.z - q.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;   // ref_dist's sum (no contraction in this file)
+    if (d2 >= re2x && d2 <= 3.402823466e38f) return;
+    float d = ref_sqrt(d2);
+    if (!(LE ? d <= re : d < re)) return;
+    if (d < mind) d = mind;
+    f(x, d, q);
+}
 template <bool LE = false, class F>
 __device__ __forceinline__ void ref_neighbours(const RefBind& b, int id, const Scalar3& tp, int cx, int cy, int cz,
                                                float re, F&& f) {
     const float mind = (float)(re * 1e-3);
+    const float re2x = ref_screen2(re);
     for (int k = -1; k <= 1; ++k)
         for (int j = -1; j <= 1; ++j)
             for (int i = -1; i <= 1; ++i) {
@@ -485,19 +503,15 @@ __device__ __forceinline__ void ref_neighbours(const RefBind& b, int id, const S
                 for (int x = s; x < e; ++x) {
                     if (b.out_id[x] < 0) continue;
                     if (x == id) continue;
-                    const Scalar3 q = b.pos[x];
-                    float d = ref_dist(tp, q);
-                    if (!(LE ? d <= re : d < re)) continue;
-                    if (d < mind) d = mind;
-                    f(x, d, q);
+                    ref_candidate<LE>(x, tp, b.pos[x], re, re2x, mind, f);
                 }
             }
 }
 
-// CalcExplicitly_Kernel (DeviceProcess_Kernel.h:390-582)
-__global__ void k_ref_explicitly(int n, const __grid_constant__ RefBind b) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
+// CalcExplicitly_Kernel (DeviceProcess_Kernel.h:390-582) for target id; nb(tp, cx, cy,
+// cz, re, f) runs the neighbour traversal
+template <class Nb>
+__device__ __forceinline__ void ref_explicitly_body(const RefBind& b, int id, Nb&& nb) {
     const CParameter& P = b.param;
     const int orig = b.id[id];
     const Scalar3 tp = b.pos[id];
@@ -517,7 +531,7 @@ __global__ void k_ref_explicitly(int n, const __grid_constant__ RefBind b) {
     const bool ep = P.bExplicitPressure;
     const bool turb = P.bTurbulance;
     if (cid >= 0 && cid < b.cell_num) {
-        ref_neighbours(b, id, tp, cx, cy, cz, re, [&](int x, float d, const Scalar3& q) {
+        nb(tp, cx, cy, cz, re, [&](int x, float d, const Scalar3& q) {
             const float w = weight(re, d);
             const Scalar3 v1 = b.vel[x];
             lap.x += (v1.x - v0.x) * w;
@@ -682,9 +696,8 @@ __global__ void k_ref_turbulence(int n, const __grid_constant__ RefBind b) {
 }
 
 // CalcExplicitPressure_Kernel (DeviceProcess_Kernel.h:921-1054)
-__global__ void k_ref_pressure(int n, const __grid_constant__ RefBind b) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
+template <class Nb>
+__device__ __forceinline__ void ref_pressure_body(const RefBind& b, int id, Nb&& nb) {
     const CParameter& P = b.param;
     const int orig = b.id[id];
     const Scalar3 tp = b.pos[id];
@@ -702,7 +715,7 @@ __global__ void k_ref_pressure(int n, const __grid_constant__ RefBind b) {
     const float re = P.GradientInfluenceRadiusCoefficient * P.InitialParticleDistance;
     const float coef = P.SonicVelocity * P.SonicVelocity * P.Density / P.ConstantParticleDensity;
     float dens = 0.0f;
-    ref_neighbours(b, id, tp, cx, cy, cz, re, [&](int, float d, const Scalar3&) { dens += weight(re, d); });
+    nb(tp, cx, cy, cz, re, [&](int, float d, const Scalar3&) { dens += weight(re, d); });
     const float riw = b.stl_distance[id].Magnitude;
     float ww = 0.0f;
     if (b.stl_id[id] >= 0 && b.stl_id[id] < b.triangle_num && riw >= 0 && riw <= re)
@@ -719,9 +732,8 @@ __global__ void k_ref_pressure(int n, const __grid_constant__ RefBind b) {
 
 // CalcExplicitPressureGradient_Kernel (DeviceProcess_Kernel.h:1056-1271), without
 // the negative-pressure branch.
-__global__ void k_ref_gradient(int n, const __grid_constant__ RefBind b) {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= n) return;
+template <class Nb>
+__device__ __forceinline__ void ref_gradient_body(const RefBind& b, int id, Nb&& nb) {
     const CParameter& P = b.param;
     const int orig = b.id[id];
     const Scalar3 tp = b.pos[id];
@@ -735,7 +747,7 @@ __global__ void k_ref_gradient(int n, const __grid_constant__ RefBind b) {
     const float re = P.GradientInfluenceRadiusCoefficient * P.InitialParticleDistance;
     Scalar3 gf = s3(0, 0, 0), gw = s3(0, 0, 0);
     const float tpress = b.pressure[id];
-    ref_neighbours(b, id, tp, cx, cy, cz, re, [&](int x, float d, const Scalar3& q) {
+    nb(tp, cx, cy, cz, re, [&](int x, float d, const Scalar3& q) {
         const float pc = (float)(0.5 * (double)(b.pressure[x] + tpress) * (double)weight(re, d));
         gf.x += pc * (q.x - tp.x) / (d * d);
         gf.y += pc * (q.y - tp.y) / (d * d);
@@ -776,7 +788,32 @@ __global__ void k_ref_gradient(int n, const __grid_constant__ RefBind b) {
     }
 }
 
+enum { REF_EXPLICITLY = 0, REF_PRESSURE = 1, REF_GRADIENT = 2 };
+template <int KIND, class Nb>
+__device__ __forceinline__ void ref_op_body(const RefBind& b, int id, Nb&& nb) {
+    if constexpr (KIND == REF_EXPLICITLY) ref_explicitly_body(b, id, nb);
+    else if constexpr (KIND == REF_PRESSURE) ref_pressure_body(b, id, nb);
+    else ref_gradient_body(b, id, nb);
+}
+// one thread per target, the traversal over global memory (the targets of a warp are
+// consecutive in the sorted order: mostly one cell, whose candidates they load together)
+template <int KIND>
+__global__ void k_ref_op(int n, const __grid_constant__ RefBind b) {
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n) return;
+    ref_op_body<KIND>(b, id, [&](const Scalar3& tp, int cx, int cy, int cz, float re, auto&& f) {
+        ref_neighbours(b, id, tp, cx, cy, cz, re, f);
+    });
+}
+
 inline int grid_of(int n) { return div_up(n, kBlock); }
+
+// the operator over targets 0 .. n-1
+template <int KIND>
+cudaError_t ref_op_launch(cudaStream_t st, int n) {
+    MPS_COUNT_LAUNCH k_ref_op<KIND><<<grid_of(n), kBlock, 0, st>>>(n, g_bind);
+    return cudaGetLastError();
+}
 
 CCTStatusType launch_status() { return cuda_status(cudaGetLastError()); }
 
@@ -1005,20 +1042,20 @@ CCTStatusType CalcDragEffect(cudaStream_t& Stream, Integer ComputeParticleNum) {
 CCTStatusType CalcExplicitly(cudaStream_t& Stream, Integer ParticleNum) {
     if (ParticleNum <= 0) return CCT_NOERR;
     if (g_bind.param.bTurbulance && (!g_bind.turb_visc || !g_bind.strain)) return CCT_PARAMERR;
-    MPS_COUNT_LAUNCH k_ref_explicitly<<<grid_of(ParticleNum), kBlock, 0, Stream>>>(ParticleNum, g_bind);
+    MPS_CUDA_TRY(ref_op_launch<REF_EXPLICITLY>(Stream, ParticleNum));
     return launch_status();
 }
 
 CCTStatusType CalcExplicitPressure(cudaStream_t& Stream, Integer ComputeParticleNum) {
     if (ComputeParticleNum <= 0) return CCT_NOERR;
-    MPS_COUNT_LAUNCH k_ref_pressure<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    MPS_CUDA_TRY(ref_op_launch<REF_PRESSURE>(Stream, ComputeParticleNum));
     return launch_status();
 }
 
 CCTStatusType CalcExplicitPressureGradient(cudaStream_t& Stream, Integer ComputeParticleNum) {
     if (ComputeParticleNum <= 0) return CCT_NOERR;
     if (g_bind.param.bNegativePressure) return CCT_PARAMERR;
-    MPS_COUNT_LAUNCH k_ref_gradient<<<grid_of(ComputeParticleNum), kBlock, 0, Stream>>>(ComputeParticleNum, g_bind);
+    MPS_CUDA_TRY(ref_op_launch<REF_GRADIENT>(Stream, ComputeParticleNum));
     return launch_status();
 }
 
