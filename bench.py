@@ -331,6 +331,16 @@ def run_gpu(args):
     nb_ms = phases["ms_predictor"] + phases["ms_list"]
     pair_evals = {"accepted_pairs_per_pass": int(pairs), "accepted_per_particle": round(pairs / n, 1),
                   "passes": 2, "pairs_per_s": 2.0 * pairs / (nb_ms / 1e3) if nb_ms > 0 else None}
+    # each neighbour pass against the HBM roofline with its algorithmic bytes (list: 8 B
+    # per stored entry + 48 B per row; predictor: 96 B per row); both are bound by
+    # instruction issue, which the small fractions show
+    nb_passes = {}
+    for key, ms, nbytes in (("list", phases["ms_list"], 8.0 * pairs + 48.0 * n),
+                            ("predictor", phases["ms_predictor"], 96.0 * n)):
+        gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        nb_passes[key] = {"ms": round(ms, 3), "bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
+                          "hbm_frac": round(gbs / peak_gbs, 4), "bound": "issue"}
+    pair_evals["passes_vs_hbm"] = nb_passes
 
     # end to end through the C-ABI from pinned host buffers
     e2e = run_e2e(fast, args)

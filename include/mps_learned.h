@@ -61,6 +61,12 @@ CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y
 /* nonzero if an MMA completion wait of the tcgen05 kernel ever ran out (the kernel then
  * stops early; its outputs are incomplete) */
 CCTStatusType mps_mlp_tc_timeouts(unsigned* out);
+/* debugging and tests: the number of polls of the inference kernel's MMA completion
+ * waits (negative: the default, 4,194,304; 0: every such wait runs out at once, so the
+ * kernel's stop path runs: each 128-row tile stops after issuing its first layer and
+ * writes no output, the MMAs in flight drain before TMEM is freed).  Synchronises the
+ * device and clears the mps_mlp_tc_timeouts flag. */
+CCTStatusType mps_mlp_debug_wait_spins(long long spins);
 /* loss = mean over rows of (y0-t0)^2 + w1 (y1-t1)^2 and the gradient of every
  * parameter (device FP32, MPS_MLP_PARAMS floats) by the tensor-core backward pass */
 CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T, float w1, float* grad,

@@ -402,6 +402,9 @@ struct TcShape {
 };
 
 __device__ unsigned g_mlp_tc_timeout;   // set when an MMA completion wait ran out
+// polls of the inference kernel's MMA completion waits (mps_mlp_debug_wait_spins)
+constexpr long long kMlpWaitSpins = 1ll << 22;
+__device__ long long g_mlp_tc_wait_spins = kMlpWaitSpins;
 
 // canonical K-major offset (bytes) of element (r, k) of an operand with K columns
 __device__ __forceinline__ int tc_off(int r, int k, int K) {
@@ -936,7 +939,7 @@ __global__ void __launch_bounds__(TcShape<NS>::Threads, 1) k_mlp_infer_tc(int M,
         if ((stop = slot_any(bar_id, bad))) break;
         if (leader) issue(0);
         for (int layer = 0; layer < 4; ++layer) {
-            const bool ok = __all_sync(0xffffffffu, tc_bar_wait(mma_done + s, ph, 1ll << 22));
+            const bool ok = __all_sync(0xffffffffu, tc_bar_wait(mma_done + s, ph, g_mlp_tc_wait_spins));
             if (!ok) {
                 if (lane == 0) {
                     atomicOr(&g_mlp_tc_timeout, 1u);
@@ -1292,6 +1295,15 @@ CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y
 CCTStatusType mps_mlp_tc_timeouts(unsigned* out) {
     if (!out) return CCT_PARAMERR;
     return cuda_status(cudaMemcpyFromSymbol(out, g_mlp_tc_timeout, sizeof(unsigned)));
+}
+
+CCTStatusType mps_mlp_debug_wait_spins(long long spins) {
+    const long long v = spins < 0 ? kMlpWaitSpins : spins;
+    const unsigned zero = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (!e) e = cudaMemcpyToSymbol(g_mlp_tc_wait_spins, &v, sizeof(v));
+    if (!e) e = cudaMemcpyToSymbol(g_mlp_tc_timeout, &zero, sizeof(zero));
+    return cuda_status(e);
 }
 
 CCTStatusType mps_mlp_loss_grad(MpsMlp* m, int M, const float* X, const float* T, float w1, float* grad,

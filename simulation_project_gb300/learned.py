@@ -27,6 +27,7 @@ _SIGS = {
     "mps_mlp_forward": (C.c_int, [P, C.c_int, P, P, P]),
     "mps_mlp_forward_variant": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
     "mps_mlp_tc_timeouts": (C.c_int, [C.POINTER(C.c_uint)]),
+    "mps_mlp_debug_wait_spins": (C.c_int, [C.c_longlong]),
     "mps_mlp_loss_grad": (C.c_int, [P, C.c_int, P, P, C.c_float, P, C.POINTER(C.c_float), P]),
     "mps_mlp_train_step": (C.c_int, [P, C.c_int, P, P, C.c_float, C.c_float, C.POINTER(C.c_float), P]),
 }
@@ -90,6 +91,12 @@ class Mlp:
         v = C.c_uint()
         _check(_lib().mps_mlp_tc_timeouts(C.byref(v)), "mps_mlp_tc_timeouts")
         return int(v.value)
+
+    @staticmethod
+    def debug_wait_spins(spins: int) -> None:
+        """Polls of the tcgen05 inference kernel's MMA completion waits (negative: the
+        default; 0: every wait runs out at once); clears the timeout flag."""
+        _check(_lib().mps_mlp_debug_wait_spins(int(spins)), "mps_mlp_debug_wait_spins")
 
     def loss_grad(self, X_dev, T_dev, M, grad_dev, w1=0.25):
         loss = C.c_float()

@@ -105,6 +105,35 @@ def test_tcgen05_inference_matches_mma_sync_and_oracle(rows):
     assert Mlp.tc_timeouts() == 0
 
 
+def test_tcgen05_inference_wait_that_runs_out():
+    """The stop path of the tcgen05 inference kernel: with its MMA completion waits
+    limited to zero polls every 128-row tile stops after issuing its first layer
+    (the slot's barrier reduction makes the stop uniform, the issuing thread drains its
+    MMAs before TMEM is freed), the timeout flag is set and no output row is written;
+    with the default limit restored the next launch is complete and correct."""
+    m, _ = _net(seed=9)
+    rows = 50021
+    X = np.random.default_rng(6).normal(0, 1, (rows, 12)).astype(np.float32)
+    dX = DeviceArray.from_host(X)
+    want = DeviceArray((rows, 2), np.float32)
+    m.forward(dX.ptr, want.ptr, rows, variant=0)
+    ref = want.download()
+    assert Mlp.tc_timeouts() == 0
+    dY = DeviceArray.from_host(np.full((rows, 2), np.nan, np.float32))
+    try:
+        Mlp.debug_wait_spins(0)
+        m.forward(dX.ptr, dY.ptr, rows, variant=0)
+        lib.call("mps_device_sync")
+        assert Mlp.tc_timeouts() != 0
+        assert np.isnan(dY.download()).all()
+    finally:
+        Mlp.debug_wait_spins(-1)
+    assert Mlp.tc_timeouts() == 0
+    m.forward(dX.ptr, dY.ptr, rows, variant=0)
+    assert np.array_equal(dY.download(), ref)
+    assert Mlp.tc_timeouts() == 0
+
+
 def test_mlp_gradient_matches_oracle():
     m, p = _net(seed=5)
     rng = np.random.default_rng(2)
