@@ -498,6 +498,21 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     TV prz = TV(0), pzq = TV(0);
     if (I < lo.n) {   // warp-uniform; every thread reaches the grid reduction
+        const int rb0 = mg.rb[I], rb1 = mg.rb[I + 1];
+        // the lane's first two rows are loaded before the stencil gathers (they do not
+        // depend on them): one dependent-load chain per warp instead of two
+        constexpr int kPf = 2;
+        TV pr[kPf], pq[kPf];
+        float pm[kPf];
+        bool pin[kPf];
+#pragma unroll
+        for (int u = 0; u < kPf; ++u) {
+            const int i = rb0 + lane + 32 * u;
+            pin[u] = i < rb1 && d.inner[i];
+            pr[u] = pin[u] ? r[i] : TV(0);
+            pm[u] = pin[u] ? m32[i] : 0.f;
+            pq[u] = (pin[u] && qf) ? qf[i] : TV(0);
+        }
         float t = 0.f;
         if (lane < 27) {
             const int J = lo.nb[(size_t)I * 27 + lane];
@@ -507,7 +522,20 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
         const float e1 = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
         if (lane == 0) lo.e2[I] = e1;
-        for (int i = mg.rb[I] + lane; i < mg.rb[I + 1]; i += 32) {
+#pragma unroll
+        for (int u = 0; u < kPf; ++u) {
+            const int i = rb0 + lane + 32 * u;
+            if (i >= rb1) break;
+            TV zi = TV(0);
+            if (pin[u]) {
+                zi = (TV)pm[u] * pr[u] + (TV)e1;
+                prz += pr[u] * zi;
+                if (qf) pzq += zi * pq[u];
+            }
+            z[i] = zi;
+            if (mode == 1) p[i] = zi;
+        }
+        for (int i = rb0 + lane + 32 * kPf; i < rb1; i += 32) {
             TV zi = TV(0);
             if (d.inner[i]) {
                 zi = (TV)m32[i] * r[i] + (TV)e1;
@@ -548,9 +576,13 @@ __global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constan
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     TV prr = TV(0);
+    // the rows of the warp's first aggregate are visited by the grid-stride loop below;
+    // the launch gives (up to the reduction buffer's limit) one aggregate per warp, so
+    // the row range and the rows are one dependent-load chain
     for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < L1.n; I += nw) {
         float s = 0.f;
-        for (int i = mg.rb[I] + lane; i < mg.rb[I + 1]; i += 32) {
+        const int rb0 = mg.rb[I], rb1 = mg.rb[I + 1];
+        for (int i = rb0 + lane; i < rb1; i += 32) {
             if (!d.inner[i]) continue;
             x[i] = x[i] + (TXA)alpha * (TXA)p[i];
             const TV ri = r[i] - alpha * q[i];

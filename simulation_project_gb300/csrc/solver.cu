@@ -1080,7 +1080,9 @@ struct Solver {
                                                                                     flex_step ? 1 : 0);
                 if constexpr (std::is_same<TV, float>::value) {
                     if (use_mg) {
-                        MPS_COUNT_LAUNCH k_mg_update_restrict<TV, TXA><<<kRedBlocks, 256, 0, st>>>(d, mg, x, r, p, q, 1);
+                        // a warp per level-1 aggregate, within the reduction buffer's 2 x kRedBlocks CTAs
+                        const int ur_blocks = std::max(1, std::min(div_up(mg.L[1].n, 8), 2 * kRedBlocks));
+                        MPS_COUNT_LAUNCH k_mg_update_restrict<TV, TXA><<<ur_blocks, 256, 0, st>>>(d, mg, x, r, p, q, 1);
                         timer.mark(PH_PRECOND, st);
                         mg_apply(r, z, p, 0, true);
                         timer.mark(PH_VEC, st);
