@@ -367,6 +367,8 @@ __global__ void k_mg_restrict_fine(const __grid_constant__ Dev d, const __grid_c
 // restricted residual.  The loads are issued in three waves (children; their stencil
 // entries and residuals; the neighbours' corrections) instead of one dependent chain
 // per term, and the terms are summed in the same order.
+// lo.r and lo.e are read through L2 (CG) where other CTAs of the same launch wrote them
+template <bool CG = false>
 __device__ __forceinline__ float mg_child_residual_warp(const MgLevel& lo, const MgLevel& hi, int I2, int lane) {
     const int child = lane < 8 ? hi.child[(size_t)I2 * 8 + lane] : -1;
     int I[7], J[7];
@@ -381,7 +383,7 @@ __device__ __forceinline__ float mg_child_residual_warp(const MgLevel& lo, const
         x[q] = 0.f;
         if (I[q] >= 0) {
             if (s == 27) {
-                x[q] = lo.r[I[q]];
+                x[q] = CG ? __ldcg(lo.r + I[q]) : lo.r[I[q]];
             } else {
                 J[q] = lo.nb[(size_t)I[q] * 27 + s];
                 a[q] = lo.a[(size_t)I[q] * 27 + s];
@@ -390,7 +392,7 @@ __device__ __forceinline__ float mg_child_residual_warp(const MgLevel& lo, const
     }
 #pragma unroll
     for (int q = 0; q < 7; ++q)
-        if (J[q] >= 0) x[q] = lo.e[J[q]];
+        if (J[q] >= 0) x[q] = CG ? __ldcg(lo.e + J[q]) : lo.e[J[q]];
     float v = 0.f;
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
@@ -477,6 +479,93 @@ __global__ void k_mg_up(const double* __restrict__ scal, MgLevel lo, MgLevel hi,
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     if (lane == 0) lo.e2[I] = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
+}
+
+// Bounded barrier of all CTAs of a cooperative launch (every CTA resident): arrive on
+// bar[0], the last arrival resets it and advances the generation bar[1]; a wait that
+// runs out sets MPS_ERR_STAGE_TIMEOUT and returns false (the CTA then stops, so the
+// others run out too).
+__device__ __forceinline__ bool coop_barrier(unsigned* bar, unsigned* err, long long spins) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+            ok = 1;
+        } else {
+            long long k = 0;
+            while (*gen == g && ++k < spins) {
+            }
+            ok = *gen != g;
+            if (!ok) atomicOr(err, MPS_ERR_STAGE_TIMEOUT);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// The coarse part of a V-cycle in one cooperative launch: the restrictions level 1 ->
+// 2 -> ... -> last with their first down sweeps (as k_mg_down, a warp per aggregate of
+// the coarser level), the dense solve of the last level (a warp per row),
+// and the up sweeps of levels last-1 .. 2 (as k_mg_up), with a grid barrier between
+// the stages; the level-2 -> 1 up sweep stays fused with the fine level
+// (k_mg_up_fine_z).  Values other CTAs wrote in this launch are read through L2.
+__global__ void __launch_bounds__(256) k_mg_coarse_cycle(const double* __restrict__ scal, Mg mg,
+                                                         unsigned* __restrict__ bar, unsigned* __restrict__ err) {
+    if (scal[S_CONV] != 0.0) return;   // the same for every CTA of the launch
+    const int lane = threadIdx.x & 31;
+    const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int lv = mg.levels;
+    const float omega = mg.omega;
+    constexpr long long kSpins = 1ll << 20;
+    for (int l = 1; l < lv; ++l) {
+        const MgLevel& lo = mg.L[l];
+        const MgLevel& hi = mg.L[l + 1];
+        for (int I2 = w0; I2 < hi.n; I2 += nw) {   // warp-uniform
+            const float s = l == 1 ? mg_child_residual_warp<false>(lo, hi, I2, lane)
+                                   : mg_child_residual_warp<true>(lo, hi, I2, lane);
+            if (lane == 0) {
+                hi.r[I2] = s;
+                hi.e[I2] = omega * hi.dinv[I2] * s;
+            }
+        }
+        if (!coop_barrier(bar, err, kSpins)) return;
+    }
+    {   // the last level: e2 = A^-1 r with the explicit inverse, a warp per row
+        const MgLevel& L = mg.L[lv];
+        for (int I = w0; I < L.n; I += nw) {
+            float v = 0.f;
+            for (int J = lane; J < L.n; J += 32) v += mg.ainv[I * L.n + J] * __ldcg(L.r + J);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) L.e2[I] = v;
+        }
+    }
+    if (lv <= 2) return;
+    if (!coop_barrier(bar, err, kSpins)) return;
+    for (int l = lv - 1; l >= 2; --l) {
+        const MgLevel& lo = mg.L[l];
+        const MgLevel& hi = mg.L[l + 1];
+        for (int I = w0; I < lo.n; I += nw) {   // warp-uniform
+            float t = 0.f;
+            if (lane < 27) {
+                const int J = lo.nb[(size_t)I * 27 + lane];
+                if (J >= 0)
+                    t = lo.a[(size_t)I * 27 + lane] * (__ldcg(lo.e + J) + __ldcg(hi.e2 + lo.nbp[(size_t)I * 27 + lane]));
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0)
+                lo.e2[I] = __ldcg(lo.e + I) + __ldcg(hi.e2 + lo.par[I]) + omega * lo.dinv[I] * (__ldcg(lo.r + I) - t);
+        }
+        if (l > 2 && !coop_barrier(bar, err, kSpins)) return;
+    }
 }
 
 // the last prolongation and up sweep (level 2 -> level 1) fused with the fine level:

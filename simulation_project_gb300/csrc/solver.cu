@@ -462,8 +462,9 @@ struct Solver {
         }
         mg_grid_levels = std::min(l, kMgMaxLevels);
         e = e ? e : mk(&mg.ainv, (size_t)kMgMaxDense * kMgMaxDense);
-        e = e ? e : mk(&mg.done, 1);
-        if (!e) e = cudaMemset(mg.done, 0, sizeof(unsigned));
+        // [0]: k_mg_down's finished CTAs; [1], [2]: k_mg_coarse_cycle's grid barrier
+        e = e ? e : mk(&mg.done, 3);
+        if (!e) e = cudaMemset(mg.done, 0, 3 * sizeof(unsigned));
         e = e ? e : mk(&mg.agg1, (size_t)nmax); e = e ? e : mk(&mg.pcc, (size_t)nmax);
         e = e ? e : mk(&mg.part, 27 * (size_t)nmax); e = e ? e : mk(&mg.partd, (size_t)nmax);
         e = e ? e : mk(&mg.rb, (size_t)d.cells + 1);
@@ -543,6 +544,25 @@ struct Solver {
     // z = M^-1 r (interior rows), rz; mode 1 also sets p = z and S_RZ, mode 0 S_BETA.
     // restricted = true: level-1 r and the first sweep are already done (by
     // k_mg_update_restrict)
+    // CTAs of the cooperative coarse V-cycle: all resident (SMs x the CTAs that fit),
+    // no more than the level-2 aggregates need (a warp each); 0: not available
+    int coop_resident = -1;
+    unsigned* coop_bar = nullptr;
+    int coarse_cycle_grid() {
+        if (coop_resident < 0) {
+            int dev = 0, sms = 0, per_sm = 0, coop = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+            if (!coop || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mg_coarse_cycle, 256, 0) != cudaSuccess)
+                per_sm = 0;
+            coop_resident = sms * per_sm;
+            coop_bar = mg.done + 1;
+        }
+        if (coop_resident <= 0) return 0;
+        return std::max(1, std::min(coop_resident, div_up(mg.L[2].n, 8)));
+    }
+
     void mg_apply(const float* r, float* z, float* p, int mode, bool restricted = false) {
         MgLevel* L = mg.L;
         const int lv = mg.levels;
@@ -555,14 +575,6 @@ struct Solver {
             MPS_COUNT_LAUNCH k_mg_smooth<<<div_up(L[1].n * 32, 256), 256, 0, st>>>(d.scal, L[1], L[1].e, L[1].e2, om);
             std::swap(L[1].e, L[1].e2);
         }
-        // the last restriction also solves the last level densely (its last CTA, of
-        // 1024 threads like the stand-alone dense solve)
-        for (int l = 1; l < lv; ++l) {
-            const int tpb = l + 1 == lv ? 1024 : 256;
-            MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, tpb), tpb, 0, st>>>(
-                d.scal, L[l], L[l + 1], om, l + 1 == lv ? mg.ainv : nullptr, mg.done);
-        }
-        if (lv == 1) MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
         // the level-2 -> level-1 up sweep carries the fine level when no extra level-1
         // sweeps follow it (and the reduction buffer holds its CTAs' partials)
         const int up1_blocks = div_up(L[1].n * 32, 256);
@@ -570,8 +582,24 @@ struct Solver {
         // the reduction buffer holds 2 partials per CTA of the fused kernel
         const bool fuse = !post && lv >= 2 && extra == 0 && up1_blocks <= 2 * kRedBlocks;
         const float* qf = (flex_step && mode == 0) ? d.q32 : nullptr;
-        for (int l = lv - 1; l >= (fuse ? 2 : 1); --l)
-            MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+        const int cg = fuse ? coarse_cycle_grid() : 0;
+        if (cg > 0) {
+            // levels 2 .. last in one cooperative launch (grid barriers between stages)
+            void* args[] = {(void*)&d.scal, (void*)&mg, (void*)&coop_bar, (void*)&d.err};
+            MPS_COUNT_LAUNCH cudaLaunchCooperativeKernel((const void*)k_mg_coarse_cycle, dim3(cg), dim3(256), args, 0,
+                                                         st);
+        } else {
+            // the last restriction also solves the last level densely (its last CTA, of
+            // 1024 threads like the stand-alone dense solve)
+            for (int l = 1; l < lv; ++l) {
+                const int tpb = l + 1 == lv ? 1024 : 256;
+                MPS_COUNT_LAUNCH k_mg_down<<<div_up(L[l + 1].n * 32, tpb), tpb, 0, st>>>(
+                    d.scal, L[l], L[l + 1], om, l + 1 == lv ? mg.ainv : nullptr, mg.done);
+            }
+            if (lv == 1) MPS_COUNT_LAUNCH k_mg_dense_solve<<<1, 1024, 0, st>>>(d.scal, L[lv], mg.ainv);
+            for (int l = lv - 1; l >= (fuse ? 2 : 1); --l)
+                MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
+        }
         if (fuse) {
             MPS_COUNT_LAUNCH k_mg_up_fine_z<float><<<up1_blocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
             return;
