@@ -73,13 +73,17 @@ struct Dev {
     double* wdir;
     int* wid;
     double* dragv;
-    // neighbour rows
-    int* nbr;
+    // neighbour rows: the list pass writes each row contiguously (row i at i*K: rnbr, rw);
+    // k_rows_sell turns the interior rows into SELL-32 (nbr, nbrw, nbr16, w16)
+    int* rnbr;
+    void* rw;
+    int* nbr;                  // SELL-32 32-bit columns: slices with sbase = -1, or every slice when rows_c32
     void* nbrw;
     unsigned short* nbr16;     // SELL-32 column offsets from the slice base (interior rows)
     int* sbase;                // [slices] smallest column index of the slice, -1: 32-bit slice
     int* skmax;                // [slices] longest interior row of a 16-bit slice, -1: 32-bit slice
     int rows16;                // nbr16 / sbase are valid for the current rows
+    int rows_c32;              // nbr holds the 32-bit columns of every slice
     __half* w16;               // FP16 copies of the FP32 weights (interior rows; inner CG operator)
     double* diag16;            // diagonal of the FP16-weight operator: coef * sum of FP16 weights + kappa
     int rows_w16;              // w16 / diag16 are valid for the current rows

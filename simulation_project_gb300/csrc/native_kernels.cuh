@@ -548,7 +548,7 @@ __device__ __forceinline__ float lap_weight_f32(float d2, float re, float mind, 
 // its lanes test 32 candidates per round, in a z window of each run found by binary
 // search on the global z bin (w of opos).  MODE:
 //   NB_PREDICT    Laplacian of the velocity -> viscosity/gravity/drag predictor
-//   NB_LIST       Laplacian rows (SELL-32), gradient rows, PND, sum of weights
+//   NB_LIST       Laplacian rows (row-major staging), gradient rows, PND, sum of weights
 // The warp's butterfly sums are parked in lane k%32 for its k-th target and the
 // epilogues run lane-parallel.
 template <class T, int MODE>
@@ -628,10 +628,10 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
         const V3<T> vi = load_v<T>(d, i);
         T a0 = 0, a1 = 0, a2 = 0, a3 = 0;   // mode-specific accumulators
         int cnt = 0, gcnt = 0;
-        const size_t row0 = sell_index(i, 0, d.K);   // SELL position of the row's entry 0
-        // the row's first entries (SELL row, gradient row): one wide multiply-add per store
-        int* const nrow = d.nbr + row0;
-        T* const wrow = (T*)d.nbrw + row0;
+        // the row's entries are stored contiguously (row i at i*K; k_rows_sell turns the
+        // interior rows into SELL-32), so a batch of 32 accepted entries is one line
+        int* const nrow = d.rnbr + (size_t)i * d.K;
+        T* const wrow = (T*)d.rw + (size_t)i * d.K;
         int* const grow = d.gnbr + (size_t)i * d.KG;
         T* const grrow = (T*)d.gnbrr + (size_t)i * d.KG;
         // z window of each run for this target: the run (3 cells stacked in z) is sorted
@@ -697,8 +697,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                     if (on) {
                         const int slot = cnt + lane;
                         if (slot < d.K) {
-                            nrow[slot * 32] = j;
-                            wrow[slot * 32] = w;
+                            nrow[slot] = j;
+                            wrow[slot] = w;
                         }
                         a0 += w;                                   // sum of Laplacian weights
                         if (rrf < reg) {
@@ -798,8 +798,8 @@ __global__ void __launch_bounds__(kNbThreads) k_neighbours(const __grid_constant
                         } else {
                             const int slot = cnt + __popc(bal & lt);
                             if (slot < d.K) {
-                                nrow[slot * 32] = j;
-                                wrow[slot * 32] = w;
+                                nrow[slot] = j;
+                                wrow[slot] = w;
                             }
                             a0 += w;                                   // sum of Laplacian weights
                             if (rr < reg) {
@@ -847,7 +847,7 @@ __global__ void k_row_idsum(const __grid_constant__ Dev d, double* out) {
     if (i >= d.n) return;
     double s = 0.0;
     const int cnt = d.nbr_cnt[i];
-    for (int k = 0; k < cnt; ++k) s += (double)d.id[d.nbr[sell_index(i, k, d.K)]];
+    for (int k = 0; k < cnt; ++k) s += (double)d.id[d.rnbr[(size_t)i * d.K + k]];
     out[i] = s;
 }
 
@@ -895,57 +895,93 @@ __device__ __forceinline__ int sell_col(const Dev& d, size_t e, int sb) {
     return __ldcs(d.nbr + e);
 }
 
-// Compressed columns of the interior rows, one read pass: warp per 32-row slice,
-// offsets j - 32*slice as signed 16 bits; a slice with an offset outside
-// [-32768, 32767] keeps its 32-bit columns (sbase = -1, found by a warp vote).
-// With w16: also the FP16 copy of each FP32 weight (round to nearest) and the
-// diagonal of that operator, coef * (sum of the FP16 weights in entry order, in FP32)
-// + kappa, so the FP16-weight operator is again a Laplacian plus kappa.
-__global__ void k_compress_rows(const __grid_constant__ Dev d, int w16) {
-    const int lane = threadIdx.x & 31;
-    const int sl = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// SELL-32 rows of the interior rows from the list pass's row-major rows, one read
+// pass: warp per 32-row slice; each 32-entry chunk of the slice's rows is loaded one
+// 128-byte line per row into a [32][33] shared-memory tile and written back transposed,
+// so entry k of the slice's 32 rows is again one contiguous store per array.
+// flags bit 0: 16-bit column offsets j - 32*slice (sbase / skmax; a slice with an offset
+// outside [-32768, 32767] keeps 32-bit columns, sbase = -1); bit 1: the FP16 copy of each
+// FP32 weight (round to nearest) and the diagonal of that operator, coef * (sum of the
+// FP16 weights in entry order, in FP32) + kappa, so the FP16-weight operator is again a
+// Laplacian plus kappa; bit 2: 32-bit columns for every slice (the wide streamed SpMV,
+// uncompressed rows); bit 3: leave the wide-entry count alone (a repeated transpose).
+// The weights (T) are always written.  A row's columns ascend (its candidates are
+// visited run by run in cell-key order, each run in index order), so its first and last
+// entries decide whether the slice fits 16 bits; every offset is still checked as it is
+// written, and an offset that breaks that order sets MPS_ERR_NEIGHBOUR_CAP.
+template <class T>
+constexpr int rows_sell_warps() { return sizeof(T) == 4 ? 4 : 2; }
+
+template <class T>
+__global__ void __launch_bounds__(rows_sell_warps<T>() * 32) k_rows_sell(const __grid_constant__ Dev d, int flags) {
+    constexpr int WARPS = rows_sell_warps<T>();
+    __shared__ int tj[WARPS][32][33];
+    __shared__ T tw[WARPS][32][33];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int sl = blockIdx.x * WARPS + wl;
     if (sl >= (d.n + 31) >> 5) return;   // warp-uniform
-    const int i = sl * 32 + lane;
-    const int cnt = (i < d.n && d.inner[i]) ? d.nbr_cnt[i] : 0;
+    const bool narrow = (flags & 1) != 0, w16 = sizeof(T) == 4 && (flags & 2) != 0, full32 = (flags & 4) != 0;
+    const int r0 = sl * 32, i = r0 + lane;
+    const int cnt = (i < d.n && d.inner[i]) ? min(d.nbr_cnt[i], d.K) : 0;
     const int kmax = __reduce_max_sync(0xffffffffu, cnt);
-    const size_t base = (size_t)sl * d.K * 32 + lane;
-    const int r0 = sl * 32;
-    const float* __restrict__ w = (const float*)d.nbrw;
-    bool fits = true;
+    const int* __restrict__ rj = d.rnbr + (size_t)r0 * d.K;
+    const T* __restrict__ rwt = (const T*)d.rw + (size_t)r0 * d.K;
+    bool fit = true;
+    if (cnt > 0) {
+        const int lo = __ldcs(rj + (size_t)lane * d.K) - r0, hi = __ldcs(rj + (size_t)lane * d.K + cnt - 1) - r0;
+        fit = lo >= -32768 && hi <= 32767;
+    }
+    const bool n16 = narrow && __all_sync(0xffffffffu, fit);
+    const bool c32 = full32 || !n16;
+    const size_t e0 = (size_t)sl * d.K * 32 + lane;   // SELL position of this lane's entry 0
+    T* __restrict__ ws = (T*)d.nbrw;
     float sw16 = 0.f;
-    for (int k = 0; k < kmax; k += 4) {
-        int j[4];
-        float wv[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            j[u] = k + u < cnt ? __ldcs(d.nbr + base + (size_t)(k + u) * 32) : r0;
-            wv[u] = (w16 && k + u < cnt) ? __ldcs(w + base + (size_t)(k + u) * 32) : 0.f;
+    bool bad = false;
+    for (int c = 0; c < kmax; c += 32) {
+#pragma unroll 8
+        for (int r = 0; r < 32; ++r) {
+            const int cr = __shfl_sync(0xffffffffu, cnt, r);
+            if (c + lane < cr) {
+                tj[wl][r][lane] = __ldcs(rj + (size_t)r * d.K + c + lane);
+                tw[wl][r][lane] = __ldcs(rwt + (size_t)r * d.K + c + lane);
+            }
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (k + u < cnt) {
-                const int off = j[u] - r0;
-                fits = fits && off >= -32768 && off <= 32767;
-                d.nbr16[base + (size_t)(k + u) * 32] = (unsigned short)(short)off;
+        __syncwarp();
+        const int m = min(32, kmax - c);
+        for (int k = 0; k < m; ++k) {
+            if (c + k < cnt) {
+                const int j = tj[wl][lane][k];
+                const T w = tw[wl][lane][k];
+                const size_t e = e0 + (size_t)(c + k) * 32;
+                ws[e] = w;
+                if (c32) d.nbr[e] = j;
+                if (n16) {
+                    const int off = j - r0;
+                    bad = bad || off < -32768 || off > 32767;
+                    d.nbr16[e] = (unsigned short)(short)off;
+                }
                 if (w16) {
-                    const __half h = __float2half_rn(wv[u]);
-                    d.w16[base + (size_t)(k + u) * 32] = h;
+                    const __half h = __float2half_rn((float)w);
+                    d.w16[e] = h;
                     sw16 += __half2float(h);
                 }
             }
         }
+        __syncwarp();   // the tile is refilled for the next chunk
     }
     if (w16 && cnt > 0) d.diag16[i] = d.c.coef_lap * (double)sw16 + d.c.kappa;
-    const bool all = __all_sync(0xffffffffu, fits);
+    if (bad) atomicOr(d.err, MPS_ERR_NEIGHBOUR_CAP);
     if (lane == 0) {
-        d.sbase[sl] = all ? r0 : -1;
-        d.skmax[sl] = all ? kmax : -1 - kmax;
+        d.sbase[sl] = n16 ? r0 : -1;
+        d.skmax[sl] = n16 ? kmax : -1 - kmax;
     }
-    // interior entries kept at 32 bits (counted for the bytes-per-launch figure)
-    int wide = all ? 0 : cnt;
+    if (narrow && !(flags & 8)) {
+        // interior entries kept at 32 bits (counted for the bytes-per-launch figure)
+        int wide = n16 ? 0 : cnt;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wide += __shfl_down_sync(0xffffffffu, wide, o);
-    if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
+        for (int o = 16; o > 0; o >>= 1) wide += __shfl_down_sync(0xffffffffu, wide, o);
+        if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
+    }
 }
 
 // a stored weight as a float or double (FP16 weights widen to float)

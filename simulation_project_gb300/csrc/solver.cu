@@ -262,6 +262,7 @@ struct Solver {
         e = e ? e : mk(&d.dragv, 3 * N);
         e = e ? e : mk(&d.tcs, 4 * (size_t)d.cells);   // list bounds of the 2 cells keys (walls, drag)
         const size_t N32 = (N + 31) / 32 * 32;
+        e = e ? e : mk(&d.rnbr, N32 * d.K); e = e ? e : mk((char**)&d.rw, N32 * d.K * wsz);
         e = e ? e : mk(&d.nbr, N32 * d.K); e = e ? e : mk((char**)&d.nbrw, N32 * d.K * wsz);
         e = e ? e : mk(&d.nbr16, N32 * d.K); e = e ? e : mk(&d.sbase, N32 / 32 + 1);
         e = e ? e : mk(&d.skmax, N32 / 32 + 1);
@@ -700,6 +701,23 @@ struct Solver {
         return cuda_status(cudaGetLastError());
     }
 
+    // SELL-32 transpose of the current rows (k_rows_sell flags)
+    void rows_sell(int flags) {
+        const int slices = (d.n + 31) / 32;
+        if (fp64())
+            MPS_COUNT_LAUNCH k_rows_sell<double><<<div_up(slices, rows_sell_warps<double>()), rows_sell_warps<double>() * 32,
+                                                   0, st>>>(d, flags);
+        else
+            MPS_COUNT_LAUNCH k_rows_sell<float><<<div_up(slices, rows_sell_warps<float>()), rows_sell_warps<float>() * 32,
+                                                  0, st>>>(d, flags);
+    }
+    // the 32-bit columns of every slice (debug entries that force the wide SpMV)
+    void ensure_cols32() {
+        if (d.rows_c32 || d.n <= 0) return;
+        rows_sell(d.rows16 | (d.rows_w16 << 1) | 4 | 8);
+        d.rows_c32 = 1;
+    }
+
     template <class T>
     void walls_distance() {
         if (d.tri_n > 0) {
@@ -720,6 +738,7 @@ struct Solver {
         residual_ready = false;
         d.rows16 = 0;
         d.rows_w16 = 0;
+        d.rows_c32 = 0;
         timer.mark(PH_GRID, st);
         cudaMemsetAsync(d.err, 0, sizeof(unsigned), st);
         cudaMemsetAsync(d.istat, 0, 2 * sizeof(int), st);
@@ -753,13 +772,20 @@ struct Solver {
         } else {
             MPS_COUNT_LAUNCH k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
             MPS_COUNT_LAUNCH k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
-            // 16-bit column offsets for the streamed SpMVs (the FP64 solver streams them
-            // with its FP64 weights; FP16 weight copies only for the FP32 inner CG)
-            if (opt.compress_rows && (!fp64() || opt.spmv_stream)) {
-                const int w16 = (!fp64() && want_inner16() && d.w16) ? 1 : 0;
-                MPS_COUNT_LAUNCH k_compress_rows<<<div_up((d.n + 31) / 32 * 32, 256), 256, 0, st>>>(d, w16);
-                d.rows16 = 1;
+            // SELL-32 rows from the list pass's row-major rows: 16-bit column offsets for
+            // the streamed SpMVs (the FP64 solver streams them with its FP64 weights), FP16
+            // weight copies only for the FP32 inner CG, 32-bit columns where they are read
+            {
+                const int narrow = (opt.compress_rows && (!fp64() || opt.spmv_stream)) ? 1 : 0;
+                const int w16 = (narrow && !fp64() && want_inner16() && d.w16) ? 1 : 0;
+                // 32-bit columns: the wide streamed kernels, the register walks of uncompressed
+                // rows, the non-streamed refinement residual (k_residual_df) and every FP64
+                // register walk (the FP64 learned-guess SpMVs, the stream's timeout fallback)
+                const int full32 = (!narrow || prefer_wide || !opt.spmv_stream || fp64()) ? 1 : 0;
+                rows_sell(narrow | (w16 << 1) | (full32 << 2));
+                d.rows16 = narrow;
                 d.rows_w16 = w16;
+                d.rows_c32 = full32;
             }
             bool use_learned = learned_ready && opt.learned;
             // the gate: a learned guess that cost more than it saved sits out a few steps
@@ -1626,6 +1652,7 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_
                                                                                                   d.rhs, 2);
     else {
         const bool keep = S.prefer_wide;
+        if (variant >= 2) S.ensure_cols32();   // k_residual_df and the wide stream read 32-bit columns
         if (variant == 3) S.prefer_wide = true;
         S.residual_df(w, variant == 1 || variant == 3);
         S.prefer_wide = keep;
@@ -1654,6 +1681,7 @@ CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_
     else if (kernel == 1 || kernel == 2 || kernel == 3 || kernel == 6) {
         const bool keep = S.prefer_wide;
         S.prefer_wide = kernel == 3 || kernel == 6;
+        if (S.prefer_wide) S.ensure_cols32();
         if (kernel == 1 || kernel == 3) S.spmv_stream<0>(w, d.p32, d.q32, nullptr, 0);
         else S.spmv_stream16(d.p32, d.q32);
         S.prefer_wide = keep;
