@@ -120,6 +120,10 @@ typedef struct MpsSolverOptions {
                                a diagonal-plus-neighbour fine operator, not symmetric, so
                                the inner solve runs as flexible CG */
     double smoother_weight; /* w of fine_smoother 1 (default 0.8) */
+    int rows_sell;          /* transpose of the list pass's row-major FP32 rows into SELL-32:
+                               0 (default) 16-byte asynchronous copies into swizzled,
+                               double-buffered shared-memory tiles; 1 register-staged tiles;
+                               same rows either way */
 } MpsSolverOptions;
 
 /* error_flags bits of MpsStepStats (set by kernels, read after the step) */

@@ -984,6 +984,117 @@ __global__ void __launch_bounds__(rows_sell_warps<T>() * 32) k_rows_sell(const _
     }
 }
 
+// FP32 rows (the step's default): the same transpose with the chunks moved global ->
+// shared by 16-byte cp.async pieces, double-buffered so that the next chunk's copies
+// are in flight while the current chunk is written out.  A warp per slice, 2 warps per
+// CTA (32 KB: 2 stages x columns and weights x 32 rows x 128 B).  Piece q (entries
+// 4q..4q+3) of row r sits at piece position q ^ (r & 7) of the row's 128 bytes, so the
+// 16-byte reads of lanes 0..7 (rows 0..7, one piece each) cover the 32 banks.  Pieces
+// of a chunk past a row's count copy stale staging entries inside the row's capacity
+// (K is a multiple of 128) and are never read.  Same outputs as k_rows_sell<float>.
+constexpr int kRsWarps = 2;
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__global__ void __launch_bounds__(kRsWarps * 32) k_rows_sell_async(const __grid_constant__ Dev d, int flags) {
+    __shared__ __align__(128) unsigned char tiles[kRsWarps][2][2][32 * 128];   // [warp][stage][cols, weights]
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int sl = blockIdx.x * kRsWarps + wl;
+    if (sl >= (d.n + 31) >> 5) return;   // warp-uniform
+    const bool narrow = (flags & 1) != 0, w16 = (flags & 2) != 0, full32 = (flags & 4) != 0;
+    const int r0 = sl * 32, i = r0 + lane;
+    const int cnt = (i < d.n && d.inner[i]) ? min(d.nbr_cnt[i], d.K) : 0;
+    const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+    const int* __restrict__ rj = d.rnbr + (size_t)r0 * d.K;
+    const float* __restrict__ rwt = (const float*)d.rw + (size_t)r0 * d.K;
+    bool fit = true;
+    if (cnt > 0) {
+        const int lo = __ldcs(rj + (size_t)lane * d.K) - r0, hi = __ldcs(rj + (size_t)lane * d.K + cnt - 1) - r0;
+        fit = lo >= -32768 && hi <= 32767;
+    }
+    const bool n16 = narrow && __all_sync(0xffffffffu, fit);
+    const bool c32 = full32 || !n16;
+    const size_t e0 = (size_t)sl * d.K * 32 + lane;
+    float* __restrict__ ws = (float*)d.nbrw;
+    // lane t copies piece t & 7 of rows 4u + t / 8, u = 0..7
+    const int cq = lane & 7, crow = lane >> 3;
+    auto issue = [&](int c, int st) {
+        unsigned char* tj = tiles[wl][st][0];
+        unsigned char* tw = tiles[wl][st][1];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int r = 4 * u + crow;
+            const int cr = __shfl_sync(0xffffffffu, cnt, r);
+            if (c < cr) {
+                const size_t g = (size_t)r * d.K + c + 4 * cq;
+                const int pos = r * 128 + ((cq ^ (r & 7)) << 4);
+                cp_async16(tj + pos, rj + g);
+                cp_async16(tw + pos, rwt + g);
+            }
+        }
+        cp_async_commit();
+    };
+    const int nch = (kmax + 31) >> 5;
+    if (nch > 0) issue(0, 0);
+    float sw16 = 0.f;
+    bool bad = false;
+    for (int ci = 0; ci < nch; ++ci) {
+        if (ci + 1 < nch) {
+            issue((ci + 1) * 32, (ci + 1) & 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncwarp();   // every lane's pieces of chunk ci have landed
+        const unsigned char* tj = tiles[wl][ci & 1][0];
+        const unsigned char* tw = tiles[wl][ci & 1][1];
+        const int c = ci * 32;
+        for (int q = 0; q < 8 && c + 4 * q < kmax; ++q) {
+            const int pos = lane * 128 + ((q ^ (lane & 7)) << 4);
+            const int4 jv = *(const int4*)(tj + pos);
+            const float4 wv = *(const float4*)(tw + pos);
+            const int jj[4] = {jv.x, jv.y, jv.z, jv.w};
+            const float wf[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = c + 4 * q + u;
+                if (k < cnt) {
+                    const size_t e = e0 + (size_t)k * 32;
+                    ws[e] = wf[u];
+                    if (c32) d.nbr[e] = jj[u];
+                    if (n16) {
+                        const int off = jj[u] - r0;
+                        bad = bad || off < -32768 || off > 32767;
+                        d.nbr16[e] = (unsigned short)(short)off;
+                    }
+                    if (w16) {
+                        const __half h = __float2half_rn(wf[u]);
+                        d.w16[e] = h;
+                        sw16 += __half2float(h);
+                    }
+                }
+            }
+        }
+        __syncwarp();   // stage ci & 1 is refilled by the next iteration's copies
+    }
+    if (w16 && cnt > 0) d.diag16[i] = d.c.coef_lap * (double)sw16 + d.c.kappa;
+    if (bad) atomicOr(d.err, MPS_ERR_NEIGHBOUR_CAP);
+    if (lane == 0) {
+        d.sbase[sl] = n16 ? r0 : -1;
+        d.skmax[sl] = n16 ? kmax : -1 - kmax;
+    }
+    if (narrow && !(flags & 8)) {
+        int wide = n16 ? 0 : cnt;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wide += __shfl_down_sync(0xffffffffu, wide, o);
+        if (lane == 0 && wide) atomicAdd(d.istat + 1, wide);
+    }
+}
+
 // a stored weight as a float or double (FP16 weights widen to float)
 __device__ __forceinline__ float to_wt(float v) { return v; }
 __device__ __forceinline__ double to_wt(double v) { return v; }

@@ -707,9 +707,11 @@ struct Solver {
         if (fp64())
             MPS_COUNT_LAUNCH k_rows_sell<double><<<div_up(slices, rows_sell_warps<double>()), rows_sell_warps<double>() * 32,
                                                    0, st>>>(d, flags);
-        else
+        else if (opt.rows_sell == 1)
             MPS_COUNT_LAUNCH k_rows_sell<float><<<div_up(slices, rows_sell_warps<float>()), rows_sell_warps<float>() * 32,
                                                   0, st>>>(d, flags);
+        else
+            MPS_COUNT_LAUNCH k_rows_sell_async<<<div_up(slices, kRsWarps), kRsWarps * 32, 0, st>>>(d, flags);
     }
     // the 32-bit columns of every slice (debug entries that force the wide SpMV)
     void ensure_cols32() {
@@ -1468,7 +1470,7 @@ struct MpsSolver {
 
 extern "C" {
 
-static_assert(sizeof(MpsSolverOptions) == 160 && sizeof(MpsStepStats) == 168,
+static_assert(sizeof(MpsSolverOptions) == 168 && sizeof(MpsStepStats) == 168,
               "the option and statistics records are part of the C ABI");
 
 void mps_solver_default_options(MpsSolverOptions* o) {
@@ -1497,6 +1499,7 @@ void mps_solver_default_options(MpsSolverOptions* o) {
     o->learned_gate = 1;
     o->fine_smoother = 0;
     o->smoother_weight = 0.8;
+    o->rows_sell = 0;
 }
 
 CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, int max_particles,
@@ -1511,6 +1514,7 @@ CCTStatusType mps_solver_create(const CParameter* param, const CGridBox* box, in
     if (o.warm_start < -1 || o.warm_start > 2) return CCT_PARAMERR;
     if (o.flexible < -1 || o.flexible > 1 || o.learned_gate < 0 || o.learned_gate > 1) return CCT_PARAMERR;
     if (o.fine_smoother < 0 || o.fine_smoother > 1 || !(o.smoother_weight >= 0.0)) return CCT_PARAMERR;
+    if (o.rows_sell < 0 || o.rows_sell > 1) return CCT_PARAMERR;
     MpsSolver* s = new MpsSolver();
     CCTStatusType rc = s->s.init(param, box, max_particles, &o);
     if (rc != CCT_NOERR) {

@@ -27,7 +27,8 @@ class MpsSolverOptions(C.Structure):
                 ("mg_omega", C.c_double), ("compress_rows", C.c_int), ("mg_sweeps", C.c_int),
                 ("matrix_free", C.c_int), ("spmv_stream", C.c_int), ("inner_weights", C.c_int),
                 ("spmv_wide", C.c_int), ("warm_start", C.c_int), ("flexible", C.c_int),
-                ("learned_gate", C.c_int), ("fine_smoother", C.c_int), ("smoother_weight", C.c_double)]
+                ("learned_gate", C.c_int), ("fine_smoother", C.c_int), ("smoother_weight", C.c_double),
+                ("rows_sell", C.c_int)]
 
 
 class MpsStepStats(C.Structure):

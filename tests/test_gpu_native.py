@@ -201,6 +201,23 @@ def test_spmv_kernels_give_identical_rows():
         assert np.array_equal(y0.view(np.uint32), yk.view(np.uint32)), (k, np.abs(yk - y0).max())
 
 
+@pytest.mark.parametrize("wide", [0, 1], ids=["16bit", "wide"])
+def test_row_transpose_variants_give_identical_steps(wide):
+    """The list pass writes each row contiguously; the asynchronous (swizzled,
+    double-buffered) and the register-staged SELL-32 transposes make the same slices,
+    so the steps are bit-identical, over 16-bit and over 32-bit columns."""
+    sc = scenes.rotating_bucket(l0=0.006, n_drag=4, drag_index=0.5)
+    a = Solver(sc, precision="fp32_ir", rows_sell=0, spmv_wide=wide)
+    b = Solver(sc, precision="fp32_ir", rows_sell=1, spmv_wide=wide)
+    for i in range(3):
+        sa, sb = a.step(i), b.step(i)
+        assert sa["error_flags"] == 0 and sb["error_flags"] == 0 and sa["cg_relres"] <= 1e-8
+        assert sa["cg_iterations"] == sb["cg_iterations"] and sa["cg_relres"] == sb["cg_relres"]
+        assert sa["nnz_wide"] == sb["nnz_wide"] and sa["rows16"] == 1
+    x, y = a.state(), b.state()
+    assert np.array_equal(x["press"], y["press"]) and np.array_equal(x["pos"], y["pos"])
+
+
 def test_streamed_residual_is_bit_identical():
     """The double-float refinement residual over streamed rows does the register
     walk's operations in the same order: identical r and norms."""

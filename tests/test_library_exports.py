@@ -57,8 +57,8 @@ def test_default_options_through_the_python_mirror(so):
     preconditioner with smoothing weight 1.3, automatic warm start and inner floor)."""
     from simulation_project_gb300.solver import default_options, MpsSolverOptions
     o = default_options()
-    # 17 ints and 10 doubles in header order, naturally aligned (three 4-byte pads)
-    assert C.sizeof(MpsSolverOptions) == 160
+    # 18 ints and 10 doubles in header order, naturally aligned (four 4-byte pads)
+    assert C.sizeof(MpsSolverOptions) == 168
     assert o.precision == 1 and o.pressure_mode == 0 and o.learned == 0
     assert o.compressibility == 1e-9 and o.cg_rtol == 1e-8 and o.cg_max_iter == 5000
     assert o.ir_inner_rtol == 0.0 and o.ir_max_outer == 12 and o.max_neighbours == 384
@@ -66,12 +66,12 @@ def test_default_options_through_the_python_mirror(so):
     assert o.preconditioner == 1 and o.mg_omega == 1.3 and o.compress_rows == 1 and o.mg_sweeps == 1
     assert o.matrix_free == 0 and o.spmv_stream == 1 and o.inner_weights == 16 and o.spmv_wide == 0
     assert o.warm_start == -1 and o.flexible == 0 and o.learned_gate == 1
-    assert o.fine_smoother == 0 and o.smoother_weight == 0.8
+    assert o.fine_smoother == 0 and o.smoother_weight == 0.8 and o.rows_sell == 0
 
 
 @pytest.mark.parametrize("bad", [{"matrix_free": 3}, {"spmv_stream": 2}, {"inner_weights": 8}, {"spmv_wide": 2},
                                  {"warm_start": 3}, {"warm_start": -2}, {"flexible": 2}, {"learned_gate": -1},
-                                 {"fine_smoother": 2}, {"smoother_weight": -1.0}])
+                                 {"fine_smoother": 2}, {"smoother_weight": -1.0}, {"rows_sell": 2}])
 def test_invalid_solver_options_are_rejected_before_any_device_work(so, bad):
     """mps_solver_create checks its options before it touches the device: an invalid
     value returns CCT_PARAMERR (2) and no solver, with or without a GPU."""
