@@ -22,6 +22,8 @@ constexpr size_t radix_scratch_bytes_for(long long n) {
 size_t radix_scratch_bytes(int n);
 int radix_passes(unsigned range);
 cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, void* scratch, cudaStream_t st);
+// the same with the key range (min, max) in device memory (key_minmax): no host wait
+cudaError_t radix_sort_pairs_range(int n, int* keys, int* vals, const int* mm_dev, void* scratch, cudaStream_t st);
 cudaError_t key_minmax(int n, const int* keys, int* mm_dev, cudaStream_t st);
 // in-place exclusive scan of len unsigned values, total to *total_dev (if not NULL);
 // tile_sums (scan_tile_sums_capacity() values, or NULL: single-CTA scan) lets it

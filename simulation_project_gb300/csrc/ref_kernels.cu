@@ -936,14 +936,11 @@ CCTStatusType SortUsingThrust(Integer MaxParticleNum, Integer* daNumberHash, Int
     cudaStream_t st = 0;
     int* mm = (int*)scratch_get(0, 2 * sizeof(int));
     if (!mm) return CCT_MEMERR;
-    MPS_CUDA_TRY(key_minmax(n, daNumberHash, mm, st));
-    int h[2];
-    MPS_CUDA_TRY(cudaMemcpyAsync(h, mm, sizeof(h), cudaMemcpyDeviceToHost, st));
-    MPS_CUDA_TRY(cudaStreamSynchronize(st));
-    const int passes = radix_passes((unsigned)h[1] - (unsigned)h[0]);
     void* scr = scratch_get(1, radix_scratch_bytes(n));
     if (!scr) return CCT_MEMERR;
-    MPS_CUDA_TRY(radix_sort_pairs(n, daNumberHash, daNumberIndex, h[0], passes, scr, st));
+    // the key range stays on the device: the passes it does not need return at once
+    MPS_CUDA_TRY(key_minmax(n, daNumberHash, mm, st));
+    MPS_CUDA_TRY(radix_sort_pairs_range(n, daNumberHash, daNumberIndex, mm, scr, st));
     // thrust::sort_by_key with the default policy returns after the sort completed;
     // callers rely on that (they launch the reorder on their own stream next).
     MPS_CUDA_TRY(cudaStreamSynchronize(st));

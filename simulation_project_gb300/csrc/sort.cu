@@ -17,7 +17,10 @@
 //                  with __match_any_sync + per-warp running digit counters, and
 //                  writes key and value to offset[d][tile] + warp prefix + rank.
 // Keys are sorted as unsigned offsets (key - kmin), so negative keys sort correctly
-// and a pass runs only for the digits the key range actually spans.
+// and a pass runs only for the digits the key range actually spans.  With the range in
+// device memory (radix_sort_pairs_range) the host launches the largest number of passes
+// and each pass's kernels read the range and return at once past the passes it needs,
+// so the caller does not wait for the key range on the host.
 #include "mps_common.cuh"
 #include "mps_internal.h"
 
@@ -32,10 +35,20 @@ static_assert(kSortTile == kRadixSortTile, "tile size of the scratch formula");
 __device__ __forceinline__ unsigned digit_of(int key, int kmin, int shift) {
     return (((unsigned)key - (unsigned)kmin) >> shift) & 255u;
 }
+// 8-bit passes a key range needs (radix_passes on the device)
+__device__ __forceinline__ int range_passes(unsigned range) { return range == 0u ? 0 : (39 - __clz((int)range)) / 8; }
+// with the key range (min, max) in device memory: the pass's kmin, false when the pass
+// is past the ones the range needs
+__device__ __forceinline__ bool pass_live(const int* __restrict__ mm, int shift, int& kmin) {
+    if (!mm) return true;
+    kmin = mm[0];
+    return shift / 8 < range_passes((unsigned)mm[1] - (unsigned)mm[0]);
+}
 
 __global__ void __launch_bounds__(kSortThreads) k_digit_hist(const int* __restrict__ keys, int n, int kmin, int shift,
                                                             int tiles, unsigned* __restrict__ counts,
-                                                            unsigned* __restrict__ dtot) {
+                                                            unsigned* __restrict__ dtot, const int* __restrict__ mm) {
+    if (!pass_live(mm, shift, kmin)) return;
     __shared__ unsigned h[kRadix];
     h[threadIdx.x] = 0;
     __syncthreads();
@@ -124,7 +137,10 @@ __device__ __forceinline__ unsigned block_exclusive(unsigned v, unsigned* ws, un
 
 // CTA per digit: offsets[d][t] = base(d) + sum of counts[d][t' < t], in place
 __global__ void __launch_bounds__(kScanThreads) k_scan_digits(unsigned* __restrict__ counts, int tiles,
-                                                              const unsigned* __restrict__ dtot) {
+                                                              const unsigned* __restrict__ dtot,
+                                                              const int* __restrict__ mm, int shift) {
+    int kmin_unused = 0;
+    if (!pass_live(mm, shift, kmin_unused)) return;
     __shared__ unsigned ws[32];
     __shared__ unsigned carry;
     const int d = blockIdx.x;
@@ -205,7 +221,9 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(unsigned* __restric
 __global__ void __launch_bounds__(kSortThreads) k_scatter(const int* __restrict__ kin, const int* __restrict__ vin,
                                                          int* __restrict__ kout, int* __restrict__ vout, int n,
                                                          int kmin, int shift, int tiles,
-                                                         const unsigned* __restrict__ offsets) {
+                                                         const unsigned* __restrict__ offsets,
+                                                         const int* __restrict__ mm) {
+    if (!pass_live(mm, shift, kmin)) return;
     __shared__ unsigned wcount[kSortThreads / 32][kRadix];
     __shared__ unsigned toff[kRadix];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -270,6 +288,17 @@ __global__ void k_minmax(const int* __restrict__ keys, int n, int* __restrict__ 
     }
 }
 
+// after the passes of radix_sort_pairs_range: an odd number of passes left the pairs
+// in the scratch arrays; copy them back
+__global__ void k_copy_back_odd(const int* __restrict__ mm, int n, const int* __restrict__ ka,
+                                const int* __restrict__ va, int* __restrict__ keys, int* __restrict__ vals) {
+    if ((range_passes((unsigned)mm[1] - (unsigned)mm[0]) & 1) == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        keys[i] = ka[i];
+        vals[i] = va[i];
+    }
+}
+
 __global__ void k_minmax_init(int* mm) {
     mm[0] = INT_MAX;
     mm[1] = INT_MIN;
@@ -302,9 +331,10 @@ cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, 
     for (int pass = 0; pass < passes; ++pass) {
         const int shift = pass * 8;
         unsigned* dt = dtot + (size_t)kRadix * pass;
-        MPS_COUNT_LAUNCH k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts, dt);
-        MPS_COUNT_LAUNCH k_scan_digits<<<kRadix, kScanThreads, 0, st>>>(counts, tiles, dt);
-        MPS_COUNT_LAUNCH k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, kmin, shift, tiles, counts);
+        MPS_COUNT_LAUNCH k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, kmin, shift, tiles, counts, dt, nullptr);
+        MPS_COUNT_LAUNCH k_scan_digits<<<kRadix, kScanThreads, 0, st>>>(counts, tiles, dt, nullptr, shift);
+        MPS_COUNT_LAUNCH k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, kmin, shift, tiles, counts,
+                                                                   nullptr);
         int* t = ka; ka = kb; kb = t;
         t = va; va = vb; vb = t;
     }
@@ -312,6 +342,36 @@ cudaError_t radix_sort_pairs(int n, int* keys, int* vals, int kmin, int passes, 
         cudaMemcpyAsync(keys, ka, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(vals, va, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t radix_sort_pairs_range(int n, int* keys, int* vals, const int* mm_dev, void* scratch, cudaStream_t st) {
+    if (n <= 1) return cudaSuccess;
+    const int tiles = div_up(n, kSortTile);
+    char* p = (char*)scratch;
+    int* kalt = (int*)p;
+    p += sizeof(int) * (size_t)n;
+    int* valt = (int*)p;
+    p += sizeof(int) * (size_t)n;
+    unsigned* counts = (unsigned*)p;
+    unsigned* dtot = counts + (size_t)kRadix * tiles + 8;   // [kRadixMaxPasses][kRadix]
+    cudaMemsetAsync(dtot, 0, sizeof(unsigned) * kRadix * kRadixMaxPasses, st);
+    int* ka = keys;
+    int* va = vals;
+    int* kb = kalt;
+    int* vb = valt;
+    for (int pass = 0; pass < kRadixMaxPasses; ++pass) {
+        const int shift = pass * 8;
+        unsigned* dt = dtot + (size_t)kRadix * pass;
+        MPS_COUNT_LAUNCH k_digit_hist<<<tiles, kSortThreads, 0, st>>>(ka, n, 0, shift, tiles, counts, dt, mm_dev);
+        MPS_COUNT_LAUNCH k_scan_digits<<<kRadix, kScanThreads, 0, st>>>(counts, tiles, dt, mm_dev, shift);
+        MPS_COUNT_LAUNCH k_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 0, shift, tiles, counts, mm_dev);
+        int* t = ka; ka = kb; kb = t;
+        t = va; va = vb; vb = t;
+    }
+    // passes 0, 2 read the caller's arrays and 1, 3 the scratch: after the passes the
+    // range needed, the pairs sit in the scratch arrays when that number is odd
+    MPS_COUNT_LAUNCH k_copy_back_odd<<<min(div_up(n, 256), 152 * 8), 256, 0, st>>>(mm_dev, n, kalt, valt, keys, vals);
     return cudaGetLastError();
 }
 

@@ -165,8 +165,14 @@ def test_training_reduces_loss_on_a_smooth_target():
 
 def test_learned_solver_converges_and_reports_gain():
     """Trains on the plain solver's own solves of a small bucket, then runs the same
-    steps with and without the network: both must reach 1e-8; the iteration counts
-    and whether the learned path needed its fallback are printed."""
+    steps with and without the network: both reach 1e-8, and in every step after the
+    first few (the network is trained on steady steps) the learned start leaves a
+    smaller initial residual than the extrapolated warm start.  It saves no CG
+    iterations on this scene (measured: 102 against 101 over steps 2-7): the residual it
+    removes is the local, high-frequency part that the first preconditioned iteration
+    removes anyway, so the test bounds the cost at one iteration per step instead of
+    claiming a gain.  The line search minimises the A-norm error, so the residual norm
+    itself may rise in an early step (step 1 here)."""
     sc = scenes.rotating_bucket(l0=0.008, n_drag=8)
     f, t = collect_samples(sc, steps=6, precision="fp64")
     p, info = train(f, t, epochs=6, batch=4096, lr=2e-3)
@@ -183,14 +189,18 @@ def test_learned_solver_converges_and_reports_gain():
         ss = scaled.step(i)
         for s in (sp, sl, ss):
             assert s["cg_relres"] <= 1e-8 and s["error_flags"] == 0, s
+        print(f"step {i}: r0 plain {sp['r0_relres']:.4e} learned {sl['r0_relres']:.4e} scaled {ss['r0_relres']:.4e}; "
+              f"its {sp['cg_iterations']} {sl['cg_iterations']} {ss['cg_iterations']}")
         if i >= 2:
             it_p += sp["cg_iterations"]
             it_l += sl["cg_iterations"]
             it_s += ss["cg_iterations"]
+        if i >= 3:
+            assert sl["r0_relres"] < sp["r0_relres"], (i, sl["r0_relres"], sp["r0_relres"])
     print(f"\nCG iterations steps 2-7: plain {it_p}, learned guess {it_l} (saved {it_p - it_l}, "
           f"{100.0 * (it_p - it_l) / max(it_p, 1):.1f}%), guess+scaling {it_s}; training {info}")
-    # the line-searched guess is never worse than the warm start in A-norm
-    assert it_l <= it_p * 1.05 + 2
+    # no iteration gain is claimed; the guess costs at most one iteration per step
+    assert it_l <= it_p + 6
     a, b = plain.state(), learned.state()
     assert np.array_equal(a["id"], b["id"])
     pm = np.abs(a["press"]).max()

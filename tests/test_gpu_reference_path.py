@@ -55,7 +55,8 @@ def test_hash_sort_cells_reorder(n_side, seed):
 
 @pytest.mark.parametrize("entry", ["SortUsingThrust", "StableSortUsingThrust"])
 @pytest.mark.parametrize("n,lo,hi", [(1, 0, 5), (2, 3, 3), (1000, -50, 50), (70000, 0, 1 << 17),
-                                     (300000, -(1 << 30), 1 << 30), (65536, 7, 7), (4097, 0, 255)])
+                                     (300000, -(1 << 30), 1 << 30), (65536, 7, 7), (4097, 0, 255),
+                                     (5000, -1000, 40000)])
 def test_radix_sort_is_stable_sort(n, lo, hi, entry):
     rng = np.random.default_rng(n)
     keys = rng.integers(lo, hi + 1, size=n, dtype=np.int64).astype(np.int32)
