@@ -460,8 +460,10 @@ def plain_fp64_roofline(scene, args, peak_gbs, steps=3):
 
 def mlp_bench(params, n, tflops_peak, reps=20):
     """The learned guess's MLP inference on n rows of features: the tcgen05 kernel the
-    solver runs (variant 0) and the mma.sync cross-check kernel (variant 1), CUDA events
-    on the legacy stream around `reps` launches after 3 warm-up launches."""
+    solver runs (variant 0), the mma.sync cross-check kernel (variant 1) and the tcgen05
+    kernel with 0..3 of every 4 pairs of hidden activations on the FMA pipe (variants
+    2..5, the share variant 0 uses among them), CUDA events on the legacy stream around
+    `reps` launches after 3 warm-up launches."""
     from simulation_project_gb300 import lib
     from simulation_project_gb300.learned import Mlp
     if params is None:
@@ -472,7 +474,8 @@ def mlp_bench(params, n, tflops_peak, reps=20):
     Y = lib.DeviceArray((n, 2), np.float32)
     out = {"rows": n, "flop_per_row_padded": 73728}
     ev0, ev1 = lib.Event(), lib.Event()
-    for v, name in ((0, "tcgen05"), (1, "mma_sync")):
+    for v, name in ((0, "tcgen05"), (1, "mma_sync"), (2, "tcgen05_silu_sfu_only"), (3, "tcgen05_silu_fma_1of4"),
+                    (4, "tcgen05_silu_fma_2of4"), (5, "tcgen05_silu_fma_3of4")):
         for _ in range(3):
             m.forward(X.ptr, Y.ptr, n, variant=v)
         lib.call("mps_device_sync")

@@ -56,7 +56,8 @@ CCTStatusType mps_mlp_get_params(MpsMlp* m, float* host_params);
 CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* stream);
 /* the same with a chosen kernel: 0 the tcgen05 FP16 kernel mps_mlp_forward uses, 1 the
  * warp-level mma.sync kernel with the BF16 / FP32 rounding points of training (a
- * cross-check) */
+ * cross-check), 2..5 the tcgen05 kernel with 0, 1, 2 or 3 of every 4 pairs of hidden
+ * activations computed on the FMA pipe (a polynomial tanh) and the rest on the SFU */
 CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, int variant, void* stream);
 /* nonzero if an MMA completion wait of the tcgen05 kernel ever ran out (the kernel then
  * stops early; its outputs are incomplete) */

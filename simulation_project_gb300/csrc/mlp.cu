@@ -782,9 +782,43 @@ __device__ __forceinline__ void tc_ld32_pack16_nowait(unsigned taddr, uint32_t (
           "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
         : "r"(taddr));
 }
+// The same SiLU on the FMA pipe, for a share of the columns while the SFU runs the
+// others: tanh |h| from a degree-8 polynomial in v = min(|h|, 4.5) - 2.25, the
+// least-squares fit of tanh on [0, 4.5] at 4000 Chebyshev nodes, coefficients rounded to
+// FP16 and evaluated by FP16x2 Horner (|error| <= 1.9e-3 over every FP16 input; tanh
+// 4.5 rounds to 1 in FP16); the sign bits of h give tanh h, then h + h tanh h.  SiLU
+// error <= 3.6e-3 absolute, 2.3e-3 relative beyond 1 (an exactly rounded FP16 tanh:
+// 2.9e-3 / 1.1e-3).  Eleven FP16x2 instructions on the FMA pipe and two logic ops.
+__device__ __forceinline__ uint32_t hfma2(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("fma.rn.f16x2 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+__device__ __forceinline__ uint32_t silu2_f16_poly(uint32_t h) {
+    uint32_t a = h & 0x7FFF7FFFu, v;
+    asm("min.f16x2 %0, %1, %2;" : "=r"(a) : "r"(a), "r"(0x44804480u));   // 4.5
+    asm("add.f16x2 %0, %1, %2;" : "=r"(v) : "r"(a), "r"(0xC080C080u));   // -2.25
+    uint32_t t = hfma2(0x09230923u, v, 0x91A791A7u);
+    t = hfma2(t, v, 0x855C855Cu);
+    t = hfma2(t, v, 0x1D6F1D6Fu);
+    t = hfma2(t, v, 0xA33BA33Bu);
+    t = hfma2(t, v, 0x26AD26ADu);
+    t = hfma2(t, v, 0xA944A944u);
+    t = hfma2(t, v, 0x29962996u);
+    t = hfma2(t, v, 0x3BD33BD3u);
+    t ^= h & 0x80008000u;   // tanh(-a) = -tanh(a)
+    return hfma2(h, t, h);
+}
+// pair u (0..3) of every group of four on the FMA pipe when bit u of POLY is set
+template <int POLY>
+__device__ __forceinline__ uint32_t silu2_mixed(uint32_t h, int u) {
+    return (POLY >> u) & 1 ? silu2_f16_poly(h) : silu2_f16(h);
+}
+
 // hidden-layer epilogue: this thread's row of the 128 FP16 accumulator columns (both
 // halves loaded before one wait), SiLU -> FP16 A operand of the next layer (row r,
 // canonical K-major, K = 144)
+template <int POLY>
 __device__ __forceinline__ void tc_epilogue_hidden(unsigned tmem_row, unsigned char* __restrict__ A, int r) {
     uint32_t v[2][32];
     tc_ld32_pack16_nowait(tmem_row, v[0]);
@@ -794,8 +828,8 @@ __device__ __forceinline__ void tc_epilogue_hidden(unsigned tmem_row, unsigned c
     for (int c = 0; c < 2; ++c) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            const uint4 o = make_uint4(silu2_f16(v[c][4 * q]), silu2_f16(v[c][4 * q + 1]),
-                                       silu2_f16(v[c][4 * q + 2]), silu2_f16(v[c][4 * q + 3]));
+            const uint4 o = make_uint4(silu2_mixed<POLY>(v[c][4 * q], 0), silu2_mixed<POLY>(v[c][4 * q + 1], 1),
+                                       silu2_mixed<POLY>(v[c][4 * q + 2], 2), silu2_mixed<POLY>(v[c][4 * q + 3], 3));
             *reinterpret_cast<uint4*>(A + tc_off(r, 64 * c + 8 * q, kTcK)) = o;
         }
     }
@@ -821,7 +855,7 @@ __device__ __forceinline__ bool slot_any(int id, bool v) {
     return r != 0;
 }
 
-template <int NS>
+template <int NS, int POLY>
 __global__ void __launch_bounds__(TcShape<NS>::Threads, 1) k_mlp_infer_tc(int M, const float* __restrict__ X,
                                                                           float* __restrict__ Y, Layers L,
                                                                           unsigned* err) {
@@ -950,7 +984,7 @@ __global__ void __launch_bounds__(TcShape<NS>::Threads, 1) k_mlp_infer_tc(int M,
                 ph ^= 1u;
                 tc_fence_after();
                 if (layer < 3) {
-                    tc_epilogue_hidden(trow, As, r);
+                    tc_epilogue_hidden<POLY>(trow, As, r);
                 } else {
                     uint32_t y0, y1;
                     tc_ld2(trow, y0, y1);
@@ -1164,28 +1198,45 @@ struct MpsMlp {
 };
 
 namespace mps {
+// the tcgen05 inference kernel with POLY's columns on the FMA pipe
+template <int POLY>
+cudaError_t mlp_forward_tc(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st, unsigned* err, int sms) {
+    static bool tc_set = false;   // the attribute is per function, set once
+    if (!tc_set) {
+        const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc<kTcSlots, POLY>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)TcShape<kTcSlots>::Smem);
+        if (e) return e;
+        tc_set = true;
+    }
+    const int tiles = (M + kTcRows - 1) / kTcRows;
+    const int grid = std::max(1, std::min(div_up(tiles, kTcSlots), std::max(sms, 1)));   // one CTA per SM
+    MPS_COUNT_LAUNCH k_mlp_infer_tc<kTcSlots, POLY>
+        <<<grid, TcShape<kTcSlots>::Threads, TcShape<kTcSlots>::Smem, st>>>(M, X, Y, m->L, err);
+    return cudaGetLastError();
+}
+// share of the SiLU pairs the solver's inference kernel runs on the FMA pipe (bit u:
+// pair u of every four)
+constexpr int kTcPolyDefault = 0x8;
+
 // forward of a created MLP on M rows of features: variant 0 the tcgen05 kernel (the
-// solver's), 1 the mma.sync kernel (kept as a cross-check of the former)
+// solver's), 1 the mma.sync kernel (kept as a cross-check of the former), 2..5 the
+// tcgen05 kernel with 0, 1, 2, 3 of every 4 SiLU pairs on the FMA pipe (the rest on the
+// SFU's tanh)
 cudaError_t mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, cudaStream_t st, int variant,
                                 unsigned* err) {
     if (M <= 0) return cudaSuccess;
-    static bool smem_set = false, tc_set = false;   // the attribute is per function, set once
+    static bool smem_set = false;   // the attribute is per function, set once
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (variant == 0) {
-        if (!tc_set) {
-            const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer_tc<kTcSlots>,
-                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)TcShape<kTcSlots>::Smem);
-            if (e) return e;
-            tc_set = true;
-        }
-        const int tiles = (M + kTcRows - 1) / kTcRows;
-        const int grid = std::max(1, std::min(div_up(tiles, kTcSlots), std::max(sms, 1)));   // one CTA per SM
-        MPS_COUNT_LAUNCH k_mlp_infer_tc<kTcSlots>
-            <<<grid, TcShape<kTcSlots>::Threads, TcShape<kTcSlots>::Smem, st>>>(M, X, Y, m->L, err);
-        return cudaGetLastError();
+    switch (variant) {
+        case 0: return mlp_forward_tc<kTcPolyDefault>(m, M, X, Y, st, err, sms);
+        case 2: return mlp_forward_tc<0x0>(m, M, X, Y, st, err, sms);
+        case 3: return mlp_forward_tc<0x8>(m, M, X, Y, st, err, sms);
+        case 4: return mlp_forward_tc<0xA>(m, M, X, Y, st, err, sms);
+        case 5: return mlp_forward_tc<0xE>(m, M, X, Y, st, err, sms);
+        default: break;
     }
     if (!smem_set) {
         const cudaError_t e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMiSmem);
@@ -1287,7 +1338,7 @@ CCTStatusType mps_mlp_forward(MpsMlp* m, int M, const float* X, float* Y, void* 
 }
 
 CCTStatusType mps_mlp_forward_variant(MpsMlp* m, int M, const float* X, float* Y, int variant, void* stream) {
-    if (!m || M < 0 || variant < 0 || variant > 1) return CCT_PARAMERR;
+    if (!m || M < 0 || variant < 0 || variant > 5) return CCT_PARAMERR;
     if (M == 0) return CCT_NOERR;
     return cuda_status(mlp_forward_variant(m, M, X, Y, (cudaStream_t)stream, variant, nullptr));
 }

@@ -80,7 +80,8 @@ class Mlp:
 
     def forward(self, X_dev, Y_dev, M, variant=None):
         """Y = MLP(X) on the device; variant None: the library's kernel (tcgen05), 0 the
-        same, 1 the mma.sync cross-check kernel."""
+        same, 1 the mma.sync cross-check kernel, 2..5 the tcgen05 kernel with 0..3 of
+        every 4 pairs of hidden activations on the FMA pipe."""
         if variant is None:
             _check(_lib().mps_mlp_forward(self.h, M, X_dev, Y_dev, None), "mps_mlp_forward")
         else:

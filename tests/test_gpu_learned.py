@@ -105,6 +105,28 @@ def test_tcgen05_inference_matches_mma_sync_and_oracle(rows):
     assert Mlp.tc_timeouts() == 0
 
 
+@pytest.mark.parametrize("variant", [2, 3, 4, 5])
+def test_tcgen05_inference_with_fma_pipe_silu(variant):
+    """The tcgen05 kernel with 0, 1, 2 or 3 of every 4 pairs of hidden activations on
+    the FMA pipe (polynomial tanh, SiLU error <= 3.6e-3 absolute) and the rest on the
+    SFU: within the oracle tolerance of the forward test, within 1e-2 of max |y| of the
+    SFU-only kernel, ragged tiles included."""
+    rows = 50021
+    m, p = _net(seed=7)
+    X = np.random.default_rng(rows).normal(0, 1, (rows, 12)).astype(np.float32)
+    dX = DeviceArray.from_host(X)
+    dY, dS = DeviceArray((rows, 2), np.float32), DeviceArray((rows, 2), np.float32)
+    m.forward(dX.ptr, dY.ptr, rows, variant=variant)
+    m.forward(dX.ptr, dS.ptr, rows, variant=2)
+    y, ys = dY.download(), dS.download()
+    ref = mo.forward(p, X)
+    scale = np.abs(ref).max()
+    assert np.isfinite(y).all()
+    assert np.abs(y - ref).max() <= 2e-2 * scale + 1e-4
+    assert np.abs(y - ys).max() <= 1e-2 * scale + 1e-4
+    assert Mlp.tc_timeouts() == 0
+
+
 def test_tcgen05_inference_wait_that_runs_out():
     """The stop path of the tcgen05 inference kernel: with its MMA completion waits
     limited to zero polls every 128-row tile stops after issuing its first layer
