@@ -3,6 +3,9 @@
     python oracle/build_ref.py            # builds oracle/liborc.so and, if possible, oracle/_ref/libref.so
 
 oracle/liborc.so   - the CPU restatement (oracle/mps_oracle.cpp), always built.
+oracle/_ref/librefgpu.so, librefgpu_nofma.so - five of the reference's particle kernels
+    compiled for sm_103a (oracle/ref_gpu_harness.cu), with and without multiply-add
+    contraction: the second baseline and a bit-for-bit check on the GPU.
 oracle/_ref/libref.so - the reference solver's own kernel header compiled for the CPU
     by oracle/ref_harness.cpp.  Its sources are decoded copies of four files of the
     reference tree (radix/SPVSOLVER/MultiGPUSolver/{DataType.h, Constant.h,
@@ -82,7 +85,41 @@ def build_ref(verbose: bool = False):
     return out
 
 
+def _nvcc():
+    import shutil
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    return None
+
+
+def build_ref_gpu(verbose: bool = False):
+    """The reference's particle kernels compiled for sm_103a by oracle/ref_gpu_harness.cu:
+    oracle/_ref/librefgpu.so (nvcc's default multiply-add contraction, as the reference's
+    project builds them) and oracle/_ref/librefgpu_nofma.so (-fmad=false, for bit-for-bit
+    comparison).  Returns the two paths, or None when the decoded sources or nvcc are
+    missing.  Call build_ref first (it writes the decoded copies)."""
+    src_dir = os.path.join(HERE, "_ref", "src")
+    nvcc = _nvcc()
+    if nvcc is None or not all(os.path.exists(os.path.join(src_dir, n)) for n in REF_FILES):
+        return None
+    harness = os.path.join(HERE, "ref_gpu_harness.cu")
+    deps = [harness] + [os.path.join(src_dir, n) for n in REF_FILES]
+    outs = []
+    for name, extra in (("librefgpu.so", []), ("librefgpu_nofma.so", ["-fmad=false"])):
+        out = os.path.join(HERE, "_ref", name)
+        if _stale(out, deps):
+            cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+                   "-Xcompiler", "-fPIC", "-cudart", "static", "-w", "-I" + src_dir] + extra + [harness, "-o", out]
+            if verbose:
+                print(" ".join(cmd))
+            subprocess.check_call(cmd)
+        outs.append(out)
+    return tuple(outs)
+
+
 if __name__ == "__main__":
     print(build_oracle(verbose=True))
     print(build_ref(verbose=True))
+    print(build_ref_gpu(verbose=True))
     sys.exit(0)

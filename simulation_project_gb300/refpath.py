@@ -60,7 +60,13 @@ class RefStep:
 
     IN = ["id", "pos", "vel", "pressure", "density", "temperature", "kin_visc", "solid_rate", "type"]
 
-    def __init__(self, scene, explicit_sonic=20.0):
+    # the particle launchers of the step, in call order; _kernel runs them
+    PARTICLE_KERNELS = ("CalcSTLDistance", "CalcDragEffect", "CalcExplicitly", "CalcExplicitPressure",
+                        "CalcExplicitPressureGradient")
+
+    def __init__(self, scene, explicit_sonic=20.0, capacity=None):
+        """capacity: entries allocated per particle array (>= the particle count; the
+        entries past it are zero), for callers whose kernels touch whole thread grids."""
         lib.load()
         p = scene.param
         p.bExplicitPressure = True
@@ -68,6 +74,8 @@ class RefStep:
         self.param, self.box = p, scene.box
         n = scene.n
         self.n = n
+        cap = n if capacity is None else max(int(capacity), n)
+        self.capacity = cap
         self.cells = scene.box.cell_num
         self.t = scene.t
         f3 = lambda: np.zeros((n, 3), np.float32)  # noqa: E731
@@ -87,6 +95,11 @@ class RefStep:
             "magnifier_count": np.zeros(n, np.int32), "turb_visc": np.zeros(n, np.float32),
             "strain": np.zeros(n, np.float32), "hash": np.zeros(n, np.int32), "index": np.zeros(n, np.int32),
         }
+        if cap > n:
+            for k, v in host.items():
+                if k not in ("triangles", "cells", "cell_start", "cell_end") and v.shape[0] == n:
+                    pad = np.zeros((cap - n,) + v.shape[1:], v.dtype)
+                    host[k] = np.concatenate([v, pad])
         self.d = {k: DeviceArray.from_host(np.ascontiguousarray(v)) for k, v in host.items()}
         tp = (CTriangleParameters * max(len(scene.tri_params), 1))(*scene.tri_params)
         dp = (DragParameter * max(len(scene.drag), 1))(*scene.drag)
@@ -124,17 +137,21 @@ class RefStep:
         self._topology(n)
         call("ResetTriangleTopology", s, self.cells, d("cells"))
         call("RegisterTriangleTopology", s, d("triangles"), self.t, d("cells"), self.cells)
-        call("CalcSTLDistance", s, n)
+        self._kernel("CalcSTLDistance", n)
         if self.drag_num:
-            call("CalcDragEffect", s, n)
-        call("CalcExplicitly", s, n)
+            self._kernel("CalcDragEffect", n)
+        self._kernel("CalcExplicitly", n)
         self._topology(n)
-        call("CalcSTLDistance", s, n)
-        call("CalcExplicitPressure", s, n)
-        call("CalcExplicitPressureGradient", s, n)
+        self._kernel("CalcSTLDistance", n)
+        self._kernel("CalcExplicitPressure", n)
+        self._kernel("CalcExplicitPressureGradient", n)
         call("UpdateTrianglePosition", s, self.t, d("triangles"))
         call("RotateTrianglePosition", s, self.t, d("triangles"), i)
         return n
+
+    def _kernel(self, name, n):
+        """One of PARTICLE_KERNELS over n particles on the step's stream."""
+        call(name, self.stream.ref(), n)
 
     def sync(self):
         self.stream.sync()
