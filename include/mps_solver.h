@@ -110,7 +110,9 @@ typedef struct MpsSolverOptions {
                                the first refinement residual it computes for the solve,
                                minus the same span of the last step without the guess, in
                                iterations of the same step; when it costs more,
-                               it is skipped for 2, 8, 32, 64 steps before the next trial.
+                               it is skipped for 2, 8, 32, 64 steps before the next trial,
+                               longer (doubling up to the ratio of its cost to its saving,
+                               at most 64) the further it falls short.
                                The first step with the guess is followed by one without it
                                (the span it is compared with).  0: it runs every step */
     int fine_smoother;      /* fine level of the multilevel preconditioner: 0 (default)

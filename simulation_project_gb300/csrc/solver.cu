@@ -180,8 +180,15 @@ struct Solver {
         S.learned_saved_its = (float)saved;
         S.learned_cost_its = (float)cost;
         if (saved < cost) {
-            gate_skip = gate_period;
-            gate_period = std::min(4 * gate_period, 64);
+            // the further the guess falls short of paying for itself, the longer it sits
+            // out: at least the current period, doubled up to the cost / saving ratio
+            // (a guess that recovers a twentieth of its cost is tried again after 32
+            // steps), at most 64
+            const double ratio = saved > 0.0 ? cost / saved : 64.0;
+            int skip = gate_period;
+            while (skip < 64 && skip < ratio) skip *= 2;
+            gate_skip = std::min(skip, 64);
+            gate_period = std::min(4 * gate_skip, 64);
         } else {
             gate_period = 2;
         }
