@@ -59,6 +59,11 @@ STEP_FIXED_B, STEP_ITER_B, STEP_IR_B = 760.0, 72.0, 48.0
 # with 16-bit column offsets: 1.3376 GB read + 2.2 MB written for 201.36M entries
 # (SELL padding included)
 SPMV_DRAM_BYTES_PER_ENTRY = (1.33758e9 + 2.24e6) / 201.362e6
+# warp instructions per particle of the two FP32 neighbour passes, counted by ncu
+# (smsp__inst_executed.sum, one launch on the bucket at l0 = 0.004, 108,186 particles):
+# the list pass 233.67M, the predictor 213.7M
+NB_LIST_INST_PER_PARTICLE = 233.67e6 / 108186
+NB_PRED_INST_PER_PARTICLE = 213.7e6 / 108186
 # the same for the FP16-weight kernel of the inner CG (k_spmv_stream<..., __half>):
 # 898.3 MB read + 1.8 MB written for 201.36M entries
 SPMV16_DRAM_BYTES_PER_ENTRY = (898.3e6 + 1.8e6) / 201.362e6
@@ -332,14 +337,21 @@ def run_gpu(args):
     pair_evals = {"accepted_pairs_per_pass": int(pairs), "accepted_per_particle": round(pairs / n, 1),
                   "passes": 2, "pairs_per_s": 2.0 * pairs / (nb_ms / 1e3) if nb_ms > 0 else None}
     # each neighbour pass against the HBM roofline with its algorithmic bytes (list: 8 B
-    # per stored entry + 48 B per row; predictor: 96 B per row); both are bound by
-    # instruction issue, which the small fractions show
+    # per stored entry + 48 B per row; predictor: 96 B per row), and against the issue
+    # rate that bounds them: the warp instructions ncu counted per particle over the
+    # event-timed pass, against one instruction per cycle per scheduler (4 per SM) at the
+    # SM clock sampled during the timed steps
     nb_passes = {}
-    for key, ms, nbytes in (("list", phases["ms_list"], 8.0 * pairs + 48.0 * n),
-                            ("predictor", phases["ms_predictor"], 96.0 * n)):
+    sms = lib_sm_count()
+    sm_hz = (clk.get("sm_mhz") or 0.0) * 1e6
+    for key, ms, nbytes, ipp in (("list", phases["ms_list"], 8.0 * pairs + 48.0 * n, NB_LIST_INST_PER_PARTICLE),
+                                 ("predictor", phases["ms_predictor"], 96.0 * n, NB_PRED_INST_PER_PARTICLE)):
         gbs = nbytes / (ms / 1e3) / 1e9 if ms > 0 else 0.0
+        issue = (ipp * n / (ms / 1e3)) / (4.0 * sms * sm_hz) if ms > 0 and sms and sm_hz else None
         nb_passes[key] = {"ms": round(ms, 3), "bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
-                          "hbm_frac": round(gbs / peak_gbs, 4), "bound": "issue"}
+                          "hbm_frac": round(gbs / peak_gbs, 4), "bound": "issue",
+                          "warp_instructions_per_particle": round(ipp, 1),
+                          "issue_frac": round(issue, 3) if issue is not None else None}
     pair_evals["passes_vs_hbm"] = nb_passes
 
     # end to end through the C-ABI from pinned host buffers
@@ -795,6 +807,13 @@ def run_e2e(solver, args):
         lib.call("mps_host_free_pinned", p)
     return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 56,
             "d2h_bytes_per_step": n * 56, "steps": steps}
+
+
+def lib_sm_count():
+    """SMs of the current device (the library's runtime query), 0 if unavailable."""
+    from simulation_project_gb300 import lib
+    c = C.c_int(0)
+    return c.value if lib.load().mps_device_sm_count(C.byref(c)) == 0 else 0
 
 
 def cpu_baseline(args):

@@ -19,6 +19,8 @@ extern "C" {
 #endif
 
 CCTStatusType mps_device_count(int* count);
+/* streaming multiprocessors of the current device */
+CCTStatusType mps_device_sm_count(int* count);
 CCTStatusType mps_set_device(int device);
 CCTStatusType mps_malloc(void** ptr, size_t bytes);
 CCTStatusType mps_free(void* ptr);

@@ -67,6 +67,13 @@ using mps::rec;
 extern "C" {
 
 CCTStatusType mps_device_count(int* count) { return rec(cudaGetDeviceCount(count)); }
+CCTStatusType mps_device_sm_count(int* count) {
+    if (!count) return CCT_PARAMERR;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(count, cudaDevAttrMultiProcessorCount, dev);
+    return rec(e);
+}
 CCTStatusType mps_set_device(int device) { return rec(cudaSetDevice(device)); }
 CCTStatusType mps_malloc(void** ptr, size_t bytes) { return rec(cudaMalloc(ptr, bytes ? bytes : 1)); }
 CCTStatusType mps_free(void* ptr) { return rec(cudaFree(ptr)); }

@@ -19,6 +19,7 @@ I = C.c_int
 _SIGS = {
     # runtime helpers (include/mps_runtime.h)
     "mps_device_count": (I, [C.POINTER(I)]),
+    "mps_device_sm_count": (I, [C.POINTER(I)]),
     "mps_set_device": (I, [I]),
     "mps_malloc": (I, [C.POINTER(P), C.c_size_t]),
     "mps_free": (I, [P]),
