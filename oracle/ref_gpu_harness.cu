@@ -124,6 +124,9 @@ int refgpu_bind(const HarnessBindings* b) {
     return 0;
 }
 
+/* layout probe: the bindings record's size, checked against the tests' OrcBindings */
+int refgpu_sizeof_bindings(void) { return (int)sizeof(HarnessBindings); }
+
 /* c_ParticleNum after a compaction (ParticleNumberToConst) */
 int refgpu_particle_num(int n) {
     HARNESS_SET(c_ParticleNum, (Integer)n);
