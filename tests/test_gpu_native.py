@@ -345,3 +345,26 @@ def test_warm_start_extrapolation_converges_to_the_same_pressure(order):
         assert sb["warm_start"] == 0 and sa["warm_start"] == min(i, order)
     pa, pb = a.state()["press"], b.state()["press"]
     assert np.abs(pa - pb).max() <= 1e-4 * np.abs(pb).max()
+
+
+@pytest.mark.parametrize("precision", ["fp32_ir", "fp64"])
+def test_neighbour_row_overflow_is_flagged_and_capped(precision):
+    """A Laplacian row longer than its capacity (max_neighbours = 128 against about 250
+    neighbours at re = 4 l0) sets MPS_ERR_NEIGHBOUR_CAP, keeps the row at the capacity
+    and reports the uncapped length as max_row: no row is cut silently and no store
+    leaves the row.  Counts are those of a full-capacity solver of the same scene,
+    capped."""
+    sc = scenes.rotating_bucket(l0=0.012, n_drag=0)
+    full = Solver(sc, precision=precision)
+    capped = Solver(sc, precision=precision, max_neighbours=128)
+    sf, sc_ = full.step(0), capped.step(0)
+    assert sf["error_flags"] == 0 and sf["max_row"] > 128, sf
+    assert sc_["error_flags"] & 2, sc_
+    assert sc_["max_row"] == sf["max_row"]
+    a, b = full.debug_ppe(), capped.debug_ppe()
+    oa, ob = np.argsort(a["id"], kind="stable"), np.argsort(b["id"], kind="stable")
+    assert np.array_equal(a["id"][oa], b["id"][ob])
+    assert np.array_equal(np.minimum(a["nbr_count"][oa], 128), b["nbr_count"][ob])
+    assert b["nbr_count"].max() == 128
+    # the solver stays usable: a second step runs and flags the overflow again
+    assert capped.step(1)["error_flags"] & 2
