@@ -17,6 +17,9 @@
   2e-3 of the largest speed, kinetic energy 1e-4 relative, positions 1e-4 l0; the
   measured errors are printed (GB300: pressure 3.4e-4, PND 6.2e-6, velocity 1.6e-4,
   kinetic energy 6.2e-5, positions 2.7e-6 l0).
+* Config 3, the benchmark's workload (the bucket at l0 = 0.002, 882,080 particles): the
+  FP64 oracle, the FP64 GPU solver and the FP32-IR GPU solver with the benchmark's
+  default settings in lockstep for 3 steps, against the FP64 and FP32 bars above.
 * The reference-named explicit schedule (CalcSTLDistance, CalcDragEffect,
   CalcExplicitly, then CalcExplicitPressure and CalcExplicitPressureGradient on the
   predicted positions) on the config-2 scene, bit-identical to the oracle, and the
@@ -47,7 +50,7 @@ def _run_pair(sc, precision, steps=STEPS, **opts):
     return o, g
 
 
-def _fp64_bar(sc, o, g):
+def _fp64_bar(sc, o, g, steps=STEPS):
     gp = g.debug_ppe()
     og = np.argsort(gp["id"], kind="stable")
     on = o.neighbours()
@@ -60,7 +63,7 @@ def _fp64_bar(sc, o, g):
     assert pmax > 0
     err_p = np.abs(a["press"] - b["press"]).max() / pmax
     err_x = np.abs(a["pos"] - b["pos"]).max() / sc.param.InitialParticleDistance
-    print(f"\n{sc.name} n={sc.n} FP64 after {STEPS} steps: pressure {err_p:.2e}, positions {err_x:.2e} l0")
+    print(f"\n{sc.name} n={sc.n} FP64 after {steps} steps: pressure {err_p:.2e}, positions {err_x:.2e} l0")
     assert err_p <= 1e-6, err_p
     assert err_x <= 1e-6, err_x
 
@@ -96,9 +99,7 @@ def _oracle_triangles(o, sc):
     return v
 
 
-def test_config2_bucket_fp32_ir_against_fp64_oracle():
-    sc = _bucket()
-    o, g = _run_pair(sc, "fp32_ir")
+def _fp32_bar(label, sc, o, g, steps=STEPS):
     a, b = g.state(), o.state()
     assert np.array_equal(a["id"], b["id"])
     l0 = sc.param.InitialParticleDistance
@@ -110,14 +111,48 @@ def test_config2_bucket_fp32_ir_against_fp64_oracle():
         "kinetic_energy": abs((a["vel"] ** 2).sum() - (b["vel"] ** 2).sum()) / (b["vel"] ** 2).sum(),
         "position_l0": np.abs(a["pos"] - b["pos"]).max() / l0,
     }
-    print(f"\nconfig 2 FP32-IR vs FP64 oracle after {STEPS} steps: " +
+    print(f"\n{label} FP32-IR vs FP64 oracle after {steps} steps: " +
           ", ".join(f"{k} {v:.2e}" for k, v in err.items()))
     assert err["pressure"] <= 2e-3, err
     assert err["pnd"] <= 1e-5, err
     assert err["velocity"] <= 2e-3, err
     assert err["kinetic_energy"] <= 1e-4, err
     assert err["position_l0"] <= 1e-4, err
+
+
+def test_config2_bucket_fp32_ir_against_fp64_oracle():
+    sc = _bucket()
+    o, g = _run_pair(sc, "fp32_ir")
+    _fp32_bar("config 2", sc, o, g)
     g.close()
+    o.close()
+
+
+CONFIG3_STEPS = 3
+
+
+def test_config3_bucket_fp64_and_fp32_ir_against_fp64_oracle():
+    """Config 3, the benchmark's own workload (the bucket at l0 = 0.002: 882,080
+    particles, 4096-triangle cylinder, 64 drag spheres; the scene bench.py times), in
+    lockstep for 3 steps: the FP64 oracle solver, the FP64 GPU solver (FP64 bar:
+    identical neighbour sets, pressure 1e-6, positions 1e-6 l0) and the FP32-IR GPU
+    solver with the default settings the benchmark runs (multilevel preconditioner,
+    FP16-weight inner operator streamed by bulk copies, pressure-history warm start;
+    FP32 bar as for config 2).  Every solve reaches the 1e-8 relative residual."""
+    sc = scenes.rotating_bucket(l0=0.002, dt=5e-5, seed=4, n_drag=64, drag_seed=3)
+    assert sc.n > 850_000 and len(sc.drag) == 1
+    o = orc.OracleSim(sc)
+    g64 = Solver(sc, precision="fp64")
+    g32 = Solver(sc, precision="fp32_ir")
+    for i in range(CONFIG3_STEPS):
+        rc, ost = o.step(i)
+        s64, s32 = g64.step(i), g32.step(i)
+        assert rc == 0 and s64["error_flags"] == 0 and s32["error_flags"] == 0, (i, s64, s32)
+        assert max(ost["cg_relres"], s64["cg_relres"], s32["cg_relres"]) <= 1e-8, (i, ost, s64, s32)
+    _fp64_bar(sc, o, g64, CONFIG3_STEPS)
+    _fp32_bar("config 3", sc, o, g32, CONFIG3_STEPS)
+    g64.close()
+    g32.close()
     o.close()
 
 
