@@ -81,7 +81,8 @@ typedef struct MpsSolverOptions {
                                through shared memory by bulk copies (a ring of 2 stages of
                                8 entries per warp); same row values.  Both solvers: the
                                FP32 inner CG, and the FP64 solver's CG products and
-                               residuals over its FP64 weights */
+                               residuals over its FP64 weights; also the multilevel
+                               preconditioner's level-1 assembly (same sums) */
     int inner_weights;      /* 16 (default): the inner CG uses FP16 copies of the FP32 weights
                                with the diagonal recomputed from the rounded weights (a
                                consistent Laplacian within ~5e-4 of the FP32 one; the
@@ -214,6 +215,13 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* r, do
  * operator (inner_weights = 16) with 16-bit / 32-bit columns, the same bits as each
  * other. */
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* x, float* y);
+/* Level-1 Galerkin stencil of the multilevel preconditioner, reassembled from the
+ * current rows (FP32_IR after a step with the multilevel preconditioner): variant 0 the
+ * register walk over the SELL-32 rows, 1 the rows streamed through shared memory by
+ * bulk copies (spmv_stream = 1); both give the same bits.  *n1 = level-1 unknowns; with
+ * a non-null a (room for cap >= 27 n1 floats) the stencil is copied out, 27 slots per
+ * unknown, slot (dx+1)*9 + (dy+1)*3 + (dz+1) of the neighbouring cell. */
+CCTStatusType mps_solver_debug_level1(MpsSolver* s, int variant, float* a, int cap, int* n1);
 /* Time step from the next step on (a dt schedule row, mps_dt_schedule_next in
  * mps_io.h): Dt, and CourantNumber when courant > 0; the constants that depend on them
  * are recomputed as at creation, so the solver continues exactly as one created with

@@ -152,6 +152,75 @@ __global__ void k_mg_particles(const __grid_constant__ Dev d, const __grid_const
 // shuffle tree, and the segment's first lane stores the 27 slot sums and the
 // diagonal sum at its row.  Fixed orders: deterministic.
 constexpr int kMgAsmWarps = 4;
+
+// entries of one SELL-32 entry group into the lane's 27 slot sums A[.][lane]
+__device__ __forceinline__ void mg_asm_add8(const Mg& mg, float (*A)[32], int lane, unsigned pi, const unsigned (&pq)[8],
+                                            const float (&wv)[8]) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        if (!(pq[u] & 0x80000000u)) continue;   // not interior, or no entry
+        const unsigned dd = (pq[u] & 0x3fffffffu) + 0x00100401u - pi;
+        const unsigned fx = dd >> 20, fy = (dd >> 10) & 1023u, fz = dd & 1023u;
+        if (fx <= 2u && fy <= 2u && fz <= 2u) A[fx * 9 + fy * 3 + fz][lane] += wv[u];
+    }
+}
+
+// the register walk of one slice's rows (8 entries' columns and weights in flight)
+template <class TW>
+__device__ __forceinline__ void mg_asm_walk(const Dev& d, const Mg& mg, const TW* __restrict__ w, float (*A)[32],
+                                            int lane, int sl, int cnt, unsigned pi) {
+    const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+    const int sb = (sizeof(TW) == 4 && d.rows16) ? d.sbase[sl] : -1;
+    const size_t base = (size_t)sl * d.K * 32 + lane;
+    for (int k = 0; k < kmax; k += 8) {
+        int jj[8];
+        float wv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const size_t e = base + (size_t)min(k + u, kmax - 1) * 32;
+            jj[u] = sb >= 0 ? sell_col<true>(d, e, sb) : sell_col<false>(d, e, sb);
+            wv[u] = (float)__ldcs(w + e);
+        }
+        unsigned pq[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) pq[u] = k + u < cnt ? mg.pcc[jj[u]] : 0u;
+        mg_asm_add8(mg, A, lane, pi, pq, wv);
+    }
+}
+
+// segmented sums over the lanes of each cell (contiguous rows) into the segment's first
+// lane, which stores the 27 slot sums and the diagonal sum at its row
+__device__ __forceinline__ void mg_asm_finish(const Dev& d, const Mg& mg, float (*A)[32], int lane, int i, bool row,
+                                              bool in, int seg) {
+    __syncwarp();
+    const int prev = __shfl_up_sync(0xffffffffu, seg, 1);
+    const bool head = row && seg >= 0 && (lane == 0 || prev != seg);
+    bool same[5];
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const int o = 1 << q;
+        const int sn = __shfl_down_sync(0xffffffffu, seg, o);
+        same[q] = lane + o < 32 && sn == seg;
+    }
+    double ds = in ? d.diag[i] : 0.0;
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        const double t = __shfl_down_sync(0xffffffffu, ds, 1 << q);
+        if (same[q]) ds += t;
+    }
+    if (head) mg.partd[i] = ds;
+    for (int t = 0; t < 27; ++t) {
+        float v = A[t][lane];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) {
+            const float x = __shfl_down_sync(0xffffffffu, v, 1 << q);
+            if (same[q]) v += x;
+        }
+        if (head) mg.part[(size_t)i * 27 + t] = v;
+    }
+    __syncwarp();
+}
+
 template <class TW>
 __global__ void __launch_bounds__(kMgAsmWarps * 32) k_mg_assemble_rows(const __grid_constant__ Dev d,
                                                                        const __grid_constant__ Mg mg,
@@ -166,62 +235,82 @@ __global__ void __launch_bounds__(kMgAsmWarps * 32) k_mg_assemble_rows(const __g
         const bool row = i < d.n;
         const bool in = row && d.inner[i];
         const int cnt = in ? d.nbr_cnt[i] : 0;
-        const int kmax = __reduce_max_sync(0xffffffffu, cnt);
         const unsigned pi = (row ? mg.pcc[i] : 0u) & 0x3fffffffu;
         const int seg = row ? mg.agg1[i] : -1;
-        const int sb = (sizeof(TW) == 4 && d.rows16) ? d.sbase[sl] : -1;
-        const size_t base = (size_t)sl * d.K * 32 + lane;
 #pragma unroll
         for (int t = 0; t < 27; ++t) A[t][lane] = 0.f;
         __syncwarp();
-        for (int k = 0; k < kmax; k += 8) {
-            int jj[8];
-            float wv[8];
+        mg_asm_walk<TW>(d, mg, w, A, lane, sl, cnt, pi);
+        mg_asm_finish(d, mg, A, lane, i, row, in, seg);
+    }
+}
+
+// The same pass over streamed rows: the 16-bit slices' columns and FP32 weights move
+// into a per-warp shared-memory ring by bulk copies (SliceRing, as the streamed SpMV),
+// so only the pcc gathers wait on memory.  Each lane adds its row's entries in row
+// order as the register walk does: the same sums, bit for bit.  32-bit slices, and
+// every slice after a stage wait that timed out (which abandons the stream), take the
+// register walk.
+template <int SC, int SS, int W, int MINB>
+__global__ void __launch_bounds__(W * 32, MINB) k_mg_assemble_stream(const __grid_constant__ Dev d,
+                                                                     const __grid_constant__ Mg mg,
+                                                                     const float* __restrict__ w) {
+    static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
+    extern __shared__ __align__(128) unsigned char stream_smem[];
+    __shared__ __align__(8) unsigned long long bars[W][SS];
+    __shared__ float acc[W][27][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float (*A)[32] = acc[warp];
+    const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
+    SliceRing<SC, SS, float, false> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, float, false>::SB, bars[warp], gw, nw);
+    for (int sl = gw; sl < R.nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const unsigned pi = (row ? mg.pcc[i] : 0u) & 0x3fffffffu;
+        const int seg = row ? mg.agg1[i] : -1;
+        const int km = d.skmax[sl];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const size_t e = base + (size_t)min(k + u, kmax - 1) * 32;
-                jj[u] = sb >= 0 ? sell_col<true>(d, e, sb) : sell_col<false>(d, e, sb);
-                wv[u] = (float)__ldcs(w + e);
-            }
-            unsigned pq[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) pq[u] = k + u < cnt ? mg.pcc[jj[u]] : 0u;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                if (!(pq[u] & 0x80000000u)) continue;   // not interior, or no entry
-                const unsigned dd = (pq[u] & 0x3fffffffu) + 0x00100401u - pi;
-                const unsigned fx = dd >> 20, fy = (dd >> 10) & 1023u, fz = dd & 1023u;
-                if (fx <= 2u && fy <= 2u && fz <= 2u) A[fx * 9 + fy * 3 + fz][lane] += wv[u];
-            }
-        }
+        for (int t = 0; t < 27; ++t) A[t][lane] = 0.f;
         __syncwarp();
-        // segmented sums over the lanes of each cell, into the segment's first lane
-        const int prev = __shfl_up_sync(0xffffffffu, seg, 1);
-        const bool head = row && seg >= 0 && (lane == 0 || prev != seg);
-        bool same[5];
+        bool done = false;
+        if (km >= 0 && R.streaming) {
+            const int nc = (km + SC - 1) / SC;
+            const int r0 = sl * 32;
+            for (int c = 0; c < nc; ++c) {
+                const unsigned char* cs;
+                const float* ws;
+                if (!R.acquire(cs, ws)) break;
+                const int k0 = c * SC;
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            const int o = 1 << q;
-            const int sn = __shfl_down_sync(0xffffffffu, seg, o);
-            same[q] = lane + o < 32 && sn == seg;
-        }
-        double ds = in ? d.diag[i] : 0.0;
+                for (int g = 0; g < SC; g += 8) {
+                    int j[8];
+                    float wv[8];
 #pragma unroll
-        for (int q = 0; q < 5; ++q) {
-            const double t = __shfl_down_sync(0xffffffffu, ds, 1 << q);
-            if (same[q]) ds += t;
-        }
-        if (head) mg.partd[i] = ds;
-        for (int t = 0; t < 27; ++t) {
-            float v = A[t][lane];
+                    for (int u = 0; u < 8; ++u) {
+                        j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
+                        wv[u] = ws[(g + u) * 32 + lane];
+                    }
+                    unsigned pq[8];
 #pragma unroll
-            for (int q = 0; q < 5; ++q) {
-                const float x = __shfl_down_sync(0xffffffffu, v, 1 << q);
-                if (same[q]) v += x;
+                    for (int u = 0; u < 8; ++u) pq[u] = k0 + g + u < cnt ? mg.pcc[j[u]] : 0u;
+                    mg_asm_add8(mg, A, lane, pi, pq, wv);
+                }
+                R.release();
             }
-            if (head) mg.part[(size_t)i * 27 + t] = v;
+            done = R.streaming;
         }
-        __syncwarp();
+        if (!done) {
+            // partial sums of an abandoned stream are dropped
+            __syncwarp();
+#pragma unroll
+            for (int t = 0; t < 27; ++t) A[t][lane] = 0.f;
+            __syncwarp();
+            mg_asm_walk<float>(d, mg, w, A, lane, sl, cnt, pi);
+        }
+        mg_asm_finish(d, mg, A, lane, i, row, in, seg);
     }
 }
 

@@ -490,6 +490,25 @@ struct Solver {
         return CCT_NOERR;
     }
 
+    // level-1 Galerkin stencil of the current rows (mg.L[1].a, dinv): variant 1 streams
+    // the 16-bit slices' rows through shared memory, 0 walks them from registers (same
+    // sums), -1 follows spmv_stream
+    int asm_grid = 0;
+    CCTStatusType mg_assemble(cudaStream_t ss, int variant) {
+        const bool stream = variant < 0 ? use_stream() : variant == 1;
+        if (stream) {
+            auto k = k_mg_assemble_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            const int g = stream_grid_for(k, kSsSmem, asm_grid);
+            if (g < 0) return CCT_CUDAERR;
+            MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, kSsSmem, ss>>>(d, mg, (const float*)d.nbrw);
+        } else {
+            MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, ss>>>(d, mg,
+                                                                                           (const float*)d.nbrw);
+        }
+        MPS_COUNT_LAUNCH k_mg_assemble_cells<<<div_up(mg.L[1].n * 32, 256), 256, 0, ss>>>(d, mg);
+        return cuda_status(cudaGetLastError());
+    }
+
     // aggregates, links and operators of the current particle order (after the PPE
     // setup: needs interior flags, diagonals and the FP32 neighbour rows)
     CCTStatusType mg_setup(cudaStream_t ss) {
@@ -525,8 +544,7 @@ struct Solver {
             MPS_COUNT_LAUNCH k_mg_nbpar<<<blocks_for(27 * L[l].n), kBlock, 0, ss>>>(L[l]);
         MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, ss>>>(d, mg);
         MPS_COUNT_LAUNCH k_mg_rows<<<blocks_for(L[1].n), kBlock, 0, ss>>>(d, mg);
-        MPS_COUNT_LAUNCH k_mg_assemble_rows<float><<<kRedBlocks, kMgAsmWarps * 32, 0, ss>>>(d, mg, (const float*)d.nbrw);
-        MPS_COUNT_LAUNCH k_mg_assemble_cells<<<div_up(L[1].n * 32, 256), 256, 0, ss>>>(d, mg);
+        if (mg_assemble(ss, -1) != CCT_NOERR) return CCT_CUDAERR;
         for (int l = 1; l < levels; ++l)
             MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, ss>>>(L[l], L[l + 1]);
         const int nd = L[levels].n;
@@ -1672,6 +1690,22 @@ CCTStatusType mps_solver_debug_residual(MpsSolver* s, int variant, double* host_
     if (relres) *relres = S.h_scal[mps::S_BNORM] > 0 ? S.h_scal[mps::S_RNORM] / S.h_scal[mps::S_BNORM] : 0.0;
     if (host_r) return mps::cuda_status(cudaMemcpy(host_r, d.r, sizeof(double) * d.n, cudaMemcpyDeviceToHost));
     return CCT_NOERR;
+}
+
+CCTStatusType mps_solver_debug_level1(MpsSolver* s, int variant, float* host_a, int cap, int* n1) {
+    if (!s || !n1 || variant < 0 || variant > 1) return CCT_PARAMERR;
+    mps::Solver& S = s->s;
+    if (S.fp64() || S.d.n <= 0 || !S.mg_ready) return CCT_PARAMERR;
+    if (variant == 1 && !S.use_stream()) return CCT_PARAMERR;
+    *n1 = S.mg.L[1].n;
+    if (!host_a) return CCT_NOERR;
+    if (cap < 27 * *n1) return CCT_PARAMERR;
+    const CCTStatusType rc = S.mg_assemble(S.st, variant);
+    if (rc != CCT_NOERR) return rc;
+    cudaError_t e = cudaMemcpyAsync(host_a, S.mg.L[1].a, sizeof(float) * 27 * (size_t)*n1, cudaMemcpyDeviceToHost,
+                                    S.st);
+    if (!e) e = cudaStreamSynchronize(S.st);
+    return mps::cuda_status(e);
 }
 
 CCTStatusType mps_solver_debug_spmv(MpsSolver* s, int kernel, const float* host_x, float* host_y) {

@@ -69,6 +69,7 @@ _SIGS = {
     "mps_solver_debug_ppe": (C.c_int, [P, P, P, P, P, P, P, P]),
     "mps_solver_debug_history": (C.c_int, [P, P, P, P, P, P]),
     "mps_solver_debug_spmv": (C.c_int, [P, C.c_int, P, P]),
+    "mps_solver_debug_level1": (C.c_int, [P, C.c_int, P, C.c_int, C.POINTER(C.c_int)]),
     "mps_solver_debug_wall_bins": (C.c_int, [P, P, P, C.c_int, C.POINTER(C.c_int)]),
     "mps_solver_save_frame": (C.c_int, [P, C.c_char_p, C.c_int, C.c_double, C.c_int, P, P]),
     "mps_solver_add_particles": (C.c_int, [P, C.c_int, P, C.POINTER(C.c_int)]),
@@ -233,6 +234,17 @@ class Solver:
         y = np.zeros(n, np.float32)
         _check(_lib().mps_solver_debug_spmv(self.h, int(kernel), _p(xs), _p(y)), "mps_solver_debug_spmv")
         return y
+
+    def debug_level1(self, variant: int) -> np.ndarray:
+        """Level-1 Galerkin stencil [n1, 27] reassembled from the current rows by the
+        register walk (variant 0) or the streamed rows (variant 1)."""
+        L = _lib()
+        n1 = C.c_int()
+        _check(L.mps_solver_debug_level1(self.h, int(variant), None, 0, C.byref(n1)), "mps_solver_debug_level1")
+        a = np.zeros((n1.value, 27), np.float32)
+        _check(L.mps_solver_debug_level1(self.h, int(variant), _p(a), a.size, C.byref(n1)),
+               "mps_solver_debug_level1")
+        return a
 
     def debug_wall_bins(self) -> dict:
         """Per-cell triangle lists of the wall search: {(cell, kind): [triangle ids]} for
