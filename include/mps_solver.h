@@ -107,10 +107,11 @@ typedef struct MpsSolverOptions {
                                pays: after each learned step the solver compares the CG
                                iterations it saved (the residual reduction it gave, at the
                                step's own contraction per iteration) with its cost: the
-                               CUDA-event time from the rows' assembly to the solve, less
-                               the first refinement residual it computes for the solve,
-                               minus the same span of the last step without the guess, in
-                               iterations of the same step; when it costs more,
+                               CUDA-event time from the rows' assembly to the solve (a
+                               span that holds the first refinement residual in every
+                               step, with or without the guess) minus the same span of the
+                               last step without the guess, in iterations of the same
+                               step; when it costs more,
                                it is skipped for 2, 8, 32, 64 steps before the next trial,
                                longer (doubling up to the ratio of its cost to its saving,
                                at most 64) the further it falls short.

@@ -607,6 +607,7 @@ __device__ __forceinline__ bool coop_barrier(unsigned* bar, unsigned* err, long 
 // (k_mg_up_fine_z).  Values other CTAs wrote in this launch are read through L2.
 __global__ void __launch_bounds__(256) k_mg_coarse_cycle(const double* __restrict__ scal, Mg mg,
                                                          unsigned* __restrict__ bar, unsigned* __restrict__ err) {
+    pdl_trigger();   // launched in stream order: only lets the next kernel's launch overlap
     if (scal[S_CONV] != 0.0) return;   // the same for every CTA of the launch
     const int lane = threadIdx.x & 31;
     const int w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
@@ -669,6 +670,8 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
                                                       const TV* __restrict__ r, TV* __restrict__ z,
                                                       TV* __restrict__ p, const float* __restrict__ m32, int mode,
                                                       int slot, const TV* __restrict__ qf = nullptr) {
+    pdl_wait();
+    pdl_trigger();
     if (d.scal[S_CONV] != 0.0) return;
     const MgLevel& lo = mg.L[1];
     const MgLevel& hi = mg.L[2];
@@ -748,6 +751,8 @@ template <class TV, class TXA>
 __global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
                                                             TXA* __restrict__ x, TV* __restrict__ r,
                                                             const TV* __restrict__ p, const TV* __restrict__ q, int slot) {
+    pdl_wait();
+    pdl_trigger();
     if (d.scal[S_CONV] != 0.0) return;
     const MgLevel& L1 = mg.L[1];
     const TV alpha = (TV)d.scal[S_ALPHA];

@@ -12,6 +12,8 @@
 
 #include "native.cuh"
 
+#include <utility>
+
 namespace mps {
 
 constexpr int kNbThreads = 256;
@@ -22,6 +24,31 @@ constexpr int kVecThreads = 256;
 enum { NB_PREDICT = 0, NB_LIST = 1 };
 
 template <class T> struct V3 { T x, y, z; };
+
+// ---- programmatic dependent launch (the CG iteration's chain of kernels) ----
+// A kernel launched by launch_pdl may be scheduled while the previous kernel of its
+// stream still runs: it waits at pdl_wait() until that kernel has completed and its
+// writes are visible, so only its launch overlaps the predecessor's tail.  Every kernel
+// launched that way calls pdl_wait() before its first read of device data; pdl_trigger()
+// lets the next kernel's CTAs be scheduled once every CTA of this one has started.
+// Both are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // ---- bulk (TMA) copies global -> shared, completed on an mbarrier ----
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -1499,6 +1526,8 @@ __global__ void __launch_bounds__(W * 32, MINB) k_spmv_stream(const __grid_const
                                                              const double* __restrict__ b, int slot) {
     static_assert(MODE == 0 || MODE == 2, "FP32 modes only");
     static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
+    pdl_wait();
+    pdl_trigger();
     if (MODE == 0 && d.scal[S_CONV] != 0.0) return;
     extern __shared__ __align__(128) unsigned char stream_smem[];
     __shared__ __align__(8) unsigned long long bars[W][SS];
@@ -1850,6 +1879,8 @@ __global__ void __launch_bounds__(256) k_cg_update(const __grid_constant__ Dev d
 
 template <class TV>
 __global__ void k_cg_p(const __grid_constant__ Dev d, TV* p, const TV* z) {
+    pdl_wait();
+    pdl_trigger();
     if (d.scal[S_CONV] != 0.0) return;
     const TV beta = (TV)d.scal[S_BETA];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.n; i += gridDim.x * blockDim.x)

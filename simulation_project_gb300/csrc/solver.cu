@@ -145,25 +145,24 @@ struct Solver {
     bool fp64() const { return opt.precision == MPS_PREC_FP64; }
 
     // ---- gate of the learned initial guess (MpsSolverOptions::learned_gate) ----
-    // events on the solver stream: [0] rows ready (warm start, learned guess, multilevel
-    // setup on either stream follow), [1, 2] the first residual of a learned step (the
-    // refinement reuses it, so it is no cost of the guess), [4, 5] the solve.  The span
-    // [0, 4] of a step without the guess (warm start + multilevel setup) is kept as the
-    // baseline; the guess costs what its step's span, less that residual, adds to it.
+    // events on the solver stream: [0] rows ready (the warm start, the first refinement
+    // residual, the learned guess and the multilevel setup on the second stream follow),
+    // [4, 5] the solve.  The span [0, 4] of a step without the guess (warm start, first
+    // residual beside the multilevel setup) is kept as the baseline; the guess costs what
+    // its step's span adds to it.
     cudaEvent_t gate_ev[6] = {};
     int gate_skip = 0, gate_period = 2;
     double gate_rb = 0.0, gate_ra = 0.0;
     double gate_span_off = -1.0;   // span of the last step without the guess [ms] (< 0: none yet)
     int gate_pending = 0;          // 1 / 2: this step's events (without / with the guess) await reading
     void gate_update(MpsStepStats& S, bool learned) {
-        float t_span = 0.f, t_res = 0.f, t_s = 0.f;
+        float t_span = 0.f, t_s = 0.f;
         cudaEventElapsedTime(&t_span, gate_ev[0], gate_ev[4]);
         cudaEventElapsedTime(&t_s, gate_ev[4], gate_ev[5]);
         if (!learned) {
             gate_span_off = t_span;
             return;
         }
-        cudaEventElapsedTime(&t_res, gate_ev[1], gate_ev[2]);
         if (gate_span_off < 0.0) {   // no baseline yet: measure one step without the guess
             gate_skip = 1;
             return;
@@ -176,7 +175,7 @@ struct Solver {
         const double per_it = std::log(S.r0_relres / S.cg_relres) / its;
         const double saved = std::log(gate_rb / gate_ra) / per_it;
         const double t_it = (double)t_s / its;
-        const double cost = ((double)t_span - (double)t_res - gate_span_off) / t_it;
+        const double cost = ((double)t_span - gate_span_off) / t_it;
         S.learned_saved_its = (float)saved;
         S.learned_cost_its = (float)cost;
         if (saved < cost) {
@@ -627,7 +626,13 @@ struct Solver {
                 MPS_COUNT_LAUNCH k_mg_up<<<div_up(L[l].n * 32, 256), 256, 0, st>>>(d.scal, L[l], L[l + 1], om);
         }
         if (fuse) {
-            MPS_COUNT_LAUNCH k_mg_up_fine_z<float><<<up1_blocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
+            if (pdl) {
+                if (MPS_COUNT_LAUNCH launch_pdl(k_mg_up_fine_z<float>, up1_blocks, 256, 0, st, d, mg, r, z, p,
+                                                (const float*)d.m32, mode, 7, qf))
+                    stream_failed = true;
+            } else {
+                MPS_COUNT_LAUNCH k_mg_up_fine_z<float><<<up1_blocks, 256, 0, st>>>(d, mg, r, z, p, d.m32, mode, 7, qf);
+            }
             return;
         }
         for (int k = 0; k < extra; ++k) {
@@ -822,14 +827,14 @@ struct Solver {
             }
             // gated steps time the span from here to the solve (with and without the guess)
             const bool gated = learned_ready && opt.learned && opt.learned_gate && !fp64();
-            const bool gate_measure = gated && use_learned;
             if (gated) cudaEventRecord(gate_ev[0], st);
             S.learned_applied = use_learned ? 1 : 0;
             flex_step = flexible_now();
             S.flexible = flex_step ? 1 : 0;
-            // the multilevel setup only needs the rows: with the learned guess it runs on
-            // the second stream meanwhile (enqueued after the learned kernels below)
-            const bool overlap_mg = use_learned && !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
+            // the multilevel setup only needs the rows: it runs on the second stream beside
+            // the warm start, the first refinement residual and the learned guess
+            // (enqueued after them, below)
+            const bool overlap_mg = !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
             mg_setup_done = false;
             if (overlap_mg) cudaEventRecord(ev_rows, st);
             const int warm = warm_order();
@@ -837,13 +842,11 @@ struct Solver {
             S.warm_start = warm;
             if (use_learned || collect) {
                 timer.mark(PH_LEARNED, st);
-                if (gate_measure) cudaEventRecord(gate_ev[1], st);
                 if (fp64())
                     MPS_COUNT_LAUNCH k_spmv<double, double, double, 1><<<kRedBlocks, 256, 0, st>>>(d, (const double*)d.nbrw, d.press,
                                                                                   d.r, d.rhs, 2);
                 else
                     residual_df((const float*)d.nbrw);
-                if (gate_measure) cudaEventRecord(gate_ev[2], st);   // the first residual: the refinement's
                 MPS_COUNT_LAUNCH k_pressure_scale<<<kRedBlocks, 256, 0, st>>>(d, 5);
                 MPS_COUNT_LAUNCH k_to_float_p<<<blocks_for(d.n), kBlock, 0, st>>>(d.n, d.press, d.pf32);
                 MPS_COUNT_LAUNCH k_features<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
@@ -866,17 +869,21 @@ struct Solver {
                 }
                 timer.mark(PH_SETUP, st);
             }
+            if (!use_learned && !collect && !fp64()) {
+                // the first refinement residual of the warm start, here so that the
+                // multilevel setup runs beside it (and inside the span the gate compares)
+                timer.mark(PH_VEC, st);
+                residual_df((const float*)d.nbrw);
+                if (stream_failed) return CCT_CUDAERR;
+                residual_ready = true;
+            }
             if (overlap_mg) {
                 cudaStreamWaitEvent(st2, ev_rows, 0);
                 if (mg_setup(st2)) return CCT_CUDAERR;
                 cudaEventRecord(ev_mg, st2);
+                timer.mark(PH_PRECOND, st);   // the solver stream waits for the rest of the setup
                 cudaStreamWaitEvent(st, ev_mg, 0);
-                mg_setup_done = true;
-            }
-            if (gated && !use_learned && !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL) {
-                // the step without the guess sets the multilevel preconditioner up here (it
-                // would at the start of the solve), inside the span the gate compares
-                if (mg_setup(st)) return CCT_CUDAERR;
+                timer.mark(PH_SETUP, st);
                 mg_setup_done = true;
             }
             if (gated) cudaEventRecord(gate_ev[4], st);
@@ -1061,8 +1068,17 @@ struct Solver {
                 return;
             }
         }
-        MPS_COUNT_LAUNCH k<<<spmv16_grid, kSsWarps * 32, kS16Smem, st>>>(d, d.w16, x, y, nullptr, 0);
+        if (pdl) {
+            if (MPS_COUNT_LAUNCH launch_pdl(k, spmv16_grid, kSsWarps * 32, kS16Smem, st, d, d.w16, x, y,
+                                            (const double*)nullptr, 0))
+                stream_failed = true;
+        } else {
+            MPS_COUNT_LAUNCH k<<<spmv16_grid, kSsWarps * 32, kS16Smem, st>>>(d, d.w16, x, y, nullptr, 0);
+        }
     }
+    // the CG iteration's kernels (SpMV, update and restriction, fine level of the
+    // V-cycle, direction update) are launched with programmatic dependent launch
+    bool pdl = true;
     // the streamed kernel needs the 16-bit slices of this step
     bool use_stream() const { return opt.spmv_stream != 0 && d.rows16; }
     // the inner CG runs on the FP16-weight operator (streamed, not matrix-free)
@@ -1163,13 +1179,25 @@ struct Solver {
                     if (use_mg) {
                         // a warp per level-1 aggregate, within the reduction buffer's 2 x kRedBlocks CTAs
                         const int ur_blocks = std::max(1, std::min(div_up(mg.L[1].n, 8), 2 * kRedBlocks));
-                        MPS_COUNT_LAUNCH k_mg_update_restrict<TV, TXA><<<ur_blocks, 256, 0, st>>>(d, mg, x, r, p, q, 1);
+                        if (pdl) {
+                            if (MPS_COUNT_LAUNCH launch_pdl(k_mg_update_restrict<TV, TXA>, ur_blocks, 256, 0, st, d, mg,
+                                                            x, r, (const TV*)p, (const TV*)q, 1))
+                                stream_failed = true;
+                        } else {
+                            MPS_COUNT_LAUNCH k_mg_update_restrict<TV, TXA><<<ur_blocks, 256, 0, st>>>(d, mg, x, r, p, q,
+                                                                                                   1);
+                        }
                         timer.mark(PH_PRECOND, st);
                         mg_apply(r, z, p, 0, true);
                         timer.mark(PH_VEC, st);
                     }
                 }
-                MPS_COUNT_LAUNCH k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
+                if (pdl && use_mg) {
+                    if (MPS_COUNT_LAUNCH launch_pdl(k_cg_p<TV>, kRedBlocks, 256, 0, st, d, p, (const TV*)z))
+                        stream_failed = true;
+                } else {
+                    MPS_COUNT_LAUNCH k_cg_p<TV><<<kRedBlocks, 256, 0, st>>>(d, p, z);
+                }
                 ++spmv_launches;
             }
             done += batch;
@@ -1265,7 +1293,7 @@ struct Solver {
                 h_nnz[2] = h_scal[S_NINT];
                 S.r0_relres = h_scal[S_BNORM] > 0 ? h_scal[S_RNORM] / h_scal[S_BNORM] : 0.0;
                 // the learned guess's residual norms before / after its update
-                gate_rb = residual_ready ? h_scal[S_TMP1] : 0.0;
+                gate_rb = (residual_ready && S.learned_applied) ? h_scal[S_TMP1] : 0.0;
                 gate_ra = h_scal[S_RNORM];
             }
             residual_ready = false;
