@@ -96,9 +96,10 @@ struct Solver {
     int models = 0;
     int walls_move = 0;
     cudaStream_t st = nullptr;
-    // second stream: the multilevel setup runs there beside the learned guess
+    // second stream: the multilevel setup runs there beside the rows' transpose, the first
+    // refinement residual and the learned guess
     cudaStream_t st2 = nullptr;
-    cudaEvent_t ev_rows = nullptr, ev_mg = nullptr;
+    cudaEvent_t ev_setup = nullptr, ev_rows = nullptr, ev_mg = nullptr;
     bool mg_setup_done = false;   // this step's hierarchy is already built
     std::vector<void*> allocs;
     void* sort_scratch = nullptr;
@@ -249,6 +250,7 @@ struct Solver {
         for (auto& e : gate_ev)
             if (cudaEventCreate(&e) != cudaSuccess) return CCT_CUDAERR;
         if (cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_setup, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_rows, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_mg, cudaEventDisableTiming) != cudaSuccess)
             return CCT_CUDAERR;
@@ -349,6 +351,7 @@ struct Solver {
         mlp = nullptr;
         if (st) cudaStreamDestroy(st);
         if (st2) cudaStreamDestroy(st2);
+        if (ev_setup) cudaEventDestroy(ev_setup);
         if (ev_rows) cudaEventDestroy(ev_rows);
         if (ev_mg) cudaEventDestroy(ev_mg);
         for (auto& e : gate_ev)
@@ -510,8 +513,17 @@ struct Solver {
 
     // aggregates, links and operators of the current particle order (after the PPE
     // setup: needs interior flags, diagonals and the FP32 neighbour rows)
+    // In two parts: the topology (aggregate flags and counts of every level) needs only
+    // the cell grid and the interior flags, the rest waits for the level counts on the
+    // host and, from the Galerkin assembly on, for the rows (rows_ready when given).
+    bool mg_topo_pending = false;   // mg_setup_topology ran, mg_setup_finish has not
     CCTStatusType mg_setup(cudaStream_t ss) {
+        const CCTStatusType rc = mg_setup_topology(ss);
+        return rc != CCT_NOERR ? rc : mg_setup_finish(ss, nullptr);
+    }
+    CCTStatusType mg_setup_topology(cudaStream_t ss) {
         mg_ready = false;
+        mg_topo_pending = false;
         if (opt.preconditioner != MPS_PRECOND_MULTILEVEL && !mg_init_done) return CCT_NOERR;
         if (opt.preconditioner == MPS_PRECOND_MULTILEVEL && !mg_init_done) {
             const CCTStatusType rc = mg_init();
@@ -528,6 +540,13 @@ struct Solver {
             cudaMemcpyAsync(mg_counts + l, mg_flag + nc, sizeof(unsigned), cudaMemcpyDeviceToDevice, ss);
         }
         cudaMemcpyAsync(h_counts, mg_counts, sizeof(unsigned) * (kMgMaxLevels + 1), cudaMemcpyDeviceToHost, ss);
+        mg_topo_pending = true;
+        return cuda_status(cudaGetLastError());
+    }
+    CCTStatusType mg_setup_finish(cudaStream_t ss, cudaEvent_t rows_ready) {
+        if (!mg_topo_pending) return CCT_NOERR;
+        mg_topo_pending = false;
+        MgLevel* L = mg.L;
         if (cudaStreamSynchronize(ss)) return CCT_CUDAERR;
         int levels = 0;
         for (int l = 1; l <= mg_grid_levels; ++l) {
@@ -543,6 +562,7 @@ struct Solver {
             MPS_COUNT_LAUNCH k_mg_nbpar<<<blocks_for(27 * L[l].n), kBlock, 0, ss>>>(L[l]);
         MPS_COUNT_LAUNCH k_mg_particles<<<blocks_for(d.n), kBlock, 0, ss>>>(d, mg);
         MPS_COUNT_LAUNCH k_mg_rows<<<blocks_for(L[1].n), kBlock, 0, ss>>>(d, mg);
+        if (rows_ready) cudaStreamWaitEvent(ss, rows_ready, 0);
         if (mg_assemble(ss, -1) != CCT_NOERR) return CCT_CUDAERR;
         for (int l = 1; l < levels; ++l)
             MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, ss>>>(L[l], L[l + 1]);
@@ -804,6 +824,16 @@ struct Solver {
         } else {
             MPS_COUNT_LAUNCH k_ppe_setup<<<blocks_for(d.n), kBlock, 0, st>>>(d);
             MPS_COUNT_LAUNCH k_count_nnz<<<kRedBlocks, 256, 0, st>>>(d, 4);
+            // the multilevel setup runs on the second stream: its topology (grid and
+            // interior flags only) beside the rows' transpose, its operators from the rows
+            // on, beside the warm start, the first refinement residual and the learned guess
+            const bool overlap_mg = !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
+            mg_setup_done = false;
+            if (overlap_mg) {
+                cudaEventRecord(ev_setup, st);
+                cudaStreamWaitEvent(st2, ev_setup, 0);
+                if (mg_setup_topology(st2)) return CCT_CUDAERR;
+            }
             // SELL-32 rows from the list pass's row-major rows: 16-bit column offsets for
             // the streamed SpMVs (the FP64 solver streams them with its FP64 weights), FP16
             // weight copies only for the FP32 inner CG, 32-bit columns where they are read
@@ -831,11 +861,6 @@ struct Solver {
             S.learned_applied = use_learned ? 1 : 0;
             flex_step = flexible_now();
             S.flexible = flex_step ? 1 : 0;
-            // the multilevel setup only needs the rows: it runs on the second stream beside
-            // the warm start, the first refinement residual and the learned guess
-            // (enqueued after them, below)
-            const bool overlap_mg = !fp64() && opt.preconditioner == MPS_PRECOND_MULTILEVEL;
-            mg_setup_done = false;
             if (overlap_mg) cudaEventRecord(ev_rows, st);
             const int warm = warm_order();
             MPS_COUNT_LAUNCH k_warm_start<<<blocks_for(d.n), kBlock, 0, st>>>(d, warm);
@@ -878,8 +903,7 @@ struct Solver {
                 residual_ready = true;
             }
             if (overlap_mg) {
-                cudaStreamWaitEvent(st2, ev_rows, 0);
-                if (mg_setup(st2)) return CCT_CUDAERR;
+                if (mg_setup_finish(st2, ev_rows)) return CCT_CUDAERR;
                 cudaEventRecord(ev_mg, st2);
                 timer.mark(PH_PRECOND, st);   // the solver stream waits for the rest of the setup
                 cudaStreamWaitEvent(st, ev_mg, 0);
