@@ -391,41 +391,45 @@ __global__ void __launch_bounds__(kMgCoarsenWarps * 32) k_mg_coarsen(MgLevel lo,
 // to 1 (its residual is always 0).
 __global__ void __launch_bounds__(1024) k_mg_dense_inverse(MgLevel lv, float* __restrict__ ainv) {
     extern __shared__ float sm[];
-    const int n = lv.n, w2 = 2 * n;
+    const int n = lv.n;
     if (n <= 0 || n > kMgMaxDense) return;
-    float* M = sm;              // [n][2n]: [A | I]
-    float* f = sm + n * w2;     // [n] elimination factors
-    for (int t = threadIdx.x; t < n * w2; t += blockDim.x) M[t] = 0.f;
+    float* M = sm;           // [n][n], Gauss-Jordan in place: column k holds the inverse's after step k
+    float* fk = sm + n * n;  // [n] the pivot column of the current step
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) M[t] = 0.f;
     __syncthreads();
     for (int t = threadIdx.x; t < n * 27; t += blockDim.x) {
         const int I = t / 27, s = t % 27;
         const int J = lv.nb[(size_t)I * 27 + s];
-        if (J >= 0) M[I * w2 + J] = lv.a[(size_t)I * 27 + s];
+        if (J >= 0) M[I * n + J] = lv.a[(size_t)I * 27 + s];
     }
-    for (int I = threadIdx.x; I < n; I += blockDim.x) M[I * w2 + n + I] = 1.f;
     __syncthreads();
     for (int I = threadIdx.x; I < n; I += blockDim.x)
-        if (!(M[I * w2 + I] > 0.f)) M[I * w2 + I] = 1.f;
+        if (!(M[I * n + I] > 0.f)) M[I * n + I] = 1.f;
     __syncthreads();
-    // each thread owns one column (col < w2) and the rows row0, row0 + rstep, ...: no
-    // index division in the elimination loop (same operations as an element loop)
-    const int col = (int)threadIdx.x % w2, row0 = (int)threadIdx.x / w2, rstep = (int)blockDim.x / w2;
-    const bool owner = (int)threadIdx.x < rstep * w2;
+    // each thread owns one column and the rows row0, row0 + rstep, ...  Step k reads the
+    // pivot, the pivot row's entry of its column and (into fk) the pivot column, then,
+    // after one barrier, writes: the pivot row divided by the pivot (1 / pivot in column
+    // k), the other rows less their multiple of it (column k: minus the multiple of
+    // 1 / pivot).  Per entry of the inverse these are the operations of elimination on
+    // [A | I], in the same order.
+    const int col = (int)threadIdx.x % n, row0 = (int)threadIdx.x / n, rstep = (int)blockDim.x / n;
+    const bool owner = (int)threadIdx.x < rstep * n;
     for (int k = 0; k < n; ++k) {
-        const float piv = M[k * w2 + k];
-        __syncthreads();
-        for (int t = threadIdx.x; t < w2; t += blockDim.x) M[k * w2 + t] /= piv;
-        __syncthreads();
-        for (int i = threadIdx.x; i < n; i += blockDim.x) f[i] = i == k ? 0.f : M[i * w2 + k];
+        const float piv = M[k * n + k];
+        const float mk = owner ? M[k * n + col] : 0.f;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) fk[i] = M[i * n + k];
         __syncthreads();
         if (owner) {
-            const float mk = M[k * w2 + col];
-            for (int i = row0; i < n; i += rstep)
-                if (i != k) M[i * w2 + col] -= f[i] * mk;
+            const float mkn = col == k ? 1.f / piv : mk / piv;
+            for (int i = row0; i < n; i += rstep) {
+                if (i == k) M[i * n + col] = mkn;
+                else if (col == k) M[i * n + col] = -(fk[i] * mkn);
+                else M[i * n + col] = __fmaf_rn(-fk[i], mkn, M[i * n + col]);
+            }
         }
         __syncthreads();
     }
-    for (int t = threadIdx.x; t < n * n; t += blockDim.x) ainv[t] = M[(t / n) * w2 + n + (t % n)];
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) ainv[t] = M[t];
 }
 
 // ---------------------------------------------------------------------------

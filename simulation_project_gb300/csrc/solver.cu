@@ -485,7 +485,7 @@ struct Solver {
         }
         if (e) return CCT_MEMERR;
         if (cudaMallocHost((void**)&h_counts, sizeof(unsigned) * (kMgMaxLevels + 1)) != cudaSuccess) return CCT_MEMERR;
-        const int smem = (2 * kMgMaxDense * kMgMaxDense + kMgMaxDense) * (int)sizeof(float);
+        const int smem = (kMgMaxDense * kMgMaxDense + kMgMaxDense) * (int)sizeof(float);
         if (cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) return CCT_CUDAERR;
         mg.omega = opt.mg_omega > 0 ? (float)opt.mg_omega : 1.3f;
         mg_on = mg_grid_levels >= 1;
@@ -567,7 +567,7 @@ struct Solver {
         for (int l = 1; l < levels; ++l)
             MPS_COUNT_LAUNCH k_mg_coarsen<<<div_up(L[l + 1].n, kMgCoarsenWarps), kMgCoarsenWarps * 32, 0, ss>>>(L[l], L[l + 1]);
         const int nd = L[levels].n;
-        MPS_COUNT_LAUNCH k_mg_dense_inverse<<<1, 1024, (2 * nd * nd + nd) * sizeof(float), ss>>>(L[levels], mg.ainv);
+        MPS_COUNT_LAUNCH k_mg_dense_inverse<<<1, 1024, (nd * nd + nd) * sizeof(float), ss>>>(L[levels], mg.ainv);
         if (fine_post())
             MPS_COUNT_LAUNCH k_mg_smoother_rows<<<blocks_for(d.n, kMgSmThreads), kMgSmThreads, 0, ss>>>(d, mg, sm_R,
                                                                                                        sm_mask);
