@@ -1182,13 +1182,14 @@ struct Solver {
 
     // CG iterations in batches with one convergence read-back after each (the kernels
     // of a batch return at once after convergence).  predict > 2 (the same pass's count
-    // in the last step): a first batch of predict - 1 iterations, then batches of 2, so
-    // few launches run past convergence; else batches of check_every.
+    // in the last step): a first batch of predict iterations, then batches of 2, so a
+    // pass whose count repeats is read back once and few launches run past convergence;
+    // else batches of check_every.
     template <class TW, class TV, class TXA>
     int cg_loop(TXA* x, TV* r, TV* z, TV* p, TV* q, const TW* w, const double* m64, const float* m32, int maxit,
                 int predict = 0) {
         const int every = opt.check_every > 0 ? opt.check_every : 8;
-        int batch = predict > 2 ? predict - 1 : every;
+        int batch = predict > 2 ? predict : every;
         int done = 0;
         while (done < maxit + every) {
             for (int k = 0; k < batch; ++k) {
