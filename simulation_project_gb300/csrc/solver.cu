@@ -683,7 +683,10 @@ struct Solver {
 
     CCTStatusType grid() {
         const int n = d.n;
-        if (n <= 0) return CCT_NOERR;
+        if (n <= 0) {   // no particles: empty cell tables (the neighbour passes find no cell)
+            cudaMemsetAsync(d.cell_count, 0, sizeof(int), st);
+            return cuda_status(cudaGetLastError());
+        }
         MPS_COUNT_LAUNCH k_hash<<<blocks_for(n), kBlock, 0, st>>>(d);
         const unsigned krange = ((unsigned)d.cells << d.zbits) - 1u;
         if (radix_sort_pairs(n, d.skey, d.idx, 0, radix_passes(krange), sort_scratch, st)) return CCT_CUDAERR;
@@ -754,6 +757,7 @@ struct Solver {
     // SELL-32 transpose of the current rows (k_rows_sell flags)
     void rows_sell(int flags) {
         const int slices = (d.n + 31) / 32;
+        if (slices == 0) return;
         if (fp64())
             MPS_COUNT_LAUNCH k_rows_sell<double><<<div_up(slices, rows_sell_warps<double>()), rows_sell_warps<double>() * 32,
                                                    0, st>>>(d, flags);
@@ -849,7 +853,7 @@ struct Solver {
                 d.rows_w16 = w16;
                 d.rows_c32 = full32;
             }
-            bool use_learned = learned_ready && opt.learned;
+            bool use_learned = learned_ready && opt.learned && d.n > 0;
             // the gate: a learned guess that cost more than it saved sits out a few steps
             if (use_learned && opt.learned_gate && !fp64() && gate_skip > 0) {
                 --gate_skip;
@@ -934,7 +938,7 @@ struct Solver {
         timer.mark(PH_CORRECT, st);
         if (!pressure_only) {
             if constexpr (sizeof(T) == 4)
-                MPS_COUNT_LAUNCH k_correct_warp<<<div_up((d.n + 31) / 32, 8), 256, 0, st>>>(d);
+                MPS_COUNT_LAUNCH k_correct_warp<<<blocks_for((d.n + 31) / 32, 8), 256, 0, st>>>(d);
             else
                 MPS_COUNT_LAUNCH k_correct<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
             std::swap(d.pos, d.pos2);

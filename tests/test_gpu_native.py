@@ -389,3 +389,37 @@ def test_streamed_level1_assembly_is_bit_identical():
     g.step(2)
     a2 = g.debug_level1(1)
     assert a2.tobytes() == g.debug_level1(0).tobytes()
+
+
+def _emptied(sc, shift=None):
+    import copy
+    e = copy.copy(sc)
+    if shift is None:   # no particles at all
+        for k in ("pos", "vel"):
+            setattr(e, k, getattr(sc, k)[:0])
+        for k in ("press", "visc", "ptype"):
+            setattr(e, k, getattr(sc, k)[:0])
+    else:               # every particle outside the compute zone
+        e.pos = sc.pos + np.asarray(shift)
+    return e
+
+
+@pytest.mark.parametrize("precision", ["fp32_ir", "fp64"])
+@pytest.mark.parametrize("case", ["no_particles", "all_outside_the_zone"])
+def test_steps_without_particles(precision, case):
+    """A scene without particles, and one whose particles all lie outside the compute
+    zone (the first compaction removes them), step without error: no particles, no CG
+    work, error flags clear, and the walls still rotate as in a step with particles."""
+    sc = scenes.rotating_bucket(l0=0.012, n_drag=0)
+    e = _emptied(sc, None if case == "no_particles" else (10.0, 10.0, 10.0))
+    g = Solver(e, precision=precision, max_particles=max(sc.n, 1))
+    ref = Solver(sc, precision=precision)
+    for i in range(3):
+        st = g.step(i)
+        ref.step(i)
+        assert st["error_flags"] == 0 and st["particles"] == 0, st
+        assert st["cg_iterations"] == 0 and st["nnz"] == 0, st
+    assert g.state()["id"].shape == (0,)
+    # the wall motion does not depend on the particles
+    assert np.array_equal(g.triangles(), ref.triangles())
+    assert not np.array_equal(g.triangles(), sc.tri_vertices.reshape(-1, 3, 3))

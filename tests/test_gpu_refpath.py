@@ -61,3 +61,29 @@ def test_refstep_matches_oracle_schedule(name, steps):
         assert got[:n].tobytes() == want[:n].tobytes(), f
     assert np.abs(st.out_pressure[:n]).max() > 0
     g.close()
+
+
+def test_launchers_without_particles_return_noerr_and_touch_nothing():
+    """N <= 0: every per-step launcher returns CCT_NOERR at once and leaves the bound
+    arrays as they were (the reference's launchers, radix/SPVSOLVER/MultiGPUSolver/
+    DeviceProcess.cu:49-409, launch nothing for an empty particle range)."""
+    from simulation_project_gb300.lib import call
+    sc = scenes.rotating_bucket(l0=0.012, n_drag=10, drag_index=5.0)
+    sc.param.bExplicitPressure = True
+    sc.param.SonicVelocity = 20.0
+    g = RefStep(sc)
+    g.step(0)
+    before = {k: g.download(k) for k in g.d}
+    s, d = g.stream.ref(), g.p
+    for n in (0, -3):
+        for name in RefStep.PARTICLE_KERNELS:
+            g._kernel(name, n)
+        call("CaculateCellIDandInitializeHash", s, n, g.cells, d("hash"), d("index"), d("out_pos"))
+        call("SortUsingThrust", n, d("hash"), d("index"))
+        call("reorderDataAndFindCellStart", s, n, g.cells, d("hash"), d("index"), d("cell_start"), d("cell_end"))
+        cnt = C.c_int(n)
+        call("CheckParticleOutsideComputeZone", s, C.byref(cnt))
+        assert cnt.value == n
+    for k, a in before.items():
+        assert g.download(k).tobytes() == a.tobytes(), k
+    g.close()
