@@ -1324,8 +1324,18 @@ __device__ __forceinline__ void df_add(float& S, float& C, float p, float lo) {
 // Two independent (hi, lo) accumulators (even / odd unrolled entries) so the TwoSum
 // chains overlap, merged with TwoSum at the end (a fixed order); two rather than four
 // keep the kernel at 32 registers (8 CTAs of 256 per SM).
-template <bool NARROW>
-__device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict__ w, const float2* __restrict__ xs,
+// x_j as its (hi, lo) words: the split FP64 iterate, or an FP32 vector (lo = 0)
+__device__ __forceinline__ void x_hl(const float2* __restrict__ x, int j, float& h, float& l) {
+    const float2 v = x[j];
+    h = v.x;
+    l = v.y;
+}
+__device__ __forceinline__ void x_hl(const float* __restrict__ x, int j, float& h, float& l) {
+    h = x[j];
+    l = 0.f;
+}
+template <bool NARROW, class TX>
+__device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict__ w, const TX* __restrict__ xs,
                                            size_t base, int cnt, int kmax, int sb, float& S_out, float& C_out) {
     float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
     for (int k = 0; k < kmax; k += 4) {
@@ -1341,8 +1351,8 @@ __device__ __forceinline__ void df_row_sum(const Dev& d, const float* __restrict
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (k + u < cnt) {
-                const float2 v = xs[id[u]];
-                const float h = v.x, l = v.y;
+                float h, l;
+                x_hl(xs, id[u], h, l);
                 const float p = __fmul_rn(wv[u], h);
                 const float pe = __fmaf_rn(wv[u], h, -p);
                 if (u & 1) df_add(S1, C1, p, __fmaf_rn(wv[u], l, pe));
@@ -1796,6 +1806,95 @@ __global__ void __launch_bounds__(W * 32, MINB) k_residual_stream(const __grid_c
         d.scal[S_RR] = out[0];
         d.scal[S_RNORM] = sqrt(out[0]);
         d.scal[S_BNORM] = sqrt(out[1]);
+    }
+}
+
+// The refinement residual after a pass, from the pass's own correction: with the FP32
+// solution d of the pass and its scale s, x += s d and r -= s A d on interior rows (A
+// the FP32-weight operator, A d in double-float as in k_residual_stream: each product
+// exact as (p, fma(w, d_j, -p)); d is FP32, so there is no low word to gather), and
+// r.r to the scalars (S_RR, S_RNORM; S_BNORM stays the first residual's).  Against
+// b - A x recomputed, this adds the FP64 rounding of the x update, 2^-53 |x_i| per row,
+// well inside the double-float residual's own 2^-44 of sum |w x|.  Non-interior rows keep
+// r = 0 and x.
+template <int SC, int SS, int W, int MINB, bool WIDE = false>
+__global__ void __launch_bounds__(W * 32, MINB) k_residual_update_stream(const __grid_constant__ Dev d,
+                                                                        const float* __restrict__ w,
+                                                                        const float* __restrict__ dv, double s,
+                                                                        double* __restrict__ x,
+                                                                        double* __restrict__ r, int slot) {
+    static_assert(SC % 8 == 0, "stages hold whole groups of 8 entries");
+    extern __shared__ __align__(128) unsigned char stream_smem[];
+    __shared__ __align__(8) unsigned long long bars[W][SS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int gw = blockIdx.x * W + warp, nw = gridDim.x * W;
+    SliceRing<SC, SS, float, WIDE> R;
+    R.init(d, w, stream_smem + warp * SS * SliceRing<SC, SS, float, WIDE>::SB, bars[warp], gw, nw);
+
+    double part0 = 0.0;
+    for (int sl = gw; sl < R.nsl; sl += nw) {
+        const int i = sl * 32 + lane;
+        const bool row = i < d.n;
+        const bool in = row && d.inner[i];
+        const int cnt = in ? d.nbr_cnt[i] : 0;
+        const int km = d.skmax[sl];
+        float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
+        bool done = false;
+        if ((WIDE || km >= 0) && R.streaming) {
+            const int nc = (slice_kmax(km) + SC - 1) / SC;
+            const int r0 = sl * 32;
+            for (int c = 0; c < nc; ++c) {
+                const unsigned char* cs;
+                const float* ws;
+                if (!R.acquire(cs, ws)) break;
+                const int k0 = c * SC;
+#pragma unroll
+                for (int g = 0; g < SC; g += 8) {
+                    int j[8];
+                    float wv[8], h[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        if constexpr (WIDE) j[u] = ((const int*)cs)[(g + u) * 32 + lane];
+                        else j[u] = r0 + (int)(short)((const unsigned short*)cs)[(g + u) * 32 + lane];
+                        wv[u] = ws[(g + u) * 32 + lane];
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) h[u] = k0 + g + u < cnt ? dv[j[u]] : 0.f;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        if (k0 + g + u < cnt) {
+                            const float p = __fmul_rn(wv[u], h[u]);
+                            const float pe = __fmaf_rn(wv[u], h[u], -p);
+                            if (u & 1) df_add(S1, C1, p, pe);
+                            else df_add(S0, C0, p, pe);
+                        }
+                    }
+                }
+                R.release();
+            }
+            if (R.streaming) {
+                df_add(S0, C0, S1, C1);
+                done = true;
+            }
+        }
+        if (!done) {
+            const int kmax = __reduce_max_sync(0xffffffffu, cnt);
+            const size_t base = (size_t)sl * d.K * 32 + lane;
+            if (km >= 0) df_row_sum<true>(d, w, dv, base, cnt, kmax, sl * 32, S0, C0);
+            else df_row_sum<false>(d, w, dv, base, cnt, kmax, -1, S0, C0);
+        }
+        if (!in) continue;
+        const double acc = (double)S0 + (double)C0;
+        const double di = (double)dv[i];
+        const double ri = r[i] - s * (d.diag[i] * di - d.c.coef_lap * acc);
+        r[i] = ri;
+        x[i] += s * di;
+        part0 += ri * ri;
+    }
+    double v[1] = {part0}, out[1];
+    if (grid_reduce<1>(v, d.red, d.red_count + slot, out) && threadIdx.x == 0) {
+        d.scal[S_RR] = out[0];
+        d.scal[S_RNORM] = sqrt(out[0]);
     }
 }
 

@@ -1288,6 +1288,31 @@ struct Solver {
         }
     }
 
+    // the residual after a refinement pass from the pass's correction (streamed rows of
+    // stored weights); else recomputed as b - A x
+    bool residual_by_update() const { return use_stream() && opt.matrix_free == 0; }
+    int upd_grid = 0, upd_wide_grid = 0;
+    void residual_update(const float* w, double s) {
+        if (prefer_wide) {
+            auto k = k_residual_update_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks, true>;
+            constexpr int smem = stream_smem_bytes<kSsEntries, kSsStages, kSsWarps, float, true>();
+            const int g = stream_grid_for(k, smem, upd_wide_grid);
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, smem, st>>>(d, w, d.d32, s, d.press, d.r, 2);
+        } else {
+            auto k = k_residual_update_stream<kSsEntries, kSsStages, kSsWarps, kSsMinBlocks>;
+            const int g = stream_grid_for(k, kSsSmem, upd_grid);
+            if (g < 0) {
+                stream_failed = true;
+                return;
+            }
+            MPS_COUNT_LAUNCH k<<<g, kSsWarps * 32, kSsSmem, st>>>(d, w, d.d32, s, d.press, d.r, 2);
+        }
+    }
+
     // inner-solve floor: the option, or automatically 7e-4 for the FP16-weight operator
     // under the multilevel preconditioner and 2e-6 otherwise.  With the FP16 weights a
     // refinement pass contracts the FP32-weight residual only down to about the weights'
@@ -1312,9 +1337,11 @@ struct Solver {
         double bnorm = 0.0;
         int outer = 0;
         for (;;) {
-            const bool from_learned = outer == 0 && residual_ready;
-            if (!from_learned) residual_df(w);
-            residual_ready = from_learned;
+            // the residual is already there for the first pass when the step computed it
+            // before the solve (or from the learned guess), and for the later passes when
+            // the last pass updated it with its correction
+            const bool have = residual_ready;
+            if (!have) residual_df(w);
             if (stream_failed || pull_scal()) return CCT_CUDAERR;
             if (outer == 0) {
                 h_nnz[0] = h_scal[S_NNZ0];
@@ -1322,7 +1349,7 @@ struct Solver {
                 h_nnz[2] = h_scal[S_NINT];
                 S.r0_relres = h_scal[S_BNORM] > 0 ? h_scal[S_RNORM] / h_scal[S_BNORM] : 0.0;
                 // the learned guess's residual norms before / after its update
-                gate_rb = (residual_ready && S.learned_applied) ? h_scal[S_TMP1] : 0.0;
+                gate_rb = (have && S.learned_applied) ? h_scal[S_TMP1] : 0.0;
                 gate_ra = h_scal[S_RNORM];
             }
             residual_ready = false;
@@ -1347,7 +1374,14 @@ struct Solver {
             if (it < 0) return CCT_CUDAERR;
             pass_its[pi] = it;
             S.cg_iterations += it;
-            MPS_COUNT_LAUNCH k_axpy_ir<<<kRedBlocks, 256, 0, st>>>(d, d.press, d.d32, rn);
+            if (residual_by_update()) {
+                // x += rn d and the next pass's residual r -= rn A d, one pass over the rows
+                residual_update(w, rn);
+                if (stream_failed) return CCT_CUDAERR;
+                residual_ready = true;
+            } else {
+                MPS_COUNT_LAUNCH k_axpy_ir<<<kRedBlocks, 256, 0, st>>>(d, d.press, d.d32, rn);
+            }
             ++outer;
         }
         S.ir_passes = outer;
