@@ -669,6 +669,9 @@ __global__ void __launch_bounds__(256) k_mg_coarse_cycle(const double* __restric
 // With qf (flexible CG, mode 0): also z.q of the last direction's product q = A p, and
 // S_BETA = -(z.q) / (p.q) (Notay's flexible CG keeping one direction) instead of the
 // ratio of successive r.z.
+// level-1 aggregates per warp in k_mg_up_fine_z (8 resident CTAs of 8 warps per SM at 32
+// registers: the 16k aggregates of the 882k-particle bucket in one wave)
+constexpr int kMgUpAgg = 2;
 template <class TV>
 __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ Dev d, const __grid_constant__ Mg mg,
                                                       const TV* __restrict__ r, TV* __restrict__ z,
@@ -680,47 +683,63 @@ __global__ void __launch_bounds__(256) k_mg_up_fine_z(const __grid_constant__ De
     const MgLevel& lo = mg.L[1];
     const MgLevel& hi = mg.L[2];
     const float omega = mg.omega;
-    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int wg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     TV prz = TV(0), pzq = TV(0);
-    if (I < lo.n) {   // warp-uniform; every thread reaches the grid reduction
-        const int rb0 = mg.rb[I], rb1 = mg.rb[I + 1];
-        // the lane's first two rows are loaded before the stencil gathers (they do not
-        // depend on them): one dependent-load chain per warp instead of two
-        constexpr int kPf = 2;
-        TV pr[kPf], pq[kPf];
-        float pm[kPf];
-        bool pin[kPf];
+    // kMgUpAgg adjacent aggregates per warp (one wave of warps for the level): every
+    // aggregate's row range, first rows and stencil terms are loaded before any is
+    // finished, so the warp has kMgUpAgg dependent-load chains in flight; the lane's first
+    // row of each is loaded before the stencil gathers (it does not depend on them)
+    constexpr int kPf = 1;
+    int I[kMgUpAgg], rb0[kMgUpAgg], rb1[kMgUpAgg];
+    TV pr[kMgUpAgg][kPf], pq[kMgUpAgg][kPf];
+    float pm[kMgUpAgg][kPf], t[kMgUpAgg];
+    bool pin[kMgUpAgg][kPf];
+#pragma unroll
+    for (int h = 0; h < kMgUpAgg; ++h) {
+        I[h] = kMgUpAgg * wg + h;
+        const bool on = I[h] < lo.n;   // warp-uniform
+        rb0[h] = on ? mg.rb[I[h]] : 0;
+        rb1[h] = on ? mg.rb[I[h] + 1] : 0;
+    }
+#pragma unroll
+    for (int h = 0; h < kMgUpAgg; ++h) {
 #pragma unroll
         for (int u = 0; u < kPf; ++u) {
-            const int i = rb0 + lane + 32 * u;
-            pin[u] = i < rb1 && d.inner[i];
-            pr[u] = pin[u] ? r[i] : TV(0);
-            pm[u] = pin[u] ? m32[i] : 0.f;
-            pq[u] = (pin[u] && qf) ? qf[i] : TV(0);
+            const int i = rb0[h] + lane + 32 * u;
+            pin[h][u] = i < rb1[h] && d.inner[i];
+            pr[h][u] = pin[h][u] ? r[i] : TV(0);
+            pm[h][u] = pin[h][u] ? m32[i] : 0.f;
+            pq[h][u] = (pin[h][u] && qf) ? qf[i] : TV(0);
         }
-        float t = 0.f;
-        if (lane < 27) {
-            const int J = lo.nb[(size_t)I * 27 + lane];
-            if (J >= 0) t = lo.a[(size_t)I * 27 + lane] * (lo.e[J] + hi.e2[lo.nbp[(size_t)I * 27 + lane]]);
+        t[h] = 0.f;
+        if (I[h] < lo.n && lane < 27) {
+            const int J = lo.nb[(size_t)I[h] * 27 + lane];
+            if (J >= 0) t[h] = lo.a[(size_t)I[h] * 27 + lane] * (lo.e[J] + hi.e2[lo.nbp[(size_t)I[h] * 27 + lane]]);
         }
+    }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        const float e1 = lo.e[I] + hi.e2[lo.par[I]] + omega * lo.dinv[I] * (lo.r[I] - t);
-        if (lane == 0) lo.e2[I] = e1;
+    for (int h = 0; h < kMgUpAgg; ++h) {
+        if (I[h] >= lo.n) break;   // warp-uniform; every thread reaches the grid reduction
+        float th = t[h];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) th += __shfl_xor_sync(0xffffffffu, th, o);
+        const int a = I[h];
+        const float e1 = lo.e[a] + hi.e2[lo.par[a]] + omega * lo.dinv[a] * (lo.r[a] - th);
+        if (lane == 0) lo.e2[a] = e1;
 #pragma unroll
         for (int u = 0; u < kPf; ++u) {
-            const int i = rb0 + lane + 32 * u;
-            if (i >= rb1) break;
+            const int i = rb0[h] + lane + 32 * u;
+            if (i >= rb1[h]) break;
             TV zi = TV(0);
-            if (pin[u]) {
-                zi = (TV)pm[u] * pr[u] + (TV)e1;
-                prz += pr[u] * zi;
-                if (qf) pzq += zi * pq[u];
+            if (pin[h][u]) {
+                zi = (TV)pm[h][u] * pr[h][u] + (TV)e1;
+                prz += pr[h][u] * zi;
+                if (qf) pzq += zi * pq[h][u];
             }
             z[i] = zi;
             if (mode == 1) p[i] = zi;
         }
-        for (int i = rb0 + lane + 32 * kPf; i < rb1; i += 32) {
+        for (int i = rb0[h] + lane + 32 * kPf; i < rb1[h]; i += 32) {
             TV zi = TV(0);
             if (d.inner[i]) {
                 zi = (TV)m32[i] * r[i] + (TV)e1;

@@ -622,7 +622,7 @@ struct Solver {
         }
         // the level-2 -> level-1 up sweep carries the fine level when no extra level-1
         // sweeps follow it (and the reduction buffer holds its CTAs' partials)
-        const int up1_blocks = div_up(L[1].n * 32, 256);
+        const int up1_blocks = div_up(L[1].n, kMgUpAgg * 8);   // 8 warps per CTA
         const bool post = fine_post();
         // the reduction buffer holds 2 partials per CTA of the fused kernel
         const bool fuse = !post && lv >= 2 && extra == 0 && up1_blocks <= 2 * kRedBlocks;
