@@ -782,25 +782,38 @@ __global__ void __launch_bounds__(256) k_mg_update_restrict(const __grid_constan
     const int lane = threadIdx.x & 31;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     TV prr = TV(0);
-    // the rows of the warp's first aggregate are visited by the grid-stride loop below;
-    // the launch gives (up to the reduction buffer's limit) one aggregate per warp, so
-    // the row range and the rows are one dependent-load chain
-    for (int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; I < L1.n; I += nw) {
-        float s = 0.f;
-        const int rb0 = mg.rb[I], rb1 = mg.rb[I + 1];
-        for (int i = rb0 + lane; i < rb1; i += 32) {
-            if (!d.inner[i]) continue;
-            x[i] = x[i] + (TXA)alpha * (TXA)p[i];
-            const TV ri = r[i] - alpha * q[i];
-            r[i] = ri;
-            prr += ri * ri;
-            s += (float)ri;
-        }
+    // two adjacent aggregates per warp and step of the grid-stride loop (the launch gives
+    // about one pair per warp: one wave): both row ranges, then both first row chunks are
+    // loaded before either is updated, so two dependent-load chains are in flight
+    auto row = [&](int i, float& s) {
+        if (!d.inner[i]) return;
+        x[i] = x[i] + (TXA)alpha * (TXA)p[i];
+        const TV ri = r[i] - alpha * q[i];
+        r[i] = ri;
+        prr += ri * ri;
+        s += (float)ri;
+    };
+    for (int I = 2 * ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); I < L1.n; I += 2 * nw) {
+        const bool two = I + 1 < L1.n;   // warp-uniform
+        const int a0 = mg.rb[I], a1 = mg.rb[I + 1], b1 = two ? mg.rb[I + 2] : a1;
+        float sa = 0.f, sb = 0.f;
+        const int ia = a0 + lane, ib = a1 + lane;
+        if (ia < a1) row(ia, sa);
+        if (ib < b1) row(ib, sb);
+        for (int i = ia + 32; i < a1; i += 32) row(i, sa);
+        for (int i = ib + 32; i < b1; i += 32) row(i, sb);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        for (int o = 16; o > 0; o >>= 1) {
+            sa += __shfl_down_sync(0xffffffffu, sa, o);
+            sb += __shfl_down_sync(0xffffffffu, sb, o);
+        }
         if (lane == 0) {
-            L1.r[I] = s;
-            L1.e[I] = mg.omega * L1.dinv[I] * s;
+            L1.r[I] = sa;
+            L1.e[I] = mg.omega * L1.dinv[I] * sa;
+            if (two) {
+                L1.r[I + 1] = sb;
+                L1.e[I + 1] = mg.omega * L1.dinv[I + 1] * sb;
+            }
         }
     }
     double v[1] = {(double)prr}, out[1];

@@ -1206,8 +1206,8 @@ struct Solver {
                                                                                     flex_step ? 1 : 0);
                 if constexpr (std::is_same<TV, float>::value) {
                     if (use_mg) {
-                        // a warp per level-1 aggregate, within the reduction buffer's 2 x kRedBlocks CTAs
-                        const int ur_blocks = std::max(1, std::min(div_up(mg.L[1].n, 8), 2 * kRedBlocks));
+                        // two level-1 aggregates per warp, within the reduction buffer's 2 x kRedBlocks CTAs
+                        const int ur_blocks = std::max(1, std::min(div_up(mg.L[1].n, 16), 2 * kRedBlocks));
                         if (pdl) {
                             if (MPS_COUNT_LAUNCH launch_pdl(k_mg_update_restrict<TV, TXA>, ur_blocks, 256, 0, st, d, mg,
                                                             x, r, (const TV*)p, (const TV*)q, 1))
