@@ -99,15 +99,17 @@ struct Solver {
     // second stream: the multilevel setup runs there beside the rows' transpose, the first
     // refinement residual and the learned guess
     cudaStream_t st2 = nullptr;
-    cudaEvent_t ev_setup = nullptr, ev_rows = nullptr, ev_mg = nullptr;
+    cudaEvent_t ev_setup = nullptr, ev_rows = nullptr, ev_mg = nullptr, ev_walls = nullptr, ev_bins = nullptr;
     bool mg_setup_done = false;   // this step's hierarchy is already built
     std::vector<void*> allocs;
     void* sort_scratch = nullptr;
     size_t sort_scratch_bytes = 0;
     unsigned *keep = nullptr, *rank = nullptr;
     unsigned* scan_sums = nullptr;   // tile sums of the multi-CTA scans
+    unsigned* scan_sums2 = nullptr;  // the same for the wall bins on the second stream
     double* h_scal = nullptr;   // pinned mirror of the device scalars
     int* h_int = nullptr;       // pinned small ints
+    int* h_bins = nullptr;      // pinned small ints of the wall binning
     // wall-bin scratch
     unsigned* bin_off = nullptr;
     size_t bin_off_cap = 0;
@@ -252,7 +254,9 @@ struct Solver {
         if (cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_setup, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_rows, cudaEventDisableTiming) != cudaSuccess ||
-            cudaEventCreateWithFlags(&ev_mg, cudaEventDisableTiming) != cudaSuccess)
+            cudaEventCreateWithFlags(&ev_mg, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_walls, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ev_bins, cudaEventDisableTiming) != cudaSuccess)
             return CCT_CUDAERR;
         const size_t N = nmax;
         const size_t wsz = sizeof(double);   // room for FP64 rows: the precision can be switched
@@ -299,6 +303,7 @@ struct Solver {
         e = e ? e : mk(&d.mlp_out, 2 * N);
         e = e ? e : mk(&d.targets, 2 * N);
         e = e ? e : mk(&scan_sums, scan_tile_sums_capacity());
+        e = e ? e : mk(&scan_sums2, scan_tile_sums_capacity());
         e = e ? e : mk(&keep, N + 1);
         e = e ? e : mk(&rank, N + 1);
         if (e != cudaSuccess) return CCT_MEMERR;
@@ -307,6 +312,7 @@ struct Solver {
         allocs.push_back(sort_scratch);
         if (cudaMallocHost((void**)&h_scal, sizeof(double) * S_COUNT) != cudaSuccess) return CCT_MEMERR;
         if (cudaMallocHost((void**)&h_int, sizeof(int) * 8) != cudaSuccess) return CCT_MEMERR;
+        if (cudaMallocHost((void**)&h_bins, sizeof(int) * 8) != cudaSuccess) return CCT_MEMERR;
         if (opt.preconditioner == MPS_PRECOND_MULTILEVEL && !fp64()) {
             const CCTStatusType rc = mg_init();
             if (rc != CCT_NOERR) return rc;
@@ -345,6 +351,7 @@ struct Solver {
         if (d.drag) cudaFree(d.drag);
         if (h_scal) cudaFreeHost(h_scal);
         if (h_int) cudaFreeHost(h_int);
+        if (h_bins) cudaFreeHost(h_bins);
         if (h_counts) cudaFreeHost(h_counts);
         timer.release();
         if (mlp) mps_mlp_destroy(mlp);
@@ -354,6 +361,8 @@ struct Solver {
         if (ev_setup) cudaEventDestroy(ev_setup);
         if (ev_rows) cudaEventDestroy(ev_rows);
         if (ev_mg) cudaEventDestroy(ev_mg);
+        if (ev_walls) cudaEventDestroy(ev_walls);
+        if (ev_bins) cudaEventDestroy(ev_bins);
         for (auto& e : gate_ev)
             if (e) cudaEventDestroy(e);
     }
@@ -668,13 +677,21 @@ struct Solver {
 
     // ---- phases ----
     CCTStatusType compact() {
+        compact_launch();
+        return compact_finish();
+    }
+    // the compaction's launches (no host wait) and, after them, the wait for the new count
+    void compact_launch() {
         const int n = d.n;
-        if (n <= 0) return CCT_NOERR;
+        if (n <= 0) return;
         MPS_COUNT_LAUNCH k_zone_flags<<<blocks_for(n), kBlock, 0, st>>>(d, keep);
         cudaMemcpyAsync(rank, keep, sizeof(unsigned) * n, cudaMemcpyDeviceToDevice, st);
         scan_exclusive(rank, n, rank + n, st, scan_sums);
         MPS_COUNT_LAUNCH k_compact<<<blocks_for(n), kBlock, 0, st>>>(d, keep, rank);
         cudaMemcpyAsync(h_int, rank + n, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    }
+    CCTStatusType compact_finish() {
+        if (d.n <= 0) return CCT_NOERR;
         if (cudaStreamSynchronize(st) != cudaSuccess) return CCT_CUDAERR;
         swap_state();
         d.n = h_int[0];
@@ -698,7 +715,9 @@ struct Solver {
         return cuda_status(cudaGetLastError());
     }
 
-    CCTStatusType bin_walls() {
+    // on stream ss with its own host buffer and scan scratch (the second stream, beside
+    // the particles' compaction, in a step)
+    CCTStatusType bin_walls(cudaStream_t ss, int* hb, unsigned* scr) {
         const int t = d.tri_n;
         if (t <= 0) return CCT_NOERR;
         // counts (t + 1 with the scan's total) and the 64-bit sum of the counts behind them
@@ -711,25 +730,25 @@ struct Solver {
             bin_off_cap = (size_t)t;
         }
         unsigned long long* total = (unsigned long long*)(bin_off + ((size_t)t + 3) / 2 * 2);
-        cudaMemsetAsync(total, 0, sizeof(unsigned long long), st);
-        MPS_COUNT_LAUNCH k_bin_count<<<blocks_for(t), kBlock, 0, st>>>(d, bin_off, total);
-        cudaMemcpyAsync(h_int + 4, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
+        cudaMemsetAsync(total, 0, sizeof(unsigned long long), ss);
+        MPS_COUNT_LAUNCH k_bin_count<<<blocks_for(t), kBlock, 0, ss>>>(d, bin_off, total);
+        cudaMemcpyAsync(hb + 4, total, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ss);
+        if (cudaStreamSynchronize(ss)) return CCT_CUDAERR;
         unsigned long long total_h = 0;
-        std::memcpy(&total_h, h_int + 4, sizeof(total_h));
+        std::memcpy(&total_h, hb + 4, sizeof(total_h));
         // every (cell, triangle) entry is indexed by an int in the sort and by the 32-bit
         // scan: a wall whose boxes hold more entries is refused, never truncated
         if (total_h > (unsigned long long)INT32_MAX) {
             note_message("wall bins: the triangles' cell boxes hold more than 2^31 - 1 (cell, triangle) entries");
             return CCT_MEMERR;
         }
-        scan_exclusive(bin_off, t + 1, nullptr, st, scan_sums);
-        cudaMemcpyAsync(h_int, bin_off + t, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-        if (cudaStreamSynchronize(st)) return CCT_CUDAERR;
-        const unsigned nv = (unsigned)h_int[0];
+        scan_exclusive(bin_off, t + 1, nullptr, ss, scr);
+        cudaMemcpyAsync(hb, bin_off + t, sizeof(unsigned), cudaMemcpyDeviceToHost, ss);
+        if (cudaStreamSynchronize(ss)) return CCT_CUDAERR;
+        const unsigned nv = (unsigned)hb[0];
         bin_entries = (int)nv;
         if (nv == 0) {
-            cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, st);
+            cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, ss);
             bins_dirty = 0;
             return CCT_NOERR;
         }
@@ -744,11 +763,11 @@ struct Solver {
         }
         int* vcell = bin_visit;
         d.tids = bin_visit + bin_visit_cap;
-        MPS_COUNT_LAUNCH k_bin_fill<<<div_up(t * 32, 256), 256, 0, st>>>(d, bin_off, vcell, d.tids);
-        if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(2 * d.cells - 1)), bin_sort, st))
+        MPS_COUNT_LAUNCH k_bin_fill<<<div_up(t * 32, 256), 256, 0, ss>>>(d, bin_off, vcell, d.tids);
+        if (radix_sort_pairs((int)nv, vcell, d.tids, 0, radix_passes((unsigned)(2 * d.cells - 1)), bin_sort, ss))
             return CCT_CUDAERR;
-        cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, st);
-        MPS_COUNT_LAUNCH k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, st>>>((int)nv, vcell, d.tcs,
+        cudaMemsetAsync(d.tcs, 0xff, sizeof(int) * 4 * d.cells, ss);
+        MPS_COUNT_LAUNCH k_bin_bounds<<<blocks_for((int)nv), kBlock, 0, ss>>>((int)nv, vcell, d.tcs,
                                                                                d.tcs + 2 * d.cells);
         bins_dirty = 0;
         return cuda_status(cudaGetLastError());
@@ -800,10 +819,20 @@ struct Solver {
         cudaMemsetAsync(d.istat, 0, 2 * sizeof(int), st);
         CCTStatusType rc;
         if (!pressure_only) {
-            if ((rc = compact())) return rc;
+            // the wall bins (the triangles moved at the end of the last step) on the second
+            // stream, their host waits and kernels beside the compaction and the grid
+            const bool bins = d.tri_n > 0 && bins_dirty;
+            if (bins) cudaEventRecord(ev_walls, st);
+            compact_launch();
+            if (bins) {
+                cudaStreamWaitEvent(st2, ev_walls, 0);
+                if ((rc = bin_walls(st2, h_bins, scan_sums2))) return rc;
+                cudaEventRecord(ev_bins, st2);
+            }
+            if ((rc = compact_finish())) return rc;
             if ((rc = grid())) return rc;
             timer.mark(PH_WALLS, st);
-            if (d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
+            if (bins) cudaStreamWaitEvent(st, ev_bins, 0);
             walls_distance<T>();
             if (d.drag_n > 0 && d.tri_n > 0) MPS_COUNT_LAUNCH k_drag<T><<<blocks_for(d.n), kBlock, 0, st>>>(d);
             else cudaMemsetAsync(d.dragv, 0, sizeof(double) * 3 * d.n, st);
@@ -817,7 +846,7 @@ struct Solver {
         if ((rc = compact())) return rc;
         if ((rc = grid())) return rc;
         timer.mark(PH_WALLS, st);
-        if (pressure_only && d.tri_n > 0 && bins_dirty && (rc = bin_walls())) return rc;
+        if (pressure_only && d.tri_n > 0 && bins_dirty && (rc = bin_walls(st, h_int, scan_sums))) return rc;
         walls_distance<T>();
         timer.mark(PH_LIST, st);
         const int nb_cells = std::max(1, std::min(d.cells, d.n));
@@ -1744,7 +1773,7 @@ CCTStatusType mps_solver_debug_wall_bins(MpsSolver* s, int* bounds, int* tids, i
     *entries = 0;
     if (d.tri_n <= 0) return CCT_NOERR;
     if (S.bins_dirty) {
-        const CCTStatusType rc = S.bin_walls();
+        const CCTStatusType rc = S.bin_walls(S.st, S.h_int, S.scan_sums);
         if (rc != CCT_NOERR) return rc;
     }
     if (cudaStreamSynchronize(S.st)) return CCT_CUDAERR;
