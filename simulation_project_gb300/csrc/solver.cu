@@ -251,7 +251,12 @@ struct Solver {
         if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CCT_CUDAERR;
         for (auto& e : gate_ev)
             if (cudaEventCreate(&e) != cudaSuccess) return CCT_CUDAERR;
-        if (cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking) != cudaSuccess ||
+        // the second stream at a higher priority: the work it takes (wall bins, multilevel
+        // setup) is on the step's critical path, and the solver-stream kernels beside it
+        // (compaction, grid, transpose, first residual) fill the SMs it leaves
+        int prio_low = 0, prio_high = 0;
+        cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+        if (cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_setup, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_rows, cudaEventDisableTiming) != cudaSuccess ||
             cudaEventCreateWithFlags(&ev_mg, cudaEventDisableTiming) != cudaSuccess ||
